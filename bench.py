@@ -1,0 +1,390 @@
+#!/usr/bin/env python
+"""DC-PSE hot-path benchmark on one GB300 (or N independent replicas).
+
+Workload: 128^3 = 2,097,152 jittered 3D particles (h = 1/127, jitter
+U(+-0.15h), seed 2), order 2, rCut = 2.8h, Gradient (3 outputs) + Laplacian
+(1 output, sum of 3 reference terms): 4 particle-ops per particle.
+
+A step is one batched FP32-weight apply of all 4 outputs over the whole
+particle set, inputs resident in HBM; the 2.9 GB weight stream is larger
+than L2, so no flush is needed between steps.  Also reported: the plain FP64
+GPU path (one pass per reference Dcpse object, the reference's order), the
+batched FP64 path, device assembly throughput (faithful and fast), the
+end-to-end call through the host-buffer C-ABI entry point, and the CPU oracle
+(the reference algorithm restated) on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DC-PSE apply Gparticle-ops/s & assembly Mparticles/s: FP32-batched vs FP64 @≤1e-6"
+UNIT = "Gparticle-ops/s"
+NOUT = 4
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nside", type=int, default=128)
+    ap.add_argument("--cpu-sample", type=int, default=32768, help="particles in the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling (200 ms) during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+# ----------------------------------------------------------------- CPU leg --
+def cpu_oracle_run(pos, rcut, f, sample, steps, warmup, nthreads):
+    """The reference algorithm restated on the CPU (oracle/): the S first
+    particles' rows (full neighbourhoods), 6 reference Dcpse objects
+    (Dx, Dy, Dz, Dxx, Dyy, Dzz), each assembled with the dense E of the
+    reference; a step applies the 4 outputs (Laplacian = sum of 3)."""
+    import oracle
+
+    S = min(sample, pos.shape[0])
+    rp, cols = oracle.neighbors(pos[:S], rcut, support=pos)
+    sigs = [(1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (0, 2, 0), (0, 0, 2)]
+    t0 = time.perf_counter()
+    terms = [oracle.assemble(pos[:S], rp, cols, s, 2, support=pos, nthreads=nthreads) for s in sigs]
+    t_asm = time.perf_counter() - t0
+
+    def step():
+        gx = oracle.apply(f, rp, cols, terms[0][2], terms[0][1], 1, f_dom=f[:S], nthreads=nthreads)
+        gy = oracle.apply(f, rp, cols, terms[1][2], terms[1][1], 1, f_dom=f[:S], nthreads=nthreads)
+        gz = oracle.apply(f, rp, cols, terms[2][2], terms[2][1], 1, f_dom=f[:S], nthreads=nthreads)
+        lap = sum(oracle.apply(f, rp, cols, terms[3 + i][2], terms[3 + i][1], 2, f_dom=f[:S], nthreads=nthreads)
+                  for i in range(3))
+        return gx, gy, gz, lap
+
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    t_apply = (time.perf_counter() - t0) / max(steps, 1)
+    return dict(S=S, nnz=int(rp[-1]), t_asm=t_asm, t_apply=t_apply,
+                apply_value=S * NOUT / t_apply / 1e9, asm_value=S / t_asm / 1e6)
+
+
+def host_cores():
+    return os.cpu_count() or 1
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from openfpm_numerics_gb300 import workloads as W
+
+    cfg = W.config2(args.nside)
+    pos = cfg["pos"]
+    f, _, _ = W.field2(pos)
+    cores = host_cores()
+    steps = max(1, min(args.steps, 20))
+    warm = max(1, min(args.warmup, 3))
+    r = cpu_oracle_run(pos, cfg["rcut"], f, args.cpu_sample, steps, warm, cores)
+    sample = ("first %d of %d particles (full neighbourhoods, %d entries); %d timed steps"
+              % (r["S"], pos.shape[0], r["nnz"], steps))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": r["apply_value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm, "ms_per_step": r["t_apply"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "128^3 jittered 3D particles, Gradient+Laplacian (6 reference Dcpse objects), "
+                               "order 2, rCut=2.8h", "particles": int(pos.shape[0])},
+        "cpu_baseline": {"value": r["apply_value"], "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "assembly": {"value": r["asm_value"], "unit": "Mparticles/s", "sample": sample},
+        "e2e": {"value": r["apply_value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "openfpm_numerics cannot be built here (openfpm_data/pdata, Eigen, Boost, MPI absent); "
+                "its CPU Dcpse algorithm is timed as restated in oracle/",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU leg --
+def run_ours(args):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    from openfpm_numerics_gb300 import _capi as C
+    from openfpm_numerics_gb300 import workloads as W
+    from openfpm_numerics_gb300.plan import DcpsePlan
+
+    cfg = W.config2(args.nside)
+    pos_np = cfg["pos"]
+    N = pos_np.shape[0]
+    f_np, grad_np, lap_np = W.field2(pos_np)
+    stream = torch.cuda.current_stream()
+    pos = torch.tensor(pos_np, device=dev)
+    f = torch.tensor(f_np, device=dev)
+    plan = DcpsePlan(3, W.grad_lap_outputs(3), order=2, stream=stream)
+    plan.set_timing(True)
+
+    # neighbour lists (device)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plan.build_neighbors(pos, cfg["rcut"])
+    torch.cuda.synchronize()
+    t_nbr = time.perf_counter() - t0
+    info = plan.info()
+    nnz = info["nnz"]
+    kbar = nnz / N
+
+    # faithful assembly (per reference Dcpse object, bit-exact with the oracle)
+    plan.reset_timing()
+    plan.assemble(pos, C.STORE_TERMS_F64 | C.STORE_OUT_F64)
+    t_asm_ref = plan.timing(C.K_ASSEMBLE)[0] / 1e3
+    nbad, first_bad, code = plan.particle_status()
+
+    # plain FP64 GPU path: the reference's apply, one pass per Dcpse object
+    out64 = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
+
+    def plain_step():
+        for o in range(NOUT):
+            plan.apply_output_f64(o, f, out64[o])
+
+    for _ in range(3):
+        plain_step()
+    plan.reset_timing()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nplain = max(3, min(args.steps, 50))
+    ev0.record(stream)
+    for _ in range(nplain):
+        plain_step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = ev0.elapsed_time(ev1) / 1e3 / nplain
+    ref_out = out64.cpu().numpy()
+
+    # batched FP64 apply
+    outb = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
+    for _ in range(3):
+        plan.apply(f, C.F64, outb)
+    ev0.record(stream)
+    for _ in range(nplain):
+        plan.apply(f, C.F64, outb)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_b64 = ev0.elapsed_time(ev1) / 1e3 / nplain
+    b64 = outb.cpu().numpy()
+
+    # fast assembly (summed right-hand sides) -> FP32 weights for the headline
+    plan.reset_timing()
+    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
+    t_asm_fast = plan.timing(C.K_ASSEMBLE)[0] / 1e3
+
+    out = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
+    clocks = Clocks(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        plan.apply(f, C.F32, out)
+    plan.reset_timing()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        plan.apply(f, C.F32, out)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_step = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    k_ms, k_launch = plan.timing(C.K_APPLY_BATCHED)
+    s_ms, s_launch = plan.timing(C.K_SPLIT)
+    clk = clocks.stop()
+    if dist:
+        tt = torch.tensor([t_step], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    res32 = out.cpu().numpy()
+
+    # end to end through the host-buffer entry point (pinned host memory)
+    hf = torch.empty(N, dtype=torch.float64, pin_memory=True)
+    hf.copy_(f.cpu())
+    hout = torch.empty((NOUT, N), dtype=torch.float64, pin_memory=True)
+    hf_np, hout_np = hf.numpy(), hout.numpy()
+    for _ in range(3):
+        plan.apply_host(hf_np, hout_np, C.F32)
+    n_e2e = max(3, min(args.steps, 200))
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(n_e2e):
+        plan.apply_host(hf_np, hout_np, C.F32)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = ev0.elapsed_time(ev1) / 1e3 / n_e2e
+    assert np.array_equal(hout_np, res32)
+
+    # accuracy
+    inner = W.interior_mask(pos_np, cfg["rcut"])
+    analytic = [grad_np[:, 0], grad_np[:, 1], grad_np[:, 2], lap_np]
+    errors = {
+        "fp32_vs_fp64_reference_order_normwise": max(rel_err(res32[o], ref_out[o]) for o in range(NOUT)),
+        "fp32_vs_fp64_reference_order_rms": max(float(np.sqrt(np.mean((res32[o] - ref_out[o]) ** 2)) /
+                                                    np.sqrt(np.mean(ref_out[o] ** 2))) for o in range(NOUT)),
+        "fp64_batched_vs_reference_order_normwise": max(rel_err(b64[o], ref_out[o]) for o in range(NOUT)),
+        "fp64_analytic_interior_normwise": [rel_err(ref_out[o][inner], analytic[o][inner]) for o in range(NOUT)],
+        "fp32_analytic_interior_normwise": [rel_err(res32[o][inner], analytic[o][inner]) for o in range(NOUT)],
+        "definition": "max|a-b| / max|b| per output, max over the 4 outputs",
+    }
+
+    hbm, peak_kind = peaks()
+    bytes_apply = W.apply_bytes(N, nnz, NOUT, 4, fbytes=8, obytes=8)
+    t_kernel = k_ms / 1e3 / max(k_launch, 1)
+    achieved = bytes_apply / t_kernel / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "apply_f32_grad_lap_128cube.txt")
+    if os.path.exists(tf):
+        for ln in open(tf):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                traffic = float(ln.split(":")[1])
+    flops_fast = W.assembly_flops(N, kbar, [(10, 3), (19, 1)])
+    flops_ref = W.assembly_flops(N, kbar, [(10, 3), (19, 3)])
+    value = world * N * NOUT / t_step / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        r = cpu_oracle_run(pos_np, cfg["rcut"], f_np, args.cpu_sample, 3, 1, host_cores())
+        cpu = {"value": r["apply_value"], "unit": UNIT, "cores": host_cores(), "kind": "port",
+               "sample": "first %d of %d particles (full neighbourhoods), 6 reference Dcpse objects, "
+                         "3 timed applies" % (r["S"], N),
+               "assembly_mparticles_s": r["asm_value"]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "128^3 jittered 3D particles (h=1/127, +-0.15h, seed 2), Gradient+Laplacian, "
+                                   "order 2, rCut=2.8h, FP32 weights, 4 outputs per particle",
+                       "particles": N, "neighbor_entries": nnz, "mean_neighbors": kbar,
+                       "max_neighbors": info["max_neighbors"],
+                       "l2": "inputs larger than L2 (%.2f GB of weights streamed per step)" % (NOUT * nnz * 4 / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": traffic, "peak_source": peak_kind, "kernel": "apply_f32_kernel",
+                         "algorithmic_bytes_per_launch": bytes_apply, "kernel_ms": t_kernel * 1e3},
+            "e2e": {"value": world * N * NOUT / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": N * 8,
+                    "d2h_bytes_per_step": NOUT * N * 8, "ms_per_step": t_e2e * 1e3,
+                    "api": "dcpse_apply_batched_host"},
+            "gpu_launches": int(k_launch + s_launch),
+            "clocks": clk,
+            "assembly": {"value": N / t_asm_fast / 1e6, "unit": "Mparticles/s", "mode": "fast (summed rhs), FP32 out",
+                         "ms": t_asm_fast * 1e3, "fp64_tflops": flops_fast / t_asm_fast / 1e12,
+                         "reference_order": {"value": N / t_asm_ref / 1e6, "ms": t_asm_ref * 1e3,
+                                             "fp64_tflops": flops_ref / t_asm_ref / 1e12},
+                         "failed_particles": nbad, "neighbors_ms": t_nbr * 1e3},
+            "fp64_plain": {"value": N * NOUT / t_plain / 1e9, "ms_per_step": t_plain * 1e3,
+                           "note": "one pass per reference Dcpse object (6), reference order"},
+            "fp64_batched": {"value": N * NOUT / t_b64 / 1e9, "ms_per_step": t_b64 * 1e3},
+            "speedup_fp32_batched_vs_fp64_plain": t_plain / t_step,
+            "errors": errors,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    plan.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+/* dcpse_capi.h -- C-ABI of the GB300 DC-PSE hot path.
+ *
+ * Plain C: POD arguments, device pointers (d_*) or host pointers (h_*), an
+ * opaque plan handle, int status.  No C++ or torch types cross this line.
+ * The C++ drop-in headers (Dcpse.hpp, DCPSE_op.hpp in this directory) and the
+ * Python package call these symbols.
+ *
+ * Citations are to the openfpm_numerics source tree (src/...).
+ *
+ * Threading: a plan is not thread-safe; every call is enqueued on the plan's
+ * stream (default: the legacy default stream) and calls that return data to
+ * the host synchronise that stream.
+ */
+#ifndef OPENFPM_DCPSE_CAPI_H
+#define OPENFPM_DCPSE_CAPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define DCPSE_OK 0
+#define DCPSE_ERR_ARG 1        /* invalid argument */
+#define DCPSE_ERR_CUDA 2       /* CUDA runtime error (dcpse_last_error has it) */
+#define DCPSE_ERR_STATE 3      /* call out of order (e.g. apply before assemble) */
+#define DCPSE_ERR_CAPACITY 4   /* a size limit was exceeded */
+#define DCPSE_ERR_IO 5         /* save/load failure */
+#define DCPSE_ERR_PARTICLES 6  /* some particles could not be assembled */
+
+/* per-particle assembly status (dcpse_particle_status / status arrays).
+ * The reference raises std::length_error for too few neighbours
+ * (src/DCPSE/Vandermonde.hpp:109-112) and asserts eps != 0
+ * (src/DCPSE/Vandermonde.hpp:80); here the particle's weights are zero and
+ * the code below is recorded. */
+#define DCPSE_PART_OK 0
+#define DCPSE_PART_TOO_FEW 1   /* fewer neighbours than basis functions */
+#define DCPSE_PART_BAD_EPS 2   /* eps not finite or not > 0 */
+#define DCPSE_PART_SINGULAR 3  /* zero pivot column in the moment matrix */
+#define DCPSE_PART_NONFINITE 4 /* non-finite kernel value */
+
+/* store flags of dcpse_assemble */
+#define DCPSE_STORE_TERMS_F64 1 /* per reference Dcpse object: calcKernels + localEpsInvPow, FP64 */
+#define DCPSE_STORE_OUT_F64 2   /* per output, terms summed, eps^-|alpha| folded in, FP64 */
+#define DCPSE_STORE_OUT_F32 4   /* per output, terms summed, eps^-|alpha| folded in, FP32 */
+#define DCPSE_ASSEMBLE_FAST 8   /* outputs from summed right-hand sides (one solve
+                                   per output and basis) instead of per-term sums */
+#define DCPSE_ASSEMBLE_ASYNC 16 /* do not synchronise; query dcpse_particle_status */
+
+/* precision of dcpse_apply_batched */
+#define DCPSE_F64 0
+#define DCPSE_F32 1
+
+typedef struct dcpse_plan_s dcpse_plan_t;
+
+/* Last error message of this thread ("" if none). */
+const char* dcpse_last_error(void);
+int dcpse_version(void);
+
+/* ---- plan ---------------------------------------------------------------
+ * A plan holds one particle set (domain == support), its neighbour list and
+ * n_outputs operators.  Output o is the sum of terms_per_output[o] reference
+ * Dcpse objects whose signatures follow in `signatures` (dim entries each):
+ *   Derivative_x   1 term  (1,0[,0])     src/DCPSE/DCPSE_op/DCPSE_op.hpp:666-679
+ *   Derivative_xx  1 term  (2,0[,0])     DCPSE_op.hpp:2216-2358
+ *   Laplacian      dim terms 2e_i        DCPSE_op.hpp:1367-1389 (VECT_DCPSE_V_SUM :388-399)
+ *   Gradient       dim outputs of e_i    DCPSE_op.hpp:1099-1120 (VECT_DCPSE_V :144-153)
+ * order = convergence order, h_over_eps = Dcpse::HOverEpsilon (Dcpse.hpp:80,
+ * 0.9 in the reference CPU path; the reference GPU path's eps = 2 <h>
+ * (Dcpse.cuh:799-807) corresponds to 0.5).
+ * Replaces: Dcpse::Dcpse (src/DCPSE/Dcpse.hpp:91-109) and the operator
+ * constructors above, minus the assembly itself. */
+int dcpse_plan_create(dcpse_plan_t** plan, int dim, int n_outputs, const int* terms_per_output,
+                      const unsigned* signatures, unsigned order, double h_over_eps);
+int dcpse_plan_destroy(dcpse_plan_t* plan);
+/* stream: a cudaStream_t (NULL = legacy default stream) */
+int dcpse_plan_set_stream(dcpse_plan_t* plan, void* stream);
+/* Domain box and periodicity (minimum-image offsets along periodic axes).
+ * Without a box the neighbour search uses the particles' bounding box and no
+ * axis is periodic.  Replaces the ghost layer the reference gets from
+ * vector_dist::ghost_get (Dcpse.hpp:107). */
+int dcpse_plan_set_box(dcpse_plan_t* plan, const double* lo, const double* hi, const int* periodic);
+/* sizes: n particles, nnz neighbour entries, terms, outputs, max neighbours */
+int dcpse_plan_info(dcpse_plan_t* plan, int64_t* n, int64_t* nnz, int* n_terms, int* n_outputs,
+                    int* max_neighbors);
+/* Basis of term t (MonomialBasis, src/DCPSE/MonomialBasis.hpp:114-157):
+ * exps gets n x dim exponents (n <= cap), returns n through *n. */
+int dcpse_term_basis(dcpse_plan_t* plan, int term, unsigned* exps, int cap, int* n);
+
+/* ---- neighbour lists ----------------------------------------------------
+ * CSR lists, ascending neighbour index, self excluded, |x_p - x_q|^2 < rc^2
+ * with rc = d_rcut_pp[p] when given (per-particle radius, the adaptive
+ * support of Dcpse.hpp:903-909) else rcut.
+ * Replaces: VerletList getVerlet<VL_NON_SYMMETRIC|VL_SKIP_REF_PART>(rCut)
+ * (e.g. src/DCPSE/tests/Dcpse_unit_tests.cpp:97) and SupportBuilderGPU
+ * (src/DCPSE/SupportBuilder.cuh:14-107, device-only here: no host scan). */
+int dcpse_build_neighbors(dcpse_plan_t* plan, const double* d_pos, int64_t n, double rcut,
+                          const double* d_rcut_pp);
+/* Use a caller-built list (e.g. the caller's own VerletList exported to CSR).
+ * The arrays are copied. */
+int dcpse_set_neighbors(dcpse_plan_t* plan, int64_t n, int64_t nnz, const int64_t* d_rowptr,
+                        const int32_t* d_cols);
+int dcpse_neighbors_ptr(dcpse_plan_t* plan, const int64_t** d_rowptr, const int32_t** d_cols);
+
+/* ---- assembly -----------------------------------------------------------
+ * Builds eps, eps^-|alpha| and the kernels of every term (and/or the summed
+ * output weights) for all particles on the device, in FP64.
+ * d_eps_fixed: optional per-particle eps override (NULL = reference eps).
+ * Returns DCPSE_ERR_PARTICLES if any particle failed (see
+ * dcpse_particle_status); the plan is still usable, failed rows are zero.
+ * Replaces: Dcpse::initializeStaticSize (src/DCPSE/Dcpse.hpp:690-796),
+ * Dcpse_gpu::assembleLocalMatrices (src/DCPSE/Dcpse.cuh:620-717). */
+int dcpse_assemble(dcpse_plan_t* plan, const double* d_pos, const double* d_eps_fixed, int flags);
+int dcpse_particle_status(dcpse_plan_t* plan, int64_t* n_bad, int64_t* first_bad, int* first_code);
+/* Device arrays owned by the plan (valid until the next assemble/destroy). */
+int dcpse_eps_ptr(dcpse_plan_t* plan, const double** d_eps, const int32_t** d_status);
+/* calcKernels / localEpsInvPow of term t (Dcpse.hpp:59-63), FP64 */
+int dcpse_term_kernels_ptr(dcpse_plan_t* plan, int term, const double** d_kernels,
+                           const double** d_eps_inv_pow);
+/* summed, eps-folded output weights (either may be NULL if not stored) */
+int dcpse_output_weights_ptr(dcpse_plan_t* plan, int output, const double** d_w64, const float** d_w32);
+
+/* ---- apply --------------------------------------------------------------
+ * Df_p = eps_p^-|alpha| sum_q (f_q + s f_p) K_pq, s = -1 for even |alpha|,
+ * in the reference's operation order (bit-exact with it).
+ * Replaces: Dcpse::computeDifferentialOperator<f,Df> (src/DCPSE/Dcpse.hpp:467-499)
+ * and the per-key form (Dcpse.hpp:560-603). */
+int dcpse_apply_term_f64(dcpse_plan_t* plan, int term, const double* d_f, double* d_out);
+/* Output o as the reference composes it (sum of its terms, VECT_DCPSE_V_SUM,
+ * DCPSE_op.hpp:388-399), FP64, one term after the other. */
+int dcpse_apply_output_f64(dcpse_plan_t* plan, int output, const double* d_f, double* d_out);
+/* All outputs in one pass over the neighbour list from the summed weights:
+ * d_out[o*n + p] = sum_q w_o,pq (f_q - f_p).  precision DCPSE_F32 uses the
+ * FP32 weights with FP32 arithmetic, DCPSE_F64 the FP64 ones.
+ * Replaces the host loop vector_dist_op_compute_op<prp,comp_host>::compute_expr
+ * (src/Operators/Vector/cuda/vector_dist_operators_cuda.cuh:444-461) for
+ * `getV<j>(parts) = Op(getV<i>(parts))`. */
+int dcpse_apply_batched(dcpse_plan_t* plan, const double* d_f, double* d_out, int precision);
+/* Same with host buffers h_f[n], h_out[n_outputs*n]: the copies are part of
+ * the call (the reference's bulk apply reads and writes host particles). */
+int dcpse_apply_batched_host(dcpse_plan_t* plan, const double* h_f, double* h_out, int precision);
+
+/* ---- timing -------------------------------------------------------------
+ * Optional CUDA-event timing of the plan's kernels on the plan's stream (the
+ * role of the reference's std::chrono prints in Dcpse.cuh:581-716).
+ * kernel ids: */
+#define DCPSE_K_APPLY_BATCHED 0
+#define DCPSE_K_SPLIT 1
+#define DCPSE_K_ASSEMBLE 2
+#define DCPSE_K_APPLY_TERM 3
+#define DCPSE_K_NEIGHBORS 4
+#define DCPSE_K_COUNT 5
+int dcpse_plan_set_timing(dcpse_plan_t* plan, int enable);
+/* Synchronises the stream; total device time and launches since the last reset. */
+int dcpse_plan_timing(dcpse_plan_t* plan, int kernel, double* total_ms, int64_t* launches);
+int dcpse_plan_reset_timing(dcpse_plan_t* plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPENFPM_DCPSE_CAPI_H */

@@ -1,0 +1,826 @@
+// dcpse_capi.cu -- the C-ABI of the GB300 DC-PSE path (plan management,
+// basis tables, neighbour build, assembly and apply entry points).
+//
+// Host-side restatement of the reference's basis machinery:
+//   MonomialBasis::generateBasis  src/DCPSE/MonomialBasis.hpp:114-157
+//   Monomial::getDerivative       src/DCPSE/Monomial.hpp:158-174
+//   DcpseRhs::getVector           src/DCPSE/DcpseRhs.hpp:26-60
+// The bases are computed once per plan and shipped to the device as tables.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "dcpse_internal.h"
+
+using namespace dcpse;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define DCPSE_CK(call)                                                                                  \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(DCPSE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
+    } while (0)
+
+struct Mono {
+    std::array<unsigned, 3> e{0, 0, 0};
+    unsigned scalar = 1;
+};
+
+// MonomialBasis.hpp:114-157: grid [0, lim)^dim with dimension 0 fastest,
+// keep alphaMin <= |m| < lim; lim = |alpha| + r, alphaMin = 1 for even
+// |alpha| > 0.
+std::vector<Mono> make_basis(int dim, unsigned msum, unsigned r) {
+    std::vector<Mono> out;
+    unsigned lim = msum + r;
+    unsigned amin = (msum % 2 == 0 && msum != 0) ? 1u : 0u;
+    long total = 1;
+    for (int d = 0; d < dim; ++d) total *= (long)lim;
+    for (long lin = 0; lin < total; ++lin) {
+        Mono m;
+        long t = lin;
+        unsigned o = 0;
+        for (int d = 0; d < dim; ++d) {
+            m.e[d] = (unsigned)(t % lim);
+            t /= lim;
+            o += m.e[d];
+        }
+        if (o < lim && o >= amin) out.push_back(m);
+    }
+    return out;
+}
+
+// (D^sig m)(0) * sign, sign = +1 for even |sig| (DcpseRhs.hpp:41-60, with
+// Monomial::getDerivative and evaluate at the origin)
+double rhs_entry(int dim, const Mono& m, const unsigned* sig) {
+    unsigned ord = 0;
+    for (int d = 0; d < dim; ++d) ord += sig[d];
+    int sign = (ord % 2 == 0) ? 1 : -1;
+    unsigned s = m.scalar;
+    double val = 1.0;
+    for (int d = 0; d < dim; ++d) {
+        int target = (int)m.e[d] - (int)sig[d];
+        for (int k = (int)m.e[d]; k > target && k >= 0; --k) s *= (unsigned)k;
+        unsigned ne = (unsigned)std::max(target, 0);
+        val = val * (ne == 0 ? 1.0 : 0.0);
+    }
+    return sign * ((double)s * val);
+}
+
+__global__ void status_summary_kernel(const int32_t* st, int64_t n, unsigned long long* out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (st[i] != 0) {
+            atomicAdd(&out[0], 1ull);
+            atomicMin(&out[1], (unsigned long long)i);
+        }
+    }
+}
+
+__global__ void row_max_kernel(const int64_t* rowptr, int64_t n, int* maxk) {
+    int m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, (int)(rowptr[i + 1] - rowptr[i]));
+    atomicMax(maxk, m);
+}
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+}  // namespace
+
+struct KernelTimer {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+    size_t used = 0;
+};
+
+struct dcpse_plan_s {
+    // optional event timing per kernel id
+    bool timing = false;
+    KernelTimer timers[DCPSE_K_COUNT];
+    void tstart(int k) {
+        if (!timing) return;
+        KernelTimer& T = timers[k];
+        if (T.used == T.ev.size()) {
+            cudaEvent_t a, b;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            T.ev.emplace_back(a, b);
+        }
+        cudaEventRecord(T.ev[T.used].first, stream);
+    }
+    void tstop(int k) {
+        if (!timing) return;
+        KernelTimer& T = timers[k];
+        cudaEventRecord(T.ev[T.used].second, stream);
+        T.used++;
+    }
+    void free_timers() {
+        for (auto& T : timers) {
+            for (auto& p : T.ev) {
+                cudaEventDestroy(p.first);
+                cudaEventDestroy(p.second);
+            }
+            T.ev.clear();
+            T.used = 0;
+        }
+    }
+    int dim = 0;
+    unsigned order = 2;
+    double hoe = 0.9;
+    int nout = 0, nterms = 0;
+    std::vector<int> term_output;
+    std::vector<std::array<unsigned, 3>> sigs;
+    std::vector<int> term_group;
+    std::vector<std::vector<Mono>> gbasis;
+    AsmTables* htab = nullptr;  // host copy
+    AsmTables* dtab = nullptr;  // device copy
+    cudaStream_t stream = nullptr;
+    bool has_box = false;
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    int per[3] = {0, 0, 0};
+    // neighbour list
+    int64_t n = -1, nnz = 0;
+    int maxk = 0;
+    int64_t* rowptr = nullptr;
+    int32_t* cols = nullptr;
+    // assembly results
+    bool assembled = false;
+    int flags = 0;
+    double* eps = nullptr;
+    int32_t* status = nullptr;
+    double* eip_group = nullptr;
+    double* k_term = nullptr;
+    double* w64 = nullptr;
+    float* w32 = nullptr;
+    unsigned long long* summary = nullptr;  // [count, first]
+    // apply scratch
+    float2* f2 = nullptr;
+    double* hf = nullptr;    // device copy of a host field (host apply)
+    double* hout = nullptr;  // device output for host apply
+
+    void free_assembly() {
+        dfree(eps);
+        dfree(status);
+        dfree(eip_group);
+        dfree(k_term);
+        dfree(w64);
+        dfree(w32);
+        assembled = false;
+    }
+    void free_all() {
+        free_assembly();
+        dfree(rowptr);
+        dfree(cols);
+        dfree(f2);
+        dfree(hf);
+        dfree(hout);
+        dfree(summary);
+        dfree(dtab);
+        delete htab;
+        htab = nullptr;
+        free_timers();
+    }
+};
+
+namespace {
+
+int build_tables(dcpse_plan_s* P) {
+    AsmTables* T = P->htab;
+    std::memset(T, 0, sizeof(AsmTables));
+    T->dim = P->dim;
+    // groups by |alpha| (the basis depends on |alpha| and the order only)
+    std::vector<unsigned> gkey;
+    P->term_group.assign(P->nterms, 0);
+    for (int t = 0; t < P->nterms; ++t) {
+        unsigned ms = 0;
+        for (int d = 0; d < P->dim; ++d) ms += P->sigs[t][d];
+        auto it = std::find(gkey.begin(), gkey.end(), ms);
+        if (it == gkey.end()) {
+            gkey.push_back(ms);
+            P->term_group[t] = (int)gkey.size() - 1;
+        } else {
+            P->term_group[t] = (int)(it - gkey.begin());
+        }
+    }
+    if ((int)gkey.size() > kMaxGroups) return fail(DCPSE_ERR_CAPACITY, "too many distinct operator orders in one plan");
+    T->ngroups = (int)gkey.size();
+    P->gbasis.clear();
+    std::vector<std::array<unsigned, 3>> uni;
+    for (int g = 0; g < T->ngroups; ++g) {
+        auto B = make_basis(P->dim, gkey[g], P->order);
+        if ((int)B.size() > kMaxBasis) return fail(DCPSE_ERR_CAPACITY, "basis larger than supported");
+        T->gn[g] = (int)B.size();
+        T->gord[g] = (int)gkey[g];
+        for (size_t i = 0; i < B.size(); ++i) {
+            auto it = std::find(uni.begin(), uni.end(), B[i].e);
+            int ui;
+            if (it == uni.end()) {
+                uni.push_back(B[i].e);
+                ui = (int)uni.size() - 1;
+            } else {
+                ui = (int)(it - uni.begin());
+            }
+            if (ui >= kMaxUnion) return fail(DCPSE_ERR_CAPACITY, "union basis larger than supported");
+            T->gidx[g][i] = (unsigned char)ui;
+        }
+        P->gbasis.push_back(B);
+    }
+    T->nu = (int)uni.size();
+    int maxe = 0;
+    for (int j = 0; j < T->nu; ++j)
+        for (int d = 0; d < P->dim; ++d) {
+            T->uexp[j][d] = (unsigned char)uni[j][d];
+            maxe = std::max(maxe, (int)uni[j][d]);
+        }
+    T->maxexp = maxe + 1;
+    if (T->maxexp > kMaxExp) return fail(DCPSE_ERR_CAPACITY, "monomial degree larger than supported");
+    // Gram entries needed by some group
+    std::vector<std::pair<int, int>> pairs;
+    for (int g = 0; g < T->ngroups; ++g)
+        for (int i = 0; i < T->gn[g]; ++i)
+            for (int j = 0; j < T->gn[g]; ++j) {
+                int a = T->gidx[g][i], b = T->gidx[g][j];
+                if (a <= b) pairs.emplace_back(a, b);
+            }
+    std::sort(pairs.begin(), pairs.end());
+    pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+    if ((int)pairs.size() > kMaxPairs) return fail(DCPSE_ERR_CAPACITY, "too many Gram entries");
+    T->npairs = (int)pairs.size();
+    for (int a = 0; a < kMaxUnion; ++a)
+        for (int b = 0; b < kMaxUnion; ++b) T->upair[a][b] = -1;
+    for (int e = 0; e < T->npairs; ++e) {
+        T->pi[e] = (unsigned char)pairs[e].first;
+        T->pj[e] = (unsigned char)pairs[e].second;
+        T->upair[pairs[e].first][pairs[e].second] = (short)e;
+    }
+    // right-hand sides
+    T->nterms = P->nterms;
+    T->noutputs = P->nout;
+    for (int t = 0; t < P->nterms; ++t) {
+        T->term_group[t] = P->term_group[t];
+        T->term_output[t] = P->term_output[t];
+    }
+    for (int g = 0; g < T->ngroups; ++g) {
+        const auto& B = P->gbasis[g];
+        for (int t = 0; t < P->nterms; ++t) {
+            if (P->term_group[t] != g) continue;
+            int r = T->nterm_rhs[g]++;
+            if (r >= kMaxRhs) return fail(DCPSE_ERR_CAPACITY, "too many terms of one order");
+            T->term_of_rhs[g][r] = t;
+            for (size_t i = 0; i < B.size(); ++i) T->b_term[g][r][i] = rhs_entry(P->dim, B[i], P->sigs[t].data());
+        }
+        for (int o = 0; o < P->nout; ++o) {
+            bool touches = false;
+            for (int t = 0; t < P->nterms; ++t) touches |= (P->term_output[t] == o && P->term_group[t] == g);
+            if (!touches) continue;
+            int r = T->nout_rhs[g]++;
+            if (r >= kMaxRhs) return fail(DCPSE_ERR_CAPACITY, "too many outputs of one order");
+            T->out_of_rhs[g][r] = o;
+            for (size_t i = 0; i < B.size(); ++i) {
+                double v = 0.0;
+                for (int t = 0; t < P->nterms; ++t)
+                    if (P->term_output[t] == o && P->term_group[t] == g)
+                        v = v + rhs_entry(P->dim, B[i], P->sigs[t].data());
+                T->b_out[g][r][i] = v;
+            }
+        }
+    }
+    return DCPSE_OK;
+}
+
+Geom plan_geom(const dcpse_plan_s* P) {
+    Geom g{};
+    for (int d = 0; d < kMaxDim; ++d) {
+        g.per[d] = (P->has_box && d < P->dim) ? P->per[d] : 0;
+        g.L[d] = P->hi[d] - P->lo[d];
+        g.half[d] = 0.5 * g.L[d];
+    }
+    return g;
+}
+
+int check_plan(dcpse_plan_t* P) {
+    if (!P) return fail(DCPSE_ERR_ARG, "null plan");
+    return DCPSE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dcpse_last_error(void) { return g_err.c_str(); }
+
+int dcpse_version(void) { return 1; }
+
+int dcpse_plan_create(dcpse_plan_t** plan, int dim, int n_outputs, const int* terms_per_output,
+                      const unsigned* signatures, unsigned order, double h_over_eps) {
+    if (!plan) return fail(DCPSE_ERR_ARG, "plan is NULL");
+    *plan = nullptr;
+    if (dim < 1 || dim > 3) return fail(DCPSE_ERR_ARG, "dim must be 1, 2 or 3");
+    if (n_outputs < 1 || n_outputs > kMaxOutputs) return fail(DCPSE_ERR_CAPACITY, "1..8 outputs per plan");
+    if (!terms_per_output || !signatures) return fail(DCPSE_ERR_ARG, "NULL terms/signatures");
+    if (!(h_over_eps > 0.0)) return fail(DCPSE_ERR_ARG, "h_over_eps must be > 0");
+    if (order < 1) return fail(DCPSE_ERR_ARG, "convergence order must be >= 1");
+    auto* P = new dcpse_plan_s();
+    P->dim = dim;
+    P->order = order;
+    P->hoe = h_over_eps;
+    P->nout = n_outputs;
+    int t = 0;
+    for (int o = 0; o < n_outputs; ++o) {
+        if (terms_per_output[o] < 1) {
+            delete P;
+            return fail(DCPSE_ERR_ARG, "each output needs at least one term");
+        }
+        for (int i = 0; i < terms_per_output[o]; ++i, ++t) {
+            std::array<unsigned, 3> s{0, 0, 0};
+            for (int d = 0; d < dim; ++d) s[d] = signatures[(size_t)t * dim + d];
+            P->sigs.push_back(s);
+            P->term_output.push_back(o);
+        }
+    }
+    P->nterms = t;
+    if (t > kMaxTerms) {
+        delete P;
+        return fail(DCPSE_ERR_CAPACITY, "too many terms in one plan");
+    }
+    P->htab = new AsmTables();
+    int rc = build_tables(P);
+    if (rc != DCPSE_OK) {
+        P->free_all();
+        delete P;
+        return rc;
+    }
+    cudaError_t e = dalloc(&P->dtab, 1);
+    if (e == cudaSuccess) e = cudaMemcpy(P->dtab, P->htab, sizeof(AsmTables), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = dalloc(&P->summary, 2);
+    if (e != cudaSuccess) {
+        P->free_all();
+        delete P;
+        return fail(DCPSE_ERR_CUDA, std::string("plan allocation: ") + cudaGetErrorString(e));
+    }
+    *plan = P;
+    return DCPSE_OK;
+}
+
+int dcpse_plan_destroy(dcpse_plan_t* P) {
+    if (!P) return DCPSE_OK;
+    if (P->stream) cudaStreamSynchronize(P->stream);
+    P->free_all();
+    delete P;
+    return DCPSE_OK;
+}
+
+int dcpse_plan_set_stream(dcpse_plan_t* P, void* stream) {
+    if (int rc = check_plan(P)) return rc;
+    P->stream = (cudaStream_t)stream;
+    return DCPSE_OK;
+}
+
+int dcpse_plan_set_box(dcpse_plan_t* P, const double* lo, const double* hi, const int* periodic) {
+    if (int rc = check_plan(P)) return rc;
+    if (!lo || !hi) {
+        P->has_box = false;
+        return DCPSE_OK;
+    }
+    for (int d = 0; d < P->dim; ++d) {
+        if (!(hi[d] > lo[d])) return fail(DCPSE_ERR_ARG, "box hi must exceed lo");
+        P->lo[d] = lo[d];
+        P->hi[d] = hi[d];
+        P->per[d] = periodic ? (periodic[d] != 0) : 0;
+    }
+    P->has_box = true;
+    return DCPSE_OK;
+}
+
+int dcpse_plan_info(dcpse_plan_t* P, int64_t* n, int64_t* nnz, int* n_terms, int* n_outputs, int* max_neighbors) {
+    if (int rc = check_plan(P)) return rc;
+    if (n) *n = P->n;
+    if (nnz) *nnz = P->nnz;
+    if (n_terms) *n_terms = P->nterms;
+    if (n_outputs) *n_outputs = P->nout;
+    if (max_neighbors) *max_neighbors = P->maxk;
+    return DCPSE_OK;
+}
+
+int dcpse_term_basis(dcpse_plan_t* P, int term, unsigned* exps, int cap, int* n) {
+    if (int rc = check_plan(P)) return rc;
+    if (term < 0 || term >= P->nterms) return fail(DCPSE_ERR_ARG, "term out of range");
+    const auto& B = P->gbasis[P->term_group[term]];
+    if (n) *n = (int)B.size();
+    if ((int)B.size() > cap) return fail(DCPSE_ERR_CAPACITY, "cap too small for the basis");
+    if (exps)
+        for (size_t i = 0; i < B.size(); ++i)
+            for (int d = 0; d < P->dim; ++d) exps[i * P->dim + d] = B[i].e[d];
+    return DCPSE_OK;
+}
+
+int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, double rcut, const double* d_rcut_pp) {
+    if (int rc = check_plan(P)) return rc;
+    if (n < 0 || (n > 0 && !d_pos)) return fail(DCPSE_ERR_ARG, "bad particle array");
+    if (n >= (int64_t)INT32_MAX) return fail(DCPSE_ERR_CAPACITY, "at most 2^31-1 particles");
+    if (!d_rcut_pp && !(rcut > 0.0)) return fail(DCPSE_ERR_ARG, "rcut must be > 0");
+    cudaStream_t s = P->stream;
+    const int dim = P->dim;
+    P->free_assembly();
+    dfree(P->rowptr);
+    dfree(P->cols);
+    P->n = n;
+    P->nnz = 0;
+    P->maxk = 0;
+    DCPSE_CK(dalloc(&P->rowptr, (size_t)n + 1));
+    if (n == 0) {
+        DCPSE_CK(cudaMemsetAsync(P->rowptr, 0, sizeof(int64_t), s));
+        DCPSE_CK(dalloc(&P->cols, 1));
+        return DCPSE_OK;
+    }
+    unsigned long long* mm = nullptr;
+    DCPSE_CK(dalloc(&mm, 2 * kMaxDim));
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (P->has_box) {
+        for (int d = 0; d < dim; ++d) {
+            lo[d] = P->lo[d];
+            hi[d] = P->hi[d];
+        }
+    } else {
+        cudaError_t e = bounding_box(dim, d_pos, n, nullptr, 0, lo, hi, mm, s);
+        if (e != cudaSuccess) {
+            dfree(mm);
+            return fail(DCPSE_ERR_CUDA, std::string("bounding box: ") + cudaGetErrorString(e));
+        }
+        for (int d = 0; d < dim; ++d) {
+            P->lo[d] = lo[d];
+            P->hi[d] = hi[d];
+            P->per[d] = 0;
+            if (!std::isfinite(lo[d]) || !std::isfinite(hi[d])) {
+                dfree(mm);
+                return fail(DCPSE_ERR_ARG, "non-finite particle positions");
+            }
+        }
+    }
+    double rmax = rcut;
+    if (d_rcut_pp) {
+        double rlo[3], rhi[3];
+        cudaError_t e = bounding_box(1, d_rcut_pp, n, nullptr, 0, rlo, rhi, mm, s);
+        if (e != cudaSuccess) {
+            dfree(mm);
+            return fail(DCPSE_ERR_CUDA, std::string("rcut range: ") + cudaGetErrorString(e));
+        }
+        if (!(rlo[0] > 0.0) || !std::isfinite(rhi[0])) {
+            dfree(mm);
+            return fail(DCPSE_ERR_ARG, "per-particle radii must be finite and > 0");
+        }
+        rmax = std::max(rcut > 0 ? rcut : 0.0, rhi[0]);
+    }
+    dfree(mm);
+    // cells no smaller than the largest radius; total bounded by ~4 n
+    CellGrid cg{};
+    double cmin = rmax * (1.0 + 1e-9);
+    double cap = std::max(4.0 * (double)n, 1024.0);
+    for (int it = 0; it < 64; ++it) {
+        double total = 1.0;
+        for (int d = 0; d < kMaxDim; ++d) {
+            if (d < dim) {
+                double L = hi[d] - lo[d];
+                double m = (L > 0.0) ? std::floor(L / cmin) : 1.0;
+                if (!(m >= 1.0)) m = 1.0;
+                cg.nc[d] = (int)std::min(m, 1.0e6);
+                cg.cs[d] = (L > 0.0) ? L / (double)cg.nc[d] : 1.0;
+                cg.lo[d] = lo[d];
+            } else {
+                cg.nc[d] = 1;
+                cg.cs[d] = 1.0;
+                cg.lo[d] = 0.0;
+            }
+            total *= cg.nc[d];
+        }
+        if (total <= cap) break;
+        cmin *= 1.25;
+    }
+    const int64_t ncell = (int64_t)cg.nc[0] * cg.nc[1] * cg.nc[2];
+    int32_t *cell = nullptr, *ccount = nullptr, *cidx = nullptr, *counts = nullptr, *tmp = nullptr;
+    int64_t *cstart = nullptr, *fill = nullptr, *scan_tmp = nullptr;
+    double* spos = nullptr;
+    int* maxk = nullptr;
+    auto cleanup = [&]() {
+        dfree(cell);
+        dfree(ccount);
+        dfree(cidx);
+        dfree(counts);
+        dfree(tmp);
+        dfree(cstart);
+        dfree(fill);
+        dfree(scan_tmp);
+        dfree(spos);
+        dfree(maxk);
+    };
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = dalloc(&cell, n);
+    if (e == cudaSuccess) e = dalloc(&ccount, ncell);
+    if (e == cudaSuccess) e = dalloc(&cidx, n);
+    if (e == cudaSuccess) e = dalloc(&counts, n);
+    if (e == cudaSuccess) e = dalloc(&cstart, ncell + 1);
+    if (e == cudaSuccess) e = dalloc(&fill, ncell);
+    if (e == cudaSuccess) e = dalloc(&scan_tmp, scan_tmp_elems(std::max<int64_t>(ncell, n)));
+    if (e == cudaSuccess) e = dalloc(&spos, (size_t)n * dim);
+    if (e == cudaSuccess) e = dalloc(&maxk, 1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(maxk, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = build_cells(dim, d_pos, n, cg, cell, ccount, cstart, fill, cidx, spos, scan_tmp, s);
+    NbrArgs a{};
+    a.dim = dim;
+    a.pd = d_pos;
+    a.n_dom = n;
+    a.spos = spos;
+    a.cidx = cidx;
+    a.cstart = cstart;
+    a.cells = cg;
+    a.geom = plan_geom(P);
+    a.rcut = rcut;
+    a.rcut_pp = d_rcut_pp;
+    a.self_skip = 1;
+    if (e == cudaSuccess) e = count_neighbors(a, counts, maxk, s);
+    if (e == cudaSuccess) e = exclusive_scan_i32(counts, n, P->rowptr, scan_tmp, s);
+    int64_t nnz = 0;
+    int hk = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&nnz, P->rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hk, maxk, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = dalloc(&tmp, nnz);
+    if (e == cudaSuccess) e = dalloc(&P->cols, nnz);
+    if (e == cudaSuccess) e = fill_neighbors(a, P->rowptr, tmp, P->cols, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cleanup();
+    if (e != cudaSuccess) return fail(DCPSE_ERR_CUDA, std::string("neighbour build: ") + cudaGetErrorString(e));
+    P->nnz = nnz;
+    P->maxk = hk;
+    return DCPSE_OK;
+}
+
+int dcpse_set_neighbors(dcpse_plan_t* P, int64_t n, int64_t nnz, const int64_t* d_rowptr, const int32_t* d_cols) {
+    if (int rc = check_plan(P)) return rc;
+    if (n < 0 || nnz < 0 || !d_rowptr || (nnz > 0 && !d_cols)) return fail(DCPSE_ERR_ARG, "bad CSR arrays");
+    cudaStream_t s = P->stream;
+    P->free_assembly();
+    dfree(P->rowptr);
+    dfree(P->cols);
+    P->n = n;
+    P->nnz = nnz;
+    DCPSE_CK(dalloc(&P->rowptr, (size_t)n + 1));
+    DCPSE_CK(dalloc(&P->cols, nnz));
+    DCPSE_CK(cudaMemcpyAsync(P->rowptr, d_rowptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToDevice, s));
+    if (nnz > 0) DCPSE_CK(cudaMemcpyAsync(P->cols, d_cols, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, s));
+    int* mk = nullptr;
+    DCPSE_CK(dalloc(&mk, 1));
+    DCPSE_CK(cudaMemsetAsync(mk, 0, sizeof(int), s));
+    if (n > 0) row_max_kernel<<<std::max(1, std::min(num_sms() * 4, (int)((n + 255) / 256))), 256, 0, s>>>(P->rowptr, n, mk);
+    int hk = 0;
+    DCPSE_CK(cudaMemcpyAsync(&hk, mk, sizeof(int), cudaMemcpyDeviceToHost, s));
+    DCPSE_CK(cudaStreamSynchronize(s));
+    dfree(mk);
+    P->maxk = hk;
+    return DCPSE_OK;
+}
+
+int dcpse_neighbors_ptr(dcpse_plan_t* P, const int64_t** d_rowptr, const int32_t** d_cols) {
+    if (int rc = check_plan(P)) return rc;
+    if (P->n < 0) return fail(DCPSE_ERR_STATE, "no neighbour list");
+    if (d_rowptr) *d_rowptr = P->rowptr;
+    if (d_cols) *d_cols = P->cols;
+    return DCPSE_OK;
+}
+
+int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fixed, int flags) {
+    if (int rc = check_plan(P)) return rc;
+    if (P->n < 0) return fail(DCPSE_ERR_STATE, "build or set the neighbour list first");
+    if (P->n > 0 && !d_pos) return fail(DCPSE_ERR_ARG, "NULL positions");
+    if (!(flags & (DCPSE_STORE_TERMS_F64 | DCPSE_STORE_OUT_F64 | DCPSE_STORE_OUT_F32)))
+        return fail(DCPSE_ERR_ARG, "nothing to store");
+    if ((flags & DCPSE_ASSEMBLE_FAST) && (flags & DCPSE_STORE_TERMS_F64))
+        return fail(DCPSE_ERR_ARG, "per-term kernels need the reference (non-fast) assembly");
+    cudaStream_t s = P->stream;
+    const int64_t n = P->n, nnz = P->nnz;
+    const int ng = P->htab->ngroups;
+    // (re)allocate what this assembly stores
+    if (!P->eps) DCPSE_CK(dalloc(&P->eps, n));
+    if (!P->status) DCPSE_CK(dalloc(&P->status, n));
+    if (!P->eip_group) DCPSE_CK(dalloc(&P->eip_group, (size_t)ng * n));
+    if ((flags & DCPSE_STORE_TERMS_F64) && !P->k_term) DCPSE_CK(dalloc(&P->k_term, (size_t)P->nterms * nnz));
+    if (!(flags & DCPSE_STORE_TERMS_F64)) dfree(P->k_term);
+    if ((flags & DCPSE_STORE_OUT_F64) && !P->w64) DCPSE_CK(dalloc(&P->w64, (size_t)P->nout * nnz));
+    if (!(flags & DCPSE_STORE_OUT_F64)) dfree(P->w64);
+    if ((flags & DCPSE_STORE_OUT_F32) && !P->w32) DCPSE_CK(dalloc(&P->w32, (size_t)P->nout * nnz));
+    if (!(flags & DCPSE_STORE_OUT_F32)) dfree(P->w32);
+    AsmArgs a{};
+    a.tab = P->dtab;
+    a.dim = P->dim;
+    a.n = n;
+    a.pos = d_pos;
+    a.rowptr = P->rowptr;
+    a.cols = P->cols;
+    a.geom = plan_geom(P);
+    a.h_over_eps = P->hoe;
+    a.eps_fixed = d_eps_fixed;
+    a.flags = flags;
+    a.eps = P->eps;
+    a.status = P->status;
+    a.eip_group = P->eip_group;
+    a.k_term = P->k_term;
+    a.w64 = P->w64;
+    a.w32 = P->w32;
+    a.nnz = nnz;
+    P->tstart(DCPSE_K_ASSEMBLE);
+    cudaError_t e = assemble(a, *P->htab, s);
+    P->tstop(DCPSE_K_ASSEMBLE);
+    if (e != cudaSuccess) return fail(DCPSE_ERR_CUDA, std::string("assembly: ") + cudaGetErrorString(e));
+    P->assembled = true;
+    P->flags = flags;
+    unsigned long long init[2] = {0ull, ~0ull};
+    DCPSE_CK(cudaMemcpyAsync(P->summary, init, sizeof init, cudaMemcpyHostToDevice, s));
+    if (n > 0)
+        status_summary_kernel<<<std::max(1, std::min(num_sms() * 4, (int)((n + 255) / 256))), 256, 0, s>>>(
+            P->status, n, P->summary);
+    DCPSE_CK(cudaGetLastError());
+    if (flags & DCPSE_ASSEMBLE_ASYNC) return DCPSE_OK;
+    int64_t nb = 0, fb = -1;
+    int fc = 0;
+    int rc = dcpse_particle_status(P, &nb, &fb, &fc);
+    if (rc != DCPSE_OK) return rc;
+    if (nb > 0) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "%lld particle(s) could not be assembled; first %lld (status %d)",
+                      (long long)nb, (long long)fb, fc);
+        return fail(DCPSE_ERR_PARTICLES, buf);
+    }
+    return DCPSE_OK;
+}
+
+int dcpse_particle_status(dcpse_plan_t* P, int64_t* n_bad, int64_t* first_bad, int* first_code) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
+    unsigned long long h[2];
+    DCPSE_CK(cudaMemcpyAsync(h, P->summary, sizeof h, cudaMemcpyDeviceToHost, P->stream));
+    DCPSE_CK(cudaStreamSynchronize(P->stream));
+    int code = 0;
+    if (h[0] > 0)
+        DCPSE_CK(cudaMemcpy(&code, P->status + h[1], sizeof(int), cudaMemcpyDeviceToHost));
+    if (n_bad) *n_bad = (int64_t)h[0];
+    if (first_bad) *first_bad = h[0] > 0 ? (int64_t)h[1] : -1;
+    if (first_code) *first_code = code;
+    return DCPSE_OK;
+}
+
+int dcpse_eps_ptr(dcpse_plan_t* P, const double** d_eps, const int32_t** d_status) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
+    if (d_eps) *d_eps = P->eps;
+    if (d_status) *d_status = P->status;
+    return DCPSE_OK;
+}
+
+int dcpse_term_kernels_ptr(dcpse_plan_t* P, int term, const double** d_kernels, const double** d_eps_inv_pow) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
+    if (term < 0 || term >= P->nterms) return fail(DCPSE_ERR_ARG, "term out of range");
+    if (d_kernels) *d_kernels = P->k_term ? P->k_term + (size_t)term * P->nnz : nullptr;
+    if (d_eps_inv_pow) *d_eps_inv_pow = P->eip_group + (size_t)P->term_group[term] * P->n;
+    return DCPSE_OK;
+}
+
+int dcpse_output_weights_ptr(dcpse_plan_t* P, int output, const double** d_w64, const float** d_w32) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
+    if (output < 0 || output >= P->nout) return fail(DCPSE_ERR_ARG, "output out of range");
+    if (d_w64) *d_w64 = P->w64 ? P->w64 + (size_t)output * P->nnz : nullptr;
+    if (d_w32) *d_w32 = P->w32 ? P->w32 + (size_t)output * P->nnz : nullptr;
+    return DCPSE_OK;
+}
+
+int dcpse_apply_term_f64(dcpse_plan_t* P, int term, const double* d_f, double* d_out) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled || !P->k_term) return fail(DCPSE_ERR_STATE, "per-term FP64 kernels not stored");
+    if (term < 0 || term >= P->nterms) return fail(DCPSE_ERR_ARG, "term out of range");
+    if (P->n > 0 && (!d_f || !d_out)) return fail(DCPSE_ERR_ARG, "NULL field");
+    unsigned ord = 0;
+    for (int d = 0; d < P->dim; ++d) ord += P->sigs[term][d];
+    P->tstart(DCPSE_K_APPLY_TERM);
+    cudaError_t e = apply_term_f64(P->n, P->rowptr, P->cols, P->k_term + (size_t)term * P->nnz,
+                                   P->eip_group + (size_t)P->term_group[term] * P->n, ord, d_f, d_out, 0, P->stream);
+    P->tstop(DCPSE_K_APPLY_TERM);
+    DCPSE_CK(e);
+    return DCPSE_OK;
+}
+
+int dcpse_apply_output_f64(dcpse_plan_t* P, int output, const double* d_f, double* d_out) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled || !P->k_term) return fail(DCPSE_ERR_STATE, "per-term FP64 kernels not stored");
+    if (output < 0 || output >= P->nout) return fail(DCPSE_ERR_ARG, "output out of range");
+    if (P->n > 0 && (!d_f || !d_out)) return fail(DCPSE_ERR_ARG, "NULL field");
+    int first = 1;
+    for (int t = 0; t < P->nterms; ++t) {
+        if (P->term_output[t] != output) continue;
+        unsigned ord = 0;
+        for (int d = 0; d < P->dim; ++d) ord += P->sigs[t][d];
+        P->tstart(DCPSE_K_APPLY_TERM);
+        cudaError_t e = apply_term_f64(P->n, P->rowptr, P->cols, P->k_term + (size_t)t * P->nnz,
+                                       P->eip_group + (size_t)P->term_group[t] * P->n, ord, d_f, d_out,
+                                       first ? 0 : 1, P->stream);
+        P->tstop(DCPSE_K_APPLY_TERM);
+        DCPSE_CK(e);
+        first = 0;
+    }
+    return DCPSE_OK;
+}
+
+int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int precision) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
+    if (P->n > 0 && (!d_f || !d_out)) return fail(DCPSE_ERR_ARG, "NULL field");
+    if (precision == DCPSE_F32) {
+        if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
+        if (!P->f2) DCPSE_CK(dalloc(&P->f2, P->n));
+        P->tstart(DCPSE_K_SPLIT);
+        cudaError_t e = split_f64(d_f, P->n, P->f2, P->stream);
+        P->tstop(DCPSE_K_SPLIT);
+        DCPSE_CK(e);
+        P->tstart(DCPSE_K_APPLY_BATCHED);
+        e = apply_batched_f32(P->n, P->nout, P->rowptr, P->cols, P->w32, P->nnz, P->f2, d_out, P->stream);
+        P->tstop(DCPSE_K_APPLY_BATCHED);
+        DCPSE_CK(e);
+    } else if (precision == DCPSE_F64) {
+        if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
+        P->tstart(DCPSE_K_APPLY_BATCHED);
+        cudaError_t e = apply_batched_f64(P->n, P->nout, P->rowptr, P->cols, P->w64, P->nnz, d_f, d_out, P->stream);
+        P->tstop(DCPSE_K_APPLY_BATCHED);
+        DCPSE_CK(e);
+    } else {
+        return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
+    }
+    return DCPSE_OK;
+}
+
+int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, int precision) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
+    if (P->n > 0 && (!h_f || !h_out)) return fail(DCPSE_ERR_ARG, "NULL field");
+    if (!P->hf) DCPSE_CK(dalloc(&P->hf, P->n));
+    if (!P->hout) DCPSE_CK(dalloc(&P->hout, (size_t)P->nout * P->n));
+    DCPSE_CK(cudaMemcpyAsync(P->hf, h_f, sizeof(double) * P->n, cudaMemcpyHostToDevice, P->stream));
+    int rc = dcpse_apply_batched(P, P->hf, P->hout, precision);
+    if (rc != DCPSE_OK) return rc;
+    DCPSE_CK(cudaMemcpyAsync(h_out, P->hout, sizeof(double) * P->nout * P->n, cudaMemcpyDeviceToHost, P->stream));
+    DCPSE_CK(cudaStreamSynchronize(P->stream));
+    return DCPSE_OK;
+}
+
+int dcpse_plan_set_timing(dcpse_plan_t* P, int enable) {
+    if (int rc = check_plan(P)) return rc;
+    P->timing = enable != 0;
+    return DCPSE_OK;
+}
+
+int dcpse_plan_timing(dcpse_plan_t* P, int kernel, double* total_ms, int64_t* launches) {
+    if (int rc = check_plan(P)) return rc;
+    if (kernel < 0 || kernel >= DCPSE_K_COUNT) return fail(DCPSE_ERR_ARG, "kernel id out of range");
+    DCPSE_CK(cudaStreamSynchronize(P->stream));
+    double tot = 0.0;
+    KernelTimer& T = P->timers[kernel];
+    for (size_t i = 0; i < T.used; ++i) {
+        float ms = 0.f;
+        DCPSE_CK(cudaEventElapsedTime(&ms, T.ev[i].first, T.ev[i].second));
+        tot += ms;
+    }
+    if (total_ms) *total_ms = tot;
+    if (launches) *launches = (int64_t)T.used;
+    return DCPSE_OK;
+}
+
+int dcpse_plan_reset_timing(dcpse_plan_t* P) {
+    if (int rc = check_plan(P)) return rc;
+    DCPSE_CK(cudaStreamSynchronize(P->stream));
+    for (auto& T : P->timers) T.used = 0;
+    return DCPSE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,131 @@
+// dcpse_internal.h -- host-side interfaces between the C-ABI layer and the
+// kernel translation units of the GB300 DC-PSE path.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dcpse_common.cuh"
+#include "openfpm_dcpse/dcpse_capi.h"
+
+#define DCPSE_ASSEMBLE_FAST_FLAG DCPSE_ASSEMBLE_FAST
+
+namespace dcpse {
+
+// ------------------------------------------------------------ neighbours --
+struct CellGrid {
+    double lo[kMaxDim];
+    double cs[kMaxDim];
+    int nc[kMaxDim];
+};
+
+// Exclusive scan of n int32 counts into out[0..n] (out[n] = total).
+// tmp must hold scan_tmp_elems(n) int64 values.
+int64_t scan_tmp_elems(int64_t n);
+cudaError_t exclusive_scan_i32(const int32_t* in, int64_t n, int64_t* out, int64_t* tmp, cudaStream_t s);
+
+// Bounding box of n_a + n_b points (lo/hi written to host arrays).
+cudaError_t bounding_box(int dim, const double* a, int64_t na, const double* b, int64_t nb, double* lo,
+                         double* hi, unsigned long long* d_tmp /* 2*kMaxDim */, cudaStream_t s);
+
+// Cell list of the support set: cell_start[ncell+1], cidx[n], spos[n*dim]
+// (positions in cell order).  d_cell (n) and d_fill (ncell) are scratch.
+cudaError_t build_cells(int dim, const double* pos, int64_t n, const CellGrid& g, int32_t* d_cell,
+                        int32_t* d_ccount, int64_t* d_cstart, int64_t* d_fill, int32_t* d_cidx, double* d_spos,
+                        int64_t* d_scan_tmp, cudaStream_t s);
+
+struct NbrArgs {
+    int dim;
+    const double* pd;   // domain positions
+    int64_t n_dom;
+    const double* spos; // support positions, cell order
+    const int32_t* cidx;
+    const int64_t* cstart;
+    CellGrid cells;
+    Geom geom;
+    double rcut;
+    const double* rcut_pp;
+    int self_skip;
+};
+
+// Count pass: counts[p] = number of neighbours; also atomically maxes *d_maxk.
+cudaError_t count_neighbors(const NbrArgs& a, int32_t* counts, int* d_maxk, cudaStream_t s);
+// Fill pass: unsorted neighbours of p into tmp[rowptr[p] ...], then sorted
+// ascending into cols.
+cudaError_t fill_neighbors(const NbrArgs& a, const int64_t* rowptr, int32_t* tmp, int32_t* cols,
+                           cudaStream_t s);
+
+// --------------------------------------------------------------- assembly --
+// Tables describing the bases of a plan, resident on the device.
+constexpr int kMaxUnion = 64;    // distinct monomials over all bases
+constexpr int kMaxGroups = 4;    // distinct |alpha| among the terms
+constexpr int kMaxBasis = 35;    // basis size per group (3D order 4 = 34)
+constexpr int kMaxTerms = 16;    // reference Dcpse objects per plan
+constexpr int kMaxOutputs = 8;
+constexpr int kMaxRhs = 8;       // right-hand sides per group
+constexpr int kMaxPairs = 1280;  // Gram entries (i <= j) needed by some group
+constexpr int kMaxExp = 8;       // highest exponent + 1
+
+struct AsmTables {
+    int dim;
+    int nu;                       // union basis size
+    unsigned char uexp[kMaxUnion][kMaxDim];
+    int maxexp;                   // largest exponent over the union, plus one
+    int npairs;
+    unsigned char pi[kMaxPairs], pj[kMaxPairs];  // union indices, pi <= pj
+    short upair[kMaxUnion][kMaxUnion];           // (lo, hi) union indices -> pair
+    int ngroups;
+    int gn[kMaxGroups];           // basis size
+    int gord[kMaxGroups];         // |alpha| of the group
+    unsigned char gidx[kMaxGroups][kMaxBasis];   // group basis -> union index
+    // right-hand sides per group: columns either per term (faithful mode) or
+    // per output (fast mode)
+    int nterm_rhs[kMaxGroups];
+    int term_of_rhs[kMaxGroups][kMaxRhs];        // term id of each faithful rhs
+    int nout_rhs[kMaxGroups];
+    int out_of_rhs[kMaxGroups][kMaxRhs];         // output id of each fast rhs
+    double b_term[kMaxGroups][kMaxRhs][kMaxBasis];
+    double b_out[kMaxGroups][kMaxRhs][kMaxBasis];
+    int nterms;
+    int term_group[kMaxTerms];
+    int term_output[kMaxTerms];
+    int noutputs;
+};
+
+struct AsmArgs {
+    const AsmTables* tab;  // device copy
+    int dim;
+    int64_t n;
+    const double* pos;
+    const int64_t* rowptr;
+    const int32_t* cols;
+    Geom geom;
+    double h_over_eps;
+    const double* eps_fixed;
+    int flags;
+    // outputs
+    double* eps;
+    int32_t* status;
+    double* eip_group;   // [ngroups][n]
+    double* k_term;      // [nterms][nnz]   (faithful kernels) or nullptr
+    double* w64;         // [noutputs][nnz] (summed, eps folded) or nullptr
+    float* w32;          // [noutputs][nnz] or nullptr
+    int64_t nnz;
+};
+
+// h: host copy of *a.tab (launch configuration is derived from it)
+cudaError_t assemble(const AsmArgs& a, const AsmTables& h, cudaStream_t s);
+
+// ----------------------------------------------------------------- apply --
+cudaError_t apply_term_f64(int64_t n, const int64_t* rowptr, const int32_t* cols, const double* K,
+                           const double* eip, unsigned ord, const double* f, double* out, int accumulate,
+                           cudaStream_t s);
+cudaError_t split_f64(const double* f, int64_t n, float2* f2, cudaStream_t s);
+cudaError_t apply_batched_f32(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const float* w,
+                              int64_t nnz, const float2* f2, double* out, cudaStream_t s);
+cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const double* w,
+                              int64_t nnz, const double* f, double* out, cudaStream_t s);
+
+int num_sms();
+
+}  // namespace dcpse

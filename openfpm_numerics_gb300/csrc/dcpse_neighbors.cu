@@ -1,0 +1,349 @@
+// dcpse_neighbors.cu -- device neighbour lists (CSR) for the DC-PSE path.
+//
+// Replaces the reference's two support builders:
+//  * CPU: openfpm VerletList getVerlet<VL_NON_SYMMETRIC|VL_SKIP_REF_PART>
+//    (used by src/DCPSE/Dcpse.hpp:721 via getNNIterator);
+//  * GPU: gatherSupportSize_gpu / assembleSupport_gpu with a host prefix sum
+//    (src/DCPSE/SupportBuilder.cuh:14-107).
+// Here every step stays on the device: cell ids, counting sort into cells,
+// a count pass, a device exclusive scan, a fill pass and a per-row sort.
+// The list of particle p is every q != p with |x_p - x_q|^2 < rc_p^2 in
+// ascending q, so it does not depend on the cell size or on the order in
+// which atomics filled the cells.
+#include <cstring>
+
+#include "dcpse_internal.h"
+
+namespace dcpse {
+
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int64_t warp_incl_scan(int64_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int64_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan (blockDim a multiple of 32); returns the
+// exclusive prefix of v and the block total in *tot.
+__device__ int64_t block_excl_scan(int64_t v, int64_t* tot) {
+    __shared__ int64_t warp_sums[33];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int64_t inc = warp_incl_scan(v);
+    if (lane == 31) warp_sums[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int64_t w = (lane < nw) ? warp_sums[lane] : 0;
+        int64_t wi = warp_incl_scan(w);
+        if (lane < nw) warp_sums[lane] = wi - w;
+        if (lane == 31) warp_sums[32] = wi;
+    }
+    __syncthreads();
+    int64_t r = warp_sums[wid] + inc - v;
+    *tot = warp_sums[32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void scan_tile_sums(const int32_t* __restrict__ in, int64_t n, int64_t* __restrict__ tile_sums) {
+    int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    int64_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i)
+        if (base + i < n) s += in[base + i];
+    int64_t tot;
+    block_excl_scan(s, &tot);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
+}
+
+// single block: exclusive scan of tile sums in place; tile_sums[ntiles] = total
+__global__ void scan_tile_offsets(int64_t* tile_sums, int64_t ntiles) {
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t b = 0; b < ntiles; b += blockDim.x) {
+        int64_t i = b + threadIdx.x;
+        int64_t v = (i < ntiles) ? tile_sums[i] : 0;
+        int64_t tot;
+        int64_t ex = block_excl_scan(v, &tot);
+        int64_t c = carry;
+        if (i < ntiles) tile_sums[i] = c + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry = c + tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tile_sums[ntiles] = carry;
+}
+
+__global__ void scan_tiles(const int32_t* __restrict__ in, int64_t n, const int64_t* __restrict__ tile_off,
+                           int64_t* __restrict__ out) {
+    int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    int64_t v[kScanItems];
+    int64_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        v[i] = (base + i < n) ? (int64_t)in[base + i] : 0;
+        s += v[i];
+    }
+    int64_t tot;
+    int64_t ex = block_excl_scan(s, &tot) + tile_off[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        if (base + i < n) out[base + i] = ex;
+        ex += v[i];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = tile_off[gridDim.x];
+}
+
+__device__ __forceinline__ unsigned long long ord_of(double x) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+double from_ord(unsigned long long u) {
+    u = (u >> 63) ? (u & 0x7fffffffffffffffull) : ~u;
+    double d;
+    memcpy(&d, &u, sizeof d);
+    return d;
+}
+
+__global__ void bbox_kernel(int dim, const double* __restrict__ p, int64_t n, unsigned long long* mm) {
+    double lo[kMaxDim], hi[kMaxDim];
+    for (int d = 0; d < kMaxDim; ++d) {
+        lo[d] = INFINITY;
+        hi[d] = -INFINITY;
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        for (int d = 0; d < dim; ++d) {
+            double x = p[i * dim + d];
+            lo[d] = fmin(lo[d], x);
+            hi[d] = fmax(hi[d], x);
+        }
+    for (int d = 0; d < dim; ++d) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(&mm[d], ord_of(lo[d]));
+            atomicMax(&mm[kMaxDim + d], ord_of(hi[d]));
+        }
+    }
+}
+
+__device__ __forceinline__ int cell_coord(double x, double lo, double cs, int nc) {
+    double v = floor((x - lo) / cs);
+    if (!(v >= 0.0)) return 0;  // also catches NaN
+    if (v >= (double)nc) return nc - 1;
+    return (int)v;
+}
+
+__global__ void cell_id_kernel(int dim, const double* __restrict__ pos, int64_t n, CellGrid g,
+                               int32_t* __restrict__ cell, int32_t* __restrict__ ccount) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int c[kMaxDim] = {0, 0, 0};
+        for (int d = 0; d < dim; ++d) c[d] = cell_coord(pos[i * dim + d], g.lo[d], g.cs[d], g.nc[d]);
+        int lin = c[0] + g.nc[0] * (c[1] + g.nc[1] * c[2]);
+        cell[i] = lin;
+        atomicAdd(&ccount[lin], 1);
+    }
+}
+
+__global__ void cell_fill_kernel(int dim, const double* __restrict__ pos, int64_t n, const int32_t* __restrict__ cell,
+                                 int64_t* fill, int32_t* __restrict__ cidx, double* __restrict__ spos) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        unsigned long long slot = atomicAdd((unsigned long long*)&fill[cell[i]], 1ull);
+        cidx[slot] = (int32_t)i;
+        for (int d = 0; d < dim; ++d) spos[slot * dim + d] = pos[i * dim + d];
+    }
+}
+
+// Stencil cells of particle p along one axis (deduplicated when a periodic
+// axis has fewer than three cells).
+__device__ __forceinline__ int axis_cells(int c, int nc, int per, int* out) {
+    int cnt = 0;
+    for (int o = -1; o <= 1; ++o) {
+        int v = c + o;
+        if (per) {
+            v = ((v % nc) + nc) % nc;
+        } else if (v < 0 || v >= nc) {
+            continue;
+        }
+        bool dup = false;
+        for (int t = 0; t < cnt; ++t) dup |= (out[t] == v);
+        if (!dup) out[cnt++] = v;
+    }
+    return cnt;
+}
+
+template <int DIM, bool FILL>
+__global__ void __launch_bounds__(256) nbr_kernel(NbrArgs a, int32_t* __restrict__ counts, int* maxk,
+                                                  const int64_t* __restrict__ rowptr, int32_t* __restrict__ tmp) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    for (int64_t p = warp0; p < a.n_dom; p += nwarps) {
+        double xp[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xp[d] = a.pd[p * DIM + d];
+        const double rc = a.rcut_pp ? a.rcut_pp[p] : a.rcut;
+        const double rc2 = rc * rc;
+        int lst[3][3];
+        int cnt[3] = {1, 1, 1};
+        lst[0][0] = lst[1][0] = lst[2][0] = 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            int c = cell_coord(xp[d], a.cells.lo[d], a.cells.cs[d], a.cells.nc[d]);
+            cnt[d] = axis_cells(c, a.cells.nc[d], a.geom.per[d], lst[d]);
+        }
+        int64_t base = FILL ? rowptr[p] : 0;
+        int k = 0;
+        for (int a2 = 0; a2 < cnt[2]; ++a2)
+            for (int a1 = 0; a1 < cnt[1]; ++a1)
+                for (int a0 = 0; a0 < cnt[0]; ++a0) {
+                    int cc = lst[0][a0] + a.cells.nc[0] * (lst[1][a1] + a.cells.nc[1] * lst[2][a2]);
+                    int64_t cb = a.cstart[cc], ce = a.cstart[cc + 1];
+                    for (int64_t t0 = cb; t0 < ce; t0 += 32) {
+                        int64_t t = t0 + lane;
+                        bool acc = false;
+                        int32_t q = -1;
+                        if (t < ce) {
+                            q = a.cidx[t];
+                            double o[DIM];
+#pragma unroll
+                            for (int d = 0; d < DIM; ++d) o[d] = offset1(a.geom, d, xp[d], a.spos[t * DIM + d]);
+                            acc = norm2<DIM>(o) < rc2;
+                            if (a.self_skip && (int64_t)q == p) acc = false;
+                        }
+                        unsigned bal = __ballot_sync(0xffffffffu, acc);
+                        if (FILL && acc) tmp[base + k + __popc(bal & lt_mask)] = q;
+                        k += __popc(bal);
+                    }
+                }
+        if (!FILL && lane == 0) {
+            counts[p] = k;
+            atomicMax(maxk, k);
+        }
+    }
+}
+
+// Warp per row: rank of each entry among the row's entries -> sorted output.
+__global__ void __launch_bounds__(256) sort_rows_kernel(int64_t n, const int64_t* __restrict__ rowptr,
+                                                        const int32_t* __restrict__ tmp, int32_t* __restrict__ cols) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t p = warp0; p < n; p += nwarps) {
+        int64_t b = rowptr[p], e = rowptr[p + 1];
+        int k = (int)(e - b);
+        for (int i0 = 0; i0 < k; i0 += 32) {
+            int i = i0 + lane;
+            int32_t v = (i < k) ? tmp[b + i] : 0;
+            int rank = 0;
+            for (int j = 0; j < k; ++j) rank += (tmp[b + j] < v);
+            if (i < k) cols[b + rank] = v;
+        }
+    }
+}
+
+int grid_for(int64_t items, int per_block) {
+    int64_t g = (items + per_block - 1) / per_block;
+    int64_t cap = (int64_t)num_sms() * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+int num_sms() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
+int64_t scan_tmp_elems(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+cudaError_t exclusive_scan_i32(const int32_t* in, int64_t n, int64_t* out, int64_t* tmp, cudaStream_t s) {
+    int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+    if (ntiles == 0) {
+        return cudaMemsetAsync(out, 0, sizeof(int64_t), s);
+    }
+    scan_tile_sums<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, tmp);
+    scan_tile_offsets<<<1, kScanThreads, 0, s>>>(tmp, ntiles);
+    scan_tiles<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, tmp, out);
+    return cudaGetLastError();
+}
+
+cudaError_t bounding_box(int dim, const double* a, int64_t na, const double* b, int64_t nb, double* lo, double* hi,
+                         unsigned long long* d_tmp, cudaStream_t s) {
+    unsigned long long init[2 * kMaxDim];
+    for (int d = 0; d < kMaxDim; ++d) {
+        init[d] = ~0ull;
+        init[kMaxDim + d] = 0ull;
+    }
+    cudaError_t e = cudaMemcpyAsync(d_tmp, init, sizeof init, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    if (na > 0) bbox_kernel<<<grid_for(na, 256), 256, 0, s>>>(dim, a, na, d_tmp);
+    if (nb > 0 && b != a) bbox_kernel<<<grid_for(nb, 256), 256, 0, s>>>(dim, b, nb, d_tmp);
+    unsigned long long res[2 * kMaxDim];
+    e = cudaMemcpyAsync(res, d_tmp, sizeof res, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    for (int d = 0; d < dim; ++d) {
+        lo[d] = from_ord(res[d]);
+        hi[d] = from_ord(res[kMaxDim + d]);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t build_cells(int dim, const double* pos, int64_t n, const CellGrid& g, int32_t* d_cell, int32_t* d_ccount,
+                        int64_t* d_cstart, int64_t* d_fill, int32_t* d_cidx, double* d_spos, int64_t* d_scan_tmp,
+                        cudaStream_t s) {
+    int64_t ncell = (int64_t)g.nc[0] * g.nc[1] * g.nc[2];
+    cudaError_t e = cudaMemsetAsync(d_ccount, 0, sizeof(int32_t) * ncell, s);
+    if (e != cudaSuccess) return e;
+    if (n > 0) cell_id_kernel<<<grid_for(n, 256), 256, 0, s>>>(dim, pos, n, g, d_cell, d_ccount);
+    e = exclusive_scan_i32(d_ccount, ncell, d_cstart, d_scan_tmp, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(d_fill, d_cstart, sizeof(int64_t) * ncell, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    if (n > 0) cell_fill_kernel<<<grid_for(n, 256), 256, 0, s>>>(dim, pos, n, d_cell, d_fill, d_cidx, d_spos);
+    return cudaGetLastError();
+}
+
+cudaError_t count_neighbors(const NbrArgs& a, int32_t* counts, int* d_maxk, cudaStream_t s) {
+    if (a.n_dom == 0) return cudaSuccess;
+    int grid = grid_for(a.n_dom * 32, 256);
+    if (a.dim == 1) nbr_kernel<1, false><<<grid, 256, 0, s>>>(a, counts, d_maxk, nullptr, nullptr);
+    else if (a.dim == 2) nbr_kernel<2, false><<<grid, 256, 0, s>>>(a, counts, d_maxk, nullptr, nullptr);
+    else nbr_kernel<3, false><<<grid, 256, 0, s>>>(a, counts, d_maxk, nullptr, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t fill_neighbors(const NbrArgs& a, const int64_t* rowptr, int32_t* tmp, int32_t* cols, cudaStream_t s) {
+    if (a.n_dom == 0) return cudaSuccess;
+    int grid = grid_for(a.n_dom * 32, 256);
+    if (a.dim == 1) nbr_kernel<1, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
+    else if (a.dim == 2) nbr_kernel<2, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
+    else nbr_kernel<3, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
+    sort_rows_kernel<<<grid, 256, 0, s>>>(a.n_dom, rowptr, tmp, cols);
+    return cudaGetLastError();
+}
+
+}  // namespace dcpse

@@ -1,0 +1,272 @@
+"""Python mirror of openfpm_numerics' DC-PSE operator API.
+
+Same names, constructor arguments and semantics as
+src/DCPSE/DCPSE_op/DCPSE_op.hpp (Derivative_x_T ... Laplacian_T, Gradient_T,
+Derivative_G_T; CPU aliases at :3485-3508, GPU aliases at :3510-3530):
+
+    parts = ParticleSet(pos)                    # vector_dist stand-in (GPU)
+    vl = parts.getVerlet(rCut)                  # getVerlet<VL_NON_SYMMETRIC|VL_SKIP_REF_PART>
+    Lap = Laplacian(parts, vl, 2, rCut)         # assembles on the GPU
+    d2f = Lap(f)                                # getV<1>(parts) = Lap(getV<0>(parts))
+    Lap.update(parts)                           # after particles moved (initializeUpdate)
+
+Calling an operator applies it in FP64 in the reference's operation order
+(bit-exact with the CPU oracle).  ``op(f, precision="f32")`` uses the batched
+FP32-weight path instead.  Errors follow the reference: too few neighbours
+raise ``ValueError`` (std::length_error in Vandermonde.hpp:109-112) unless the
+operator was built with ``allow_failed_particles=True``.
+"""
+from __future__ import annotations
+
+import enum
+
+import torch
+
+from . import _capi as C
+from .plan import DcpsePlan
+
+dcpse_oversampling_factor = 1.9  # DCPSE_op.hpp:20
+rcut_verlet = 3.1                # DCPSE_op.hpp:21
+
+
+class support_options(enum.IntEnum):
+    """src/DCPSE/SupportBuilder.hpp:13-19"""
+    RADIUS = 0
+    LOAD = 1
+    ADAPTIVE = 2
+    AT_LEAST_N_PARTICLES = 3
+
+
+class VerletList:
+    """Neighbour lists in CSR form (rowptr int64 [n+1], cols int32), built on
+    the device: every q != p with |x_p - x_q|^2 < rCut^2, ascending q."""
+
+    def __init__(self, parts, rCut, rcut_pp=None):
+        self.rCut = float(rCut)
+        plan = DcpsePlan(parts.dims, [[(1,) + (0,) * (parts.dims - 1)]], box=parts.box)
+        plan.build_neighbors(parts.getPosTensor(), self.rCut, rcut_pp)
+        rp, cl = plan.neighbors()
+        self.rowptr = rp.clone()
+        self.cols = cl.clone()
+        plan.close()
+
+    def getNNPart(self, p):
+        return int(self.rowptr[p + 1] - self.rowptr[p])
+
+    def get(self, p, j):
+        return int(self.cols[int(self.rowptr[p]) + j])
+
+
+class ParticleSet:
+    """Minimal stand-in for openfpm's vector_dist on one GPU: positions as a
+    float64 [n, dim] CUDA tensor, optional box with periodicity, and named
+    properties."""
+
+    def __init__(self, pos, box=None, periodic=None):
+        if not isinstance(pos, torch.Tensor):
+            pos = torch.as_tensor(pos, dtype=torch.float64)
+        self.pos = pos.to(device="cuda", dtype=torch.float64).contiguous()
+        self.dims = self.pos.shape[1]
+        self.box = None
+        if box is not None:
+            lo, hi = box
+            self.box = (tuple(lo), tuple(hi), tuple(periodic) if periodic is not None else (0,) * self.dims)
+        self.props = {}
+        self._map_ctr = 0
+
+    def size_local(self):
+        return self.pos.shape[0]
+
+    def getPosTensor(self):
+        return self.pos
+
+    def getPos(self, p):
+        return self.pos[p]
+
+    def setPos(self, pos):
+        self.pos = pos.to(device="cuda", dtype=torch.float64).contiguous()
+        self._map_ctr += 1
+
+    def getVerlet(self, rCut):
+        return VerletList(self, rCut)
+
+    def ghost_get_subset(self):
+        """No-op: a single GPU holds all particles; periodic images are
+        handled by minimum-image offsets."""
+
+
+def _unit(dim, axis, power=1):
+    return tuple(power if d == axis else 0 for d in range(dim))
+
+
+class _DcpseOp:
+    """Common machinery: one plan holding the operator's reference terms."""
+
+    _kind = None  # "single" | "sum" | "vector"
+
+    def __init__(self, parts, verletList, ord, rCut, opt=support_options.RADIUS, *, outputs, kind,
+                 allow_failed_particles=False, h_over_eps=0.9):
+        if opt not in (support_options.RADIUS, support_options.LOAD):
+            raise NotImplementedError("support option %r" % (opt,))
+        self.dim = parts.dims
+        self.ord = int(ord)
+        self.rCut = float(rCut)
+        self._outputs = outputs
+        self._kind = kind
+        self._allow = allow_failed_particles
+        self.HOverEpsilon = h_over_eps
+        self.verletList = verletList
+        self.plan = DcpsePlan(self.dim, outputs, order=self.ord, h_over_eps=h_over_eps, box=parts.box)
+        self.plan.set_neighbors(verletList.rowptr, verletList.cols)
+        self._assembled = False
+        if opt == support_options.RADIUS:
+            self._assemble(parts)
+
+    def _assemble(self, parts):
+        rc = self.plan.assemble(parts.getPosTensor(),
+                                C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+        if rc == C.ERR_PARTICLES and not self._allow:
+            nb, first, code = self.plan.particle_status()
+            if code == C.PART_TOO_FEW:
+                raise ValueError("Not enough neighbour points passed for Vandermonde matrix construction! "
+                                 "(%d particles, first %d)" % (nb, first))
+            raise RuntimeError("DC-PSE assembly failed for %d particles (first %d, status %d)" % (nb, first, code))
+        self._assembled = True
+
+    def update(self, parts, verletList=None):
+        """initializeUpdate (Dcpse.hpp:675-687): re-assemble after particles
+        moved; pass the updated Verlet list (the reference requires
+        updateVerlet first)."""
+        if verletList is not None:
+            self.verletList = verletList
+        self.plan.set_neighbors(self.verletList.rowptr, self.verletList.cols)
+        self._assemble(parts)
+
+    def deallocate(self, parts=None):
+        self.plan.close()
+
+    def __call__(self, f, precision="f64"):
+        if not self._assembled:
+            raise RuntimeError("operator not assembled (support_options.LOAD without update)")
+        if isinstance(f, str):
+            raise TypeError("pass the field tensor")
+        f = f.to(device="cuda", dtype=torch.float64).contiguous()
+        if precision == "f64":
+            res = [self.plan.apply_output_f64(o, f) for o in range(len(self._outputs))]
+            out = torch.stack(res) if len(res) > 1 else res[0]
+        elif precision in ("f32", "f64-batched"):
+            out = self.plan.apply(f, C.F32 if precision == "f32" else C.F64)
+            out = out if len(self._outputs) > 1 else out[0]
+        else:
+            raise ValueError("precision must be 'f64', 'f64-batched' or 'f32'")
+        return out
+
+    # accessors of the reference (Dcpse.hpp:507-550), for the first term
+    def getNumNN(self, p):
+        return self.verletList.getNNPart(p)
+
+    def getIndexNN(self, p, j):
+        return self.verletList.get(p, j)
+
+    def getCoeffNN(self, p, j, term=0):
+        K, _ = self.plan.term_kernels(term)
+        return float(K[int(self.verletList.rowptr[p]) + j])
+
+    def getEpsilonInvPrefactor(self, p, term=0):
+        _, eip = self.plan.term_kernels(term)
+        return float(eip[p])
+
+    def getSign(self, term=0):
+        order = sum(self._outputs_flat()[term])
+        return -1.0 if (order % 2 == 0 and order != 0) else 1.0
+
+    def _outputs_flat(self):
+        return [s for o in self._outputs for s in o]
+
+
+class Derivative_G(_DcpseOp):
+    """Derivative_G_T (DCPSE_op.hpp:3387-3482): arbitrary signature p."""
+
+    def __init__(self, parts, verletList, ord, rCut, p, opt=support_options.RADIUS, **kw):
+        super().__init__(parts, verletList, ord, rCut, opt, outputs=[[tuple(p)]], kind="single", **kw)
+
+
+def _single(name, sig_fn, ref):
+    def init(self, parts, verletList, ord, rCut, opt=support_options.RADIUS, **kw):
+        _DcpseOp.__init__(self, parts, verletList, ord, rCut, opt, outputs=[[sig_fn(parts.dims)]], kind="single",
+                          **kw)
+
+    return type(name, (_DcpseOp,), {"__init__": init, "__doc__": "%s (%s)" % (name, ref)})
+
+
+Derivative_x = _single("Derivative_x", lambda d: _unit(d, 0), "DCPSE_op.hpp:649-797")
+Derivative_y = _single("Derivative_y", lambda d: _unit(d, 1), "DCPSE_op.hpp:799-941")
+Derivative_z = _single("Derivative_z", lambda d: _unit(d, 2), "DCPSE_op.hpp:943-1079")
+Derivative_xx = _single("Derivative_xx", lambda d: _unit(d, 0, 2), "DCPSE_op.hpp:2216-2358")
+Derivative_yy = _single("Derivative_yy", lambda d: _unit(d, 1, 2), "DCPSE_op.hpp:2360-2502")
+Derivative_zz = _single("Derivative_zz", lambda d: _unit(d, 2, 2), "DCPSE_op.hpp:2504-2634")
+Derivative_xy = _single("Derivative_xy", lambda d: tuple(1 if i < 2 else 0 for i in range(d)),
+                        "DCPSE_op.hpp:1783-1925")
+Derivative_yz = _single("Derivative_yz", lambda d: tuple(1 if i in (1, 2) else 0 for i in range(d)),
+                        "DCPSE_op.hpp:1927-2069")
+Derivative_xz = _single("Derivative_xz", lambda d: tuple(1 if i in (0, 2) else 0 for i in range(d)),
+                        "DCPSE_op.hpp:2071-2214")
+Derivative_xxx = _single("Derivative_xxx", lambda d: _unit(d, 0, 3), "DCPSE_op.hpp:2636-2774")
+Derivative_yyy = _single("Derivative_yyy", lambda d: _unit(d, 1, 3), "DCPSE_op.hpp:3056-3192")
+Derivative_xxy = _single("Derivative_xxy", lambda d: tuple({0: 2, 1: 1}.get(i, 0) for i in range(d)),
+                         "DCPSE_op.hpp:2776-2914")
+Derivative_yyx = _single("Derivative_yyx", lambda d: tuple({0: 1, 1: 2}.get(i, 0) for i in range(d)),
+                         "DCPSE_op.hpp:2916-3054")
+Derivative_xxxx = _single("Derivative_xxxx", lambda d: _unit(d, 0, 4), "DCPSE_op.hpp:3194-3256")
+Derivative_yyyy = _single("Derivative_yyyy", lambda d: _unit(d, 1, 4), "DCPSE_op.hpp:3258-3320")
+Derivative_xxyy = _single("Derivative_xxyy", lambda d: tuple({0: 2, 1: 2}.get(i, 0) for i in range(d)),
+                          "DCPSE_op.hpp:3322-3385")
+
+
+class Laplacian(_DcpseOp):
+    """Laplacian_T (DCPSE_op.hpp:1350-1500): sum of dim Dcpse objects with
+    signatures 2e_i, evaluated as VECT_DCPSE_V_SUM (:388-399)."""
+
+    def __init__(self, parts, verletList, ord, rCut, opt=support_options.RADIUS, **kw):
+        d = parts.dims
+        super().__init__(parts, verletList, ord, rCut, opt, outputs=[[_unit(d, i, 2) for i in range(d)]],
+                         kind="sum", **kw)
+
+
+class Gradient(_DcpseOp):
+    """Gradient_T (DCPSE_op.hpp:1081-1224): dim Dcpse objects e_i evaluated as
+    VECT_DCPSE_V (:144-153); the result is a [dim, n] tensor."""
+
+    def __init__(self, parts, verletList, ord, rCut, opt=support_options.RADIUS, **kw):
+        d = parts.dims
+        super().__init__(parts, verletList, ord, rCut, opt, outputs=[[_unit(d, i)] for i in range(d)],
+                         kind="vector", **kw)
+
+
+class OperatorSet(_DcpseOp):
+    """Several operators assembled and applied together over one neighbour
+    list (one persistent assembly launch, one apply pass).  ``ops`` is a list
+    of operator names ('x','y','z','xx',...,'laplacian','gradient')."""
+
+    def __init__(self, parts, verletList, ord, rCut, ops, opt=support_options.RADIUS, **kw):
+        d = parts.dims
+        outs = []
+        for name in ops:
+            if name == "laplacian":
+                outs.append([_unit(d, i, 2) for i in range(d)])
+            elif name == "gradient":
+                outs.extend([[_unit(d, i)] for i in range(d)])
+            else:
+                axes = {"x": 0, "y": 1, "z": 2}
+                sig = [0] * d
+                for ch in name:
+                    sig[axes[ch]] += 1
+                outs.append([tuple(sig)])
+        super().__init__(parts, verletList, ord, rCut, opt, outputs=outs, kind="vector", **kw)
+
+
+# GPU aliases of the reference (DCPSE_op.hpp:3510-3530) name the same classes
+Derivative_x_gpu, Derivative_y_gpu, Derivative_z_gpu = Derivative_x, Derivative_y, Derivative_z
+Derivative_xx_gpu, Derivative_yy_gpu, Derivative_zz_gpu = Derivative_xx, Derivative_yy, Derivative_zz
+Derivative_xy_gpu, Derivative_yz_gpu, Derivative_xz_gpu = Derivative_xy, Derivative_yz, Derivative_xz
+Laplacian_gpu, Gradient_gpu, Derivative_G_gpu = Laplacian, Gradient, Derivative_G

@@ -1,0 +1,234 @@
+"""Python host side of the DC-PSE C-ABI: a plan object over torch tensors.
+
+PyTorch is only plumbing here (device memory, streams).  Every computation is
+a call into ``libdcpse_gb300.so``; there is no CPU or PyTorch fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _capi as C
+
+
+class _DevView:
+    """Zero-copy view of a plan-owned device array for torch.as_tensor."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {
+            "shape": tuple(int(s) for s in shape),
+            "typestr": typestr,
+            "data": (int(ptr), True),
+            "version": 3,
+            "strides": None,
+        }
+
+
+def _view(ptr, shape, dtype):
+    ts = {torch.float64: "<f8", torch.float32: "<f4", torch.int64: "<i8", torch.int32: "<i4"}[dtype]
+    if int(np.prod(shape)) == 0 or not ptr:
+        return torch.empty(shape, dtype=dtype, device="cuda")
+    return torch.as_tensor(_DevView(ptr, shape, ts), device="cuda")
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+class DcpsePlan:
+    """One particle set, its neighbour list and a set of DC-PSE outputs.
+
+    ``outputs`` is a list of outputs, each a list of signatures (one per
+    reference Dcpse term); e.g. a 3D Gradient + Laplacian is
+    ``[[(1,0,0)], [(0,1,0)], [(0,0,1)], [(2,0,0),(0,2,0),(0,0,2)]]``.
+    """
+
+    def __init__(self, dim, outputs, order=2, h_over_eps=0.9, box=None, stream=None):
+        self.dim = int(dim)
+        self.outputs = [[tuple(int(x) for x in s) for s in o] for o in outputs]
+        self.order = int(order)
+        self.h_over_eps = float(h_over_eps)
+        terms = [len(o) for o in self.outputs]
+        sigs = [x for o in self.outputs for s in o for x in s]
+        for o in self.outputs:
+            for s in o:
+                if len(s) != self.dim:
+                    raise ValueError("signature %r does not have %d entries" % (s, self.dim))
+        tarr = (ctypes.c_int * len(terms))(*terms)
+        sarr = (ctypes.c_uint * len(sigs))(*sigs)
+        h = ctypes.c_void_p()
+        C.call("dcpse_plan_create", ctypes.byref(h), self.dim, len(terms), tarr, sarr, self.order,
+               self.h_over_eps)
+        self._h = h
+        self.stream = stream
+        C.call("dcpse_plan_set_stream", self._h, _stream_ptr(stream))
+        self.box = None
+        if box is not None:
+            self.set_box(*box)
+        self.n = None
+
+    # -- lifetime -------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            C.load().dcpse_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- set-up ---------------------------------------------------------
+    def set_box(self, lo, hi, periodic=None):
+        lo = (ctypes.c_double * self.dim)(*[float(x) for x in lo])
+        hi = (ctypes.c_double * self.dim)(*[float(x) for x in hi])
+        per = (ctypes.c_int * self.dim)(*([int(bool(p)) for p in periodic] if periodic is not None else
+                                          [0] * self.dim))
+        C.call("dcpse_plan_set_box", self._h, lo, hi, per)
+        self.box = (tuple(lo), tuple(hi), tuple(per))
+
+    @property
+    def n_terms(self):
+        return sum(len(o) for o in self.outputs)
+
+    @property
+    def n_outputs(self):
+        return len(self.outputs)
+
+    def info(self):
+        n, nnz = ctypes.c_int64(), ctypes.c_int64()
+        nt, no, mk = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        C.call("dcpse_plan_info", self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(nt), ctypes.byref(no),
+               ctypes.byref(mk))
+        return {"n": n.value, "nnz": nnz.value, "terms": nt.value, "outputs": no.value, "max_neighbors": mk.value}
+
+    def term_basis(self, term):
+        cap = 64
+        ex = (ctypes.c_uint * (cap * self.dim))()
+        n = ctypes.c_int()
+        C.call("dcpse_term_basis", self._h, int(term), ex, cap, ctypes.byref(n))
+        return np.array(ex[: n.value * self.dim], dtype=np.uint32).reshape(n.value, self.dim)
+
+    def build_neighbors(self, pos, rcut, rcut_pp=None):
+        pos = self._check_pos(pos)
+        if rcut_pp is not None:
+            rcut_pp = rcut_pp.contiguous().to(torch.float64)
+        C.call("dcpse_build_neighbors", self._h, _ptr(pos), pos.shape[0], float(rcut), _ptr(rcut_pp))
+        self.n = pos.shape[0]
+
+    def set_neighbors(self, rowptr, cols):
+        rowptr = rowptr.contiguous().to(device="cuda", dtype=torch.int64)
+        cols = cols.contiguous().to(device="cuda", dtype=torch.int32)
+        n = rowptr.numel() - 1
+        C.call("dcpse_set_neighbors", self._h, n, cols.numel(), _ptr(rowptr), _ptr(cols))
+        self.n = n
+
+    def neighbors(self):
+        """(rowptr, cols) as torch views of the plan's arrays."""
+        rp, cl = ctypes.c_void_p(), ctypes.c_void_p()
+        C.call("dcpse_neighbors_ptr", self._h, ctypes.byref(rp), ctypes.byref(cl))
+        info = self.info()
+        return (_view(rp.value, (info["n"] + 1,), torch.int64), _view(cl.value, (info["nnz"],), torch.int32))
+
+    # -- assembly -------------------------------------------------------
+    def assemble(self, pos, flags=C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32, eps_fixed=None,
+                 allow_failed_particles=True):
+        pos = self._check_pos(pos)
+        if eps_fixed is not None:
+            eps_fixed = eps_fixed.contiguous().to(torch.float64)
+        allow = (C.ERR_PARTICLES,) if allow_failed_particles else ()
+        return C.call("dcpse_assemble", self._h, _ptr(pos), _ptr(eps_fixed), int(flags), allow=allow)
+
+    def particle_status(self):
+        nb, fb, fc = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        C.call("dcpse_particle_status", self._h, ctypes.byref(nb), ctypes.byref(fb), ctypes.byref(fc))
+        return nb.value, fb.value, fc.value
+
+    def eps(self):
+        e, s = ctypes.c_void_p(), ctypes.c_void_p()
+        C.call("dcpse_eps_ptr", self._h, ctypes.byref(e), ctypes.byref(s))
+        n = self.info()["n"]
+        return _view(e.value, (n,), torch.float64), _view(s.value, (n,), torch.int32)
+
+    def term_kernels(self, term):
+        k, e = ctypes.c_void_p(), ctypes.c_void_p()
+        C.call("dcpse_term_kernels_ptr", self._h, int(term), ctypes.byref(k), ctypes.byref(e))
+        info = self.info()
+        K = _view(k.value, (info["nnz"],), torch.float64) if k.value else None
+        return K, _view(e.value, (info["n"],), torch.float64)
+
+    def output_weights(self, output):
+        w64, w32 = ctypes.c_void_p(), ctypes.c_void_p()
+        C.call("dcpse_output_weights_ptr", self._h, int(output), ctypes.byref(w64), ctypes.byref(w32))
+        nnz = self.info()["nnz"]
+        return (_view(w64.value, (nnz,), torch.float64) if w64.value else None,
+                _view(w32.value, (nnz,), torch.float32) if w32.value else None)
+
+    # -- apply ----------------------------------------------------------
+    def apply_term_f64(self, term, f, out=None):
+        f = self._check_field(f)
+        out = torch.empty_like(f) if out is None else out
+        C.call("dcpse_apply_term_f64", self._h, int(term), _ptr(f), _ptr(out))
+        return out
+
+    def apply_output_f64(self, output, f, out=None):
+        f = self._check_field(f)
+        out = torch.empty_like(f) if out is None else out
+        C.call("dcpse_apply_output_f64", self._h, int(output), _ptr(f), _ptr(out))
+        return out
+
+    def apply(self, f, precision=C.F32, out=None):
+        """All outputs in one pass: returns a [n_outputs, n] float64 tensor."""
+        f = self._check_field(f)
+        if out is None:
+            out = torch.empty((self.n_outputs, f.shape[0]), dtype=torch.float64, device=f.device)
+        C.call("dcpse_apply_batched", self._h, _ptr(f), _ptr(out), int(precision))
+        return out
+
+    def apply_host(self, f_host, out_host=None, precision=C.F32):
+        """Host numpy arrays in and out (the copies are part of the call)."""
+        f_host = np.ascontiguousarray(f_host, dtype=np.float64)
+        if out_host is None:
+            out_host = np.empty((self.n_outputs, f_host.shape[0]), dtype=np.float64)
+        C.call("dcpse_apply_batched_host", self._h, f_host.ctypes.data_as(ctypes.c_void_p),
+               out_host.ctypes.data_as(ctypes.c_void_p), int(precision))
+        return out_host
+
+    # -- timing ---------------------------------------------------------
+    def set_timing(self, enable=True):
+        C.call("dcpse_plan_set_timing", self._h, int(bool(enable)))
+
+    def reset_timing(self):
+        C.call("dcpse_plan_reset_timing", self._h)
+
+    def timing(self, kernel):
+        """(total device ms, launches) of a kernel id since the last reset."""
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        C.call("dcpse_plan_timing", self._h, int(kernel), ctypes.byref(ms), ctypes.byref(n))
+        return ms.value, n.value
+
+    # -- helpers --------------------------------------------------------
+    def _check_pos(self, pos):
+        if pos.dtype != torch.float64 or pos.dim() != 2 or pos.shape[1] != self.dim:
+            raise ValueError("positions must be a float64 [n, %d] CUDA tensor" % self.dim)
+        return pos.contiguous()
+
+    def _check_field(self, f):
+        if f.dtype != torch.float64 or f.dim() != 1:
+            raise ValueError("fields are float64 [n] CUDA tensors")
+        return f.contiguous()

@@ -1,0 +1,234 @@
+"""CPU FP64 oracle for the DC-PSE hot path (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline /
+reference legs may import this package; the product never does.  The C++
+restatement lives in ``dcpse_oracle.cpp`` (see its header for the reference
+file:line each function follows) and is compiled by :func:`build` with g++
+into ``oracle/_build/liborc.so``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "dcpse_oracle.cpp")
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD_DIR, "liborc.so")
+
+# -ffp-contract=off: every fused multiply-add is an explicit std::fma in the
+# source, so the rounding of each step is fixed (the CUDA side follows the
+# same operation sequence).
+CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread"]
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
+        return LIB
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["g++", *CXXFLAGS, SRC, "-o", tmp])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+_D = ctypes.POINTER(ctypes.c_double)
+_U = ctypes.POINTER(ctypes.c_uint)
+_I32 = ctypes.POINTER(ctypes.c_int32)
+_I64 = ctypes.POINTER(ctypes.c_int64)
+_INT = ctypes.POINTER(ctypes.c_int)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.orc_exp.restype = ctypes.c_double
+        L.orc_exp.argtypes = [ctypes.c_double]
+        L.orc_exp_array.argtypes = [_D, _D, ctypes.c_int64]
+        L.orc_ipow.restype = ctypes.c_double
+        L.orc_ipow.argtypes = [ctypes.c_double, ctypes.c_uint]
+        L.orc_basis.restype = ctypes.c_int
+        L.orc_basis.argtypes = [ctypes.c_int, _U, ctypes.c_uint, _U, _U, ctypes.c_int]
+        L.orc_rhs.restype = ctypes.c_int
+        L.orc_rhs.argtypes = [ctypes.c_int, _U, ctypes.c_uint, _D, ctypes.c_int]
+        L.orc_monomial_derivative.argtypes = [ctypes.c_int, _U, ctypes.c_uint, _U, _U, _U]
+        L.orc_monomial_eval.restype = ctypes.c_double
+        L.orc_monomial_eval.argtypes = [ctypes.c_int, _U, ctypes.c_uint, _D]
+        nb = [ctypes.c_int, _D, ctypes.c_int64, _D, ctypes.c_int64, ctypes.c_int, ctypes.c_double, _D,
+              _D, _D, _INT, _I64, _I32, ctypes.c_int64]
+        L.orc_neighbors.restype = ctypes.c_int64
+        L.orc_neighbors.argtypes = nb
+        L.orc_neighbors_brute.restype = ctypes.c_int64
+        L.orc_neighbors_brute.argtypes = nb
+        L.orc_assemble.restype = ctypes.c_int64
+        L.orc_assemble.argtypes = [ctypes.c_int, _D, ctypes.c_int64, _D, _I64, _I32, _D, _D, _INT, _U,
+                                   ctypes.c_uint, ctypes.c_double, _D, _D, _D, _D, _I32, ctypes.c_int]
+        L.orc_apply.argtypes = [ctypes.c_int64, _D, _D, _I64, _I32, _D, _D, ctypes.c_uint, _D, ctypes.c_int]
+        L.orc_apply_sum.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _D, _I64, _I32,
+                                    ctypes.POINTER(_D), ctypes.POINTER(_D), _U, _D, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    if a is None:
+        return None
+    return a.ctypes.data_as(t)
+
+
+def _c(a, dtype):
+    return None if a is None else np.ascontiguousarray(a, dtype=dtype)
+
+
+def exp(x):
+    x = _c(np.atleast_1d(x), np.float64)
+    y = np.empty_like(x)
+    lib().orc_exp_array(_p(x, _D), _p(y, _D), x.size)
+    return y
+
+
+def basis(dim, sig, order):
+    sig = _c(sig, np.uint32)
+    e = np.zeros(1024 * dim, np.uint32)
+    s = np.zeros(1024, np.uint32)
+    n = lib().orc_basis(dim, _p(sig, _U), order, _p(e, _U), _p(s, _U), 1024)
+    return e[: n * dim].reshape(n, dim), s[:n]
+
+
+def rhs(dim, sig, order):
+    sig = _c(sig, np.uint32)
+    b = np.zeros(1024)
+    n = lib().orc_rhs(dim, _p(sig, _U), order, _p(b, _D), 1024)
+    return b[:n]
+
+
+def monomial_derivative(exps, scalar, dord):
+    exps = _c(exps, np.uint32)
+    dord = _c(dord, np.uint32)
+    oe = np.zeros_like(exps)
+    os_ = np.zeros(1, np.uint32)
+    lib().orc_monomial_derivative(len(exps), _p(exps, _U), scalar, _p(dord, _U), _p(oe, _U), _p(os_, _U))
+    return oe, int(os_[0])
+
+
+def monomial_eval(exps, scalar, x):
+    exps = _c(exps, np.uint32)
+    x = _c(x, np.float64)
+    return lib().orc_monomial_eval(len(exps), _p(exps, _U), scalar, _p(x, _D))
+
+
+def _box(box, dim):
+    if box is None:
+        return None, None, None
+    lo = _c(box[0], np.float64)
+    hi = _c(box[1], np.float64)
+    per = _c(box[2] if len(box) > 2 else [0] * dim, np.int32)
+    return lo, hi, per
+
+
+def neighbors(pos, rcut, *, support=None, self_skip=True, rcut_pp=None, box=None, brute=False):
+    """CSR neighbour list (rowptr int64 [n+1], cols int32), ascending q."""
+    pos = _c(pos, np.float64)
+    n, dim = pos.shape
+    sup = pos if support is None else _c(support, np.float64)
+    rpp = _c(rcut_pp, np.float64)
+    lo, hi, per = _box(box, dim)
+    fn = lib().orc_neighbors_brute if brute else lib().orc_neighbors
+    rowptr = np.zeros(n + 1, np.int64)
+    args = (dim, _p(pos, _D), n, _p(sup, _D), sup.shape[0], int(self_skip), float(rcut), _p(rpp, _D),
+            _p(lo, _D), _p(hi, _D), _p(per, _INT), _p(rowptr, _I64))
+    nnz = fn(*args, None, 0)
+    cols = np.zeros(max(nnz, 1), np.int32)
+    nnz2 = fn(*args, _p(cols, _I32), cols.size)
+    assert nnz2 == nnz
+    return rowptr, cols[:nnz]
+
+
+def assemble(pos, rowptr, cols, sig, order, *, support=None, box=None, h_over_eps=0.9, eps_fixed=None,
+             nthreads=1):
+    """One reference Dcpse object: returns (eps, eps_inv_pow, kernels, status)."""
+    pos = _c(pos, np.float64)
+    n, dim = pos.shape
+    sup = pos if support is None else _c(support, np.float64)
+    rowptr = _c(rowptr, np.int64)
+    cols = _c(cols, np.int32)
+    sig = _c(sig, np.uint32)
+    lo, hi, per = _box(box, dim)
+    ef = _c(eps_fixed, np.float64)
+    eps = np.zeros(n)
+    eip = np.zeros(n)
+    K = np.zeros(max(int(rowptr[-1]), 1))
+    st = np.zeros(n, np.int32)
+    lib().orc_assemble(dim, _p(pos, _D), n, _p(sup, _D), _p(rowptr, _I64), _p(cols, _I32), _p(lo, _D),
+                       _p(hi, _D), _p(per, _INT), _p(sig, _U), order, float(h_over_eps), _p(ef, _D),
+                       _p(eps, _D), _p(eip, _D), _p(K, _D), _p(st, _I32), int(nthreads))
+    return eps, eip, K[: int(rowptr[-1])], st
+
+
+def apply(f, rowptr, cols, K, eip, diff_order, *, f_dom=None, nthreads=1):
+    f = _c(f, np.float64)
+    fd = f if f_dom is None else _c(f_dom, np.float64)
+    rowptr = _c(rowptr, np.int64)
+    cols = _c(cols, np.int32)
+    K = _c(K, np.float64)
+    eip = _c(eip, np.float64)
+    n = rowptr.size - 1
+    out = np.zeros(n)
+    lib().orc_apply(n, _p(f, _D), _p(fd, _D), _p(rowptr, _I64), _p(cols, _I32), _p(K, _D), _p(eip, _D),
+                    int(diff_order), _p(out, _D), int(nthreads))
+    return out
+
+
+def apply_sum(f, rowptr, cols, Ks, eips, diff_orders, *, nthreads=1):
+    f = _c(f, np.float64)
+    rowptr = _c(rowptr, np.int64)
+    cols = _c(cols, np.int32)
+    Ks = [_c(k, np.float64) for k in Ks]
+    eips = [_c(e, np.float64) for e in eips]
+    kp = (_D * len(Ks))(*[_p(k, _D) for k in Ks])
+    ep = (_D * len(eips))(*[_p(e, _D) for e in eips])
+    do = _c(diff_orders, np.uint32)
+    n = rowptr.size - 1
+    out = np.zeros(n)
+    lib().orc_apply_sum(n, len(Ks), _p(f, _D), _p(f, _D), _p(rowptr, _I64), _p(cols, _I32), kp, ep,
+                        _p(do, _U), _p(out, _D), int(nthreads))
+    return out
+
+
+# ---------------------------------------------------------------- helpers --
+
+SIGS = {
+    "x": (1, 0, 0), "y": (0, 1, 0), "z": (0, 0, 1),
+    "xx": (2, 0, 0), "yy": (0, 2, 0), "zz": (0, 0, 2),
+    "xy": (1, 1, 0), "yz": (0, 1, 1), "xz": (1, 0, 1),
+}
+
+
+def sig(name, dim):
+    return SIGS[name][:dim]
+
+
+def operator(pos, rowptr, cols, name, order=2, **kw):
+    """Reference operator object as a list of (sig, eps, eip, K, status) per
+    Dcpse component: 'laplacian' and 'gradient' expand to dim components
+    (DCPSE_op.hpp:1367-1389, 1099-1120)."""
+    dim = np.asarray(pos).shape[1]
+    if name == "laplacian":
+        comps = [tuple(2 if d == i else 0 for d in range(dim)) for i in range(dim)]
+    elif name == "gradient":
+        comps = [tuple(1 if d == i else 0 for d in range(dim)) for i in range(dim)]
+    else:
+        comps = [sig(name, dim)]
+    out = []
+    for s in comps:
+        eps, eip, K, st = assemble(pos, rowptr, cols, s, order, **kw)
+        out.append((s, eps, eip, K, st))
+    return out

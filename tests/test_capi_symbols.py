@@ -1,0 +1,30 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every symbol the
+header declares (no compute calls: runs without a GPU)."""
+import ctypes
+
+from openfpm_numerics_gb300 import _capi as C
+
+
+def test_library_exports_declared_symbols():
+    lib = C.load()
+    declared = C.declared_symbols()
+    assert len(declared) >= 20
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+    # every declared symbol has a ctypes signature in the binding
+    assert set(declared) <= set(C.SIGNATURES), set(declared) - set(C.SIGNATURES)
+
+
+def test_host_only_calls():
+    lib = C.load()
+    assert lib.dcpse_version() >= 1
+    # argument validation runs on the host and reports through the status
+    h = ctypes.c_void_p()
+    rc = lib.dcpse_plan_create(ctypes.byref(h), 4, 1, (ctypes.c_int * 1)(1), (ctypes.c_uint * 4)(1, 0, 0, 0), 2, 0.9)
+    assert rc == C.ERR_ARG and b"dim" in lib.dcpse_last_error()
+    rc = lib.dcpse_plan_create(None, 2, 1, (ctypes.c_int * 1)(1), (ctypes.c_uint * 2)(1, 0), 2, 0.9)
+    assert rc == C.ERR_ARG
+    rc = lib.dcpse_plan_destroy(None)
+    assert rc == C.OK
+    rc = lib.dcpse_apply_batched(None, None, None, 0)
+    assert rc == C.ERR_ARG

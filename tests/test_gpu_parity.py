@@ -1,0 +1,233 @@
+"""Parity of the CUDA path (through the C-ABI) with the CPU oracle.
+
+Bars (FP64): neighbour lists, eps, eps^-|alpha|, per-term kernels, the
+per-term apply and the reference-order output apply are bit-exact; the
+batched FP64 apply and the fast (summed right-hand side) assembly are within
+1e-12 normwise relative; the batched FP32 apply within 1e-6 normwise relative
+(max |err| / max |ref|).
+"""
+import numpy as np
+import pytest
+import torch
+
+from openfpm_numerics_gb300 import _capi as C
+from openfpm_numerics_gb300 import workloads as W
+from openfpm_numerics_gb300.plan import DcpsePlan
+
+pytestmark = pytest.mark.gpu
+
+GRAD_LAP_2D = [[(1, 0)], [(0, 1)], [(2, 0), (0, 2)], [(1, 1)]]
+GRAD_LAP_3D = W.grad_lap_outputs(3)
+
+
+def _case(name):
+    if name == "2d":
+        pos, h = W.lattice(24, 2, jitter=0.15, seed=11)
+        return dict(pos=pos, rcut=3.1 * h, outputs=GRAD_LAP_2D, order=2)
+    if name == "3d":
+        pos, h = W.lattice(12, 3, jitter=0.15, seed=12)
+        return dict(pos=pos, rcut=2.8 * h, outputs=GRAD_LAP_3D, order=2)
+    if name == "3d_periodic":
+        h = 1.0 / 10
+        pos, _ = W.lattice(10, 3, h=h, jitter=0.1, seed=13)
+        pos = np.mod(pos, 1.0)
+        return dict(pos=pos, rcut=2.8 * h, outputs=[[(2, 0, 0), (0, 2, 0), (0, 0, 2)]], order=2,
+                    box=((0.0,) * 3, (1.0,) * 3, (1, 1, 1)))
+    if name == "2d_lattice":
+        pos, h = W.lattice(16, 2)
+        return dict(pos=pos, rcut=3.1 * h, outputs=[[(1, 0)], [(2, 0), (0, 2)]], order=2)
+    if name == "2d_order3":
+        pos, h = W.lattice(20, 2, jitter=0.1, seed=14)
+        return dict(pos=pos, rcut=3.6 * h, outputs=[[(1, 0)], [(2, 0), (0, 2)]], order=3)
+    if name == "2d_adaptive":
+        pos, h = W.lattice(20, 2, jitter=0.1, seed=15)
+        rpp = (2.9 + 0.6 * np.random.default_rng(15).random(pos.shape[0])) * h
+        return dict(pos=pos, rcut=0.0, rcut_pp=rpp, outputs=[[(1, 0)], [(0, 1)], [(2, 0), (0, 2)]], order=2)
+    if name == "2d_hoe05":
+        pos, h = W.lattice(18, 2, jitter=0.1, seed=16)
+        return dict(pos=pos, rcut=3.1 * h, outputs=[[(1, 0)], [(2, 0), (0, 2)]], order=2, hoe=0.5)
+    if name == "2d_sparse":
+        pos, h = W.lattice(14, 2, jitter=0.2, seed=17)
+        return dict(pos=pos, rcut=2.05 * h, outputs=[[(1, 0)], [(2, 0), (0, 2)]], order=2)
+    raise KeyError(name)
+
+
+CASES = ["2d", "3d", "3d_periodic", "2d_lattice", "2d_order3", "2d_adaptive", "2d_hoe05", "2d_sparse"]
+
+
+def _build(c, flags=C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32):
+    dim = c["pos"].shape[1]
+    plan = DcpsePlan(dim, c["outputs"], order=c["order"], h_over_eps=c.get("hoe", 0.9), box=c.get("box"))
+    pos = torch.tensor(c["pos"], device="cuda")
+    rpp = torch.tensor(c["rcut_pp"], device="cuda") if c.get("rcut_pp") is not None else None
+    plan.build_neighbors(pos, c["rcut"], rpp)
+    rc = plan.assemble(pos, flags)
+    return plan, pos, rc
+
+
+def _oracle_terms(orc, c, rp, cols):
+    res = []
+    for o, out in enumerate(c["outputs"]):
+        for s in out:
+            eps, eip, K, st = orc.assemble(c["pos"], rp, cols, s, c["order"], box=c.get("box"),
+                                           h_over_eps=c.get("hoe", 0.9))
+            res.append(dict(sig=s, out=o, eps=eps, eip=eip, K=K, st=st))
+    return res
+
+
+def _group_order(terms):
+    keys = []
+    for t in terms:
+        k = sum(t["sig"])
+        if k not in keys:
+            keys.append(k)
+    return keys
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_neighbors_bitexact(cuda, orc, name):
+    c = _case(name)
+    plan, pos, _ = _build(c)
+    rp_o, cols_o = orc.neighbors(c["pos"], c["rcut"], rcut_pp=c.get("rcut_pp"), box=c.get("box"))
+    rp, cols = plan.neighbors()
+    assert np.array_equal(rp.cpu().numpy(), rp_o)
+    assert np.array_equal(cols.cpu().numpy(), cols_o)
+    assert plan.info()["max_neighbors"] == int(np.diff(rp_o).max())
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_assembly_bitexact(cuda, orc, name):
+    c = _case(name)
+    plan, pos, rc = _build(c)
+    rp, cols = (x.cpu().numpy() for x in plan.neighbors())
+    terms = _oracle_terms(orc, c, rp, cols)
+    eps, st = (x.cpu().numpy() for x in plan.eps())
+    # eps is the same for every term
+    assert np.array_equal(eps.view(np.int64), terms[0]["eps"].view(np.int64))
+    for t, ref in enumerate(terms):
+        K, eip = plan.term_kernels(t)
+        K = K.cpu().numpy()
+        eip = eip.cpu().numpy()
+        assert np.array_equal(eip, ref["eip"]), "eps^-|alpha| of term %d" % t
+        ok = ref["st"] == 0
+        assert np.array_equal(K, ref["K"]), "kernels of term %d differ: max %g" % (t, np.abs(K - ref["K"]).max())
+    # particle status = first failing basis in group order
+    keys = _group_order(terms)
+    expect = np.zeros_like(st)
+    for k in keys:
+        s_g = next(t["st"] for t in terms if sum(t["sig"]) == k)
+        expect = np.where(expect == 0, s_g, expect)
+    assert np.array_equal(st, expect)
+    assert (rc == C.ERR_PARTICLES) == bool(np.any(expect != 0))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_apply_parity(cuda, orc, name):
+    c = _case(name)
+    plan, pos, _ = _build(c)
+    rp, cols = (x.cpu().numpy() for x in plan.neighbors())
+    terms = _oracle_terms(orc, c, rp, cols)
+    f = np.random.default_rng(5).standard_normal(c["pos"].shape[0])
+    ft = torch.tensor(f, device="cuda")
+    # per term, reference order: bit-exact
+    for t, ref in enumerate(terms):
+        got = plan.apply_term_f64(t, ft).cpu().numpy()
+        exp = orc.apply(f, rp, cols, ref["K"], ref["eip"], sum(ref["sig"]))
+        assert np.array_equal(got, exp), "term %d" % t
+    # outputs composed as the reference does (VECT_DCPSE_V_SUM): bit-exact
+    refs = []
+    for o in range(len(c["outputs"])):
+        ts = [t for t in terms if t["out"] == o]
+        exp = orc.apply_sum(f, rp, cols, [t["K"] for t in ts], [t["eip"] for t in ts], [sum(t["sig"]) for t in ts])
+        got = plan.apply_output_f64(o, ft).cpu().numpy()
+        assert np.array_equal(got, exp), "output %d" % o
+        refs.append(exp)
+    refs = np.stack(refs)
+    # batched FP64 (summed, eps-folded weights, difference form)
+    b64 = plan.apply(ft, C.F64).cpu().numpy()
+    for o in range(len(refs)):
+        err = np.abs(b64[o] - refs[o]).max() / np.abs(refs[o]).max()
+        assert err <= 1e-12, (o, err)
+    # batched FP32
+    b32 = plan.apply(ft, C.F32).cpu().numpy()
+    for o in range(len(refs)):
+        err = np.abs(b32[o] - refs[o]).max() / np.abs(refs[o]).max()
+        assert err <= 1e-6, (o, err)
+    # host-buffer entry point equals the device one
+    h32 = plan.apply_host(f, precision=C.F32)
+    assert np.array_equal(h32, b32)
+
+
+@pytest.mark.parametrize("name", ["2d", "3d", "3d_periodic", "2d_order3"])
+def test_fast_assembly_close(cuda, orc, name):
+    c = _case(name)
+    plan, pos, _ = _build(c, C.ASSEMBLE_FAST | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+    rp, cols = (x.cpu().numpy() for x in plan.neighbors())
+    terms = _oracle_terms(orc, c, rp, cols)
+    _, st = plan.eps()
+    ok = st.cpu().numpy() == 0
+    for o in range(len(c["outputs"])):
+        w_ref = np.zeros(rp[-1])
+        for t in terms:
+            if t["out"] == o:
+                w_ref = w_ref + t["K"] * np.repeat(t["eip"], np.diff(rp))
+        w64, w32 = plan.output_weights(o)
+        w64 = w64.cpu().numpy()
+        for p in np.where(ok)[0]:
+            a, b = rp[p], rp[p + 1]
+            scale = np.abs(w_ref[a:b]).max()
+            assert np.abs(w64[a:b] - w_ref[a:b]).max() <= 1e-12 * scale, (o, p)
+        assert np.array_equal(w32.cpu().numpy(), w64.astype(np.float32))
+
+
+def test_analytic_config1_laplacian(cuda):
+    cfg = W.config1()
+    c = dict(pos=cfg["pos"], rcut=cfg["rcut"], outputs=[[(2, 0), (0, 2)]], order=2)
+    plan, pos, _ = _build(c)
+    f, lf = W.field1(cfg["pos"])
+    ft = torch.tensor(f, device="cuda")
+    inner = W.interior_mask(cfg["pos"], cfg["rcut"])
+    for prec in (C.F64, C.F32):
+        lap = plan.apply(ft, prec)[0].cpu().numpy()
+        rel = np.abs(lap - lf)[inner].max() / np.abs(lf).max()
+        assert rel < 2e-2
+
+
+def test_edge_cases(cuda):
+    # empty particle set
+    plan = DcpsePlan(2, [[(1, 0)]])
+    pos = torch.zeros((0, 2), dtype=torch.float64, device="cuda")
+    plan.build_neighbors(pos, 0.1)
+    assert plan.info()["nnz"] == 0
+    assert plan.assemble(pos) == C.OK
+    out = plan.apply(torch.zeros(0, dtype=torch.float64, device="cuda"))
+    assert out.shape == (1, 0)
+    # isolated particle and a NaN position: flagged, weights zero, others fine
+    p, h = W.lattice(10, 2, jitter=0.1, seed=3)
+    p = np.concatenate([p, [[5.0, 5.0]], [[np.nan, 0.5]]])
+    plan = DcpsePlan(2, [[(1, 0)]], box=((0, 0), (6, 6), (0, 0)))
+    pt = torch.tensor(p, device="cuda")
+    plan.build_neighbors(pt, 3.1 * h)
+    rc = plan.assemble(pt)
+    assert rc == C.ERR_PARTICLES
+    nb, first, code = plan.particle_status()
+    eps, st = plan.eps()
+    st = st.cpu().numpy()
+    assert st[-1] != 0 and st[-2] == C.PART_TOO_FEW and first <= len(p) - 2
+    w64, _ = plan.output_weights(0)
+    assert torch.isfinite(w64).all()
+    # state errors
+    plan2 = DcpsePlan(2, [[(1, 0)]])
+    with pytest.raises(C.DcpseError) as ei:
+        plan2.apply(torch.zeros(4, dtype=torch.float64, device="cuda"))
+    assert ei.value.code == C.ERR_STATE
+
+
+def test_term_basis_matches_oracle(cuda, orc):
+    plan = DcpsePlan(3, GRAD_LAP_3D, order=2)
+    t = 0
+    for out in GRAD_LAP_3D:
+        for s in out:
+            e, _ = orc.basis(3, s, 2)
+            assert np.array_equal(plan.term_basis(t), e)
+            t += 1

@@ -1,0 +1,214 @@
+"""Pins the CPU oracle against the reference's own unit tests (known answers
+and analytic error bars).  CPU only."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from openfpm_numerics_gb300 import workloads as W
+
+KA = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_known_answers.json")))
+
+
+def test_monomial_known_answers(orc):
+    for c in KA["monomial_evaluate"]:
+        assert orc.monomial_eval(c["exps"], 1, c["x"]) == c["value"]
+    for c in KA["monomial_derivative"]:
+        oe, os_ = orc.monomial_derivative(c["exps"], 1, c["d"])
+        assert list(oe) == c["out_exps"] and os_ == c["out_scalar"]
+    for c in KA["monomial_order"]:
+        oe, os_ = orc.monomial_derivative(c["exps"], 1, [0, 0, 0])
+        assert sum(oe) == c["order"] and os_ == 1
+
+
+def test_basis_known_answers(orc):
+    for c in KA["basis_2d"]:
+        e, s = orc.basis(2, c["sig"], c["order"])
+        got = {tuple(int(v) for v in r) for r in e}
+        assert all(tuple(x) in got for x in c["contains"])
+        if c["size"] is not None:
+            assert len(got) == c["size"]
+        assert np.all(s == 1)
+    for c in KA["basis_sizes"]:
+        e, _ = orc.basis(c["dim"], c["sig"], c["order"])
+        assert e.shape[0] == c["size"]
+
+
+def test_basis_filter_definition(orc):
+    # alphaMin <= |m| < |alpha| + r, alphaMin = 1 for even |alpha| > 0
+    for dim in (2, 3):
+        for sig in [(1,) + (0,) * (dim - 1), (2,) + (0,) * (dim - 1), (1, 1) + (0,) * (dim - 2),
+                    (0,) * dim, (3,) + (0,) * (dim - 1)]:
+            for r in (1, 2, 3):
+                e, _ = orc.basis(dim, sig, r)
+                ms = sum(sig)
+                lim = ms + r
+                amin = 1 if (ms % 2 == 0 and ms > 0) else 0
+                import itertools
+                expect = [m[::-1] for m in itertools.product(range(lim), repeat=dim) if amin <= sum(m) < lim]
+                assert [tuple(int(v) for v in row) for row in e] == [tuple(m) for m in expect]
+
+
+def test_row_builder_patterns(orc):
+    e, _ = orc.basis(2, (1, 0), 2)
+    for c in KA["row_builder"]:
+        u = np.array(c["x"], float) / c["eps"]
+        row = np.array([orc.monomial_eval(m, 1, u) for m in e])
+        if c["pattern"] == "all_ones":
+            assert np.all(row == 1)
+        elif c["pattern"] == "one_where_no_y":
+            assert np.all(row == (e[:, 1] == 0))
+        else:
+            assert np.all(row == (e[:, 0] == 0))
+
+
+def test_rhs_known_answers(orc):
+    for c in KA["rhs"]:
+        b = orc.rhs(2, c["sig"], c["order"])
+        e, s = orc.basis(2, c["sig"], c["order"])
+        assert b.size == c["size"]
+        for i, m in enumerate(e):
+            de, ds = orc.monomial_derivative(m, int(s[i]), c["sig"])
+            expect = c["sign"] * orc.monomial_eval(de, ds, [0.0, 0.0])
+            assert b[i] == expect
+
+
+def test_exp_accuracy(orc):
+    rng = np.random.default_rng(0)
+    x = np.concatenate([-rng.random(200000) * 40.0, rng.uniform(-740, 700, 20000), [0.0, -0.0, 1e-300, -1e-20]])
+    y = orc.exp(x)
+    z = np.exp(x)
+    ok = z > 1e-300
+    ulp = np.abs(y[ok] - z[ok]) / np.spacing(z[ok])
+    assert ulp.max() <= 1.0
+    assert orc.exp(np.array([np.nan]))[0] != orc.exp(np.array([np.nan]))[0]
+    assert orc.exp(np.array([-800.0]))[0] == 0.0 and np.isinf(orc.exp(np.array([800.0]))[0])
+
+
+@pytest.mark.parametrize("dim,periodic,adaptive", [(2, False, False), (3, False, False), (3, True, False),
+                                                   (2, False, True), (1, False, False)])
+def test_neighbors_cell_vs_brute(orc, dim, periodic, adaptive):
+    n = {1: 40, 2: 14, 3: 8}[dim]
+    pos, h = W.lattice(n, dim, jitter=0.2, seed=7)
+    box = None
+    if periodic:
+        pos = np.mod(pos, 1.0)
+        box = ((0.0,) * dim, (1.0,) * dim, (1,) * dim)
+    rpp = None
+    if adaptive:
+        rpp = (2.0 + np.random.default_rng(1).random(pos.shape[0])) * h
+    rp1, c1 = orc.neighbors(pos, 2.6 * h, rcut_pp=rpp, box=box)
+    rp2, c2 = orc.neighbors(pos, 2.6 * h, rcut_pp=rpp, box=box, brute=True)
+    assert np.array_equal(rp1, rp2) and np.array_equal(c1, c2)
+    for p in range(pos.shape[0]):
+        row = c1[rp1[p]:rp1[p + 1]]
+        assert np.all(np.diff(row) > 0) and p not in row
+
+
+def test_moment_identity(orc):
+    pos, h = W.lattice(14, 2, jitter=0.15, seed=3)
+    rp, cols = orc.neighbors(pos, 3.1 * h)
+    for sig in [(1, 0), (0, 1), (2, 0), (1, 1)]:
+        eps, eip, K, st = orc.assemble(pos, rp, cols, sig, 2)
+        e, _ = orc.basis(2, sig, 2)
+        assert np.all((st == 0) | (np.diff(rp) < e.shape[0]))
+        b = orc.rhs(2, sig, 2)
+        for p in (1, 50, 97, 195):
+            assert st[p] == 0
+            X = pos[p] - pos[cols[rp[p]:rp[p + 1]]]
+            U = X / eps[p]
+            V = np.stack([np.prod(U ** m, axis=1) for m in e], 1)
+            mom = V.T @ K[rp[p]:rp[p + 1]]
+            assert np.allclose(mom, b, atol=1e-9)
+
+
+def _grid(nside, dim, h, jitter_sigma=None, seed=None):
+    ax = np.arange(nside) * h
+    g = np.meshgrid(*([ax] * dim), indexing="ij")
+    pos = np.stack([g[dim - 1 - d].reshape(-1) for d in range(dim)], axis=1)
+    if jitter_sigma is not None:
+        pos = pos + np.random.default_rng(seed).normal(0.0, jitter_sigma, pos.shape)
+    return np.ascontiguousarray(pos)
+
+
+def test_dcpse_2d_dx(orc):
+    # Dcpse_unit_tests.cpp:36-133
+    h = 1.0 / 39
+    pos = _grid(40, 2, h)
+    rp, cols = orc.neighbors(pos, 3.1 * h)
+    eps, eip, K, st = orc.assemble(pos, rp, cols, (1, 0), 2)
+    df = orc.apply(np.sin(pos[:, 0]), rp, cols, K, eip, 1)
+    assert np.max(np.abs(df - np.cos(pos[:, 0]))) < 2 * (2 * h) ** 2
+
+
+def test_dcpse_2d_perturbed_dx(orc):
+    # Dcpse_unit_tests.cpp:135-241 (normal jitter with standard deviation h^2/4;
+    # numpy's generator stands in for std::mt19937{6666666})
+    h = 1.0 / 39
+    s2 = h * h / 4
+    pos = _grid(40, 2, h, jitter_sigma=s2, seed=6666666)
+    rc = 2 * (h + np.sqrt(s2))
+    rp, cols = orc.neighbors(pos, rc)
+    eps, eip, K, st = orc.assemble(pos, rp, cols, (1, 0), 2)
+    df = orc.apply(np.sin(pos[:, 0]), rp, cols, K, eip, 1)
+    avg = 2 * h + 2 * np.sqrt(s2)
+    assert np.max(np.abs(df - np.cos(pos[:, 0]))) < 2 * avg * avg
+
+
+def test_dcpse_3d_dz(orc):
+    # Dcpse_unit_tests.cpp:243-337
+    h = 1.0 / 39
+    pos = _grid(40, 3, h)
+    rp, cols = orc.neighbors(pos, 3.1 * h)
+    eps, eip, K, st = orc.assemble(pos, rp, cols, (0, 0, 1), 2, nthreads=os.cpu_count())
+    df = orc.apply(np.sin(pos[:, 2]), rp, cols, K, eip, 1)
+    assert np.max(np.abs(df - np.cos(pos[:, 2]))) < (3 * h) ** 2
+
+
+def test_dcpse_op_2dx_plus_dy(orc):
+    # DCPSE_op_test_base_tests.cpp:30-101: v = 2 Dx(P) + Dy(P), worst < 0.03
+    h = 2 * np.pi / 79
+    pos = _grid(80, 2, h)
+    rp, cols = orc.neighbors(pos, 3.9 * h)
+    f = np.sin(pos[:, 0]) + np.sin(pos[:, 1])
+    ox = orc.operator(pos, rp, cols, "x")[0]
+    oy = orc.operator(pos, rp, cols, "y")[0]
+    dx = orc.apply(f, rp, cols, ox[3], ox[2], 1)
+    dy = orc.apply(f, rp, cols, oy[3], oy[2], 1)
+    v = 2 * dx + dy
+    assert np.max(np.abs(v - (2 * np.cos(pos[:, 0]) + np.cos(pos[:, 1])))) < 0.03
+
+
+def test_dcpse_op_laplacian(orc):
+    # DCPSE_op_test_base_tests.cpp:394-467: Laplacian on 163^2, worst < 0.3
+    h = 2 * np.pi / 162
+    pos = _grid(163, 2, h)
+    rp, cols = orc.neighbors(pos, 3.9 * h)
+    f = np.sin(pos[:, 0]) + np.sin(pos[:, 1])
+    comps = orc.operator(pos, rp, cols, "laplacian", nthreads=os.cpu_count())
+    lap = orc.apply_sum(f, rp, cols, [c[3] for c in comps], [c[2] for c in comps], [2, 2],
+                        nthreads=os.cpu_count())
+    assert np.max(np.abs(lap + f)) < 0.3
+
+
+def test_config1_laplacian_accuracy(orc):
+    c = W.config1()
+    pos = c["pos"]
+    rp, cols = orc.neighbors(pos, c["rcut"])
+    comps = orc.operator(pos, rp, cols, "laplacian")
+    f, lf = W.field1(pos)
+    lap = orc.apply_sum(f, rp, cols, [x[3] for x in comps], [x[2] for x in comps], [2, 2])
+    inner = W.interior_mask(pos, c["rcut"])
+    rel = np.max(np.abs(lap - lf)[inner]) / np.max(np.abs(lf))
+    assert rel < 2e-2  # second order at h = 1/63: about 0.9 %
+
+
+def test_too_few_neighbors_status(orc):
+    pos, h = W.lattice(8, 2, jitter=0.1, seed=9)
+    rp, cols = orc.neighbors(pos, 1.05 * h)   # ~4 neighbours < 6 basis functions
+    eps, eip, K, st = orc.assemble(pos, rp, cols, (1, 0), 2)
+    k = np.diff(rp)
+    assert np.all((st == 1) == (k < 6))
+    for p in np.where(st == 1)[0]:
+        assert np.all(K[rp[p]:rp[p + 1]] == 0)
