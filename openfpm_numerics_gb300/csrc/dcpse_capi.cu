@@ -89,6 +89,19 @@ __global__ void status_summary_kernel(const int32_t* st, int64_t n, unsigned lon
     }
 }
 
+// Checks a caller-supplied CSR list: rowptr[0] = 0, rowptr[n] = nnz, rows
+// non-decreasing, every column in [0, n).  bad[0] counts violations.
+__global__ void csr_check_kernel(const int64_t* rowptr, const int32_t* cols, int64_t n, int64_t nnz,
+                                 unsigned long long* bad) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (int64_t i = t0; i < n; i += stride)
+        if (rowptr[i + 1] < rowptr[i]) atomicAdd(bad, 1ull);
+    for (int64_t j = t0; j < nnz; j += stride)
+        if (cols[j] < 0 || (int64_t)cols[j] >= n) atomicAdd(bad, 1ull);
+    if (t0 == 0 && (rowptr[0] != 0 || rowptr[n] != nnz)) atomicAdd(bad, 1ull);
+}
+
 __global__ void row_max_kernel(const int64_t* rowptr, int64_t n, int* maxk) {
     int m = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -591,6 +604,26 @@ int dcpse_set_neighbors(dcpse_plan_t* P, int64_t n, int64_t nnz, const int64_t* 
     DCPSE_CK(dalloc(&P->cols, nnz));
     DCPSE_CK(cudaMemcpyAsync(P->rowptr, d_rowptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToDevice, s));
     if (nnz > 0) DCPSE_CK(cudaMemcpyAsync(P->cols, d_cols, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, s));
+    {
+        unsigned long long* bad = nullptr;
+        DCPSE_CK(dalloc(&bad, 1));
+        DCPSE_CK(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), s));
+        int64_t work = std::max<int64_t>(n, nnz);
+        csr_check_kernel<<<std::max(1, (int)std::min<int64_t>(num_sms() * 8, (work + 255) / 256)), 256, 0, s>>>(
+            P->rowptr, P->cols, n, nnz, bad);
+        unsigned long long hb = 0;
+        cudaError_t e = cudaMemcpyAsync(&hb, bad, sizeof hb, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        dfree(bad);
+        DCPSE_CK(e);
+        if (hb != 0) {
+            dfree(P->rowptr);
+            dfree(P->cols);
+            P->n = -1;
+            P->nnz = 0;
+            return fail(DCPSE_ERR_ARG, "invalid CSR neighbour list (row offsets or column indices)");
+        }
+    }
     int* mk = nullptr;
     DCPSE_CK(dalloc(&mk, 1));
     DCPSE_CK(cudaMemsetAsync(mk, 0, sizeof(int), s));

@@ -206,6 +206,7 @@ __global__ void __launch_bounds__(256) nbr_kernel(NbrArgs a, int32_t* __restrict
             cnt[d] = axis_cells(c, a.cells.nc[d], a.geom.per[d], lst[d]);
         }
         int64_t base = FILL ? rowptr[p] : 0;
+        const int64_t cap = FILL ? rowptr[p + 1] - base : 0;  // the count pass's result
         int k = 0;
         for (int a2 = 0; a2 < cnt[2]; ++a2)
             for (int a1 = 0; a1 < cnt[1]; ++a1)
@@ -225,7 +226,10 @@ __global__ void __launch_bounds__(256) nbr_kernel(NbrArgs a, int32_t* __restrict
                             if (a.self_skip && (int64_t)q == p) acc = false;
                         }
                         unsigned bal = __ballot_sync(0xffffffffu, acc);
-                        if (FILL && acc) tmp[base + k + __popc(bal & lt_mask)] = q;
+                        if (FILL && acc) {
+                            int64_t slot = k + __popc(bal & lt_mask);
+                            if (slot < cap) tmp[base + slot] = q;
+                        }
                         k += __popc(bal);
                     }
                 }
