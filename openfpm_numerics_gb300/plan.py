@@ -20,7 +20,7 @@ class _DevView:
         self.__cuda_array_interface__ = {
             "shape": tuple(int(s) for s in shape),
             "typestr": typestr,
-            "data": (int(ptr), True),
+            "data": (int(ptr), False),
             "version": 3,
             "strides": None,
         }
