@@ -141,6 +141,27 @@ int dcpse_apply_batched(dcpse_plan_t* plan, const double* d_f, double* d_out, in
  * the call (the reference's bulk apply reads and writes host particles). */
 int dcpse_apply_batched_host(dcpse_plan_t* plan, const double* h_f, double* h_out, int precision);
 
+/* ---- batched FP32 apply that allocates nothing --------------------------
+ * No counterpart in the reference.  For callers that must not allocate
+ * device memory: code running inside an allocator or memory-pool callback,
+ * in a host function enqueued on a stream, in a latency-critical loop that
+ * cannot wait on the driver's allocator, or next to a framework that owns all
+ * device memory.  The caller passes everything as device pointers (the CSR
+ * list, the FP32 weights of n_outputs outputs laid out [o * w_stride + j],
+ * the FP64 field and the [n_outputs * n] output); the only scratch, the
+ * (hi, lo) split of the field, is a fixed device array inside the library.
+ * Limits: n <= DCPSE_NOALLOC_MAX_PARTICLES (larger n is rejected with
+ * DCPSE_ERR_CAPACITY); that array (16 MiB) is held on every GPU that loads
+ * the library until the process exits.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (e.g. on two streams) race and must be serialised by
+ * the caller.  Results equal dcpse_apply_batched(..., DCPSE_F32). */
+#define DCPSE_NOALLOC_MAX_PARTICLES 2097152
+int dcpse_apply_batched_f32_noalloc(int64_t n, int n_outputs, const int64_t* d_rowptr, const int32_t* d_cols,
+                                    const float* d_w, int64_t w_stride, const double* d_f, double* d_out,
+                                    void* stream);
+
 /* ---- timing -------------------------------------------------------------
  * Optional CUDA-event timing of the plan's kernels on the plan's stream (the
  * role of the reference's std::chrono prints in Dcpse.cuh:581-716).

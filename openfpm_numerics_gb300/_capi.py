@@ -45,6 +45,7 @@ SIGNATURES = {
     "dcpse_apply_output_f64": (_I, [_P, _I, _P, _P]),
     "dcpse_apply_batched": (_I, [_P, _P, _P, _I]),
     "dcpse_apply_batched_host": (_I, [_P, _P, _P, _I]),
+    "dcpse_apply_batched_f32_noalloc": (_I, [_I64, _I, _P, _P, _P, _I64, _P, _P, _P]),
     "dcpse_plan_set_timing": (_I, [_P, _I]),
     "dcpse_plan_timing": (_I, [_P, _I, _c.POINTER(_D), _PI64]),
     "dcpse_plan_reset_timing": (_I, [_P]),

@@ -124,6 +124,8 @@ void dfree(T*& p) {
 
 }  // namespace
 
+int dcpse::set_error(int code, const char* msg) { return fail(code, msg); }
+
 struct KernelTimer {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
     size_t used = 0;

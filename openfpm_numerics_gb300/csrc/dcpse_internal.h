@@ -128,4 +128,7 @@ cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const 
 
 int num_sms();
 
+// Records msg as this thread's dcpse_last_error() and returns code.
+int set_error(int code, const char* msg);
+
 }  // namespace dcpse
