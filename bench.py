@@ -45,6 +45,10 @@ def parse():
     ap.add_argument("--nside", type=int, default=128)
     ap.add_argument("--cpu-sample", type=int, default=32768, help="particles in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", choices=["apply", "assemble"], default=None,
+                    help="small-footprint run of one kernel family (for profiler captures)")
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--mode", type=int, default=0, help="apply loading: 0 auto, 1 direct, 2 TMA-staged")
     return ap.parse_args()
 
 
@@ -72,7 +76,7 @@ class Clocks:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -127,14 +131,11 @@ def cpu_oracle_run(pos, rcut, f, sample, steps, warmup, nthreads):
     t0 = time.perf_counter()
     terms = [oracle.assemble(pos[:S], rp, cols, s, 2, support=pos, nthreads=nthreads) for s in sigs]
     t_asm = time.perf_counter() - t0
+    multi = oracle.MultiApply(rp, cols, [(t[2], t[1], sum(s)) for t, s in zip(terms, sigs)],
+                              [0, 1, 2, 3, 3, 3], NOUT, f, f_dom=f[:S])
 
     def step():
-        gx = oracle.apply(f, rp, cols, terms[0][2], terms[0][1], 1, f_dom=f[:S], nthreads=nthreads)
-        gy = oracle.apply(f, rp, cols, terms[1][2], terms[1][1], 1, f_dom=f[:S], nthreads=nthreads)
-        gz = oracle.apply(f, rp, cols, terms[2][2], terms[2][1], 1, f_dom=f[:S], nthreads=nthreads)
-        lap = sum(oracle.apply(f, rp, cols, terms[3 + i][2], terms[3 + i][1], 2, f_dom=f[:S], nthreads=nthreads)
-                  for i in range(3))
-        return gx, gy, gz, lap
+        return multi(nthreads)
 
     for _ in range(warmup):
         step()
@@ -261,8 +262,25 @@ def run_ours(args):
 
     # fast assembly (summed right-hand sides) -> FP32 weights for the headline
     plan.reset_timing()
-    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
+    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID)
     t_asm_fast = plan.timing(C.K_ASSEMBLE)[0] / 1e3
+
+    # schedule autotuning (untimed): lanes per row x direct / TMA-staged loads
+    from openfpm_numerics_gb300 import autotune
+
+    tuned = autotune.tune_apply(plan, f, C.F32, reps=5, warmup=2)
+
+    # FP32 with the bf16 residual correction (near-FP64 accuracy)
+    outr = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
+    for _ in range(3):
+        plan.apply(f, C.F32_RESID, outr)
+    ev0.record(stream)
+    for _ in range(nplain):
+        plan.apply(f, C.F32_RESID, outr)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_resid = ev0.elapsed_time(ev1) / 1e3 / nplain
+    resr = outr.cpu().numpy()
 
     out = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
     clocks = Clocks(local)
@@ -282,6 +300,7 @@ def run_ours(args):
     k_ms, k_launch = plan.timing(C.K_APPLY_BATCHED)
     s_ms, s_launch = plan.timing(C.K_SPLIT)
     clk = clocks.stop()
+    plan.check()
     if dist:
         tt = torch.tensor([t_step], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -312,6 +331,8 @@ def run_ours(args):
         "fp32_vs_fp64_reference_order_normwise": max(rel_err(res32[o], ref_out[o]) for o in range(NOUT)),
         "fp32_vs_fp64_reference_order_rms": max(float(np.sqrt(np.mean((res32[o] - ref_out[o]) ** 2)) /
                                                     np.sqrt(np.mean(ref_out[o] ** 2))) for o in range(NOUT)),
+        "fp32_per_output_normwise": [rel_err(res32[o], ref_out[o]) for o in range(NOUT)],
+        "fp32_resid_vs_fp64_reference_order_normwise": max(rel_err(resr[o], ref_out[o]) for o in range(NOUT)),
         "fp64_batched_vs_reference_order_normwise": max(rel_err(b64[o], ref_out[o]) for o in range(NOUT)),
         "fp64_analytic_interior_normwise": [rel_err(ref_out[o][inner], analytic[o][inner]) for o in range(NOUT)],
         "fp32_analytic_interior_normwise": [rel_err(res32[o][inner], analytic[o][inner]) for o in range(NOUT)],
@@ -352,7 +373,8 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (%.2f GB of weights streamed per step)" % (NOUT * nnz * 4 / 1e9),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": traffic, "peak_source": peak_kind, "kernel": "apply_f32_kernel",
+                         "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "apply_f32_tma_kernel" if tuned["mode"] == "tma-staged" else "apply_f32_kernel",
                          "algorithmic_bytes_per_launch": bytes_apply, "kernel_ms": t_kernel * 1e3},
             "e2e": {"value": world * N * NOUT / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": N * 8,
                     "d2h_bytes_per_step": NOUT * N * 8, "ms_per_step": t_e2e * 1e3,
@@ -367,6 +389,9 @@ def run_ours(args):
             "fp64_plain": {"value": N * NOUT / t_plain / 1e9, "ms_per_step": t_plain * 1e3,
                            "note": "one pass per reference Dcpse object (6), reference order"},
             "fp64_batched": {"value": N * NOUT / t_b64 / 1e9, "ms_per_step": t_b64 * 1e3},
+            "fp32_resid": {"value": N * NOUT / t_resid / 1e9, "ms_per_step": t_resid * 1e3,
+                           "note": "FP32 weights + bf16 residual stream (2 B/entry/output)"},
+            "autotune": tuned,
             "speedup_fp32_batched_vs_fp64_plain": t_plain / t_step,
             "errors": errors,
             "cpu_baseline": cpu,
@@ -378,8 +403,59 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_only(args):
+    """One kernel family on the benchmark geometry, nothing else resident:
+    --only apply keeps just the FP32 weights (fast assembly), --only assemble
+    runs the reference-order and fast assemblies."""
+    import torch
+
+    from openfpm_numerics_gb300 import _capi as C
+    from openfpm_numerics_gb300 import workloads as W
+    from openfpm_numerics_gb300.plan import DcpsePlan
+
+    torch.cuda.set_device(0)
+    cfg = W.config2(args.nside)
+    pos = torch.tensor(cfg["pos"], device="cuda")
+    f = torch.tensor(W.field2(cfg["pos"])[0], device="cuda")
+    N = pos.shape[0]
+    stream = torch.cuda.current_stream()
+    plan = DcpsePlan(3, W.grad_lap_outputs(3), order=2, stream=stream)
+    plan.set_timing(True)
+    plan.build_neighbors(pos, cfg["rcut"])
+    nnz = plan.info()["nnz"]
+    res = {"only": args.only, "particles": N, "nnz": nnz}
+    if args.only == "apply":
+        plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
+        plan.set_apply_config(args.lanes, args.mode)
+        out = torch.empty((NOUT, N), dtype=torch.float64, device="cuda")
+        for _ in range(args.warmup):
+            plan.apply(f, C.F32, out)
+        plan.reset_timing()
+        for _ in range(args.steps):
+            plan.apply(f, C.F32, out)
+        ms, k = plan.timing(C.K_APPLY_BATCHED)
+        res["apply_ms"] = ms / max(k, 1)
+        res["achieved_gbs"] = W.apply_bytes(N, nnz, NOUT, 4) / (ms / max(k, 1) / 1e3) / 1e9
+    else:
+        for _ in range(max(1, args.steps)):
+            plan.reset_timing()
+            plan.assemble(pos, C.STORE_TERMS_F64)
+            t_ref = plan.timing(C.K_ASSEMBLE)[0]
+            plan.reset_timing()
+            plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
+            t_fast = plan.timing(C.K_ASSEMBLE)[0]
+        res["assemble_ref_ms"] = t_ref
+        res["assemble_fast_ms"] = t_fast
+    plan.check()
+    plan.close()
+    print(json.dumps(res), flush=True)
+
+
 def main():
     args = parse()
+    if args.only:
+        run_only(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

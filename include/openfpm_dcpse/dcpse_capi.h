@@ -28,6 +28,7 @@ extern "C" {
 #define DCPSE_ERR_CAPACITY 4   /* a size limit was exceeded */
 #define DCPSE_ERR_IO 5         /* save/load failure */
 #define DCPSE_ERR_PARTICLES 6  /* some particles could not be assembled */
+#define DCPSE_ERR_TIMEOUT 7    /* a bounded device wait ran out (results invalid) */
 
 /* per-particle assembly status (dcpse_particle_status / status arrays).
  * The reference raises std::length_error for too few neighbours
@@ -47,10 +48,12 @@ extern "C" {
 #define DCPSE_ASSEMBLE_FAST 8   /* outputs from summed right-hand sides (one solve
                                    per output and basis) instead of per-term sums */
 #define DCPSE_ASSEMBLE_ASYNC 16 /* do not synchronise; query dcpse_particle_status */
+#define DCPSE_STORE_OUT_F32_RESID 32 /* also bf16 residuals w64 - w32 of the FP32 weights */
 
 /* precision of dcpse_apply_batched */
 #define DCPSE_F64 0
-#define DCPSE_F32 1
+#define DCPSE_F32 1       /* FP32 weights, exact differences, compensated sums */
+#define DCPSE_F32_RESID 2 /* FP32 weights + bf16 residual correction (near-FP64 accuracy) */
 
 typedef struct dcpse_plan_s dcpse_plan_t;
 
@@ -173,6 +176,13 @@ int dcpse_apply_batched_f32_noalloc(int64_t n, int n_outputs, const int64_t* d_r
 #define DCPSE_K_NEIGHBORS 4
 #define DCPSE_K_COUNT 5
 int dcpse_plan_set_timing(dcpse_plan_t* plan, int enable);
+/* Apply schedule knobs (autotuning): lanes per row (0 = from the mean row
+ * length, else 4/8/16/32) and staging mode (0 = TMA-staged when the tiles
+ * fit in shared memory, 1 = direct loads, 2 = staged). */
+int dcpse_plan_set_apply_config(dcpse_plan_t* plan, int lanes, int mode);
+/* Synchronises the stream and reports DCPSE_ERR_TIMEOUT if a kernel's
+ * bounded wait ran out since the plan was created. */
+int dcpse_plan_check(dcpse_plan_t* plan);
 /* Synchronises the stream; total device time and launches since the last reset. */
 int dcpse_plan_timing(dcpse_plan_t* plan, int kernel, double* total_ms, int64_t* launches);
 int dcpse_plan_reset_timing(dcpse_plan_t* plan);

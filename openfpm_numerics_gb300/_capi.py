@@ -47,6 +47,8 @@ SIGNATURES = {
     "dcpse_apply_batched_host": (_I, [_P, _P, _P, _I]),
     "dcpse_apply_batched_f32_noalloc": (_I, [_I64, _I, _P, _P, _P, _I64, _P, _P, _P]),
     "dcpse_plan_set_timing": (_I, [_P, _I]),
+    "dcpse_plan_set_apply_config": (_I, [_P, _I, _I]),
+    "dcpse_plan_check": (_I, [_P]),
     "dcpse_plan_timing": (_I, [_P, _I, _c.POINTER(_D), _PI64]),
     "dcpse_plan_reset_timing": (_I, [_P]),
 }
@@ -60,15 +62,18 @@ ERR_STATE = 3
 ERR_CAPACITY = 4
 ERR_IO = 5
 ERR_PARTICLES = 6
+ERR_TIMEOUT = 7
 
 STORE_TERMS_F64 = 1
 STORE_OUT_F64 = 2
 STORE_OUT_F32 = 4
 ASSEMBLE_FAST = 8
 ASSEMBLE_ASYNC = 16
+STORE_OUT_F32_RESID = 32
 
 F64 = 0
 F32 = 1
+F32_RESID = 2
 
 PART_OK, PART_TOO_FEW, PART_BAD_EPS, PART_SINGULAR, PART_NONFINITE = range(5)
 

@@ -8,20 +8,34 @@
 //  * apply_term_f64: one reference Dcpse object, FP64, in the reference's
 //    order  Df_p = (sum_q (f_q + s f_p) K_pq) * eps_p^-|alpha|.  Compiled with
 //    -fmad=false, so it matches the CPU oracle bit for bit.
-//  * apply_batched_{f32,f64}: every output of a plan in one pass over the
-//    neighbour list, with eps^-|alpha| folded into the weights and the
-//    difference form  Df_p = sum_q w_pq (f_q - f_p)  (equal to the reference
-//    formula because the kernels of even |alpha| annihilate constants by
-//    construction and those of odd |alpha| sum to zero by the moment
-//    condition on the constant monomial).  G lanes share a row; each lane
-//    streams G-strided neighbour entries, the G partial sums are combined by
-//    shuffles.  The FP32 path reads f as an exact (hi, lo) float pair so that
-//    f_q - f_p keeps full FP32 relative accuracy.
+//  * batched applies: every output of a plan in one pass over the neighbour
+//    list, eps^-|alpha| folded into the weights, difference form
+//    Df_p = sum_q w_pq (f_q - f_p)  (equal to the reference formula: kernels
+//    of even |alpha| annihilate constants by construction, those of odd
+//    |alpha| sum to zero by the moment condition on the constant monomial).
+//    G lanes share a row; lane l takes entries l, l+G, l+2G, ...; the G
+//    partial sums are combined by a shuffle tree.
+//
+// FP32 arithmetic of the batched apply: the field is an exact (hi, lo) float
+// pair; f_q - f_p is formed exactly as dh + dl with TwoSum (Knuth); each
+// product w*dh enters a compensated sum (TwoSum of the running sum and the
+// product, plus the product's exact error from fmaf), so the result carries
+// the FP32 weight rounding and little else.  An optional bf16 residual of
+// every weight (w64 - w32) restores the weights to ~2^-33 relative.
+//
+// Two kernels implement it with the same per-lane order (identical results):
+//  * apply_f32_kernel reads the CSR streams straight from global memory;
+//  * apply_f32_tma_kernel stages each tile of rows' columns and weight
+//    streams into shared memory with cp.async.bulk (TMA bulk copies)
+//    completing on an mbarrier, several tiles in flight per CTA.
+#include <cuda_bf16.h>
+
 #include "dcpse_internal.h"
 
 namespace dcpse {
 namespace {
 
+// ------------------------------------------------------------ FP64 term ---
 __global__ void __launch_bounds__(256) apply_term_f64_kernel(int64_t n, const int64_t* __restrict__ rowptr,
                                                              const int32_t* __restrict__ cols,
                                                              const double* __restrict__ K,
@@ -47,41 +61,270 @@ __global__ void split_kernel(const double* __restrict__ f, int64_t n, float2* __
     }
 }
 
-template <int G, int NO>
-__global__ void __launch_bounds__(256) apply_f32_kernel(int64_t n, const int64_t* __restrict__ rowptr,
-                                                        const int32_t* __restrict__ cols,
-                                                        const float* __restrict__ w, int64_t nnz,
-                                                        const float2* __restrict__ f2, double* __restrict__ out) {
+// ----------------------------------------------------- FP32 row arithmetic --
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+template <int NO, bool RESID>
+struct RowAcc {
+    float s[NO], c[NO];
+    __device__ __forceinline__ void init() {
+#pragma unroll
+        for (int o = 0; o < NO; ++o) s[o] = c[o] = 0.0f;
+    }
+    // one neighbour: weights w[o] (and residuals r[o]), field pair fq, fp
+    __device__ __forceinline__ void add(const float (&w)[NO], const float (&r)[NO], float2 fq, float2 fp) {
+        float dh, e0;
+        two_sum(fq.x, -fp.x, dh, e0);
+        const float dl = e0 + (fq.y - fp.y);
+#pragma unroll
+        for (int o = 0; o < NO; ++o) {
+            const float p = w[o] * dh;
+            float ns, e;
+            two_sum(s[o], p, ns, e);
+            s[o] = ns;
+            float t = fmaf(w[o], dh, -p) + e;
+            t = fmaf(w[o], dl, t);
+            if (RESID) t = fmaf(r[o], dh, t);
+            c[o] = c[o] + t;
+        }
+    }
+    template <int G>
+    __device__ __forceinline__ void reduce() {
+#pragma unroll
+        for (int o = 0; o < NO; ++o) {
+#pragma unroll
+            for (int m = G / 2; m > 0; m >>= 1) {
+                float os = __shfl_xor_sync(0xffffffffu, s[o], m);
+                float oc = __shfl_xor_sync(0xffffffffu, c[o], m);
+                float ns, e;
+                two_sum(s[o], os, ns, e);
+                s[o] = ns;
+                c[o] = (c[o] + oc) + e;
+            }
+        }
+    }
+    __device__ __forceinline__ double value(int o) const { return (double)s[o] + (double)c[o]; }
+};
+
+struct F32Args {
+    int64_t n;
+    const int64_t* rowptr;
+    const int32_t* cols;
+    const float* w;                 // [NO][ws]
+    const __nv_bfloat16* r;         // [NO][ws] or null
+    int64_t ws;                     // weight stream stride (elements)
+    const float2* f2;
+    double* out;                    // [NO][n]
+};
+
+template <int G, int NO, bool RESID>
+__global__ void __launch_bounds__(256) apply_f32_kernel(F32Args a) {
     const int lane = threadIdx.x & 31;
     const int sub = lane & (G - 1);
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t rows_per_pass = ((int64_t)gridDim.x * blockDim.x) / G;
-    // every lane of a warp runs the same number of passes (shuffles below)
     const int64_t first = (tid - lane) / G;
-    for (int64_t base = first; base < n; base += rows_per_pass) {
+    for (int64_t base = first; base < a.n; base += rows_per_pass) {
         const int64_t row = base + lane / G;
-        float acc[NO];
+        RowAcc<NO, RESID> acc;
+        acc.init();
+        if (row < a.n) {
+            const float2 fp = a.f2[row];
+            const int64_t e = a.rowptr[row + 1];
+            for (int64_t j = a.rowptr[row] + sub; j < e; j += G) {
+                float w[NO], r[NO];
 #pragma unroll
-        for (int o = 0; o < NO; ++o) acc[o] = 0.0f;
-        if (row < n) {
-            const float2 fp = f2[row];
-            const int64_t e = rowptr[row + 1];
-            for (int64_t j = rowptr[row] + sub; j < e; j += G) {
-                const float2 fq = f2[cols[j]];
-                const float d = (fq.x - fp.x) + (fq.y - fp.y);
-#pragma unroll
-                for (int o = 0; o < NO; ++o) acc[o] = fmaf(w[(int64_t)o * nnz + j], d, acc[o]);
+                for (int o = 0; o < NO; ++o) {
+                    w[o] = a.w[(int64_t)o * a.ws + j];
+                    r[o] = RESID ? __bfloat162float(a.r[(int64_t)o * a.ws + j]) : 0.0f;
+                }
+                acc.add(w, r, a.f2[a.cols[j]], fp);
             }
         }
-#pragma unroll
-        for (int o = 0; o < NO; ++o) {
-#pragma unroll
-            for (int s = G / 2; s > 0; s >>= 1) acc[o] += __shfl_xor_sync(0xffffffffu, acc[o], s);
-        }
-        if (row < n) {
+        acc.template reduce<G>();
+        if (row < a.n) {
 #pragma unroll
             for (int o = 0; o < NO; ++o)
-                if (sub == (o & (G - 1))) out[(int64_t)o * n + row] = (double)acc[o];
+                if (sub == (o & (G - 1))) a.out[(int64_t)o * a.n + row] = acc.value(o);
+        }
+    }
+}
+
+// ------------------------------------------------------- TMA bulk staging --
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: returns false after ~2^22 polls (each try_wait itself blocks
+// for a while), so a copy that never lands cannot hang the GPU.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    for (uint32_t it = 0; it < (1u << 22); ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+struct TmaCfg {
+    int stages;
+    int ecap;        // entries per stage buffer (multiple of 8)
+    int stage_bytes; // bytes of one stage (16-byte multiple)
+    int64_t ntiles;
+    int64_t nnz;     // stride of the weight streams (element offset o*nnz)
+};
+
+// 16-byte aligned window [a0, a1) of a 4-byte stream covering [b, e)
+__device__ __forceinline__ int64_t win_lo4(int64_t b) { return b & ~int64_t(3); }
+__device__ __forceinline__ int64_t win_hi4(int64_t e) { return (e + 3) & ~int64_t(3); }
+__device__ __forceinline__ int64_t win_lo8(int64_t b) { return b & ~int64_t(7); }
+__device__ __forceinline__ int64_t win_hi8(int64_t e) { return (e + 7) & ~int64_t(7); }
+
+// Layout of one stage: cols[ecap] i32 | w[NO][ecap] f32 | r[NO][ecap] bf16
+template <int NO, bool RESID>
+__device__ __forceinline__ void issue_tile(const F32Args& a, const TmaCfg& c, int64_t tile, int R, unsigned char* stage,
+                                           uint32_t bar) {
+    const int64_t r0 = tile * R;
+    const int64_t r1 = min(r0 + R, a.n);
+    const int64_t e0 = a.rowptr[r0], e1 = a.rowptr[r1];
+    uint32_t total = 0;
+    const int64_t c0 = win_lo4(e0), c1 = win_hi4(e1);
+    total += (uint32_t)((c1 - c0) * 4);
+#pragma unroll
+    for (int o = 0; o < NO; ++o) {
+        const int64_t b = (int64_t)o * a.ws + e0, e = (int64_t)o * a.ws + e1;
+        total += (uint32_t)((win_hi4(e) - win_lo4(b)) * 4);
+        if (RESID) total += (uint32_t)((win_hi8(e) - win_lo8(b)) * 2);
+    }
+    mbar_expect_tx(bar, total);
+    unsigned char* p = stage;
+    if (c1 > c0) bulk_g2s(smem_u32(p), a.cols + c0, (uint32_t)((c1 - c0) * 4), bar);
+    p += (size_t)c.ecap * 4;
+#pragma unroll
+    for (int o = 0; o < NO; ++o) {
+        const int64_t b = (int64_t)o * a.ws + e0, e = (int64_t)o * a.ws + e1;
+        if (win_hi4(e) > win_lo4(b))
+            bulk_g2s(smem_u32(p + (size_t)o * c.ecap * 4), a.w + win_lo4(b), (uint32_t)((win_hi4(e) - win_lo4(b)) * 4),
+                     bar);
+    }
+    if (RESID) {
+        p += (size_t)NO * c.ecap * 4;
+#pragma unroll
+        for (int o = 0; o < NO; ++o) {
+            const int64_t b = (int64_t)o * a.ws + e0, e = (int64_t)o * a.ws + e1;
+            if (win_hi8(e) > win_lo8(b))
+                bulk_g2s(smem_u32(p + (size_t)o * c.ecap * 2), a.r + win_lo8(b),
+                         (uint32_t)((win_hi8(e) - win_lo8(b)) * 2), bar);
+        }
+    }
+}
+
+template <int G, int NO, bool RESID>
+__global__ void __launch_bounds__(256) apply_f32_tma_kernel(F32Args a, TmaCfg c, int* err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr int R = 256 / G;  // rows per tile: one G-lane group per row
+    __shared__ __align__(8) unsigned long long bars[16];
+    __shared__ int s_ok;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int sub = lane & (G - 1);
+    const int grp = tid / G;
+    const int S = c.stages;
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) {
+            int64_t t = blockIdx.x + (int64_t)s * gridDim.x;
+            if (t < c.ntiles) issue_tile<NO, RESID>(a, c, t, R, smem + (size_t)s * c.stage_bytes, smem_u32(&bars[s]));
+        }
+    }
+    for (int64_t i = 0;; ++i) {
+        const int64_t t = blockIdx.x + i * gridDim.x;
+        if (t >= c.ntiles) break;
+        const int s = (int)(i % S);
+        const uint32_t parity = (uint32_t)((i / S) & 1);
+        if (tid == 0) s_ok = mbar_wait_bounded(smem_u32(&bars[s]), parity) ? 1 : 0;
+        __syncthreads();
+        if (!s_ok) {
+            if (tid == 0) {
+                atomicExch(err, 1);
+                // let copies already issued for later stages land (bounded)
+                for (int64_t k = 1; k < S; ++k) {
+                    const int64_t ii = i + k;
+                    if (blockIdx.x + ii * gridDim.x >= c.ntiles) break;
+                    mbar_wait_bounded(smem_u32(&bars[ii % S]), (uint32_t)((ii / S) & 1));
+                }
+            }
+            return;
+        }
+        const unsigned char* stage = smem + (size_t)s * c.stage_bytes;
+        const int64_t r0 = t * R;
+        const int64_t e0 = a.rowptr[r0];
+        const int32_t* scols = reinterpret_cast<const int32_t*>(stage);
+        const float* sw = reinterpret_cast<const float*>(stage + (size_t)c.ecap * 4);
+        const __nv_bfloat16* sr = reinterpret_cast<const __nv_bfloat16*>(stage + (size_t)c.ecap * 4 * (1 + NO));
+        const int64_t row = r0 + grp;
+        RowAcc<NO, RESID> acc;
+        acc.init();
+        if (row < a.n) {
+            const float2 fp = a.f2[row];
+            const int64_t rb = a.rowptr[row], re = a.rowptr[row + 1];
+            const int64_t cb = rb - win_lo4(e0);
+            int64_t wb[NO], rbo[NO];
+#pragma unroll
+            for (int o = 0; o < NO; ++o) {
+                wb[o] = (int64_t)o * a.ws + rb - win_lo4((int64_t)o * a.ws + e0);
+                rbo[o] = (int64_t)o * a.ws + rb - win_lo8((int64_t)o * a.ws + e0);
+            }
+            for (int64_t j = sub; j < re - rb; j += G) {
+                float w[NO], r[NO];
+#pragma unroll
+                for (int o = 0; o < NO; ++o) {
+                    w[o] = sw[(size_t)o * c.ecap + wb[o] + j];
+                    r[o] = RESID ? __bfloat162float(sr[(size_t)o * c.ecap + rbo[o] + j]) : 0.0f;
+                }
+                acc.add(w, r, a.f2[scols[cb + j]], fp);
+            }
+        }
+        acc.template reduce<G>();
+        if (row < a.n) {
+#pragma unroll
+            for (int o = 0; o < NO; ++o)
+                if (sub == (o & (G - 1))) a.out[(int64_t)o * a.n + row] = acc.value(o);
+        }
+        __syncthreads();  // every thread is done with stage s
+        if (tid == 0) {
+            const int64_t t2 = t + (int64_t)S * gridDim.x;
+            if (t2 < c.ntiles) {
+                fence_proxy_async();
+                issue_tile<NO, RESID>(a, c, t2, R, smem + (size_t)s * c.stage_bytes, smem_u32(&bars[s]));
+            }
         }
     }
 }
@@ -131,40 +374,101 @@ int grid_rows(int64_t rows, int rows_per_block) {
     return (int)g;
 }
 
-template <int G, typename W, typename F>
-cudaError_t launch_batched(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const W* w, int64_t nnz,
-                           const F* f, double* out, cudaStream_t s) {
-    const int grid = grid_rows(n, 256 / G);
-#define DCPSE_CASE(NO)                                                                        \
-    case NO:                                                                                  \
-        if constexpr (sizeof(W) == 4)                                                         \
-            apply_f32_kernel<G, NO><<<grid, 256, 0, s>>>(n, rowptr, cols, (const float*)w, nnz, \
-                                                         (const float2*)f, out);              \
-        else                                                                                  \
-            apply_f64_kernel<G, NO><<<grid, 256, 0, s>>>(n, rowptr, cols, (const double*)w, nnz, \
-                                                         (const double*)f, out);              \
-        break;
-    switch (nout) {
-        DCPSE_CASE(1)
-        DCPSE_CASE(2)
-        DCPSE_CASE(3)
-        DCPSE_CASE(4)
-        DCPSE_CASE(5)
-        DCPSE_CASE(6)
-        DCPSE_CASE(7)
-        DCPSE_CASE(8)
-        default:
-            return cudaErrorInvalidValue;
-    }
-#undef DCPSE_CASE
-    return cudaGetLastError();
-}
-
 int lanes_for(int64_t n, int64_t nnz) {
     double avg = n > 0 ? (double)nnz / (double)n : 0.0;
     if (avg <= 24.0) return 8;
     if (avg <= 96.0) return 16;
     return 32;
+}
+
+template <int G, int NO, bool RESID>
+cudaError_t launch_f32_direct(const F32Args& a, cudaStream_t s) {
+    apply_f32_kernel<G, NO, RESID><<<grid_rows(a.n, 256 / G), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int G, int NO, bool RESID>
+cudaError_t launch_f32_tma(const F32Args& a, int maxk, int* err, cudaStream_t s, bool* used) {
+    *used = false;
+    constexpr int R = 256 / G;
+    TmaCfg c{};
+    c.ecap = ((R * maxk + 16) + 7) & ~7;
+    size_t per = (size_t)c.ecap * (4 + 4 * NO + (RESID ? 2 * NO : 0));
+    per = (per + 127) & ~size_t(127);
+    c.stage_bytes = (int)per;
+    c.ntiles = (a.n + R - 1) / R;
+    c.nnz = a.ws;
+    int dev = 0, smem_max = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    // two CTAs per SM, as many stages as fit (2..8)
+    int stages = (int)((smem_max / 2 - 1024) / per);
+    if (stages > 8) stages = 8;
+    if (stages < 2) return cudaSuccess;  // rows too long for staging: caller uses the direct kernel
+    c.stages = stages;
+    size_t bytes = per * stages;
+    auto kern = apply_f32_tma_kernel<G, NO, RESID>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, bytes);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaSuccess;
+    int64_t grid = (int64_t)num_sms() * per_sm;
+    if (grid > c.ntiles) grid = c.ntiles;
+    kern<<<(unsigned)grid, 256, bytes, s>>>(a, c, err);
+    *used = true;
+    return cudaGetLastError();
+}
+
+template <int G, bool RESID>
+cudaError_t dispatch_f32(const F32Args& a, int nout, int maxk, int* err, int mode, cudaStream_t s) {
+#define DCPSE_F32_CASE(NO)                                                            \
+    case NO: {                                                                        \
+        if (mode != 1) {                                                              \
+            bool used = false;                                                        \
+            cudaError_t e = launch_f32_tma<G, NO, RESID>(a, maxk, err, s, &used);     \
+            if (e != cudaSuccess || used) return e;                                   \
+        }                                                                             \
+        return launch_f32_direct<G, NO, RESID>(a, s);                                 \
+    }
+    switch (nout) {
+        DCPSE_F32_CASE(1)
+        DCPSE_F32_CASE(2)
+        DCPSE_F32_CASE(3)
+        DCPSE_F32_CASE(4)
+        DCPSE_F32_CASE(5)
+        DCPSE_F32_CASE(6)
+        DCPSE_F32_CASE(7)
+        DCPSE_F32_CASE(8)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef DCPSE_F32_CASE
+}
+
+template <int G>
+cudaError_t launch_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const double* w, int64_t nnz,
+                       const double* f, double* out, cudaStream_t s) {
+    const int grid = grid_rows(n, 256 / G);
+#define DCPSE_F64_CASE(NO)                                                                            \
+    case NO:                                                                                          \
+        apply_f64_kernel<G, NO><<<grid, 256, 0, s>>>(n, rowptr, cols, w, nnz, f, out);                \
+        break;
+    switch (nout) {
+        DCPSE_F64_CASE(1)
+        DCPSE_F64_CASE(2)
+        DCPSE_F64_CASE(3)
+        DCPSE_F64_CASE(4)
+        DCPSE_F64_CASE(5)
+        DCPSE_F64_CASE(6)
+        DCPSE_F64_CASE(7)
+        DCPSE_F64_CASE(8)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef DCPSE_F64_CASE
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -188,23 +492,62 @@ cudaError_t split_f64(const double* f, int64_t n, float2* f2, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s) {
+    if (p.n == 0) return cudaSuccess;
+    F32Args a{};
+    a.n = p.n;
+    a.rowptr = p.rowptr;
+    a.cols = p.cols;
+    a.w = p.w;
+    a.r = reinterpret_cast<const __nv_bfloat16*>(p.resid);
+    a.ws = p.ws;
+    a.f2 = p.f2;
+    a.out = p.out;
+    const int G = p.lanes ? p.lanes : lanes_for(p.n, p.nnz);
+    const bool resid = p.resid != nullptr;
+    const int mode = p.mode;  // 0 auto (staged if it fits), 1 direct, 2 staged
+#define DCPSE_G(GG)                                                                                  \
+    case GG:                                                                                         \
+        return resid ? dispatch_f32<GG, true>(a, p.nout, p.maxk, p.err, mode, s)                     \
+                     : dispatch_f32<GG, false>(a, p.nout, p.maxk, p.err, mode, s);
+    switch (G) {
+        DCPSE_G(4)
+        DCPSE_G(8)
+        DCPSE_G(16)
+        DCPSE_G(32)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef DCPSE_G
+}
+
 cudaError_t apply_batched_f32(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const float* w,
                               int64_t nnz, const float2* f2, double* out, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    switch (lanes_for(n, nnz)) {
-        case 8: return launch_batched<8>(n, nout, rowptr, cols, w, nnz, f2, out, s);
-        case 16: return launch_batched<16>(n, nout, rowptr, cols, w, nnz, f2, out, s);
-        default: return launch_batched<32>(n, nout, rowptr, cols, w, nnz, f2, out, s);
-    }
+    ApplyF32 p{};
+    p.n = n;
+    p.nout = nout;
+    p.rowptr = rowptr;
+    p.cols = cols;
+    p.w = w;
+    p.ws = nnz;
+    p.nnz = -1;
+    p.f2 = f2;
+    p.out = out;
+    p.mode = 1;  // caller-owned arrays: no over-read of padded windows
+    // lanes from the mean row length (needs nnz; read from rowptr[n] is a
+    // host sync, so the caller's stride stands in when it equals nnz)
+    p.lanes = 0;
+    p.nnz = nnz;
+    return apply_batched_f32x(p, s);
 }
 
 cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const double* w,
                               int64_t nnz, const double* f, double* out, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     switch (lanes_for(n, nnz)) {
-        case 8: return launch_batched<8>(n, nout, rowptr, cols, w, nnz, f, out, s);
-        case 16: return launch_batched<16>(n, nout, rowptr, cols, w, nnz, f, out, s);
-        default: return launch_batched<32>(n, nout, rowptr, cols, w, nnz, f, out, s);
+        case 8: return launch_f64<8>(n, nout, rowptr, cols, w, nnz, f, out, s);
+        case 16: return launch_f64<16>(n, nout, rowptr, cols, w, nnz, f, out, s);
+        default: return launch_f64<32>(n, nout, rowptr, cols, w, nnz, f, out, s);
     }
 }
 

@@ -26,6 +26,8 @@
 // neighbour count is handled with fixed shared memory.
 #include <cstdio>
 
+#include <cuda_bf16.h>
+
 #include "dcpse_internal.h"
 
 namespace dcpse {
@@ -365,7 +367,11 @@ __global__ void __launch_bounds__(kWarps * 32) assemble_kernel(AsmArgs a, Layout
             }
             for (int t = 0; t < noutputs; ++t) {
                 if (a.w64) a.w64[(int64_t)t * a.nnz + beg + q] = wout[t];
-                if (a.w32) a.w32[(int64_t)t * a.nnz + beg + q] = (float)wout[t];
+                const float w32 = (float)wout[t];
+                if (a.w32) a.w32[(int64_t)t * a.nnz + beg + q] = w32;
+                if (a.r16)
+                    reinterpret_cast<__nv_bfloat16*>(a.r16)[(int64_t)t * a.nnz + beg + q] =
+                        __float2bfloat16_rn((float)(wout[t] - (double)w32));
             }
         }
         nonfinite = __any_sync(0xffffffffu, nonfinite);
@@ -378,6 +384,8 @@ __global__ void __launch_bounds__(kWarps * 32) assemble_kernel(AsmArgs a, Layout
                 for (int t = 0; t < noutputs; ++t) {
                     if (a.w64) a.w64[(int64_t)t * a.nnz + beg + q] = 0.0;
                     if (a.w32) a.w32[(int64_t)t * a.nnz + beg + q] = 0.0f;
+                    if (a.r16)
+                        reinterpret_cast<__nv_bfloat16*>(a.r16)[(int64_t)t * a.nnz + beg + q] = __float2bfloat16_rn(0.0f);
                 }
             }
         } else if (st_terms) {

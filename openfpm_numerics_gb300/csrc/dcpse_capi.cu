@@ -109,6 +109,11 @@ __global__ void row_max_kernel(const int64_t* rowptr, int64_t n, int* maxk) {
     atomicMax(maxk, m);
 }
 
+// Entries of padding after the column and FP32 weight arrays: the staged
+// apply copies 16-byte aligned windows that may end up to 7 entries past the
+// last used one.
+constexpr int64_t kPad = 8;
+
 template <typename T>
 cudaError_t dalloc(T** p, size_t count) {
     *p = nullptr;
@@ -190,7 +195,10 @@ struct dcpse_plan_s {
     double* k_term = nullptr;
     double* w64 = nullptr;
     float* w32 = nullptr;
+    void* r16 = nullptr;  // bf16 residuals of w32
     unsigned long long* summary = nullptr;  // [count, first]
+    int* d_err = nullptr;                   // set by kernels whose bounded wait ran out
+    int apply_lanes = 0, apply_mode = 0;
     // apply scratch
     float2* f2 = nullptr;
     double* hf = nullptr;    // device copy of a host field (host apply)
@@ -203,6 +211,8 @@ struct dcpse_plan_s {
         dfree(k_term);
         dfree(w64);
         dfree(w32);
+        if (r16) cudaFree(r16);
+        r16 = nullptr;
         assembled = false;
     }
     void free_all() {
@@ -213,6 +223,7 @@ struct dcpse_plan_s {
         dfree(hf);
         dfree(hout);
         dfree(summary);
+        dfree(d_err);
         dfree(dtab);
         delete htab;
         htab = nullptr;
@@ -391,6 +402,8 @@ int dcpse_plan_create(dcpse_plan_t** plan, int dim, int n_outputs, const int* te
     cudaError_t e = dalloc(&P->dtab, 1);
     if (e == cudaSuccess) e = cudaMemcpy(P->dtab, P->htab, sizeof(AsmTables), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = dalloc(&P->summary, 2);
+    if (e == cudaSuccess) e = dalloc(&P->d_err, 1);
+    if (e == cudaSuccess) e = cudaMemset(P->d_err, 0, sizeof(int));
     if (e != cudaSuccess) {
         P->free_all();
         delete P;
@@ -468,7 +481,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     DCPSE_CK(dalloc(&P->rowptr, (size_t)n + 1));
     if (n == 0) {
         DCPSE_CK(cudaMemsetAsync(P->rowptr, 0, sizeof(int64_t), s));
-        DCPSE_CK(dalloc(&P->cols, 1));
+        DCPSE_CK(dalloc(&P->cols, kPad));
         return DCPSE_OK;
     }
     unsigned long long* mm = nullptr;
@@ -583,7 +596,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     if (e == cudaSuccess) e = cudaMemcpyAsync(&hk, maxk, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e == cudaSuccess) e = dalloc(&tmp, nnz);
-    if (e == cudaSuccess) e = dalloc(&P->cols, nnz);
+    if (e == cudaSuccess) e = dalloc(&P->cols, nnz + kPad);
     if (e == cudaSuccess) e = fill_neighbors(a, P->rowptr, tmp, P->cols, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cleanup();
@@ -603,7 +616,7 @@ int dcpse_set_neighbors(dcpse_plan_t* P, int64_t n, int64_t nnz, const int64_t* 
     P->n = n;
     P->nnz = nnz;
     DCPSE_CK(dalloc(&P->rowptr, (size_t)n + 1));
-    DCPSE_CK(dalloc(&P->cols, nnz));
+    DCPSE_CK(dalloc(&P->cols, nnz + kPad));
     DCPSE_CK(cudaMemcpyAsync(P->rowptr, d_rowptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToDevice, s));
     if (nnz > 0) DCPSE_CK(cudaMemcpyAsync(P->cols, d_cols, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, s));
     {
@@ -665,8 +678,16 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     if (!(flags & DCPSE_STORE_TERMS_F64)) dfree(P->k_term);
     if ((flags & DCPSE_STORE_OUT_F64) && !P->w64) DCPSE_CK(dalloc(&P->w64, (size_t)P->nout * nnz));
     if (!(flags & DCPSE_STORE_OUT_F64)) dfree(P->w64);
-    if ((flags & DCPSE_STORE_OUT_F32) && !P->w32) DCPSE_CK(dalloc(&P->w32, (size_t)P->nout * nnz));
+    if ((flags & DCPSE_STORE_OUT_F32) && !P->w32) DCPSE_CK(dalloc(&P->w32, (size_t)P->nout * nnz + kPad));
     if (!(flags & DCPSE_STORE_OUT_F32)) dfree(P->w32);
+    if ((flags & DCPSE_STORE_OUT_F32_RESID) && !(flags & DCPSE_STORE_OUT_F32))
+        return fail(DCPSE_ERR_ARG, "residuals need DCPSE_STORE_OUT_F32");
+    if ((flags & DCPSE_STORE_OUT_F32_RESID) && !P->r16)
+        DCPSE_CK(cudaMalloc(&P->r16, ((size_t)P->nout * nnz + kPad) * 2));
+    if (!(flags & DCPSE_STORE_OUT_F32_RESID) && P->r16) {
+        cudaFree(P->r16);
+        P->r16 = nullptr;
+    }
     AsmArgs a{};
     a.tab = P->dtab;
     a.dim = P->dim;
@@ -684,6 +705,7 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     a.k_term = P->k_term;
     a.w64 = P->w64;
     a.w32 = P->w32;
+    a.r16 = P->r16;
     a.nnz = nnz;
     P->tstart(DCPSE_K_ASSEMBLE);
     cudaError_t e = assemble(a, *P->htab, s);
@@ -792,15 +814,32 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
     if (int rc = check_plan(P)) return rc;
     if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
     if (P->n > 0 && (!d_f || !d_out)) return fail(DCPSE_ERR_ARG, "NULL field");
-    if (precision == DCPSE_F32) {
+    if (precision == DCPSE_F32 || precision == DCPSE_F32_RESID) {
         if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
+        if (precision == DCPSE_F32_RESID && !P->r16)
+            return fail(DCPSE_ERR_STATE, "FP32 residuals not stored (DCPSE_STORE_OUT_F32_RESID)");
         if (!P->f2) DCPSE_CK(dalloc(&P->f2, P->n));
         P->tstart(DCPSE_K_SPLIT);
         cudaError_t e = split_f64(d_f, P->n, P->f2, P->stream);
         P->tstop(DCPSE_K_SPLIT);
         DCPSE_CK(e);
+        ApplyF32 ap{};
+        ap.n = P->n;
+        ap.nout = P->nout;
+        ap.rowptr = P->rowptr;
+        ap.cols = P->cols;
+        ap.w = P->w32;
+        ap.resid = (precision == DCPSE_F32_RESID) ? P->r16 : nullptr;
+        ap.ws = P->nnz;
+        ap.nnz = P->nnz;
+        ap.maxk = P->maxk;
+        ap.f2 = P->f2;
+        ap.out = d_out;
+        ap.err = P->d_err;
+        ap.mode = P->apply_mode;
+        ap.lanes = P->apply_lanes;
         P->tstart(DCPSE_K_APPLY_BATCHED);
-        e = apply_batched_f32(P->n, P->nout, P->rowptr, P->cols, P->w32, P->nnz, P->f2, d_out, P->stream);
+        e = apply_batched_f32x(ap, P->stream);
         P->tstop(DCPSE_K_APPLY_BATCHED);
         DCPSE_CK(e);
     } else if (precision == DCPSE_F64) {
@@ -825,7 +864,25 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
     int rc = dcpse_apply_batched(P, P->hf, P->hout, precision);
     if (rc != DCPSE_OK) return rc;
     DCPSE_CK(cudaMemcpyAsync(h_out, P->hout, sizeof(double) * P->nout * P->n, cudaMemcpyDeviceToHost, P->stream));
+    return dcpse_plan_check(P);
+}
+
+int dcpse_plan_check(dcpse_plan_t* P) {
+    if (int rc = check_plan(P)) return rc;
+    int herr = 0;
+    DCPSE_CK(cudaMemcpyAsync(&herr, P->d_err, sizeof(int), cudaMemcpyDeviceToHost, P->stream));
     DCPSE_CK(cudaStreamSynchronize(P->stream));
+    if (herr) return fail(DCPSE_ERR_TIMEOUT, "a bounded device wait ran out; results of this plan are invalid");
+    return DCPSE_OK;
+}
+
+int dcpse_plan_set_apply_config(dcpse_plan_t* P, int lanes, int mode) {
+    if (int rc = check_plan(P)) return rc;
+    if (lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+        return fail(DCPSE_ERR_ARG, "lanes must be 0, 4, 8, 16 or 32");
+    if (mode < 0 || mode > 2) return fail(DCPSE_ERR_ARG, "mode must be 0, 1 or 2");
+    P->apply_lanes = lanes;
+    P->apply_mode = mode;
     return DCPSE_OK;
 }
 

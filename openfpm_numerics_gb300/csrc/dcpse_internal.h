@@ -110,6 +110,7 @@ struct AsmArgs {
     double* k_term;      // [nterms][nnz]   (faithful kernels) or nullptr
     double* w64;         // [noutputs][nnz] (summed, eps folded) or nullptr
     float* w32;          // [noutputs][nnz] or nullptr
+    void* r16;           // bf16 [noutputs][nnz]: w64 - w32, or nullptr
     int64_t nnz;
 };
 
@@ -121,8 +122,29 @@ cudaError_t apply_term_f64(int64_t n, const int64_t* rowptr, const int32_t* cols
                            const double* eip, unsigned ord, const double* f, double* out, int accumulate,
                            cudaStream_t s);
 cudaError_t split_f64(const double* f, int64_t n, float2* f2, cudaStream_t s);
+// Batched FP32 apply with caller-owned arrays: direct (unstaged) kernel,
+// lanes per row from nnz / n.
 cudaError_t apply_batched_f32(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const float* w,
                               int64_t nnz, const float2* f2, double* out, cudaStream_t s);
+
+// Full description of a batched FP32 apply (plan-owned, padded arrays).
+struct ApplyF32 {
+    int64_t n;
+    int nout;
+    const int64_t* rowptr;
+    const int32_t* cols;   // padded by >= 8 entries past nnz
+    const float* w;        // [nout][ws], padded by >= 8 entries past nout*ws
+    const void* resid;     // bf16 [nout][ws] residuals (w64 - w32) or null
+    int64_t ws;            // stream stride
+    int64_t nnz;
+    int maxk;              // longest row (sizes the staging buffers)
+    const float2* f2;
+    double* out;           // [nout][n]
+    int* err;              // device error word (bounded waits that ran out)
+    int mode;              // 0 staged if it fits else direct, 1 direct, 2 staged
+    int lanes;             // lanes per row (0 = from the mean row length)
+};
+cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s);
 cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const double* w,
                               int64_t nnz, const double* f, double* out, cudaStream_t s);
 

@@ -213,6 +213,15 @@ class DcpsePlan:
     def set_timing(self, enable=True):
         C.call("dcpse_plan_set_timing", self._h, int(bool(enable)))
 
+    def set_apply_config(self, lanes=0, mode=0):
+        """lanes per row (0 = automatic, else 4/8/16/32); mode 0 = TMA-staged
+        when it fits, 1 = direct loads, 2 = staged."""
+        C.call("dcpse_plan_set_apply_config", self._h, int(lanes), int(mode))
+
+    def check(self):
+        """Synchronise; raise if a kernel's bounded device wait ran out."""
+        C.call("dcpse_plan_check", self._h)
+
     def reset_timing(self):
         C.call("dcpse_plan_reset_timing", self._h)
 

@@ -74,6 +74,8 @@ def lib():
         L.orc_apply.argtypes = [ctypes.c_int64, _D, _D, _I64, _I32, _D, _D, ctypes.c_uint, _D, ctypes.c_int]
         L.orc_apply_sum.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _D, _I64, _I32,
                                     ctypes.POINTER(_D), ctypes.POINTER(_D), _U, _D, ctypes.c_int]
+        L.orc_apply_multi.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _D, _I64, _I32, ctypes.POINTER(_D),
+                                      ctypes.POINTER(_D), _U, _INT, ctypes.c_int, _D, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -201,6 +203,31 @@ def apply_sum(f, rowptr, cols, Ks, eips, diff_orders, *, nthreads=1):
     lib().orc_apply_sum(n, len(Ks), _p(f, _D), _p(f, _D), _p(rowptr, _I64), _p(cols, _I32), kp, ep,
                         _p(do, _U), _p(out, _D), int(nthreads))
     return out
+
+
+class MultiApply:
+    """Prepared arguments of orc_apply_multi (reused across timed calls)."""
+
+    def __init__(self, rowptr, cols, terms, term_output, nout, f_sup, f_dom=None):
+        self.rowptr = _c(rowptr, np.int64)
+        self.cols = _c(cols, np.int32)
+        self.Ks = [_c(t[0], np.float64) for t in terms]       # (K, eip, order)
+        self.eips = [_c(t[1], np.float64) for t in terms]
+        self.orders = _c([t[2] for t in terms], np.uint32)
+        self.tout = _c(term_output, np.int32)
+        self.nout = int(nout)
+        self.f = _c(f_sup, np.float64)
+        self.fd = self.f if f_dom is None else _c(f_dom, np.float64)
+        self.n = self.rowptr.size - 1
+        self.kp = (_D * len(self.Ks))(*[_p(k, _D) for k in self.Ks])
+        self.ep = (_D * len(self.eips))(*[_p(e, _D) for e in self.eips])
+        self.out = np.zeros((self.nout, self.n))
+
+    def __call__(self, nthreads=1):
+        lib().orc_apply_multi(self.n, len(self.Ks), _p(self.f, _D), _p(self.fd, _D), _p(self.rowptr, _I64),
+                              _p(self.cols, _I32), self.kp, self.ep, _p(self.orders, _U), _p(self.tout, _INT),
+                              self.nout, _p(self.out, _D), int(nthreads))
+        return self.out
 
 
 # ---------------------------------------------------------------- helpers --

@@ -647,4 +647,31 @@ void orc_apply_sum(int64_t n_dom, int ncomp, const double* f_sup, const double* 
     });
 }
 
+// Several outputs in one sweep over the particles, the way the reference's
+// expression evaluation visits them (vector_dist_op_compute_op<prp,comp_host>
+// ::compute_expr, src/Operators/Vector/cuda/vector_dist_operators_cuda.cuh:
+// 447-461): for each particle, each output, its terms in order
+// (VECT_DCPSE_V_SUM / VECT_DCPSE_V, DCPSE_op.hpp:144-153, 388-399).
+// term_output[t] gives the output of term t; out is [nout][n_dom].
+void orc_apply_multi(int64_t n_dom, int nterms, const double* f_sup, const double* f_dom, const int64_t* rowptr,
+                     const int32_t* cols, const double* const* kernels, const double* const* eps_inv_pow,
+                     const unsigned* diff_order, const int* term_output, int nout, double* out, int nthreads) {
+    parallel_for(n_dom, nthreads, [&](int64_t b, int64_t e) {
+        for (int64_t p = b; p < e; ++p) {
+            for (int o = 0; o < nout; ++o) {
+                double v = 0.0;
+                for (int c = 0; c < nterms; ++c) {
+                    if (term_output[c] != o) continue;
+                    const double sign = (diff_order[c] % 2 == 0) ? -1.0 : 1.0;
+                    double fxp = sign * f_dom[p];
+                    double D = 0.0;
+                    for (int64_t j = rowptr[p]; j < rowptr[p + 1]; ++j) D = D + (f_sup[cols[j]] + fxp) * kernels[c][j];
+                    v = v + D * eps_inv_pow[c][p];
+                }
+                out[(int64_t)o * n_dom + p] = v;
+            }
+        }
+    });
+}
+
 }  // extern "C"

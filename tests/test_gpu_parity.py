@@ -180,6 +180,46 @@ def test_fast_assembly_close(cuda, orc, name):
         assert np.array_equal(w32.cpu().numpy(), w64.astype(np.float32))
 
 
+@pytest.mark.parametrize("name", ["2d", "3d", "2d_adaptive", "2d_sparse"])
+def test_apply_schedules(cuda, orc, name):
+    """Direct and TMA-staged loading give identical bits; every lane count
+    and the bf16-residual correction stay within their bars."""
+    c = _case(name)
+    plan, pos, _ = _build(c, C.STORE_TERMS_F64 | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID)
+    f = torch.tensor(np.random.default_rng(8).standard_normal(c["pos"].shape[0]), device="cuda")
+    refs = torch.stack([plan.apply_output_f64(o, f) for o in range(len(c["outputs"]))]).cpu().numpy()
+    for lanes in (4, 8, 16, 32):
+        res = {}
+        for mode in (1, 2):
+            plan.set_apply_config(lanes, mode)
+            res[mode] = plan.apply(f, C.F32).clone()
+            plan.check()
+        assert torch.equal(res[1], res[2]), lanes
+        got = res[1].cpu().numpy()
+        for o in range(len(refs)):
+            assert np.abs(got[o] - refs[o]).max() <= 1e-6 * np.abs(refs[o]).max()
+        for mode in (1, 2):
+            plan.set_apply_config(lanes, mode)
+            g = plan.apply(f, C.F32_RESID).cpu().numpy()
+            for o in range(len(refs)):
+                err = np.abs(g[o] - refs[o]).max() / np.abs(refs[o]).max()
+                assert err <= 1e-9, (lanes, mode, o, err)
+    plan.set_apply_config(0, 0)
+
+
+def test_autotune(cuda):
+    from openfpm_numerics_gb300 import autotune
+
+    c = _case("3d")
+    plan, pos, _ = _build(c, C.STORE_OUT_F32)
+    f = torch.tensor(np.random.default_rng(9).standard_normal(c["pos"].shape[0]), device="cuda")
+    ref = plan.apply(f, C.F32).clone()
+    best = autotune.tune_apply(plan, f, reps=2, warmup=1)
+    assert len(best["sweep"]) == 6 and best["lanes"] in (8, 16, 32)
+    got = plan.apply(f, C.F32)
+    assert torch.allclose(got, ref, rtol=0, atol=1e-6 * ref.abs().max().item())
+
+
 def test_analytic_config1_laplacian(cuda):
     cfg = W.config1()
     c = dict(pos=cfg["pos"], rcut=cfg["rcut"], outputs=[[(2, 0), (0, 2)]], order=2)
