@@ -159,7 +159,9 @@ int dcpse_apply_batched_host(dcpse_plan_t* plan, const double* h_f, double* h_ou
  * the array's device address (cudaGetSymbolAddress), so make that first
  * call before any stream capture.  All calls share the array: calls that
  * overlap on the GPU (e.g. on two streams) race and must be serialised by
- * the caller.  Results equal dcpse_apply_batched(..., DCPSE_F32). */
+ * the caller.  Every output takes the compensated FP32 sum, so results equal
+ * dcpse_apply_batched(..., DCPSE_F32) of a plan configured with
+ * DCPSE_APPLY_COMPENSATE_ALL and direct loading (mode 1) at the same lanes. */
 #define DCPSE_NOALLOC_MAX_PARTICLES 2097152
 int dcpse_apply_batched_f32_noalloc(int64_t n, int n_outputs, const int64_t* d_rowptr, const int32_t* d_cols,
                                     const float* d_w, int64_t w_stride, const double* d_f, double* d_out,
@@ -177,8 +179,12 @@ int dcpse_apply_batched_f32_noalloc(int64_t n, int n_outputs, const int64_t* d_r
 #define DCPSE_K_COUNT 5
 int dcpse_plan_set_timing(dcpse_plan_t* plan, int enable);
 /* Apply schedule knobs (autotuning): lanes per row (0 = from the mean row
- * length, else 4/8/16/32) and staging mode (0 = TMA-staged when the tiles
- * fit in shared memory, 1 = direct loads, 2 = staged). */
+ * length, else 4/8/16/32) and loading mode (0 = TMA-staged when the tiles
+ * fit in shared memory, 1 = direct loads, 2 = staged, 3 = direct loads with
+ * 8-deep batches).  OR-ing DCPSE_APPLY_COMPENSATE_ALL into the mode makes
+ * every output of the FP32 apply use the compensated sum (by default only
+ * outputs with a term of order >= 2 do; the others take plain fused sums). */
+#define DCPSE_APPLY_COMPENSATE_ALL 16
 int dcpse_plan_set_apply_config(dcpse_plan_t* plan, int lanes, int mode);
 /* Synchronises the stream and reports DCPSE_ERR_TIMEOUT if a kernel's
  * bounded wait ran out since the plan was created. */

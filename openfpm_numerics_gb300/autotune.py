@@ -12,10 +12,10 @@ import torch
 
 from . import _capi as C
 
-MODES = {1: "direct", 2: "tma-staged"}
+MODES = {1: "direct", 2: "tma-staged", 3: "direct-x8"}
 
 
-def tune_apply(plan, f, precision=C.F32, lanes=(8, 16, 32), modes=(1, 2), reps=10, warmup=2):
+def tune_apply(plan, f, precision=C.F32, lanes=(4, 8, 16), modes=(1, 2, 3), reps=10, warmup=2):
     out = torch.empty((plan.n_outputs, f.shape[0]), dtype=torch.float64, device=f.device)
     stream = plan.stream or torch.cuda.current_stream()
     table = []

@@ -75,21 +75,32 @@ struct RowAcc {
 #pragma unroll
         for (int o = 0; o < NO; ++o) s[o] = c[o] = 0.0f;
     }
-    // one neighbour: weights w[o] (and residuals r[o]), field pair fq, fp
-    __device__ __forceinline__ void add(const float (&w)[NO], const float (&r)[NO], float2 fq, float2 fp) {
+    // one neighbour: weights w[o] (and residuals r[o]), field pair fq, fp.
+    // Outputs whose bit is set in comp take the compensated sum (derivatives
+    // of order >= 2, whose first-order contributions cancel); the others a
+    // plain fused multiply-add into (s, c).
+    __device__ __forceinline__ void add(const float (&w)[NO], const float (&r)[NO], float2 fq, float2 fp,
+                                        uint32_t comp) {
         float dh, e0;
         two_sum(fq.x, -fp.x, dh, e0);
         const float dl = e0 + (fq.y - fp.y);
 #pragma unroll
         for (int o = 0; o < NO; ++o) {
-            const float p = w[o] * dh;
-            float ns, e;
-            two_sum(s[o], p, ns, e);
-            s[o] = ns;
-            float t = fmaf(w[o], dh, -p) + e;
-            t = fmaf(w[o], dl, t);
-            if (RESID) t = fmaf(r[o], dh, t);
-            c[o] = c[o] + t;
+            if (comp & (1u << o)) {
+                const float p = w[o] * dh;
+                float ns, e;
+                two_sum(s[o], p, ns, e);
+                s[o] = ns;
+                float t = fmaf(w[o], dh, -p) + e;
+                t = fmaf(w[o], dl, t);
+                if (RESID) t = fmaf(r[o], dh, t);
+                c[o] = c[o] + t;
+            } else {
+                s[o] = fmaf(w[o], dh, s[o]);
+                float t = fmaf(w[o], dl, c[o]);
+                if (RESID) t = fmaf(r[o], dh, t);
+                c[o] = t;
+            }
         }
     }
     template <int G>
@@ -119,9 +130,41 @@ struct F32Args {
     int64_t ws;                     // weight stream stride (elements)
     const float2* f2;
     double* out;                    // [NO][n]
+    uint32_t comp;                  // outputs that take the compensated sum
 };
 
-template <int G, int NO, bool RESID>
+// Neighbour entries of one lane, U at a time: all loads of a batch are issued
+// before any arithmetic (memory-level parallelism), then the entries are
+// accumulated in ascending order.  Entries past the row end read the row's
+// own particle with zero weights, which adds exactly nothing.
+template <int G, int NO, bool RESID, int U, typename ColF, typename WF, typename RF>
+__device__ __forceinline__ void row_entries(RowAcc<NO, RESID>& acc, int k, int sub, int32_t self, float2 fp,
+                                            const float2* __restrict__ f2, uint32_t comp, ColF col, WF wgt, RF res) {
+    // batches of U entries per lane; entry order within the lane ascending
+    // for every U (the accumulation order does not depend on U)
+    for (int j0 = sub; j0 < k; j0 += G * U) {
+        int32_t q[U];
+        float w[U][NO], r[U][NO];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = j0 + u * G;
+            const bool ok = j < k;
+            q[u] = ok ? col(j) : self;
+#pragma unroll
+            for (int o = 0; o < NO; ++o) {
+                w[u][o] = ok ? wgt(o, j) : 0.0f;
+                r[u][o] = (RESID && ok) ? res(o, j) : 0.0f;
+            }
+        }
+        float2 fq[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) fq[u] = f2[q[u]];
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc.add(w[u], r[u], fq[u], fp, comp);
+    }
+}
+
+template <int G, int NO, bool RESID, int U>
 __global__ void __launch_bounds__(256) apply_f32_kernel(F32Args a) {
     const int lane = threadIdx.x & 31;
     const int sub = lane & (G - 1);
@@ -134,16 +177,16 @@ __global__ void __launch_bounds__(256) apply_f32_kernel(F32Args a) {
         acc.init();
         if (row < a.n) {
             const float2 fp = a.f2[row];
-            const int64_t e = a.rowptr[row + 1];
-            for (int64_t j = a.rowptr[row] + sub; j < e; j += G) {
-                float w[NO], r[NO];
-#pragma unroll
-                for (int o = 0; o < NO; ++o) {
-                    w[o] = a.w[(int64_t)o * a.ws + j];
-                    r[o] = RESID ? __bfloat162float(a.r[(int64_t)o * a.ws + j]) : 0.0f;
-                }
-                acc.add(w, r, a.f2[a.cols[j]], fp);
-            }
+            const int64_t rb = a.rowptr[row];
+            const int k = (int)(a.rowptr[row + 1] - rb);
+            const int32_t* c = a.cols + rb;
+            const float* w0 = a.w + rb;
+            const __nv_bfloat16* r0 = RESID ? a.r + rb : nullptr;
+            const int64_t ws = a.ws;
+            row_entries<G, NO, RESID, U>(
+                acc, k, sub, (int32_t)row, fp, a.f2, a.comp, [&](int j) { return c[j]; },
+                [&](int o, int j) { return w0[o * ws + j]; },
+                [&](int o, int j) { return __bfloat162float(r0[o * ws + j]); });
         }
         acc.template reduce<G>();
         if (row < a.n) {
@@ -295,22 +338,18 @@ __global__ void __launch_bounds__(256) apply_f32_tma_kernel(F32Args a, TmaCfg c,
         if (row < a.n) {
             const float2 fp = a.f2[row];
             const int64_t rb = a.rowptr[row], re = a.rowptr[row + 1];
-            const int64_t cb = rb - win_lo4(e0);
-            int64_t wb[NO], rbo[NO];
+            const int32_t* cptr = scols + (rb - win_lo4(e0));
+            const float* wp[NO];
+            const __nv_bfloat16* rpp[NO];
 #pragma unroll
             for (int o = 0; o < NO; ++o) {
-                wb[o] = (int64_t)o * a.ws + rb - win_lo4((int64_t)o * a.ws + e0);
-                rbo[o] = (int64_t)o * a.ws + rb - win_lo8((int64_t)o * a.ws + e0);
+                wp[o] = sw + (size_t)o * c.ecap + ((int64_t)o * a.ws + rb - win_lo4((int64_t)o * a.ws + e0));
+                rpp[o] = sr + (size_t)o * c.ecap + ((int64_t)o * a.ws + rb - win_lo8((int64_t)o * a.ws + e0));
             }
-            for (int64_t j = sub; j < re - rb; j += G) {
-                float w[NO], r[NO];
-#pragma unroll
-                for (int o = 0; o < NO; ++o) {
-                    w[o] = sw[(size_t)o * c.ecap + wb[o] + j];
-                    r[o] = RESID ? __bfloat162float(sr[(size_t)o * c.ecap + rbo[o] + j]) : 0.0f;
-                }
-                acc.add(w, r, a.f2[scols[cb + j]], fp);
-            }
+            row_entries<G, NO, RESID, 4>(
+                acc, (int)(re - rb), sub, (int32_t)row, fp, a.f2, a.comp, [&](int j) { return cptr[j]; },
+                [&](int o, int j) { return wp[o][j]; },
+                [&](int o, int j) { return __bfloat162float(rpp[o][j]); });
         }
         acc.template reduce<G>();
         if (row < a.n) {
@@ -381,9 +420,9 @@ int lanes_for(int64_t n, int64_t nnz) {
     return 32;
 }
 
-template <int G, int NO, bool RESID>
+template <int G, int NO, bool RESID, int U>
 cudaError_t launch_f32_direct(const F32Args& a, cudaStream_t s) {
-    apply_f32_kernel<G, NO, RESID><<<grid_rows(a.n, 256 / G), 256, 0, s>>>(a);
+    apply_f32_kernel<G, NO, RESID, U><<<grid_rows(a.n, 256 / G), 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -425,12 +464,13 @@ template <int G, bool RESID>
 cudaError_t dispatch_f32(const F32Args& a, int nout, int maxk, int* err, int mode, cudaStream_t s) {
 #define DCPSE_F32_CASE(NO)                                                            \
     case NO: {                                                                        \
-        if (mode != 1) {                                                              \
+        if (mode == 0 || mode == 2) {                                                 \
             bool used = false;                                                        \
             cudaError_t e = launch_f32_tma<G, NO, RESID>(a, maxk, err, s, &used);     \
             if (e != cudaSuccess || used) return e;                                   \
         }                                                                             \
-        return launch_f32_direct<G, NO, RESID>(a, s);                                 \
+        if (mode == 3 && !RESID && G <= 8) return launch_f32_direct<G, NO, RESID, 8>(a, s); \
+        return launch_f32_direct<G, NO, RESID, 4>(a, s);                              \
     }
     switch (nout) {
         DCPSE_F32_CASE(1)
@@ -503,9 +543,10 @@ cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s) {
     a.ws = p.ws;
     a.f2 = p.f2;
     a.out = p.out;
+    a.comp = p.comp;
     const int G = p.lanes ? p.lanes : lanes_for(p.n, p.nnz);
     const bool resid = p.resid != nullptr;
-    const int mode = p.mode;  // 0 auto (staged if it fits), 1 direct, 2 staged
+    const int mode = p.mode;  // 0 auto (staged if it fits), 1 direct, 2 staged, 3 direct x8
 #define DCPSE_G(GG)                                                                                  \
     case GG:                                                                                         \
         return resid ? dispatch_f32<GG, true>(a, p.nout, p.maxk, p.err, mode, s)                     \
@@ -534,6 +575,7 @@ cudaError_t apply_batched_f32(int64_t n, int nout, const int64_t* rowptr, const 
     p.f2 = f2;
     p.out = out;
     p.mode = 1;  // caller-owned arrays: no over-read of padded windows
+    p.comp = 0xffffffffu;  // every output compensated
     // lanes from the mean row length (needs nnz; read from rowptr[n] is a
     // host sync, so the caller's stride stands in when it equals nnz)
     p.lanes = 0;

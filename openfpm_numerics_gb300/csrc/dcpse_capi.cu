@@ -836,8 +836,18 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
         ap.f2 = P->f2;
         ap.out = d_out;
         ap.err = P->d_err;
-        ap.mode = P->apply_mode;
+        ap.mode = P->apply_mode & 15;
         ap.lanes = P->apply_lanes;
+        // compensated sums for outputs with a term of order >= 2 (their
+        // first-order contributions cancel), or for all outputs on request
+        ap.comp = 0;
+        for (int t = 0; t < P->nterms; ++t) {
+            unsigned ord = 0;
+            for (int d = 0; d < P->dim; ++d) ord += P->sigs[t][d];
+            if (ord >= 2) ap.comp |= 1u << P->term_output[t];
+        }
+        // the residual correction only pays off with compensated sums
+        if ((P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) || precision == DCPSE_F32_RESID) ap.comp = 0xffffffffu;
         P->tstart(DCPSE_K_APPLY_BATCHED);
         e = apply_batched_f32x(ap, P->stream);
         P->tstop(DCPSE_K_APPLY_BATCHED);
@@ -880,7 +890,8 @@ int dcpse_plan_set_apply_config(dcpse_plan_t* P, int lanes, int mode) {
     if (int rc = check_plan(P)) return rc;
     if (lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
         return fail(DCPSE_ERR_ARG, "lanes must be 0, 4, 8, 16 or 32");
-    if (mode < 0 || mode > 2) return fail(DCPSE_ERR_ARG, "mode must be 0, 1 or 2");
+    if ((mode & ~(15 | DCPSE_APPLY_COMPENSATE_ALL)) != 0 || (mode & 15) > 3)
+        return fail(DCPSE_ERR_ARG, "mode must be 0..3, optionally | DCPSE_APPLY_COMPENSATE_ALL");
     P->apply_lanes = lanes;
     P->apply_mode = mode;
     return DCPSE_OK;

@@ -141,8 +141,9 @@ struct ApplyF32 {
     const float2* f2;
     double* out;           // [nout][n]
     int* err;              // device error word (bounded waits that ran out)
-    int mode;              // 0 staged if it fits else direct, 1 direct, 2 staged
+    int mode;              // 0 staged if it fits else direct, 1 direct, 2 staged, 3 direct x8
     int lanes;             // lanes per row (0 = from the mean row length)
+    uint32_t comp;         // outputs taking the compensated FP32 sum (bit per output)
 };
 cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s);
 cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const double* w,

@@ -190,14 +190,15 @@ def test_apply_schedules(cuda, orc, name):
     refs = torch.stack([plan.apply_output_f64(o, f) for o in range(len(c["outputs"]))]).cpu().numpy()
     for lanes in (4, 8, 16, 32):
         res = {}
-        for mode in (1, 2):
+        for mode in (1, 2, 3, 1 | 16):
             plan.set_apply_config(lanes, mode)
             res[mode] = plan.apply(f, C.F32).clone()
             plan.check()
-        assert torch.equal(res[1], res[2]), lanes
-        got = res[1].cpu().numpy()
-        for o in range(len(refs)):
-            assert np.abs(got[o] - refs[o]).max() <= 1e-6 * np.abs(refs[o]).max()
+        assert torch.equal(res[1], res[2]) and torch.equal(res[1], res[3]), lanes
+        for m in (1, 1 | 16):
+            got = res[m].cpu().numpy()
+            for o in range(len(refs)):
+                assert np.abs(got[o] - refs[o]).max() <= 1e-6 * np.abs(refs[o]).max()
         for mode in (1, 2):
             plan.set_apply_config(lanes, mode)
             g = plan.apply(f, C.F32_RESID).cpu().numpy()
@@ -215,7 +216,7 @@ def test_autotune(cuda):
     f = torch.tensor(np.random.default_rng(9).standard_normal(c["pos"].shape[0]), device="cuda")
     ref = plan.apply(f, C.F32).clone()
     best = autotune.tune_apply(plan, f, reps=2, warmup=1)
-    assert len(best["sweep"]) == 6 and best["lanes"] in (8, 16, 32)
+    assert len(best["sweep"]) == 9 and best["lanes"] in (4, 8, 16)
     got = plan.apply(f, C.F32)
     assert torch.allclose(got, ref, rtol=0, atol=1e-6 * ref.abs().max().item())
 

@@ -40,6 +40,9 @@ def test_noalloc_apply_matches_plan_apply(cuda):
     rng = np.random.default_rng(3)
     for call in range(2):                    # two calls in a row share the scratch
         f = torch.tensor(rng.standard_normal(n) + call, device="cuda")
+        plan.set_apply_config(0, 0)          # the plan's default schedule: within the FP32 bar
+        ref_default = plan.apply(f, C.F32).clone()
+        plan.set_apply_config(0, 1 | 16)     # same schedule as the allocation-free call: identical
         ref = plan.apply(f, C.F32)
         out = torch.full((len(outputs), n), float("nan"), dtype=torch.float64, device="cuda")
         rc = lib.dcpse_apply_batched_f32_noalloc(n, len(outputs), _p(rowptr), _p(cols), _p(w32), nnz, _p(f),
@@ -47,6 +50,8 @@ def test_noalloc_apply_matches_plan_apply(cuda):
         assert rc == C.OK, lib.dcpse_last_error()
         torch.cuda.synchronize()
         assert torch.equal(out, ref), "call %d" % call
+        scale = ref_default.abs().amax(dim=1, keepdim=True)
+        assert bool(((out - ref_default).abs() <= 1e-6 * scale).all()), "call %d" % call
     plan.close()
 
 
