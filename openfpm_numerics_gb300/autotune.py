@@ -23,6 +23,13 @@ def tune_apply(plan, f, precision=C.F32, lanes=(4, 8, 16), modes=(1, 2, 3), reps
     for ln in lanes:
         for md in modes:
             plan.set_apply_config(ln, md)
+            try:
+                plan.apply(f, precision, out)
+            except C.DcpseError as e:
+                if e.code != C.ERR_CAPACITY:
+                    raise
+                table.append({"lanes": ln, "mode": MODES[md], "ms": None, "skipped": "tiles do not fit"})
+                continue
             for _ in range(warmup):
                 plan.apply(f, precision, out)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

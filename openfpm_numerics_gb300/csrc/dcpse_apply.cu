@@ -468,6 +468,7 @@ cudaError_t dispatch_f32(const F32Args& a, int nout, int maxk, int* err, int mod
             bool used = false;                                                        \
             cudaError_t e = launch_f32_tma<G, NO, RESID>(a, maxk, err, s, &used);     \
             if (e != cudaSuccess || used) return e;                                   \
+            if (mode == 2) return cudaErrorInvalidConfiguration; /* tiles too big */  \
         }                                                                             \
         if (mode == 3 && !RESID && G <= 8) return launch_f32_direct<G, NO, RESID, 8>(a, s); \
         return launch_f32_direct<G, NO, RESID, 4>(a, s);                              \

@@ -851,6 +851,9 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
         P->tstart(DCPSE_K_APPLY_BATCHED);
         e = apply_batched_f32x(ap, P->stream);
         P->tstop(DCPSE_K_APPLY_BATCHED);
+        if (e == cudaErrorInvalidConfiguration && (P->apply_mode & 15) == 2)
+            return fail(DCPSE_ERR_CAPACITY, "TMA-staged tiles of this plan do not fit in shared memory "
+                                            "(fewer lanes per row or another mode)");
         DCPSE_CK(e);
     } else if (precision == DCPSE_F64) {
         if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");

@@ -188,23 +188,32 @@ def test_apply_schedules(cuda, orc, name):
     plan, pos, _ = _build(c, C.STORE_TERMS_F64 | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID)
     f = torch.tensor(np.random.default_rng(8).standard_normal(c["pos"].shape[0]), device="cuda")
     refs = torch.stack([plan.apply_output_f64(o, f) for o in range(len(c["outputs"]))]).cpu().numpy()
+    staged = 0
     for lanes in (4, 8, 16, 32):
         res = {}
         for mode in (1, 2, 3, 1 | 16):
             plan.set_apply_config(lanes, mode)
-            res[mode] = plan.apply(f, C.F32).clone()
+            try:
+                res[mode] = plan.apply(f, C.F32).clone()
+            except C.DcpseError as e:  # staged tiles larger than shared memory
+                assert mode == 2 and e.code == C.ERR_CAPACITY
+                continue
             plan.check()
-        assert torch.equal(res[1], res[2]) and torch.equal(res[1], res[3]), lanes
+        assert torch.equal(res[1], res[3]), lanes
+        if 2 in res:
+            staged += 1
+            assert torch.equal(res[1], res[2]), lanes
         for m in (1, 1 | 16):
             got = res[m].cpu().numpy()
             for o in range(len(refs)):
                 assert np.abs(got[o] - refs[o]).max() <= 1e-6 * np.abs(refs[o]).max()
-        for mode in (1, 2):
+        for mode in (1, 2) if 2 in res else (1,):
             plan.set_apply_config(lanes, mode)
             g = plan.apply(f, C.F32_RESID).cpu().numpy()
             for o in range(len(refs)):
                 err = np.abs(g[o] - refs[o]).max() / np.abs(refs[o]).max()
                 assert err <= 1e-9, (lanes, mode, o, err)
+    assert staged >= 1  # the TMA-staged kernel ran for at least one lane count
     plan.set_apply_config(0, 0)
 
 
