@@ -209,7 +209,11 @@ def test_apply_schedules(cuda, orc, name):
                 assert np.abs(got[o] - refs[o]).max() <= 1e-6 * np.abs(refs[o]).max()
         for mode in (1, 2) if 2 in res else (1,):
             plan.set_apply_config(lanes, mode)
-            g = plan.apply(f, C.F32_RESID).cpu().numpy()
+            try:
+                g = plan.apply(f, C.F32_RESID).cpu().numpy()
+            except C.DcpseError as e:  # the residual streams make the tiles larger
+                assert mode == 2 and e.code == C.ERR_CAPACITY
+                continue
             for o in range(len(refs)):
                 err = np.abs(g[o] - refs[o]).max() / np.abs(refs[o]).max()
                 assert err <= 1e-9, (lanes, mode, o, err)
