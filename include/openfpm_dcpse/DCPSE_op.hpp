@@ -1,0 +1,386 @@
+// DCPSE_op.hpp -- drop-in for openfpm_numerics' DC-PSE operator classes
+// (src/DCPSE/DCPSE_op/DCPSE_op.hpp): Derivative_x/y/z, Derivative_xx/yy/zz,
+// Derivative_xy/yz/xz, the third and fourth order ones, Derivative_G,
+// Laplacian and Gradient, with the same constructors
+//     Op<VerletList_type> op(parts, verletList, ord, rCut [, opt])
+// and the same use in assignments
+//     getV<1>(parts) = Lap(getV<0>(parts));
+//     getV<1>(parts) = 2 * Dx(getV<0>(parts)) + Dy(getV<0>(parts));
+// Each operator owns one GB300 plan holding all of its reference Dcpse terms
+// (a Laplacian's dim terms 2e_i share one neighbour list and one moment
+// matrix); an assignment evaluates every operator node on the GPU in FP64 in
+// the reference's order (VECT_DCPSE :65-67, VECT_DCPSE_V :144-153,
+// VECT_DCPSE_V_SUM :388-399) and combines the nodes on the host.
+// Only linear combinations of operator nodes are supported on the right-hand
+// side (the reference's general expression engine is not part of this path).
+#pragma once
+
+#include <array>
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "Dcpse.hpp"
+
+namespace openfpm_dcpse {
+
+const double dcpse_oversampling_factor = 1.9;  // DCPSE_op.hpp:20
+const double rcut_verlet = 3.1;                // DCPSE_op.hpp:21
+
+// ------------------------------------------------------------ expressions --
+template <unsigned int prp, typename vector_type>
+struct PropRef;
+
+// One operator applied to one property: result[c][p] for c < ncomp.
+struct Node {
+    std::function<void(std::vector<std::vector<double>>&)> eval;
+    int ncomp = 1;
+    double coef = 1.0;
+};
+
+struct Expr {
+    std::vector<Node> nodes;
+};
+
+inline Expr operator*(double c, Expr e) {
+    for (auto& n : e.nodes) n.coef *= c;
+    return e;
+}
+inline Expr operator*(Expr e, double c) { return c * e; }
+inline Expr operator+(Expr a, const Expr& b) {
+    a.nodes.insert(a.nodes.end(), b.nodes.begin(), b.nodes.end());
+    return a;
+}
+inline Expr operator-(Expr a, Expr b) { return a + (-1.0) * b; }
+
+namespace detail {
+template <typename V>
+auto prop_component(V& v, int c, std::true_type) -> decltype(v[c])& {
+    return v[c];
+}
+template <typename V>
+V& prop_component(V& v, int, std::false_type) {
+    return v;
+}
+template <typename V, typename = void>
+struct is_indexable : std::false_type {};
+template <typename V>
+struct is_indexable<V, std::void_t<decltype(std::declval<V&>()[0])>> : std::true_type {};
+}  // namespace detail
+
+// getV<prp>(parts): a property of a particle set, usable as an operand and
+// as the target of an assignment.
+template <unsigned int prp, typename vector_type>
+struct PropRef {
+    vector_type& v;
+    typedef vector_type vtype;
+    vector_type& getVector() const { return v; }
+
+    std::vector<double> values() const {
+        std::vector<double> f(v.size_local());
+        for (std::size_t p = 0; p < f.size(); ++p) f[p] = (double)v.template getProp<prp>(p);
+        return f;
+    }
+
+    // getV<prp>(parts) = expr: evaluate every node and combine
+    PropRef& operator=(const Expr& e) {
+        const std::size_t n = v.size_local();
+        int ncomp = e.nodes.empty() ? 1 : e.nodes[0].ncomp;
+        std::vector<std::vector<double>> acc(ncomp, std::vector<double>(n, 0.0)), tmp;
+        bool first = true;
+        for (const auto& node : e.nodes) {
+            if (node.ncomp != ncomp) throw std::invalid_argument("mixing scalar and vector operator results");
+            node.eval(tmp);
+            for (int c = 0; c < ncomp; ++c)
+                for (std::size_t p = 0; p < n; ++p)
+                    acc[c][p] = (first && node.coef == 1.0) ? tmp[c][p] : acc[c][p] + node.coef * tmp[c][p];
+            first = false;
+        }
+        typedef typename std::remove_reference<decltype(v.template getProp<prp>(0))>::type PT;
+        for (std::size_t p = 0; p < n; ++p)
+            for (int c = 0; c < ncomp; ++c) {
+                auto& slot = detail::prop_component(v.template getProp<prp>(p), c, detail::is_indexable<PT>{});
+                slot = acc[c][p];
+            }
+        return *this;
+    }
+};
+
+template <unsigned int prp, typename vector_type>
+PropRef<prp, vector_type> getV(vector_type& v) {
+    return PropRef<prp, vector_type>{v};
+}
+
+// Verlet list of a particle set built on the GPU: every q != p with
+// |x_p - x_q|^2 < rCut^2, ascending q (the role of
+// vector_dist::getVerlet<VL_NON_SYMMETRIC|VL_SKIP_REF_PART>(rCut)).
+template <typename particles_type>
+VerletList getVerlet(particles_type& parts, double rCut) {
+    const int dim = particles_type::dims;
+    std::vector<unsigned> sig(dim, 0);
+    sig[0] = 1;
+    int terms = 1;
+    dcpse_plan_t* plan = nullptr;
+    detail::check(dcpse_plan_create(&plan, dim, 1, &terms, sig.data(), 2, 0.9));
+    std::unique_ptr<dcpse_plan_t, int (*)(dcpse_plan_t*)> guard(plan, dcpse_plan_destroy);
+    const std::size_t n = parts.size_local();
+    std::vector<double> pos(n * dim);
+    for (std::size_t p = 0; p < n; ++p)
+        for (int d = 0; d < dim; ++d) pos[p * dim + d] = (double)parts.getPos(p)[d];
+    detail::DevBuf dpos;
+    dpos.upload(pos.data(), std::max<std::size_t>(pos.size(), 1) * sizeof(double));
+    detail::check(dcpse_build_neighbors(plan, (const double*)dpos.get(), (int64_t)n, rCut, nullptr));
+    int64_t nn = 0, nnz = 0;
+    detail::check(dcpse_plan_info(plan, &nn, &nnz, nullptr, nullptr, nullptr));
+    const int64_t* drp = nullptr;
+    const int32_t* dcl = nullptr;
+    detail::check(dcpse_neighbors_ptr(plan, &drp, &dcl));
+    VerletList vl;
+    vl.rowptr.resize(n + 1);
+    vl.cols.resize((std::size_t)nnz);
+    detail::check(dcpse_copy(vl.rowptr.data(), drp, (n + 1) * sizeof(int64_t)));
+    if (nnz > 0) detail::check(dcpse_copy(vl.cols.data(), dcl, (std::size_t)nnz * sizeof(int32_t)));
+    return vl;
+}
+
+// --------------------------------------------------------------- operators --
+// outputs: list of outputs, each a list of signatures summed into it.
+template <typename VerletList_type>
+class DcpseOperator {
+public:
+    template <typename particles_type>
+    DcpseOperator(particles_type& parts, VerletList_type& verletList, unsigned int ord,
+                  typename particles_type::stype rCut, std::vector<std::vector<std::vector<unsigned>>> outputs,
+                  support_options opt, double h_over_eps = 0.9)
+        : vl_(verletList), outputs_(std::move(outputs)), ord_(ord), hoe_(h_over_eps), dim_(particles_type::dims) {
+        (void)rCut;
+        parts.ghost_get_subset();
+        build(parts, opt != support_options::LOAD);
+    }
+
+    // initializeUpdate of every Dcpse term (DCPSE_op.hpp:779-785)
+    template <typename particles_type>
+    void update(particles_type& parts) {
+        build(parts, true);
+    }
+
+    template <typename particles_type>
+    void deallocate(particles_type&) {
+        plan_.reset();
+    }
+
+    // operand: getV<i>(parts)
+    template <unsigned int prp, typename vector_type>
+    Expr operator()(PropRef<prp, vector_type> arg) {
+        Node nd;
+        nd.ncomp = (int)outputs_.size();
+        detail::PlanHost* P = plan_.get();
+        const std::size_t outs = outputs_.size();
+        nd.eval = [P, arg, outs](std::vector<std::vector<double>>& out) {
+            std::vector<double> f = arg.values();
+            out.assign(outs, std::vector<double>(f.size()));
+            for (std::size_t o = 0; o < outs; ++o) P->apply_output((int)o, f.data(), out[o].data());
+        };
+        Expr e;
+        e.nodes.push_back(nd);
+        return e;
+    }
+
+    // FP32 batched apply of every output of this operator (one pass)
+    template <unsigned int prp, typename vector_type>
+    std::vector<std::vector<double>> apply_f32(PropRef<prp, vector_type> arg) {
+        std::vector<double> f = arg.values();
+        std::vector<double> flat(outputs_.size() * f.size());
+        detail::check(dcpse_apply_batched_host(plan_->plan(), f.data(), flat.data(), DCPSE_F32));
+        std::vector<std::vector<double>> out(outputs_.size());
+        for (std::size_t o = 0; o < outputs_.size(); ++o)
+            out[o].assign(flat.begin() + o * f.size(), flat.begin() + (o + 1) * f.size());
+        return out;
+    }
+
+    template <typename particles_type>
+    void save(particles_type&, const std::string& file) {
+        save_impl(file);
+    }
+    template <typename particles_type>
+    void load(particles_type&, const std::string& file) {
+        load_impl(file);
+    }
+
+    // adds the kernels (all terms) of particle k to property prp of its neighbours
+    template <unsigned int prp, typename particles_type>
+    void DrawKernel(particles_type& particles, int k) {
+        for (int t = 0; t < plan_->n_terms(); ++t) {
+            const auto& K = plan_->kernels(t);
+            for (int64_t j = plan_->rowptr()[k]; j < plan_->rowptr()[k + 1]; ++j)
+                particles.template getProp<prp>((std::size_t)plan_->cols()[j]) += K[j];
+        }
+    }
+
+    dcpse_plan_t* plan() const { return plan_->plan(); }
+
+private:
+    template <typename particles_type>
+    void build(particles_type& parts, bool assemble) {
+        plan_.reset(new detail::PlanHost(dim_, outputs_, ord_, hoe_));
+        plan_->set_particles(parts, vl_);
+        if (!assemble) return;
+        int64_t nbad = plan_->assemble(DCPSE_STORE_TERMS_F64 | DCPSE_STORE_OUT_F32);
+        detail::throw_too_few(plan_->last_fail_code(), nbad);
+    }
+
+    void save_impl(const std::string& file) {
+        std::ofstream dump(file + "_0", std::ios::out | std::ios::binary);
+        if (!dump.is_open()) {
+            std::cerr << __FILE__ << ":" << __LINE__ << " Unable to write " << file << "_0" << std::endl;
+            return;
+        }
+        const char magic[8] = {'D', 'C', 'P', 'S', 'E', 'O', 'P', '1'};
+        uint64_t hdr[3] = {(uint64_t)plan_->n(), (uint64_t)plan_->nnz(), (uint64_t)plan_->n_terms()};
+        dump.write(magic, 8);
+        dump.write((const char*)hdr, sizeof hdr);
+        const auto& eps = plan_->eps();
+        dump.write((const char*)eps.data(), eps.size() * sizeof(double));
+        for (int t = 0; t < plan_->n_terms(); ++t) {
+            dump.write((const char*)plan_->eps_inv_pow(t).data(), plan_->n() * sizeof(double));
+            dump.write((const char*)plan_->kernels(t).data(), plan_->nnz() * sizeof(double));
+        }
+    }
+    void load_impl(const std::string& file) {
+        std::ifstream in(file + "_0", std::ios::in | std::ios::binary);
+        if (!in.is_open()) {
+            std::cerr << __FILE__ << ":" << __LINE__ << " error, opening file: " << file << std::endl;
+            return;
+        }
+        char magic[8];
+        uint64_t hdr[3];
+        in.read(magic, 8);
+        in.read((char*)hdr, sizeof hdr);
+        if (!in || std::memcmp(magic, "DCPSEOP1", 8) != 0 || (int64_t)hdr[0] != plan_->n() ||
+            (int64_t)hdr[1] != plan_->nnz() || (int)hdr[2] != plan_->n_terms()) {
+            std::cerr << __FILE__ << ":" << __LINE__ << " error, " << file << " does not match this operator"
+                      << std::endl;
+            return;
+        }
+        std::vector<double> eps(hdr[0]);
+        in.read((char*)eps.data(), eps.size() * sizeof(double));
+        std::vector<std::vector<double>> eip(hdr[2], std::vector<double>(hdr[0])), K(hdr[2], std::vector<double>(hdr[1]));
+        for (uint64_t t = 0; t < hdr[2]; ++t) {
+            in.read((char*)eip[t].data(), hdr[0] * sizeof(double));
+            in.read((char*)K[t].data(), hdr[1] * sizeof(double));
+        }
+        if (!in) {
+            std::cerr << __FILE__ << ":" << __LINE__ << " error, truncated file " << file << std::endl;
+            return;
+        }
+        for (uint64_t t = 0; t < hdr[2]; ++t) plan_->install((int)t, K[t], eps, eip[t]);
+    }
+
+    VerletList_type& vl_;
+    std::vector<std::vector<std::vector<unsigned>>> outputs_;
+    unsigned ord_;
+    double hoe_;
+    int dim_;
+    std::unique_ptr<detail::PlanHost> plan_;
+};
+
+namespace detail {
+inline std::vector<unsigned> unit(int dim, int axis, unsigned power = 1) {
+    std::vector<unsigned> s(dim, 0);
+    s[axis] = power;
+    return s;
+}
+inline std::vector<unsigned> mixed(int dim, std::initializer_list<std::pair<int, unsigned>> l) {
+    std::vector<unsigned> s(dim, 0);
+    for (auto& p : l) s[p.first] = p.second;
+    return s;
+}
+}  // namespace detail
+
+#define OPENFPM_DCPSE_SINGLE_OP(NAME, SIGEXPR)                                                                  \
+    template <typename VerletList_type>                                                                        \
+    class NAME : public DcpseOperator<VerletList_type> {                                                       \
+    public:                                                                                                    \
+        template <typename particles_type>                                                                     \
+        NAME(particles_type& parts, VerletList_type& verletList, unsigned int ord,                             \
+             typename particles_type::stype rCut, support_options opt = support_options::RADIUS)               \
+            : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut,                                     \
+                                             {{[](int dim) { return SIGEXPR; }(particles_type::dims)}}, opt) {} \
+    };
+
+// Derivative_x_T ... (DCPSE_op.hpp:649-3385)
+OPENFPM_DCPSE_SINGLE_OP(Derivative_x, detail::unit(dim, 0))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_y, detail::unit(dim, 1))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_z, detail::unit(dim, 2))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_xx, detail::unit(dim, 0, 2))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_yy, detail::unit(dim, 1, 2))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_zz, detail::unit(dim, 2, 2))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_xy, detail::mixed(dim, {{0, 1}, {1, 1}}))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_yz, detail::mixed(dim, {{1, 1}, {2, 1}}))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_xz, detail::mixed(dim, {{0, 1}, {2, 1}}))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_xxx, detail::unit(dim, 0, 3))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_yyy, detail::unit(dim, 1, 3))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_xxy, detail::mixed(dim, {{0, 2}, {1, 1}}))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_yyx, detail::mixed(dim, {{0, 1}, {1, 2}}))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_xxxx, detail::unit(dim, 0, 4))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_yyyy, detail::unit(dim, 1, 4))
+OPENFPM_DCPSE_SINGLE_OP(Derivative_xxyy, detail::mixed(dim, {{0, 2}, {1, 2}}))
+#undef OPENFPM_DCPSE_SINGLE_OP
+
+// Derivative_G_T (DCPSE_op.hpp:3387-3482): arbitrary signature p
+template <typename VerletList_type>
+class Derivative_G : public DcpseOperator<VerletList_type> {
+public:
+    template <typename particles_type, typename Sig>
+    Derivative_G(particles_type& parts, VerletList_type& verletList, unsigned int ord,
+                 typename particles_type::stype rCut, const Sig& p, support_options opt = support_options::RADIUS)
+        : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut,
+                                         {{detail::sig_vector(p, particles_type::dims)}}, opt) {}
+};
+
+// Laplacian_T (DCPSE_op.hpp:1350-1500): one output, sum of dim terms 2e_i
+template <typename VerletList_type>
+class Laplacian : public DcpseOperator<VerletList_type> {
+    static std::vector<std::vector<std::vector<unsigned>>> outs(int dim) {
+        std::vector<std::vector<unsigned>> t;
+        for (int i = 0; i < dim; ++i) t.push_back(detail::unit(dim, i, 2));
+        return {t};
+    }
+
+public:
+    template <typename particles_type>
+    Laplacian(particles_type& parts, VerletList_type& verletList, unsigned int ord, typename particles_type::stype rCut,
+              support_options opt = support_options::RADIUS)
+        : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut, outs(particles_type::dims), opt) {}
+};
+
+// Gradient_T (DCPSE_op.hpp:1081-1224): dim outputs e_i (vector result)
+template <typename VerletList_type>
+class Gradient : public DcpseOperator<VerletList_type> {
+    static std::vector<std::vector<std::vector<unsigned>>> outs(int dim) {
+        std::vector<std::vector<std::vector<unsigned>>> o;
+        for (int i = 0; i < dim; ++i) o.push_back({detail::unit(dim, i)});
+        return o;
+    }
+
+public:
+    template <typename particles_type>
+    Gradient(particles_type& parts, VerletList_type& verletList, unsigned int ord, typename particles_type::stype rCut,
+             support_options opt = support_options::RADIUS)
+        : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut, outs(particles_type::dims), opt) {}
+};
+
+// GPU aliases of the reference (DCPSE_op.hpp:3510-3530) name the same classes
+template <typename VL> using Derivative_x_gpu = Derivative_x<VL>;
+template <typename VL> using Derivative_y_gpu = Derivative_y<VL>;
+template <typename VL> using Derivative_z_gpu = Derivative_z<VL>;
+template <typename VL> using Derivative_xx_gpu = Derivative_xx<VL>;
+template <typename VL> using Derivative_yy_gpu = Derivative_yy<VL>;
+template <typename VL> using Derivative_zz_gpu = Derivative_zz<VL>;
+template <typename VL> using Derivative_xy_gpu = Derivative_xy<VL>;
+template <typename VL> using Laplacian_gpu = Laplacian<VL>;
+template <typename VL> using Gradient_gpu = Gradient<VL>;
+template <typename VL> using Derivative_G_gpu = Derivative_G<VL>;
+
+}  // namespace openfpm_dcpse

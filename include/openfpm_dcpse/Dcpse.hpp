@@ -1,0 +1,428 @@
+// Dcpse.hpp -- drop-in for openfpm_numerics' Dcpse<dim, VerletList_type,
+// vector_type> (src/DCPSE/Dcpse.hpp:43-826) on the GB300 C-ABI.
+//
+// Same constructor arguments, the same bulk and per-key
+// computeDifferentialOperator, the same accessors (getNumNN, getCoeffNN,
+// getIndexNN, getSign, getEpsilonInvPrefactor), initializeUpdate, save/load,
+// checkMomenta and DrawKernel.  Assembly and application run on the GPU
+// through include/openfpm_dcpse/dcpse_capi.h; the FP64 results are those of
+// the reference algorithm in its operation order.  Host code here needs no
+// CUDA headers: device memory goes through dcpse_device_alloc / dcpse_copy.
+//
+// The particle and Verlet-list types are template parameters, as in the
+// reference; only these members are used:
+//   particles.size_local(), particles.getPos(p)[d], particles.getProp<i>(p)
+//   verletList.getNNPart(p), verletList.get(p, j)
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "dcpse_capi.h"
+#include "particles.hpp"
+
+namespace openfpm_dcpse {
+
+// src/DCPSE/SupportBuilder.hpp:13-19
+enum support_options { RADIUS, LOAD, ADAPTIVE, AT_LEAST_N_PARTICLES };
+
+namespace detail {
+
+inline void check(int rc, bool allow_particles = false) {
+    if (rc == DCPSE_OK || (allow_particles && rc == DCPSE_ERR_PARTICLES)) return;
+    throw std::runtime_error(std::string("DC-PSE: ") + dcpse_last_error());
+}
+
+// Device buffer owned by host code.
+class DevBuf {
+public:
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void* get() const { return p_; }
+    void ensure(std::size_t bytes) {
+        if (bytes <= bytes_) return;
+        release();
+        check(dcpse_device_alloc(&p_, bytes));
+        bytes_ = bytes;
+    }
+    void upload(const void* h, std::size_t bytes) {
+        ensure(bytes);
+        check(dcpse_copy(p_, h, bytes));
+    }
+    void download(void* h, std::size_t bytes) const { check(dcpse_copy(h, p_, bytes)); }
+    void release() {
+        if (p_) dcpse_device_free(p_);
+        p_ = nullptr;
+        bytes_ = 0;
+    }
+
+private:
+    void* p_ = nullptr;
+    std::size_t bytes_ = 0;
+};
+
+// A plan plus the host <-> device staging of positions, lists and fields.
+class PlanHost {
+public:
+    // outputs[o] = list of signatures (dim entries each) summed into output o
+    PlanHost(int dim, const std::vector<std::vector<std::vector<unsigned>>>& outputs, unsigned order,
+             double h_over_eps)
+        : dim_(dim) {
+        std::vector<int> terms;
+        std::vector<unsigned> sigs;
+        for (const auto& o : outputs) {
+            terms.push_back((int)o.size());
+            for (const auto& s : o) {
+                unsigned ord = 0;
+                for (int d = 0; d < dim; ++d) {
+                    sigs.push_back(s[d]);
+                    ord += s[d];
+                }
+                term_order_.push_back(ord);
+            }
+        }
+        check(dcpse_plan_create(&plan_, dim, (int)outputs.size(), terms.data(), sigs.data(), order, h_over_eps));
+        nout_ = (int)outputs.size();
+    }
+    PlanHost(const PlanHost&) = delete;
+    PlanHost& operator=(const PlanHost&) = delete;
+    ~PlanHost() {
+        if (plan_) dcpse_plan_destroy(plan_);
+    }
+
+    dcpse_plan_t* plan() const { return plan_; }
+    int64_t n() const { return n_; }
+    int64_t nnz() const { return (int64_t)cols_.size(); }
+    const std::vector<int64_t>& rowptr() const { return rowptr_; }
+    const std::vector<int32_t>& cols() const { return cols_; }
+    unsigned term_order(int t) const { return term_order_[t]; }
+    int n_terms() const { return (int)term_order_.size(); }
+
+    template <typename Parts, typename VL>
+    void set_particles(Parts& parts, VL& vl) {
+        n_ = (int64_t)parts.size_local();
+        std::vector<double> pos((std::size_t)n_ * dim_);
+        for (int64_t p = 0; p < n_; ++p)
+            for (int d = 0; d < dim_; ++d) pos[(std::size_t)p * dim_ + d] = (double)parts.getPos(p)[d];
+        pos_.upload(pos.data(), pos.size() * sizeof(double));
+        rowptr_.assign((std::size_t)n_ + 1, 0);
+        cols_.clear();
+        for (int64_t p = 0; p < n_; ++p) {
+            std::size_t k = vl.getNNPart((std::size_t)p);
+            for (std::size_t j = 0; j < k; ++j) cols_.push_back((int32_t)vl.get((std::size_t)p, j));
+            rowptr_[(std::size_t)p + 1] = (int64_t)cols_.size();
+        }
+        DevBuf drp, dcl;
+        drp.upload(rowptr_.data(), rowptr_.size() * sizeof(int64_t));
+        dcl.upload(cols_.data(), std::max<std::size_t>(cols_.size(), 1) * sizeof(int32_t));
+        check(dcpse_set_neighbors(plan_, n_, (int64_t)cols_.size(), (const int64_t*)drp.get(),
+                                  (const int32_t*)dcl.get()));
+        cache_valid_ = false;
+    }
+
+    // returns the number of particles that could not be assembled
+    int64_t assemble(int flags) {
+        int rc = dcpse_assemble(plan_, (const double*)pos_.get(), nullptr, flags);
+        check(rc, true);
+        cache_valid_ = false;
+        if (rc == DCPSE_ERR_PARTICLES) {
+            int64_t nb = 0, first = -1;
+            int code = 0;
+            check(dcpse_particle_status(plan_, &nb, &first, &code));
+            last_fail_code_ = code;
+            return nb;
+        }
+        last_fail_code_ = 0;
+        return 0;
+    }
+    int last_fail_code() const { return last_fail_code_; }
+
+    // FP64 output o of the field f (host arrays of n values)
+    void apply_output(int o, const double* f, double* out) {
+        fd_.upload(f, (std::size_t)n_ * sizeof(double));
+        od_.ensure((std::size_t)std::max<int64_t>(n_, 1) * sizeof(double));
+        check(dcpse_apply_output_f64(plan_, o, (const double*)fd_.get(), (double*)od_.get()));
+        od_.download(out, (std::size_t)n_ * sizeof(double));
+    }
+    void apply_term(int t, const double* f, double* out) {
+        fd_.upload(f, (std::size_t)n_ * sizeof(double));
+        od_.ensure((std::size_t)std::max<int64_t>(n_, 1) * sizeof(double));
+        check(dcpse_apply_term_f64(plan_, t, (const double*)fd_.get(), (double*)od_.get()));
+        od_.download(out, (std::size_t)n_ * sizeof(double));
+    }
+
+    // host copies of the kernels of every term, eps and eps^-|alpha|
+    void fetch() {
+        if (cache_valid_) return;
+        const int T = n_terms();
+        K_.assign(T, {});
+        eip_.assign(T, {});
+        eps_.assign((std::size_t)n_, 0.0);
+        const double* de = nullptr;
+        const int32_t* ds = nullptr;
+        check(dcpse_eps_ptr(plan_, &de, &ds));
+        if (n_ > 0) check(dcpse_copy(eps_.data(), de, (std::size_t)n_ * sizeof(double)));
+        for (int t = 0; t < T; ++t) {
+            const double *dk = nullptr, *dip = nullptr;
+            check(dcpse_term_kernels_ptr(plan_, t, &dk, &dip));
+            K_[t].assign((std::size_t)nnz(), 0.0);
+            eip_[t].assign((std::size_t)n_, 0.0);
+            if (nnz() > 0) check(dcpse_copy(K_[t].data(), dk, (std::size_t)nnz() * sizeof(double)));
+            if (n_ > 0) check(dcpse_copy(eip_[t].data(), dip, (std::size_t)n_ * sizeof(double)));
+        }
+        cache_valid_ = true;
+    }
+    const std::vector<double>& kernels(int t) {
+        fetch();
+        return K_[t];
+    }
+    const std::vector<double>& eps_inv_pow(int t) {
+        fetch();
+        return eip_[t];
+    }
+    const std::vector<double>& eps() {
+        fetch();
+        return eps_;
+    }
+    void install(int t, const std::vector<double>& K, const std::vector<double>& eps, const std::vector<double>& eip) {
+        DevBuf dk, de, di;
+        dk.upload(K.data(), std::max<std::size_t>(K.size(), 1) * sizeof(double));
+        de.upload(eps.data(), std::max<std::size_t>(eps.size(), 1) * sizeof(double));
+        di.upload(eip.data(), std::max<std::size_t>(eip.size(), 1) * sizeof(double));
+        check(dcpse_set_term_kernels(plan_, t, (const double*)dk.get(), (const double*)de.get(),
+                                     (const double*)di.get()));
+        cache_valid_ = false;
+    }
+    std::vector<std::vector<unsigned>> basis(int t) const {
+        unsigned e[64 * 3];
+        int nb = 0;
+        check(dcpse_term_basis(plan_, t, e, 64, &nb));
+        std::vector<std::vector<unsigned>> out(nb, std::vector<unsigned>(dim_));
+        for (int i = 0; i < nb; ++i)
+            for (int d = 0; d < dim_; ++d) out[i][d] = e[i * dim_ + d];
+        return out;
+    }
+
+private:
+    int dim_ = 0, nout_ = 0;
+    dcpse_plan_t* plan_ = nullptr;
+    int64_t n_ = 0;
+    std::vector<unsigned> term_order_;
+    std::vector<int64_t> rowptr_;
+    std::vector<int32_t> cols_;
+    DevBuf pos_, fd_, od_;
+    bool cache_valid_ = false;
+    std::vector<std::vector<double>> K_, eip_;
+    std::vector<double> eps_;
+    int last_fail_code_ = 0;
+};
+
+template <typename Sig>
+std::vector<unsigned> sig_vector(const Sig& s, int dim) {
+    std::vector<unsigned> v(dim);
+    for (int d = 0; d < dim; ++d) v[d] = (unsigned)s.get(d);
+    return v;
+}
+
+inline void throw_too_few(int code, int64_t nbad) {
+    if (nbad == 0) return;
+    if (code == DCPSE_PART_TOO_FEW)
+        throw std::length_error("Not enough neighbour points passed for Vandermonde matrix construction!");
+    throw std::runtime_error("DC-PSE assembly failed for " + std::to_string(nbad) + " particle(s)");
+}
+
+}  // namespace detail
+
+template <unsigned int dim, typename VerletList_type, typename vector_type, typename vector_type2 = vector_type>
+class Dcpse {
+public:
+    typedef typename vector_type::stype T;
+    typedef vector_type vtype;
+
+    // c = HOverEpsilon: eps = <h> / c, <h> the mean L1 spacing of the support
+    // (Dcpse.hpp:80; read at construction and at update)
+    T HOverEpsilon = 0.9;
+
+    template <typename Sig>
+    Dcpse(vector_type& particles, VerletList_type& verletList, const Sig& differentialSignature,
+          unsigned int convergenceOrder, T rCut, support_options opt = support_options::RADIUS)
+        : verletList_(verletList),
+          sig_(detail::sig_vector(differentialSignature, dim)),
+          convergenceOrder_(convergenceOrder),
+          rCut_(rCut),
+          opt_(opt) {
+        differentialOrder_ = 0;
+        for (unsigned s : sig_) differentialOrder_ += s;
+        particles.ghost_get_subset();
+        plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder, (double)HOverEpsilon));
+        plan_->set_particles(particles, verletList_);
+        if (opt == support_options::LOAD) return;  // empty operator: load() or update later (Dcpse.hpp:703-707)
+        assemble();
+    }
+
+    // Bulk apply: Df at every particle from property fValuePos into
+    // DfValuePos (Dcpse.hpp:467-499).
+    template <unsigned int fValuePos, unsigned int DfValuePos>
+    void computeDifferentialOperator(vector_type& particles) {
+        const int64_t n = plan_->n();
+        std::vector<double> f((std::size_t)n), out((std::size_t)n);
+        for (int64_t p = 0; p < n; ++p) f[(std::size_t)p] = (double)particles.template getProp<fValuePos>(p);
+        plan_->apply_term(0, f.data(), out.data());
+        for (int64_t p = 0; p < n; ++p) particles.template getProp<DfValuePos>(p) = (T)out[(std::size_t)p];
+    }
+
+    // Per-key form (Dcpse.hpp:560-603): o1.value(key) gives the field.
+    template <typename op_type>
+    T computeDifferentialOperator(const vect_dist_key_dx& p, op_type& o1) {
+        const auto& K = plan_->kernels(0);
+        const auto& eip = plan_->eps_inv_pow(0);
+        const T sign = (differentialOrder_ % 2 == 0) ? -1 : 1;
+        const T fxp = sign * o1.value(p);
+        T D = 0;
+        const int64_t b = plan_->rowptr()[p.getKey()];
+        const std::size_t k = verletList_.getNNPart(p.getKey());
+        for (std::size_t j = 0; j < k; ++j) {
+            const T fxq = o1.value(vect_dist_key_dx(verletList_.get(p.getKey(), j)));
+            D = D + (fxq + fxp) * K[(std::size_t)(b + (int64_t)j)];
+        }
+        return D * eip[p.getKey()];
+    }
+
+    // accessors (Dcpse.hpp:507-550)
+    int getNumNN(const vect_dist_key_dx& p) { return (int)verletList_.getNNPart(p.getKey()); }
+    T getCoeffNN(const vect_dist_key_dx& p, int j) {
+        return plan_->kernels(0)[(std::size_t)(plan_->rowptr()[p.getKey()] + j)];
+    }
+    std::size_t getIndexNN(const vect_dist_key_dx& p, int q) { return verletList_.get(p.getKey(), q); }
+    T getSign() { return (differentialOrder_ % 2 == 0 && differentialOrder_ != 0) ? -1 : 1; }
+    T getEpsilonInvPrefactor(const vect_dist_key_dx& p) { return plan_->eps_inv_pow(0)[p.getKey()]; }
+
+    // after particles moved (and the Verlet list was updated): Dcpse.hpp:675-687
+    void initializeUpdate(vector_type& particles) {
+        plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder_, (double)HOverEpsilon));
+        plan_->set_particles(particles, verletList_);
+        assemble();
+    }
+
+    // Own versioned binary format, same content and order as the reference's
+    // Packer stream (localEps, localEpsInvPow, calcKernels, kerOffsets;
+    // Dcpse.hpp:302-331), written to file + "_" + rank (rank 0 here).
+    void save(const std::string& file) {
+        std::ofstream dump(file + "_0", std::ios::out | std::ios::binary);
+        if (!dump.is_open()) {
+            std::cerr << __FILE__ << ":" << __LINE__ << " Unable to write " << file << "_0" << std::endl;
+            return;
+        }
+        const auto& eps = plan_->eps();
+        const auto& eip = plan_->eps_inv_pow(0);
+        const auto& K = plan_->kernels(0);
+        const char magic[8] = {'D', 'C', 'P', 'S', 'E', 'G', 'B', '1'};
+        uint64_t hdr[3] = {(uint64_t)plan_->n(), (uint64_t)K.size(), (uint64_t)dim};
+        dump.write(magic, 8);
+        dump.write((const char*)hdr, sizeof hdr);
+        dump.write((const char*)eps.data(), eps.size() * sizeof(double));
+        dump.write((const char*)eip.data(), eip.size() * sizeof(double));
+        dump.write((const char*)K.data(), K.size() * sizeof(double));
+        std::vector<uint64_t> off(plan_->rowptr().begin(), plan_->rowptr().end() - (plan_->n() > 0 ? 1 : 0));
+        dump.write((const char*)off.data(), off.size() * sizeof(uint64_t));
+    }
+
+    // Dcpse.hpp:337-379; the neighbour list of the constructor must match.
+    void load(const std::string& file) {
+        std::ifstream in(file + "_0", std::ios::in | std::ios::binary);
+        if (!in.is_open()) {
+            std::cerr << __FILE__ << ":" << __LINE__ << " error, opening file: " << file << std::endl;
+            return;
+        }
+        char magic[8];
+        uint64_t hdr[3];
+        in.read(magic, 8);
+        in.read((char*)hdr, sizeof hdr);
+        if (!in || std::memcmp(magic, "DCPSEGB1", 8) != 0 || (int64_t)hdr[0] != plan_->n() ||
+            (int64_t)hdr[1] != plan_->nnz() || hdr[2] != dim) {
+            std::cerr << __FILE__ << ":" << __LINE__ << " error, " << file << " does not match this operator"
+                      << std::endl;
+            return;
+        }
+        std::vector<double> eps(hdr[0]), eip(hdr[0]), K(hdr[1]);
+        in.read((char*)eps.data(), eps.size() * sizeof(double));
+        in.read((char*)eip.data(), eip.size() * sizeof(double));
+        in.read((char*)K.data(), K.size() * sizeof(double));
+        if (!in) {
+            std::cerr << __FILE__ << ":" << __LINE__ << " error, truncated file " << file << std::endl;
+            return;
+        }
+        plan_->install(0, K, eps, eip);
+    }
+
+    // min / max over particles of each moment sum_q K_pq m_j(x_pq / eps_p)
+    // (Dcpse.hpp:381-457)
+    void checkMomenta(vector_type& particles) {
+        const auto B = plan_->basis(0);
+        const auto& K = plan_->kernels(0);
+        const auto& eps = plan_->eps();
+        std::vector<double> mn(B.size(), 3000000000.0), mx(B.size(), -3000000000.0);
+        for (int64_t p = 0; p < plan_->n(); ++p) {
+            std::vector<double> acc(B.size(), 0.0);
+            const int64_t b = plan_->rowptr()[p];
+            for (int64_t j = b; j < plan_->rowptr()[p + 1]; ++j) {
+                const std::size_t q = (std::size_t)plan_->cols()[j];
+                for (std::size_t i = 0; i < B.size(); ++i) {
+                    double m = 1.0;
+                    for (int d = 0; d < (int)dim; ++d)
+                        m *= std::pow(((double)particles.getPos(p)[d] - (double)particles.getPos(q)[d]) / eps[p],
+                                      (double)B[i][d]);
+                    acc[i] += m * K[j];
+                }
+            }
+            for (std::size_t i = 0; i < B.size(); ++i) {
+                mn[i] = std::min(mn[i], acc[i]);
+                mx[i] = std::max(mx[i], acc[i]);
+            }
+        }
+        for (std::size_t i = 0; i < B.size(); ++i) {
+            std::cout << "MOMENTA: 1 :";
+            for (int d = 0; d < (int)dim; ++d) std::cout << " " << B[i][d];
+            std::cout << " Min: " << mn[i] << "  Max: " << mx[i] << std::endl;
+        }
+    }
+
+    // adds the kernel of particle p to property prp of its neighbours (Dcpse.hpp:151-163)
+    template <unsigned int prp>
+    void DrawKernel(vector_type& particles, int p) {
+        const auto& K = plan_->kernels(0);
+        const int64_t b = plan_->rowptr()[p];
+        for (int64_t j = b; j < plan_->rowptr()[p + 1]; ++j)
+            particles.template getProp<prp>((std::size_t)plan_->cols()[j]) += K[j];
+    }
+
+    dcpse_plan_t* plan() const { return plan_->plan(); }
+
+private:
+    void assemble() {
+        int64_t nbad = plan_->assemble(DCPSE_STORE_TERMS_F64);
+        detail::throw_too_few(plan_->last_fail_code(), nbad);
+    }
+
+    VerletList_type& verletList_;
+    std::vector<unsigned> sig_;
+    unsigned differentialOrder_ = 0;
+    unsigned convergenceOrder_;
+    T rCut_;
+    support_options opt_;
+    std::unique_ptr<detail::PlanHost> plan_;
+};
+
+}  // namespace openfpm_dcpse

@@ -123,6 +123,20 @@ int dcpse_term_kernels_ptr(dcpse_plan_t* plan, int term, const double** d_kernel
                            const double** d_eps_inv_pow);
 /* summed, eps-folded output weights (either may be NULL if not stored) */
 int dcpse_output_weights_ptr(dcpse_plan_t* plan, int output, const double** d_w64, const float** d_w32);
+/* Installs previously saved kernels of term t (calcKernels[nnz], localEps[n],
+ * localEpsInvPow[n], device pointers, copied) on a plan whose neighbour list
+ * is set; the plan then counts as assembled for the per-term FP64 entry
+ * points.  Replaces: Dcpse::load (src/DCPSE/Dcpse.hpp:337-379). */
+int dcpse_set_term_kernels(dcpse_plan_t* plan, int term, const double* d_kernels, const double* d_eps,
+                           const double* d_eps_inv_pow);
+
+/* ---- device memory helpers ----------------------------------------------
+ * So that host code above this ABI needs no CUDA headers.  Replace the role
+ * of openfpm_devices' CudaMemory (hostToDevice / deviceToHost). */
+int dcpse_device_alloc(void** ptr, uint64_t bytes);
+int dcpse_device_free(void* ptr);
+/* synchronous copy between any host / device pointers */
+int dcpse_copy(void* dst, const void* src, uint64_t bytes);
 
 /* ---- apply --------------------------------------------------------------
  * Df_p = eps_p^-|alpha| sum_q (f_q + s f_p) K_pq, s = -1 for even |alpha|,

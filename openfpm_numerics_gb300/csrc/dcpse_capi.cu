@@ -774,6 +774,61 @@ int dcpse_output_weights_ptr(dcpse_plan_t* P, int output, const double** d_w64, 
     return DCPSE_OK;
 }
 
+int dcpse_set_term_kernels(dcpse_plan_t* P, int term, const double* d_kernels, const double* d_eps,
+                           const double* d_eps_inv_pow) {
+    if (int rc = check_plan(P)) return rc;
+    if (P->n < 0) return fail(DCPSE_ERR_STATE, "set the neighbour list first");
+    if (term < 0 || term >= P->nterms) return fail(DCPSE_ERR_ARG, "term out of range");
+    if ((P->nnz > 0 && !d_kernels) || (P->n > 0 && (!d_eps || !d_eps_inv_pow)))
+        return fail(DCPSE_ERR_ARG, "NULL array");
+    const int64_t n = P->n, nnz = P->nnz;
+    if (!P->assembled) {
+        // fresh plan (support_options::LOAD): kernels of every term start at zero
+        P->free_assembly();
+        DCPSE_CK(dalloc(&P->eps, n));
+        DCPSE_CK(dalloc(&P->status, n));
+        DCPSE_CK(dalloc(&P->eip_group, (size_t)P->htab->ngroups * n));
+        DCPSE_CK(dalloc(&P->k_term, (size_t)P->nterms * nnz));
+        DCPSE_CK(cudaMemsetAsync(P->status, 0, sizeof(int32_t) * n, P->stream));
+        DCPSE_CK(cudaMemsetAsync(P->k_term, 0, sizeof(double) * P->nterms * nnz, P->stream));
+        unsigned long long init[2] = {0ull, ~0ull};
+        DCPSE_CK(cudaMemcpyAsync(P->summary, init, sizeof init, cudaMemcpyHostToDevice, P->stream));
+        P->assembled = true;
+        P->flags = DCPSE_STORE_TERMS_F64;
+    }
+    if (!P->k_term) return fail(DCPSE_ERR_STATE, "plan was assembled without per-term kernels");
+    cudaStream_t s = P->stream;
+    if (nnz > 0)
+        DCPSE_CK(cudaMemcpyAsync(P->k_term + (size_t)term * nnz, d_kernels, sizeof(double) * nnz,
+                                 cudaMemcpyDefault, s));
+    if (n > 0) {
+        DCPSE_CK(cudaMemcpyAsync(P->eps, d_eps, sizeof(double) * n, cudaMemcpyDefault, s));
+        DCPSE_CK(cudaMemcpyAsync(P->eip_group + (size_t)P->term_group[term] * n, d_eps_inv_pow, sizeof(double) * n,
+                                 cudaMemcpyDefault, s));
+    }
+    DCPSE_CK(cudaStreamSynchronize(s));
+    return DCPSE_OK;
+}
+
+int dcpse_device_alloc(void** ptr, uint64_t bytes) {
+    if (!ptr) return fail(DCPSE_ERR_ARG, "NULL pointer");
+    *ptr = nullptr;
+    DCPSE_CK(cudaMalloc(ptr, bytes ? bytes : 1));
+    return DCPSE_OK;
+}
+
+int dcpse_device_free(void* ptr) {
+    if (ptr) DCPSE_CK(cudaFree(ptr));
+    return DCPSE_OK;
+}
+
+int dcpse_copy(void* dst, const void* src, uint64_t bytes) {
+    if (bytes == 0) return DCPSE_OK;
+    if (!dst || !src) return fail(DCPSE_ERR_ARG, "NULL pointer");
+    DCPSE_CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDefault));
+    return DCPSE_OK;
+}
+
 int dcpse_apply_term_f64(dcpse_plan_t* P, int term, const double* d_f, double* d_out) {
     if (int rc = check_plan(P)) return rc;
     if (!P->assembled || !P->k_term) return fail(DCPSE_ERR_STATE, "per-term FP64 kernels not stored");

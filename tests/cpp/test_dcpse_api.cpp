@@ -1,0 +1,201 @@
+// C++ drop-in API on the GPU: the reference's own DC-PSE test scenarios
+// (src/DCPSE/tests/Dcpse_unit_tests.cpp, src/DCPSE/DCPSE_op/tests/
+// DCPSE_op_test_base_tests.cpp) written against include/openfpm_dcpse, plus
+// bit-exact comparisons with the CPU oracle (linked from oracle/_build).
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "openfpm_dcpse/DCPSE_op.hpp"
+
+using namespace openfpm_dcpse;
+
+extern "C" {
+int64_t orc_assemble(int dim, const double* pd, int64_t n_dom, const double* ps, const int64_t* rowptr,
+                     const int32_t* cols, const double* box_lo, const double* box_hi, const int* periodic,
+                     const unsigned* sig, unsigned order, double h_over_eps, const double* eps_fixed, double* eps,
+                     double* eps_inv_pow, double* kernels, int32_t* status, int nthreads);
+void orc_apply(int64_t n_dom, const double* f_sup, const double* f_dom, const int64_t* rowptr, const int32_t* cols,
+               const double* kernels, const double* eps_inv_pow, unsigned diff_order, double* out, int nthreads);
+}
+
+static int failures = 0;
+#define EXPECT(cond, msg)                                              \
+    do {                                                               \
+        if (!(cond)) {                                                 \
+            std::printf("FAIL %s (%s:%d)\n", msg, __FILE__, __LINE__); \
+            ++failures;                                                \
+        } else {                                                       \
+            std::printf("ok   %s\n", msg);                             \
+        }                                                              \
+    } while (0)
+
+typedef vector_dist<2, double, double, double, double, double, std::array<double, 2>> Parts2;
+
+static Parts2 lattice2(int nside, double h) {
+    Parts2 d(nside * nside);
+    for (int j = 0; j < nside; ++j)
+        for (int i = 0; i < nside; ++i) {
+            std::size_t p = (std::size_t)j * nside + i;
+            d.getPos(p)[0] = i * h;
+            d.getPos(p)[1] = j * h;
+        }
+    return d;
+}
+
+// Dcpse_unit_tests.cpp:36-133 with the Dcpse class itself, and bit-exact
+// against the oracle
+static void test_dcpse_class() {
+    const int nside = 40;
+    const double h = 1.0 / (nside - 1), rCut = 3.1 * h;
+    Parts2 domain = lattice2(nside, h);
+    for (std::size_t p = 0; p < domain.size_local(); ++p) {
+        domain.getProp<0>(p) = std::sin(domain.getPos(p)[0]);
+        domain.getProp<2>(p) = std::cos(domain.getPos(p)[0]);
+    }
+    VerletList vl = getVerlet(domain, rCut);
+    Dcpse<2, VerletList, Parts2> dcpse(domain, vl, Point<2, unsigned>({1, 0}), 2, rCut, support_options::RADIUS);
+    dcpse.computeDifferentialOperator<0, 1>(domain);
+    double worst = 0;
+    for (std::size_t p = 0; p < domain.size_local(); ++p)
+        worst = std::max(worst, std::fabs(domain.getProp<1>(p) - domain.getProp<2>(p)));
+    EXPECT(worst < 2 * (2 * h) * (2 * h), "Dcpse 2D Dx within 2(2h)^2");
+
+    // oracle on the same list: kernels, eps^-|alpha| and Df bit for bit
+    const std::size_t n = domain.size_local();
+    std::vector<double> eps(n), eip(n), K(vl.cols.size()), f(n), out(n);
+    std::vector<int32_t> st(n);
+    unsigned sig[2] = {1, 0};
+    orc_assemble(2, domain.posData(), (int64_t)n, domain.posData(), vl.rowptr.data(), vl.cols.data(), nullptr,
+                 nullptr, nullptr, sig, 2, 0.9, nullptr, eps.data(), eip.data(), K.data(), st.data(), 1);
+    for (std::size_t p = 0; p < n; ++p) f[p] = domain.getProp<0>(p);
+    orc_apply((int64_t)n, f.data(), f.data(), vl.rowptr.data(), vl.cols.data(), K.data(), eip.data(), 1, out.data(), 1);
+    bool same = true;
+    for (std::size_t p = 0; p < n; ++p) same &= (out[p] == domain.getProp<1>(p));
+    EXPECT(same, "Dcpse::computeDifferentialOperator bit-exact with the oracle");
+    bool coeff = true;
+    for (std::size_t p = 0; p < n; p += 97) {
+        vect_dist_key_dx key(p);
+        for (int j = 0; j < dcpse.getNumNN(key); ++j)
+            coeff &= (dcpse.getCoeffNN(key, j) == K[vl.rowptr[p] + j]) && (dcpse.getIndexNN(key, j) == (std::size_t)vl.cols[vl.rowptr[p] + j]);
+        coeff &= dcpse.getEpsilonInvPrefactor(key) == eip[p];
+    }
+    EXPECT(coeff, "getCoeffNN / getIndexNN / getEpsilonInvPrefactor equal the oracle's");
+    EXPECT(dcpse.getSign() == 1.0, "getSign of an odd-order operator");
+    // per-key form: o1.value(key)
+    struct Field {
+        Parts2& d;
+        double value(const vect_dist_key_dx& k) const { return d.getProp<0>(k.getKey()); }
+    } fld{domain};
+    bool perkey = true;
+    for (std::size_t p = 0; p < n; p += 31) perkey &= dcpse.computeDifferentialOperator(vect_dist_key_dx(p), fld) == out[p];
+    EXPECT(perkey, "per-key computeDifferentialOperator equals the bulk apply");
+}
+
+// DCPSE_op_test_base_tests.cpp:30-101: v = 2 Dx(P) + Dy(P), worst < 0.03
+static void test_op_combination() {
+    const int nside = 80;
+    const double h = 2 * M_PI / (nside - 1), rCut = 3.9 * h;
+    Parts2 domain = lattice2(nside, h);
+    for (std::size_t p = 0; p < domain.size_local(); ++p) {
+        double x = domain.getPos(p)[0], y = domain.getPos(p)[1];
+        domain.getProp<0>(p) = std::sin(x) + std::sin(y);
+        domain.getProp<2>(p) = 2 * std::cos(x) + std::cos(y);
+    }
+    VerletList vl = getVerlet(domain, rCut);
+    Derivative_x<VerletList> Dx(domain, vl, 2, rCut);
+    Derivative_y<VerletList> Dy(domain, vl, 2, rCut);
+    auto v = getV<1>(domain);
+    auto P = getV<0>(domain);
+    v = 2 * Dx(P) + Dy(P);
+    double worst = 0;
+    for (std::size_t p = 0; p < domain.size_local(); ++p)
+        worst = std::max(worst, std::fabs(domain.getProp<1>(p) - domain.getProp<2>(p)));
+    EXPECT(worst < 0.03, "2 Dx(P) + Dy(P) worst < 0.03");
+
+    // Gradient into a vector property
+    Gradient<VerletList> Grad(domain, vl, 2, rCut);
+    getV<4>(domain) = Grad(P);
+    double wg = 0;
+    for (std::size_t p = 0; p < domain.size_local(); ++p) {
+        double x = domain.getPos(p)[0], y = domain.getPos(p)[1];
+        wg = std::max(wg, std::fabs(domain.getProp<4>(p)[0] - std::cos(x)));
+        wg = std::max(wg, std::fabs(domain.getProp<4>(p)[1] - std::cos(y)));
+    }
+    EXPECT(wg < 0.03, "Gradient components worst < 0.03");
+
+    // save / load round trip (support_options::LOAD builds an empty operator)
+    Dx.save(domain, "dcpse_cpp_test_dx");
+    Derivative_x<VerletList> Dx2(domain, vl, 2, rCut, support_options::LOAD);
+    Dx2.load(domain, "dcpse_cpp_test_dx");
+    getV<3>(domain) = Dx2(P);
+    getV<1>(domain) = Dx(P);
+    bool eq = true;
+    for (std::size_t p = 0; p < domain.size_local(); ++p) eq &= domain.getProp<3>(p) == domain.getProp<1>(p);
+    EXPECT(eq, "save + load reproduces the operator bit for bit");
+    std::remove("dcpse_cpp_test_dx_0");
+}
+
+// DCPSE_op_test_base_tests.cpp:394-467: Laplacian on 163^2, worst < 0.3
+static void test_laplacian() {
+    const int nside = 163;
+    const double h = 2 * M_PI / (nside - 1), rCut = 3.9 * h;
+    Parts2 domain = lattice2(nside, h);
+    for (std::size_t p = 0; p < domain.size_local(); ++p) {
+        double x = domain.getPos(p)[0], y = domain.getPos(p)[1];
+        domain.getProp<0>(p) = std::sin(x) + std::sin(y);
+        domain.getProp<1>(p) = -std::sin(x) - std::sin(y);
+    }
+    VerletList vl = getVerlet(domain, rCut);
+    Laplacian<VerletList> Lap(domain, vl, 2, rCut);
+    getV<2>(domain) = Lap(getV<0>(domain));
+    double worst = 0;
+    for (std::size_t p = 0; p < domain.size_local(); ++p)
+        worst = std::max(worst, std::fabs(domain.getProp<1>(p) - domain.getProp<2>(p)));
+    EXPECT(worst < 0.3, "Laplacian worst < 0.3");
+
+    // update after the particles moved equals a freshly built operator
+    for (std::size_t p = 0; p < domain.size_local(); ++p) domain.getPos(p)[0] += 1e-3 * h * std::sin(7.0 * p);
+    VerletList vl2 = getVerlet(domain, rCut);
+    vl = vl2;
+    Lap.update(domain);
+    getV<2>(domain) = Lap(getV<0>(domain));
+    Laplacian<VerletList> Lap2(domain, vl, 2, rCut);
+    getV<3>(domain) = Lap2(getV<0>(domain));
+    bool eq = true;
+    for (std::size_t p = 0; p < domain.size_local(); ++p) eq &= domain.getProp<2>(p) == domain.getProp<3>(p);
+    EXPECT(eq, "update() equals re-construction");
+}
+
+// too few neighbours raise std::length_error (Vandermonde.hpp:109-112)
+static void test_too_few() {
+    const int nside = 8;
+    const double h = 1.0 / (nside - 1);
+    Parts2 domain = lattice2(nside, h);
+    VerletList vl = getVerlet(domain, 1.05 * h);
+    bool thrown = false;
+    try {
+        Derivative_x<VerletList> Dx(domain, vl, 2, 1.05 * h);
+    } catch (const std::length_error&) {
+        thrown = true;
+    }
+    EXPECT(thrown, "too few neighbours throw std::length_error");
+}
+
+int main() {
+    try {
+        test_dcpse_class();
+        test_op_combination();
+        test_laplacian();
+        test_too_few();
+    } catch (const std::exception& e) {
+        std::printf("FAIL exception: %s\n", e.what());
+        return 2;
+    }
+    std::printf("%s (%d failures)\n", failures ? "FAILED" : "ALL OK", failures);
+    return failures ? 1 : 0;
+}
