@@ -158,6 +158,21 @@ int dcpse_apply_batched(dcpse_plan_t* plan, const double* d_f, double* d_out, in
  * the call (the reference's bulk apply reads and writes host particles). */
 int dcpse_apply_batched_host(dcpse_plan_t* plan, const double* h_f, double* h_out, int precision);
 
+/* ---- adjoint ------------------------------------------------------------
+ * No counterpart in the reference (its operators have no derivatives); these
+ * differentiate the batched apply y_o = L_o f with the neighbour list held
+ * fixed.
+ * Field VJP: d_out[q] = sum_o (L_o^T g_o)_q for a cotangent d_g[o*n + p],
+ * from the FP64 (DCPSE_F64) or FP32 (DCPSE_F32) output weights, through a
+ * transposed neighbour list built once per list (fixed summation order). */
+int dcpse_vjp_field(dcpse_plan_t* plan, const double* d_g, double* d_out, int precision);
+/* Position VJP: d_grad[i*dim + d] = d/dx_i,d of sum_o,p g_o,p (L_o f)_p,
+ * differentiating through every particle's moment-matrix solve, eps and the
+ * scaling eps^-|alpha| (FP64).  d_pos must be the positions the plan was
+ * assembled with; d_eps_fixed the override used there, or NULL. */
+int dcpse_vjp_positions(dcpse_plan_t* plan, const double* d_pos, const double* d_eps_fixed, const double* d_f,
+                        const double* d_g, double* d_grad);
+
 /* ---- batched FP32 apply that allocates nothing --------------------------
  * No counterpart in the reference.  For callers that must not allocate
  * device memory: code running inside an allocator or memory-pool callback,

@@ -47,6 +47,8 @@ SIGNATURES = {
     "dcpse_apply_batched_host": (_I, [_P, _P, _P, _I]),
     "dcpse_apply_batched_f32_noalloc": (_I, [_I64, _I, _P, _P, _P, _I64, _P, _P, _P]),
     "dcpse_set_term_kernels": (_I, [_P, _I, _P, _P, _P]),
+    "dcpse_vjp_field": (_I, [_P, _P, _P, _I]),
+    "dcpse_vjp_positions": (_I, [_P, _P, _P, _P, _P, _P]),
     "dcpse_device_alloc": (_I, [_PP, _c.c_uint64]),
     "dcpse_device_free": (_I, [_P]),
     "dcpse_copy": (_I, [_P, _P, _c.c_uint64]),

@@ -199,6 +199,21 @@ struct dcpse_plan_s {
     unsigned long long* summary = nullptr;  // [count, first]
     int* d_err = nullptr;                   // set by kernels whose bounded wait ran out
     int apply_lanes = 0, apply_mode = 0;
+    // transposed list and weight row sums (adjoint), built on demand
+    int64_t* t_row = nullptr;
+    int32_t* t_src = nullptr;
+    int64_t* t_idx = nullptr;
+    double* rowsum = nullptr;
+    int rowsum_prec = -1;
+    double* gentry = nullptr;
+    void free_transpose() {
+        dfree(t_row);
+        dfree(t_src);
+        dfree(t_idx);
+        dfree(rowsum);
+        dfree(gentry);
+        rowsum_prec = -1;
+    }
     // apply scratch
     float2* f2 = nullptr;
     double* hf = nullptr;    // device copy of a host field (host apply)
@@ -213,10 +228,13 @@ struct dcpse_plan_s {
         dfree(w32);
         if (r16) cudaFree(r16);
         r16 = nullptr;
+        dfree(rowsum);
+        rowsum_prec = -1;
         assembled = false;
     }
     void free_all() {
         free_assembly();
+        free_transpose();
         dfree(rowptr);
         dfree(cols);
         dfree(f2);
@@ -473,6 +491,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     cudaStream_t s = P->stream;
     const int dim = P->dim;
     P->free_assembly();
+    P->free_transpose();
     dfree(P->rowptr);
     dfree(P->cols);
     P->n = n;
@@ -611,6 +630,7 @@ int dcpse_set_neighbors(dcpse_plan_t* P, int64_t n, int64_t nnz, const int64_t* 
     if (n < 0 || nnz < 0 || !d_rowptr || (nnz > 0 && !d_cols)) return fail(DCPSE_ERR_ARG, "bad CSR arrays");
     cudaStream_t s = P->stream;
     P->free_assembly();
+    P->free_transpose();
     dfree(P->rowptr);
     dfree(P->cols);
     P->n = n;
@@ -807,6 +827,88 @@ int dcpse_set_term_kernels(dcpse_plan_t* P, int term, const double* d_kernels, c
                                  cudaMemcpyDefault, s));
     }
     DCPSE_CK(cudaStreamSynchronize(s));
+    return DCPSE_OK;
+}
+
+namespace {
+int ensure_transpose(dcpse_plan_t* P) {
+    if (P->t_row) return DCPSE_OK;
+    cudaStream_t s = P->stream;
+    const int64_t n = P->n, nnz = P->nnz;
+    int32_t *cnt = nullptr, *src_tmp = nullptr;
+    int64_t *fill = nullptr, *idx_tmp = nullptr, *scan_tmp = nullptr;
+    cudaError_t e = dalloc(&P->t_row, (size_t)n + 1);
+    if (e == cudaSuccess) e = dalloc(&P->t_src, nnz);
+    if (e == cudaSuccess) e = dalloc(&P->t_idx, nnz);
+    if (e == cudaSuccess) e = dalloc(&cnt, n);
+    if (e == cudaSuccess) e = dalloc(&fill, n);
+    if (e == cudaSuccess) e = dalloc(&src_tmp, nnz);
+    if (e == cudaSuccess) e = dalloc(&idx_tmp, nnz);
+    if (e == cudaSuccess) e = dalloc(&scan_tmp, scan_tmp_elems(n));
+    if (e == cudaSuccess && n == 0) e = cudaMemsetAsync(P->t_row, 0, sizeof(int64_t), s);
+    if (e == cudaSuccess)
+        e = build_transpose(P->rowptr, P->cols, n, nnz, cnt, P->t_row, fill, src_tmp, idx_tmp, P->t_src, P->t_idx,
+                            scan_tmp, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    dfree(cnt);
+    dfree(fill);
+    dfree(src_tmp);
+    dfree(idx_tmp);
+    dfree(scan_tmp);
+    if (e != cudaSuccess) {
+        P->free_transpose();
+        return fail(DCPSE_ERR_CUDA, std::string("transposed list: ") + cudaGetErrorString(e));
+    }
+    return DCPSE_OK;
+}
+}  // namespace
+
+int dcpse_vjp_field(dcpse_plan_t* P, const double* d_g, double* d_out, int precision) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
+    if (P->n > 0 && (!d_g || !d_out)) return fail(DCPSE_ERR_ARG, "NULL array");
+    const double* w64 = nullptr;
+    const float* w32 = nullptr;
+    if (precision == DCPSE_F64) {
+        if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
+        w64 = P->w64;
+    } else if (precision == DCPSE_F32) {
+        if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
+        w32 = P->w32;
+    } else {
+        return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F64 or DCPSE_F32");
+    }
+    if (int rc = ensure_transpose(P)) return rc;
+    if (P->rowsum_prec != precision) {
+        if (!P->rowsum) DCPSE_CK(dalloc(&P->rowsum, (size_t)P->nout * P->n));
+        DCPSE_CK(row_sums(P->rowptr, P->n, P->nout, w64, w32, P->nnz, P->rowsum, P->stream));
+        P->rowsum_prec = precision;
+    }
+    DCPSE_CK(vjp_field(P->t_row, P->t_src, P->t_idx, P->n, P->nout, w64, w32, P->nnz, P->rowsum, d_g, d_out,
+                       P->stream));
+    return DCPSE_OK;
+}
+
+int dcpse_vjp_positions(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fixed, const double* d_f,
+                        const double* d_g, double* d_grad) {
+    if (int rc = check_plan(P)) return rc;
+    if (P->n < 0) return fail(DCPSE_ERR_STATE, "no neighbour list");
+    if (P->n > 0 && (!d_pos || !d_f || !d_g || !d_grad)) return fail(DCPSE_ERR_ARG, "NULL array");
+    if (int rc = ensure_transpose(P)) return rc;
+    if (!P->gentry) DCPSE_CK(dalloc(&P->gentry, (size_t)P->nnz * P->dim));
+    VjpArgs a{};
+    a.tab = P->dtab;
+    a.n = P->n;
+    a.pos = d_pos;
+    a.rowptr = P->rowptr;
+    a.cols = P->cols;
+    a.geom = plan_geom(P);
+    a.h_over_eps = P->hoe;
+    a.eps_fixed = d_eps_fixed;
+    a.f = d_f;
+    a.gbar = d_g;
+    a.gentry = P->gentry;
+    DCPSE_CK(vjp_positions(a, *P->htab, P->t_row, P->t_idx, d_grad, P->stream));
     return DCPSE_OK;
 }
 

@@ -149,6 +149,33 @@ cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s);
 cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const double* w,
                               int64_t nnz, const double* f, double* out, cudaStream_t s);
 
+// --------------------------------------------------------------- adjoint --
+// transposed list: trow[n+1], per entry the source row tsrc and entry index tidx
+cudaError_t build_transpose(const int64_t* rowptr, const int32_t* cols, int64_t n, int64_t nnz, int32_t* cnt,
+                            int64_t* trow, int64_t* fill, int32_t* tsrc_tmp, int64_t* tidx_tmp, int32_t* tsrc,
+                            int64_t* tidx, int64_t* scan_tmp, cudaStream_t s);
+cudaError_t row_sums(const int64_t* rowptr, int64_t n, int nout, const double* w64, const float* w32, int64_t ws,
+                     double* rs, cudaStream_t s);
+cudaError_t vjp_field(const int64_t* trow, const int32_t* tsrc, const int64_t* tidx, int64_t n, int nout,
+                      const double* w64, const float* w32, int64_t ws, const double* rs, const double* g, double* out,
+                      cudaStream_t s);
+
+struct VjpArgs {
+    const AsmTables* tab;
+    int64_t n;
+    const double* pos;
+    const int64_t* rowptr;
+    const int32_t* cols;
+    Geom geom;
+    double h_over_eps;
+    const double* eps_fixed;
+    const double* f;      // field [n]
+    const double* gbar;   // cotangent [noutputs][n]
+    double* gentry;       // scratch [nnz][dim]: dPhi_p / dx_pq
+};
+cudaError_t vjp_positions(const VjpArgs& a, const AsmTables& h, const int64_t* trow, const int64_t* tidx, double* grad,
+                          cudaStream_t s);
+
 int num_sms();
 
 // Records msg as this thread's dcpse_last_error() and returns code.

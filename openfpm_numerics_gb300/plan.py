@@ -209,6 +209,30 @@ class DcpsePlan:
                out_host.ctypes.data_as(ctypes.c_void_p), int(precision))
         return out_host
 
+    # -- adjoint --------------------------------------------------------
+    def vjp_field(self, g, precision=C.F64, out=None):
+        """sum_o L_o^T g_o for a cotangent g [n_outputs, n] -> [n]."""
+        g = g.contiguous().to(torch.float64)
+        if g.dim() == 1:
+            g = g.unsqueeze(0)
+        out = torch.empty(g.shape[1], dtype=torch.float64, device=g.device) if out is None else out
+        C.call("dcpse_vjp_field", self._h, _ptr(g), _ptr(out), int(precision))
+        return out
+
+    def vjp_positions(self, pos, f, g, eps_fixed=None):
+        """d/dpos of sum_o,p g[o,p] (L_o f)_p with the neighbour list fixed
+        -> [n, dim] (FP64; pos must be the assembled positions)."""
+        pos = self._check_pos(pos)
+        f = self._check_field(f)
+        g = g.contiguous().to(torch.float64)
+        if g.dim() == 1:
+            g = g.unsqueeze(0)
+        if eps_fixed is not None:
+            eps_fixed = eps_fixed.contiguous().to(torch.float64)
+        grad = torch.empty_like(pos)
+        C.call("dcpse_vjp_positions", self._h, _ptr(pos), _ptr(eps_fixed), _ptr(f), _ptr(g), _ptr(grad))
+        return grad
+
     # -- timing ---------------------------------------------------------
     def set_timing(self, enable=True):
         C.call("dcpse_plan_set_timing", self._h, int(bool(enable)))

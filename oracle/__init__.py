@@ -76,6 +76,9 @@ def lib():
                                     ctypes.POINTER(_D), ctypes.POINTER(_D), _U, _D, ctypes.c_int]
         L.orc_apply_multi.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _D, _I64, _I32, ctypes.POINTER(_D),
                                       ctypes.POINTER(_D), _U, _INT, ctypes.c_int, _D, ctypes.c_int]
+        L.orc_vjp_positions.restype = ctypes.c_int64
+        L.orc_vjp_positions.argtypes = [ctypes.c_int, _D, ctypes.c_int64, _I64, _I32, ctypes.c_int, _U, _INT,
+                                        ctypes.c_uint, ctypes.c_double, _D, _D, _D]
         _lib = L
     return _lib
 
@@ -203,6 +206,23 @@ def apply_sum(f, rowptr, cols, Ks, eips, diff_orders, *, nthreads=1):
     lib().orc_apply_sum(n, len(Ks), _p(f, _D), _p(f, _D), _p(rowptr, _I64), _p(cols, _I32), kp, ep,
                         _p(do, _U), _p(out, _D), int(nthreads))
     return out
+
+
+def vjp_positions(pos, rowptr, cols, outputs, f, g, order=2, h_over_eps=0.9):
+    """Reference adjoint: d/dx of sum_o,p g[o,p] (L_o f)_p, lists fixed.
+    outputs: list of outputs, each a list of term signatures."""
+    pos = _c(pos, np.float64)
+    n, dim = pos.shape
+    sigs = _c([x for o in outputs for s in o for x in s], np.uint32)
+    tout = _c([o for o, out in enumerate(outputs) for _ in out], np.int32)
+    f = _c(f, np.float64)
+    g = _c(g, np.float64)
+    grad = np.zeros((n, dim))
+    rowptr = _c(rowptr, np.int64)
+    cols = _c(cols, np.int32)
+    lib().orc_vjp_positions(dim, _p(pos, _D), n, _p(rowptr, _I64), _p(cols, _I32), len(tout), _p(sigs, _U),
+                            _p(tout, _INT), order, float(h_over_eps), _p(f, _D), _p(g, _D), _p(grad, _D))
+    return grad
 
 
 class MultiApply:

@@ -647,6 +647,141 @@ void orc_apply_sum(int64_t n_dom, int ncomp, const double* f_sup, const double* 
     });
 }
 
+// Reference adjoint (FP64) of y_o,p = sum_q W_o,pq (f_q - f_p) with respect
+// to positions, W_o = sum_{t in o} eps_p^-|alpha_t| K_t (the weights of
+// Dcpse.hpp:690-809), neighbour lists fixed.  Written per term directly from
+// K_t,q = omega_q v_q^T a_t, a_t = A^-1 b_t, A = sum_q omega_q v_q v_q^T,
+// omega_q = exp(-|u_q|^2), u_q = x_pq / eps,
+// eps = sum_q |x_pq|_1 / (k HOverEpsilon):
+//   Phi_t = g_o(t),p e_t s^T a_t,  s = sum_q c_q omega_q v_q, lambda = A^-1 s,
+//   dPhi/domega_q = e g (v.a)(c - v.lambda), dPhi/dv_q = e g omega ((c - v.lambda) a - (v.a) lambda),
+// then the chain rule through u_q, eps and e_t = eps^-|alpha_t|.
+// grad is [n][dim] and accumulated (zero it first).  Positions, f, g: domain
+// arrays; sigs: nterms x dim; term_output: output of each term; g: [nout][n].
+int64_t orc_vjp_positions(int dim, const double* pos, int64_t n, const int64_t* rowptr, const int32_t* cols,
+                          int nterms, const unsigned* sigs, const int* term_output, unsigned order, double h_over_eps,
+                          const double* f, const double* g, double* grad) {
+    Geom geo = make_geom(dim, nullptr, nullptr, nullptr);
+    std::vector<Basis> bases;
+    std::vector<std::vector<double>> rhs;
+    for (int t = 0; t < nterms; ++t) {
+        bases.push_back(make_basis(dim, sigs + t * dim, order));
+        std::vector<double> b(bases.back().n);
+        make_rhs(bases.back(), sigs + t * dim, b.data());
+        rhs.push_back(b);
+    }
+    int64_t skipped = 0;
+    for (int64_t p = 0; p < n; ++p) {
+        const int64_t beg = rowptr[p];
+        const int k = (int)(rowptr[p + 1] - beg);
+        std::vector<double> X((size_t)k * dim);
+        double s1 = 0.0;
+        for (int q = 0; q < k; ++q)
+            for (int d = 0; d < dim; ++d) {
+                X[(size_t)q * dim + d] = offset1(geo, d, pos[p * dim + d], pos[(int64_t)cols[beg + q] * dim + d]);
+                s1 += std::fabs(X[(size_t)q * dim + d]);
+            }
+        const double eps = s1 / k / h_over_eps;
+        bool ok = k > 0 && eps > 0 && std::isfinite(eps);
+        for (int t = 0; t < nterms && ok; ++t) ok = k >= bases[t].n;
+        if (!ok) {
+            ++skipped;
+            continue;
+        }
+        std::vector<double> U((size_t)k * dim), om(k), c(k);
+        for (int q = 0; q < k; ++q) {
+            double r2 = 0.0;
+            for (int d = 0; d < dim; ++d) {
+                U[(size_t)q * dim + d] = X[(size_t)q * dim + d] / eps;
+                r2 += U[(size_t)q * dim + d] * U[(size_t)q * dim + d];
+            }
+            om[q] = std::exp(-r2);
+            c[q] = f[cols[beg + q]] - f[p];
+        }
+        std::vector<double> Gq((size_t)k * dim, 0.0);  // dPhi / du_q
+        double dPhi_deps_explicit = 0.0;
+        for (int t = 0; t < nterms; ++t) {
+            const Basis& B = bases[t];
+            const int nb = B.n;
+            const double gt = g[(int64_t)term_output[t] * n + p];
+            unsigned m = 0;
+            for (int d = 0; d < dim; ++d) m += sigs[t * dim + d];
+            const double et = 1.0 / std::pow(eps, (double)m);
+            std::vector<double> V((size_t)k * nb), dV((size_t)k * nb * dim);
+            for (int q = 0; q < k; ++q)
+                for (int i = 0; i < nb; ++i) {
+                    const unsigned* e = &B.exps[i * dim];
+                    double val = 1.0;
+                    for (int d = 0; d < dim; ++d) val *= std::pow(U[(size_t)q * dim + d], (double)e[d]);
+                    V[(size_t)q * nb + i] = val;
+                    for (int d = 0; d < dim; ++d) {
+                        double dv = 0.0;
+                        if (e[d] > 0) {
+                            dv = e[d] * std::pow(U[(size_t)q * dim + d], (double)e[d] - 1.0);
+                            for (int d2 = 0; d2 < dim; ++d2)
+                                if (d2 != d) dv *= std::pow(U[(size_t)q * dim + d2], (double)e[d2]);
+                        }
+                        dV[((size_t)q * nb + i) * dim + d] = dv;
+                    }
+                }
+            std::vector<double> A((size_t)nb * nb, 0.0), sv(nb, 0.0);
+            for (int q = 0; q < k; ++q)
+                for (int i = 0; i < nb; ++i) {
+                    sv[i] += c[q] * om[q] * V[(size_t)q * nb + i];
+                    for (int j = 0; j < nb; ++j) A[(size_t)i * nb + j] += om[q] * V[(size_t)q * nb + i] * V[(size_t)q * nb + j];
+                }
+            std::vector<double> C(2 * (size_t)nb), sol(2 * (size_t)nb);
+            for (int i = 0; i < nb; ++i) {
+                C[i * 2] = rhs[t][i];
+                C[i * 2 + 1] = sv[i];
+            }
+            std::vector<double> Ac(A);
+            if (!cpqr_solve(nb, 2, Ac.data(), C.data(), sol.data())) {
+                ok = false;
+                break;
+            }
+            double sa = 0.0;
+            for (int i = 0; i < nb; ++i) sa += sv[i] * sol[i * 2];
+            dPhi_deps_explicit += gt * (-(double)m) * et * sa / eps;
+            for (int q = 0; q < k; ++q) {
+                double va = 0.0, vl = 0.0;
+                for (int i = 0; i < nb; ++i) {
+                    va += V[(size_t)q * nb + i] * sol[i * 2];
+                    vl += V[(size_t)q * nb + i] * sol[i * 2 + 1];
+                }
+                const double dom = gt * et * va * (c[q] - vl);
+                for (int d = 0; d < dim; ++d) {
+                    double acc = dom * (-2.0 * om[q] * U[(size_t)q * dim + d]);
+                    for (int i = 0; i < nb; ++i) {
+                        const double beta = gt * et * om[q] * ((c[q] - vl) * sol[i * 2] - va * sol[i * 2 + 1]);
+                        acc += beta * dV[((size_t)q * nb + i) * dim + d];
+                    }
+                    Gq[(size_t)q * dim + d] += acc;
+                }
+            }
+        }
+        if (!ok) {
+            ++skipped;
+            continue;
+        }
+        double gu_dot_u = 0.0;
+        for (int q = 0; q < k; ++q)
+            for (int d = 0; d < dim; ++d) gu_dot_u += Gq[(size_t)q * dim + d] * U[(size_t)q * dim + d];
+        const double Dtot = dPhi_deps_explicit - gu_dot_u / eps;
+        for (int q = 0; q < k; ++q) {
+            const int64_t qq = cols[beg + q];
+            for (int d = 0; d < dim; ++d) {
+                const double x = X[(size_t)q * dim + d];
+                const double sg = x > 0 ? 1.0 : (x < 0 ? -1.0 : 0.0);
+                const double G = Gq[(size_t)q * dim + d] / eps + Dtot * sg / (k * h_over_eps);
+                grad[p * dim + d] += G;
+                grad[qq * dim + d] -= G;
+            }
+        }
+    }
+    return skipped;
+}
+
 // Several outputs in one sweep over the particles, the way the reference's
 // expression evaluation visits them (vector_dist_op_compute_op<prp,comp_host>
 // ::compute_expr, src/Operators/Vector/cuda/vector_dist_operators_cuda.cuh:
