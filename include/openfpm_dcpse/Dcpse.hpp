@@ -236,6 +236,30 @@ std::vector<unsigned> sig_vector(const Sig& s, int dim) {
     return v;
 }
 
+// D = sum_j (f_j + fxp) * K_j in the reference's order with every product
+// and sum rounded separately (no contraction into fused multiply-adds, which
+// compilers apply by default on some hosts), then D * eip.
+#if defined(__clang__)
+#define OPENFPM_DCPSE_NO_CONTRACT
+#elif defined(__GNUC__)
+#define OPENFPM_DCPSE_NO_CONTRACT __attribute__((optimize("fp-contract=off")))
+#else
+#define OPENFPM_DCPSE_NO_CONTRACT
+#endif
+template <typename T, typename FQ>
+OPENFPM_DCPSE_NO_CONTRACT T reference_sum(std::size_t k, FQ fq, T fxp, const double* K, double eip) {
+#if defined(__clang__)
+#pragma clang fp contract(off)
+#endif
+    T D = 0;
+    for (std::size_t j = 0; j < k; ++j) {
+        const T t = fq(j) + fxp;
+        const T prod = t * (T)K[j];
+        D = D + prod;
+    }
+    return D * (T)eip;
+}
+
 inline void throw_too_few(int code, int64_t nbad) {
     if (nbad == 0) return;
     if (code == DCPSE_PART_TOO_FEW)
@@ -290,14 +314,12 @@ public:
         const auto& eip = plan_->eps_inv_pow(0);
         const T sign = (differentialOrder_ % 2 == 0) ? -1 : 1;
         const T fxp = sign * o1.value(p);
-        T D = 0;
         const int64_t b = plan_->rowptr()[p.getKey()];
         const std::size_t k = verletList_.getNNPart(p.getKey());
-        for (std::size_t j = 0; j < k; ++j) {
-            const T fxq = o1.value(vect_dist_key_dx(verletList_.get(p.getKey(), j)));
-            D = D + (fxq + fxp) * K[(std::size_t)(b + (int64_t)j)];
-        }
-        return D * eip[p.getKey()];
+        auto fq = [&](std::size_t j) -> T {
+            return o1.value(vect_dist_key_dx(verletList_.get(p.getKey(), j)));
+        };
+        return detail::reference_sum<T>(k, fq, fxp, K.data() + b, eip[p.getKey()]);
     }
 
     // accessors (Dcpse.hpp:507-550)
