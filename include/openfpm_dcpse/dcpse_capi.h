@@ -173,6 +173,27 @@ int dcpse_vjp_field(dcpse_plan_t* plan, const double* d_g, double* d_out, int pr
 int dcpse_vjp_positions(dcpse_plan_t* plan, const double* d_pos, const double* d_eps_fixed, const double* d_f,
                         const double* d_g, double* d_grad);
 
+/* ---- RK4 time stepping of two-species reaction-diffusion ----------------
+ * Gray-Scott:  du = Du L u - u v^2 + F (1 - u),  dv = Dv L v + u v^2 - (F+k) v
+ * with L = output 0 of the plan (a Laplacian; FP32 weights for
+ * precision DCPSE_F32 with float state arrays, FP64 output weights for
+ * DCPSE_F64 with double arrays).  params = {Du, Dv, F, k, dt}.
+ * One call is one classic RK4 stage (stage 0..3; see dcpse_rk4.cu for the
+ * buffers each stage reads and writes); four calls make a step and contain
+ * no synchronisation or allocation, so a step can be captured in a CUDA
+ * graph.  Replaces: boost odeint runge_kutta4 over the DC-PSE Laplacian as
+ * used in src/OdeIntegrators/tests/OdeIntegratores_base_tests.cpp:33-72,478-577. */
+int dcpse_rk4_gs_stage(dcpse_plan_t* plan, int stage, int precision, const void* Yu, const void* Yv, const void* y0u,
+                       const void* y0v, void* accu, void* accv, void* outu, void* outv, const double* params);
+/* Builds the transposed Laplacian weights used by the adjoint stages
+ * (call after assembly, outside graph capture). */
+int dcpse_rk4_gs_adjoint_prepare(dcpse_plan_t* plan, int precision);
+/* One reverse RK4 stage: acc += J(Y)^T kbar; next = cy * ybar + cY * J(Y)^T kbar
+ * (next may be NULL).  params = {Du, Dv, F, k, dt}. */
+int dcpse_rk4_gs_adjoint_stage(dcpse_plan_t* plan, int precision, const void* Yu, const void* Yv, const void* kbu,
+                               const void* kbv, const void* ybu, const void* ybv, void* accu, void* accv, void* next_u,
+                               void* next_v, double cy, double cY, const double* params);
+
 /* ---- batched FP32 apply that allocates nothing --------------------------
  * No counterpart in the reference.  For callers that must not allocate
  * device memory: code running inside an allocator or memory-pool callback,

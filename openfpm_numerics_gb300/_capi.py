@@ -49,6 +49,9 @@ SIGNATURES = {
     "dcpse_set_term_kernels": (_I, [_P, _I, _P, _P, _P]),
     "dcpse_vjp_field": (_I, [_P, _P, _P, _I]),
     "dcpse_vjp_positions": (_I, [_P, _P, _P, _P, _P, _P]),
+    "dcpse_rk4_gs_stage": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _c.POINTER(_D)]),
+    "dcpse_rk4_gs_adjoint_prepare": (_I, [_P, _I]),
+    "dcpse_rk4_gs_adjoint_stage": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _D, _c.POINTER(_D)]),
     "dcpse_device_alloc": (_I, [_PP, _c.c_uint64]),
     "dcpse_device_free": (_I, [_P]),
     "dcpse_copy": (_I, [_P, _P, _c.c_uint64]),

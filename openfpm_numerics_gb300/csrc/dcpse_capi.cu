@@ -206,12 +206,19 @@ struct dcpse_plan_s {
     double* rowsum = nullptr;
     int rowsum_prec = -1;
     double* gentry = nullptr;
+    // transposed Laplacian weights of output 0 for the RK4 adjoint
+    float *wT32 = nullptr, *rs32 = nullptr;
+    double *wT64 = nullptr, *rs64 = nullptr;
     void free_transpose() {
         dfree(t_row);
         dfree(t_src);
         dfree(t_idx);
         dfree(rowsum);
         dfree(gentry);
+        dfree(wT32);
+        dfree(rs32);
+        dfree(wT64);
+        dfree(rs64);
         rowsum_prec = -1;
     }
     // apply scratch
@@ -230,6 +237,10 @@ struct dcpse_plan_s {
         r16 = nullptr;
         dfree(rowsum);
         rowsum_prec = -1;
+        dfree(wT32);
+        dfree(rs32);
+        dfree(wT64);
+        dfree(rs64);
         assembled = false;
     }
     void free_all() {
@@ -909,6 +920,80 @@ int dcpse_vjp_positions(dcpse_plan_t* P, const double* d_pos, const double* d_ep
     a.gbar = d_g;
     a.gentry = P->gentry;
     DCPSE_CK(vjp_positions(a, *P->htab, P->t_row, P->t_idx, d_grad, P->stream));
+    return DCPSE_OK;
+}
+
+int dcpse_rk4_gs_stage(dcpse_plan_t* P, int stage, int precision, const void* Yu, const void* Yv, const void* y0u,
+                       const void* y0v, void* accu, void* accv, void* outu, void* outv, const double* params) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
+    if (stage < 0 || stage > 3 || !params) return fail(DCPSE_ERR_ARG, "stage 0..3 and params {Du,Dv,F,k,dt}");
+    if (P->n > 0 && (!Yu || !Yv || !y0u || !y0v || !accu || !accv || !outu || !outv))
+        return fail(DCPSE_ERR_ARG, "NULL array");
+    const int lanes = P->apply_lanes ? P->apply_lanes : (P->nnz <= 24 * P->n ? 8 : 16);
+    if (precision == DCPSE_F32) {
+        if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
+        RkArgs<float> a{P->n, P->rowptr, P->cols, P->w32, (const float*)Yu, (const float*)Yv, (const float*)y0u,
+                        (const float*)y0v, (float*)accu, (float*)accv, (float*)outu, (float*)outv,
+                        params[0], params[1], params[2], params[3], params[4], stage};
+        DCPSE_CK(rk_stage<float>(a, lanes, P->stream));
+    } else if (precision == DCPSE_F64) {
+        if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
+        RkArgs<double> a{P->n, P->rowptr, P->cols, P->w64, (const double*)Yu, (const double*)Yv, (const double*)y0u,
+                         (const double*)y0v, (double*)accu, (double*)accv, (double*)outu, (double*)outv,
+                         params[0], params[1], params[2], params[3], params[4], stage};
+        DCPSE_CK(rk_stage<double>(a, lanes, P->stream));
+    } else {
+        return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
+    }
+    return DCPSE_OK;
+}
+
+int dcpse_rk4_gs_adjoint_prepare(dcpse_plan_t* P, int precision) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
+    if (int rc = ensure_transpose(P)) return rc;
+    if (precision == DCPSE_F32) {
+        if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
+        if (!P->wT32) DCPSE_CK(dalloc(&P->wT32, P->nnz));
+        if (!P->rs32) DCPSE_CK(dalloc(&P->rs32, P->n));
+        DCPSE_CK(rk_transpose_weights<float>(P->rowptr, P->t_idx, P->n, P->nnz, P->w32, P->wT32, P->rs32, P->stream));
+    } else if (precision == DCPSE_F64) {
+        if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
+        if (!P->wT64) DCPSE_CK(dalloc(&P->wT64, P->nnz));
+        if (!P->rs64) DCPSE_CK(dalloc(&P->rs64, P->n));
+        DCPSE_CK(rk_transpose_weights<double>(P->rowptr, P->t_idx, P->n, P->nnz, P->w64, P->wT64, P->rs64, P->stream));
+    } else {
+        return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
+    }
+    DCPSE_CK(cudaStreamSynchronize(P->stream));
+    return DCPSE_OK;
+}
+
+int dcpse_rk4_gs_adjoint_stage(dcpse_plan_t* P, int precision, const void* Yu, const void* Yv, const void* kbu,
+                               const void* kbv, const void* ybu, const void* ybv, void* accu, void* accv, void* next_u,
+                               void* next_v, double cy, double cY, const double* params) {
+    if (int rc = check_plan(P)) return rc;
+    if (!params) return fail(DCPSE_ERR_ARG, "params {Du,Dv,F,k,dt}");
+    if (P->n > 0 && (!Yu || !Yv || !kbu || !kbv || !ybu || !ybv || !accu || !accv))
+        return fail(DCPSE_ERR_ARG, "NULL array");
+    if (precision == DCPSE_F32) {
+        if (!P->wT32) return fail(DCPSE_ERR_STATE, "call dcpse_rk4_gs_adjoint_prepare first");
+        RkAdjArgs<float> a{P->n, P->t_row, P->t_src, P->wT32, P->rs32, (const float*)Yu, (const float*)Yv,
+                           (const float*)kbu, (const float*)kbv, (const float*)ybu, (const float*)ybv, (float*)accu,
+                           (float*)accv, (float*)next_u, (float*)next_v, cy, cY, params[0], params[1], params[2],
+                           params[3]};
+        DCPSE_CK(rk_adjoint_stage<float>(a, P->stream));
+    } else if (precision == DCPSE_F64) {
+        if (!P->wT64) return fail(DCPSE_ERR_STATE, "call dcpse_rk4_gs_adjoint_prepare first");
+        RkAdjArgs<double> a{P->n, P->t_row, P->t_src, P->wT64, P->rs64, (const double*)Yu, (const double*)Yv,
+                            (const double*)kbu, (const double*)kbv, (const double*)ybu, (const double*)ybv,
+                            (double*)accu, (double*)accv, (double*)next_u, (double*)next_v, cy, cY, params[0],
+                            params[1], params[2], params[3]};
+        DCPSE_CK(rk_adjoint_stage<double>(a, P->stream));
+    } else {
+        return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
+    }
     return DCPSE_OK;
 }
 

@@ -176,6 +176,43 @@ struct VjpArgs {
 cudaError_t vjp_positions(const VjpArgs& a, const AsmTables& h, const int64_t* trow, const int64_t* tidx, double* grad,
                           cudaStream_t s);
 
+// ------------------------------------------------- RK4 reaction-diffusion --
+template <typename T>
+struct RkArgs {
+    int64_t n;
+    const int64_t* rowptr;
+    const int32_t* cols;
+    const T* w;                     // Laplacian weights [nnz]
+    const T *Yu, *Yv;               // stage input (gathered)
+    const T *y0u, *y0v;             // state at the start of the step
+    T *accu, *accv;                 // k1 + 2 k2 + 2 k3
+    T *outu, *outv;                 // next stage input, or the new state
+    double Du, Dv, F, K, dt;
+    int stage;                      // 0..3
+};
+template <typename T>
+struct RkAdjArgs {
+    int64_t n;
+    const int64_t* trow;
+    const int32_t* tsrc;
+    const T* wT;                    // transposed Laplacian weights
+    const T* rs;                    // row sums of the weights
+    const T *Yu, *Yv;               // stage state
+    const T *kbu, *kbv;             // kbar of this stage
+    const T *ybu, *ybv;             // ybar of the step
+    T *accu, *accv;                 // ybar_n accumulator (+= Ybar)
+    T *next_u, *next_v;             // kbar of the previous stage, or null
+    double cy, cY;                  // next kbar = cy ybar + cY Ybar
+    double Du, Dv, F, K;
+};
+template <typename T>
+cudaError_t rk_stage(const RkArgs<T>& a, int lanes, cudaStream_t s);
+template <typename T>
+cudaError_t rk_adjoint_stage(const RkAdjArgs<T>& a, cudaStream_t s);
+template <typename T>
+cudaError_t rk_transpose_weights(const int64_t* rowptr, const int64_t* tidx, int64_t n, int64_t nnz, const T* w,
+                                 T* wT, T* rs, cudaStream_t s);
+
 int num_sms();
 
 // Records msg as this thread's dcpse_last_error() and returns code.

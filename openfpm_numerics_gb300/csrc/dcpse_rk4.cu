@@ -1,0 +1,188 @@
+// dcpse_rk4.cu -- classic RK4 for two-species reaction-diffusion with a
+// DC-PSE Laplacian (the Gray-Scott system), forward and adjoint stages.
+//
+// Replaces the reference's pattern of boost::numeric::odeint::runge_kutta4
+// over openfpm state types with the DC-PSE Laplacian evaluated on the host
+// every stage (src/OdeIntegrators/tests/OdeIntegratores_base_tests.cpp:33-72,
+// 478-577; GPU algebra for_each*_ker in vector_algebra_ofp_gpu.hpp:13-190).
+// Here one kernel per stage does the two Laplacian gathers (one weight
+// stream, both species), the reaction terms and the RK4 stage update:
+//   du = Du L u - u v^2 + F (1 - u),   dv = Dv L v + u v^2 - (F + k) v
+//   Y1 = y; Y2 = y + dt/2 k1; Y3 = y + dt/2 k2; Y4 = y + dt k3;
+//   y' = y + dt/6 (k1 + 2 k2 + 2 k3 + k4).
+// The adjoint stage computes J(Y)^T kbar with L^T through the transposed
+// neighbour list:
+//   ubar = Du L^T kbar_u - (v^2 + F) kbar_u + v^2 kbar_v
+//   vbar = Dv L^T kbar_v - 2 u v kbar_u + (2 u v - F - k) kbar_v
+// and the reverse RK4 recursion
+//   kbar4 = dt/6 ybar; Ybar4 = J4^T kbar4; kbar3 = dt/3 ybar + dt Ybar4;
+//   Ybar3 = J3^T kbar3; kbar2 = dt/3 ybar + dt/2 Ybar3; Ybar2 = J2^T kbar2;
+//   kbar1 = dt/6 ybar + dt/2 Ybar2; Ybar1 = J1^T kbar1;
+//   ybar_n = ybar + Ybar1 + Ybar2 + Ybar3 + Ybar4.
+#include "dcpse_internal.h"
+
+namespace dcpse {
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T tfma(T a, T b, T c);
+template <>
+__device__ __forceinline__ float tfma<float>(float a, float b, float c) {
+    return fmaf(a, b, c);
+}
+template <>
+__device__ __forceinline__ double tfma<double>(double a, double b, double c) {
+    return fma(a, b, c);
+}
+
+template <typename T, int G>
+__global__ void __launch_bounds__(256) gs_stage_kernel(RkArgs<T> a) {
+    const int lane = threadIdx.x & 31;
+    const int sub = lane & (G - 1);
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t rows_per_pass = ((int64_t)gridDim.x * blockDim.x) / G;
+    const int64_t first = (tid - lane) / G;
+    for (int64_t base = first; base < a.n; base += rows_per_pass) {
+        const int64_t row = base + lane / G;
+        T lu = 0, lv = 0;
+        T up = 0, vp = 0;
+        if (row < a.n) {
+            up = a.Yu[row];
+            vp = a.Yv[row];
+            const int64_t rb = a.rowptr[row];
+            const int k = (int)(a.rowptr[row + 1] - rb);
+            const int32_t* c = a.cols + rb;
+            const T* w = a.w + rb;
+            for (int j = sub; j < k; j += G) {
+                const int32_t q = c[j];
+                const T wq = w[j];
+                lu = tfma<T>(wq, a.Yu[q] - up, lu);
+                lv = tfma<T>(wq, a.Yv[q] - vp, lv);
+            }
+        }
+#pragma unroll
+        for (int m = G / 2; m > 0; m >>= 1) {
+            lu += __shfl_xor_sync(0xffffffffu, lu, m);
+            lv += __shfl_xor_sync(0xffffffffu, lv, m);
+        }
+        if (row < a.n && sub == 0) {
+            const T uvv = up * vp * vp;
+            const T ku = (T)a.Du * lu - uvv + (T)a.F * ((T)1 - up);
+            const T kv = (T)a.Dv * lv + uvv - ((T)a.F + (T)a.K) * vp;
+            const T dt = (T)a.dt;
+            const T y0u = a.y0u[row], y0v = a.y0v[row];
+            switch (a.stage) {
+                case 0:
+                    a.accu[row] = ku;
+                    a.accv[row] = kv;
+                    a.outu[row] = y0u + (dt / (T)2) * ku;
+                    a.outv[row] = y0v + (dt / (T)2) * kv;
+                    break;
+                case 1:
+                    a.accu[row] += (T)2 * ku;
+                    a.accv[row] += (T)2 * kv;
+                    a.outu[row] = y0u + (dt / (T)2) * ku;
+                    a.outv[row] = y0v + (dt / (T)2) * kv;
+                    break;
+                case 2:
+                    a.accu[row] += (T)2 * ku;
+                    a.accv[row] += (T)2 * kv;
+                    a.outu[row] = y0u + dt * ku;
+                    a.outv[row] = y0v + dt * kv;
+                    break;
+                default:
+                    a.outu[row] = y0u + (dt / (T)6) * (a.accu[row] + ku);
+                    a.outv[row] = y0v + (dt / (T)6) * (a.accv[row] + kv);
+                    break;
+            }
+        }
+    }
+}
+
+// adjoint stage: thread per particle over the transposed list
+template <typename T>
+__global__ void __launch_bounds__(256) gs_adjoint_kernel(RkAdjArgs<T> a) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.n; p += (int64_t)gridDim.x * blockDim.x) {
+        T lu = 0, lv = 0;
+        for (int64_t t = a.trow[p]; t < a.trow[p + 1]; ++t) {
+            const int32_t s = a.tsrc[t];
+            const T w = a.wT[t];
+            lu = tfma<T>(w, a.kbu[s], lu);
+            lv = tfma<T>(w, a.kbv[s], lv);
+        }
+        const T kbu = a.kbu[p], kbv = a.kbv[p];
+        lu = lu - a.rs[p] * kbu;
+        lv = lv - a.rs[p] * kbv;
+        const T u = a.Yu[p], v = a.Yv[p];
+        const T Ybu = (T)a.Du * lu - (v * v + (T)a.F) * kbu + v * v * kbv;
+        const T Ybv = (T)a.Dv * lv - (T)2 * u * v * kbu + ((T)2 * u * v - (T)a.F - (T)a.K) * kbv;
+        a.accu[p] += Ybu;
+        a.accv[p] += Ybv;
+        if (a.next_u) {
+            a.next_u[p] = (T)a.cy * a.ybu[p] + (T)a.cY * Ybu;
+            a.next_v[p] = (T)a.cy * a.ybv[p] + (T)a.cY * Ybv;
+        }
+    }
+}
+
+template <typename T>
+__global__ void gather_kernel(const int64_t* __restrict__ tidx, int64_t nnz, const T* __restrict__ w,
+                              T* __restrict__ wT) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nnz; t += (int64_t)gridDim.x * blockDim.x)
+        wT[t] = w[tidx[t]];
+}
+
+template <typename T>
+__global__ void rowsum_t_kernel(const int64_t* __restrict__ rowptr, int64_t n, const T* __restrict__ w,
+                                T* __restrict__ rs) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        T s = 0;
+        for (int64_t j = rowptr[p]; j < rowptr[p + 1]; ++j) s += w[j];
+        rs[p] = s;
+    }
+}
+
+int grid_n(int64_t items, int per_block) {
+    int64_t g = (items + per_block - 1) / per_block, cap = (int64_t)num_sms() * 8;
+    return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t rk_stage(const RkArgs<T>& a, int lanes, cudaStream_t s) {
+    if (a.n == 0) return cudaSuccess;
+    switch (lanes) {
+        case 4: gs_stage_kernel<T, 4><<<grid_n(a.n, 64), 256, 0, s>>>(a); break;
+        case 8: gs_stage_kernel<T, 8><<<grid_n(a.n, 32), 256, 0, s>>>(a); break;
+        case 16: gs_stage_kernel<T, 16><<<grid_n(a.n, 16), 256, 0, s>>>(a); break;
+        default: gs_stage_kernel<T, 32><<<grid_n(a.n, 8), 256, 0, s>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t rk_adjoint_stage(const RkAdjArgs<T>& a, cudaStream_t s) {
+    if (a.n == 0) return cudaSuccess;
+    gs_adjoint_kernel<T><<<grid_n(a.n, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t rk_transpose_weights(const int64_t* rowptr, const int64_t* tidx, int64_t n, int64_t nnz, const T* w,
+                                 T* wT, T* rs, cudaStream_t s) {
+    if (nnz > 0) gather_kernel<T><<<grid_n(nnz, 256), 256, 0, s>>>(tidx, nnz, w, wT);
+    if (n > 0) rowsum_t_kernel<T><<<grid_n(n, 256), 256, 0, s>>>(rowptr, n, w, rs);
+    return cudaGetLastError();
+}
+
+template cudaError_t rk_stage<float>(const RkArgs<float>&, int, cudaStream_t);
+template cudaError_t rk_stage<double>(const RkArgs<double>&, int, cudaStream_t);
+template cudaError_t rk_adjoint_stage<float>(const RkAdjArgs<float>&, cudaStream_t);
+template cudaError_t rk_adjoint_stage<double>(const RkAdjArgs<double>&, cudaStream_t);
+template cudaError_t rk_transpose_weights<float>(const int64_t*, const int64_t*, int64_t, int64_t, const float*,
+                                                 float*, float*, cudaStream_t);
+template cudaError_t rk_transpose_weights<double>(const int64_t*, const int64_t*, int64_t, int64_t, const double*,
+                                                  double*, double*, cudaStream_t);
+
+}  // namespace dcpse

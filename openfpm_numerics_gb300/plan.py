@@ -94,6 +94,11 @@ class DcpsePlan:
             pass
 
     # -- set-up ---------------------------------------------------------
+    def set_stream(self, stream):
+        """Enqueue the plan's work on a torch.cuda.Stream (None = legacy default)."""
+        C.call("dcpse_plan_set_stream", self._h, _stream_ptr(stream))
+        self.stream = stream
+
     def set_box(self, lo, hi, periodic=None):
         lo = (ctypes.c_double * self.dim)(*[float(x) for x in lo])
         hi = (ctypes.c_double * self.dim)(*[float(x) for x in hi])
