@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--nside", type=int, default=128)
     ap.add_argument("--cpu-sample", type=int, default=32768, help="particles in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["apply", "assemble"], default=None,
+    ap.add_argument("--only", choices=["apply", "assemble", "gray-scott"], default=None,
                     help="small-footprint run of one kernel family (for profiler captures)")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--mode", type=int, default=0, help="apply loading: 0 auto, 1 direct, 2 TMA-staged")
@@ -403,6 +403,68 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_gray_scott(args):
+    """3D Gray-Scott on 96^3 = 884,736 jittered particles in a periodic unit
+    cube (jitter +-0.1h, seed 6), DC-PSE Laplacian order 2, rCut = 2.8h, two
+    FP32 species, Du=2e-5, Dv=1e-5, F=0.04, k=0.06, dt = 0.2 h^2/Du,
+    1000 RK4 steps replayed from CUDA graphs of 10 steps; then the gradient of
+    sum(v_final) with respect to v 100 steps earlier by the checkpointed
+    adjoint (checkpoints every 10 steps)."""
+    import torch
+
+    from openfpm_numerics_gb300 import _capi as C
+    from openfpm_numerics_gb300 import workloads as W
+    from openfpm_numerics_gb300.odeint import GrayScottRK4
+    from openfpm_numerics_gb300.plan import DcpsePlan
+
+    torch.cuda.set_device(0)
+    nside = args.nside if args.nside != 128 else 96
+    cfg = W.config5(nside)
+    s = torch.cuda.Stream()
+    plan = DcpsePlan(3, [[(2, 0, 0), (0, 2, 0), (0, 0, 2)]], box=cfg["box"], stream=s)
+    pos = torch.tensor(cfg["pos"], device="cuda")
+    with torch.cuda.stream(s):
+        plan.build_neighbors(pos, cfg["rcut"])
+        plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
+        u0, v0 = W.gray_scott_initial(cfg["pos"])
+        u = torch.tensor(u0, device="cuda", dtype=torch.float32)
+        v = torch.tensor(v0, device="cuda", dtype=torch.float32)
+    s.synchronize()
+    Du, Dv, F, K = 2e-5, 1e-5, 0.04, 0.06
+    dt = 0.2 * cfg["h"] ** 2 / Du
+    gs = GrayScottRK4(plan, u, v, Du, Dv, F, K, dt)
+    gs.capture(10, s)  # includes one eager warm-up step
+    total, window, every = 1000, 100, 10
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(s):
+        ev0.record(s)
+        gs.run(total - 1 - window - 9)  # steps before the backward window (graph multiples)
+        ev1.record(s)
+    s.synchronize()
+    t_fwd = ev0.elapsed_time(ev1) / (total - 1 - window - 9)
+    with torch.cuda.stream(s):
+        for _ in range(9):
+            gs.step()
+        ckpts = []
+        for _ in range(window // every):
+            ckpts.append((gs.u.clone(), gs.v.clone()))
+            gs.run(every)
+        s.synchronize()
+        ybar = (torch.zeros_like(gs.u), torch.ones_like(gs.v))
+        ev0.record(s)
+        ub, vb = gs.backward(ckpts, every, ybar)
+        ev1.record(s)
+    s.synchronize()
+    t_bwd = ev0.elapsed_time(ev1)
+    res = {"only": "gray-scott", "particles": pos.shape[0], "nnz": plan.info()["nnz"], "steps": total,
+           "ms_per_step_graph": t_fwd, "backward_window_steps": window, "checkpoint_every": every,
+           "backward_ms": t_bwd, "backward_ms_per_step": t_bwd / window,
+           "v_final_mean": float(gs.v.mean()), "grad_v_norm": float(vb.norm()),
+           "finite": bool(torch.isfinite(gs.v).all() and torch.isfinite(vb).all())}
+    plan.check()
+    print(json.dumps(res), flush=True)
+
+
 def run_only(args):
     """One kernel family on the benchmark geometry, nothing else resident:
     --only apply keeps just the FP32 weights (fast assembly), --only assemble
@@ -413,6 +475,9 @@ def run_only(args):
     from openfpm_numerics_gb300 import workloads as W
     from openfpm_numerics_gb300.plan import DcpsePlan
 
+    if args.only == "gray-scott":
+        run_gray_scott(args)
+        return
     torch.cuda.set_device(0)
     cfg = W.config2(args.nside)
     pos = torch.tensor(cfg["pos"], device="cuda")
