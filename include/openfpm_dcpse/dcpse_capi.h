@@ -236,6 +236,10 @@ int dcpse_plan_set_timing(dcpse_plan_t* plan, int enable);
  * outputs with a term of order >= 2 do; the others take plain fused sums). */
 #define DCPSE_APPLY_COMPENSATE_ALL 16
 int dcpse_plan_set_apply_config(dcpse_plan_t* plan, int lanes, int mode);
+/* Assembly schedule knobs (autotuning): particles are processed in bins of
+ * neighbour count of width bin_width (0 = index order; uneven clouds keep
+ * warps of one CTA on similar work) by CTAs of `warps` warps (2, 4 or 8). */
+int dcpse_plan_set_assembly_config(dcpse_plan_t* plan, int bin_width, int warps);
 /* Synchronises the stream and reports DCPSE_ERR_TIMEOUT if a kernel's
  * bounded wait ran out since the plan was created. */
 int dcpse_plan_check(dcpse_plan_t* plan);

@@ -45,3 +45,25 @@ def tune_apply(plan, f, precision=C.F32, lanes=(4, 8, 16), modes=(1, 2, 3), reps
     plan.set_apply_config(best[0], best[1])
     plan.check()
     return {"lanes": best[0], "mode": MODES[best[1]], "ms": best[2], "sweep": table}
+
+
+def tune_assembly(plan, pos, flags, bin_widths=(0, 4, 16), warps=(2, 4, 8), reps=1):
+    """Sweeps the neighbour-count bin width and the warps per CTA of the
+    persistent assembly launch (device time from the plan's event timers);
+    keeps the fastest."""
+    plan.set_timing(True)
+    table = []
+    best = None
+    for bw in bin_widths:
+        for wp in warps:
+            plan.set_assembly_config(bw, wp)
+            plan.assemble(pos, flags)  # warm-up (and the binning for this width)
+            plan.reset_timing()
+            for _ in range(reps):
+                plan.assemble(pos, flags)
+            ms = plan.timing(C.K_ASSEMBLE)[0] / reps
+            table.append({"bin_width": bw, "warps": wp, "ms": ms})
+            if best is None or ms < best[2]:
+                best = (bw, wp, ms)
+    plan.set_assembly_config(best[0], best[1])
+    return {"bin_width": best[0], "warps": best[1], "ms": best[2], "sweep": table}

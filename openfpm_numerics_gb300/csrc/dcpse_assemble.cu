@@ -24,6 +24,7 @@
 // explicit fma calls), so the FP64 kernels equal the oracle's bit for bit.
 // Neighbour rows are processed in chunks of 32 (one row per lane), so any
 // neighbour count is handled with fixed shared memory.
+#include <algorithm>
 #include <cstdio>
 
 #include <cuda_bf16.h>
@@ -78,7 +79,7 @@ __device__ __forceinline__ void load_offset(const AsmArgs& a, const double* xp, 
 }
 
 template <int DIM, int MAXE, int NPP>
-__global__ void __launch_bounds__(kWarps * 32) assemble_kernel(AsmArgs a, Layout L) {
+__global__ void __launch_bounds__(256) assemble_kernel(AsmArgs a, Layout L) {
     extern __shared__ double smem[];
     const AsmTables& T = *a.tab;
     const int lane = threadIdx.x & 31;
@@ -107,9 +108,11 @@ __global__ void __launch_bounds__(kWarps * 32) assemble_kernel(AsmArgs a, Layout
         pj[t] = (e < npairs) ? T.pj[e] : 0;
     }
 
-    const int64_t gw = ((int64_t)blockIdx.x * kWarps + wib);
-    const int64_t nw = (int64_t)gridDim.x * kWarps;
-    for (int64_t p = gw; p < a.n; p += nw) {
+    const int wpc = blockDim.x >> 5;
+    const int64_t gw = ((int64_t)blockIdx.x * wpc + wib);
+    const int64_t nw = (int64_t)gridDim.x * wpc;
+    for (int64_t it = gw; it < a.n; it += nw) {
+        const int64_t p = a.order ? (int64_t)a.order[it] : it;
         const int64_t beg = a.rowptr[p];
         const int k = (int)(a.rowptr[p + 1] - beg);
         double xp[DIM];
@@ -404,20 +407,34 @@ __global__ void __launch_bounds__(kWarps * 32) assemble_kernel(AsmArgs a, Layout
 
 template <int DIM, int MAXE, int NPP>
 cudaError_t launch(const AsmArgs& a, const Layout& L, cudaStream_t s) {
-    size_t bytes = (size_t)L.words * sizeof(double) * kWarps;
+    const int warps = (a.warps == 2 || a.warps == 8) ? a.warps : kWarps;
+    size_t bytes = (size_t)L.words * sizeof(double) * warps;
     auto kern = assemble_kernel<DIM, MAXE, NPP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, bytes);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, bytes);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    int64_t need = (a.n + kWarps - 1) / kWarps;
+    int64_t need = (a.n + warps - 1) / warps;
     int64_t grid = (int64_t)num_sms() * per_sm;
     if (grid > need) grid = need;
     if (grid < 1) grid = 1;
-    kern<<<(unsigned)grid, kWarps * 32, bytes, s>>>(a, L);
+    kern<<<(unsigned)grid, warps * 32, bytes, s>>>(a, L);
     return cudaGetLastError();
+}
+
+__global__ void khist_kernel(const int64_t* __restrict__ rowptr, int64_t n, int width, int32_t* __restrict__ hist) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&hist[(int)(rowptr[p + 1] - rowptr[p]) / width], 1);
+}
+
+__global__ void kscatter_kernel(const int64_t* __restrict__ rowptr, int64_t n, int width, int64_t* fill,
+                                int32_t* __restrict__ order) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const int b = (int)(rowptr[p + 1] - rowptr[p]) / width;
+        order[atomicAdd((unsigned long long*)&fill[b], 1ull)] = (int32_t)p;
+    }
 }
 
 template <int DIM>
@@ -432,6 +449,28 @@ cudaError_t dispatch(const AsmArgs& a, const AsmTables& h, const Layout& L, cuda
 }
 
 }  // namespace
+
+int64_t binning_tmp_elems(int64_t n, int maxk, int width) {
+    const int64_t nb = maxk / (width > 0 ? width : 1) + 1;
+    return nb + 1 + scan_tmp_elems(nb);
+}
+
+cudaError_t bin_by_count(const int64_t* rowptr, int64_t n, int maxk, int width, int32_t* order, int32_t* hist,
+                         int64_t* tmp64, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if (width < 1) width = 1;
+    const int64_t nb = maxk / width + 1;
+    int64_t* starts = tmp64;            // nb + 1
+    int64_t* scan_tmp = tmp64 + nb + 1;
+    cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(int32_t) * nb, s);
+    if (e != cudaSuccess) return e;
+    const int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 8);
+    khist_kernel<<<grid, 256, 0, s>>>(rowptr, n, width, hist);
+    e = exclusive_scan_i32(hist, nb, starts, scan_tmp, s);
+    if (e != cudaSuccess) return e;
+    kscatter_kernel<<<grid, 256, 0, s>>>(rowptr, n, width, starts, order);
+    return cudaGetLastError();
+}
 
 cudaError_t assemble(const AsmArgs& a, const AsmTables& h, cudaStream_t s) {
     if (a.n == 0) return cudaSuccess;

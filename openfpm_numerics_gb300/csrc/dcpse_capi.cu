@@ -199,6 +199,9 @@ struct dcpse_plan_s {
     unsigned long long* summary = nullptr;  // [count, first]
     int* d_err = nullptr;                   // set by kernels whose bounded wait ran out
     int apply_lanes = 0, apply_mode = 0;
+    int asm_bin_width = 0, asm_warps = 4;
+    int32_t* korder = nullptr;  // k-binned particle order of the current list
+    int korder_width = 0;
     // transposed list and weight row sums (adjoint), built on demand
     int64_t* t_row = nullptr;
     int32_t* t_src = nullptr;
@@ -210,6 +213,8 @@ struct dcpse_plan_s {
     float *wT32 = nullptr, *rs32 = nullptr;
     double *wT64 = nullptr, *rs64 = nullptr;
     void free_transpose() {
+        dfree(korder);
+        korder_width = 0;
         dfree(t_row);
         dfree(t_src);
         dfree(t_idx);
@@ -738,6 +743,25 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     a.w32 = P->w32;
     a.r16 = P->r16;
     a.nnz = nnz;
+    a.warps = P->asm_warps;
+    a.order = nullptr;
+    if (P->asm_bin_width > 0 && n > 0) {
+        if (!P->korder || P->korder_width != P->asm_bin_width) {
+            if (!P->korder) DCPSE_CK(dalloc(&P->korder, n));
+            const int64_t nb = P->maxk / P->asm_bin_width + 1;
+            int32_t* hist = nullptr;
+            int64_t* tmp = nullptr;
+            DCPSE_CK(dalloc(&hist, nb));
+            DCPSE_CK(dalloc(&tmp, binning_tmp_elems(n, P->maxk, P->asm_bin_width)));
+            cudaError_t eb = bin_by_count(P->rowptr, n, P->maxk, P->asm_bin_width, P->korder, hist, tmp, s);
+            if (eb == cudaSuccess) eb = cudaStreamSynchronize(s);
+            dfree(hist);
+            dfree(tmp);
+            DCPSE_CK(eb);
+            P->korder_width = P->asm_bin_width;
+        }
+        a.order = P->korder;
+    }
     P->tstart(DCPSE_K_ASSEMBLE);
     cudaError_t e = assemble(a, *P->htab, s);
     P->tstop(DCPSE_K_ASSEMBLE);
@@ -1139,6 +1163,15 @@ int dcpse_plan_set_apply_config(dcpse_plan_t* P, int lanes, int mode) {
         return fail(DCPSE_ERR_ARG, "mode must be 0..3, optionally | DCPSE_APPLY_COMPENSATE_ALL");
     P->apply_lanes = lanes;
     P->apply_mode = mode;
+    return DCPSE_OK;
+}
+
+int dcpse_plan_set_assembly_config(dcpse_plan_t* P, int bin_width, int warps) {
+    if (int rc = check_plan(P)) return rc;
+    if (bin_width < 0) return fail(DCPSE_ERR_ARG, "bin_width must be >= 0");
+    if (warps != 2 && warps != 4 && warps != 8) return fail(DCPSE_ERR_ARG, "warps must be 2, 4 or 8");
+    P->asm_bin_width = bin_width;
+    P->asm_warps = warps;
     return DCPSE_OK;
 }
 

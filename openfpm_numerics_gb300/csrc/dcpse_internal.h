@@ -112,7 +112,16 @@ struct AsmArgs {
     float* w32;          // [noutputs][nnz] or nullptr
     void* r16;           // bf16 [noutputs][nnz]: w64 - w32, or nullptr
     int64_t nnz;
+    const int32_t* order; // processing order of the particles (k-binned) or nullptr
+    int warps;            // warps per CTA (2, 4 or 8)
 };
+
+// Particle order binned by neighbour count: bins of `width` counts
+// ascending (a counting sort on k / width); order[n], tmp sized by
+// binning_tmp_elems.
+int64_t binning_tmp_elems(int64_t n, int maxk, int width);
+cudaError_t bin_by_count(const int64_t* rowptr, int64_t n, int maxk, int width, int32_t* order, int32_t* tmp32,
+                         int64_t* tmp64, cudaStream_t s);
 
 // h: host copy of *a.tab (launch configuration is derived from it)
 cudaError_t assemble(const AsmArgs& a, const AsmTables& h, cudaStream_t s);

@@ -221,6 +221,23 @@ def test_apply_schedules(cuda, orc, name):
     plan.set_apply_config(0, 0)
 
 
+@pytest.mark.parametrize("name", ["2d_adaptive", "3d"])
+def test_assembly_schedules_bitexact(cuda, orc, name):
+    """Neighbour-count binning and CTA size change the schedule only."""
+    c = _case(name)
+    plan, pos, _ = _build(c)
+    ref = [plan.term_kernels(t)[0].clone() for t in range(plan.n_terms)]
+    for bw, wp in ((4, 2), (16, 8), (1, 4)):
+        plan.set_assembly_config(bw, wp)
+        plan.assemble(pos, C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+        for t in range(plan.n_terms):
+            assert torch.equal(plan.term_kernels(t)[0], ref[t]), (bw, wp, t)
+    from openfpm_numerics_gb300 import autotune
+
+    best = autotune.tune_assembly(plan, pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
+    assert len(best["sweep"]) == 9 and best["warps"] in (2, 4, 8)
+
+
 def test_autotune(cuda):
     from openfpm_numerics_gb300 import autotune
 
