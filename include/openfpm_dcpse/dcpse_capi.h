@@ -228,6 +228,10 @@ int dcpse_apply_batched_f32_noalloc(int64_t n, int n_outputs, const int64_t* d_r
 #define DCPSE_K_NEIGHBORS 4
 #define DCPSE_K_COUNT 5
 int dcpse_plan_set_timing(dcpse_plan_t* plan, int enable);
+/* Measured FP64 fused multiply-add throughput of the current GPU in TFLOP/s
+ * (2 flops per FMA): the ceiling the FP64 assembly is reported against.
+ * No counterpart in the reference. */
+int dcpse_measure_fp64_peak(void* stream, double* tflops);
 /* Apply schedule knobs (autotuning): lanes per row (0 = from the mean row
  * length, else 4/8/16/32) and loading mode (0 = TMA-staged when the tiles
  * fit in shared memory, 1 = direct loads, 2 = staged, 3 = direct loads with
