@@ -49,6 +49,7 @@ def parse():
                     help="small-footprint run of one kernel family (for profiler captures)")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--mode", type=int, default=0, help="apply loading: 0 auto, 1 direct, 2 TMA-staged")
+    ap.add_argument("--qr-lanes", type=int, default=0, help="assembly QR lanes per particle (0 = automatic)")
     return ap.parse_args()
 
 
@@ -577,6 +578,7 @@ def run_only(args):
         res["apply_ms"] = ms / max(k, 1)
         res["achieved_gbs"] = W.apply_bytes(N, nnz, NOUT, 4) / (ms / max(k, 1) / 1e3) / 1e9
     else:
+        plan.set_assembly_config(0, 4, args.qr_lanes)
         for _ in range(max(1, args.steps)):
             plan.reset_timing()
             plan.assemble(pos, C.STORE_TERMS_F64)

@@ -242,8 +242,13 @@ int dcpse_measure_fp64_peak(void* stream, double* tflops);
 int dcpse_plan_set_apply_config(dcpse_plan_t* plan, int lanes, int mode);
 /* Assembly schedule knobs (autotuning): particles are processed in bins of
  * neighbour count of width bin_width (0 = index order; uneven clouds keep
- * warps of one CTA on similar work) by CTAs of `warps` warps (2, 4 or 8). */
-int dcpse_plan_set_assembly_config(dcpse_plan_t* plan, int bin_width, int warps);
+ * warps of one CTA on similar work); the Gram and weight kernels run CTAs of
+ * `warps` warps (2, 4 or 8); the QR kernel factorises each particle's
+ * matrices with qr_lanes lanes (1, 2, 4, 8, 16 or 32; 0 = the fewest that
+ * keep 6 warps per SM resident).  A lane count whose work space exceeds
+ * shared memory makes dcpse_assemble return DCPSE_ERR_CAPACITY.  None of
+ * these changes a result bit. */
+int dcpse_plan_set_assembly_config(dcpse_plan_t* plan, int bin_width, int warps, int qr_lanes);
 /* Synchronises the stream and reports DCPSE_ERR_TIMEOUT if a kernel's
  * bounded wait ran out since the plan was created. */
 int dcpse_plan_check(dcpse_plan_t* plan);

@@ -57,7 +57,7 @@ SIGNATURES = {
     "dcpse_copy": (_I, [_P, _P, _c.c_uint64]),
     "dcpse_plan_set_timing": (_I, [_P, _I]),
     "dcpse_plan_set_apply_config": (_I, [_P, _I, _I]),
-    "dcpse_plan_set_assembly_config": (_I, [_P, _I, _I]),
+    "dcpse_plan_set_assembly_config": (_I, [_P, _I, _I, _I]),
     "dcpse_measure_fp64_peak": (_I, [_P, _c.POINTER(_D)]),
     "dcpse_plan_check": (_I, [_P]),
     "dcpse_plan_timing": (_I, [_P, _I, _c.POINTER(_D), _PI64]),

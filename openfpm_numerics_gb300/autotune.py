@@ -47,23 +47,38 @@ def tune_apply(plan, f, precision=C.F32, lanes=(4, 8, 16), modes=(1, 2, 3), reps
     return {"lanes": best[0], "mode": MODES[best[1]], "ms": best[2], "sweep": table}
 
 
-def tune_assembly(plan, pos, flags, bin_widths=(0, 4, 16), warps=(2, 4, 8), reps=1):
+def tune_assembly(plan, pos, flags, bin_widths=(0, 4, 16), warps=(2, 4, 8), qr_lanes=(2, 4, 8, 16), reps=1):
     """Sweeps the neighbour-count bin width and the warps per CTA of the
-    persistent assembly launch (device time from the plan's event timers);
-    keeps the fastest."""
+    Gram and weight kernels, then the lanes per particle of the QR kernel
+    (device time from the plan's event timers); keeps the fastest.  Lane
+    counts whose work space does not fit in shared memory are skipped."""
     plan.set_timing(True)
     table = []
+
+    def timed(bw, wp, ql):
+        plan.set_assembly_config(bw, wp, ql)
+        try:
+            plan.assemble(pos, flags)  # warm-up (and the binning for this width)
+        except C.DcpseError as e:
+            if e.code != C.ERR_CAPACITY:
+                raise
+            return None
+        plan.reset_timing()
+        for _ in range(reps):
+            plan.assemble(pos, flags)
+        ms = plan.timing(C.K_ASSEMBLE)[0] / reps
+        table.append({"bin_width": bw, "warps": wp, "qr_lanes": ql, "ms": ms})
+        return ms
+
     best = None
     for bw in bin_widths:
         for wp in warps:
-            plan.set_assembly_config(bw, wp)
-            plan.assemble(pos, flags)  # warm-up (and the binning for this width)
-            plan.reset_timing()
-            for _ in range(reps):
-                plan.assemble(pos, flags)
-            ms = plan.timing(C.K_ASSEMBLE)[0] / reps
-            table.append({"bin_width": bw, "warps": wp, "ms": ms})
-            if best is None or ms < best[2]:
-                best = (bw, wp, ms)
-    plan.set_assembly_config(best[0], best[1])
-    return {"bin_width": best[0], "warps": best[1], "ms": best[2], "sweep": table}
+            ms = timed(bw, wp, 0)
+            if ms is not None and (best is None or ms < best[3]):
+                best = (bw, wp, 0, ms)
+    for ql in qr_lanes:
+        ms = timed(best[0], best[1], ql)
+        if ms is not None and ms < best[3]:
+            best = (best[0], best[1], ql, ms)
+    plan.set_assembly_config(best[0], best[1], best[2])
+    return {"bin_width": best[0], "warps": best[1], "qr_lanes": best[2], "ms": best[3], "sweep": table}

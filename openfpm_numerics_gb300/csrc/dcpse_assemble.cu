@@ -5,25 +5,35 @@
 // 620-717: per-thread global scratch B, cuBLAS batched LU without pivoting,
 // a separate calcKernels_gpu pass and host round trips).
 //
-// One warp per particle, persistent grid.  For particle p with k neighbours:
-//  1. eps   = (sum_q sum_d |x_pq,d|) / k / HOverEpsilon   (Vandermonde.hpp:63-81)
-//  2. Gram  A_ij = sum_q B_qi B_qj,  B_qj = E_q V_qj,
-//           V_qj = m_j(x_pq/eps), E_q = exp(-|x_pq|^2 / (2 eps^2))
-//           (Vandermonde.hpp:36-49, DcpseDiagonalScalingMatrix.hpp:21-41,
-//            Dcpse.hpp:755-757).  Computed once over the union of the bases
-//           of all terms of the plan (Dx,Dy,Dz share one basis, Dxx,Dyy,Dzz
-//           another); each lane owns Gram entries and accumulates them over q
-//           in neighbour order.
-//  3. Solve A a = b for every right-hand side of each basis with a
-//           warp-parallel column-pivoting Householder QR (Businger-Golub; the
-//           role of Eigen's colPivHouseholderQr at Dcpse.hpp:766).
-//  4. K_q = exp(-|x_pq/eps|^2) sum_i a_i V_qi        (Dcpse.hpp:768-809)
+// Particles are assembled in batches, each by three kernels that hand their
+// results over through a plan-owned scratch buffer:
+//  1. gram_kernel (one warp per particle)
+//       eps  = (sum_q sum_d |x_pq,d|) / k / HOverEpsilon   (Vandermonde.hpp:63-81)
+//       Gram A_ij = sum_q B_qi B_qj,  B_qj = E_q V_qj,
+//            V_qj = m_j(x_pq/eps), E_q = exp(-|x_pq|^2 / (2 eps^2))
+//            (Vandermonde.hpp:36-49, DcpseDiagonalScalingMatrix.hpp:21-41,
+//             Dcpse.hpp:755-757).  Computed once over the union of the bases
+//            of all terms (Dx,Dy,Dz share one basis, Dxx,Dyy,Dzz another);
+//            each lane owns Gram entries and accumulates them over q in
+//            neighbour order.  Written to scratch with a status word per
+//            particle (4 bits per basis group).
+//  2. qr_kernel (a group of LPP lanes per particle, 32/LPP particles per
+//       warp): solve A a = b for every right-hand side of each basis with
+//       column-pivoting Householder QR (Businger-Golub; the role of Eigen's
+//       colPivHouseholderQr at Dcpse.hpp:766), columns split over the lanes
+//       of the group.  The QR is a long chain of scalar steps (pivot search,
+//       square root, divisions); with few lanes per particle one warp
+//       instruction advances many particles, which is what the FP64 pipe of
+//       this part needs.  Coefficients go back to scratch.
+//  3. weights_kernel (one warp per particle)
+//       K_q = exp(-|x_pq/eps|^2) sum_i a_i V_qi        (Dcpse.hpp:768-809)
 //
 // Every floating-point operation follows the order of the CPU oracle, and
 // this translation unit is compiled with -fmad=false (fused multiply-adds are
-// explicit fma calls), so the FP64 kernels equal the oracle's bit for bit.
-// Neighbour rows are processed in chunks of 32 (one row per lane), so any
-// neighbour count is handled with fixed shared memory.
+// explicit fma calls), so the FP64 kernels equal the oracle's bit for bit
+// whatever the batch size, lane grouping or CTA size.  Neighbour rows are
+// processed in chunks of 32 (one row per lane), so any neighbour count is
+// handled with fixed shared memory.
 #include <algorithm>
 #include <cstdio>
 
@@ -34,43 +44,25 @@
 namespace dcpse {
 namespace {
 
-constexpr int kWarps = 4;  // warps per CTA
+constexpr int kWarps = 4;  // warps per CTA of the Gram and weight kernels
 constexpr int kCh = 32;    // neighbour rows per chunk
-constexpr int kRhs = 8;    // right-hand sides per basis held in registers
+constexpr int kQrWarps = 2;  // warps per CTA of the QR kernel
 
-struct Layout {
-    int ldb;        // row stride of the B chunk (doubles)
-    int ldr;        // row stride of the QR work matrix
-    int nmax;       // largest basis
-    int off_b, off_g, off_r, off_z, off_a, off_perm, words;  // offsets in doubles
-    int a_off[kMaxGroups];  // coefficient block of each group inside A region
+// Scratch layout and shared-memory sizes of one assembly.
+struct Split {
+    int gstride;             // doubles of Gram entries per particle
+    int cstride;             // doubles of coefficients per particle
+    int nrhs[kMaxGroups];    // right-hand sides per group (per term or per output)
+    int c_off[kMaxGroups];   // coefficient block of each group, [gn][nrhs]
+    int nmax, rmax, ldr;     // largest basis, most right-hand sides, row stride of [A|b]
+    int pstride;             // doubles of QR work space per particle (set per lane grouping)
+    int ldb;                 // row stride of the B chunk of the Gram kernel
+    int nslots;              // monomial program slots per lane
+    int nout;                // outputs of the plan
+    double* gram;            // [nb][gstride]
+    double* coef;            // [nb][cstride]
+    int32_t* gst;            // [nb] group status words
 };
-
-__device__ __forceinline__ double sel_pow(const double (&pw)[8], int e, int maxe) {
-    double r = pw[0];
-#pragma unroll
-    for (int t = 1; t < 8; ++t)
-        if (t < maxe) r = (e == t) ? pw[t] : r;
-    return r;
-}
-
-template <int DIM, int MAXE>
-__device__ __forceinline__ void powers(const double* u, double (&pw)[kMaxDim][8]) {
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-#pragma unroll
-        for (int e = 0; e < 8; ++e) pw[d][e] = (e < MAXE) ? ipow(u[d], (unsigned)e) : 0.0;
-    }
-}
-
-// m_j(u) = ((scalar * u0^e0) * u1^e1) * u2^e2 with scalar 1 (Monomial.hpp:146-156)
-template <int DIM, int MAXE>
-__device__ __forceinline__ double mono(const double (&pw)[kMaxDim][8], const unsigned char* e) {
-    double r = 1.0;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) r = r * sel_pow(pw[d], e[d], MAXE);
-    return r;
-}
 
 template <int DIM>
 __device__ __forceinline__ void load_offset(const AsmArgs& a, const double* xp, int64_t q, double* o) {
@@ -78,26 +70,94 @@ __device__ __forceinline__ void load_offset(const AsmArgs& a, const double* xp, 
     for (int d = 0; d < DIM; ++d) o[d] = offset1(a.geom, d, xp[d], a.pos[q * DIM + d]);
 }
 
-template <int DIM, int MAXE, int NPP>
-__global__ void __launch_bounds__(256) assemble_kernel(AsmArgs a, Layout L) {
-    extern __shared__ double smem[];
+__device__ __forceinline__ int group_status(int32_t word, int g) { return (word >> (4 * g)) & 15; }
+
+// isfinite on the exponent bits (integer pipe, not the FP64 one)
+__device__ __forceinline__ bool finite_bits(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
+
+// Tables every lane reads each row, staged in shared memory once per CTA.
+struct ProgShared {
+    unsigned char prog[kMaxSlots][2];
+    unsigned char uslot[kMaxUnion];
+};
+
+__device__ __forceinline__ void stage_program(const AsmTables& T, ProgShared& P) {
+    for (int e = threadIdx.x; e < T.nprog; e += blockDim.x) {
+        P.prog[e][0] = T.prog[e][0];
+        P.prog[e][1] = T.prog[e][1];
+    }
+    for (int e = threadIdx.x; e < T.nu; e += blockDim.x) P.uslot[e] = T.uslot[e];
+    __syncthreads();
+}
+
+// Monomials of the union basis at u, into this lane's column of V
+// ([slot][32]): m_j(u) = ((u0^e0) * u1^e1) * u2^e2 (Monomial.hpp:146-156)
+// with the powers by ipow's squaring steps; the program performs exactly
+// these multiplications, skipping factors equal to 1.0.
+template <int DIM>
+__device__ __forceinline__ void monomials(const double* u, double* V, const ProgShared& P, int nprog, int lane) {
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) V[d * 32 + lane] = u[d];
+    V[DIM * 32 + lane] = 1.0;
+    for (int o = 0; o < nprog; ++o)
+        V[(DIM + 1 + o) * 32 + lane] = V[P.prog[o][0] * 32 + lane] * V[P.prog[o][1] * 32 + lane];
+}
+
+// ----------------------------------------------------------------- 0. eps --
+// One thread per particle: eps = (sum_q sum_d |x_pq,d|) / k / HOverEpsilon
+// summed sequentially over q (Vandermonde::computeEps), and the status of
+// each basis group (too few neighbours for that basis, or a bad eps).
+template <int DIM>
+__global__ void __launch_bounds__(256) eps_kernel(AsmArgs a, Split S, int64_t b0, int64_t b1) {
     const AsmTables& T = *a.tab;
+    const int ngroups = T.ngroups;
+    for (int64_t it = b0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < b1;
+         it += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = a.order ? (int64_t)a.order[it] : it;
+        const int64_t beg = a.rowptr[p];
+        const int k = (int)(a.rowptr[p + 1] - beg);
+        double xp[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xp[d] = a.pos[p * DIM + d];
+        double s = 0.0;
+        for (int q = 0; q < k; ++q) {
+            double o[DIM];
+            load_offset<DIM>(a, xp, a.cols[beg + q], o);
+            double acc = 0.0;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) acc = acc + fabs(o[d]);
+            s = s + acc;
+        }
+        s = s / (double)k;
+        double eps = s / a.h_over_eps;
+        if (a.eps_fixed) eps = a.eps_fixed[p];
+        int32_t word = 0;
+        const bool eps_ok = (eps > 0.0) && isfinite(eps);
+        for (int g = 0; g < ngroups; ++g) {
+            const int st = (k < T.gn[g]) ? ST_TOO_FEW : (eps_ok ? ST_OK : ST_BAD_EPS);
+            word |= st << (4 * g);
+        }
+        a.eps[p] = eps;
+        for (int g = 0; g < ngroups; ++g) a.eip_group[(int64_t)g * a.n + p] = 1.0 / ipow(eps, (unsigned)T.gord[g]);
+        S.gst[it - b0] = word;
+    }
+}
+
+// ---------------------------------------------------------------- 1. Gram --
+template <int DIM, int NPP>
+__global__ void __launch_bounds__(256) gram_kernel(AsmArgs a, Split S, int64_t b0, int64_t b1) {
+    extern __shared__ double smem[];
+    __shared__ ProgShared P;
+    const AsmTables& T = *a.tab;
+    stage_program(T, P);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    double* S = smem + (size_t)wib * L.words;
-    double* Bs = S + L.off_b;
-    double* Gs = S + L.off_g;
-    double* R = S + L.off_r;
-    double* Z = S + L.off_z;
-    double* Acoef = S + L.off_a;
-    int* perm = reinterpret_cast<int*>(S + L.off_perm);
-
+    double* Bs = smem + (size_t)wib * (kCh * S.ldb + S.nslots * 32);
+    double* V = Bs + kCh * S.ldb;
     const int nu = T.nu;
     const int npairs = T.npairs;
     const int ngroups = T.ngroups;
-    const bool fast = (a.flags & DCPSE_ASSEMBLE_FAST_FLAG) != 0;
-    const bool st_terms = a.k_term != nullptr;
-    const int noutputs = T.noutputs;
+    const int nprog = T.nprog;
 
     // Gram entries owned by this lane
     int pi[NPP], pj[NPP];
@@ -109,121 +169,118 @@ __global__ void __launch_bounds__(256) assemble_kernel(AsmArgs a, Layout L) {
     }
 
     const int wpc = blockDim.x >> 5;
-    const int64_t gw = ((int64_t)blockIdx.x * wpc + wib);
     const int64_t nw = (int64_t)gridDim.x * wpc;
-    for (int64_t it = gw; it < a.n; it += nw) {
+    for (int64_t it = b0 + (int64_t)blockIdx.x * wpc + wib; it < b1; it += nw) {
+        const int64_t slot = it - b0;
         const int64_t p = a.order ? (int64_t)a.order[it] : it;
         const int64_t beg = a.rowptr[p];
         const int k = (int)(a.rowptr[p + 1] - beg);
+        const int32_t word = S.gst[slot];
+        bool any_ok = false;
+        for (int g = 0; g < ngroups; ++g) any_ok |= group_status(word, g) == ST_OK;
+        if (!any_ok) continue;  // warp-uniform
+        const double eps = a.eps[p];
         double xp[DIM];
 #pragma unroll
         for (int d = 0; d < DIM; ++d) xp[d] = a.pos[p * DIM + d];
 
-        // ---- 1. eps (sequential sum over q, as Vandermonde::computeEps) ----
-        double s = 0.0;
-        for (int c0 = 0; c0 < k; c0 += kCh) {
-            int q = c0 + lane;
-            double v = 0.0;
-            if (q < k) {
-                double o[DIM];
-                load_offset<DIM>(a, xp, a.cols[beg + q], o);
-                double acc = 0.0;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) acc = acc + fabs(o[d]);
-                v = acc;
-            }
-            int cnt = min(kCh, k - c0);
-            for (int t = 0; t < kCh; ++t) {
-                double w = __shfl_sync(0xffffffffu, v, t);
-                if (t < cnt) s = s + w;
-            }
-        }
-        s = s / (double)k;
-        double eps = s / a.h_over_eps;
-        if (a.eps_fixed) eps = a.eps_fixed[p];
-        // per-group status: too few neighbours for that basis, or bad eps
-        int gst[kMaxGroups];
-        bool any_ok = false;
-        const bool eps_ok = (eps > 0.0) && isfinite(eps);
-        for (int g = 0; g < ngroups; ++g) {
-            gst[g] = (k < T.gn[g]) ? ST_TOO_FEW : (eps_ok ? ST_OK : ST_BAD_EPS);
-            any_ok |= (gst[g] == ST_OK);
-        }
-        if (lane == 0) {
-            a.eps[p] = eps;
-            for (int g = 0; g < ngroups; ++g) a.eip_group[(int64_t)g * a.n + p] = 1.0 / ipow(eps, (unsigned)T.gord[g]);
-        }
-
-        // ---- 2. Gram over the union basis ----
+        // A_ij = sum_q B_qi B_qj, B_qj = E_q m_j(x_pq / eps)
         double acc[NPP];
 #pragma unroll
         for (int t = 0; t < NPP; ++t) acc[t] = 0.0;
-        if (any_ok) {
-            for (int c0 = 0; c0 < k; c0 += kCh) {
-                int q = c0 + lane;
-                const int cnt = min(kCh, k - c0);
-                if (q < k) {
-                    double o[DIM], u[DIM];
-                    load_offset<DIM>(a, xp, a.cols[beg + q], o);
+        for (int c0 = 0; c0 < k; c0 += kCh) {
+            int q = c0 + lane;
+            const int cnt = min(kCh, k - c0);
+            if (q < k) {
+                double o[DIM], u[DIM];
+                load_offset<DIM>(a, xp, a.cols[beg + q], o);
 #pragma unroll
-                    for (int d = 0; d < DIM; ++d) u[d] = o[d] / eps;
-                    double E = cw_exp(-norm2<DIM>(o) / (2.0 * eps * eps));
-                    double pw[kMaxDim][8];
-                    powers<DIM, MAXE>(u, pw);
-                    for (int j = 0; j < nu; ++j) Bs[lane * L.ldb + j] = E * mono<DIM, MAXE>(pw, T.uexp[j]);
-                }
-                __syncwarp();
-                for (int r = 0; r < cnt; ++r) {
-                    const double* row = Bs + r * L.ldb;
-#pragma unroll
-                    for (int t = 0; t < NPP; ++t)
-                        if (t * 32 + lane < npairs) acc[t] = fma(row[pi[t]], row[pj[t]], acc[t]);
-                }
-                __syncwarp();
+                for (int d = 0; d < DIM; ++d) u[d] = o[d] / eps;
+                const double E = cw_exp(-norm2<DIM>(o) / (2.0 * eps * eps));
+                monomials<DIM>(u, V, P, nprog, lane);
+                for (int j = 0; j < nu; ++j) Bs[lane * S.ldb + j] = E * V[P.uslot[j] * 32 + lane];
             }
+            __syncwarp();
+            for (int r = 0; r < cnt; ++r) {
+                const double* row = Bs + r * S.ldb;
 #pragma unroll
-            for (int t = 0; t < NPP; ++t)
-                if (t * 32 + lane < npairs) Gs[t * 32 + lane] = acc[t];
+                for (int t = 0; t < NPP; ++t)
+                    if (t * 32 + lane < npairs) acc[t] = fma(row[pi[t]], row[pj[t]], acc[t]);
+            }
             __syncwarp();
         }
+        double* G = S.gram + slot * S.gstride;
+#pragma unroll
+        for (int t = 0; t < NPP; ++t)
+            if (t * 32 + lane < npairs) G[t * 32 + lane] = acc[t];
+    }
+}
 
-        // ---- 3. per basis: column-pivoting QR solve ----
+// ------------------------------------------------------------------ 2. QR --
+// All lanes of a warp run the same loop trip counts (the basis sizes are the
+// plan's); particles differ only in their data, so every shuffle and warp
+// barrier is reached by the whole warp.  A group whose factorisation breaks
+// down (or that was not assembled) keeps running on its own work space and
+// only its stores are suppressed.
+template <int LPP>
+__global__ void __launch_bounds__(kQrWarps * 32) qr_kernel(AsmArgs a, Split S, int64_t nb) {
+    constexpr int PPW = 32 / LPP;
+    extern __shared__ double smem[];
+    const AsmTables& T = *a.tab;
+    const bool fast = (a.flags & DCPSE_ASSEMBLE_FAST_FLAG) != 0;
+    const int lane = threadIdx.x & 31;
+    const int l = lane & (LPP - 1);
+    const int sub = lane / LPP;
+    const int wib = threadIdx.x >> 5;
+    const int wpc = blockDim.x >> 5;
+    const int pidx = wib * PPW + sub;  // particle slot of this lane group in the CTA
+    double* R = smem + (size_t)pidx * S.pstride;
+    double* Z = R + S.nmax * S.ldr;
+    int* perm = reinterpret_cast<int*>(smem + (size_t)wpc * PPW * S.pstride) + pidx * S.nmax;
+    const int ldr = S.ldr, rmax = S.rmax;
+    const int ngroups = T.ngroups;
+
+    for (int64_t w0 = ((int64_t)blockIdx.x * wpc + wib) * PPW; w0 < nb; w0 += (int64_t)gridDim.x * wpc * PPW) {
+        const int64_t slot = w0 + sub;
+        const bool valid = slot < nb;
+        int32_t word = valid ? S.gst[slot] : 0x11111111;
+        const double* G = S.gram + (valid ? slot : 0) * S.gstride;
         for (int g = 0; g < ngroups; ++g) {
-            if (gst[g] != ST_OK) continue;
             const int n = T.gn[g];
-            const int nrhs = fast ? T.nout_rhs[g] : T.nterm_rhs[g];
+            const int nrhs = S.nrhs[g];
             const int ncol = n + nrhs;
+            const bool active = valid && group_status(word, g) == ST_OK;
             // R = [A | b...]
-            for (int e = lane; e < n * ncol; e += 32) {
-                int i = e / ncol, j = e - i * ncol;
-                double v;
-                if (j < n) {
-                    int ui = T.gidx[g][i], uj = T.gidx[g][j];
-                    int lo = min(ui, uj), hi = max(ui, uj);
-                    v = Gs[T.upair[lo][hi]];
-                } else {
-                    v = fast ? T.b_out[g][j - n][i] : T.b_term[g][j - n][i];
+            for (int e = l; e < n * ncol; e += LPP) {
+                const int i = e / ncol, j = e - i * ncol;
+                double v = 0.0;
+                if (active) {
+                    if (j < n) {
+                        const int ui = T.gidx[g][i], uj = T.gidx[g][j];
+                        v = G[T.upair[min(ui, uj)][max(ui, uj)]];
+                    } else {
+                        v = fast ? T.b_out[g][j - n][i] : T.b_term[g][j - n][i];
+                    }
                 }
-                R[i * L.ldr + j] = v;
+                R[i * ldr + j] = v;
             }
-            for (int i = lane; i < n; i += 32) perm[i] = i;
+            for (int i = l; i < n; i += LPP) perm[i] = i;
             __syncwarp();
-            bool singular = false;
+            bool dead = !active;
             for (int kk = 0; kk < n; ++kk) {
                 // column norms of the trailing block, pivot = first largest
                 double best = -1.0;
                 int bidx = 0x7fffffff;
-                for (int j = lane; j < n; j += 32) {
-                    if (j < kk) continue;
+                for (int j = kk + ((l - kk) & (LPP - 1)); j < n; j += LPP) {
                     double sn = 0.0;
-                    for (int i = kk; i < n; ++i) sn = fma(R[i * L.ldr + j], R[i * L.ldr + j], sn);
+                    for (int i = kk; i < n; ++i) sn = fma(R[i * ldr + j], R[i * ldr + j], sn);
                     if (sn > best) {
                         best = sn;
                         bidx = j;
                     }
                 }
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
+                for (int o = LPP / 2; o > 0; o >>= 1) {
                     double ob = __shfl_xor_sync(0xffffffffu, best, o);
                     int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
                     if (ob > best || (ob == best && oi < bidx)) {
@@ -231,74 +288,108 @@ __global__ void __launch_bounds__(256) assemble_kernel(AsmArgs a, Layout L) {
                         bidx = oi;
                     }
                 }
-                int piv = (bidx == 0x7fffffff) ? kk : bidx;
+                const int piv = (bidx == 0x7fffffff) ? kk : bidx;
                 // sigma = the pivot column's norm (NaN when all norms were NaN)
                 double sigma;
                 if (bidx == 0x7fffffff) {
                     double sn = 0.0;
-                    for (int i = kk; i < n; ++i) sn = fma(R[i * L.ldr + kk], R[i * L.ldr + kk], sn);
+                    for (int i = kk; i < n; ++i) sn = fma(R[i * ldr + kk], R[i * ldr + kk], sn);
                     sigma = sn;
                 } else {
                     sigma = best;
                 }
-                if (!(sigma > 0.0)) {
-                    singular = true;
-                    break;
-                }
+                dead |= !(sigma > 0.0);
                 if (piv != kk) {
-                    for (int i = lane; i < n; i += 32) {
-                        double t0 = R[i * L.ldr + kk];
-                        R[i * L.ldr + kk] = R[i * L.ldr + piv];
-                        R[i * L.ldr + piv] = t0;
+                    for (int i = l; i < n; i += LPP) {
+                        const double t0 = R[i * ldr + kk];
+                        R[i * ldr + kk] = R[i * ldr + piv];
+                        R[i * ldr + piv] = t0;
                     }
-                    if (lane == 0) {
-                        int t0 = perm[kk];
+                    if (l == 0) {
+                        const int t0 = perm[kk];
                         perm[kk] = perm[piv];
                         perm[piv] = t0;
                     }
                 }
                 __syncwarp();
-                const double alpha = R[kk * L.ldr + kk];
+                const double alpha = R[kk * ldr + kk];
                 const double nr = sqrt(sigma);
                 const double beta = (alpha >= 0.0) ? -nr : nr;
                 const double den = alpha - beta;
                 const double tau = (beta - alpha) / beta;
                 __syncwarp();
-                for (int i = kk + 1 + lane; i < n; i += 32) R[i * L.ldr + kk] = R[i * L.ldr + kk] / den;
+                for (int i = kk + 1 + l; i < n; i += LPP) R[i * ldr + kk] = R[i * ldr + kk] / den;
                 __syncwarp();
-                if (lane == 0) R[kk * L.ldr + kk] = beta;
-                for (int j = kk + 1 + lane; j < ncol; j += 32) {
-                    double sv = R[kk * L.ldr + j];
-                    for (int i = kk + 1; i < n; ++i) sv = fma(R[i * L.ldr + kk], R[i * L.ldr + j], sv);
+                if (l == 0) R[kk * ldr + kk] = beta;
+                for (int j = kk + 1 + l; j < ncol; j += LPP) {
+                    double sv = R[kk * ldr + j];
+                    for (int i = kk + 1; i < n; ++i) sv = fma(R[i * ldr + kk], R[i * ldr + j], sv);
                     sv = sv * tau;
-                    R[kk * L.ldr + j] = R[kk * L.ldr + j] - sv;
-                    for (int i = kk + 1; i < n; ++i) R[i * L.ldr + j] = fma(-sv, R[i * L.ldr + kk], R[i * L.ldr + j]);
+                    R[kk * ldr + j] = R[kk * ldr + j] - sv;
+                    for (int i = kk + 1; i < n; ++i) R[i * ldr + j] = fma(-sv, R[i * ldr + kk], R[i * ldr + j]);
                 }
                 __syncwarp();
             }
-            if (singular) {
-                gst[g] = ST_SINGULAR;
-                __syncwarp();
-                continue;
-            }
-            // back substitution, one right-hand side per lane
-            double* Ag = Acoef + L.a_off[g];
-            for (int r = lane; r < nrhs; r += 32) {
+            // back substitution, right-hand sides split over the lanes
+            for (int r = l; r < nrhs; r += LPP) {
                 for (int i = n - 1; i >= 0; --i) {
-                    double sv = R[i * L.ldr + n + r];
-                    for (int j = i + 1; j < n; ++j) sv = fma(-R[i * L.ldr + j], Z[j * kMaxRhs + r], sv);
-                    Z[i * kMaxRhs + r] = sv / R[i * L.ldr + i];
+                    double sv = R[i * ldr + n + r];
+                    for (int j = i + 1; j < n; ++j) sv = fma(-R[i * ldr + j], Z[j * rmax + r], sv);
+                    Z[i * rmax + r] = sv / R[i * ldr + i];
                 }
             }
             __syncwarp();
-            for (int e = lane; e < n * nrhs; e += 32) {
-                int i = e / nrhs, r = e - i * nrhs;
-                Ag[perm[i] * kRhs + r] = Z[i * kMaxRhs + r];
+            if (!dead) {
+                double* C = S.coef + slot * S.cstride + S.c_off[g];
+                for (int e = l; e < n * nrhs; e += LPP) {
+                    const int i = e / nrhs, r = e - i * nrhs;
+                    C[perm[i] * nrhs + r] = Z[i * rmax + r];
+                }
+            } else if (active) {
+                word = (word & ~(15 << (4 * g))) | (ST_SINGULAR << (4 * g));
             }
             __syncwarp();
         }
+        if (valid && l == 0) S.gst[slot] = word;
+    }
+}
 
-        // ---- 4. kernels ----
+// ------------------------------------------------------------- 3. weights --
+// One warp per particle, one neighbour row per lane.  The right-hand sides
+// and outputs are run-time loops (no work predicated off on the FP64 pipe);
+// per-output sums live in this lane's column of shared memory.
+template <int DIM>
+__global__ void __launch_bounds__(256) weights_kernel(AsmArgs a, Split S, int64_t b0, int64_t b1) {
+    extern __shared__ double smem[];
+    __shared__ ProgShared P;
+    const AsmTables& T = *a.tab;
+    stage_program(T, P);
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    double* Cs = smem + (size_t)wib * (S.cstride + (S.nslots + S.nout) * 32);
+    double* V = Cs + S.cstride;
+    double* Wacc = V + S.nslots * 32;
+    const int ngroups = T.ngroups;
+    const int nprog = T.nprog;
+    const bool fast = (a.flags & DCPSE_ASSEMBLE_FAST_FLAG) != 0;
+    const bool st_terms = a.k_term != nullptr;
+    const int noutputs = T.noutputs;
+
+    const int wpc = blockDim.x >> 5;
+    const int64_t nw = (int64_t)gridDim.x * wpc;
+    for (int64_t it = b0 + (int64_t)blockIdx.x * wpc + wib; it < b1; it += nw) {
+        const int64_t slot = it - b0;
+        const int64_t p = a.order ? (int64_t)a.order[it] : it;
+        const int64_t beg = a.rowptr[p];
+        const int k = (int)(a.rowptr[p + 1] - beg);
+        double xp[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xp[d] = a.pos[p * DIM + d];
+        const double eps = a.eps[p];
+        const int32_t word = S.gst[slot];
+        for (int e = lane; e < S.cstride; e += 32) Cs[e] = S.coef[slot * S.cstride + e];
+        __syncwarp();
+
         double eipg[kMaxGroups];
 #pragma unroll
         for (int g = 0; g < kMaxGroups; ++g) eipg[g] = (g < ngroups) ? 1.0 / ipow(eps, (unsigned)T.gord[g]) : 0.0;
@@ -310,71 +401,55 @@ __global__ void __launch_bounds__(256) assemble_kernel(AsmArgs a, Layout L) {
             load_offset<DIM>(a, xp, a.cols[beg + q], o);
 #pragma unroll
             for (int d = 0; d < DIM; ++d) u[d] = o[d] / eps;
-            double pw[kMaxDim][8];
-            powers<DIM, MAXE>(u, pw);
+            monomials<DIM>(u, V, P, nprog, lane);
             const double ef = cw_exp(-norm2<DIM>(u));
-            double wout[kMaxOutputs];
-#pragma unroll
-            for (int t = 0; t < kMaxOutputs; ++t) wout[t] = 0.0;
+            for (int t = 0; t < noutputs; ++t) Wacc[t * 32 + lane] = 0.0;
             for (int g = 0; g < ngroups; ++g) {
                 const int n = T.gn[g];
-                const int nrhs = fast ? T.nout_rhs[g] : T.nterm_rhs[g];
-                const bool ok = (gst[g] == ST_OK);
-                const double* Ag = Acoef + L.a_off[g];
-                double res[kRhs];
-#pragma unroll
-                for (int r = 0; r < kRhs; ++r) res[r] = 0.0;
-                if (ok) {
-                    for (int i = 0; i < n; ++i) {
-                        double v = mono<DIM, MAXE>(pw, T.uexp[T.gidx[g][i]]);
-#pragma unroll
-                        for (int r = 0; r < kRhs; ++r) {
-                            if (r < nrhs) {
-                                if (fast) {
-                                    res[r] = fma(Ag[i * kRhs + r], v, res[r]);
-                                } else {
-                                    double t0 = Ag[i * kRhs + r] * v;
-                                    t0 = t0 * ef;
-                                    res[r] = res[r] + t0;
-                                }
-                            }
-                        }
-                    }
-                }
+                const int nrhs = S.nrhs[g];
+                const bool ok = group_status(word, g) == ST_OK;
+                const double* Ag = Cs + S.c_off[g];
                 double eip = eipg[0];
 #pragma unroll
                 for (int t = 1; t < kMaxGroups; ++t)
                     if (t == g) eip = eipg[t];
-#pragma unroll
-                for (int r = 0; r < kRhs; ++r) {
-                    if (r < nrhs) {
+                for (int r = 0; r < nrhs; ++r) {
+                    double res = 0.0;
+                    if (ok) {
                         if (fast) {
-                            double Kq = ok ? (res[r] * ef) : 0.0;
-                            nonfinite |= !isfinite(Kq);
-                            int o2 = T.out_of_rhs[g][r];
-#pragma unroll
-                            for (int t = 0; t < kMaxOutputs; ++t)
-                                if (t == o2) wout[t] = wout[t] + Kq * eip;
+                            for (int i = 0; i < n; ++i)
+                                res = fma(Ag[i * nrhs + r], V[P.uslot[T.gidx[g][i]] * 32 + lane], res);
                         } else {
-                            double Kq = res[r];
-                            nonfinite |= !isfinite(Kq);
-                            int term = T.term_of_rhs[g][r];
-                            if (st_terms) a.k_term[(int64_t)term * a.nnz + beg + q] = Kq;
-                            int o2 = T.term_output[term];
-#pragma unroll
-                            for (int t = 0; t < kMaxOutputs; ++t)
-                                if (t == o2) wout[t] = wout[t] + Kq * eip;
+                            for (int i = 0; i < n; ++i) {
+                                double t0 = Ag[i * nrhs + r] * V[P.uslot[T.gidx[g][i]] * 32 + lane];
+                                t0 = t0 * ef;
+                                res = res + t0;
+                            }
                         }
                     }
+                    double Kq;
+                    int o2;
+                    if (fast) {
+                        Kq = ok ? (res * ef) : 0.0;
+                        o2 = T.out_of_rhs[g][r];
+                    } else {
+                        Kq = res;
+                        const int term = T.term_of_rhs[g][r];
+                        if (st_terms) a.k_term[(int64_t)term * a.nnz + beg + q] = Kq;
+                        o2 = T.term_output[term];
+                    }
+                    nonfinite |= !finite_bits(Kq);
+                    Wacc[o2 * 32 + lane] = Wacc[o2 * 32 + lane] + Kq * eip;
                 }
             }
             for (int t = 0; t < noutputs; ++t) {
-                if (a.w64) a.w64[(int64_t)t * a.nnz + beg + q] = wout[t];
-                const float w32 = (float)wout[t];
+                const double w = Wacc[t * 32 + lane];
+                if (a.w64) a.w64[(int64_t)t * a.nnz + beg + q] = w;
+                const float w32 = (float)w;
                 if (a.w32) a.w32[(int64_t)t * a.nnz + beg + q] = w32;
                 if (a.r16)
                     reinterpret_cast<__nv_bfloat16*>(a.r16)[(int64_t)t * a.nnz + beg + q] =
-                        __float2bfloat16_rn((float)(wout[t] - (double)w32));
+                        __float2bfloat16_rn((float)(w - (double)w32));
             }
         }
         nonfinite = __any_sync(0xffffffffu, nonfinite);
@@ -391,13 +466,11 @@ __global__ void __launch_bounds__(256) assemble_kernel(AsmArgs a, Layout L) {
                         reinterpret_cast<__nv_bfloat16*>(a.r16)[(int64_t)t * a.nnz + beg + q] = __float2bfloat16_rn(0.0f);
                 }
             }
-        } else if (st_terms) {
-            // failed groups: their term kernels are zero (written above as 0)
         }
         if (lane == 0) {
             int st = ST_OK;
             for (int g = 0; g < ngroups; ++g)
-                if (st == ST_OK && gst[g] != ST_OK) st = gst[g];
+                if (st == ST_OK && group_status(word, g) != ST_OK) st = group_status(word, g);
             if (st == ST_OK && nonfinite) st = ST_NONFINITE;
             a.status[p] = st;
         }
@@ -405,25 +478,177 @@ __global__ void __launch_bounds__(256) assemble_kernel(AsmArgs a, Layout L) {
     }
 }
 
-template <int DIM, int MAXE, int NPP>
-cudaError_t launch(const AsmArgs& a, const Layout& L, cudaStream_t s) {
-    const int warps = (a.warps == 2 || a.warps == 8) ? a.warps : kWarps;
-    size_t bytes = (size_t)L.words * sizeof(double) * warps;
-    auto kern = assemble_kernel<DIM, MAXE, NPP>;
+// ---------------------------------------------------------------- launches --
+int warps_of(const AsmArgs& a) { return (a.warps == 2 || a.warps == 8) ? a.warps : kWarps; }
+
+template <typename K>
+cudaError_t persistent(K kern, int threads, size_t bytes, int64_t work_per_cta, int64_t units, int& grid_out) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, bytes);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, bytes);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    int64_t need = (a.n + warps - 1) / warps;
+    int64_t need = (units + work_per_cta - 1) / work_per_cta;
     int64_t grid = (int64_t)num_sms() * per_sm;
     if (grid > need) grid = need;
     if (grid < 1) grid = 1;
-    kern<<<(unsigned)grid, warps * 32, bytes, s>>>(a, L);
+    grid_out = (int)grid;
+    return cudaSuccess;
+}
+
+template <int DIM>
+cudaError_t launch_eps(const AsmArgs& a, const Split& S, int64_t b0, int64_t b1, cudaStream_t s) {
+    auto kern = eps_kernel<DIM>;
+    int grid = 0;
+    cudaError_t e = persistent(kern, 256, 0, 256, b1 - b0, grid);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, 256, 0, s>>>(a, S, b0, b1);
     return cudaGetLastError();
 }
 
+template <int DIM, int NPP>
+cudaError_t launch_gram(const AsmArgs& a, const Split& S, int64_t b0, int64_t b1, cudaStream_t s) {
+    const int warps = warps_of(a);
+    const size_t bytes = (size_t)(kCh * S.ldb + S.nslots * 32) * sizeof(double) * warps;
+    auto kern = gram_kernel<DIM, NPP>;
+    int grid = 0;
+    cudaError_t e = persistent(kern, warps * 32, bytes, warps, b1 - b0, grid);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, warps * 32, bytes, s>>>(a, S, b0, b1);
+    return cudaGetLastError();
+}
+
+// Work space of one particle: R then Z, padded to LPP mod 16 doubles so that
+// the lane groups of a half warp (16 lanes, 64-bit accesses) fall on
+// distinct shared-memory banks.
+int qr_pstride(const Split& S, int lpp) {
+    const int words = S.nmax * S.ldr + S.nmax * S.rmax;
+    return words + ((lpp - words) & 15);
+}
+
+size_t qr_bytes(const Split& S, int lpp) {
+    return (size_t)kQrWarps * (32 / lpp) * (qr_pstride(S, lpp) * sizeof(double) + S.nmax * sizeof(int));
+}
+
+template <int LPP>
+cudaError_t launch_qr(const AsmArgs& a, Split S, int64_t nb, cudaStream_t s) {
+    constexpr int PPW = 32 / LPP;
+    S.pstride = qr_pstride(S, LPP);
+    const size_t bytes = qr_bytes(S, LPP);
+    auto kern = qr_kernel<LPP>;
+    int grid = 0;
+    cudaError_t e = persistent(kern, kQrWarps * 32, bytes, (int64_t)kQrWarps * PPW, nb, grid);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kQrWarps * 32, bytes, s>>>(a, S, nb);
+    return cudaGetLastError();
+}
+
+template <int DIM>
+cudaError_t launch_weights(const AsmArgs& a, const Split& S, int64_t b0, int64_t b1, cudaStream_t s) {
+    const int warps = warps_of(a);
+    const size_t bytes = (size_t)(S.cstride + (S.nslots + S.nout) * 32) * sizeof(double) * warps;
+    auto kern = weights_kernel<DIM>;
+    int grid = 0;
+    cudaError_t e = persistent(kern, warps * 32, bytes, warps, b1 - b0, grid);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, warps * 32, bytes, s>>>(a, S, b0, b1);
+    return cudaGetLastError();
+}
+
+int smem_attr(cudaDeviceAttr attr, int fallback) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, attr, dev) != cudaSuccess) return fallback;
+    return v;
+}
+
+// lanes per particle of the QR: the fewest that still leave >= 6 warps per SM
+// resident within the shared-memory budget (on the 128^3 gradient+Laplacian
+// cloud 4 lanes / 6 warps beat 8 lanes / 12 warps and 2 lanes / 2 warps)
+int qr_lanes_auto(const Split& S) {
+    const int per_sm = smem_attr(cudaDevAttrMaxSharedMemoryPerMultiprocessor, 228 * 1024);
+    const int per_block = smem_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, 227 * 1024);
+    for (int lpp : {1, 2, 4, 8, 16}) {
+        const size_t b = qr_bytes(S, lpp);
+        if (b > (size_t)per_block) continue;
+        const int blocks = (int)(per_sm / (b + 1024));
+        if (blocks * kQrWarps >= 6) return lpp;
+    }
+    return 32;
+}
+
+cudaError_t launch_qr_any(const AsmArgs& a, const Split& S, int lpp, int64_t nb, cudaStream_t s) {
+    switch (lpp) {
+        case 1: return launch_qr<1>(a, S, nb, s);
+        case 2: return launch_qr<2>(a, S, nb, s);
+        case 4: return launch_qr<4>(a, S, nb, s);
+        case 8: return launch_qr<8>(a, S, nb, s);
+        case 16: return launch_qr<16>(a, S, nb, s);
+        default: return launch_qr<32>(a, S, nb, s);
+    }
+}
+
+template <int DIM, int NPP>
+cudaError_t run(const AsmArgs& a, const Split& S, int lpp, cudaStream_t s) {
+    for (int64_t b0 = 0; b0 < a.n; b0 += a.scratch_particles) {
+        const int64_t b1 = std::min(a.n, b0 + a.scratch_particles);
+        cudaError_t e = launch_eps<DIM>(a, S, b0, b1, s);
+        if (e == cudaSuccess) e = launch_gram<DIM, NPP>(a, S, b0, b1, s);
+        if (e == cudaSuccess) e = launch_qr_any(a, S, lpp, b1 - b0, s);
+        if (e == cudaSuccess) e = launch_weights<DIM>(a, S, b0, b1, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <int DIM>
+cudaError_t dispatch(const AsmArgs& a, const AsmTables& h, const Split& S, int lpp, cudaStream_t s) {
+    // Gram entries per lane: the smallest instantiated count that holds them
+    // all (a slot no lane uses would still occupy the FP64 pipe every row)
+    const int npp = (h.npairs + 31) / 32;
+    if (npp <= 2) return run<DIM, 2>(a, S, lpp, s);
+    if (npp <= 4) return run<DIM, 4>(a, S, lpp, s);
+    if (npp <= 7) return run<DIM, 7>(a, S, lpp, s);
+    if (npp <= 8) return run<DIM, 8>(a, S, lpp, s);
+    if (npp <= 16) return run<DIM, 16>(a, S, lpp, s);
+    return run<DIM, 40>(a, S, lpp, s);
+}
+
+Split make_split(const AsmTables& h, int flags) {
+    Split S{};
+    const bool fast = (flags & DCPSE_ASSEMBLE_FAST_FLAG) != 0;
+    S.gstride = (h.npairs + 1) & ~1;
+    S.nmax = 1;
+    S.rmax = 1;
+    int off = 0;
+    for (int g = 0; g < h.ngroups; ++g) {
+        S.nrhs[g] = fast ? h.nout_rhs[g] : h.nterm_rhs[g];
+        S.c_off[g] = off;
+        off += h.gn[g] * S.nrhs[g];
+        S.nmax = std::max(S.nmax, h.gn[g]);
+        S.rmax = std::max(S.rmax, S.nrhs[g]);
+    }
+    S.cstride = (off + 1) & ~1;
+    S.ldr = S.nmax + S.rmax;
+    S.ldb = h.nu | 1;
+    S.nslots = h.nslots;
+    S.nout = h.noutputs;
+    return S;
+}
+
+}  // namespace
+
+int64_t assembly_scratch_bytes(const AsmTables& h, int flags) {
+    const Split S = make_split(h, flags);
+    return (int64_t)(S.gstride + S.cstride) * (int64_t)sizeof(double) + (int64_t)sizeof(int32_t);
+}
+
+int64_t binning_tmp_elems(int64_t n, int maxk, int width) {
+    const int64_t nb = maxk / (width > 0 ? width : 1) + 1;
+    return nb + 1 + scan_tmp_elems(nb);
+}
+
+namespace {
 __global__ void khist_kernel(const int64_t* __restrict__ rowptr, int64_t n, int width, int32_t* __restrict__ hist) {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
         atomicAdd(&hist[(int)(rowptr[p + 1] - rowptr[p]) / width], 1);
@@ -436,24 +661,7 @@ __global__ void kscatter_kernel(const int64_t* __restrict__ rowptr, int64_t n, i
         order[atomicAdd((unsigned long long*)&fill[b], 1ull)] = (int32_t)p;
     }
 }
-
-template <int DIM>
-cudaError_t dispatch(const AsmArgs& a, const AsmTables& h, const Layout& L, cudaStream_t s) {
-    const int npp = (h.npairs + 31) / 32;
-    if (h.maxexp <= 4) {
-        if (npp <= 8) return launch<DIM, 4, 8>(a, L, s);
-        return launch<DIM, 4, 40>(a, L, s);
-    }
-    if (npp <= 8) return launch<DIM, 8, 8>(a, L, s);
-    return launch<DIM, 8, 40>(a, L, s);
-}
-
 }  // namespace
-
-int64_t binning_tmp_elems(int64_t n, int maxk, int width) {
-    const int64_t nb = maxk / (width > 0 ? width : 1) + 1;
-    return nb + 1 + scan_tmp_elems(nb);
-}
 
 cudaError_t bin_by_count(const int64_t* rowptr, int64_t n, int maxk, int width, int32_t* order, int32_t* hist,
                          int64_t* tmp64, cudaStream_t s) {
@@ -474,36 +682,20 @@ cudaError_t bin_by_count(const int64_t* rowptr, int64_t n, int maxk, int width, 
 
 cudaError_t assemble(const AsmArgs& a, const AsmTables& h, cudaStream_t s) {
     if (a.n == 0) return cudaSuccess;
-    Layout L{};
-    L.ldb = h.nu | 1;
-    L.nmax = 1;
-    int rmax = 1;
-    for (int g = 0; g < h.ngroups; ++g) {
-        L.nmax = L.nmax > h.gn[g] ? L.nmax : h.gn[g];
-        int r = (a.flags & DCPSE_ASSEMBLE_FAST_FLAG) ? h.nout_rhs[g] : h.nterm_rhs[g];
-        rmax = rmax > r ? rmax : r;
-    }
-    L.ldr = (L.nmax + rmax) | 1;
-    int off = 0;
-    L.off_b = off;
-    off += kCh * L.ldb;
-    L.off_g = off;
-    off += h.npairs;
-    L.off_r = off;
-    off += L.nmax * L.ldr;
-    L.off_z = off;
-    off += L.nmax * kMaxRhs;
-    L.off_a = off;
-    for (int g = 0; g < h.ngroups; ++g) {
-        L.a_off[g] = off - L.off_a;
-        off += h.gn[g] * kRhs;
-    }
-    L.off_perm = off;
-    off += (L.nmax + 1) / 2;
-    L.words = off + (off & 1);  // keep each warp's block 16-byte aligned
-    if (h.dim == 3) return dispatch<3>(a, h, L, s);
-    if (h.dim == 2) return dispatch<2>(a, h, L, s);
-    return dispatch<1>(a, h, L, s);
+    if (!a.scratch || a.scratch_particles < 1) return cudaErrorInvalidValue;
+    Split S = make_split(h, a.flags);
+    const int64_t nb = a.scratch_particles;
+    S.gram = a.scratch;
+    S.coef = S.gram + nb * S.gstride;
+    S.gst = reinterpret_cast<int32_t*>(S.coef + nb * S.cstride);
+    int lpp = a.qr_lanes;
+    if (lpp != 1 && lpp != 2 && lpp != 4 && lpp != 8 && lpp != 16 && lpp != 32) lpp = qr_lanes_auto(S);
+    // a lane grouping whose work space does not fit is refused before any launch
+    if (qr_bytes(S, lpp) > (size_t)smem_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, 227 * 1024))
+        return cudaErrorInvalidConfiguration;
+    if (h.dim == 3) return dispatch<3>(a, h, S, lpp, s);
+    if (h.dim == 2) return dispatch<2>(a, h, S, lpp, s);
+    return dispatch<1>(a, h, S, lpp, s);
 }
 
 }  // namespace dcpse

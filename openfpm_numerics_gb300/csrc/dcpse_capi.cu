@@ -114,6 +114,10 @@ __global__ void row_max_kernel(const int64_t* rowptr, int64_t n, int* maxk) {
 // last used one.
 constexpr int64_t kPad = 8;
 
+// Largest scratch of one assembly batch; larger clouds are assembled in
+// batches of particles (the result does not depend on the batch size).
+constexpr int64_t kAsmScratchBytes = int64_t(512) << 20;
+
 template <typename T>
 cudaError_t dalloc(T** p, size_t count) {
     *p = nullptr;
@@ -199,7 +203,9 @@ struct dcpse_plan_s {
     unsigned long long* summary = nullptr;  // [count, first]
     int* d_err = nullptr;                   // set by kernels whose bounded wait ran out
     int apply_lanes = 0, apply_mode = 0;
-    int asm_bin_width = 0, asm_warps = 4;
+    int asm_bin_width = 0, asm_warps = 4, asm_qr_lanes = 0;
+    double* asm_scratch = nullptr;  // assembly batch scratch
+    int64_t asm_scratch_bytes = 0;
     int32_t* korder = nullptr;  // k-binned particle order of the current list
     int korder_width = 0;
     // transposed list and weight row sums (adjoint), built on demand
@@ -258,6 +264,8 @@ struct dcpse_plan_s {
         dfree(hout);
         dfree(summary);
         dfree(d_err);
+        dfree(asm_scratch);
+        asm_scratch_bytes = 0;
         dfree(dtab);
         delete htab;
         htab = nullptr;
@@ -266,6 +274,60 @@ struct dcpse_plan_s {
 };
 
 namespace {
+
+// Monomial program of the union basis (see AsmTables::prog).  Powers follow
+// ipow's square-and-multiply steps, keyed by the exponent reached, so every
+// intermediate power is computed once; monomials multiply their non-unit
+// factors left to right in dimension order, sharing common prefixes.
+int build_program(AsmTables* T) {
+    const int dim = T->dim;
+    T->nprog = 0;
+    auto op = [&](int x, int y) -> int {
+        if (dim + 1 + T->nprog >= kMaxSlots) return -1;
+        T->prog[T->nprog][0] = (unsigned char)x;
+        T->prog[T->nprog][1] = (unsigned char)y;
+        return dim + 1 + T->nprog++;
+    };
+    std::map<std::pair<int, int>, int> pw;  // (d, exponent) -> slot
+    auto power = [&](int d, int e) -> int {
+        int top = 0;
+        while ((e >> (top + 1)) != 0) ++top;
+        int cur = d, p = 1;
+        for (int b = top - 1; b >= 0 && cur >= 0; --b) {
+            p = 2 * p;
+            auto it = pw.find({d, p});
+            cur = (it != pw.end()) ? it->second : (pw[{d, p}] = op(cur, cur));
+            if (cur >= 0 && ((e >> b) & 1)) {
+                p = p + 1;
+                auto jt = pw.find({d, p});
+                cur = (jt != pw.end()) ? jt->second : (pw[{d, p}] = op(cur, d));
+            }
+        }
+        return cur;
+    };
+    std::map<std::vector<int>, int> prod;  // factor slots -> slot of their product
+    for (int j = 0; j < T->nu; ++j) {
+        std::vector<int> f;
+        for (int d = 0; d < dim; ++d)
+            if (T->uexp[j][d] > 0) f.push_back(power(d, T->uexp[j][d]));
+        for (int x : f)
+            if (x < 0) return -1;
+        int cur = dim;  // the constant 1.0
+        if (!f.empty()) {
+            cur = f[0];
+            std::vector<int> key{f[0]};
+            for (size_t m = 1; m < f.size() && cur >= 0; ++m) {
+                key.push_back(f[m]);
+                auto it = prod.find(key);
+                cur = (it != prod.end()) ? it->second : (prod[key] = op(cur, f[m]));
+            }
+        }
+        if (cur < 0) return -1;
+        T->uslot[j] = (unsigned char)cur;
+    }
+    T->nslots = dim + 1 + T->nprog;
+    return 0;
+}
 
 int build_tables(dcpse_plan_s* P) {
     AsmTables* T = P->htab;
@@ -317,6 +379,7 @@ int build_tables(dcpse_plan_s* P) {
         }
     T->maxexp = maxe + 1;
     if (T->maxexp > kMaxExp) return fail(DCPSE_ERR_CAPACITY, "monomial degree larger than supported");
+    if (build_program(T) != 0) return fail(DCPSE_ERR_CAPACITY, "monomial program larger than supported");
     // Gram entries needed by some group
     std::vector<std::pair<int, int>> pairs;
     for (int g = 0; g < T->ngroups; ++g)
@@ -744,7 +807,23 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     a.r16 = P->r16;
     a.nnz = nnz;
     a.warps = P->asm_warps;
+    a.qr_lanes = P->asm_qr_lanes;
     a.order = nullptr;
+    if (n > 0) {
+        // batches of at most kAsmScratchBytes of scratch (Gram entries and
+        // coefficients of the particles in flight)
+        const int64_t per = assembly_scratch_bytes(*P->htab, flags);
+        const int64_t nb = std::min<int64_t>(n, std::max<int64_t>(4096, kAsmScratchBytes / per));
+        const int64_t bytes = nb * per + 16;
+        if (P->asm_scratch_bytes < bytes) {
+            dfree(P->asm_scratch);
+            P->asm_scratch_bytes = 0;
+            DCPSE_CK(dalloc(&P->asm_scratch, (size_t)(bytes + 7) / 8));
+            P->asm_scratch_bytes = bytes;
+        }
+        a.scratch = P->asm_scratch;
+        a.scratch_particles = nb;
+    }
     if (P->asm_bin_width > 0 && n > 0) {
         if (!P->korder || P->korder_width != P->asm_bin_width) {
             if (!P->korder) DCPSE_CK(dalloc(&P->korder, n));
@@ -765,6 +844,8 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     P->tstart(DCPSE_K_ASSEMBLE);
     cudaError_t e = assemble(a, *P->htab, s);
     P->tstop(DCPSE_K_ASSEMBLE);
+    if (e == cudaErrorInvalidConfiguration)
+        return fail(DCPSE_ERR_CAPACITY, "assembly: the QR work space of this lane grouping exceeds shared memory");
     if (e != cudaSuccess) return fail(DCPSE_ERR_CUDA, std::string("assembly: ") + cudaGetErrorString(e));
     P->assembled = true;
     P->flags = flags;
@@ -1166,12 +1247,16 @@ int dcpse_plan_set_apply_config(dcpse_plan_t* P, int lanes, int mode) {
     return DCPSE_OK;
 }
 
-int dcpse_plan_set_assembly_config(dcpse_plan_t* P, int bin_width, int warps) {
+int dcpse_plan_set_assembly_config(dcpse_plan_t* P, int bin_width, int warps, int qr_lanes) {
     if (int rc = check_plan(P)) return rc;
     if (bin_width < 0) return fail(DCPSE_ERR_ARG, "bin_width must be >= 0");
     if (warps != 2 && warps != 4 && warps != 8) return fail(DCPSE_ERR_ARG, "warps must be 2, 4 or 8");
+    if (qr_lanes != 0 && qr_lanes != 1 && qr_lanes != 2 && qr_lanes != 4 && qr_lanes != 8 && qr_lanes != 16 &&
+        qr_lanes != 32)
+        return fail(DCPSE_ERR_ARG, "qr_lanes must be 0, 1, 2, 4, 8, 16 or 32");
     P->asm_bin_width = bin_width;
     P->asm_warps = warps;
+    P->asm_qr_lanes = qr_lanes;
     return DCPSE_OK;
 }
 

@@ -65,6 +65,7 @@ constexpr int kMaxOutputs = 8;
 constexpr int kMaxRhs = 8;       // right-hand sides per group
 constexpr int kMaxPairs = 1280;  // Gram entries (i <= j) needed by some group
 constexpr int kMaxExp = 8;       // highest exponent + 1
+constexpr int kMaxSlots = 192;   // monomial program: inputs, constant and products
 
 struct AsmTables {
     int dim;
@@ -90,6 +91,15 @@ struct AsmTables {
     int term_group[kMaxTerms];
     int term_output[kMaxTerms];
     int noutputs;
+    // Monomial program: per-lane value slots [0, dim) hold u, slot dim holds
+    // 1.0, and step s writes slot dim + 1 + s = slot prog[s][0] * slot
+    // prog[s][1].  The steps are exactly the multiplications of ipow and of
+    // the left-to-right monomial product, each shared value computed once
+    // (factors equal to 1.0 are skipped: x * 1.0 == x).
+    int nprog;
+    int nslots;
+    unsigned char prog[kMaxSlots][2];
+    unsigned char uslot[kMaxUnion];              // slot holding union monomial j
 };
 
 struct AsmArgs {
@@ -113,8 +123,15 @@ struct AsmArgs {
     void* r16;           // bf16 [noutputs][nnz]: w64 - w32, or nullptr
     int64_t nnz;
     const int32_t* order; // processing order of the particles (k-binned) or nullptr
-    int warps;            // warps per CTA (2, 4 or 8)
+    int warps;            // warps per CTA of the Gram and weight kernels (2, 4 or 8)
+    int qr_lanes;         // lanes per particle of the QR kernel (0 = automatic)
+    double* scratch;      // assembly_scratch_bytes() per particle of a batch
+    int64_t scratch_particles;  // batch size the scratch holds
 };
+
+// Scratch bytes per particle of an assembly batch (Gram entries,
+// coefficients and a status word) for the plan's tables and flags.
+int64_t assembly_scratch_bytes(const AsmTables& h, int flags);
 
 // Particle order binned by neighbour count: bins of `width` counts
 // ascending (a counting sort on k / width); order[n], tmp sized by

@@ -247,10 +247,11 @@ class DcpsePlan:
         when it fits, 1 = direct loads, 2 = staged."""
         C.call("dcpse_plan_set_apply_config", self._h, int(lanes), int(mode))
 
-    def set_assembly_config(self, bin_width=0, warps=4):
+    def set_assembly_config(self, bin_width=0, warps=4, qr_lanes=0):
         """Assembly schedule: neighbour-count bins of width bin_width (0 =
-        index order), CTAs of 2/4/8 warps."""
-        C.call("dcpse_plan_set_assembly_config", self._h, int(bin_width), int(warps))
+        index order), CTAs of 2/4/8 warps for the Gram and weight kernels,
+        qr_lanes lanes per particle in the QR kernel (0 = automatic)."""
+        C.call("dcpse_plan_set_assembly_config", self._h, int(bin_width), int(warps), int(qr_lanes))
 
     def check(self):
         """Synchronise; raise if a kernel's bounded device wait ran out."""

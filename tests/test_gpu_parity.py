@@ -223,19 +223,24 @@ def test_apply_schedules(cuda, orc, name):
 
 @pytest.mark.parametrize("name", ["2d_adaptive", "3d"])
 def test_assembly_schedules_bitexact(cuda, orc, name):
-    """Neighbour-count binning and CTA size change the schedule only."""
+    """Neighbour-count binning, CTA size and QR lane grouping change the
+    schedule only."""
     c = _case(name)
     plan, pos, _ = _build(c)
     ref = [plan.term_kernels(t)[0].clone() for t in range(plan.n_terms)]
-    for bw, wp in ((4, 2), (16, 8), (1, 4)):
-        plan.set_assembly_config(bw, wp)
-        plan.assemble(pos, C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+    for bw, wp, ql in ((4, 2, 0), (16, 8, 1), (1, 4, 2), (0, 4, 4), (0, 4, 8), (0, 2, 16), (0, 8, 32)):
+        plan.set_assembly_config(bw, wp, ql)
+        try:
+            plan.assemble(pos, C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+        except C.DcpseError as e:  # QR work space larger than shared memory
+            assert ql in (1, 2) and e.code == C.ERR_CAPACITY
+            continue
         for t in range(plan.n_terms):
-            assert torch.equal(plan.term_kernels(t)[0], ref[t]), (bw, wp, t)
+            assert torch.equal(plan.term_kernels(t)[0], ref[t]), (bw, wp, ql, t)
     from openfpm_numerics_gb300 import autotune
 
     best = autotune.tune_assembly(plan, pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
-    assert len(best["sweep"]) == 9 and best["warps"] in (2, 4, 8)
+    assert len(best["sweep"]) >= 11 and best["warps"] in (2, 4, 8) and best["qr_lanes"] in (0, 2, 4, 8, 16)
 
 
 def test_autotune(cuda):
