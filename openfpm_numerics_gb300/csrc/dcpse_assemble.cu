@@ -54,7 +54,8 @@ struct Split {
     int cstride;             // doubles of coefficients per particle
     int nrhs[kMaxGroups];    // right-hand sides per group (per term or per output)
     int c_off[kMaxGroups];   // coefficient block of each group, [gn][nrhs]
-    int nmax, rmax, ldr;     // largest basis, most right-hand sides, row stride of [A|b]
+    int nmax;                // largest basis
+    int qwords;              // doubles of the largest [A|b] plus its solution block
     int pstride;             // doubles of QR work space per particle (set per lane grouping)
     int ldb;                 // row stride of the B chunk of the Gram kernel
     int nslots;              // monomial program slots per lane
@@ -235,9 +236,7 @@ __global__ void __launch_bounds__(kQrWarps * 32) qr_kernel(AsmArgs a, Split S, i
     const int wpc = blockDim.x >> 5;
     const int pidx = wib * PPW + sub;  // particle slot of this lane group in the CTA
     double* R = smem + (size_t)pidx * S.pstride;
-    double* Z = R + S.nmax * S.ldr;
     int* perm = reinterpret_cast<int*>(smem + (size_t)wpc * PPW * S.pstride) + pidx * S.nmax;
-    const int ldr = S.ldr, rmax = S.rmax;
     const int ngroups = T.ngroups;
 
     for (int64_t w0 = ((int64_t)blockIdx.x * wpc + wib) * PPW; w0 < nb; w0 += (int64_t)gridDim.x * wpc * PPW) {
@@ -249,6 +248,8 @@ __global__ void __launch_bounds__(kQrWarps * 32) qr_kernel(AsmArgs a, Split S, i
             const int n = T.gn[g];
             const int nrhs = S.nrhs[g];
             const int ncol = n + nrhs;
+            const int ldr = ncol;         // [A | b...], n rows
+            double* Z = R + n * ncol;     // solutions, n x nrhs
             const bool active = valid && group_status(word, g) == ST_OK;
             // R = [A | b...]
             for (int e = l; e < n * ncol; e += LPP) {
@@ -334,8 +335,8 @@ __global__ void __launch_bounds__(kQrWarps * 32) qr_kernel(AsmArgs a, Split S, i
             for (int r = l; r < nrhs; r += LPP) {
                 for (int i = n - 1; i >= 0; --i) {
                     double sv = R[i * ldr + n + r];
-                    for (int j = i + 1; j < n; ++j) sv = fma(-R[i * ldr + j], Z[j * rmax + r], sv);
-                    Z[i * rmax + r] = sv / R[i * ldr + i];
+                    for (int j = i + 1; j < n; ++j) sv = fma(-R[i * ldr + j], Z[j * nrhs + r], sv);
+                    Z[i * nrhs + r] = sv / R[i * ldr + i];
                 }
             }
             __syncwarp();
@@ -343,7 +344,7 @@ __global__ void __launch_bounds__(kQrWarps * 32) qr_kernel(AsmArgs a, Split S, i
                 double* C = S.coef + slot * S.cstride + S.c_off[g];
                 for (int e = l; e < n * nrhs; e += LPP) {
                     const int i = e / nrhs, r = e - i * nrhs;
-                    C[perm[i] * nrhs + r] = Z[i * rmax + r];
+                    C[perm[i] * nrhs + r] = Z[i * nrhs + r];
                 }
             } else if (active) {
                 word = (word & ~(15 << (4 * g))) | (ST_SINGULAR << (4 * g));
@@ -519,13 +520,10 @@ cudaError_t launch_gram(const AsmArgs& a, const Split& S, int64_t b0, int64_t b1
     return cudaGetLastError();
 }
 
-// Work space of one particle: R then Z, padded to LPP mod 16 doubles so that
-// the lane groups of a half warp (16 lanes, 64-bit accesses) fall on
-// distinct shared-memory banks.
-int qr_pstride(const Split& S, int lpp) {
-    const int words = S.nmax * S.ldr + S.nmax * S.rmax;
-    return words + ((lpp - words) & 15);
-}
+// Work space of one particle: [A|b] then the solutions of the largest group,
+// padded to LPP mod 16 doubles so that the lane groups of a half warp (16
+// lanes, 64-bit accesses) fall on distinct shared-memory banks.
+int qr_pstride(const Split& S, int lpp) { return S.qwords + ((lpp - S.qwords) & 15); }
 
 size_t qr_bytes(const Split& S, int lpp) {
     return (size_t)kQrWarps * (32 / lpp) * (qr_pstride(S, lpp) * sizeof(double) + S.nmax * sizeof(int));
@@ -619,17 +617,17 @@ Split make_split(const AsmTables& h, int flags) {
     const bool fast = (flags & DCPSE_ASSEMBLE_FAST_FLAG) != 0;
     S.gstride = (h.npairs + 1) & ~1;
     S.nmax = 1;
-    S.rmax = 1;
+    S.qwords = 1;
     int off = 0;
     for (int g = 0; g < h.ngroups; ++g) {
+        const int n = h.gn[g];
         S.nrhs[g] = fast ? h.nout_rhs[g] : h.nterm_rhs[g];
         S.c_off[g] = off;
-        off += h.gn[g] * S.nrhs[g];
-        S.nmax = std::max(S.nmax, h.gn[g]);
-        S.rmax = std::max(S.rmax, S.nrhs[g]);
+        off += n * S.nrhs[g];
+        S.nmax = std::max(S.nmax, n);
+        S.qwords = std::max(S.qwords, n * (n + S.nrhs[g]) + n * S.nrhs[g]);
     }
     S.cstride = (off + 1) & ~1;
-    S.ldr = S.nmax + S.rmax;
     S.ldb = h.nu | 1;
     S.nslots = h.nslots;
     S.nout = h.noutputs;
