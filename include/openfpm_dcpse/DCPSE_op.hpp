@@ -112,36 +112,14 @@ PropRef<prp, vector_type> getV(vector_type& v) {
     return PropRef<prp, vector_type>{v};
 }
 
-// Verlet list of a particle set built on the GPU: every q != p with
-// |x_p - x_q|^2 < rCut^2, ascending q (the role of
-// vector_dist::getVerlet<VL_NON_SYMMETRIC|VL_SKIP_REF_PART>(rCut)).
+// Verlet list of a particle set built on the GPU: every q with
+// |x_p - x_q|^2 < rCut^2 in ascending q, without q == p unless skip_ref is
+// false (the roles of vector_dist::getVerlet<VL_NON_SYMMETRIC|VL_SKIP_REF_PART>
+// and getVerlet<VL_NON_SYMMETRIC>).
 template <typename particles_type>
-VerletList getVerlet(particles_type& parts, double rCut) {
+VerletList getVerlet(particles_type& parts, double rCut, bool skip_ref = true) {
     const int dim = particles_type::dims;
-    std::vector<unsigned> sig(dim, 0);
-    sig[0] = 1;
-    int terms = 1;
-    dcpse_plan_t* plan = nullptr;
-    detail::check(dcpse_plan_create(&plan, dim, 1, &terms, sig.data(), 2, 0.9));
-    std::unique_ptr<dcpse_plan_t, int (*)(dcpse_plan_t*)> guard(plan, dcpse_plan_destroy);
-    const std::size_t n = parts.size_local();
-    std::vector<double> pos(n * dim);
-    for (std::size_t p = 0; p < n; ++p)
-        for (int d = 0; d < dim; ++d) pos[p * dim + d] = (double)parts.getPos(p)[d];
-    detail::DevBuf dpos;
-    dpos.upload(pos.data(), std::max<std::size_t>(pos.size(), 1) * sizeof(double));
-    detail::check(dcpse_build_neighbors(plan, (const double*)dpos.get(), (int64_t)n, rCut, nullptr));
-    int64_t nn = 0, nnz = 0;
-    detail::check(dcpse_plan_info(plan, &nn, &nnz, nullptr, nullptr, nullptr));
-    const int64_t* drp = nullptr;
-    const int32_t* dcl = nullptr;
-    detail::check(dcpse_neighbors_ptr(plan, &drp, &dcl));
-    VerletList vl;
-    vl.rowptr.resize(n + 1);
-    vl.cols.resize((std::size_t)nnz);
-    detail::check(dcpse_copy(vl.rowptr.data(), drp, (n + 1) * sizeof(int64_t)));
-    if (nnz > 0) detail::check(dcpse_copy(vl.cols.data(), dcl, (std::size_t)nnz * sizeof(int32_t)));
-    return vl;
+    return detail::build_verlet(dim, detail::positions(parts, dim), nullptr, rCut, skip_ref);
 }
 
 // --------------------------------------------------------------- operators --

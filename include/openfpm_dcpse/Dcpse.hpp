@@ -112,11 +112,27 @@ public:
 
     template <typename Parts, typename VL>
     void set_particles(Parts& parts, VL& vl) {
-        n_ = (int64_t)parts.size_local();
+        set_particles(parts, parts, vl, false);
+    }
+
+    // two sets: rows are the domain particles, columns the support particles
+    template <typename Sup, typename Dom, typename VL>
+    void set_particles(Sup& sup, Dom& dom, VL& vl, bool two_set) {
+        n_ = (int64_t)dom.size_local();
+        n_sup_ = two_set ? (int64_t)sup.size_local() : n_;
         std::vector<double> pos((std::size_t)n_ * dim_);
         for (int64_t p = 0; p < n_; ++p)
-            for (int d = 0; d < dim_; ++d) pos[(std::size_t)p * dim_ + d] = (double)parts.getPos(p)[d];
-        pos_.upload(pos.data(), pos.size() * sizeof(double));
+            for (int d = 0; d < dim_; ++d) pos[(std::size_t)p * dim_ + d] = (double)dom.getPos(p)[d];
+        pos_.upload(pos.data(), std::max<std::size_t>(pos.size(), 1) * sizeof(double));
+        if (two_set) {
+            std::vector<double> sp((std::size_t)n_sup_ * dim_);
+            for (int64_t q = 0; q < n_sup_; ++q)
+                for (int d = 0; d < dim_; ++d) sp[(std::size_t)q * dim_ + d] = (double)sup.getPos(q)[d];
+            spos_.upload(sp.data(), std::max<std::size_t>(sp.size(), 1) * sizeof(double));
+            check(dcpse_plan_set_support(plan_, (const double*)spos_.get(), n_sup_, 1));
+        } else {
+            check(dcpse_plan_set_support(plan_, nullptr, 0, 1));
+        }
         rowptr_.assign((std::size_t)n_ + 1, 0);
         cols_.clear();
         for (int64_t p = 0; p < n_; ++p) {
@@ -156,6 +172,14 @@ public:
         check(dcpse_apply_output_f64(plan_, o, (const double*)fd_.get(), (double*)od_.get()));
         od_.download(out, (std::size_t)n_ * sizeof(double));
     }
+    // Dcpse::p2p of term t: f is [n_support][ncomp], out [n][ncomp]
+    void p2p(int t, const double* f, int ncomp, double* out) {
+        fd_.upload(f, (std::size_t)std::max<int64_t>(n_sup_ * ncomp, 1) * sizeof(double));
+        od_.ensure((std::size_t)std::max<int64_t>(n_ * ncomp, 1) * sizeof(double));
+        check(dcpse_p2p_f64(plan_, t, (const double*)fd_.get(), ncomp, (double*)od_.get()));
+        od_.download(out, (std::size_t)(n_ * ncomp) * sizeof(double));
+    }
+    int64_t n_support() const { return n_sup_; }
     void apply_term(int t, const double* f, double* out) {
         fd_.upload(f, (std::size_t)n_ * sizeof(double));
         od_.ensure((std::size_t)std::max<int64_t>(n_, 1) * sizeof(double));
@@ -218,11 +242,11 @@ public:
 private:
     int dim_ = 0, nout_ = 0;
     dcpse_plan_t* plan_ = nullptr;
-    int64_t n_ = 0;
+    int64_t n_ = 0, n_sup_ = 0;
     std::vector<unsigned> term_order_;
     std::vector<int64_t> rowptr_;
     std::vector<int32_t> cols_;
-    DevBuf pos_, fd_, od_;
+    DevBuf pos_, spos_, fd_, od_;
     bool cache_valid_ = false;
     std::vector<std::vector<double>> K_, eip_;
     std::vector<double> eps_;
@@ -260,6 +284,49 @@ OPENFPM_DCPSE_NO_CONTRACT T reference_sum(std::size_t k, FQ fq, T fxp, const dou
     return D * (T)eip;
 }
 
+// Neighbour lists built on the GPU: rows are the particles at dom, columns
+// the particles at sup (or dom itself, with or without the particle in its
+// own list when sup is null).
+inline VerletList build_verlet(int dim, const std::vector<double>& dom, const std::vector<double>* sup, double rCut,
+                               bool skip_ref) {
+    std::vector<unsigned> sig(dim, 0);
+    sig[0] = 1;
+    int terms = 1;
+    dcpse_plan_t* plan = nullptr;
+    check(dcpse_plan_create(&plan, dim, 1, &terms, sig.data(), 2, 0.9));
+    std::unique_ptr<dcpse_plan_t, int (*)(dcpse_plan_t*)> guard(plan, dcpse_plan_destroy);
+    const int64_t n = (int64_t)(dom.size() / dim);
+    DevBuf dpos, spos;
+    dpos.upload(dom.data(), std::max<std::size_t>(dom.size(), 1) * sizeof(double));
+    if (sup) {
+        spos.upload(sup->data(), std::max<std::size_t>(sup->size(), 1) * sizeof(double));
+        check(dcpse_plan_set_support(plan, (const double*)spos.get(), (int64_t)(sup->size() / dim), 1));
+    } else {
+        check(dcpse_plan_set_support(plan, nullptr, 0, skip_ref ? 1 : 0));
+    }
+    check(dcpse_build_neighbors(plan, (const double*)dpos.get(), n, rCut, nullptr));
+    int64_t nn = 0, nnz = 0;
+    check(dcpse_plan_info(plan, &nn, &nnz, nullptr, nullptr, nullptr));
+    const int64_t* drp = nullptr;
+    const int32_t* dcl = nullptr;
+    check(dcpse_neighbors_ptr(plan, &drp, &dcl));
+    VerletList vl;
+    vl.rowptr.resize((std::size_t)n + 1);
+    vl.cols.resize((std::size_t)nnz);
+    check(dcpse_copy(vl.rowptr.data(), drp, (std::size_t)(n + 1) * sizeof(int64_t)));
+    if (nnz > 0) check(dcpse_copy(vl.cols.data(), dcl, (std::size_t)nnz * sizeof(int32_t)));
+    return vl;
+}
+
+template <typename Parts>
+std::vector<double> positions(Parts& parts, int dim) {
+    const std::size_t n = parts.size_local();
+    std::vector<double> pos(n * dim);
+    for (std::size_t p = 0; p < n; ++p)
+        for (int d = 0; d < dim; ++d) pos[p * dim + d] = (double)parts.getPos(p)[d];
+    return pos;
+}
+
 inline void throw_too_few(int code, int64_t nbad) {
     if (nbad == 0) return;
     if (code == DCPSE_PART_TOO_FEW)
@@ -289,11 +356,64 @@ public:
           opt_(opt) {
         differentialOrder_ = 0;
         for (unsigned s : sig_) differentialOrder_ += s;
+        support_ = &particles;
+        domain_ = same_set(particles);
         particles.ghost_get_subset();
         plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder, (double)HOverEpsilon));
         plan_->set_particles(particles, verletList_);
         if (opt == support_options::LOAD) return;  // empty operator: load() or update later (Dcpse.hpp:703-707)
         assemble();
+    }
+
+    // Two particle sets (Dcpse.hpp:113-131): kernels of the domain particles
+    // over supports drawn from particlesSupport (verletList rows = domain
+    // particles, entries = support particles), as PPInterpolation uses.
+    template <typename Sig>
+    Dcpse(vector_type& particlesSupport, vector_type2& particlesDomain, VerletList_type& verletList,
+          const Sig& differentialSignature, unsigned int convergenceOrder, T rCut,
+          support_options opt = support_options::RADIUS)
+        : verletList_(verletList),
+          sig_(detail::sig_vector(differentialSignature, dim)),
+          convergenceOrder_(convergenceOrder),
+          rCut_(rCut),
+          opt_(opt) {
+        differentialOrder_ = 0;
+        for (unsigned s : sig_) differentialOrder_ += s;
+        support_ = &particlesSupport;
+        domain_ = &particlesDomain;
+        particlesSupport.ghost_get_subset();
+        plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder, (double)HOverEpsilon));
+        set_sets();
+        if (opt == support_options::LOAD) return;
+        assemble();
+    }
+
+    // Particle to particle interpolation (Dcpse.hpp:198-227): property prp2
+    // of every domain particle = epsInvPow_p * sum_q f_q K_pq, f = property
+    // prp1 of the support particles.
+    template <unsigned int prp1, unsigned int prp2>
+    void p2p() {
+        const int64_t ns = plan_->n_support(), n = plan_->n();
+        std::vector<double> f((std::size_t)ns), out((std::size_t)n);
+        for (int64_t q = 0; q < ns; ++q) f[(std::size_t)q] = (double)support_->template getProp<prp1>(q);
+        plan_->p2p(0, f.data(), 1, out.data());
+        typedef typename std::remove_reference<decltype(domain_->template getProp<prp2>(0))>::type T2;
+        for (int64_t p = 0; p < n; ++p) domain_->template getProp<prp2>(p) = (T2)out[(std::size_t)p];
+    }
+
+    // vector properties of N1 components (Dcpse.hpp:239-297)
+    template <unsigned int prp1, unsigned int prp2, std::size_t N1>
+    void p2p() {
+        const int64_t ns = plan_->n_support(), n = plan_->n();
+        std::vector<double> f((std::size_t)ns * N1), out((std::size_t)n * N1);
+        for (int64_t q = 0; q < ns; ++q)
+            for (std::size_t c = 0; c < N1; ++c)
+                f[(std::size_t)q * N1 + c] = (double)support_->template getProp<prp1>(q)[c];
+        plan_->p2p(0, f.data(), (int)N1, out.data());
+        typedef typename std::remove_reference<decltype(domain_->template getProp<prp2>(0)[0])>::type T2;
+        for (int64_t p = 0; p < n; ++p)
+            for (std::size_t c = 0; c < N1; ++c)
+                domain_->template getProp<prp2>(p)[c] = (T2)out[(std::size_t)p * N1 + c];
     }
 
     // Bulk apply: Df at every particle from property fValuePos into
@@ -333,8 +453,17 @@ public:
 
     // after particles moved (and the Verlet list was updated): Dcpse.hpp:675-687
     void initializeUpdate(vector_type& particles) {
+        support_ = &particles;
+        domain_ = same_set(particles);
         plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder_, (double)HOverEpsilon));
         plan_->set_particles(particles, verletList_);
+        assemble();
+    }
+    void initializeUpdate(vector_type& particlesSupport, vector_type2& particlesDomain) {
+        support_ = &particlesSupport;
+        domain_ = &particlesDomain;
+        plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder_, (double)HOverEpsilon));
+        set_sets();
         assemble();
     }
 
@@ -438,6 +567,22 @@ private:
         detail::throw_too_few(plan_->last_fail_code(), nbad);
     }
 
+    // the domain set of a one-set operator is the support set itself
+    vector_type2* same_set(vector_type& particles) {
+        if constexpr (std::is_same<vector_type, vector_type2>::value)
+            return &particles;
+        else
+            return nullptr;
+    }
+
+    // one set when both references name the same object
+    void set_sets() {
+        const bool two = (const void*)support_ != (const void*)domain_;
+        plan_->set_particles(*support_, *domain_, verletList_, two);
+    }
+
+    vector_type* support_ = nullptr;
+    vector_type2* domain_ = nullptr;
     VerletList_type& verletList_;
     std::vector<unsigned> sig_;
     unsigned differentialOrder_ = 0;

@@ -84,6 +84,18 @@ int dcpse_plan_set_stream(dcpse_plan_t* plan, void* stream);
  * axis is periodic.  Replaces the ghost layer the reference gets from
  * vector_dist::ghost_get (Dcpse.hpp:107). */
 int dcpse_plan_set_box(dcpse_plan_t* plan, const double* lo, const double* hi, const int* periodic);
+/* Support set of the neighbour lists (the columns).  With d_pos_support
+ * non-NULL the plan is a two-set operator: rows are the domain particles
+ * passed to dcpse_build_neighbors / dcpse_assemble, columns index the n_support
+ * support particles, and no entry is skipped (Dcpse's two-set constructor,
+ * Dcpse.hpp:113-131, as used by PPInterpolation, DcpseInterpolation.hpp:
+ * 55-81, with createVerletTwoPhase lists).  With NULL the domain set is its
+ * own support and self_skip selects VL_SKIP_REF_PART (1, the default) or a
+ * plain VL_NON_SYMMETRIC list that holds the particle itself (0).  The plan
+ * keeps the pointer, as the reference keeps a reference to the set; the
+ * neighbour list is dropped (build it again).  Derivative applies, adjoints
+ * and RK4 stages need one set and return DCPSE_ERR_STATE on two. */
+int dcpse_plan_set_support(dcpse_plan_t* plan, const double* d_pos_support, int64_t n_support, int self_skip);
 /* sizes: n particles, nnz neighbour entries, terms, outputs, max neighbours */
 int dcpse_plan_info(dcpse_plan_t* plan, int64_t* n, int64_t* nnz, int* n_terms, int* n_outputs,
                     int* max_neighbors);
@@ -157,6 +169,18 @@ int dcpse_apply_batched(dcpse_plan_t* plan, const double* d_f, double* d_out, in
 /* Same with host buffers h_f[n], h_out[n_outputs*n]: the copies are part of
  * the call (the reference's bulk apply reads and writes host particles). */
 int dcpse_apply_batched_host(dcpse_plan_t* plan, const double* h_f, double* h_out, int precision);
+
+/* ---- particle to particle interpolation --------------------------------
+ * Replaces Dcpse::p2p<prp1,prp2>() and p2p<prp1,prp2,N1>() (Dcpse.hpp:198-
+ * 297) behind PPInterpolation::p2p (DcpseInterpolation.hpp:133-160): for every
+ * domain particle p and component c,
+ *     out[p*ncomp + c] = epsInvPow_p * sum_q f[q*ncomp + c] K_pq
+ * with f on the support set (no f_p term).  dcpse_p2p_f64 uses the per-term
+ * FP64 kernels in the reference's order (DCPSE_STORE_TERMS_F64);
+ * dcpse_p2p applies every output at once from the summed weights, FP64 or
+ * FP32 (field as an exact float pair), out[o*n*ncomp + p*ncomp + c]. */
+int dcpse_p2p_f64(dcpse_plan_t* plan, int term, const double* d_f_support, int ncomp, double* d_out);
+int dcpse_p2p(dcpse_plan_t* plan, const double* d_f_support, int ncomp, double* d_out, int precision);
 
 /* ---- adjoint ------------------------------------------------------------
  * No counterpart in the reference (its operators have no derivatives); these

@@ -31,6 +31,7 @@ SIGNATURES = {
     "dcpse_plan_destroy": (_I, [_P]),
     "dcpse_plan_set_stream": (_I, [_P, _P]),
     "dcpse_plan_set_box": (_I, [_P, _c.POINTER(_D), _c.POINTER(_D), _PI]),
+    "dcpse_plan_set_support": (_I, [_P, _P, _I64, _I]),
     "dcpse_plan_info": (_I, [_P, _PI64, _PI64, _PI, _PI, _PI]),
     "dcpse_term_basis": (_I, [_P, _I, _PU, _I, _PI]),
     "dcpse_build_neighbors": (_I, [_P, _P, _I64, _D, _P]),
@@ -46,6 +47,8 @@ SIGNATURES = {
     "dcpse_apply_batched": (_I, [_P, _P, _P, _I]),
     "dcpse_apply_batched_host": (_I, [_P, _P, _P, _I]),
     "dcpse_apply_batched_f32_noalloc": (_I, [_I64, _I, _P, _P, _P, _I64, _P, _P, _P]),
+    "dcpse_p2p_f64": (_I, [_P, _I, _P, _I, _P]),
+    "dcpse_p2p": (_I, [_P, _P, _I, _P, _I]),
     "dcpse_set_term_kernels": (_I, [_P, _I, _P, _P, _P]),
     "dcpse_vjp_field": (_I, [_P, _P, _P, _I]),
     "dcpse_vjp_positions": (_I, [_P, _P, _P, _P, _P, _P]),

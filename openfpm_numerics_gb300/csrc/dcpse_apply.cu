@@ -52,9 +52,25 @@ __global__ void __launch_bounds__(256) apply_term_f64_kernel(int64_t n, const in
     }
 }
 
-__global__ void split_kernel(const double* __restrict__ f, int64_t n, float2* __restrict__ f2) {
+// Dcpse::p2p (Dcpse.hpp:198-297): Df_p = epsInvPow_p * (sum_q f_q K_pq) per
+// component, f on the support set ([n_sup][ncomp]), out on the domain set.
+__global__ void __launch_bounds__(256) p2p_f64_kernel(int64_t n, const int64_t* __restrict__ rowptr,
+                                                      const int32_t* __restrict__ cols, const double* __restrict__ K,
+                                                      const double* __restrict__ eip, int ncomp,
+                                                      const double* __restrict__ f, double* __restrict__ out) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = rowptr[p], e = rowptr[p + 1];
+        for (int c = 0; c < ncomp; ++c) {
+            double D = 0.0;
+            for (int64_t j = b; j < e; ++j) D = D + f[(int64_t)cols[j] * ncomp + c] * K[j];
+            out[p * ncomp + c] = eip[p] * D;
+        }
+    }
+}
+
+__global__ void split_kernel(const double* __restrict__ f, int64_t n, int64_t stride, float2* __restrict__ f2) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double v = f[i];
+        double v = f[i * stride];
         float hi = (float)v;
         float lo = (float)(v - (double)hi);
         f2[i] = make_float2(hi, lo);
@@ -129,8 +145,10 @@ struct F32Args {
     const __nv_bfloat16* r;         // [NO][ws] or null
     int64_t ws;                     // weight stream stride (elements)
     const float2* f2;
-    double* out;                    // [NO][n]
+    double* out;                    // output o of row r at out[o * oos + r * ors]
+    int64_t oos, ors;
     uint32_t comp;                  // outputs that take the compensated sum
+    int no_self;                    // interpolation: no f_p term, f2 indexed by the support set
 };
 
 // Neighbour entries of one lane, U at a time: all loads of a batch are issued
@@ -176,7 +194,7 @@ __global__ void __launch_bounds__(256) apply_f32_kernel(F32Args a) {
         RowAcc<NO, RESID> acc;
         acc.init();
         if (row < a.n) {
-            const float2 fp = a.f2[row];
+            const float2 fp = a.no_self ? make_float2(0.f, 0.f) : a.f2[row];
             const int64_t rb = a.rowptr[row];
             const int k = (int)(a.rowptr[row + 1] - rb);
             const int32_t* c = a.cols + rb;
@@ -184,7 +202,7 @@ __global__ void __launch_bounds__(256) apply_f32_kernel(F32Args a) {
             const __nv_bfloat16* r0 = RESID ? a.r + rb : nullptr;
             const int64_t ws = a.ws;
             row_entries<G, NO, RESID, U>(
-                acc, k, sub, (int32_t)row, fp, a.f2, a.comp, [&](int j) { return c[j]; },
+                acc, k, sub, a.no_self ? 0 : (int32_t)row, fp, a.f2, a.comp, [&](int j) { return c[j]; },
                 [&](int o, int j) { return w0[o * ws + j]; },
                 [&](int o, int j) { return __bfloat162float(r0[o * ws + j]); });
         }
@@ -192,7 +210,7 @@ __global__ void __launch_bounds__(256) apply_f32_kernel(F32Args a) {
         if (row < a.n) {
 #pragma unroll
             for (int o = 0; o < NO; ++o)
-                if (sub == (o & (G - 1))) a.out[(int64_t)o * a.n + row] = acc.value(o);
+                if (sub == (o & (G - 1))) a.out[(int64_t)o * a.oos + row * a.ors] = acc.value(o);
         }
     }
 }
@@ -336,7 +354,7 @@ __global__ void __launch_bounds__(256) apply_f32_tma_kernel(F32Args a, TmaCfg c,
         RowAcc<NO, RESID> acc;
         acc.init();
         if (row < a.n) {
-            const float2 fp = a.f2[row];
+            const float2 fp = a.no_self ? make_float2(0.f, 0.f) : a.f2[row];
             const int64_t rb = a.rowptr[row], re = a.rowptr[row + 1];
             const int32_t* cptr = scols + (rb - win_lo4(e0));
             const float* wp[NO];
@@ -347,7 +365,7 @@ __global__ void __launch_bounds__(256) apply_f32_tma_kernel(F32Args a, TmaCfg c,
                 rpp[o] = sr + (size_t)o * c.ecap + ((int64_t)o * a.ws + rb - win_lo8((int64_t)o * a.ws + e0));
             }
             row_entries<G, NO, RESID, 4>(
-                acc, (int)(re - rb), sub, (int32_t)row, fp, a.f2, a.comp, [&](int j) { return cptr[j]; },
+                acc, (int)(re - rb), sub, a.no_self ? 0 : (int32_t)row, fp, a.f2, a.comp, [&](int j) { return cptr[j]; },
                 [&](int o, int j) { return wp[o][j]; },
                 [&](int o, int j) { return __bfloat162float(rpp[o][j]); });
         }
@@ -355,7 +373,7 @@ __global__ void __launch_bounds__(256) apply_f32_tma_kernel(F32Args a, TmaCfg c,
         if (row < a.n) {
 #pragma unroll
             for (int o = 0; o < NO; ++o)
-                if (sub == (o & (G - 1))) a.out[(int64_t)o * a.n + row] = acc.value(o);
+                if (sub == (o & (G - 1))) a.out[(int64_t)o * a.oos + row * a.ors] = acc.value(o);
         }
         __syncthreads();  // every thread is done with stage s
         if (tid == 0) {
@@ -372,7 +390,8 @@ template <int G, int NO>
 __global__ void __launch_bounds__(256) apply_f64_kernel(int64_t n, const int64_t* __restrict__ rowptr,
                                                         const int32_t* __restrict__ cols,
                                                         const double* __restrict__ w, int64_t nnz,
-                                                        const double* __restrict__ f, double* __restrict__ out) {
+                                                        const double* __restrict__ f, double* __restrict__ out,
+                                                        int no_self, int64_t oos, int64_t ors, int64_t fs) {
     const int lane = threadIdx.x & 31;
     const int sub = lane & (G - 1);
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -384,10 +403,10 @@ __global__ void __launch_bounds__(256) apply_f64_kernel(int64_t n, const int64_t
 #pragma unroll
         for (int o = 0; o < NO; ++o) acc[o] = 0.0;
         if (row < n) {
-            const double fp = f[row];
+            const double fp = no_self ? 0.0 : f[row * fs];
             const int64_t e = rowptr[row + 1];
             for (int64_t j = rowptr[row] + sub; j < e; j += G) {
-                const double d = f[cols[j]] - fp;
+                const double d = f[(int64_t)cols[j] * fs] - fp;
 #pragma unroll
                 for (int o = 0; o < NO; ++o) acc[o] = fma(w[(int64_t)o * nnz + j], d, acc[o]);
             }
@@ -400,7 +419,7 @@ __global__ void __launch_bounds__(256) apply_f64_kernel(int64_t n, const int64_t
         if (row < n) {
 #pragma unroll
             for (int o = 0; o < NO; ++o)
-                if (sub == (o & (G - 1))) out[(int64_t)o * n + row] = acc[o];
+                if (sub == (o & (G - 1))) out[(int64_t)o * oos + row * ors] = acc[o];
         }
     }
 }
@@ -490,11 +509,12 @@ cudaError_t dispatch_f32(const F32Args& a, int nout, int maxk, int* err, int mod
 
 template <int G>
 cudaError_t launch_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const double* w, int64_t nnz,
-                       const double* f, double* out, cudaStream_t s) {
+                       const double* f, double* out, int no_self, int64_t oos, int64_t ors, int64_t fs,
+                       cudaStream_t s) {
     const int grid = grid_rows(n, 256 / G);
-#define DCPSE_F64_CASE(NO)                                                                            \
-    case NO:                                                                                          \
-        apply_f64_kernel<G, NO><<<grid, 256, 0, s>>>(n, rowptr, cols, w, nnz, f, out);                \
+#define DCPSE_F64_CASE(NO)                                                                                     \
+    case NO:                                                                                                   \
+        apply_f64_kernel<G, NO><<<grid, 256, 0, s>>>(n, rowptr, cols, w, nnz, f, out, no_self, oos, ors, fs);  \
         break;
     switch (nout) {
         DCPSE_F64_CASE(1)
@@ -525,11 +545,20 @@ cudaError_t apply_term_f64(int64_t n, const int64_t* rowptr, const int32_t* cols
     return cudaGetLastError();
 }
 
-cudaError_t split_f64(const double* f, int64_t n, float2* f2, cudaStream_t s) {
+cudaError_t split_f64(const double* f, int64_t n, float2* f2, cudaStream_t s, int64_t stride) {
     if (n == 0) return cudaSuccess;
     int64_t g = (n + 255) / 256;
     int64_t cap = (int64_t)num_sms() * 8;
-    split_kernel<<<(unsigned)(g < cap ? g : cap), 256, 0, s>>>(f, n, f2);
+    split_kernel<<<(unsigned)(g < cap ? g : cap), 256, 0, s>>>(f, n, stride, f2);
+    return cudaGetLastError();
+}
+
+cudaError_t p2p_f64(int64_t n, const int64_t* rowptr, const int32_t* cols, const double* K, const double* eip,
+                    int ncomp, const double* f, double* out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    int64_t g = (n + 255) / 256;
+    int64_t cap = (int64_t)num_sms() * 8;
+    p2p_f64_kernel<<<(unsigned)(g < cap ? g : cap), 256, 0, s>>>(n, rowptr, cols, K, eip, ncomp, f, out);
     return cudaGetLastError();
 }
 
@@ -544,7 +573,10 @@ cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s) {
     a.ws = p.ws;
     a.f2 = p.f2;
     a.out = p.out;
+    a.oos = p.oos ? p.oos : p.n;
+    a.ors = p.ors ? p.ors : 1;
     a.comp = p.comp;
+    a.no_self = p.no_self;
     const int G = p.lanes ? p.lanes : lanes_for(p.n, p.nnz);
     const bool resid = p.resid != nullptr;
     const int mode = p.mode;  // 0 auto (staged if it fits), 1 direct, 2 staged, 3 direct x8
@@ -585,12 +617,16 @@ cudaError_t apply_batched_f32(int64_t n, int nout, const int64_t* rowptr, const 
 }
 
 cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const double* w,
-                              int64_t nnz, const double* f, double* out, cudaStream_t s) {
+                              int64_t nnz, const double* f, double* out, cudaStream_t s, int no_self, int64_t oos,
+                              int64_t ors, int64_t fs) {
     if (n == 0) return cudaSuccess;
+    if (oos == 0) oos = n;
+    if (ors == 0) ors = 1;
+    if (fs == 0) fs = 1;
     switch (lanes_for(n, nnz)) {
-        case 8: return launch_f64<8>(n, nout, rowptr, cols, w, nnz, f, out, s);
-        case 16: return launch_f64<16>(n, nout, rowptr, cols, w, nnz, f, out, s);
-        default: return launch_f64<32>(n, nout, rowptr, cols, w, nnz, f, out, s);
+        case 8: return launch_f64<8>(n, nout, rowptr, cols, w, nnz, f, out, no_self, oos, ors, fs, s);
+        case 16: return launch_f64<16>(n, nout, rowptr, cols, w, nnz, f, out, no_self, oos, ors, fs, s);
+        default: return launch_f64<32>(n, nout, rowptr, cols, w, nnz, f, out, no_self, oos, ors, fs, s);
     }
 }
 

@@ -68,7 +68,7 @@ struct Split {
 template <int DIM>
 __device__ __forceinline__ void load_offset(const AsmArgs& a, const double* xp, int64_t q, double* o) {
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) o[d] = offset1(a.geom, d, xp[d], a.pos[q * DIM + d]);
+    for (int d = 0; d < DIM; ++d) o[d] = offset1(a.geom, d, xp[d], a.spos[q * DIM + d]);
 }
 
 __device__ __forceinline__ int group_status(int32_t word, int g) { return (word >> (4 * g)) & 15; }

@@ -91,14 +91,14 @@ __global__ void status_summary_kernel(const int32_t* st, int64_t n, unsigned lon
 
 // Checks a caller-supplied CSR list: rowptr[0] = 0, rowptr[n] = nnz, rows
 // non-decreasing, every column in [0, n).  bad[0] counts violations.
-__global__ void csr_check_kernel(const int64_t* rowptr, const int32_t* cols, int64_t n, int64_t nnz,
+__global__ void csr_check_kernel(const int64_t* rowptr, const int32_t* cols, int64_t n, int64_t nnz, int64_t ncols,
                                  unsigned long long* bad) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     for (int64_t i = t0; i < n; i += stride)
         if (rowptr[i + 1] < rowptr[i]) atomicAdd(bad, 1ull);
     for (int64_t j = t0; j < nnz; j += stride)
-        if (cols[j] < 0 || (int64_t)cols[j] >= n) atomicAdd(bad, 1ull);
+        if (cols[j] < 0 || (int64_t)cols[j] >= ncols) atomicAdd(bad, 1ull);
     if (t0 == 0 && (rowptr[0] != 0 || rowptr[n] != nnz)) atomicAdd(bad, 1ull);
 }
 
@@ -185,6 +185,12 @@ struct dcpse_plan_s {
     bool has_box = false;
     double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     int per[3] = {0, 0, 0};
+    // support set of the columns (PPInterpolation, two-set Dcpse); null: the
+    // domain set itself, with or without the particle itself in its list
+    const double* sup_pos = nullptr;
+    int64_t n_sup = 0;
+    int self_skip = 1;
+    bool two_set() const { return sup_pos != nullptr; }
     // neighbour list
     int64_t n = -1, nnz = 0;
     int maxk = 0;
@@ -234,6 +240,7 @@ struct dcpse_plan_s {
     }
     // apply scratch
     float2* f2 = nullptr;
+    int64_t f2_len = 0;
     double* hf = nullptr;    // device copy of a host field (host apply)
     double* hout = nullptr;  // device output for host apply
 
@@ -449,6 +456,29 @@ int check_plan(dcpse_plan_t* P) {
     return DCPSE_OK;
 }
 
+// Derivative applies, adjoints and the RK4 stages read f on the rows and on
+// the columns: they need the domain set to be its own support.
+int check_single_set(dcpse_plan_t* P) {
+    if (P->two_set())
+        return fail(DCPSE_ERR_STATE, "this operation needs a single particle set (use dcpse_p2p on two sets)");
+    return DCPSE_OK;
+}
+
+// FP32 split of n field values (stride apart) into the plan's scratch
+int split_into_plan(dcpse_plan_t* P, const double* d_f, int64_t n, int64_t stride) {
+    if (P->f2_len < n) {
+        dfree(P->f2);
+        P->f2_len = 0;
+        DCPSE_CK(dalloc(&P->f2, (size_t)n));
+        P->f2_len = n;
+    }
+    P->tstart(DCPSE_K_SPLIT);
+    cudaError_t e = split_f64(d_f, n, P->f2, P->stream, stride);
+    P->tstop(DCPSE_K_SPLIT);
+    DCPSE_CK(e);
+    return DCPSE_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -540,6 +570,24 @@ int dcpse_plan_set_box(dcpse_plan_t* P, const double* lo, const double* hi, cons
     return DCPSE_OK;
 }
 
+int dcpse_plan_set_support(dcpse_plan_t* P, const double* d_pos_support, int64_t n_support, int self_skip) {
+    if (int rc = check_plan(P)) return rc;
+    if (d_pos_support && n_support < 0) return fail(DCPSE_ERR_ARG, "bad support set size");
+    if (d_pos_support && n_support >= (int64_t)INT32_MAX) return fail(DCPSE_ERR_CAPACITY, "at most 2^31-1 particles");
+    // the neighbour list and everything assembled on it refer to the old sets
+    P->free_assembly();
+    P->free_transpose();
+    dfree(P->rowptr);
+    dfree(P->cols);
+    P->n = -1;
+    P->nnz = 0;
+    P->maxk = 0;
+    P->sup_pos = d_pos_support;
+    P->n_sup = d_pos_support ? n_support : 0;
+    P->self_skip = self_skip ? 1 : 0;
+    return DCPSE_OK;
+}
+
 int dcpse_plan_info(dcpse_plan_t* P, int64_t* n, int64_t* nnz, int* n_terms, int* n_outputs, int* max_neighbors) {
     if (int rc = check_plan(P)) return rc;
     if (n) *n = P->n;
@@ -591,7 +639,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
             hi[d] = P->hi[d];
         }
     } else {
-        cudaError_t e = bounding_box(dim, d_pos, n, nullptr, 0, lo, hi, mm, s);
+        cudaError_t e = bounding_box(dim, d_pos, n, P->sup_pos, P->two_set() ? P->n_sup : 0, lo, hi, mm, s);
         if (e != cudaSuccess) {
             dfree(mm);
             return fail(DCPSE_ERR_CUDA, std::string("bounding box: ") + cudaGetErrorString(e));
@@ -621,10 +669,13 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
         rmax = std::max(rcut > 0 ? rcut : 0.0, rhi[0]);
     }
     dfree(mm);
+    // the cell list holds the support set (the domain set itself for one set)
+    const double* ps = P->two_set() ? P->sup_pos : d_pos;
+    const int64_t ns = P->two_set() ? P->n_sup : n;
     // cells no smaller than the largest radius; total bounded by ~4 n
     CellGrid cg{};
     double cmin = rmax * (1.0 + 1e-9);
-    double cap = std::max(4.0 * (double)n, 1024.0);
+    double cap = std::max(4.0 * (double)std::max(n, ns), 1024.0);
     for (int it = 0; it < 64; ++it) {
         double total = 1.0;
         for (int d = 0; d < kMaxDim; ++d) {
@@ -663,17 +714,17 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
         dfree(maxk);
     };
     cudaError_t e = cudaSuccess;
-    if (e == cudaSuccess) e = dalloc(&cell, n);
+    if (e == cudaSuccess) e = dalloc(&cell, ns);
     if (e == cudaSuccess) e = dalloc(&ccount, ncell);
-    if (e == cudaSuccess) e = dalloc(&cidx, n);
+    if (e == cudaSuccess) e = dalloc(&cidx, ns);
     if (e == cudaSuccess) e = dalloc(&counts, n);
     if (e == cudaSuccess) e = dalloc(&cstart, ncell + 1);
     if (e == cudaSuccess) e = dalloc(&fill, ncell);
     if (e == cudaSuccess) e = dalloc(&scan_tmp, scan_tmp_elems(std::max<int64_t>(ncell, n)));
-    if (e == cudaSuccess) e = dalloc(&spos, (size_t)n * dim);
+    if (e == cudaSuccess) e = dalloc(&spos, (size_t)ns * dim);
     if (e == cudaSuccess) e = dalloc(&maxk, 1);
     if (e == cudaSuccess) e = cudaMemsetAsync(maxk, 0, sizeof(int), s);
-    if (e == cudaSuccess) e = build_cells(dim, d_pos, n, cg, cell, ccount, cstart, fill, cidx, spos, scan_tmp, s);
+    if (e == cudaSuccess) e = build_cells(dim, ps, ns, cg, cell, ccount, cstart, fill, cidx, spos, scan_tmp, s);
     NbrArgs a{};
     a.dim = dim;
     a.pd = d_pos;
@@ -685,7 +736,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     a.geom = plan_geom(P);
     a.rcut = rcut;
     a.rcut_pp = d_rcut_pp;
-    a.self_skip = 1;
+    a.self_skip = P->two_set() ? 0 : P->self_skip;
     if (e == cudaSuccess) e = count_neighbors(a, counts, maxk, s);
     if (e == cudaSuccess) e = exclusive_scan_i32(counts, n, P->rowptr, scan_tmp, s);
     int64_t nnz = 0;
@@ -724,7 +775,7 @@ int dcpse_set_neighbors(dcpse_plan_t* P, int64_t n, int64_t nnz, const int64_t* 
         DCPSE_CK(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), s));
         int64_t work = std::max<int64_t>(n, nnz);
         csr_check_kernel<<<std::max(1, (int)std::min<int64_t>(num_sms() * 8, (work + 255) / 256)), 256, 0, s>>>(
-            P->rowptr, P->cols, n, nnz, bad);
+            P->rowptr, P->cols, n, nnz, P->two_set() ? P->n_sup : n, bad);
         unsigned long long hb = 0;
         cudaError_t e = cudaMemcpyAsync(&hb, bad, sizeof hb, cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -792,6 +843,7 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     a.dim = P->dim;
     a.n = n;
     a.pos = d_pos;
+    a.spos = P->two_set() ? P->sup_pos : d_pos;
     a.rowptr = P->rowptr;
     a.cols = P->cols;
     a.geom = plan_geom(P);
@@ -981,6 +1033,7 @@ int ensure_transpose(dcpse_plan_t* P) {
 
 int dcpse_vjp_field(dcpse_plan_t* P, const double* d_g, double* d_out, int precision) {
     if (int rc = check_plan(P)) return rc;
+    if (int rc = check_single_set(P)) return rc;
     if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
     if (P->n > 0 && (!d_g || !d_out)) return fail(DCPSE_ERR_ARG, "NULL array");
     const double* w64 = nullptr;
@@ -1008,6 +1061,7 @@ int dcpse_vjp_field(dcpse_plan_t* P, const double* d_g, double* d_out, int preci
 int dcpse_vjp_positions(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fixed, const double* d_f,
                         const double* d_g, double* d_grad) {
     if (int rc = check_plan(P)) return rc;
+    if (int rc = check_single_set(P)) return rc;
     if (P->n < 0) return fail(DCPSE_ERR_STATE, "no neighbour list");
     if (P->n > 0 && (!d_pos || !d_f || !d_g || !d_grad)) return fail(DCPSE_ERR_ARG, "NULL array");
     if (int rc = ensure_transpose(P)) return rc;
@@ -1031,6 +1085,7 @@ int dcpse_vjp_positions(dcpse_plan_t* P, const double* d_pos, const double* d_ep
 int dcpse_rk4_gs_stage(dcpse_plan_t* P, int stage, int precision, const void* Yu, const void* Yv, const void* y0u,
                        const void* y0v, void* accu, void* accv, void* outu, void* outv, const double* params) {
     if (int rc = check_plan(P)) return rc;
+    if (int rc = check_single_set(P)) return rc;
     if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
     if (stage < 0 || stage > 3 || !params) return fail(DCPSE_ERR_ARG, "stage 0..3 and params {Du,Dv,F,k,dt}");
     if (P->n > 0 && (!Yu || !Yv || !y0u || !y0v || !accu || !accv || !outu || !outv))
@@ -1056,6 +1111,7 @@ int dcpse_rk4_gs_stage(dcpse_plan_t* P, int stage, int precision, const void* Yu
 
 int dcpse_rk4_gs_adjoint_prepare(dcpse_plan_t* P, int precision) {
     if (int rc = check_plan(P)) return rc;
+    if (int rc = check_single_set(P)) return rc;
     if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
     if (int rc = ensure_transpose(P)) return rc;
     if (precision == DCPSE_F32) {
@@ -1123,6 +1179,7 @@ int dcpse_copy(void* dst, const void* src, uint64_t bytes) {
 
 int dcpse_apply_term_f64(dcpse_plan_t* P, int term, const double* d_f, double* d_out) {
     if (int rc = check_plan(P)) return rc;
+    if (int rc = check_single_set(P)) return rc;
     if (!P->assembled || !P->k_term) return fail(DCPSE_ERR_STATE, "per-term FP64 kernels not stored");
     if (term < 0 || term >= P->nterms) return fail(DCPSE_ERR_ARG, "term out of range");
     if (P->n > 0 && (!d_f || !d_out)) return fail(DCPSE_ERR_ARG, "NULL field");
@@ -1138,6 +1195,7 @@ int dcpse_apply_term_f64(dcpse_plan_t* P, int term, const double* d_f, double* d
 
 int dcpse_apply_output_f64(dcpse_plan_t* P, int output, const double* d_f, double* d_out) {
     if (int rc = check_plan(P)) return rc;
+    if (int rc = check_single_set(P)) return rc;
     if (!P->assembled || !P->k_term) return fail(DCPSE_ERR_STATE, "per-term FP64 kernels not stored");
     if (output < 0 || output >= P->nout) return fail(DCPSE_ERR_ARG, "output out of range");
     if (P->n > 0 && (!d_f || !d_out)) return fail(DCPSE_ERR_ARG, "NULL field");
@@ -1159,17 +1217,14 @@ int dcpse_apply_output_f64(dcpse_plan_t* P, int output, const double* d_f, doubl
 
 int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int precision) {
     if (int rc = check_plan(P)) return rc;
+    if (int rc = check_single_set(P)) return rc;
     if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
     if (P->n > 0 && (!d_f || !d_out)) return fail(DCPSE_ERR_ARG, "NULL field");
     if (precision == DCPSE_F32 || precision == DCPSE_F32_RESID) {
         if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
         if (precision == DCPSE_F32_RESID && !P->r16)
             return fail(DCPSE_ERR_STATE, "FP32 residuals not stored (DCPSE_STORE_OUT_F32_RESID)");
-        if (!P->f2) DCPSE_CK(dalloc(&P->f2, P->n));
-        P->tstart(DCPSE_K_SPLIT);
-        cudaError_t e = split_f64(d_f, P->n, P->f2, P->stream);
-        P->tstop(DCPSE_K_SPLIT);
-        DCPSE_CK(e);
+        if (int rc = split_into_plan(P, d_f, P->n, 1)) return rc;
         ApplyF32 ap{};
         ap.n = P->n;
         ap.nout = P->nout;
@@ -1196,7 +1251,7 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
         // the residual correction only pays off with compensated sums
         if ((P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) || precision == DCPSE_F32_RESID) ap.comp = 0xffffffffu;
         P->tstart(DCPSE_K_APPLY_BATCHED);
-        e = apply_batched_f32x(ap, P->stream);
+        cudaError_t e = apply_batched_f32x(ap, P->stream);
         P->tstop(DCPSE_K_APPLY_BATCHED);
         if (e == cudaErrorInvalidConfiguration && (P->apply_mode & 15) == 2)
             return fail(DCPSE_ERR_CAPACITY, "TMA-staged tiles of this plan do not fit in shared memory "
@@ -1216,6 +1271,7 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
 
 int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, int precision) {
     if (int rc = check_plan(P)) return rc;
+    if (int rc = check_single_set(P)) return rc;
     if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
     if (P->n > 0 && (!h_f || !h_out)) return fail(DCPSE_ERR_ARG, "NULL field");
     if (!P->hf) DCPSE_CK(dalloc(&P->hf, P->n));
@@ -1225,6 +1281,72 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
     if (rc != DCPSE_OK) return rc;
     DCPSE_CK(cudaMemcpyAsync(h_out, P->hout, sizeof(double) * P->nout * P->n, cudaMemcpyDeviceToHost, P->stream));
     return dcpse_plan_check(P);
+}
+
+int dcpse_p2p_f64(dcpse_plan_t* P, int term, const double* d_f_support, int ncomp, double* d_out) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled || !P->k_term) return fail(DCPSE_ERR_STATE, "per-term FP64 kernels not stored");
+    if (term < 0 || term >= P->nterms) return fail(DCPSE_ERR_ARG, "term out of range");
+    if (ncomp < 1) return fail(DCPSE_ERR_ARG, "ncomp must be >= 1");
+    if ((P->two_set() ? P->n_sup : P->n) > 0 && !d_f_support) return fail(DCPSE_ERR_ARG, "NULL field");
+    if (P->n > 0 && !d_out) return fail(DCPSE_ERR_ARG, "NULL output");
+    P->tstart(DCPSE_K_APPLY_TERM);
+    cudaError_t e = p2p_f64(P->n, P->rowptr, P->cols, P->k_term + (size_t)term * P->nnz,
+                            P->eip_group + (size_t)P->term_group[term] * P->n, ncomp, d_f_support, d_out, P->stream);
+    P->tstop(DCPSE_K_APPLY_TERM);
+    DCPSE_CK(e);
+    return DCPSE_OK;
+}
+
+int dcpse_p2p(dcpse_plan_t* P, const double* d_f_support, int ncomp, double* d_out, int precision) {
+    if (int rc = check_plan(P)) return rc;
+    if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
+    if (ncomp < 1) return fail(DCPSE_ERR_ARG, "ncomp must be >= 1");
+    const int64_t nf = P->two_set() ? P->n_sup : P->n;
+    if (nf > 0 && !d_f_support) return fail(DCPSE_ERR_ARG, "NULL field");
+    if (P->n > 0 && !d_out) return fail(DCPSE_ERR_ARG, "NULL output");
+    for (int c = 0; c < ncomp; ++c) {
+        if (precision == DCPSE_F32) {
+            if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
+            if (nf > 0)
+                if (int rc = split_into_plan(P, d_f_support + c, nf, ncomp)) return rc;
+            ApplyF32 ap{};
+            ap.n = P->n;
+            ap.nout = P->nout;
+            ap.rowptr = P->rowptr;
+            ap.cols = P->cols;
+            ap.w = P->w32;
+            ap.ws = P->nnz;
+            ap.nnz = P->nnz;
+            ap.maxk = P->maxk;
+            ap.f2 = P->f2;
+            ap.out = d_out + c;
+            ap.oos = P->n * ncomp;
+            ap.ors = ncomp;
+            ap.err = P->d_err;
+            ap.mode = P->apply_mode & 15;
+            ap.lanes = P->apply_lanes;
+            ap.comp = (P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) ? 0xffffffffu : 0u;
+            ap.no_self = 1;
+            P->tstart(DCPSE_K_APPLY_BATCHED);
+            cudaError_t e = apply_batched_f32x(ap, P->stream);
+            P->tstop(DCPSE_K_APPLY_BATCHED);
+            if (e == cudaErrorInvalidConfiguration && (P->apply_mode & 15) == 2)
+                return fail(DCPSE_ERR_CAPACITY, "TMA-staged tiles of this plan do not fit in shared memory");
+            DCPSE_CK(e);
+        } else if (precision == DCPSE_F64) {
+            if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
+            P->tstart(DCPSE_K_APPLY_BATCHED);
+            cudaError_t e = apply_batched_f64(P->n, P->nout, P->rowptr, P->cols, P->w64, P->nnz,
+                                              nf > 0 ? d_f_support + c : nullptr, d_out + c, P->stream, 1,
+                                              P->n * ncomp, ncomp, ncomp);
+            P->tstop(DCPSE_K_APPLY_BATCHED);
+            DCPSE_CK(e);
+        } else {
+            return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
+        }
+    }
+    return DCPSE_OK;
 }
 
 int dcpse_plan_check(dcpse_plan_t* P) {

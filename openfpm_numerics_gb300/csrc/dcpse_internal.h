@@ -106,7 +106,8 @@ struct AsmArgs {
     const AsmTables* tab;  // device copy
     int dim;
     int64_t n;
-    const double* pos;
+    const double* pos;     // domain positions (the rows)
+    const double* spos;    // support positions (the columns); pos for one set
     const int64_t* rowptr;
     const int32_t* cols;
     Geom geom;
@@ -147,7 +148,11 @@ cudaError_t assemble(const AsmArgs& a, const AsmTables& h, cudaStream_t s);
 cudaError_t apply_term_f64(int64_t n, const int64_t* rowptr, const int32_t* cols, const double* K,
                            const double* eip, unsigned ord, const double* f, double* out, int accumulate,
                            cudaStream_t s);
-cudaError_t split_f64(const double* f, int64_t n, float2* f2, cudaStream_t s);
+// (hi, lo) float pair of f[i * stride], i < n
+cudaError_t split_f64(const double* f, int64_t n, float2* f2, cudaStream_t s, int64_t stride = 1);
+// Dcpse::p2p: out[p][c] = eip_p * sum_q f[q][c] K_pq (reference order)
+cudaError_t p2p_f64(int64_t n, const int64_t* rowptr, const int32_t* cols, const double* K, const double* eip,
+                    int ncomp, const double* f, double* out, cudaStream_t s);
 // Batched FP32 apply with caller-owned arrays: direct (unstaged) kernel,
 // lanes per row from nnz / n.
 cudaError_t apply_batched_f32(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const float* w,
@@ -170,10 +175,13 @@ struct ApplyF32 {
     int mode;              // 0 staged if it fits else direct, 1 direct, 2 staged, 3 direct x8
     int lanes;             // lanes per row (0 = from the mean row length)
     uint32_t comp;         // outputs taking the compensated FP32 sum (bit per output)
+    int no_self;           // interpolation: sum w f_q without the f_p term; f2 on the support set
+    int64_t oos, ors;      // output o of row r at out[o * oos + r * ors] (0: n and 1)
 };
 cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s);
 cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const double* w,
-                              int64_t nnz, const double* f, double* out, cudaStream_t s);
+                              int64_t nnz, const double* f, double* out, cudaStream_t s, int no_self = 0,
+                              int64_t oos = 0, int64_t ors = 0, int64_t fs = 0);
 
 // --------------------------------------------------------------- adjoint --
 // transposed list: trow[n+1], per entry the source row tsrc and entry index tidx

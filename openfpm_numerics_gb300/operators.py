@@ -37,13 +37,27 @@ class support_options(enum.IntEnum):
     AT_LEAST_N_PARTICLES = 3
 
 
+# Verlet-list options of openfpm's vector_dist::getVerlet<opt> that decide
+# the DC-PSE supports (flag values are this mirror's own)
+VL_NON_SYMMETRIC = 1
+VL_SKIP_REF_PART = 2
+
+
 class VerletList:
     """Neighbour lists in CSR form (rowptr int64 [n+1], cols int32), built on
-    the device: every q != p with |x_p - x_q|^2 < rCut^2, ascending q."""
+    the device: every q with |x_p - x_q|^2 < rCut^2 in ascending q, without
+    q == p when VL_SKIP_REF_PART is set.  With ``support`` the rows are the
+    particles of ``parts`` and the columns those of ``support``
+    (createVerletTwoPhase)."""
 
-    def __init__(self, parts, rCut, rcut_pp=None):
+    def __init__(self, parts, rCut, rcut_pp=None, opt=VL_NON_SYMMETRIC | VL_SKIP_REF_PART, support=None):
         self.rCut = float(rCut)
+        self.support = support
         plan = DcpsePlan(parts.dims, [[(1,) + (0,) * (parts.dims - 1)]], box=parts.box)
+        if support is not None:
+            plan.set_support(support.getPosTensor())
+        else:
+            plan.set_support(None, self_skip=bool(opt & VL_SKIP_REF_PART))
         plan.build_neighbors(parts.getPosTensor(), self.rCut, rcut_pp)
         rp, cl = plan.neighbors()
         self.rowptr = rp.clone()
@@ -87,8 +101,8 @@ class ParticleSet:
         self.pos = pos.to(device="cuda", dtype=torch.float64).contiguous()
         self._map_ctr += 1
 
-    def getVerlet(self, rCut):
-        return VerletList(self, rCut)
+    def getVerlet(self, rCut, opt=VL_NON_SYMMETRIC | VL_SKIP_REF_PART):
+        return VerletList(self, rCut, opt=opt)
 
     def ghost_get_subset(self):
         """No-op: a single GPU holds all particles; periodic images are
@@ -263,6 +277,86 @@ class OperatorSet(_DcpseOp):
                     sig[axes[ch]] += 1
                 outs.append([tuple(sig)])
         super().__init__(parts, verletList, ord, rCut, opt, outputs=outs, kind="vector", **kw)
+
+
+def createVerletTwoPhase(particlesDomain, particlesSupport, rCut, cellList=None):
+    """Lists of the support particles within rCut of every domain particle
+    (openfpm's createVerletTwoPhase, used by the two-set tests of
+    DCPSE_op_test_base_tests.cpp:369-372).  The cell list argument of the
+    reference is accepted and ignored: the lists are built on the device."""
+    return VerletList(particlesDomain, rCut, support=particlesSupport)
+
+
+class PPInterpolation:
+    """PPInterpolation (src/DCPSE/DcpseInterpolation.hpp:28-195): DC-PSE
+    particle to particle interpolation from particlesSupport to
+    particlesDomain, i.e. a Dcpse with signature 0 on two particle sets
+    (Dcpse.hpp:113-131) evaluated by p2p (Dcpse.hpp:198-297).
+
+        Fx = PPInterpolation(support, domain, verletList, 2, rCut)
+        Fx.p2p(0, 1)        # domain.props[1] = interpolation of support.props[0]
+        g = Fx(f_support)   # the same on tensors
+
+    The neighbour list rows are the domain particles, the columns the support
+    particles (createVerletTwoPhase, or getVerlet of one set that is both)."""
+
+    def __init__(self, particlesSupport, particlesDomain, verletList, ord, rCut, opt=support_options.RADIUS,
+                 *, allow_failed_particles=False, h_over_eps=0.9):
+        if opt not in (support_options.RADIUS, support_options.LOAD):
+            raise NotImplementedError("support option %r" % (opt,))
+        self.particlesSupport = particlesSupport
+        self.particlesDomain = particlesDomain
+        self.verletList = verletList
+        self.dim = particlesDomain.dims
+        self.ord = int(ord)
+        self.rCut = float(rCut)
+        self._allow = allow_failed_particles
+        self.plan = DcpsePlan(self.dim, [[(0,) * self.dim]], order=self.ord, h_over_eps=h_over_eps,
+                              box=particlesDomain.box)
+        self._assembled = False
+        if opt == support_options.RADIUS:
+            self.update()
+
+    def update(self, verletList=None):
+        """initializeUpdate(particlesSupport, particlesDomain)
+        (DcpseInterpolation.hpp:187-190): re-assemble on the current positions."""
+        if verletList is not None:
+            self.verletList = verletList
+        two = self.particlesSupport is not self.particlesDomain
+        self.plan.set_support(self.particlesSupport.getPosTensor() if two else None)
+        self.plan.set_neighbors(self.verletList.rowptr, self.verletList.cols)
+        rc = self.plan.assemble(self.particlesDomain.getPosTensor(),
+                                C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+        if rc == C.ERR_PARTICLES and not self._allow:
+            nb, first, code = self.plan.particle_status()
+            if code == C.PART_TOO_FEW:
+                raise ValueError("Not enough neighbour points passed for Vandermonde matrix construction! "
+                                 "(%d particles, first %d)" % (nb, first))
+            raise RuntimeError("DC-PSE assembly failed for %d particles (first %d, status %d)" % (nb, first, code))
+        self._assembled = True
+
+    def __call__(self, f, precision="f64"):
+        """Interpolated field on the domain set: f is [n_support] or
+        [n_support, N1] (vector property, p2p<prp1,prp2,N1>)."""
+        if not self._assembled:
+            raise RuntimeError("operator not assembled (support_options.LOAD without update)")
+        f = f.to(device="cuda", dtype=torch.float64).contiguous()
+        if precision == "f64":
+            return self.plan.p2p_f64(0, f)
+        if precision in ("f32", "f64-batched"):
+            return self.plan.p2p(f, C.F32 if precision == "f32" else C.F64)[0]
+        raise ValueError("precision must be 'f64', 'f64-batched' or 'f32'")
+
+    def p2p(self, propSupport, propDomain, N1=None):
+        """p2p<propSupport, propDomain>() and p2p<propSupport, propDomain, N1>()
+        (DcpseInterpolation.hpp:133-160) on the sets' named properties."""
+        f = self.particlesSupport.props[propSupport]
+        if N1 is not None and (f.dim() != 2 or f.shape[1] != N1):
+            raise ValueError("property %r is not a vector of %d components" % (propSupport, N1))
+        self.particlesDomain.props[propDomain] = self(f)
+
+    def deallocate(self):
+        self.plan.close()
 
 
 # GPU aliases of the reference (DCPSE_op.hpp:3510-3530) name the same classes

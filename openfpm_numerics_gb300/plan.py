@@ -129,6 +129,20 @@ class DcpsePlan:
         C.call("dcpse_term_basis", self._h, int(term), ex, cap, ctypes.byref(n))
         return np.array(ex[: n.value * self.dim], dtype=np.uint32).reshape(n.value, self.dim)
 
+    def set_support(self, pos_support=None, self_skip=True):
+        """Columns of the neighbour lists: a second particle set (two-set
+        operator, as PPInterpolation's Dcpse) or, with None, the domain set
+        itself, where self_skip=False keeps each particle in its own list (a
+        plain VL_NON_SYMMETRIC list).  The plan keeps a reference to the
+        tensor; the neighbour list must be built again."""
+        if pos_support is not None:
+            pos_support = self._check_pos(pos_support)
+            C.call("dcpse_plan_set_support", self._h, _ptr(pos_support), pos_support.shape[0], int(bool(self_skip)))
+        else:
+            C.call("dcpse_plan_set_support", self._h, None, 0, int(bool(self_skip)))
+        self._support = pos_support
+        self.n = None
+
     def build_neighbors(self, pos, rcut, rcut_pp=None):
         pos = self._check_pos(pos)
         if rcut_pp is not None:
@@ -213,6 +227,35 @@ class DcpsePlan:
         C.call("dcpse_apply_batched_host", self._h, f_host.ctypes.data_as(ctypes.c_void_p),
                out_host.ctypes.data_as(ctypes.c_void_p), int(precision))
         return out_host
+
+    # -- particle to particle interpolation -----------------------------
+    @staticmethod
+    def _check_support_field(f):
+        if f.dtype != torch.float64 or f.dim() not in (1, 2):
+            raise ValueError("support fields are float64 [n_support] or [n_support, ncomp] CUDA tensors")
+        return f.contiguous()
+
+    def p2p_f64(self, term, f, out=None):
+        """Dcpse::p2p of one term in the reference's order: eps^-|a| sum_q
+        f_q K_pq on the domain rows; f is [n_support] or [n_support, ncomp]."""
+        f = self._check_support_field(f)
+        ncomp = 1 if f.dim() == 1 else f.shape[1]
+        n = self.info()["n"]
+        shape = (n,) if f.dim() == 1 else (n, ncomp)
+        out = torch.empty(shape, dtype=torch.float64, device=f.device) if out is None else out
+        C.call("dcpse_p2p_f64", self._h, int(term), _ptr(f), int(ncomp), _ptr(out))
+        return out
+
+    def p2p(self, f, precision=C.F32, out=None):
+        """Every output's interpolation in one pass from the summed weights:
+        [n_outputs, n] (or [n_outputs, n, ncomp] for vector fields)."""
+        f = self._check_support_field(f)
+        ncomp = 1 if f.dim() == 1 else f.shape[1]
+        n = self.info()["n"]
+        shape = (self.n_outputs, n) if f.dim() == 1 else (self.n_outputs, n, ncomp)
+        out = torch.empty(shape, dtype=torch.float64, device=f.device) if out is None else out
+        C.call("dcpse_p2p", self._h, _ptr(f), int(ncomp), _ptr(out), int(precision))
+        return out
 
     # -- adjoint --------------------------------------------------------
     def vjp_field(self, g, precision=C.F64, out=None):

@@ -72,6 +72,7 @@ def lib():
         L.orc_assemble.argtypes = [ctypes.c_int, _D, ctypes.c_int64, _D, _I64, _I32, _D, _D, _INT, _U,
                                    ctypes.c_uint, ctypes.c_double, _D, _D, _D, _D, _I32, ctypes.c_int]
         L.orc_apply.argtypes = [ctypes.c_int64, _D, _D, _I64, _I32, _D, _D, ctypes.c_uint, _D, ctypes.c_int]
+        L.orc_p2p.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _I64, _I32, _D, _D, _D, ctypes.c_int]
         L.orc_apply_sum.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _D, _I64, _I32,
                                     ctypes.POINTER(_D), ctypes.POINTER(_D), _U, _D, ctypes.c_int]
         L.orc_apply_multi.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _D, _I64, _I32, ctypes.POINTER(_D),
@@ -189,6 +190,21 @@ def apply(f, rowptr, cols, K, eip, diff_order, *, f_dom=None, nthreads=1):
     out = np.zeros(n)
     lib().orc_apply(n, _p(f, _D), _p(fd, _D), _p(rowptr, _I64), _p(cols, _I32), _p(K, _D), _p(eip, _D),
                     int(diff_order), _p(out, _D), int(nthreads))
+    return out
+
+
+def p2p(f_sup, rowptr, cols, K, eip, *, nthreads=1):
+    """Dcpse::p2p: eps^-|a|_p sum_q f_q K_pq; f_sup is [n_sup] or [n_sup, ncomp]."""
+    f = _c(f_sup, np.float64)
+    ncomp = 1 if f.ndim == 1 else f.shape[1]
+    rowptr = _c(rowptr, np.int64)
+    cols = _c(cols, np.int32)
+    K = _c(K, np.float64)
+    eip = _c(eip, np.float64)
+    n = rowptr.size - 1
+    out = np.zeros((n,) if f.ndim == 1 else (n, ncomp))
+    lib().orc_p2p(n, ncomp, _p(f, _D), _p(rowptr, _I64), _p(cols, _I32), _p(K, _D), _p(eip, _D), _p(out, _D),
+                  int(nthreads))
     return out
 
 

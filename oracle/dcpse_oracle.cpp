@@ -809,4 +809,20 @@ void orc_apply_multi(int64_t n_dom, int nterms, const double* f_sup, const doubl
     });
 }
 
+// Dcpse::p2p (Dcpse.hpp:198-227 scalar, :239-297 vector of N1 components):
+// Df_p = epsInvPow_p * sum_q f_q K_pq with f on the support set and no f_p
+// term; the components are independent sums in neighbour order.
+void orc_p2p(int64_t n_dom, int ncomp, const double* f_sup, const int64_t* rowptr, const int32_t* cols,
+             const double* kernels, const double* eps_inv_pow, double* out, int nthreads) {
+    parallel_for(n_dom, nthreads, [&](int64_t b, int64_t e) {
+        std::vector<double> D((size_t)ncomp);
+        for (int64_t p = b; p < e; ++p) {
+            for (int c = 0; c < ncomp; ++c) D[c] = 0.0;
+            for (int64_t j = rowptr[p]; j < rowptr[p + 1]; ++j)
+                for (int c = 0; c < ncomp; ++c) D[c] = D[c] + f_sup[(int64_t)cols[j] * ncomp + c] * kernels[j];
+            for (int c = 0; c < ncomp; ++c) out[p * ncomp + c] = eps_inv_pow[p] * D[c];
+        }
+    });
+}
+
 }  // extern "C"

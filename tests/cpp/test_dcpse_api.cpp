@@ -10,7 +10,10 @@
 #include <string>
 #include <vector>
 
+#include <random>
+
 #include "openfpm_dcpse/DCPSE_op.hpp"
+#include "openfpm_dcpse/DcpseInterpolation.hpp"
 
 using namespace openfpm_dcpse;
 
@@ -21,6 +24,8 @@ int64_t orc_assemble(int dim, const double* pd, int64_t n_dom, const double* ps,
                      double* eps_inv_pow, double* kernels, int32_t* status, int nthreads);
 void orc_apply(int64_t n_dom, const double* f_sup, const double* f_dom, const int64_t* rowptr, const int32_t* cols,
                const double* kernels, const double* eps_inv_pow, unsigned diff_order, double* out, int nthreads);
+void orc_p2p(int64_t n_dom, int ncomp, const double* f_sup, const int64_t* rowptr, const int32_t* cols,
+             const double* kernels, const double* eps_inv_pow, double* out, int nthreads);
 }
 
 static int failures = 0;
@@ -34,7 +39,7 @@ static int failures = 0;
         }                                                              \
     } while (0)
 
-typedef vector_dist<2, double, double, double, double, double, std::array<double, 2>> Parts2;
+typedef vector_dist<2, double, double, double, double, double, std::array<double, 2>, std::array<double, 2>> Parts2;
 
 static Parts2 lattice2(int nside, double h) {
     Parts2 d(nside * nside);
@@ -186,12 +191,102 @@ static void test_too_few() {
     EXPECT(thrown, "too few neighbours throw std::length_error");
 }
 
+// DCPSE_op_test_base_tests.cpp:245-300 (dcpse_op_tests_fa): one set that is
+// its own support with the particle in its own list (getVerlet<VL_NON_SYMMETRIC>),
+// p2p of sin x + sin y, worst < 0.03
+static void test_interpolation_same_set() {
+    const int nside = 80;
+    const double h = 2 * M_PI / (nside - 1), rCut = 4.1 * h;
+    Parts2 domain = lattice2(nside, h);
+    for (std::size_t p = 0; p < domain.size_local(); ++p)
+        domain.getProp<0>(p) = std::sin(domain.getPos(p)[0]) + std::sin(domain.getPos(p)[1]);
+    VerletList vl = getVerlet(domain, rCut, false);
+    PPInterpolation<Parts2, Parts2, VerletList> Fx(domain, domain, vl, 2, rCut);
+    Fx.p2p<0, 1>();
+    double worst = 0;
+    for (std::size_t p = 0; p < domain.size_local(); ++p)
+        worst = std::max(worst, std::fabs(domain.getProp<1>(p) - domain.getProp<0>(p)));
+    EXPECT(worst < 0.03, "PPInterpolation on one set worst < 0.03");
+    Fx.deallocate();
+}
+
+// DCPSE_op_test_base_tests.cpp:302-385 (dcpse_op_tests_mfa): interpolation
+// from a jittered copy (normal jitter of standard deviation h^2/4, boundary
+// particles kept) onto the lattice, worst < 0.03; bit-exact with the oracle;
+// vector properties component by component
+static void test_interpolation_two_sets() {
+    const int nside = 80;
+    const double h = 2 * M_PI / (nside - 1), rCut = 3.9 * h;
+    const double hi = (nside - 1) * h;
+    Parts2 domain = lattice2(nside, h);
+    Parts2 support = lattice2(nside, h);
+    std::mt19937 rng(6666666);
+    std::normal_distribution<double> gaussian(0.0, h * h / 4);
+    for (std::size_t p = 0; p < support.size_local(); ++p) {
+        const double x = support.getPos(p)[0], y = support.getPos(p)[1];
+        if (x != 0 && y != 0 && x != hi && y != hi) {
+            support.getPos(p)[0] = x + gaussian(rng);
+            support.getPos(p)[1] = y + gaussian(rng);
+        }
+        const double xs = support.getPos(p)[0], ys = support.getPos(p)[1];
+        support.getProp<0>(p) = std::sin(xs) + std::sin(ys);
+        support.getProp<4>(p)[0] = std::sin(xs);
+        support.getProp<4>(p)[1] = std::cos(ys);
+        domain.getProp<0>(p) = std::sin(domain.getPos(p)[0]) + std::sin(domain.getPos(p)[1]);
+    }
+    VerletList vl = createVerletTwoPhase(domain, support, rCut);
+    PPInterpolation<Parts2, Parts2, VerletList> Fx(support, domain, vl, 2, rCut);
+    Fx.p2p<0, 1>();
+    double worst = 0;
+    for (std::size_t p = 0; p < domain.size_local(); ++p)
+        worst = std::max(worst, std::fabs(domain.getProp<1>(p) - domain.getProp<0>(p)));
+    EXPECT(worst < 0.03, "PPInterpolation between two sets worst < 0.03");
+
+    const std::size_t n = domain.size_local();
+    std::vector<double> eps(n), eip(n), K(vl.cols.size()), f(n), out(n), fv(2 * n), ov(2 * n);
+    std::vector<int32_t> st(n);
+    unsigned sig[2] = {0, 0};
+    orc_assemble(2, domain.posData(), (int64_t)n, support.posData(), vl.rowptr.data(), vl.cols.data(), nullptr,
+                 nullptr, nullptr, sig, 2, 0.9, nullptr, eps.data(), eip.data(), K.data(), st.data(), 1);
+    for (std::size_t q = 0; q < n; ++q) {
+        f[q] = support.getProp<0>(q);
+        fv[2 * q] = support.getProp<4>(q)[0];
+        fv[2 * q + 1] = support.getProp<4>(q)[1];
+    }
+    orc_p2p((int64_t)n, 1, f.data(), vl.rowptr.data(), vl.cols.data(), K.data(), eip.data(), out.data(), 1);
+    bool same = true;
+    for (std::size_t p = 0; p < n; ++p) same &= (out[p] == domain.getProp<1>(p));
+    EXPECT(same, "PPInterpolation::p2p bit-exact with the oracle");
+
+    Fx.p2p<4, 5, 2>();
+    orc_p2p((int64_t)n, 2, fv.data(), vl.rowptr.data(), vl.cols.data(), K.data(), eip.data(), ov.data(), 1);
+    bool vsame = true;
+    for (std::size_t p = 0; p < n; ++p)
+        vsame &= (ov[2 * p] == domain.getProp<5>(p)[0]) && (ov[2 * p + 1] == domain.getProp<5>(p)[1]);
+    EXPECT(vsame, "vector p2p<4, 5, 2> bit-exact with the oracle");
+
+    // update after the support moved equals a new operator
+    for (std::size_t q = 0; q < n; ++q) support.getPos(q)[1] += 1e-3 * h * std::cos(3.0 * q);
+    vl = createVerletTwoPhase(domain, support, rCut);
+    Fx.update();
+    Fx.p2p<0, 1>();
+    PPInterpolation<Parts2, Parts2, VerletList> Fx2(support, domain, vl, 2, rCut);
+    Fx2.p2p<0, 3>();
+    bool eq = true;
+    for (std::size_t p = 0; p < n; ++p) eq &= domain.getProp<1>(p) == domain.getProp<3>(p);
+    EXPECT(eq, "PPInterpolation::update equals re-construction");
+    Fx.deallocate();
+    Fx2.deallocate();
+}
+
 int main() {
     try {
         test_dcpse_class();
         test_op_combination();
         test_laplacian();
         test_too_few();
+        test_interpolation_same_set();
+        test_interpolation_two_sets();
     } catch (const std::exception& e) {
         std::printf("FAIL exception: %s\n", e.what());
         return 2;

@@ -212,3 +212,48 @@ def test_too_few_neighbors_status(orc):
     assert np.all((st == 1) == (k < 6))
     for p in np.where(st == 1)[0]:
         assert np.all(K[rp[p]:rp[p + 1]] == 0)
+
+
+def test_p2p_same_set(orc):
+    # DCPSE_op_test_base_tests.cpp:245-300 (dcpse_op_tests_fa): one set, the
+    # particle in its own list (getVerlet<VL_NON_SYMMETRIC>), rCut 4.1h,
+    # worst |p2p(f) - f| < 0.03 for f = sin x + sin y
+    h = 2 * np.pi / 79
+    pos = _grid(80, 2, h)
+    rp, cols = orc.neighbors(pos, 4.1 * h, self_skip=False)
+    eps, eip, K, st = orc.assemble(pos, rp, cols, (0, 0), 2, nthreads=os.cpu_count())
+    f = np.sin(pos[:, 0]) + np.sin(pos[:, 1])
+    assert np.max(np.abs(orc.p2p(f, rp, cols, K, eip) - f)) < 0.03
+
+
+def test_p2p_two_sets(orc):
+    # DCPSE_op_test_base_tests.cpp:302-385 (dcpse_op_tests_mfa): from a copy
+    # jittered by N(0, (h^2/4)^2) (boundary particles kept) onto the lattice,
+    # rCut 3.9h, createVerletTwoPhase lists, worst < 0.03
+    h = 2 * np.pi / 79
+    pos = _grid(80, 2, h)
+    hi = pos.max(axis=0)
+    inner = (pos[:, 0] != 0) & (pos[:, 1] != 0) & (pos[:, 0] != hi[0]) & (pos[:, 1] != hi[1])
+    sup = pos.copy()
+    sup[inner] += np.random.default_rng(6666666).normal(0.0, h * h / 4, (inner.sum(), 2))
+    rp, cols = orc.neighbors(pos, 3.9 * h, support=sup, self_skip=False)
+    eps, eip, K, st = orc.assemble(pos, rp, cols, (0, 0), 2, support=sup, nthreads=os.cpu_count())
+    f = np.sin(sup[:, 0]) + np.sin(sup[:, 1])
+    g = orc.p2p(f, rp, cols, K, eip)
+    assert np.max(np.abs(g - (np.sin(pos[:, 0]) + np.sin(pos[:, 1])))) < 0.03
+    # vector property: components are independent interpolations
+    fv = np.stack([f, np.cos(sup[:, 1])], 1)
+    gv = orc.p2p(fv, rp, cols, K, eip)
+    assert np.array_equal(gv[:, 0], g)
+    assert np.max(np.abs(gv[:, 1] - np.cos(pos[:, 1]))) < 0.03
+
+
+def test_p2p_reproduces_linear_fields(orc):
+    # moment conditions of the zero signature (Dcpse.hpp:755-766): at order 2
+    # the kernels reproduce polynomials of degree 1 exactly
+    pos, h = W.lattice(20, 2)
+    sup = pos + np.random.default_rng(3).uniform(-0.3 * h, 0.3 * h, pos.shape)
+    rp, cols = orc.neighbors(pos, 3.1 * h, support=sup, self_skip=False)
+    eps, eip, K, st = orc.assemble(pos, rp, cols, (0, 0), 2, support=sup)
+    g = orc.p2p(1.5 - sup[:, 0] + 4 * sup[:, 1], rp, cols, K, eip)
+    assert np.max(np.abs(g - (1.5 - pos[:, 0] + 4 * pos[:, 1]))[st == 0]) < 1e-12
