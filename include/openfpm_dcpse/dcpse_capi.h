@@ -182,6 +182,20 @@ int dcpse_apply_batched_host(dcpse_plan_t* plan, const double* h_f, double* h_ou
 int dcpse_p2p_f64(dcpse_plan_t* plan, int term, const double* d_f_support, int ncomp, double* d_out);
 int dcpse_p2p(dcpse_plan_t* plan, const double* d_f_support, int ncomp, double* d_out, int precision);
 
+/* ---- operator matrices --------------------------------------------------
+ * CSR rows of output `output` times coeff, as DCPSE_scheme::impose builds
+ * them from value_nz (DCPSE_op.hpp:70-83, :405-420; DCPSE_Solver.hpp:980-
+ * 1030): for row r (particle p = d_rows[r], or r when d_rows is NULL and
+ * n_rows is ignored), column q*nvar + var holds sum_terms (K_pq * coeff) *
+ * epsInvPow_p and column p*nvar + var the diagonal sum_terms sum_q
+ * ((sign * K_pq) * coeff) * epsInvPow_p with Dcpse::getSign(), accumulated in
+ * the reference's order; columns ascending, a zero diagonal for a row
+ * without neighbours.  Two calls: with d_cols_out = d_vals_out = NULL it
+ * writes d_rowptr_out[n_rows+1] (device) and *nnz_out (host); then with
+ * arrays of *nnz_out entries it fills them.  Needs DCPSE_STORE_TERMS_F64. */
+int dcpse_operator_csr(dcpse_plan_t* plan, int output, double coeff, const int64_t* d_rows, int64_t n_rows, int nvar,
+                       int var, int64_t* d_rowptr_out, int64_t* d_cols_out, double* d_vals_out, int64_t* nnz_out);
+
 /* ---- adjoint ------------------------------------------------------------
  * No counterpart in the reference (its operators have no derivatives); these
  * differentiate the batched apply y_o = L_o f with the neighbour list held

@@ -49,6 +49,7 @@ SIGNATURES = {
     "dcpse_apply_batched_f32_noalloc": (_I, [_I64, _I, _P, _P, _P, _I64, _P, _P, _P]),
     "dcpse_p2p_f64": (_I, [_P, _I, _P, _I, _P]),
     "dcpse_p2p": (_I, [_P, _P, _I, _P, _I]),
+    "dcpse_operator_csr": (_I, [_P, _I, _D, _P, _I64, _I, _I, _P, _P, _P, _PI64]),
     "dcpse_set_term_kernels": (_I, [_P, _I, _P, _P, _P]),
     "dcpse_vjp_field": (_I, [_P, _P, _P, _I]),
     "dcpse_vjp_positions": (_I, [_P, _P, _P, _P, _P, _P]),

@@ -102,6 +102,11 @@ __global__ void csr_check_kernel(const int64_t* rowptr, const int32_t* cols, int
     if (t0 == 0 && (rowptr[0] != 0 || rowptr[n] != nnz)) atomicAdd(bad, 1ull);
 }
 
+__global__ void index_check_kernel(const int64_t* idx, int64_t m, int64_t n, unsigned long long* bad) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        if (idx[i] < 0 || idx[i] >= n) atomicAdd(bad, 1ull);
+}
+
 __global__ void row_max_kernel(const int64_t* rowptr, int64_t n, int* maxk) {
     int m = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -1346,6 +1351,72 @@ int dcpse_p2p(dcpse_plan_t* P, const double* d_f_support, int ncomp, double* d_o
             return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
         }
     }
+    return DCPSE_OK;
+}
+
+int dcpse_operator_csr(dcpse_plan_t* P, int output, double coeff, const int64_t* d_rows, int64_t n_rows, int nvar,
+                       int var, int64_t* d_rowptr_out, int64_t* d_cols_out, double* d_vals_out, int64_t* nnz_out) {
+    if (int rc = check_plan(P)) return rc;
+    if (int rc = check_single_set(P)) return rc;
+    if (!P->assembled || !P->k_term) return fail(DCPSE_ERR_STATE, "per-term FP64 kernels not stored");
+    if (output < 0 || output >= P->nout) return fail(DCPSE_ERR_ARG, "output out of range");
+    if (nvar < 1 || var < 0 || var >= nvar) return fail(DCPSE_ERR_ARG, "need 0 <= var < nvar");
+    if (!nnz_out || !d_rowptr_out) return fail(DCPSE_ERR_ARG, "NULL row offsets or count");
+    if (!d_rows) n_rows = P->n;
+    if (n_rows < 0) return fail(DCPSE_ERR_ARG, "bad row count");
+    if ((d_cols_out == nullptr) != (d_vals_out == nullptr)) return fail(DCPSE_ERR_ARG, "pass both or neither of cols/vals");
+    cudaStream_t s = P->stream;
+    if (d_rows && n_rows > 0) {
+        unsigned long long* bad = nullptr;
+        DCPSE_CK(dalloc(&bad, 1));
+        cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(unsigned long long), s);
+        if (e == cudaSuccess) {
+            index_check_kernel<<<std::max(1, (int)std::min<int64_t>(num_sms() * 8, (n_rows + 255) / 256)), 256, 0, s>>>(
+                d_rows, n_rows, P->n, bad);
+            e = cudaGetLastError();
+        }
+        unsigned long long hb = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&hb, bad, sizeof hb, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        dfree(bad);
+        DCPSE_CK(e);
+        if (hb) return fail(DCPSE_ERR_ARG, "row particle index out of range");
+    }
+    int32_t* counts = nullptr;
+    int64_t* tmp = nullptr;
+    cudaError_t e = dalloc(&counts, (size_t)std::max<int64_t>(n_rows, 1));
+    if (e == cudaSuccess) e = dalloc(&tmp, (size_t)scan_tmp_elems(std::max<int64_t>(n_rows, 1)));
+    if (e == cudaSuccess) e = csr_row_counts(P->rowptr, P->cols, d_rows, n_rows, counts, s);
+    if (e == cudaSuccess) e = exclusive_scan_i32(counts, n_rows, d_rowptr_out, tmp, s);
+    int64_t nnz = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&nnz, d_rowptr_out + n_rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    dfree(counts);
+    dfree(tmp);
+    DCPSE_CK(e);
+    *nnz_out = nnz;
+    if (!d_cols_out) return DCPSE_OK;
+    MatArgs a{};
+    a.rowptr = P->rowptr;
+    a.cols = P->cols;
+    a.rows = d_rows;
+    a.nrows = n_rows;
+    a.coeff = coeff;
+    a.nvar = nvar;
+    a.var = var;
+    a.out_rowptr = d_rowptr_out;
+    a.out_cols = d_cols_out;
+    a.out_vals = d_vals_out;
+    for (int t = 0; t < P->nterms; ++t) {
+        if (P->term_output[t] != output) continue;
+        unsigned ord = 0;
+        for (int d = 0; d < P->dim; ++d) ord += P->sigs[t][d];
+        a.K[a.nterms] = P->k_term + (size_t)t * P->nnz;
+        a.eip[a.nterms] = P->eip_group + (size_t)P->term_group[t] * P->n;
+        a.sign[a.nterms] = (ord % 2 == 0 && ord != 0) ? -1.0 : 1.0;
+        a.nterms++;
+    }
+    DCPSE_CK(csr_fill(a, s));
     return DCPSE_OK;
 }
 

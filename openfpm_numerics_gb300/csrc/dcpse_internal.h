@@ -183,6 +183,27 @@ cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const 
                               int64_t nnz, const double* f, double* out, cudaStream_t s, int no_self = 0,
                               int64_t oos = 0, int64_t ors = 0, int64_t fs = 0);
 
+// ---------------------------------------------------------- CSR export --
+struct MatArgs {
+    const int64_t* rowptr;       // neighbour list
+    const int32_t* cols;
+    const int64_t* rows;         // particles of the exported rows, or null (all)
+    int64_t nrows;
+    int nterms;                  // terms of the exported output
+    const double* K[kMaxTerms];  // their per-term kernels [nnz]
+    const double* eip[kMaxTerms];
+    double sign[kMaxTerms];      // Dcpse::getSign of each term
+    double coeff;
+    int64_t nvar, var;           // column index = particle * nvar + var
+    const int64_t* out_rowptr;   // [nrows + 1]
+    int64_t* out_cols;
+    double* out_vals;
+};
+// entries per exported row (neighbours plus the diagonal unless present)
+cudaError_t csr_row_counts(const int64_t* rowptr, const int32_t* cols, const int64_t* rows, int64_t nrows,
+                           int32_t* counts, cudaStream_t s);
+cudaError_t csr_fill(const MatArgs& a, cudaStream_t s);
+
 // --------------------------------------------------------------- adjoint --
 // transposed list: trow[n+1], per entry the source row tsrc and entry index tidx
 cudaError_t build_transpose(const int64_t* rowptr, const int32_t* cols, int64_t n, int64_t nnz, int32_t* cnt,

@@ -257,6 +257,26 @@ class DcpsePlan:
         C.call("dcpse_p2p", self._h, _ptr(f), int(ncomp), _ptr(out), int(precision))
         return out
 
+    # -- operator matrices ----------------------------------------------
+    def operator_csr(self, output=0, coeff=1.0, rows=None, nvar=1, var=0):
+        """CSR rows (value_nz order) of one output times coeff for the
+        particles ``rows`` (int64 CUDA tensor; None = all) -> (rowptr int64
+        [nrows+1], cols int64, vals float64) on the device; column index =
+        particle * nvar + var."""
+        if rows is not None:
+            rows = rows.contiguous().to(device="cuda", dtype=torch.int64)
+            nrows = rows.numel()
+        else:
+            nrows = self.info()["n"]
+        rp = torch.empty(nrows + 1, dtype=torch.int64, device="cuda")
+        nnz = ctypes.c_int64()
+        args = (self._h, int(output), float(coeff), _ptr(rows), int(nrows), int(nvar), int(var), _ptr(rp))
+        C.call("dcpse_operator_csr", *args, None, None, ctypes.byref(nnz))
+        cols = torch.empty(max(nnz.value, 1), dtype=torch.int64, device="cuda")
+        vals = torch.empty(max(nnz.value, 1), dtype=torch.float64, device="cuda")
+        C.call("dcpse_operator_csr", *args, _ptr(cols), _ptr(vals), ctypes.byref(nnz))
+        return rp, cols[: nnz.value], vals[: nnz.value]
+
     # -- adjoint --------------------------------------------------------
     def vjp_field(self, g, precision=C.F64, out=None):
         """sum_o L_o^T g_o for a cotangent g [n_outputs, n] -> [n]."""

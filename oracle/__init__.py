@@ -73,6 +73,9 @@ def lib():
                                    ctypes.c_uint, ctypes.c_double, _D, _D, _D, _D, _I32, ctypes.c_int]
         L.orc_apply.argtypes = [ctypes.c_int64, _D, _D, _I64, _I32, _D, _D, ctypes.c_uint, _D, ctypes.c_int]
         L.orc_p2p.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _I64, _I32, _D, _D, _D, ctypes.c_int]
+        L.orc_operator_csr.argtypes = [ctypes.c_int64, _I64, _I64, _I32, ctypes.c_int, ctypes.POINTER(_D),
+                                       ctypes.POINTER(_D), _D, ctypes.c_double, ctypes.c_int64, ctypes.c_int64, _I64,
+                                       _I64, _D]
         L.orc_apply_sum.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _D, _I64, _I32,
                                     ctypes.POINTER(_D), ctypes.POINTER(_D), _U, _D, ctypes.c_int]
         L.orc_apply_multi.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _D, _I64, _I32, ctypes.POINTER(_D),
@@ -206,6 +209,28 @@ def p2p(f_sup, rowptr, cols, K, eip, *, nthreads=1):
     lib().orc_p2p(n, ncomp, _p(f, _D), _p(rowptr, _I64), _p(cols, _I32), _p(K, _D), _p(eip, _D), _p(out, _D),
                   int(nthreads))
     return out
+
+
+def operator_csr(rowptr, cols, Ks, eips, diff_orders, *, coeff=1.0, rows=None, nvar=1, var=0):
+    """value_nz rows of a sum of Dcpse terms (K, eip, |alpha| per term) as
+    DCPSE_scheme::impose collects them -> (rowptr, cols, vals)."""
+    rowptr = _c(rowptr, np.int64)
+    cols = _c(cols, np.int32)
+    Ks = [_c(k, np.float64) for k in Ks]
+    eips = [_c(e, np.float64) for e in eips]
+    sign = _c([-1.0 if (o % 2 == 0 and o != 0) else 1.0 for o in diff_orders], np.float64)
+    kp = (_D * len(Ks))(*[_p(k, _D) for k in Ks])
+    ep = (_D * len(eips))(*[_p(e, _D) for e in eips])
+    rows_a = None if rows is None else _c(rows, np.int64)
+    nrows = rowptr.size - 1 if rows is None else rows_a.size
+    out_rp = np.zeros(nrows + 1, np.int64)
+    args = (nrows, None if rows_a is None else _p(rows_a, _I64), _p(rowptr, _I64), _p(cols, _I32), len(Ks), kp, ep,
+            _p(sign, _D), float(coeff), int(nvar), int(var), _p(out_rp, _I64))
+    lib().orc_operator_csr(*args, None, None)
+    out_cols = np.zeros(max(int(out_rp[-1]), 1), np.int64)
+    out_vals = np.zeros(max(int(out_rp[-1]), 1))
+    lib().orc_operator_csr(*args, _p(out_cols, _I64), _p(out_vals, _D))
+    return out_rp, out_cols[: out_rp[-1]], out_vals[: out_rp[-1]]
 
 
 def apply_sum(f, rowptr, cols, Ks, eips, diff_orders, *, nthreads=1):

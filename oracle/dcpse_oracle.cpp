@@ -48,6 +48,7 @@
 // signs) and its analytic error bars (tests/test_oracle_*.py).
 
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -823,6 +824,39 @@ void orc_p2p(int64_t n_dom, int ncomp, const double* f_sup, const int64_t* rowpt
             for (int c = 0; c < ncomp; ++c) out[p * ncomp + c] = eps_inv_pow[p] * D[c];
         }
     });
+}
+
+// Operator matrix rows as DCPSE_scheme::impose_git (DCPSE_Solver.hpp:980-1030)
+// collects them from value_nz (DCPSE_op.hpp:70-83 one Dcpse, :405-420 a sum
+// of Dcpse objects): per row a map column -> coefficient, filled by
+//   for term t, neighbour j:  cols[q_j] += (K_tj * coeff) * eip_t(p);
+//                             cols[p]   += ((sign_t * K_tj) * coeff) * eip_t(p)
+// then a zero diagonal if none was set; written out in ascending columns.
+// Two calls: out_cols == NULL fills out_rowptr only.
+void orc_operator_csr(int64_t nrows, const int64_t* rows, const int64_t* rowptr, const int32_t* cols, int nterms,
+                      const double* const* K, const double* const* eip, const double* sign, double coeff,
+                      int64_t nvar, int64_t var, int64_t* out_rowptr, int64_t* out_cols, double* out_vals) {
+    out_rowptr[0] = 0;
+    for (int64_t r = 0; r < nrows; ++r) {
+        const int64_t p = rows ? rows[r] : r;
+        std::map<int64_t, double> m;
+        for (int t = 0; t < nterms; ++t)
+            for (int64_t j = rowptr[p]; j < rowptr[p + 1]; ++j) {
+                const double kc = K[t][j] * coeff;
+                m[(int64_t)cols[j] * nvar + var] += kc * eip[t][p];
+                const double skc = (sign[t] * K[t][j]) * coeff;
+                m[p * nvar + var] += skc * eip[t][p];
+            }
+        if (m.find(p * nvar + var) == m.end()) m[p * nvar + var] = 0.0;
+        int64_t o = out_rowptr[r];
+        if (out_cols)
+            for (const auto& kv : m) {
+                out_cols[o] = kv.first;
+                out_vals[o] = kv.second;
+                ++o;
+            }
+        out_rowptr[r + 1] = out_rowptr[r] + (int64_t)m.size();
+    }
 }
 
 }  // extern "C"

@@ -257,3 +257,39 @@ def test_p2p_reproduces_linear_fields(orc):
     eps, eip, K, st = orc.assemble(pos, rp, cols, (0, 0), 2, support=sup)
     g = orc.p2p(1.5 - sup[:, 0] + 4 * sup[:, 1], rp, cols, K, eip)
     assert np.max(np.abs(g - (1.5 - pos[:, 0] + 4 * pos[:, 1]))[st == 0]) < 1e-12
+
+
+def test_operator_csr_matches_apply(orc):
+    # value_nz rows (DCPSE_op.hpp:70-83, :405-420) times f equal the apply
+    # (Dcpse.hpp:467-499) up to rounding, for even (Laplacian) and odd (Dx)
+    # orders and a list holding the particle itself
+    import scipy.sparse as sp
+
+    pos, h = W.lattice(16, 2, jitter=0.1, seed=5)
+    f = np.sin(2 * pos[:, 0]) * np.cos(pos[:, 1])
+    for self_skip, sigs in ((True, [(2, 0), (0, 2)]), (False, [(1, 0)])):
+        rp, cols = orc.neighbors(pos, 3.1 * h, self_skip=self_skip)
+        terms = [orc.assemble(pos, rp, cols, s, 2) for s in sigs]
+        R, Cc, V = orc.operator_csr(rp, cols, [t[2] for t in terms], [t[1] for t in terms], [sum(s) for s in sigs])
+        A = sp.csr_matrix((V, Cc, R), shape=(len(pos), len(pos)))
+        ref = orc.apply_sum(f, rp, cols, [t[2] for t in terms], [t[1] for t in terms], [sum(s) for s in sigs])
+        assert np.abs(A @ f - ref).max() <= 1e-12 * np.abs(ref).max()
+        assert np.all(np.diff(R) == np.diff(rp) + (1 if self_skip else 0))
+
+
+def test_bicgstab_cpu():
+    # the solver of the implicit scheme on a small nonsymmetric system
+    import scipy.sparse as sp
+    import torch
+
+    from openfpm_numerics_gb300.scheme import bicgstab
+
+    n = 200
+    rng = np.random.default_rng(7)
+    M = sp.random(n, n, density=0.03, random_state=7) + sp.eye(n) * 4.0
+    M = M.tocsr()
+    A = torch.sparse_csr_tensor(torch.tensor(M.indptr), torch.tensor(M.indices), torch.tensor(M.data), (n, n))
+    xe = rng.standard_normal(n)
+    b = torch.tensor(M @ xe)
+    x, it, res = bicgstab(A, b, tol=1e-12)
+    assert res <= 1e-12 and np.abs(x.numpy() - xe).max() < 1e-9
