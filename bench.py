@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--nside", type=int, default=128)
     ap.add_argument("--cpu-sample", type=int, default=32768, help="particles in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["apply", "assemble", "gray-scott", "graded"], default=None,
+    ap.add_argument("--only", choices=["apply", "assemble", "gray-scott", "graded", "interp"], default=None,
                     help="small-footprint run of one kernel family (for profiler captures)")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--mode", type=int, default=0, help="apply loading: 0 auto, 1 direct, 2 TMA-staged")
@@ -475,6 +475,93 @@ def run_gray_scott(args):
     print(json.dumps(res), flush=True)
 
 
+def run_interp(args):
+    """Particle to particle interpolation (PPInterpolation::p2p): from a
+    jittered copy of the 128^3 lattice (jitter U(+-0.3h), seed 7) onto the
+    lattice (h = 1/127, jitter U(+-0.15h), seed 2), order 2, rCut = 2.8h,
+    two-set lists (createVerletTwoPhase).  Times the assembly, the
+    reference-order FP64 p2p (per-term kernels), and the batched p2p from
+    the summed weights in FP64 and FP32 (field as an exact float pair)."""
+    import torch
+
+    from openfpm_numerics_gb300 import _capi as C
+    from openfpm_numerics_gb300 import workloads as W
+    from openfpm_numerics_gb300.plan import DcpsePlan
+
+    torch.cuda.set_device(0)
+    cfg = W.config2(args.nside)
+    dom_np = cfg["pos"]
+    h = cfg["h"]
+    sup_np = dom_np + np.random.default_rng(7).uniform(-0.3 * h, 0.3 * h, dom_np.shape)
+    N = dom_np.shape[0]
+    dom = torch.tensor(dom_np, device="cuda")
+    sup = torch.tensor(sup_np, device="cuda")
+    f = torch.tensor(W.field2(sup_np)[0], device="cuda")
+    stream = torch.cuda.current_stream()
+    plan = DcpsePlan(3, [[(0, 0, 0)]], order=2, stream=stream)
+    plan.set_timing(True)
+    plan.set_support(sup)
+    plan.build_neighbors(dom, cfg["rcut"])
+    nnz = plan.info()["nnz"]
+    plan.reset_timing()
+    plan.assemble(dom, C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+    t_asm = plan.timing(C.K_ASSEMBLE)[0]
+    nbad = plan.particle_status()[0]
+    out = torch.empty(N, dtype=torch.float64, device="cuda")
+    outb = torch.empty((1, N), dtype=torch.float64, device="cuda")
+    res = {"only": "interp", "particles": N, "support_particles": N, "nnz": nnz, "mean_neighbors": nnz / N,
+           "assembly_ms": t_asm, "failed_particles": nbad}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, min(args.steps, 50))
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        plan.reset_timing()
+        ev0.record(stream)
+        for _ in range(reps):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    res["p2p_f64_reference_ms"] = timed(lambda: plan.p2p_f64(0, f, out))
+    ref = out.clone()
+    res["p2p_f64_batched_ms"] = timed(lambda: plan.p2p(f, C.F64, outb))
+    b64 = outb[0].clone()
+    sweep = []
+    for lanes in (4, 8, 16):
+        for mode in (1, 3):
+            plan.set_apply_config(lanes, mode)
+            sweep.append({"lanes": lanes, "mode": mode, "ms": timed(lambda: plan.p2p(f, C.F32, outb))})
+    best = min(sweep, key=lambda r: r["ms"])
+    res["p2p_f32_sweep"] = sweep
+    plan.set_apply_config(0, 0)
+    res["p2p_f32_auto_ms"] = timed(lambda: plan.p2p(f, C.F32, outb))
+    plan.set_apply_config(best["lanes"], best["mode"])
+    res["p2p_f32_ms"] = timed(lambda: plan.p2p(f, C.F32, outb))
+    res["p2p_f32_schedule"] = {"lanes": best["lanes"], "mode": best["mode"]}
+    k_ms, k_n = plan.timing(C.K_APPLY_BATCHED)
+    b32 = outb[0].clone()
+    fmax = f.abs().max().item()
+    res["err_f64_batched_vs_reference"] = (b64 - ref).abs().max().item() / fmax
+    res["err_f32_vs_reference"] = (b32 - ref).abs().max().item() / fmax
+    exact = torch.tensor(W.field2(dom_np)[0], device="cuda")
+    inner = torch.tensor(W.interior_mask(dom_np, cfg["rcut"]), device="cuda")
+    res["err_reference_vs_analytic_interior"] = ((ref - exact)[inner]).abs().max().item() / fmax
+    hbm, peak_kind = peaks()
+    # row offsets, columns, FP32 weights, the split field gathered once, FP64 output
+    bytes_f32 = 8 * (N + 1) + nnz * (4 + 4) + 8 * N + 8 * N
+    kern_ms = k_ms / max(k_n, 1)
+    res["p2p_f32_kernel_ms"] = kern_ms
+    res["roofline_f32"] = {"bound": "hbm", "algorithmic_bytes": bytes_f32, "achieved_gbs": bytes_f32 / kern_ms / 1e6,
+                           "peak_gbs": hbm, "frac": bytes_f32 / kern_ms / 1e6 / hbm, "peak_source": peak_kind}
+    res["value_gparticles_s_f32"] = N / res["p2p_f32_ms"] / 1e6
+    plan.check()
+    plan.close()
+    print(json.dumps(res), flush=True)
+
+
 def run_graded(args):
     """Uneven 2D cloud: 1,000,000 particles, density growing 4x along x
     (inverse-CDF sampling, seed 3), per-particle cutoff 3.1 h_p, five
@@ -553,6 +640,9 @@ def run_only(args):
         return
     if args.only == "graded":
         run_graded(args)
+        return
+    if args.only == "interp":
+        run_interp(args)
         return
     torch.cuda.set_device(0)
     cfg = W.config2(args.nside)

@@ -15,6 +15,7 @@
 // side (the reference's general expression engine is not part of this path).
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <functional>
 #include <memory>
@@ -208,51 +209,44 @@ private:
         detail::throw_too_few(plan_->last_fail_code(), nbad);
     }
 
+    // one Dcpse file per term in Dcpse::save's layout: file + "_0" for an
+    // operator of one term (what the reference's Derivative_* save writes),
+    // file + "_term<t>_0" for each term of a sum or vector operator
+    std::string term_file(const std::string& file, int t) const {
+        return plan_->n_terms() == 1 ? file + "_0" : file + "_term" + std::to_string(t) + "_0";
+    }
     void save_impl(const std::string& file) {
-        std::ofstream dump(file + "_0", std::ios::out | std::ios::binary);
-        if (!dump.is_open()) {
-            std::cerr << __FILE__ << ":" << __LINE__ << " Unable to write " << file << "_0" << std::endl;
-            return;
-        }
-        const char magic[8] = {'D', 'C', 'P', 'S', 'E', 'O', 'P', '1'};
-        uint64_t hdr[3] = {(uint64_t)plan_->n(), (uint64_t)plan_->nnz(), (uint64_t)plan_->n_terms()};
-        dump.write(magic, 8);
-        dump.write((const char*)hdr, sizeof hdr);
-        const auto& eps = plan_->eps();
-        dump.write((const char*)eps.data(), eps.size() * sizeof(double));
         for (int t = 0; t < plan_->n_terms(); ++t) {
-            dump.write((const char*)plan_->eps_inv_pow(t).data(), plan_->n() * sizeof(double));
-            dump.write((const char*)plan_->kernels(t).data(), plan_->nnz() * sizeof(double));
+            detail::KernelSet k;
+            k.eps = plan_->eps();
+            k.eip = plan_->eps_inv_pow(t);
+            k.K = plan_->kernels(t);
+            k.offsets.assign(plan_->rowptr().begin(), plan_->rowptr().end() - (plan_->n() > 0 ? 1 : 0));
+            if (!detail::write_kernel_file(term_file(file, t), k)) {
+                std::cerr << __FILE__ << ":" << __LINE__ << " Unable to write " << term_file(file, t) << std::endl;
+                return;
+            }
         }
     }
     void load_impl(const std::string& file) {
-        std::ifstream in(file + "_0", std::ios::in | std::ios::binary);
-        if (!in.is_open()) {
-            std::cerr << __FILE__ << ":" << __LINE__ << " error, opening file: " << file << std::endl;
-            return;
+        std::vector<detail::KernelSet> ks((std::size_t)plan_->n_terms());
+        for (int t = 0; t < plan_->n_terms(); ++t) {
+            detail::KernelSet& k = ks[(std::size_t)t];
+            if (!detail::read_kernel_file(term_file(file, t), k)) {
+                std::cerr << __FILE__ << ":" << __LINE__ << " error, opening file: " << term_file(file, t) << std::endl;
+                return;
+            }
+            if ((int64_t)k.eps.size() != plan_->n() || k.eip.size() != k.eps.size() ||
+                (int64_t)k.K.size() != plan_->nnz() || k.offsets.size() != k.eps.size() ||
+                !std::equal(k.offsets.begin(), k.offsets.end(), plan_->rowptr().begin(),
+                            [](uint64_t a, int64_t b) { return (int64_t)a == b; })) {
+                std::cerr << __FILE__ << ":" << __LINE__ << " error, " << term_file(file, t)
+                          << " does not match this operator" << std::endl;
+                return;
+            }
         }
-        char magic[8];
-        uint64_t hdr[3];
-        in.read(magic, 8);
-        in.read((char*)hdr, sizeof hdr);
-        if (!in || std::memcmp(magic, "DCPSEOP1", 8) != 0 || (int64_t)hdr[0] != plan_->n() ||
-            (int64_t)hdr[1] != plan_->nnz() || (int)hdr[2] != plan_->n_terms()) {
-            std::cerr << __FILE__ << ":" << __LINE__ << " error, " << file << " does not match this operator"
-                      << std::endl;
-            return;
-        }
-        std::vector<double> eps(hdr[0]);
-        in.read((char*)eps.data(), eps.size() * sizeof(double));
-        std::vector<std::vector<double>> eip(hdr[2], std::vector<double>(hdr[0])), K(hdr[2], std::vector<double>(hdr[1]));
-        for (uint64_t t = 0; t < hdr[2]; ++t) {
-            in.read((char*)eip[t].data(), hdr[0] * sizeof(double));
-            in.read((char*)K[t].data(), hdr[1] * sizeof(double));
-        }
-        if (!in) {
-            std::cerr << __FILE__ << ":" << __LINE__ << " error, truncated file " << file << std::endl;
-            return;
-        }
-        for (uint64_t t = 0; t < hdr[2]; ++t) plan_->install((int)t, K[t], eps, eip[t]);
+        for (int t = 0; t < plan_->n_terms(); ++t)
+            plan_->install(t, ks[(std::size_t)t].K, ks[(std::size_t)t].eps, ks[(std::size_t)t].eip);
     }
 
     VerletList_type& vl_;

@@ -15,6 +15,7 @@
 //   verletList.getNNPart(p), verletList.get(p, j)
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -253,6 +254,53 @@ private:
     int last_fail_code_ = 0;
 };
 
+// Byte layout of Dcpse::save (Dcpse.hpp:302-331): openfpm's Packer writes
+// each openfpm::vector of a primitive type as its element count (size_t)
+// followed by the elements in native byte order, here localEps,
+// localEpsInvPow, calcKernels (doubles) and kerOffsets (size_t), into
+// file + "_" + rank.
+template <typename T>
+void pack_vector(std::ostream& out, const std::vector<T>& v) {
+    const uint64_t n = (uint64_t)v.size();
+    out.write((const char*)&n, sizeof n);
+    out.write((const char*)v.data(), (std::streamsize)(v.size() * sizeof(T)));
+}
+
+template <typename T>
+bool unpack_vector(std::istream& in, std::vector<T>& v, uint64_t max_elems) {
+    uint64_t n = 0;
+    in.read((char*)&n, sizeof n);
+    if (!in || n > max_elems) return false;
+    v.resize((std::size_t)n);
+    in.read((char*)v.data(), (std::streamsize)(n * sizeof(T)));
+    return (bool)in;
+}
+
+struct KernelSet {
+    std::vector<double> eps, eip, K;
+    std::vector<uint64_t> offsets;
+};
+
+inline bool write_kernel_file(const std::string& path, const KernelSet& k) {
+    std::ofstream dump(path, std::ios::out | std::ios::binary);
+    if (!dump.is_open()) return false;
+    pack_vector(dump, k.eps);
+    pack_vector(dump, k.eip);
+    pack_vector(dump, k.K);
+    pack_vector(dump, k.offsets);
+    return (bool)dump;
+}
+
+inline bool read_kernel_file(const std::string& path, KernelSet& k) {
+    std::ifstream in(path, std::ios::in | std::ios::binary | std::ios::ate);
+    if (!in.is_open()) return false;
+    const uint64_t bytes = (uint64_t)in.tellg();
+    in.seekg(0);
+    const uint64_t cap = bytes / sizeof(double);
+    return unpack_vector(in, k.eps, cap) && unpack_vector(in, k.eip, cap) && unpack_vector(in, k.K, cap) &&
+           unpack_vector(in, k.offsets, cap);
+}
+
 template <typename Sig>
 std::vector<unsigned> sig_vector(const Sig& s, int dim) {
     std::vector<unsigned> v(dim);
@@ -467,55 +515,35 @@ public:
         assemble();
     }
 
-    // Own versioned binary format, same content and order as the reference's
-    // Packer stream (localEps, localEpsInvPow, calcKernels, kerOffsets;
-    // Dcpse.hpp:302-331), written to file + "_" + rank (rank 0 here).
+    // Dcpse::save (Dcpse.hpp:302-331): localEps, localEpsInvPow, calcKernels
+    // and kerOffsets in openfpm's Packer layout, to file + "_" + rank (rank 0)
     void save(const std::string& file) {
-        std::ofstream dump(file + "_0", std::ios::out | std::ios::binary);
-        if (!dump.is_open()) {
+        detail::KernelSet k;
+        k.eps = plan_->eps();
+        k.eip = plan_->eps_inv_pow(0);
+        k.K = plan_->kernels(0);
+        k.offsets.assign(plan_->rowptr().begin(), plan_->rowptr().end() - (plan_->n() > 0 ? 1 : 0));
+        if (!detail::write_kernel_file(file + "_0", k))
             std::cerr << __FILE__ << ":" << __LINE__ << " Unable to write " << file << "_0" << std::endl;
-            return;
-        }
-        const auto& eps = plan_->eps();
-        const auto& eip = plan_->eps_inv_pow(0);
-        const auto& K = plan_->kernels(0);
-        const char magic[8] = {'D', 'C', 'P', 'S', 'E', 'G', 'B', '1'};
-        uint64_t hdr[3] = {(uint64_t)plan_->n(), (uint64_t)K.size(), (uint64_t)dim};
-        dump.write(magic, 8);
-        dump.write((const char*)hdr, sizeof hdr);
-        dump.write((const char*)eps.data(), eps.size() * sizeof(double));
-        dump.write((const char*)eip.data(), eip.size() * sizeof(double));
-        dump.write((const char*)K.data(), K.size() * sizeof(double));
-        std::vector<uint64_t> off(plan_->rowptr().begin(), plan_->rowptr().end() - (plan_->n() > 0 ? 1 : 0));
-        dump.write((const char*)off.data(), off.size() * sizeof(uint64_t));
     }
 
-    // Dcpse.hpp:337-379; the neighbour list of the constructor must match.
+    // Dcpse::load (Dcpse.hpp:337-379): the neighbour list of the constructor
+    // must be the one the file was saved with (checked through kerOffsets)
     void load(const std::string& file) {
-        std::ifstream in(file + "_0", std::ios::in | std::ios::binary);
-        if (!in.is_open()) {
+        detail::KernelSet k;
+        if (!detail::read_kernel_file(file + "_0", k)) {
             std::cerr << __FILE__ << ":" << __LINE__ << " error, opening file: " << file << std::endl;
             return;
         }
-        char magic[8];
-        uint64_t hdr[3];
-        in.read(magic, 8);
-        in.read((char*)hdr, sizeof hdr);
-        if (!in || std::memcmp(magic, "DCPSEGB1", 8) != 0 || (int64_t)hdr[0] != plan_->n() ||
-            (int64_t)hdr[1] != plan_->nnz() || hdr[2] != dim) {
+        if ((int64_t)k.eps.size() != plan_->n() || k.eip.size() != k.eps.size() ||
+            (int64_t)k.K.size() != plan_->nnz() || k.offsets.size() != k.eps.size() ||
+            !std::equal(k.offsets.begin(), k.offsets.end(), plan_->rowptr().begin(),
+                        [](uint64_t a, int64_t b) { return (int64_t)a == b; })) {
             std::cerr << __FILE__ << ":" << __LINE__ << " error, " << file << " does not match this operator"
                       << std::endl;
             return;
         }
-        std::vector<double> eps(hdr[0]), eip(hdr[0]), K(hdr[1]);
-        in.read((char*)eps.data(), eps.size() * sizeof(double));
-        in.read((char*)eip.data(), eip.size() * sizeof(double));
-        in.read((char*)K.data(), K.size() * sizeof(double));
-        if (!in) {
-            std::cerr << __FILE__ << ":" << __LINE__ << " error, truncated file " << file << std::endl;
-            return;
-        }
-        plan_->install(0, K, eps, eip);
+        plan_->install(0, k.K, k.eps, k.eip);
     }
 
     // min / max over particles of each moment sum_q K_pq m_j(x_pq / eps_p)

@@ -138,7 +138,8 @@ int dcpse_output_weights_ptr(dcpse_plan_t* plan, int output, const double** d_w6
 /* Installs previously saved kernels of term t (calcKernels[nnz], localEps[n],
  * localEpsInvPow[n], device pointers, copied) on a plan whose neighbour list
  * is set; the plan then counts as assembled for the per-term FP64 entry
- * points.  Replaces: Dcpse::load (src/DCPSE/Dcpse.hpp:337-379). */
+ * points (summed output weights of an earlier assembly are dropped).
+ * Replaces: Dcpse::load (src/DCPSE/Dcpse.hpp:337-379). */
 int dcpse_set_term_kernels(dcpse_plan_t* plan, int term, const double* d_kernels, const double* d_eps,
                            const double* d_eps_inv_pow);
 
@@ -271,9 +272,9 @@ int dcpse_plan_set_timing(dcpse_plan_t* plan, int enable);
  * No counterpart in the reference. */
 int dcpse_measure_fp64_peak(void* stream, double* tflops);
 /* Apply schedule knobs (autotuning): lanes per row (0 = from the mean row
- * length, else 4/8/16/32) and loading mode (0 = TMA-staged when the tiles
- * fit in shared memory, 1 = direct loads, 2 = staged, 3 = direct loads with
- * 8-deep batches).  OR-ing DCPSE_APPLY_COMPENSATE_ALL into the mode makes
+ * length, else 4/8/16/32) and loading mode (0 = automatic: direct loads,
+ * which beat the staged kernel at every size measured on GB300; 1 = direct
+ * loads, 2 = TMA-staged, 3 = direct loads with 8-deep batches).  OR-ing DCPSE_APPLY_COMPENSATE_ALL into the mode makes
  * every output of the FP32 apply use the compensated sum (by default only
  * outputs with a term of order >= 2 do; the others take plain fused sums). */
 #define DCPSE_APPLY_COMPENSATE_ALL 16

@@ -432,11 +432,22 @@ int grid_rows(int64_t rows, int rows_per_block) {
     return (int)g;
 }
 
+// FP64 batched apply: one entry per lane per step
 int lanes_for(int64_t n, int64_t nnz) {
     double avg = n > 0 ? (double)nnz / (double)n : 0.0;
     if (avg <= 24.0) return 8;
     if (avg <= 96.0) return 16;
     return 32;
+}
+
+// FP32 batched apply (4-deep load batches): 8 to 16 entries per lane, the
+// best of the sweeps on GB300 (128^3 cloud, 84 entries per row: 8 lanes
+// 0.727 ms, 4 lanes 0.763 ms, 16 lanes 0.998 ms)
+int lanes_for_f32(int64_t n, int64_t nnz) {
+    const double avg = n > 0 ? (double)nnz / (double)n : 0.0;
+    int g = 4;
+    while (g < 32 && avg / (2 * g) >= 8.0) g *= 2;
+    return g;
 }
 
 template <int G, int NO, bool RESID, int U>
@@ -577,9 +588,11 @@ cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s) {
     a.ors = p.ors ? p.ors : 1;
     a.comp = p.comp;
     a.no_self = p.no_self;
-    const int G = p.lanes ? p.lanes : lanes_for(p.n, p.nnz);
+    const int G = p.lanes ? p.lanes : lanes_for_f32(p.n, p.nnz);
     const bool resid = p.resid != nullptr;
-    const int mode = p.mode;  // 0 auto (staged if it fits), 1 direct, 2 staged, 3 direct x8
+    // 0 auto = direct loads (the staged kernel was slower at every size
+    // measured on GB300), 1 direct, 2 staged, 3 direct x8
+    const int mode = p.mode == 0 ? 1 : p.mode;
 #define DCPSE_G(GG)                                                                                  \
     case GG:                                                                                         \
         return resid ? dispatch_f32<GG, true>(a, p.nout, p.maxk, p.err, mode, s)                     \

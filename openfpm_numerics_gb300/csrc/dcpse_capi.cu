@@ -990,6 +990,15 @@ int dcpse_set_term_kernels(dcpse_plan_t* P, int term, const double* d_kernels, c
         P->flags = DCPSE_STORE_TERMS_F64;
     }
     if (!P->k_term) return fail(DCPSE_ERR_STATE, "plan was assembled without per-term kernels");
+    // summed output weights of an earlier assembly no longer match: drop
+    // them (the batched applies then ask for a new assembly)
+    dfree(P->w64);
+    dfree(P->w32);
+    if (P->r16) cudaFree(P->r16);
+    P->r16 = nullptr;
+    P->flags &= ~(DCPSE_STORE_OUT_F64 | DCPSE_STORE_OUT_F32 | DCPSE_STORE_OUT_F32_RESID);
+    dfree(P->rowsum);
+    P->rowsum_prec = -1;
     cudaStream_t s = P->stream;
     if (nnz > 0)
         DCPSE_CK(cudaMemcpyAsync(P->k_term + (size_t)term * nnz, d_kernels, sizeof(double) * nnz,

@@ -172,7 +172,7 @@ struct ApplyF32 {
     const float2* f2;
     double* out;           // [nout][n]
     int* err;              // device error word (bounded waits that ran out)
-    int mode;              // 0 staged if it fits else direct, 1 direct, 2 staged, 3 direct x8
+    int mode;              // 0 automatic (direct), 1 direct, 2 staged, 3 direct x8
     int lanes;             // lanes per row (0 = from the mean row length)
     uint32_t comp;         // outputs taking the compensated FP32 sum (bit per output)
     int no_self;           // interpolation: sum w f_q without the f_p term; f2 on the support set

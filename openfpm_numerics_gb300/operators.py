@@ -20,6 +20,8 @@ from __future__ import annotations
 
 import enum
 
+import numpy as np
+
 import torch
 
 from . import _capi as C
@@ -158,6 +160,37 @@ class _DcpseOp:
 
     def deallocate(self, parts=None):
         self.plan.close()
+
+    # Dcpse::save / load (Dcpse.hpp:302-379) through the operators'
+    # save(parts, file) / load(parts, file) (DCPSE_op.hpp:759-773): one file
+    # per term, file + "_0" for an operator of one term (the reference's
+    # name), file + "_term<t>_0" for each term of a sum or vector operator
+    def _term_file(self, file, t):
+        return file + "_0" if self.plan.n_terms == 1 else "%s_term%d_0" % (file, t)
+
+    def save(self, parts, file):
+        from . import kernel_file
+
+        eps = self.plan.eps()[0].cpu().numpy()
+        offsets = self.verletList.rowptr[:-1].cpu().numpy().astype(np.uint64)
+        for t in range(self.plan.n_terms):
+            K, eip = self.plan.term_kernels(t)
+            kernel_file.write(self._term_file(file, t), eps, eip.cpu().numpy(), K.cpu().numpy(), offsets)
+
+    def load(self, parts, file):
+        from . import kernel_file
+
+        rp = self.verletList.rowptr.cpu().numpy()
+        data = []
+        for t in range(self.plan.n_terms):
+            eps, eip, K, offsets = kernel_file.read(self._term_file(file, t))
+            if (eps.size != rp.size - 1 or eip.size != eps.size or K.size != rp[-1]
+                    or not np.array_equal(offsets, rp[:-1].astype(np.uint64))):
+                raise ValueError("%s does not match this operator's neighbour list" % self._term_file(file, t))
+            data.append((K, eps, eip))
+        for t, (K, eps, eip) in enumerate(data):
+            self.plan.set_term_kernels(t, K, eps, eip)
+        self._assembled = True
 
     def __call__(self, f, precision="f64"):
         if not self._assembled:

@@ -191,6 +191,14 @@ class DcpsePlan:
         K = _view(k.value, (info["nnz"],), torch.float64) if k.value else None
         return K, _view(e.value, (info["n"],), torch.float64)
 
+    def set_term_kernels(self, term, K, eps, eip):
+        """Install kernels of one term (Dcpse::load): K [nnz], eps and
+        eps^-|alpha| [n], host numpy or device tensors."""
+        def dev(x):
+            return torch.as_tensor(x, dtype=torch.float64).to("cuda").contiguous()
+        K, eps, eip = dev(K), dev(eps), dev(eip)
+        C.call("dcpse_set_term_kernels", self._h, int(term), _ptr(K), _ptr(eps), _ptr(eip))
+
     def output_weights(self, output):
         w64, w32 = ctypes.c_void_p(), ctypes.c_void_p()
         C.call("dcpse_output_weights_ptr", self._h, int(output), ctypes.byref(w64), ctypes.byref(w32))
@@ -306,8 +314,9 @@ class DcpsePlan:
         C.call("dcpse_plan_set_timing", self._h, int(bool(enable)))
 
     def set_apply_config(self, lanes=0, mode=0):
-        """lanes per row (0 = automatic, else 4/8/16/32); mode 0 = TMA-staged
-        when it fits, 1 = direct loads, 2 = staged."""
+        """lanes per row (0 = automatic, else 4/8/16/32); mode 0 = automatic
+        (direct loads), 1 = direct loads, 2 = TMA-staged, 3 = direct loads in
+        8-deep batches; | 16 = compensated sums for every output."""
         C.call("dcpse_plan_set_apply_config", self._h, int(lanes), int(mode))
 
     def set_assembly_config(self, bin_width=0, warps=4, qr_lanes=0):

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <fstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -135,6 +136,21 @@ static void test_op_combination() {
 
     // save / load round trip (support_options::LOAD builds an empty operator)
     Dx.save(domain, "dcpse_cpp_test_dx");
+    {
+        // Dcpse::save layout: size_t count + elements for eps, eps^-1, kernels, offsets
+        std::ifstream in("dcpse_cpp_test_dx_0", std::ios::binary | std::ios::ate);
+        const std::size_t n = domain.size_local(), nnz = vl.cols.size();
+        const std::size_t expect = 4 * 8 + (3 * n + nnz) * 8;
+        bool layout = in.is_open() && (std::size_t)in.tellg() == expect;
+        uint64_t c[1] = {0};
+        in.seekg(0);
+        in.read((char*)c, 8);
+        layout &= c[0] == n;
+        in.seekg(8 + 8 * n + 8 + 8 * n);
+        in.read((char*)c, 8);
+        layout &= c[0] == nnz;
+        EXPECT(layout, "save writes the Packer layout (counts and sizes)");
+    }
     Derivative_x<VerletList> Dx2(domain, vl, 2, rCut, support_options::LOAD);
     Dx2.load(domain, "dcpse_cpp_test_dx");
     getV<3>(domain) = Dx2(P);

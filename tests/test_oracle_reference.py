@@ -293,3 +293,27 @@ def test_bicgstab_cpu():
     b = torch.tensor(M @ xe)
     x, it, res = bicgstab(A, b, tol=1e-12)
     assert res <= 1e-12 and np.abs(x.numpy() - xe).max() < 1e-9
+
+
+def test_kernel_file_layout(tmp_path):
+    # Dcpse::save layout (Dcpse.hpp:302-331): for localEps, localEpsInvPow,
+    # calcKernels and kerOffsets, a size_t count then the elements
+    import struct
+
+    from openfpm_numerics_gb300 import kernel_file
+
+    eps = np.array([0.5, 0.25])
+    eip = np.array([2.0, 4.0])
+    K = np.array([1.0, -1.0, 0.5])
+    off = np.array([0, 2], dtype=np.uint64)
+    path = str(tmp_path / "op_0")
+    kernel_file.write(path, eps, eip, K, off)
+    end = "<" if np.little_endian else ">"
+    expect = (struct.pack(end + "Q2d", 2, *eps) + struct.pack(end + "Q2d", 2, *eip) +
+              struct.pack(end + "Q3d", 3, *K) + struct.pack(end + "Q2Q", 2, 0, 2))
+    assert open(path, "rb").read() == expect
+    e2, i2, K2, o2 = kernel_file.read(path)
+    assert np.array_equal(e2, eps) and np.array_equal(i2, eip) and np.array_equal(K2, K) and np.array_equal(o2, off)
+    open(path, "wb").write(expect[:-4])
+    with pytest.raises(ValueError):
+        kernel_file.read(path)
