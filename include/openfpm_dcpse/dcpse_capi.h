@@ -96,6 +96,21 @@ int dcpse_plan_set_box(dcpse_plan_t* plan, const double* lo, const double* hi, c
  * neighbour list is dropped (build it again).  Derivative applies, adjoints
  * and RK4 stages need one set and return DCPSE_ERR_STATE on two. */
 int dcpse_plan_set_support(dcpse_plan_t* plan, const double* d_pos_support, int64_t n_support, int self_skip);
+/* Surface DC-PSE (SurfaceDcpse, Dcpse.hpp:829-1085; the surface operators of
+ * DCPSE_surface_op.hpp and PPInterpolation's surface form).  With d_normals
+ * non-NULL (unit normals [n_base][dim] of the support set: the domain set, or
+ * the second set of dcpse_plan_set_support), dcpse_build_neighbors extends
+ * the support by 2*n_count virtual particles per base particle p at
+ * x_p +- (i s_p) n_p, i = 1..n_count (createNormalParticles, Dcpse.hpp:855-
+ * 876), s_p = d_n_spacings[p] if given (support_options::ADAPTIVE) else
+ * n_spacing; dcpse_assemble then assembles on the extended support and adds
+ * every virtual particle's kernels onto its base particle
+ * (accumulateAndDeleteNormalParticles, Dcpse.hpp:947-1015): the neighbour
+ * list holds each base particle once, in order of first appearance.  The
+ * plan keeps the pointers; each assembly needs its own neighbour build.
+ * NULL normals switch surface mode off.  The neighbour list is dropped. */
+int dcpse_plan_set_surface(dcpse_plan_t* plan, const double* d_normals, int n_count, double n_spacing,
+                           const double* d_n_spacings);
 /* sizes: n particles, nnz neighbour entries, terms, outputs, max neighbours */
 int dcpse_plan_info(dcpse_plan_t* plan, int64_t* n, int64_t* nnz, int* n_terms, int* n_outputs,
                     int* max_neighbors);

@@ -32,6 +32,7 @@ SIGNATURES = {
     "dcpse_plan_set_stream": (_I, [_P, _P]),
     "dcpse_plan_set_box": (_I, [_P, _c.POINTER(_D), _c.POINTER(_D), _PI]),
     "dcpse_plan_set_support": (_I, [_P, _P, _I64, _I]),
+    "dcpse_plan_set_surface": (_I, [_P, _P, _I, _D, _P]),
     "dcpse_plan_info": (_I, [_P, _PI64, _PI64, _PI, _PI, _PI]),
     "dcpse_term_basis": (_I, [_P, _I, _PU, _I, _PI]),
     "dcpse_build_neighbors": (_I, [_P, _P, _I64, _D, _P]),

@@ -196,6 +196,16 @@ struct dcpse_plan_s {
     int64_t n_sup = 0;
     int self_skip = 1;
     bool two_set() const { return sup_pos != nullptr; }
+    // surface DC-PSE: normals (and optional per-particle spacings) of the base
+    // support particles; the extended support is plan-owned
+    const double* surf_normals = nullptr;
+    const double* surf_spacings = nullptr;
+    double surf_spacing = 0.0;
+    int surf_count = 0;
+    double* surf_ext = nullptr;
+    int64_t surf_nb = 0;          // base particles of the extended support
+    bool surf_pending = false;    // the list refers to the extended support
+    bool surface() const { return surf_normals != nullptr; }
     // neighbour list
     int64_t n = -1, nnz = 0;
     int maxk = 0;
@@ -278,6 +288,7 @@ struct dcpse_plan_s {
         dfree(d_err);
         dfree(asm_scratch);
         asm_scratch_bytes = 0;
+        dfree(surf_ext);
         dfree(dtab);
         delete htab;
         htab = nullptr;
@@ -484,6 +495,106 @@ int split_into_plan(dcpse_plan_t* P, const double* d_f, int64_t n, int64_t strid
     return DCPSE_OK;
 }
 
+// SurfaceDcpse::accumulateAndDeleteNormalParticles on the plan's arrays: the
+// list over the extended support becomes a list over the base particles,
+// the per-term kernels and FP64 output weights are accumulated, FP32 weights
+// (and residuals) are derived from the accumulated FP64 weights.
+int surface_finish(dcpse_plan_s* P, int flags) {
+    cudaStream_t s = P->stream;
+    const int64_t n = P->n, nnz = P->nnz;
+    int32_t* counts = nullptr;
+    int64_t *rp2 = nullptr, *tmp = nullptr;
+    int32_t* cols2 = nullptr;
+    double *k2 = nullptr, *w2 = nullptr;
+    auto cleanup = [&]() {
+        dfree(counts);
+        dfree(tmp);
+        dfree(rp2);
+        dfree(cols2);
+        dfree(k2);
+        dfree(w2);
+    };
+    cudaError_t e = dalloc(&counts, (size_t)std::max<int64_t>(n, 1));
+    if (e == cudaSuccess) e = dalloc(&tmp, (size_t)scan_tmp_elems(std::max<int64_t>(n, 1)));
+    if (e == cudaSuccess) e = dalloc(&rp2, (size_t)n + 1);
+    if (e == cudaSuccess) e = surface_count(P->rowptr, P->cols, n, P->surf_nb, P->surf_count, counts, s);
+    if (e == cudaSuccess) e = exclusive_scan_i32(counts, n, rp2, tmp, s);
+    int64_t nnz2 = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&nnz2, rp2 + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = dalloc(&cols2, (size_t)nnz2 + kPad);
+    if (e == cudaSuccess && nnz2 + kPad > 0) e = cudaMemsetAsync(cols2, 0, sizeof(int32_t) * (nnz2 + kPad), s);
+    if (e == cudaSuccess && P->k_term) e = dalloc(&k2, (size_t)P->nterms * std::max<int64_t>(nnz2, 1));
+    if (e == cudaSuccess && P->w64) e = dalloc(&w2, (size_t)P->nout * std::max<int64_t>(nnz2, 1));
+    if (e != cudaSuccess) {
+        cleanup();
+        return fail(DCPSE_ERR_CUDA, std::string("surface accumulation: ") + cudaGetErrorString(e));
+    }
+    SurfAcc a{};
+    a.rowptr = P->rowptr;
+    a.cols = P->cols;
+    a.n = n;
+    a.nb = P->surf_nb;
+    a.n_count = P->surf_count;
+    a.out_rowptr = rp2;
+    a.out_cols = cols2;
+    if (k2)
+        for (int t = 0; t < P->nterms; ++t) {
+            a.in[a.nst] = P->k_term + (size_t)t * nnz;
+            a.out[a.nst++] = k2 + (size_t)t * nnz2;
+        }
+    if (w2)
+        for (int o = 0; o < P->nout; ++o) {
+            a.in[a.nst] = P->w64 + (size_t)o * nnz;
+            a.out[a.nst++] = w2 + (size_t)o * nnz2;
+        }
+    e = surface_fill(a, s);
+    if (e != cudaSuccess) {
+        cleanup();
+        return fail(DCPSE_ERR_CUDA, std::string("surface accumulation: ") + cudaGetErrorString(e));
+    }
+    // the plan now holds the accumulated operator over the base particles
+    P->free_transpose();
+    dfree(P->rowptr);
+    dfree(P->cols);
+    dfree(P->k_term);
+    dfree(P->w64);
+    dfree(P->w32);
+    if (P->r16) cudaFree(P->r16);
+    P->r16 = nullptr;
+    P->rowptr = rp2;
+    P->cols = cols2;
+    P->k_term = k2;
+    P->w64 = w2;
+    rp2 = nullptr;
+    cols2 = nullptr;
+    k2 = nullptr;
+    w2 = nullptr;
+    cleanup();
+    P->nnz = nnz2;
+    P->surf_pending = false;
+    int* mk = nullptr;
+    DCPSE_CK(dalloc(&mk, 1));
+    DCPSE_CK(cudaMemsetAsync(mk, 0, sizeof(int), s));
+    if (n > 0) row_max_kernel<<<std::max(1, std::min(num_sms() * 4, (int)((n + 255) / 256))), 256, 0, s>>>(P->rowptr, n, mk);
+    int hk = 0;
+    DCPSE_CK(cudaMemcpyAsync(&hk, mk, sizeof(int), cudaMemcpyDeviceToHost, s));
+    DCPSE_CK(cudaStreamSynchronize(s));
+    dfree(mk);
+    P->maxk = hk;
+    if (flags & DCPSE_STORE_OUT_F32) {
+        DCPSE_CK(dalloc(&P->w32, (size_t)P->nout * nnz2 + kPad));
+        DCPSE_CK(cudaMemsetAsync(P->w32, 0, sizeof(float) * ((size_t)P->nout * nnz2 + kPad), s));
+        if (flags & DCPSE_STORE_OUT_F32_RESID) {
+            DCPSE_CK(cudaMalloc(&P->r16, ((size_t)P->nout * nnz2 + kPad) * 2));
+            DCPSE_CK(cudaMemsetAsync(P->r16, 0, ((size_t)P->nout * nnz2 + kPad) * 2, s));
+        }
+        DCPSE_CK(narrow_weights(P->w64, (int64_t)P->nout * nnz2, P->w32, P->r16, s));
+        if (!(flags & DCPSE_STORE_OUT_F64)) dfree(P->w64);
+    }
+    return DCPSE_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -593,6 +704,27 @@ int dcpse_plan_set_support(dcpse_plan_t* P, const double* d_pos_support, int64_t
     return DCPSE_OK;
 }
 
+int dcpse_plan_set_surface(dcpse_plan_t* P, const double* d_normals, int n_count, double n_spacing,
+                           const double* d_n_spacings) {
+    if (int rc = check_plan(P)) return rc;
+    if (d_normals && n_count < 1) return fail(DCPSE_ERR_ARG, "n_count must be >= 1");
+    if (d_normals && !d_n_spacings && !(n_spacing > 0.0)) return fail(DCPSE_ERR_ARG, "n_spacing must be > 0");
+    P->free_assembly();
+    P->free_transpose();
+    dfree(P->rowptr);
+    dfree(P->cols);
+    dfree(P->surf_ext);
+    P->n = -1;
+    P->nnz = 0;
+    P->maxk = 0;
+    P->surf_normals = d_normals;
+    P->surf_count = d_normals ? n_count : 0;
+    P->surf_spacing = n_spacing;
+    P->surf_spacings = d_normals ? d_n_spacings : nullptr;
+    P->surf_pending = false;
+    return DCPSE_OK;
+}
+
 int dcpse_plan_info(dcpse_plan_t* P, int64_t* n, int64_t* nnz, int* n_terms, int* n_outputs, int* max_neighbors) {
     if (int rc = check_plan(P)) return rc;
     if (n) *n = P->n;
@@ -635,6 +767,23 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
         DCPSE_CK(dalloc(&P->cols, kPad));
         return DCPSE_OK;
     }
+    // the support set: the domain set itself, a second set, or (surface
+    // operators) either of them extended along the normals
+    const double* ps = P->two_set() ? P->sup_pos : d_pos;
+    int64_t ns = P->two_set() ? P->n_sup : n;
+    P->surf_pending = false;
+    if (P->surface()) {
+        dfree(P->surf_ext);
+        const int64_t next = ns * (1 + 2 * (int64_t)P->surf_count);
+        DCPSE_CK(dalloc(&P->surf_ext, (size_t)std::max<int64_t>(next, 1) * dim));
+        DCPSE_CK(surface_extend(dim, ps, P->surf_normals, ns, P->surf_count, P->surf_spacing, P->surf_spacings,
+                                P->surf_ext, s));
+        P->surf_nb = ns;
+        ps = P->surf_ext;
+        ns = next;
+    }
+    if (ns >= (int64_t)INT32_MAX) return fail(DCPSE_ERR_CAPACITY, "at most 2^31-1 support particles");
+    const bool other_support = P->two_set() || P->surface();
     unsigned long long* mm = nullptr;
     DCPSE_CK(dalloc(&mm, 2 * kMaxDim));
     double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
@@ -644,7 +793,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
             hi[d] = P->hi[d];
         }
     } else {
-        cudaError_t e = bounding_box(dim, d_pos, n, P->sup_pos, P->two_set() ? P->n_sup : 0, lo, hi, mm, s);
+        cudaError_t e = bounding_box(dim, d_pos, n, other_support ? ps : nullptr, other_support ? ns : 0, lo, hi, mm, s);
         if (e != cudaSuccess) {
             dfree(mm);
             return fail(DCPSE_ERR_CUDA, std::string("bounding box: ") + cudaGetErrorString(e));
@@ -674,9 +823,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
         rmax = std::max(rcut > 0 ? rcut : 0.0, rhi[0]);
     }
     dfree(mm);
-    // the cell list holds the support set (the domain set itself for one set)
-    const double* ps = P->two_set() ? P->sup_pos : d_pos;
-    const int64_t ns = P->two_set() ? P->n_sup : n;
+    // the cell list holds the support set
     // cells no smaller than the largest radius; total bounded by ~4 n
     CellGrid cg{};
     double cmin = rmax * (1.0 + 1e-9);
@@ -757,11 +904,13 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     if (e != cudaSuccess) return fail(DCPSE_ERR_CUDA, std::string("neighbour build: ") + cudaGetErrorString(e));
     P->nnz = nnz;
     P->maxk = hk;
+    P->surf_pending = P->surface();
     return DCPSE_OK;
 }
 
 int dcpse_set_neighbors(dcpse_plan_t* P, int64_t n, int64_t nnz, const int64_t* d_rowptr, const int32_t* d_cols) {
     if (int rc = check_plan(P)) return rc;
+    if (P->surface()) return fail(DCPSE_ERR_STATE, "surface operators build their own lists (dcpse_build_neighbors)");
     if (n < 0 || nnz < 0 || !d_rowptr || (nnz > 0 && !d_cols)) return fail(DCPSE_ERR_ARG, "bad CSR arrays");
     cudaStream_t s = P->stream;
     P->free_assembly();
@@ -822,6 +971,16 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
         return fail(DCPSE_ERR_ARG, "nothing to store");
     if ((flags & DCPSE_ASSEMBLE_FAST) && (flags & DCPSE_STORE_TERMS_F64))
         return fail(DCPSE_ERR_ARG, "per-term kernels need the reference (non-fast) assembly");
+    if ((flags & DCPSE_STORE_OUT_F32_RESID) && !(flags & DCPSE_STORE_OUT_F32))
+        return fail(DCPSE_ERR_ARG, "residuals need DCPSE_STORE_OUT_F32");
+    if (P->surface() && !P->surf_pending)
+        return fail(DCPSE_ERR_STATE, "surface operators assemble once per neighbour build (build it again)");
+    // surface operators accumulate FP64 values; FP32 weights follow from them
+    const int user_flags = flags;
+    if (P->surface()) {
+        if (flags & DCPSE_STORE_OUT_F32) flags |= DCPSE_STORE_OUT_F64;
+        flags &= ~(DCPSE_STORE_OUT_F32 | DCPSE_STORE_OUT_F32_RESID);
+    }
     cudaStream_t s = P->stream;
     const int64_t n = P->n, nnz = P->nnz;
     const int ng = P->htab->ngroups;
@@ -835,8 +994,6 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     if (!(flags & DCPSE_STORE_OUT_F64)) dfree(P->w64);
     if ((flags & DCPSE_STORE_OUT_F32) && !P->w32) DCPSE_CK(dalloc(&P->w32, (size_t)P->nout * nnz + kPad));
     if (!(flags & DCPSE_STORE_OUT_F32)) dfree(P->w32);
-    if ((flags & DCPSE_STORE_OUT_F32_RESID) && !(flags & DCPSE_STORE_OUT_F32))
-        return fail(DCPSE_ERR_ARG, "residuals need DCPSE_STORE_OUT_F32");
     if ((flags & DCPSE_STORE_OUT_F32_RESID) && !P->r16)
         DCPSE_CK(cudaMalloc(&P->r16, ((size_t)P->nout * nnz + kPad) * 2));
     if (!(flags & DCPSE_STORE_OUT_F32_RESID) && P->r16) {
@@ -848,7 +1005,7 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     a.dim = P->dim;
     a.n = n;
     a.pos = d_pos;
-    a.spos = P->two_set() ? P->sup_pos : d_pos;
+    a.spos = P->surface() ? P->surf_ext : (P->two_set() ? P->sup_pos : d_pos);
     a.rowptr = P->rowptr;
     a.cols = P->cols;
     a.geom = plan_geom(P);
@@ -904,6 +1061,10 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     if (e == cudaErrorInvalidConfiguration)
         return fail(DCPSE_ERR_CAPACITY, "assembly: the QR work space of this lane grouping exceeds shared memory");
     if (e != cudaSuccess) return fail(DCPSE_ERR_CUDA, std::string("assembly: ") + cudaGetErrorString(e));
+    if (P->surface()) {
+        if (int rc = surface_finish(P, user_flags)) return rc;
+        flags = user_flags;
+    }
     P->assembled = true;
     P->flags = flags;
     unsigned long long init[2] = {0ull, ~0ull};

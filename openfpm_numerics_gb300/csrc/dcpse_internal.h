@@ -204,6 +204,30 @@ cudaError_t csr_row_counts(const int64_t* rowptr, const int32_t* cols, const int
                            int32_t* counts, cudaStream_t s);
 cudaError_t csr_fill(const MatArgs& a, cudaStream_t s);
 
+// ------------------------------------------------------------- surface --
+// support extension along the normals (base particles, then 2 n_count
+// virtual particles per base particle) and accumulation of the virtual
+// particles' kernels onto their base particles
+cudaError_t surface_extend(int dim, const double* base, const double* normals, int64_t nb, int n_count, double spacing,
+                           const double* spacings, double* out, cudaStream_t s);
+cudaError_t surface_count(const int64_t* rowptr, const int32_t* cols, int64_t n, int64_t nb, int n_count,
+                          int32_t* counts, cudaStream_t s);
+constexpr int kMaxStreams = kMaxTerms + kMaxOutputs;
+struct SurfAcc {
+    const int64_t* rowptr;        // list over the extended support
+    const int32_t* cols;
+    int64_t n, nb;
+    int n_count;
+    const int64_t* out_rowptr;    // accumulated list over the base particles
+    int32_t* out_cols;
+    int nst;                      // value streams (per-term kernels, output weights)
+    const double* in[kMaxStreams];
+    double* out[kMaxStreams];
+};
+cudaError_t surface_fill(const SurfAcc& a, cudaStream_t s);
+// w32 = (float)w64 and the bf16 residual w64 - w32 (r16 may be null)
+cudaError_t narrow_weights(const double* w64, int64_t m, float* w32, void* r16, cudaStream_t s);
+
 // --------------------------------------------------------------- adjoint --
 // transposed list: trow[n+1], per entry the source row tsrc and entry index tidx
 cudaError_t build_transpose(const int64_t* rowptr, const int32_t* cols, int64_t n, int64_t nnz, int32_t* cnt,

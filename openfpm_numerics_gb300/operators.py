@@ -55,6 +55,8 @@ class VerletList:
     def __init__(self, parts, rCut, rcut_pp=None, opt=VL_NON_SYMMETRIC | VL_SKIP_REF_PART, support=None):
         self.rCut = float(rCut)
         self.support = support
+        self.skip_ref = bool(opt & VL_SKIP_REF_PART) and support is None
+        self.rcut_pp = rcut_pp
         plan = DcpsePlan(parts.dims, [[(1,) + (0,) * (parts.dims - 1)]], box=parts.box)
         if support is not None:
             plan.set_support(support.getPosTensor())
@@ -133,10 +135,14 @@ class _DcpseOp:
         self.HOverEpsilon = h_over_eps
         self.verletList = verletList
         self.plan = DcpsePlan(self.dim, outputs, order=self.ord, h_over_eps=h_over_eps, box=parts.box)
-        self.plan.set_neighbors(verletList.rowptr, verletList.cols)
         self._assembled = False
+        self._prepare(parts)
         if opt == support_options.RADIUS:
             self._assemble(parts)
+
+    def _prepare(self, parts):
+        """Hand the neighbour list to the plan (before every assembly)."""
+        self.plan.set_neighbors(self.verletList.rowptr, self.verletList.cols)
 
     def _assemble(self, parts):
         rc = self.plan.assemble(parts.getPosTensor(),
@@ -155,7 +161,7 @@ class _DcpseOp:
         updateVerlet first)."""
         if verletList is not None:
             self.verletList = verletList
-        self.plan.set_neighbors(self.verletList.rowptr, self.verletList.cols)
+        self._prepare(parts)
         self._assemble(parts)
 
     def deallocate(self, parts=None):
@@ -312,6 +318,81 @@ class OperatorSet(_DcpseOp):
         super().__init__(parts, verletList, ord, rCut, opt, outputs=outs, kind="vector", **kw)
 
 
+class _SurfaceOp(_DcpseOp):
+    """Surface DC-PSE operator (SurfaceDcpse, Dcpse.hpp:829-1085): the
+    support of every particle is extended by nCount virtual particles on each
+    side along its normal, the operator is assembled on the extended support
+    and the virtual particles' kernels are added onto their surface particle.
+    The Verlet list passed in gives the cutoff (its rCut, or per-particle
+    radii) and whether a particle is its own neighbour; like the reference,
+    the operator replaces its lists with the accumulated ones."""
+
+    def __init__(self, parts, verletList, ord, rCut, nSpacing, nCount, opt=support_options.RADIUS, *, sig,
+                 normal, **kw):
+        if opt not in (support_options.RADIUS, support_options.LOAD, support_options.ADAPTIVE):
+            raise NotImplementedError("support option %r" % (opt,))
+        self.nSpacing = float(nSpacing)
+        self.nCount = int(nCount)
+        self.normal = normal
+        self._adaptive = opt == support_options.ADAPTIVE
+        if self._adaptive and verletList.rcut_pp is None:
+            raise ValueError("support_options.ADAPTIVE needs a Verlet list with per-particle radii")
+        _DcpseOp.__init__(self, parts, verletList, ord, rCut,
+                          support_options.LOAD if opt == support_options.LOAD else support_options.RADIUS,
+                          outputs=[[tuple(sig)]], kind="single", **kw)
+
+    def _prepare(self, parts):
+        normals = parts.props[self.normal]
+        spacings = None
+        if self._adaptive:
+            # nSpacing_p = property 0 / nCount (Dcpse.hpp:1057-1066)
+            spacings = parts.props[0].to(torch.float64) / self.nCount
+        self.plan.set_support(None, self_skip=self.verletList.skip_ref)
+        self.plan.set_surface(normals, self.nCount, self.nSpacing, spacings)
+        rpp = self.verletList.rcut_pp
+        self.plan.build_neighbors(parts.getPosTensor(), self.verletList.rCut if rpp is None else 0.0, rpp)
+
+    def _assemble(self, parts):
+        _DcpseOp._assemble(self, parts)
+        rp, cl = self.plan.neighbors()
+        self.verletList.rowptr = rp.clone()
+        self.verletList.cols = cl.clone()
+
+
+def _surface(name, sig_fn, ref):
+    def init(self, parts, verletList, ord, rCut, nSpacing, nCount, opt=support_options.RADIUS, *, normal, **kw):
+        _SurfaceOp.__init__(self, parts, verletList, ord, rCut, nSpacing, nCount, opt, sig=sig_fn(parts.dims),
+                            normal=normal, **kw)
+
+    return type(name, (_SurfaceOp,), {"__init__": init, "__doc__": "%s (%s); normal = property holding the "
+                                                                   "unit normals (NORMAL_ID)" % (name, ref)})
+
+
+SurfaceDerivative_x = _surface("SurfaceDerivative_x", lambda d: _unit(d, 0), "DCPSE_surface_op.hpp:11-109")
+SurfaceDerivative_y = _surface("SurfaceDerivative_y", lambda d: _unit(d, 1), "DCPSE_surface_op.hpp:125-209")
+SurfaceDerivative_z = _surface("SurfaceDerivative_z", lambda d: _unit(d, 2), "DCPSE_surface_op.hpp:225-309")
+SurfaceDerivative_xx = _surface("SurfaceDerivative_xx", lambda d: _unit(d, 0, 2), "DCPSE_surface_op.hpp:426-509")
+SurfaceDerivative_yy = _surface("SurfaceDerivative_yy", lambda d: _unit(d, 1, 2), "DCPSE_surface_op.hpp:525-607")
+SurfaceDerivative_zz = _surface("SurfaceDerivative_zz", lambda d: _unit(d, 2, 2), "DCPSE_surface_op.hpp:623-706")
+SurfaceDerivative_xy = _surface("SurfaceDerivative_xy", lambda d: tuple(1 if i < 2 else 0 for i in range(d)),
+                                "DCPSE_surface_op.hpp:709-819")
+SurfaceDerivative_yz = _surface("SurfaceDerivative_yz", lambda d: tuple(1 if i in (1, 2) else 0 for i in range(d)),
+                                "DCPSE_surface_op.hpp:821-919")
+SurfaceDerivative_xz = _surface("SurfaceDerivative_xz", lambda d: tuple(1 if i in (0, 2) else 0 for i in range(d)),
+                                "DCPSE_surface_op.hpp:921-1020")
+# the reference builds Laplace_Beltrami as one Dcpse of signature (2, 2, 2)
+# (DCPSE_surface_op.hpp:326-347), kept as is
+Laplace_Beltrami = _surface("Laplace_Beltrami", lambda d: (2,) * d, "DCPSE_surface_op.hpp:326-410")
+
+
+class SurfaceDerivative_G(_SurfaceOp):
+    """SurfaceDerivative_G (DCPSE_surface_op.hpp:1022-1100): signature p."""
+
+    def __init__(self, parts, verletList, ord, rCut, nSpacing, nCount, p, opt=support_options.RADIUS, *, normal,
+                 **kw):
+        super().__init__(parts, verletList, ord, rCut, nSpacing, nCount, opt, sig=tuple(p), normal=normal, **kw)
+
+
 def createVerletTwoPhase(particlesDomain, particlesSupport, rCut, cellList=None):
     """Lists of the support particles within rCut of every domain particle
     (openfpm's createVerletTwoPhase, used by the two-set tests of
@@ -334,9 +415,19 @@ class PPInterpolation:
     particles (createVerletTwoPhase, or getVerlet of one set that is both)."""
 
     def __init__(self, particlesSupport, particlesDomain, verletList, ord, rCut, opt=support_options.RADIUS,
-                 *, allow_failed_particles=False, h_over_eps=0.9):
+                 *, allow_failed_particles=False, h_over_eps=0.9, nSpacing=None, isSurfaceInterpolation=False,
+                 normal=None):
+        """With isSurfaceInterpolation=True (the reference's surface
+        constructor, DcpseInterpolation.hpp:94-113) the support particles are
+        extended along their normals (property ``normal`` of the support
+        set) with nCount = int(rCut / nSpacing) virtual particles per side."""
         if opt not in (support_options.RADIUS, support_options.LOAD):
             raise NotImplementedError("support option %r" % (opt,))
+        self._surface = bool(isSurfaceInterpolation)
+        if self._surface and (nSpacing is None or normal is None):
+            raise ValueError("surface interpolation needs nSpacing and the normal property")
+        self.nSpacing = None if nSpacing is None else float(nSpacing)
+        self.normal = normal
         self.particlesSupport = particlesSupport
         self.particlesDomain = particlesDomain
         self.verletList = verletList
@@ -356,8 +447,14 @@ class PPInterpolation:
         if verletList is not None:
             self.verletList = verletList
         two = self.particlesSupport is not self.particlesDomain
-        self.plan.set_support(self.particlesSupport.getPosTensor() if two else None)
-        self.plan.set_neighbors(self.verletList.rowptr, self.verletList.cols)
+        self.plan.set_support(self.particlesSupport.getPosTensor() if two else None,
+                              self_skip=getattr(self.verletList, "skip_ref", False))
+        if self._surface:
+            n_count = int(self.rCut / self.nSpacing)
+            self.plan.set_surface(self.particlesSupport.props[self.normal], n_count, self.nSpacing)
+            self.plan.build_neighbors(self.particlesDomain.getPosTensor(), self.verletList.rCut)
+        else:
+            self.plan.set_neighbors(self.verletList.rowptr, self.verletList.cols)
         rc = self.plan.assemble(self.particlesDomain.getPosTensor(),
                                 C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
         if rc == C.ERR_PARTICLES and not self._allow:
@@ -366,6 +463,10 @@ class PPInterpolation:
                 raise ValueError("Not enough neighbour points passed for Vandermonde matrix construction! "
                                  "(%d particles, first %d)" % (nb, first))
             raise RuntimeError("DC-PSE assembly failed for %d particles (first %d, status %d)" % (nb, first, code))
+        if self._surface:
+            rp, cl = self.plan.neighbors()
+            self.verletList.rowptr = rp.clone()
+            self.verletList.cols = cl.clone()
         self._assembled = True
 
     def __call__(self, f, precision="f64"):

@@ -143,6 +143,22 @@ class DcpsePlan:
         self._support = pos_support
         self.n = None
 
+    def set_surface(self, normals=None, n_count=0, n_spacing=0.0, n_spacings=None):
+        """Surface operator (SurfaceDcpse): unit normals [n_base, dim] of the
+        support particles, n_count virtual particles on each side at spacing
+        n_spacing (or per particle n_spacings).  None switches it off.  The
+        plan keeps references; the neighbour list must be built again."""
+        if normals is not None:
+            normals = normals.to(device="cuda", dtype=torch.float64).contiguous()
+            if n_spacings is not None:
+                n_spacings = n_spacings.to(device="cuda", dtype=torch.float64).contiguous()
+            C.call("dcpse_plan_set_surface", self._h, _ptr(normals), int(n_count), float(n_spacing),
+                   _ptr(n_spacings))
+        else:
+            C.call("dcpse_plan_set_surface", self._h, None, 0, 0.0, None)
+        self._surface = (normals, n_spacings)
+        self.n = None
+
     def build_neighbors(self, pos, rcut, rcut_pp=None):
         pos = self._check_pos(pos)
         if rcut_pp is not None:

@@ -76,6 +76,10 @@ def lib():
         L.orc_operator_csr.argtypes = [ctypes.c_int64, _I64, _I64, _I32, ctypes.c_int, ctypes.POINTER(_D),
                                        ctypes.POINTER(_D), _D, ctypes.c_double, ctypes.c_int64, ctypes.c_int64, _I64,
                                        _I64, _D]
+        L.orc_surface_extend.argtypes = [ctypes.c_int, _D, _D, ctypes.c_int64, ctypes.c_int, ctypes.c_double, _D,
+                                         _D]
+        L.orc_surface_accumulate.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int, _I64, _I32, ctypes.c_int,
+                                             ctypes.POINTER(_D), _I64, _I32, ctypes.POINTER(_D)]
         L.orc_apply_sum.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _D, _I64, _I32,
                                     ctypes.POINTER(_D), ctypes.POINTER(_D), _U, _D, ctypes.c_int]
         L.orc_apply_multi.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _D, _I64, _I32, ctypes.POINTER(_D),
@@ -231,6 +235,39 @@ def operator_csr(rowptr, cols, Ks, eips, diff_orders, *, coeff=1.0, rows=None, n
     out_vals = np.zeros(max(int(out_rp[-1]), 1))
     lib().orc_operator_csr(*args, _p(out_cols, _I64), _p(out_vals, _D))
     return out_rp, out_cols[: out_rp[-1]], out_vals[: out_rp[-1]]
+
+
+def surface_extend(base, normals, n_count, spacing=0.0, spacings=None):
+    """SurfaceDcpse::createNormalParticles: base particles followed by 2
+    n_count virtual particles along each normal -> [nb (1 + 2 n_count), dim]."""
+    base = _c(base, np.float64)
+    nb, dim = base.shape
+    normals = _c(normals, np.float64)
+    sp = None if spacings is None else _c(spacings, np.float64)
+    out = np.zeros((nb * (1 + 2 * n_count), dim))
+    lib().orc_surface_extend(dim, _p(base, _D), _p(normals, _D), nb, int(n_count), float(spacing),
+                             None if sp is None else _p(sp, _D), _p(out, _D))
+    return out
+
+
+def surface_accumulate(rowptr, cols, Ks, nb, n_count):
+    """SurfaceDcpse::accumulateAndDeleteNormalParticles -> (rowptr, cols,
+    [K per term]) over the base particles."""
+    rowptr = _c(rowptr, np.int64)
+    cols = _c(cols, np.int32)
+    Ks = [_c(k, np.float64) for k in Ks]
+    n = rowptr.size - 1
+    kp = (_D * len(Ks))(*[_p(k, _D) for k in Ks])
+    out_rp = np.zeros(n + 1, np.int64)
+    lib().orc_surface_accumulate(n, int(nb), int(n_count), _p(rowptr, _I64), _p(cols, _I32), len(Ks), kp,
+                                 _p(out_rp, _I64), None, None)
+    m = int(out_rp[-1])
+    out_cols = np.zeros(max(m, 1), np.int32)
+    out_K = [np.zeros(max(m, 1)) for _ in Ks]
+    okp = (_D * len(Ks))(*[_p(k, _D) for k in out_K])
+    lib().orc_surface_accumulate(n, int(nb), int(n_count), _p(rowptr, _I64), _p(cols, _I32), len(Ks), kp,
+                                 _p(out_rp, _I64), _p(out_cols, _I32), okp)
+    return out_rp, out_cols[:m], [k[:m] for k in out_K]
 
 
 def apply_sum(f, rowptr, cols, Ks, eips, diff_orders, *, nthreads=1):

@@ -859,4 +859,61 @@ void orc_operator_csr(int64_t nrows, const int64_t* rows, const int64_t* rowptr,
     }
 }
 
+// SurfaceDcpse::createNormalParticles (Dcpse.hpp:855-876): after the nb base
+// (surface) particles come 2*n_count virtual particles per base particle p,
+// for i = 1..n_count first x_p + i*s_p*n_p then x_p - i*s_p*n_p, each
+// coordinate xp[j] + (i*s_p)*N[j] (resp. minus), with s_p = spacings[p] if
+// given (support_options::ADAPTIVE), else spacing.  out holds
+// nb*(1 + 2*n_count) positions.
+void orc_surface_extend(int dim, const double* base, const double* normals, int64_t nb, int n_count, double spacing,
+                        const double* spacings, double* out) {
+    for (int64_t p = 0; p < nb * dim; ++p) out[p] = base[p];
+    int64_t v = nb;
+    for (int64_t p = 0; p < nb; ++p) {
+        const double s = spacings ? spacings[p] : spacing;
+        for (int i = 1; i <= n_count; ++i) {
+            const double is = (double)i * s;
+            for (int j = 0; j < dim; ++j) out[v * dim + j] = base[p * dim + j] + is * normals[p * dim + j];
+            ++v;
+            for (int j = 0; j < dim; ++j) out[v * dim + j] = base[p * dim + j] - is * normals[p * dim + j];
+            ++v;
+        }
+    }
+}
+
+// SurfaceDcpse::accumulateAndDeleteNormalParticles (Dcpse.hpp:947-1015): the
+// kernels of every virtual support particle are added onto its base particle
+// (q < nb: itself; else (q - nb) / (2 n_count)); the new list holds each base
+// particle once, in order of first appearance, with the running sums
+// (first value, then += in list order).  Two calls: out_cols == NULL fills
+// out_rowptr only.  nterms kernel arrays share the list.
+void orc_surface_accumulate(int64_t n_dom, int64_t nb, int n_count, const int64_t* rowptr, const int32_t* cols,
+                            int nterms, const double* const* K, int64_t* out_rowptr, int32_t* out_cols,
+                            double* const* out_K) {
+    out_rowptr[0] = 0;
+    std::vector<int64_t> seen;
+    for (int64_t p = 0; p < n_dom; ++p) {
+        seen.clear();
+        const int64_t o = out_rowptr[p];
+        for (int64_t j = rowptr[p]; j < rowptr[p + 1]; ++j) {
+            const int64_t q = cols[j];
+            const int64_t real = (q < nb) ? q : (q - nb) / (2 * (int64_t)n_count);
+            int64_t slot = -1;
+            for (size_t s2 = 0; s2 < seen.size(); ++s2)
+                if (seen[s2] == real) slot = (int64_t)s2;
+            if (slot < 0) {
+                slot = (int64_t)seen.size();
+                seen.push_back(real);
+                if (out_cols) {
+                    out_cols[o + slot] = (int32_t)real;
+                    for (int t = 0; t < nterms; ++t) out_K[t][o + slot] = K[t][j];
+                }
+            } else if (out_cols) {
+                for (int t = 0; t < nterms; ++t) out_K[t][o + slot] = out_K[t][o + slot] + K[t][j];
+            }
+        }
+        out_rowptr[p + 1] = o + (int64_t)seen.size();
+    }
+}
+
 }  // extern "C"

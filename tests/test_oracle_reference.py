@@ -317,3 +317,38 @@ def test_kernel_file_layout(tmp_path):
     open(path, "wb").write(expect[:-4])
     with pytest.raises(ValueError):
         kernel_file.read(path)
+
+
+def _circle(n):
+    th = np.arange(n) * (2 * np.pi / n)
+    pos = np.stack([np.cos(th), np.sin(th)], 1)
+    return th, pos
+
+
+def test_surface_circle(orc):
+    # DCPSE_op_Surface_tests.cpp:97-182 (dcpse_surface_circle): 512 particles
+    # on the unit circle, rCut = 5.1 h (h = 3/511), nCount = 5 virtual
+    # particles per side at spacing h; SDxx + SDyy of sin(theta) = -sin(theta),
+    # worst < 0.03
+    n = 512
+    h = 3.0 / 511
+    rcut = 5.1 * h
+    nc = int(rcut / h)
+    th, pos = _circle(n)
+    ext = orc.surface_extend(pos, pos, nc, h)
+    assert ext.shape == (n * (1 + 2 * nc), 2)
+    assert np.array_equal(ext[n + 2 * nc * 7 + 2 * 2], pos[7] + (3.0 * h) * pos[7])   # i = 3, + side
+    rp, cols = orc.neighbors(pos, rcut, support=ext, self_skip=True)
+    terms = [orc.assemble(pos, rp, cols, s, 2, support=ext) for s in [(2, 0), (0, 2)]]
+    rp2, c2, K2 = orc.surface_accumulate(rp, cols, [t[2] for t in terms], n, nc)
+    assert c2.max() < n and np.all(np.diff(rp2) <= np.diff(rp))
+    out = orc.apply_sum(np.sin(th), rp2, c2, K2, [t[1] for t in terms], [2, 2])
+    assert np.max(np.abs(out + np.sin(th))) < 0.03
+    # each base particle appears once per row, in order of first appearance
+    p = 11
+    seen = []
+    for q in cols[rp[p]:rp[p + 1]]:
+        r = q if q < n else (q - n) // (2 * nc)
+        if r not in seen:
+            seen.append(r)
+    assert list(c2[rp2[p]:rp2[p + 1]]) == seen
