@@ -11,8 +11,9 @@
 // matrix); an assignment evaluates every operator node on the GPU in FP64 in
 // the reference's order (VECT_DCPSE :65-67, VECT_DCPSE_V :144-153,
 // VECT_DCPSE_V_SUM :388-399) and combines the nodes on the host.
-// Only linear combinations of operator nodes are supported on the right-hand
-// side (the reference's general expression engine is not part of this path).
+// Divergence, Advection and Curl2D are operator nodes too.  Only linear
+// combinations of operator nodes are supported on the right-hand side (the
+// reference's general expression engine is not part of this path).
 #pragma once
 
 #include <algorithm>
@@ -20,6 +21,8 @@
 #include <functional>
 #include <memory>
 #include <string>
+#include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "Dcpse.hpp"
@@ -68,6 +71,15 @@ template <typename V, typename = void>
 struct is_indexable : std::false_type {};
 template <typename V>
 struct is_indexable<V, std::void_t<decltype(std::declval<V&>()[0])>> : std::true_type {};
+
+// components of a property: N for std::array<T, N> or T[N], else 1
+template <typename V, typename = void>
+struct prop_ncomp : std::integral_constant<int, 1> {};
+template <typename V>
+struct prop_ncomp<V, std::enable_if_t<(std::tuple_size<V>::value > 0)>>
+    : std::integral_constant<int, (int)std::tuple_size<V>::value> {};
+template <typename T, std::size_t N>
+struct prop_ncomp<T[N], void> : std::integral_constant<int, (int)N> {};
 }  // namespace detail
 
 // getV<prp>(parts): a property of a particle set, usable as an operand and
@@ -78,9 +90,17 @@ struct PropRef {
     typedef vector_type vtype;
     vector_type& getVector() const { return v; }
 
-    std::vector<double> values() const {
+    typedef typename std::remove_reference<decltype(std::declval<vector_type&>().template getProp<prp>(0))>::type
+        prop_type;
+    static constexpr int ncomp = detail::prop_ncomp<prop_type>::value;
+
+    std::vector<double> values() const { return component(0); }
+
+    // component c of every particle (the value itself for a scalar property)
+    std::vector<double> component(int c) const {
         std::vector<double> f(v.size_local());
-        for (std::size_t p = 0; p < f.size(); ++p) f[p] = (double)v.template getProp<prp>(p);
+        for (std::size_t p = 0; p < f.size(); ++p)
+            f[p] = (double)detail::prop_component(v.template getProp<prp>(p), c, detail::is_indexable<prop_type>{});
         return f;
     }
 
@@ -198,6 +218,9 @@ public:
     }
 
     dcpse_plan_t* plan() const { return plan_->plan(); }
+
+protected:
+    detail::PlanHost* host() const { return plan_.get(); }
 
 private:
     template <typename particles_type>
@@ -343,6 +366,109 @@ public:
         : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut, outs(particles_type::dims), opt) {}
 };
 
+// Divergence_T (DCPSE_op.hpp:1503-1630): dim terms e_i applied to the
+// components of a vector property, VECT_DCPSE_V_DIV (:446-475):
+// div = ((0 + D_0 v_0) + D_1 v_1) + ...
+template <typename VerletList_type>
+class Divergence : public DcpseOperator<VerletList_type> {
+    static std::vector<std::vector<std::vector<unsigned>>> outs(int dim) {
+        std::vector<std::vector<std::vector<unsigned>>> o;
+        for (int i = 0; i < dim; ++i) o.push_back({detail::unit(dim, i)});
+        return o;
+    }
+
+public:
+    template <typename particles_type>
+    Divergence(particles_type& parts, VerletList_type& verletList, unsigned int ord,
+               typename particles_type::stype rCut, support_options opt = support_options::RADIUS)
+        : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut, outs(particles_type::dims), opt),
+          dim_(particles_type::dims) {}
+
+    template <unsigned int prp, typename vector_type>
+    Expr operator()(PropRef<prp, vector_type> arg) {
+        Node nd;
+        nd.ncomp = 1;
+        detail::PlanHost* P = this->host();
+        const int dim = dim_;
+        nd.eval = [P, arg, dim](std::vector<std::vector<double>>& out) {
+            const std::size_t n = arg.v.size_local();
+            out.assign(1, std::vector<double>(n, 0.0));
+            std::vector<double> d(n);
+            for (int i = 0; i < dim; ++i) {
+                std::vector<double> f = arg.component(i);
+                P->apply_output(i, f.data(), d.data());
+                for (std::size_t p = 0; p < n; ++p) out[0][p] = out[0][p] + d[p];
+            }
+        };
+        Expr e;
+        e.nodes.push_back(nd);
+        return e;
+    }
+
+private:
+    int dim_;
+};
+
+// Advection_T (DCPSE_op.hpp:1632-1781): (v . grad) f, VECT_DCPSE_V_DOT
+// (:531-565): adv = ((0 + v_0 D_0 f) + v_1 D_1 f) + ..., component-wise for a
+// vector property f
+template <typename VerletList_type>
+class Advection : public Divergence<VerletList_type> {
+public:
+    using Divergence<VerletList_type>::Divergence;
+
+    template <unsigned int p1, typename vt1, unsigned int p2, typename vt2>
+    Expr operator()(PropRef<p1, vt1> vel, PropRef<p2, vt2> arg) {
+        Node nd;
+        nd.ncomp = PropRef<p2, vt2>::ncomp;
+        detail::PlanHost* P = this->host();
+        const int dim = vt1::dims;
+        nd.eval = [P, vel, arg, dim](std::vector<std::vector<double>>& out) {
+            const std::size_t n = arg.v.size_local();
+            const int nc = PropRef<p2, vt2>::ncomp;
+            out.assign(nc, std::vector<double>(n, 0.0));
+            std::vector<double> d(n);
+            for (int c = 0; c < nc; ++c) {
+                std::vector<double> f = arg.component(c);
+                for (int i = 0; i < dim; ++i) {
+                    const std::vector<double> vi = vel.component(i);
+                    P->apply_output(i, f.data(), d.data());
+                    for (std::size_t p = 0; p < n; ++p) out[c][p] = out[c][p] + vi[p] * d[p];
+                }
+            }
+        };
+        Expr e;
+        e.nodes.push_back(nd);
+        return e;
+    }
+};
+
+// Curl2D_T (DCPSE_op.hpp:1227-1340): terms e_1 and e_0, VECT_DCPSE_V_CURL2D
+// (:206-233): (D_y f, -D_x f)
+template <typename VerletList_type>
+class Curl2D : public DcpseOperator<VerletList_type> {
+    static std::vector<std::vector<std::vector<unsigned>>> outs(int dim) {
+        return {{detail::unit(dim, 1)}, {detail::unit(dim, 0)}};
+    }
+
+public:
+    template <typename particles_type>
+    Curl2D(particles_type& parts, VerletList_type& verletList, unsigned int ord, typename particles_type::stype rCut,
+           support_options opt = support_options::RADIUS)
+        : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut, outs(particles_type::dims), opt) {}
+
+    template <unsigned int prp, typename vector_type>
+    Expr operator()(PropRef<prp, vector_type> arg) {
+        Expr e = DcpseOperator<VerletList_type>::operator()(arg);
+        auto inner = e.nodes[0].eval;
+        e.nodes[0].eval = [inner](std::vector<std::vector<double>>& out) {
+            inner(out);
+            for (auto& x : out[1]) x = -x;
+        };
+        return e;
+    }
+};
+
 // GPU aliases of the reference (DCPSE_op.hpp:3510-3530) name the same classes
 template <typename VL> using Derivative_x_gpu = Derivative_x<VL>;
 template <typename VL> using Derivative_y_gpu = Derivative_y<VL>;
@@ -354,5 +480,14 @@ template <typename VL> using Derivative_xy_gpu = Derivative_xy<VL>;
 template <typename VL> using Laplacian_gpu = Laplacian<VL>;
 template <typename VL> using Gradient_gpu = Gradient<VL>;
 template <typename VL> using Derivative_G_gpu = Derivative_G<VL>;
+template <typename VL> using Derivative_yz_gpu = Derivative_yz<VL>;
+template <typename VL> using Derivative_xz_gpu = Derivative_xz<VL>;
+template <typename VL> using Derivative_xxx_gpu = Derivative_xxx<VL>;
+template <typename VL> using Derivative_xxy_gpu = Derivative_xxy<VL>;
+template <typename VL> using Derivative_yyx_gpu = Derivative_yyx<VL>;
+template <typename VL> using Derivative_yyy_gpu = Derivative_yyy<VL>;
+template <typename VL> using Divergence_gpu = Divergence<VL>;
+template <typename VL> using Advection_gpu = Advection<VL>;
+template <typename VL> using Curl2D_gpu = Curl2D<VL>;
 
 }  // namespace openfpm_dcpse

@@ -296,6 +296,67 @@ class Gradient(_DcpseOp):
                          kind="vector", **kw)
 
 
+class Divergence(_DcpseOp):
+    """Divergence_T (DCPSE_op.hpp:1503-1630): dim Dcpse objects e_i applied
+    to the components of a vector field and summed, VECT_DCPSE_V_DIV
+    (:446-475): div = ((0 + D_0 v_0) + D_1 v_1) + ..."""
+
+    def __init__(self, parts, verletList, ord, rCut, opt=support_options.RADIUS, **kw):
+        d = parts.dims
+        super().__init__(parts, verletList, ord, rCut, opt, outputs=[[_unit(d, i)] for i in range(d)],
+                         kind="div", **kw)
+
+    def __call__(self, v, precision="f64"):
+        if not self._assembled:
+            raise RuntimeError("operator not assembled (support_options.LOAD without update)")
+        v = v.to(device="cuda", dtype=torch.float64)
+        out = torch.zeros(v.shape[0], dtype=torch.float64, device=v.device)
+        for i in range(self.dim):
+            out = out + self._component(i, v[:, i].contiguous(), precision)
+        return out
+
+    def _component(self, i, f, precision):
+        if precision == "f64":
+            return self.plan.apply_output_f64(i, f)
+        if precision in ("f32", "f64-batched"):
+            return self.plan.apply(f, C.F32 if precision == "f32" else C.F64)[i]
+        raise ValueError("precision must be 'f64', 'f64-batched' or 'f32'")
+
+
+class Advection(Divergence):
+    """Advection_T (DCPSE_op.hpp:1632-1781): (v . grad) f with dim Dcpse
+    objects e_i, VECT_DCPSE_V_DOT (:531-565): adv = ((0 + v_0 D_0 f) +
+    v_1 D_1 f) + ...; f may be a vector field [n, m] (component-wise)."""
+
+    def __call__(self, v, f, precision="f64"):
+        if not self._assembled:
+            raise RuntimeError("operator not assembled (support_options.LOAD without update)")
+        v = v.to(device="cuda", dtype=torch.float64)
+        f = f.to(device="cuda", dtype=torch.float64)
+        cols = [f] if f.dim() == 1 else [f[:, c].contiguous() for c in range(f.shape[1])]
+        res = []
+        for fc in cols:
+            out = torch.zeros(v.shape[0], dtype=torch.float64, device=v.device)
+            for i in range(self.dim):
+                out = out + v[:, i] * self._component(i, fc.contiguous(), precision)
+            res.append(out)
+        return res[0] if f.dim() == 1 else torch.stack(res, 1)
+
+
+class Curl2D(_DcpseOp):
+    """Curl2D_T (DCPSE_op.hpp:1227-1340): Dcpse objects e_1 and e_0,
+    VECT_DCPSE_V_CURL2D (:206-233): (D_y f, -D_x f) as a [2, n] tensor."""
+
+    def __init__(self, parts, verletList, ord, rCut, opt=support_options.RADIUS, **kw):
+        d = parts.dims
+        super().__init__(parts, verletList, ord, rCut, opt, outputs=[[_unit(d, 1)], [_unit(d, 0)]],
+                         kind="vector", **kw)
+
+    def __call__(self, f, precision="f64"):
+        out = _DcpseOp.__call__(self, f, precision)
+        return torch.stack([out[0], -out[1]])
+
+
 class OperatorSet(_DcpseOp):
     """Several operators assembled and applied together over one neighbour
     list (one persistent assembly launch, one apply pass).  ``ops`` is a list
@@ -498,3 +559,6 @@ Derivative_x_gpu, Derivative_y_gpu, Derivative_z_gpu = Derivative_x, Derivative_
 Derivative_xx_gpu, Derivative_yy_gpu, Derivative_zz_gpu = Derivative_xx, Derivative_yy, Derivative_zz
 Derivative_xy_gpu, Derivative_yz_gpu, Derivative_xz_gpu = Derivative_xy, Derivative_yz, Derivative_xz
 Laplacian_gpu, Gradient_gpu, Derivative_G_gpu = Laplacian, Gradient, Derivative_G
+Divergence_gpu, Advection_gpu, Curl2D_gpu = Divergence, Advection, Curl2D
+Derivative_xxx_gpu, Derivative_xxy_gpu = Derivative_xxx, Derivative_xxy
+Derivative_yyx_gpu, Derivative_yyy_gpu = Derivative_yyx, Derivative_yyy

@@ -295,6 +295,53 @@ static void test_interpolation_two_sets() {
     Fx2.deallocate();
 }
 
+// DCPSE_op_test_base_tests.cpp:469-551 (Divergence) and :553-660
+// (Advection) with the C++ operators; Curl2D against Dy and -Dx
+static void test_vector_operators() {
+    const int nside = 63;
+    const double h = 10.0 / (nside - 1), rCut = 3.1 * h;
+    Parts2 domain = lattice2(nside, h);
+    for (std::size_t p = 0; p < domain.size_local(); ++p) {
+        const double x = domain.getPos(p)[0], y = domain.getPos(p)[1];
+        domain.getProp<4>(p)[0] = std::sin(x) + std::sin(y);
+        domain.getProp<4>(p)[1] = std::cos(x) + std::cos(y);
+        domain.getProp<0>(p) = std::sin(x) + std::sin(y);
+        domain.getProp<2>(p) = std::cos(x) - std::sin(y);
+    }
+    VerletList vl = getVerlet(domain, rCut);
+    Divergence<VerletList> Div(domain, vl, 2, rCut);
+    getV<1>(domain) = Div(getV<4>(domain));
+    double worst = 0;
+    for (std::size_t p = 0; p < domain.size_local(); ++p)
+        worst = std::max(worst, std::fabs(domain.getProp<1>(p) - domain.getProp<2>(p)));
+    EXPECT(worst < 0.05, "Divergence worst < 0.05");
+
+    Advection<VerletList> Adv(domain, vl, 2, rCut);
+    getV<3>(domain) = Adv(getV<4>(domain), getV<0>(domain));
+    double wa = 0;
+    for (std::size_t p = 0; p < domain.size_local(); ++p) {
+        const double x = domain.getPos(p)[0], y = domain.getPos(p)[1];
+        const double ex = std::cos(x) * (std::sin(x) + std::sin(y)) + std::cos(y) * (std::cos(x) + std::cos(y));
+        wa = std::max(wa, std::fabs(domain.getProp<3>(p) - ex));
+    }
+    EXPECT(wa < 0.1, "Advection of a scalar within second-order error");
+    getV<5>(domain) = Adv(getV<4>(domain), getV<4>(domain));
+    bool comp = true;
+    for (std::size_t p = 0; p < domain.size_local(); ++p) comp &= domain.getProp<5>(p)[0] == domain.getProp<3>(p);
+    EXPECT(comp, "Advection of a vector property is component-wise");
+
+    Curl2D<VerletList> Curl(domain, vl, 2, rCut);
+    Derivative_x<VerletList> Dx(domain, vl, 2, rCut);
+    Derivative_y<VerletList> Dy(domain, vl, 2, rCut);
+    getV<5>(domain) = Curl(getV<0>(domain));
+    getV<1>(domain) = Dy(getV<0>(domain));
+    getV<2>(domain) = Dx(getV<0>(domain));
+    bool curl = true;
+    for (std::size_t p = 0; p < domain.size_local(); ++p)
+        curl &= domain.getProp<5>(p)[0] == domain.getProp<1>(p) && domain.getProp<5>(p)[1] == -domain.getProp<2>(p);
+    EXPECT(curl, "Curl2D = (Dy f, -Dx f) bit for bit");
+}
+
 int main() {
     try {
         test_dcpse_class();
@@ -303,6 +350,7 @@ int main() {
         test_too_few();
         test_interpolation_same_set();
         test_interpolation_two_sets();
+        test_vector_operators();
     } catch (const std::exception& e) {
         std::printf("FAIL exception: %s\n", e.what());
         return 2;

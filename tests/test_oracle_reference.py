@@ -352,3 +352,34 @@ def test_surface_circle(orc):
         if r not in seen:
             seen.append(r)
     assert list(c2[rp2[p]:rp2[p + 1]]) == seen
+
+
+def test_divergence_reference_bar(orc):
+    # DCPSE_op_test_base_tests.cpp:469-551: Div(v), v = (sin x + sin y,
+    # cos x + cos y) on 63^2 over [0,10]^2, rCut 3.1h: cos x - sin y, worst < 0.05
+    h = 10.0 / 62
+    pos = _grid(63, 2, h)
+    rp, cols = orc.neighbors(pos, 3.1 * h)
+    v0 = np.sin(pos[:, 0]) + np.sin(pos[:, 1])
+    v1 = np.cos(pos[:, 0]) + np.cos(pos[:, 1])
+    dx = orc.operator(pos, rp, cols, "x")[0]
+    dy = orc.operator(pos, rp, cols, "y")[0]
+    div = (0.0 + orc.apply(v0, rp, cols, dx[3], dx[2], 1)) + orc.apply(v1, rp, cols, dy[3], dy[2], 1)
+    assert np.max(np.abs(div - (np.cos(pos[:, 0]) - np.sin(pos[:, 1])))) < 0.05
+
+
+def test_advection_reference_bar(orc):
+    # DCPSE_op_test_base_tests.cpp:553-660: Adv(v, P) = v . grad P on 321^2
+    # over [0,10]^2, rCut 3.1h, worst < 0.03
+    h = 10.0 / 320
+    pos = _grid(321, 2, h)
+    rp, cols = orc.neighbors(pos, 3.1 * h)
+    x, y = pos[:, 0], pos[:, 1]
+    P = np.sin(x) + np.sin(y)
+    v = np.stack([np.sin(x) + np.sin(y), np.cos(x) + np.cos(y)], 1)
+    ops = [orc.operator(pos, rp, cols, s, nthreads=os.cpu_count())[0] for s in ("x", "y")]
+    adv = np.zeros(len(pos))
+    for i in range(2):
+        adv = adv + v[:, i] * orc.apply(P, rp, cols, ops[i][3], ops[i][2], 1, nthreads=os.cpu_count())
+    exact = np.cos(x) * (np.sin(x) + np.sin(y)) + np.cos(y) * (np.cos(x) + np.cos(y))
+    assert np.max(np.abs(adv - exact)) < 0.03
