@@ -158,9 +158,11 @@ public:
         build(parts, opt != support_options::LOAD);
     }
 
-    // initializeUpdate of every Dcpse term (DCPSE_op.hpp:779-785)
+    // initializeUpdate of every Dcpse term (DCPSE_op.hpp:779-785); a surface
+    // operator extends the support again from the current normals
     template <typename particles_type>
     void update(particles_type& parts) {
+        if (surf_.on) surf_.normals = surf_.read_normals();
         build(parts, true);
     }
 
@@ -222,14 +224,33 @@ public:
 protected:
     detail::PlanHost* host() const { return plan_.get(); }
 
+    // surface operators (DCPSE_surface_op.hpp)
+    template <typename particles_type>
+    DcpseOperator(particles_type& parts, VerletList_type& verletList, unsigned int ord,
+                  std::vector<std::vector<std::vector<unsigned>>> outputs, support_options opt,
+                  const detail::SurfaceCfg& surf)
+        : vl_(verletList), outputs_(std::move(outputs)), ord_(ord), hoe_(0.9), dim_(particles_type::dims),
+          surf_(surf) {
+        build(parts, opt != support_options::LOAD);
+    }
+
 private:
     template <typename particles_type>
     void build(particles_type& parts, bool assemble) {
         plan_.reset(new detail::PlanHost(dim_, outputs_, ord_, hoe_));
-        plan_->set_particles(parts, vl_);
+        if (surf_.on)
+            plan_->set_surface_particles(parts, parts, false, surf_);
+        else
+            plan_->set_particles(parts, vl_);
         if (!assemble) return;
         int64_t nbad = plan_->assemble(DCPSE_STORE_TERMS_F64 | DCPSE_STORE_OUT_F32);
         detail::throw_too_few(plan_->last_fail_code(), nbad);
+        // a surface operator hands the accumulated lists back (Dcpse.hpp:1001-1005)
+        if constexpr (std::is_same<VerletList_type, VerletList>::value)
+            if (surf_.on) {
+                vl_.rowptr = plan_->rowptr();
+                vl_.cols = plan_->cols();
+            }
     }
 
     // one Dcpse file per term in Dcpse::save's layout: file + "_0" for an
@@ -277,6 +298,7 @@ private:
     unsigned ord_;
     double hoe_;
     int dim_;
+    detail::SurfaceCfg surf_;
     std::unique_ptr<detail::PlanHost> plan_;
 };
 

@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <iostream>
 #include <limits>
 #include <memory>
@@ -73,6 +74,55 @@ private:
     void* p_ = nullptr;
     std::size_t bytes_ = 0;
 };
+
+// Surface operator set-up (SurfaceDcpse, Dcpse.hpp:829-1085): unit normals
+// of the support particles, nCount virtual particles per side at spacing
+// nSpacing, and the cutoff / self option of the Verlet list handed in.
+struct SurfaceCfg {
+    bool on = false;
+    std::vector<double> normals;
+    std::function<std::vector<double>()> read_normals;  // normals of the current positions (updates)
+    int n_count = 0;
+    double spacing = 0.0;
+    double rcut = 0.0;
+    bool skip_ref = true;
+};
+
+template <typename VL>
+double list_rcut(const VL& vl, double fallback) {
+    if constexpr (std::is_same<VL, VerletList>::value)
+        return vl.rCut > 0.0 ? vl.rCut : fallback;
+    else
+        return fallback;
+}
+
+template <typename VL>
+bool list_skip_ref(const VL& vl) {
+    if constexpr (std::is_same<VL, VerletList>::value)
+        return vl.skip_ref;
+    else
+        return true;
+}
+
+template <unsigned int NORMAL_ID, typename Parts, typename VL>
+SurfaceCfg surface_cfg(Parts& sup, const VL& vl, double rCut, double nSpacing, unsigned nCount) {
+    SurfaceCfg c;
+    c.on = true;
+    Parts* ps = &sup;
+    c.read_normals = [ps]() {
+        const int dim = Parts::dims;
+        std::vector<double> nrm(ps->size_local() * dim);
+        for (std::size_t p = 0; p < ps->size_local(); ++p)
+            for (int d = 0; d < dim; ++d) nrm[p * dim + d] = (double)ps->template getProp<NORMAL_ID>(p)[d];
+        return nrm;
+    };
+    c.normals = c.read_normals();
+    c.n_count = (int)nCount;
+    c.spacing = nSpacing;
+    c.rcut = list_rcut(vl, rCut);
+    c.skip_ref = list_skip_ref(vl);
+    return c;
+}
 
 // A plan plus the host <-> device staging of positions, lists and fields.
 class PlanHost {
@@ -154,6 +204,7 @@ public:
         int rc = dcpse_assemble(plan_, (const double*)pos_.get(), nullptr, flags);
         check(rc, true);
         cache_valid_ = false;
+        if (surface_) refresh_list();
         if (rc == DCPSE_ERR_PARTICLES) {
             int64_t nb = 0, first = -1;
             int code = 0;
@@ -173,6 +224,46 @@ public:
         check(dcpse_apply_output_f64(plan_, o, (const double*)fd_.get(), (double*)od_.get()));
         od_.download(out, (std::size_t)n_ * sizeof(double));
     }
+    // surface operator: the device builds the lists over the support
+    // extended along the normals and accumulates them at assembly
+    template <typename Sup, typename Dom>
+    void set_surface_particles(Sup& sup, Dom& dom, bool two_set, const SurfaceCfg& c) {
+        n_ = (int64_t)dom.size_local();
+        n_sup_ = two_set ? (int64_t)sup.size_local() : n_;
+        std::vector<double> pos((std::size_t)n_ * dim_);
+        for (int64_t p = 0; p < n_; ++p)
+            for (int d = 0; d < dim_; ++d) pos[(std::size_t)p * dim_ + d] = (double)dom.getPos(p)[d];
+        pos_.upload(pos.data(), std::max<std::size_t>(pos.size(), 1) * sizeof(double));
+        if (two_set) {
+            std::vector<double> sp((std::size_t)n_sup_ * dim_);
+            for (int64_t q = 0; q < n_sup_; ++q)
+                for (int d = 0; d < dim_; ++d) sp[(std::size_t)q * dim_ + d] = (double)sup.getPos(q)[d];
+            spos_.upload(sp.data(), std::max<std::size_t>(sp.size(), 1) * sizeof(double));
+        }
+        nrm_.upload(c.normals.data(), std::max<std::size_t>(c.normals.size(), 1) * sizeof(double));
+        check(dcpse_plan_set_support(plan_, two_set ? (const double*)spos_.get() : nullptr, two_set ? n_sup_ : 0,
+                                     c.skip_ref ? 1 : 0));
+        check(dcpse_plan_set_surface(plan_, (const double*)nrm_.get(), c.n_count, c.spacing, nullptr));
+        check(dcpse_build_neighbors(plan_, (const double*)pos_.get(), n_, c.rcut, nullptr));
+        surface_ = true;
+        cache_valid_ = false;
+    }
+    bool surface() const { return surface_; }
+
+    // host copy of the plan's neighbour list (after a surface assembly it
+    // holds the accumulated lists)
+    void refresh_list() {
+        int64_t nn = 0, nnz = 0;
+        check(dcpse_plan_info(plan_, &nn, &nnz, nullptr, nullptr, nullptr));
+        const int64_t* drp = nullptr;
+        const int32_t* dcl = nullptr;
+        check(dcpse_neighbors_ptr(plan_, &drp, &dcl));
+        rowptr_.resize((std::size_t)nn + 1);
+        cols_.resize((std::size_t)nnz);
+        check(dcpse_copy(rowptr_.data(), drp, (std::size_t)(nn + 1) * sizeof(int64_t)));
+        if (nnz > 0) check(dcpse_copy(cols_.data(), dcl, (std::size_t)nnz * sizeof(int32_t)));
+    }
+
     // Dcpse::p2p of term t: f is [n_support][ncomp], out [n][ncomp]
     void p2p(int t, const double* f, int ncomp, double* out) {
         fd_.upload(f, (std::size_t)std::max<int64_t>(n_sup_ * ncomp, 1) * sizeof(double));
@@ -247,7 +338,8 @@ private:
     std::vector<unsigned> term_order_;
     std::vector<int64_t> rowptr_;
     std::vector<int32_t> cols_;
-    DevBuf pos_, spos_, fd_, od_;
+    DevBuf pos_, spos_, nrm_, fd_, od_;
+    bool surface_ = false;
     bool cache_valid_ = false;
     std::vector<std::vector<double>> K_, eip_;
     std::vector<double> eps_;
@@ -353,12 +445,14 @@ inline VerletList build_verlet(int dim, const std::vector<double>& dom, const st
         check(dcpse_plan_set_support(plan, nullptr, 0, skip_ref ? 1 : 0));
     }
     check(dcpse_build_neighbors(plan, (const double*)dpos.get(), n, rCut, nullptr));
+    VerletList vl;
+    vl.rCut = rCut;
+    vl.skip_ref = skip_ref && !sup;
     int64_t nn = 0, nnz = 0;
     check(dcpse_plan_info(plan, &nn, &nnz, nullptr, nullptr, nullptr));
     const int64_t* drp = nullptr;
     const int32_t* dcl = nullptr;
     check(dcpse_neighbors_ptr(plan, &drp, &dcl));
-    VerletList vl;
     vl.rowptr.resize((std::size_t)n + 1);
     vl.cols.resize((std::size_t)nnz);
     check(dcpse_copy(vl.rowptr.data(), drp, (std::size_t)(n + 1) * sizeof(int64_t)));
@@ -393,6 +487,8 @@ public:
     // c = HOverEpsilon: eps = <h> / c, <h> the mean L1 spacing of the support
     // (Dcpse.hpp:80; read at construction and at update)
     T HOverEpsilon = 0.9;
+
+    virtual ~Dcpse() = default;
 
     template <typename Sig>
     Dcpse(vector_type& particles, VerletList_type& verletList, const Sig& differentialSignature,
@@ -436,6 +532,29 @@ public:
         assemble();
     }
 
+protected:
+    // surface operators (SurfaceDcpse below)
+    template <typename Sig>
+    Dcpse(vector_type& particlesSupport, vector_type2& particlesDomain, VerletList_type& verletList,
+          const Sig& differentialSignature, unsigned int convergenceOrder, T rCut, support_options opt,
+          const detail::SurfaceCfg& surface)
+        : verletList_(verletList),
+          sig_(detail::sig_vector(differentialSignature, dim)),
+          convergenceOrder_(convergenceOrder),
+          rCut_(rCut),
+          opt_(opt),
+          surface_(surface) {
+        differentialOrder_ = 0;
+        for (unsigned s : sig_) differentialOrder_ += s;
+        support_ = &particlesSupport;
+        domain_ = &particlesDomain;
+        plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder, (double)HOverEpsilon));
+        set_sets();
+        if (opt == support_options::LOAD) return;
+        assemble();
+    }
+
+public:
     // Particle to particle interpolation (Dcpse.hpp:198-227): property prp2
     // of every domain particle = epsInvPow_p * sum_q f_q K_pq, f = property
     // prp1 of the support particles.
@@ -504,13 +623,19 @@ public:
         support_ = &particles;
         domain_ = same_set(particles);
         plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder_, (double)HOverEpsilon));
-        plan_->set_particles(particles, verletList_);
+        if (surface_.on) {
+            surface_.normals = surface_.read_normals();
+            set_sets();
+        } else {
+            plan_->set_particles(particles, verletList_);
+        }
         assemble();
     }
     void initializeUpdate(vector_type& particlesSupport, vector_type2& particlesDomain) {
         support_ = &particlesSupport;
         domain_ = &particlesDomain;
         plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder_, (double)HOverEpsilon));
+        if (surface_.on) surface_.normals = surface_.read_normals();
         set_sets();
         assemble();
     }
@@ -593,6 +718,13 @@ private:
     void assemble() {
         int64_t nbad = plan_->assemble(DCPSE_STORE_TERMS_F64);
         detail::throw_too_few(plan_->last_fail_code(), nbad);
+        // a surface operator replaces the caller's lists with the
+        // accumulated ones, as the reference does (Dcpse.hpp:1001-1005)
+        if constexpr (std::is_same<VerletList_type, VerletList>::value)
+            if (surface_.on) {
+                verletList_.rowptr = plan_->rowptr();
+                verletList_.cols = plan_->cols();
+            }
     }
 
     // the domain set of a one-set operator is the support set itself
@@ -606,7 +738,10 @@ private:
     // one set when both references name the same object
     void set_sets() {
         const bool two = (const void*)support_ != (const void*)domain_;
-        plan_->set_particles(*support_, *domain_, verletList_, two);
+        if (surface_.on)
+            plan_->set_surface_particles(*support_, *domain_, two, surface_);
+        else
+            plan_->set_particles(*support_, *domain_, verletList_, two);
     }
 
     vector_type* support_ = nullptr;
@@ -617,7 +752,29 @@ private:
     unsigned convergenceOrder_;
     T rCut_;
     support_options opt_;
+    detail::SurfaceCfg surface_;
     std::unique_ptr<detail::PlanHost> plan_;
+};
+
+// SurfaceDcpse (Dcpse.hpp:829-1085): the support of every particle is
+// extended by nCount virtual particles on each side along the normal
+// (property NORMAL_ID of the support set), the kernels are assembled on the
+// extended support and every virtual particle's kernel is added onto its
+// surface particle.  The Verlet list handed in gives the cutoff and whether
+// a particle is its own neighbour, and receives the accumulated lists.
+// support_options::ADAPTIVE (per-particle spacings) is not provided here.
+template <unsigned int dim, typename VerletList_type, typename vector_type, typename vector_type2 = vector_type>
+class SurfaceDcpse : public Dcpse<dim, VerletList_type, vector_type, vector_type2> {
+    typedef Dcpse<dim, VerletList_type, vector_type, vector_type2> base;
+
+public:
+    template <typename Sig, unsigned int NORMAL_ID>
+    SurfaceDcpse(vector_type& particlesSupport, vector_type2& particlesDomain, VerletList_type& verletList,
+                 const Sig& differentialSignature, unsigned int convergenceOrder, typename base::T rCut,
+                 typename base::T nSpacing, unsigned int nCount, value_t<NORMAL_ID>,
+                 support_options opt = support_options::RADIUS)
+        : base(particlesSupport, particlesDomain, verletList, differentialSignature, convergenceOrder, rCut, opt,
+               detail::surface_cfg<NORMAL_ID>(particlesSupport, verletList, (double)rCut, (double)nSpacing, nCount)) {}
 };
 
 }  // namespace openfpm_dcpse

@@ -9,8 +9,9 @@
 // The operator is a Dcpse with the zero signature on two particle sets
 // (Dcpse.hpp:113-131); p2p evaluates epsInvPow_p * sum_q f_q K_pq on the GPU
 // in the reference's operation order (dcpse_p2p_f64).  The surface form
-// (the constructor taking nSpacing and isSurfaceInterpolation) needs
-// SurfaceDcpse and is not provided.
+// (the constructor taking nSpacing and isSurfaceInterpolation) builds a
+// SurfaceDcpse over the support set extended along its normals (property
+// NORMAL_ID) with nCount = rCut / nSpacing virtual particles per side.
 #pragma once
 
 #include <climits>
@@ -49,6 +50,24 @@ public:
         Point<particlesSupport_type::dims, unsigned int> p;
         p.zero();
         dcpse_ = new dcpse_type(particlesSupport, particlesDomain, verletList, p, ord, rCut, opt);
+    }
+
+    // surface interpolation (DcpseInterpolation.hpp:94-113)
+    PPInterpolation(particlesSupport_type& particlesSupport, particlesDomain_type& particlesDomain,
+                    VerletList_type& verletList, unsigned int ord, typename particlesSupport_type::stype rCut,
+                    typename particlesSupport_type::stype nSpacing, bool isSurfaceInterpolation,
+                    support_options opt = support_options::RADIUS)
+        : particlesSupport_(particlesSupport), particlesDomain_(particlesDomain) {
+        Point<particlesSupport_type::dims, unsigned int> p;
+        p.zero();
+        if (!isSurfaceInterpolation) {
+            dcpse_ = new dcpse_type(particlesSupport, particlesDomain, verletList, p, ord, rCut, opt);
+            return;
+        }
+        typedef SurfaceDcpse<particlesSupport_type::dims, VerletList_type, particlesSupport_type, particlesDomain_type>
+            surface_type;
+        dcpse_ = new surface_type(particlesSupport, particlesDomain, verletList, p, ord, rCut, nSpacing,
+                                  static_cast<unsigned int>(rCut / nSpacing), value_t<NORMAL_ID>(), opt);
     }
 
     // p2p<propSupport, propDomain>() (DcpseInterpolation.hpp:133-137)

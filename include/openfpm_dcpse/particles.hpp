@@ -104,6 +104,8 @@ class VerletList {
 public:
     std::vector<int64_t> rowptr{0};
     std::vector<int32_t> cols;
+    double rCut = 0.0;        // cutoff the list was built with
+    bool skip_ref = true;     // VL_SKIP_REF_PART: a particle is not its own neighbour
 
     std::size_t getNNPart(std::size_t p) const { return (std::size_t)(rowptr[p + 1] - rowptr[p]); }
     std::size_t getNNPart(vect_dist_key_dx p) const { return getNNPart(p.getKey()); }
@@ -111,5 +113,10 @@ public:
     std::size_t get(vect_dist_key_dx p, std::size_t j) const { return get(p.getKey(), j); }
     std::size_t size() const { return rowptr.size() - 1; }
 };
+
+// openfpm's value_t<i>: a tag naming property i (here the property that
+// holds the unit normals of a surface operator)
+template <unsigned int i>
+struct value_t {};
 
 }  // namespace openfpm_dcpse

@@ -15,6 +15,7 @@
 
 #include "openfpm_dcpse/DCPSE_op.hpp"
 #include "openfpm_dcpse/DcpseInterpolation.hpp"
+#include "openfpm_dcpse/DCPSE_surface_op.hpp"
 
 using namespace openfpm_dcpse;
 
@@ -342,6 +343,51 @@ static void test_vector_operators() {
     EXPECT(curl, "Curl2D = (Dy f, -Dx f) bit for bit");
 }
 
+// DCPSE_op_Surface_tests.cpp:97-182 (dcpse_surface_circle): SDxx + SDyy of
+// sin(theta) on 512 particles of the unit circle, normals in property 4,
+// rCut = 5.1 h, nCount = 5; worst < 0.03.  The same Verlet list object serves
+// both operators (its cutoff is what they read) and ends up accumulated.
+static void test_surface_operators() {
+    const int n = 512;
+    const double h = 3.0 / 511, rCut = 5.1 * h;
+    Parts2 s(n);
+    for (int i = 0; i < n; ++i) {
+        const double th = i * (2 * M_PI / n);
+        s.getPos(i)[0] = std::cos(th);
+        s.getPos(i)[1] = std::sin(th);
+        s.getProp<4>(i)[0] = std::cos(th);
+        s.getProp<4>(i)[1] = std::sin(th);
+        s.getProp<3>(i) = std::sin(th);
+        s.getProp<1>(i) = -std::sin(th);
+    }
+    VerletList vl = getVerlet(s, rCut);
+    const std::size_t k0 = vl.cols.size();
+    SurfaceDerivative_xx<4, VerletList> SDxx(s, vl, 2, rCut, h, (unsigned)(rCut / h));
+    SurfaceDerivative_yy<4, VerletList> SDyy(s, vl, 2, rCut, h, (unsigned)(rCut / h));
+    getV<0>(s) = SDxx(getV<3>(s)) + SDyy(getV<3>(s));
+    double worst = 0;
+    for (int i = 0; i < n; ++i) worst = std::max(worst, std::fabs(s.getProp<0>(i) - s.getProp<1>(i)));
+    EXPECT(worst < 0.03, "surface SDxx + SDyy on the circle worst < 0.03");
+    bool listed = vl.cols.size() <= k0 + (std::size_t)n && vl.rowptr.size() == (std::size_t)n + 1;
+    for (int32_t c : vl.cols) listed &= c >= 0 && c < n;
+    EXPECT(listed, "surface operators hand back the accumulated lists over the surface particles");
+
+    // surface interpolation from the circle onto a rotated copy of it
+    Parts2 t(n);
+    for (int i = 0; i < n; ++i) {
+        const double th = (i + 0.5) * (2 * M_PI / n);
+        t.getPos(i)[0] = std::cos(th);
+        t.getPos(i)[1] = std::sin(th);
+    }
+    VerletList vl2 = createVerletTwoPhase(t, s, rCut);
+    PPInterpolation<Parts2, Parts2, VerletList, 4> pp(s, t, vl2, 2, rCut, h, true);
+    pp.p2p<3, 0>();
+    double wi = 0;
+    for (int i = 0; i < n; ++i) wi = std::max(wi, std::fabs(t.getProp<0>(i) - std::sin((i + 0.5) * (2 * M_PI / n))));
+    EXPECT(wi < 1e-3, "surface interpolation on the circle");
+    pp.deallocate();
+}
+
 int main() {
     try {
         test_dcpse_class();
@@ -351,6 +397,7 @@ int main() {
         test_interpolation_same_set();
         test_interpolation_two_sets();
         test_vector_operators();
+        test_surface_operators();
     } catch (const std::exception& e) {
         std::printf("FAIL exception: %s\n", e.what());
         return 2;
