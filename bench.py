@@ -436,6 +436,8 @@ def run_gray_scott(args):
     with torch.cuda.stream(s):
         plan.build_neighbors(pos, cfg["rcut"])
         plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
+        if args.lanes:
+            plan.set_apply_config(args.lanes, 1)
         u0, v0 = W.gray_scott_initial(cfg["pos"])
         u = torch.tensor(u0, device="cuda", dtype=torch.float32)
         v = torch.tensor(v0, device="cuda", dtype=torch.float32)
@@ -466,8 +468,18 @@ def run_gray_scott(args):
         ev1.record(s)
     s.synchronize()
     t_bwd = ev0.elapsed_time(ev1)
-    res = {"only": "gray-scott", "particles": pos.shape[0], "nnz": plan.info()["nnz"], "steps": total,
-           "ms_per_step_graph": t_fwd, "backward_window_steps": window, "checkpoint_every": every,
+    nnz = plan.info()["nnz"]
+    n = pos.shape[0]
+    # per stage: row offsets, columns and FP32 weights once, the stage input
+    # (2 species, gathered from L2), the step's start state, the accumulator
+    # (read and written), the stage output
+    step_bytes = 4 * (8 * (n + 1) + 8 * nnz + 8 * n + 8 * n + 16 * n + 8 * n)
+    hbm, peak_kind = peaks()
+    res = {"only": "gray-scott", "particles": n, "nnz": nnz, "steps": total,
+           "ms_per_step_graph": t_fwd,
+           "roofline": {"bound": "hbm", "algorithmic_bytes_per_step": step_bytes,
+                        "achieved_gbs": step_bytes / t_fwd / 1e6, "peak_gbs": hbm,
+                        "frac": step_bytes / t_fwd / 1e6 / hbm, "peak_source": peak_kind}, "backward_window_steps": window, "checkpoint_every": every,
            "backward_ms": t_bwd, "backward_ms_per_step": t_bwd / window,
            "v_final_mean": float(gs.v.mean()), "grad_v_norm": float(vb.norm()),
            "finite": bool(torch.isfinite(gs.v).all() and torch.isfinite(vb).all())}

@@ -268,6 +268,7 @@ struct RkArgs {
     T *outu, *outv;                 // next stage input, or the new state
     double Du, Dv, F, K, dt;
     int stage;                      // 0..3
+    void* pack;                     // scratch [n] of (u, v) pairs (float2 / double2) for the gathers
 };
 template <typename T>
 struct RkAdjArgs {

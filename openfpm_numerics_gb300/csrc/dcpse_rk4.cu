@@ -35,8 +35,34 @@ __device__ __forceinline__ double tfma<double>(double a, double b, double c) {
     return fma(a, b, c);
 }
 
+// the two species of the stage input side by side, so a neighbour's pair
+// is one 8-byte (FP32) or 16-byte (FP64) gather instead of two
+template <typename T>
+struct Pair;
+template <>
+struct Pair<float> {
+    typedef float2 type;
+};
+template <>
+struct Pair<double> {
+    typedef double2 type;
+};
+
+template <typename T>
+__global__ void pack_kernel(const T* __restrict__ u, const T* __restrict__ v, int64_t n,
+                            typename Pair<T>::type* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        typename Pair<T>::type p;
+        p.x = u[i];
+        p.y = v[i];
+        out[i] = p;
+    }
+}
+
 template <typename T, int G>
 __global__ void __launch_bounds__(256) gs_stage_kernel(RkArgs<T> a) {
+    typedef typename Pair<T>::type P2;
+    const P2* __restrict__ Y2 = static_cast<const P2*>(a.pack);
     const int lane = threadIdx.x & 31;
     const int sub = lane & (G - 1);
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -51,13 +77,29 @@ __global__ void __launch_bounds__(256) gs_stage_kernel(RkArgs<T> a) {
             vp = a.Yv[row];
             const int64_t rb = a.rowptr[row];
             const int k = (int)(a.rowptr[row + 1] - rb);
-            const int32_t* c = a.cols + rb;
-            const T* w = a.w + rb;
-            for (int j = sub; j < k; j += G) {
-                const int32_t q = c[j];
-                const T wq = w[j];
-                lu = tfma<T>(wq, a.Yu[q] - up, lu);
-                lv = tfma<T>(wq, a.Yv[q] - vp, lv);
+            const int32_t* __restrict__ c = a.cols + rb;
+            const T* __restrict__ w = a.w + rb;
+            // U entries per lane in flight: every load of a batch is issued
+            // before its arithmetic; entries past the row end gather the row's
+            // own values with weight 0
+            constexpr int U = 4;
+            for (int j0 = sub; j0 < k; j0 += G * U) {
+                int32_t q[U];
+                T wq[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int j = j0 + u * G;
+                    q[u] = j < k ? c[j] : (int32_t)row;
+                    wq[u] = j < k ? w[j] : (T)0;
+                }
+                P2 y[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) y[u] = Y2[q[u]];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    lu = tfma<T>(wq[u], y[u].x - up, lu);
+                    lv = tfma<T>(wq[u], y[u].y - vp, lv);
+                }
             }
         }
 #pragma unroll
@@ -152,6 +194,7 @@ int grid_n(int64_t items, int per_block) {
 template <typename T>
 cudaError_t rk_stage(const RkArgs<T>& a, int lanes, cudaStream_t s) {
     if (a.n == 0) return cudaSuccess;
+    pack_kernel<T><<<grid_n(a.n, 256), 256, 0, s>>>(a.Yu, a.Yv, a.n, static_cast<typename Pair<T>::type*>(a.pack));
     switch (lanes) {
         case 4: gs_stage_kernel<T, 4><<<grid_n(a.n, 64), 256, 0, s>>>(a); break;
         case 8: gs_stage_kernel<T, 8><<<grid_n(a.n, 32), 256, 0, s>>>(a); break;
