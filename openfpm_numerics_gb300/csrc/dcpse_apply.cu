@@ -147,6 +147,7 @@ struct F32Args {
     const float2* f2;
     double* out;                    // output o of row r at out[o * oos + r * ors]
     int64_t oos, ors;
+    int64_t row0;                   // rows [row0, n) (direct kernel)
     uint32_t comp;                  // outputs that take the compensated sum
     int no_self;                    // interpolation: no f_p term, f2 indexed by the support set
 };
@@ -189,7 +190,7 @@ __global__ void __launch_bounds__(256) apply_f32_kernel(F32Args a) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t rows_per_pass = ((int64_t)gridDim.x * blockDim.x) / G;
     const int64_t first = (tid - lane) / G;
-    for (int64_t base = first; base < a.n; base += rows_per_pass) {
+    for (int64_t base = a.row0 + first; base < a.n; base += rows_per_pass) {
         const int64_t row = base + lane / G;
         RowAcc<NO, RESID> acc;
         acc.init();
@@ -452,7 +453,7 @@ int lanes_for_f32(int64_t n, int64_t nnz) {
 
 template <int G, int NO, bool RESID, int U>
 cudaError_t launch_f32_direct(const F32Args& a, cudaStream_t s) {
-    apply_f32_kernel<G, NO, RESID, U><<<grid_rows(a.n, 256 / G), 256, 0, s>>>(a);
+    apply_f32_kernel<G, NO, RESID, U><<<grid_rows(a.n - a.row0, 256 / G), 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -576,7 +577,11 @@ cudaError_t p2p_f64(int64_t n, const int64_t* rowptr, const int32_t* cols, const
 cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s) {
     if (p.n == 0) return cudaSuccess;
     F32Args a{};
-    a.n = p.n;
+    a.n = p.row1 ? p.row1 : p.n;
+    a.row0 = p.row0;
+    if (a.row0 >= a.n) return cudaSuccess;
+    // the staged kernel tiles whole lists: row ranges take the direct kernel
+    if ((a.row0 != 0 || a.n != p.n) && p.mode == 2) return cudaErrorInvalidValue;
     a.rowptr = p.rowptr;
     a.cols = p.cols;
     a.w = p.w;

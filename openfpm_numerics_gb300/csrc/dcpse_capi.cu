@@ -259,6 +259,9 @@ struct dcpse_plan_s {
     // apply scratch
     float2* f2 = nullptr;
     int64_t f2_len = 0;
+    // host-buffer applies: output copies overlap the apply of later rows
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t chunk_ev[8] = {};
     double* hf = nullptr;    // device copy of a host field (host apply)
     double* hout = nullptr;  // device output for host apply
 
@@ -293,6 +296,15 @@ struct dcpse_plan_s {
         asm_scratch_bytes = 0;
         dfree(rk_pack);
         rk_pack_n = 0;
+        if (copy_stream) {
+            cudaStreamSynchronize(copy_stream);
+            for (auto& ev : chunk_ev) {
+                if (ev) cudaEventDestroy(ev);
+                ev = nullptr;
+            }
+            cudaStreamDestroy(copy_stream);
+            copy_stream = nullptr;
+        }
         dfree(surf_ext);
         dfree(dtab);
         delete htab;
@@ -1410,48 +1422,69 @@ int dcpse_apply_output_f64(dcpse_plan_t* P, int output, const double* d_f, doubl
     return DCPSE_OK;
 }
 
+namespace {
+// The FP32 batched apply of rows [r0, r1) (0, 0: all rows) from the plan's
+// split field into d_out ([n_outputs][n]).
+int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, int64_t r1) {
+    ApplyF32 ap{};
+    ap.n = P->n;
+    ap.nout = P->nout;
+    ap.rowptr = P->rowptr;
+    ap.cols = P->cols;
+    ap.w = P->w32;
+    ap.resid = (precision == DCPSE_F32_RESID) ? P->r16 : nullptr;
+    ap.ws = P->nnz;
+    ap.nnz = P->nnz;
+    ap.maxk = P->maxk;
+    ap.f2 = P->f2;
+    ap.out = d_out;
+    ap.err = P->d_err;
+    ap.mode = P->apply_mode & 15;
+    ap.lanes = P->apply_lanes;
+    ap.row0 = r0;
+    ap.row1 = r1;
+    // compensated sums for outputs with a term of order >= 2 (their
+    // first-order contributions cancel), or for all outputs on request
+    ap.comp = 0;
+    for (int t = 0; t < P->nterms; ++t) {
+        unsigned ord = 0;
+        for (int d = 0; d < P->dim; ++d) ord += P->sigs[t][d];
+        if (ord >= 2) ap.comp |= 1u << P->term_output[t];
+    }
+    // the residual correction only pays off with compensated sums
+    if ((P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) || precision == DCPSE_F32_RESID) ap.comp = 0xffffffffu;
+    P->tstart(DCPSE_K_APPLY_BATCHED);
+    cudaError_t e = apply_batched_f32x(ap, P->stream);
+    P->tstop(DCPSE_K_APPLY_BATCHED);
+    if (e == cudaErrorInvalidConfiguration && (P->apply_mode & 15) == 2)
+        return fail(DCPSE_ERR_CAPACITY, "TMA-staged tiles of this plan do not fit in shared memory "
+                                        "(fewer lanes per row or another mode)");
+    DCPSE_CK(e);
+    return DCPSE_OK;
+}
+
+int check_f32_weights(dcpse_plan_t* P, int precision) {
+    if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
+    if (precision == DCPSE_F32_RESID && !P->r16)
+        return fail(DCPSE_ERR_STATE, "FP32 residuals not stored (DCPSE_STORE_OUT_F32_RESID)");
+    return DCPSE_OK;
+}
+
+// Host-buffer applies copy the outputs back in this many row chunks on a
+// second stream, each chunk's copy overlapping the next chunk's apply.
+constexpr int kHostChunks = 8;
+constexpr int64_t kHostChunkMinRows = 65536;
+}  // namespace
+
 int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int precision) {
     if (int rc = check_plan(P)) return rc;
     if (int rc = check_single_set(P)) return rc;
     if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
     if (P->n > 0 && (!d_f || !d_out)) return fail(DCPSE_ERR_ARG, "NULL field");
     if (precision == DCPSE_F32 || precision == DCPSE_F32_RESID) {
-        if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
-        if (precision == DCPSE_F32_RESID && !P->r16)
-            return fail(DCPSE_ERR_STATE, "FP32 residuals not stored (DCPSE_STORE_OUT_F32_RESID)");
+        if (int rc = check_f32_weights(P, precision)) return rc;
         if (int rc = split_into_plan(P, d_f, P->n, 1)) return rc;
-        ApplyF32 ap{};
-        ap.n = P->n;
-        ap.nout = P->nout;
-        ap.rowptr = P->rowptr;
-        ap.cols = P->cols;
-        ap.w = P->w32;
-        ap.resid = (precision == DCPSE_F32_RESID) ? P->r16 : nullptr;
-        ap.ws = P->nnz;
-        ap.nnz = P->nnz;
-        ap.maxk = P->maxk;
-        ap.f2 = P->f2;
-        ap.out = d_out;
-        ap.err = P->d_err;
-        ap.mode = P->apply_mode & 15;
-        ap.lanes = P->apply_lanes;
-        // compensated sums for outputs with a term of order >= 2 (their
-        // first-order contributions cancel), or for all outputs on request
-        ap.comp = 0;
-        for (int t = 0; t < P->nterms; ++t) {
-            unsigned ord = 0;
-            for (int d = 0; d < P->dim; ++d) ord += P->sigs[t][d];
-            if (ord >= 2) ap.comp |= 1u << P->term_output[t];
-        }
-        // the residual correction only pays off with compensated sums
-        if ((P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) || precision == DCPSE_F32_RESID) ap.comp = 0xffffffffu;
-        P->tstart(DCPSE_K_APPLY_BATCHED);
-        cudaError_t e = apply_batched_f32x(ap, P->stream);
-        P->tstop(DCPSE_K_APPLY_BATCHED);
-        if (e == cudaErrorInvalidConfiguration && (P->apply_mode & 15) == 2)
-            return fail(DCPSE_ERR_CAPACITY, "TMA-staged tiles of this plan do not fit in shared memory "
-                                            "(fewer lanes per row or another mode)");
-        DCPSE_CK(e);
+        return apply_f32_rows(P, precision, d_out, 0, 0);
     } else if (precision == DCPSE_F64) {
         if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
         P->tstart(DCPSE_K_APPLY_BATCHED);
@@ -1472,9 +1505,44 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
     if (!P->hf) DCPSE_CK(dalloc(&P->hf, P->n));
     if (!P->hout) DCPSE_CK(dalloc(&P->hout, (size_t)P->nout * P->n));
     DCPSE_CK(cudaMemcpyAsync(P->hf, h_f, sizeof(double) * P->n, cudaMemcpyHostToDevice, P->stream));
-    int rc = dcpse_apply_batched(P, P->hf, P->hout, precision);
-    if (rc != DCPSE_OK) return rc;
-    DCPSE_CK(cudaMemcpyAsync(h_out, P->hout, sizeof(double) * P->nout * P->n, cudaMemcpyDeviceToHost, P->stream));
+    const bool f32 = precision == DCPSE_F32 || precision == DCPSE_F32_RESID;
+    if (!f32 || (P->apply_mode & 15) == 2 || P->n < kHostChunkMinRows) {
+        int rc = dcpse_apply_batched(P, P->hf, P->hout, precision);
+        if (rc != DCPSE_OK) return rc;
+        DCPSE_CK(cudaMemcpyAsync(h_out, P->hout, sizeof(double) * P->nout * P->n, cudaMemcpyDeviceToHost,
+                                 P->stream));
+        return dcpse_plan_check(P);
+    }
+    // rows in chunks: the outputs of chunk c go back on the copy stream while
+    // chunk c + 1 is applied
+    if (int rc = check_f32_weights(P, precision)) return rc;
+    if (!P->copy_stream) {
+        DCPSE_CK(cudaStreamCreateWithFlags(&P->copy_stream, cudaStreamNonBlocking));
+        for (int c = 0; c < kHostChunks; ++c) {
+            cudaError_t e = cudaEventCreateWithFlags(&P->chunk_ev[c], cudaEventDisableTiming);
+            if (e != cudaSuccess) {
+                for (int d = 0; d < c; ++d) cudaEventDestroy(P->chunk_ev[d]);
+                cudaStreamDestroy(P->copy_stream);
+                P->copy_stream = nullptr;
+                return fail(DCPSE_ERR_CUDA, cudaGetErrorString(e));
+            }
+        }
+    }
+    if (int rc = split_into_plan(P, P->hf, P->n, 1)) return rc;
+    const int64_t n = P->n;
+    for (int c = 0; c < kHostChunks; ++c) {
+        const int64_t r0 = n * c / kHostChunks, r1 = n * (c + 1) / kHostChunks;
+        if (int rc = apply_f32_rows(P, precision, P->hout, r0, r1)) {
+            cudaStreamSynchronize(P->copy_stream);
+            return rc;
+        }
+        DCPSE_CK(cudaEventRecord(P->chunk_ev[c], P->stream));
+        DCPSE_CK(cudaStreamWaitEvent(P->copy_stream, P->chunk_ev[c], 0));
+        for (int o = 0; o < P->nout; ++o)
+            DCPSE_CK(cudaMemcpyAsync(h_out + (size_t)o * n + r0, P->hout + (size_t)o * n + r0,
+                                     sizeof(double) * (size_t)(r1 - r0), cudaMemcpyDeviceToHost, P->copy_stream));
+    }
+    DCPSE_CK(cudaStreamSynchronize(P->copy_stream));
     return dcpse_plan_check(P);
 }
 

@@ -177,6 +177,7 @@ struct ApplyF32 {
     uint32_t comp;         // outputs taking the compensated FP32 sum (bit per output)
     int no_self;           // interpolation: sum w f_q without the f_p term; f2 on the support set
     int64_t oos, ors;      // output o of row r at out[o * oos + r * ors] (0: n and 1)
+    int64_t row0, row1;    // rows [row0, row1) (0, 0: all; a row range needs a direct mode)
 };
 cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s);
 cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const double* w,
