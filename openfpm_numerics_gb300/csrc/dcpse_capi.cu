@@ -107,6 +107,19 @@ __global__ void index_check_kernel(const int64_t* idx, int64_t m, int64_t n, uns
         if (idx[i] < 0 || idx[i] >= n) atomicAdd(bad, 1ull);
 }
 
+// largest field index each row chunk reads (its neighbours and itself);
+// chunk c holds rows [n c / nch, n (c + 1) / nch)
+__global__ void chunk_reach_kernel(const int64_t* rowptr, const int32_t* cols, int64_t n, int nch,
+                                   unsigned long long* reach) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        int c = 0;
+        while (c + 1 < nch && n * (c + 1) / nch <= r) ++c;
+        int64_t m = r;
+        for (int64_t j = rowptr[r]; j < rowptr[r + 1]; ++j) m = max(m, (int64_t)cols[j]);
+        atomicMax(&reach[c], (unsigned long long)m);
+    }
+}
+
 __global__ void row_max_kernel(const int64_t* rowptr, int64_t n, int* maxk) {
     int m = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -259,9 +272,15 @@ struct dcpse_plan_s {
     // apply scratch
     float2* f2 = nullptr;
     int64_t f2_len = 0;
-    // host-buffer applies: output copies overlap the apply of later rows
-    cudaStream_t copy_stream = nullptr;
+    // host-buffer applies: the field arrives in pieces on h2d_stream, row
+    // chunks start once the pieces they read have arrived, and their outputs
+    // go back on copy_stream while later chunks run
+    cudaStream_t copy_stream = nullptr, h2d_stream = nullptr;
     cudaEvent_t chunk_ev[8] = {};
+    cudaEvent_t piece_ev[8] = {};
+    int64_t chunk_reach[8] = {};
+    int64_t list_version = 0;            // bumped whenever the neighbour list changes
+    int64_t reach_version = -1;          // list version the reaches were computed for
     double* hf = nullptr;    // device copy of a host field (host apply)
     double* hout = nullptr;  // device output for host apply
 
@@ -298,13 +317,18 @@ struct dcpse_plan_s {
         rk_pack_n = 0;
         if (copy_stream) {
             cudaStreamSynchronize(copy_stream);
-            for (auto& ev : chunk_ev) {
-                if (ev) cudaEventDestroy(ev);
-                ev = nullptr;
-            }
+            cudaStreamSynchronize(h2d_stream);
+            for (auto* evs : {chunk_ev, piece_ev})
+                for (int i = 0; i < 8; ++i) {
+                    if (evs[i]) cudaEventDestroy(evs[i]);
+                    evs[i] = nullptr;
+                }
             cudaStreamDestroy(copy_stream);
+            cudaStreamDestroy(h2d_stream);
             copy_stream = nullptr;
+            h2d_stream = nullptr;
         }
+        reach_version = -1;
         dfree(surf_ext);
         dfree(dtab);
         delete htab;
@@ -573,6 +597,7 @@ int surface_finish(dcpse_plan_s* P, int flags) {
     // the plan now holds the accumulated operator over the base particles
     P->free_transpose();
     dfree(P->rowptr);
+    P->list_version++;
     dfree(P->cols);
     dfree(P->k_term);
     dfree(P->w64);
@@ -711,6 +736,7 @@ int dcpse_plan_set_support(dcpse_plan_t* P, const double* d_pos_support, int64_t
     P->free_assembly();
     P->free_transpose();
     dfree(P->rowptr);
+    P->list_version++;
     dfree(P->cols);
     P->n = -1;
     P->nnz = 0;
@@ -729,6 +755,7 @@ int dcpse_plan_set_surface(dcpse_plan_t* P, const double* d_normals, int n_count
     P->free_assembly();
     P->free_transpose();
     dfree(P->rowptr);
+    P->list_version++;
     dfree(P->cols);
     dfree(P->surf_ext);
     P->n = -1;
@@ -774,6 +801,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     P->free_assembly();
     P->free_transpose();
     dfree(P->rowptr);
+    P->list_version++;
     dfree(P->cols);
     P->n = n;
     P->nnz = 0;
@@ -933,6 +961,7 @@ int dcpse_set_neighbors(dcpse_plan_t* P, int64_t n, int64_t nnz, const int64_t* 
     P->free_assembly();
     P->free_transpose();
     dfree(P->rowptr);
+    P->list_version++;
     dfree(P->cols);
     P->n = n;
     P->nnz = nnz;
@@ -954,6 +983,7 @@ int dcpse_set_neighbors(dcpse_plan_t* P, int64_t n, int64_t nnz, const int64_t* 
         DCPSE_CK(e);
         if (hb != 0) {
             dfree(P->rowptr);
+            P->list_version++;
             dfree(P->cols);
             P->n = -1;
             P->nnz = 0;
@@ -1497,6 +1527,52 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
     return DCPSE_OK;
 }
 
+namespace {
+// streams and events of the pipelined host-buffer apply (created once)
+int ensure_host_pipeline(dcpse_plan_t* P) {
+    if (P->copy_stream) return DCPSE_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&P->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->h2d_stream, cudaStreamNonBlocking);
+    for (int c = 0; c < kHostChunks && e == cudaSuccess; ++c) {
+        e = cudaEventCreateWithFlags(&P->chunk_ev[c], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->piece_ev[c], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        for (int c = 0; c < kHostChunks; ++c) {
+            if (P->chunk_ev[c]) cudaEventDestroy(P->chunk_ev[c]);
+            if (P->piece_ev[c]) cudaEventDestroy(P->piece_ev[c]);
+            P->chunk_ev[c] = P->piece_ev[c] = nullptr;
+        }
+        if (P->copy_stream) cudaStreamDestroy(P->copy_stream);
+        if (P->h2d_stream) cudaStreamDestroy(P->h2d_stream);
+        P->copy_stream = P->h2d_stream = nullptr;
+        return fail(DCPSE_ERR_CUDA, cudaGetErrorString(e));
+    }
+    return DCPSE_OK;
+}
+
+// largest field index read by each row chunk, for the current list
+int ensure_chunk_reach(dcpse_plan_t* P) {
+    if (P->reach_version == P->list_version) return DCPSE_OK;
+    unsigned long long* d = nullptr;
+    DCPSE_CK(dalloc(&d, kHostChunks));
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * kHostChunks, P->stream);
+    if (e == cudaSuccess) {
+        chunk_reach_kernel<<<std::max(1, std::min(num_sms() * 8, (int)((P->n + 255) / 256))), 256, 0, P->stream>>>(
+            P->rowptr, P->cols, P->n, kHostChunks, d);
+        e = cudaGetLastError();
+    }
+    unsigned long long h[kHostChunks] = {};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, P->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+    dfree(d);
+    DCPSE_CK(e);
+    for (int c = 0; c < kHostChunks; ++c) P->chunk_reach[c] = (int64_t)h[c];
+    P->reach_version = P->list_version;
+    return DCPSE_OK;
+}
+}  // namespace
+
 int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, int precision) {
     if (int rc = check_plan(P)) return rc;
     if (int rc = check_single_set(P)) return rc;
@@ -1504,44 +1580,71 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
     if (P->n > 0 && (!h_f || !h_out)) return fail(DCPSE_ERR_ARG, "NULL field");
     if (!P->hf) DCPSE_CK(dalloc(&P->hf, P->n));
     if (!P->hout) DCPSE_CK(dalloc(&P->hout, (size_t)P->nout * P->n));
-    DCPSE_CK(cudaMemcpyAsync(P->hf, h_f, sizeof(double) * P->n, cudaMemcpyHostToDevice, P->stream));
     const bool f32 = precision == DCPSE_F32 || precision == DCPSE_F32_RESID;
     if (!f32 || (P->apply_mode & 15) == 2 || P->n < kHostChunkMinRows) {
+        DCPSE_CK(cudaMemcpyAsync(P->hf, h_f, sizeof(double) * P->n, cudaMemcpyHostToDevice, P->stream));
         int rc = dcpse_apply_batched(P, P->hf, P->hout, precision);
         if (rc != DCPSE_OK) return rc;
         DCPSE_CK(cudaMemcpyAsync(h_out, P->hout, sizeof(double) * P->nout * P->n, cudaMemcpyDeviceToHost,
                                  P->stream));
         return dcpse_plan_check(P);
     }
-    // rows in chunks: the outputs of chunk c go back on the copy stream while
-    // chunk c + 1 is applied
+    // Pipelined: the field goes up in kHostChunks pieces (copy + split on
+    // h2d_stream); row chunk c starts once the pieces up to its largest read
+    // index have arrived; its outputs go back on copy_stream while later
+    // chunks run.
     if (int rc = check_f32_weights(P, precision)) return rc;
-    if (!P->copy_stream) {
-        DCPSE_CK(cudaStreamCreateWithFlags(&P->copy_stream, cudaStreamNonBlocking));
-        for (int c = 0; c < kHostChunks; ++c) {
-            cudaError_t e = cudaEventCreateWithFlags(&P->chunk_ev[c], cudaEventDisableTiming);
-            if (e != cudaSuccess) {
-                for (int d = 0; d < c; ++d) cudaEventDestroy(P->chunk_ev[d]);
-                cudaStreamDestroy(P->copy_stream);
-                P->copy_stream = nullptr;
-                return fail(DCPSE_ERR_CUDA, cudaGetErrorString(e));
-            }
-        }
-    }
-    if (int rc = split_into_plan(P, P->hf, P->n, 1)) return rc;
+    if (int rc = ensure_host_pipeline(P)) return rc;
+    if (int rc = ensure_chunk_reach(P)) return rc;
     const int64_t n = P->n;
+    if (P->f2_len < n) {
+        dfree(P->f2);
+        P->f2_len = 0;
+        DCPSE_CK(dalloc(&P->f2, (size_t)n));
+        P->f2_len = n;
+    }
+    // earlier work of the plan's stream on these buffers comes first
+    DCPSE_CK(cudaEventRecord(P->chunk_ev[0], P->stream));
+    DCPSE_CK(cudaStreamWaitEvent(P->h2d_stream, P->chunk_ev[0], 0));
+    // pieces are issued just ahead of the first chunk that reads them, so the
+    // first chunk's launch is not queued behind the whole upload
+    int issued = -1, waited = -1;
+    auto issue_piece = [&](int i) -> cudaError_t {
+        const int64_t i0 = n * i / kHostChunks, i1 = n * (i + 1) / kHostChunks;
+        cudaError_t e = cudaMemcpyAsync(P->hf + i0, h_f + i0, sizeof(double) * (size_t)(i1 - i0),
+                                        cudaMemcpyHostToDevice, P->h2d_stream);
+        if (e == cudaSuccess) e = split_f64(P->hf + i0, i1 - i0, P->f2 + i0, P->h2d_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(P->piece_ev[i], P->h2d_stream);
+        return e;
+    };
     for (int c = 0; c < kHostChunks; ++c) {
         const int64_t r0 = n * c / kHostChunks, r1 = n * (c + 1) / kHostChunks;
+        // the piece holding the largest index this chunk reads
+        int need = 0;
+        while (need + 1 < kHostChunks && n * (need + 1) / kHostChunks <= P->chunk_reach[c]) ++need;
+        // one piece of look-ahead keeps the copy engine busy
+        const int upto = std::min(kHostChunks - 1, std::max(need, c + 1));
+        while (issued < upto) DCPSE_CK(issue_piece(++issued));
+        if (need > waited) {
+            DCPSE_CK(cudaStreamWaitEvent(P->stream, P->piece_ev[need], 0));
+            waited = need;
+        }
         if (int rc = apply_f32_rows(P, precision, P->hout, r0, r1)) {
+            cudaStreamSynchronize(P->h2d_stream);
             cudaStreamSynchronize(P->copy_stream);
             return rc;
         }
         DCPSE_CK(cudaEventRecord(P->chunk_ev[c], P->stream));
         DCPSE_CK(cudaStreamWaitEvent(P->copy_stream, P->chunk_ev[c], 0));
-        for (int o = 0; o < P->nout; ++o)
-            DCPSE_CK(cudaMemcpyAsync(h_out + (size_t)o * n + r0, P->hout + (size_t)o * n + r0,
-                                     sizeof(double) * (size_t)(r1 - r0), cudaMemcpyDeviceToHost, P->copy_stream));
+        // rows [r0, r1) of every output: one strided copy
+        DCPSE_CK(cudaMemcpy2DAsync(h_out + r0, sizeof(double) * (size_t)n, P->hout + r0, sizeof(double) * (size_t)n,
+                                   sizeof(double) * (size_t)(r1 - r0), (size_t)P->nout, cudaMemcpyDeviceToHost,
+                                   P->copy_stream));
     }
+    while (issued < kHostChunks - 1) DCPSE_CK(issue_piece(++issued));
+    // rows never wait on pieces beyond their reach; the last piece must
+    // still be done before the call returns
+    DCPSE_CK(cudaStreamSynchronize(P->h2d_stream));
     DCPSE_CK(cudaStreamSynchronize(P->copy_stream));
     return dcpse_plan_check(P);
 }
