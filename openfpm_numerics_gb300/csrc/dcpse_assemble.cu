@@ -62,6 +62,9 @@ struct Split {
     int nout;                // outputs of the plan
     double* gram;            // [nb][gstride]
     double* coef;            // [nb][cstride]
+    double* usc;             // [nb][dim][maxk] scaled offsets u = x_pq / eps of every row
+    int64_t ustride;         // dim * maxk
+    int maxk;
     int32_t* gst;            // [nb] group status words
 };
 
@@ -197,6 +200,9 @@ __global__ void __launch_bounds__(256) gram_kernel(AsmArgs a, Split S, int64_t b
                 load_offset<DIM>(a, xp, a.cols[beg + q], o);
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) u[d] = o[d] / eps;
+                double* Ur = S.usc + slot * S.ustride;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) Ur[d * S.maxk + q] = u[d];
                 const double E = cw_exp(-norm2<DIM>(o) / (2.0 * eps * eps));
                 monomials<DIM>(u, V, P, nprog, lane);
                 for (int j = 0; j < nu; ++j) Bs[lane * S.ldb + j] = E * V[P.uslot[j] * 32 + lane];
@@ -383,9 +389,6 @@ __global__ void __launch_bounds__(256) weights_kernel(AsmArgs a, Split S, int64_
         const int64_t p = a.order ? (int64_t)a.order[it] : it;
         const int64_t beg = a.rowptr[p];
         const int k = (int)(a.rowptr[p + 1] - beg);
-        double xp[DIM];
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) xp[d] = a.pos[p * DIM + d];
         const double eps = a.eps[p];
         const int32_t word = S.gst[slot];
         for (int e = lane; e < S.cstride; e += 32) Cs[e] = S.coef[slot * S.cstride + e];
@@ -398,10 +401,12 @@ __global__ void __launch_bounds__(256) weights_kernel(AsmArgs a, Split S, int64_
         for (int c0 = 0; c0 < k; c0 += kCh) {
             int q = c0 + lane;
             if (q >= k) break;  // rows of this lane are done; no warp sync below
-            double o[DIM], u[DIM];
-            load_offset<DIM>(a, xp, a.cols[beg + q], o);
+            // u = x_pq / eps as the Gram kernel computed it (rows of particles
+            // with no assembled group were skipped there and are not used here)
+            double u[DIM];
+            const double* Ur = S.usc + slot * S.ustride;
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) u[d] = o[d] / eps;
+            for (int d = 0; d < DIM; ++d) u[d] = Ur[d * S.maxk + q];
             monomials<DIM>(u, V, P, nprog, lane);
             const double ef = cw_exp(-norm2<DIM>(u));
             for (int t = 0; t < noutputs; ++t) Wacc[t * 32 + lane] = 0.0;
@@ -636,9 +641,10 @@ Split make_split(const AsmTables& h, int flags) {
 
 }  // namespace
 
-int64_t assembly_scratch_bytes(const AsmTables& h, int flags) {
+int64_t assembly_scratch_bytes(const AsmTables& h, int flags, int maxk) {
     const Split S = make_split(h, flags);
-    return (int64_t)(S.gstride + S.cstride) * (int64_t)sizeof(double) + (int64_t)sizeof(int32_t);
+    return (int64_t)(S.gstride + S.cstride + (int64_t)h.dim * std::max(maxk, 1)) * (int64_t)sizeof(double) +
+           (int64_t)sizeof(int32_t);
 }
 
 int64_t binning_tmp_elems(int64_t n, int maxk, int width) {
@@ -685,7 +691,10 @@ cudaError_t assemble(const AsmArgs& a, const AsmTables& h, cudaStream_t s) {
     const int64_t nb = a.scratch_particles;
     S.gram = a.scratch;
     S.coef = S.gram + nb * S.gstride;
-    S.gst = reinterpret_cast<int32_t*>(S.coef + nb * S.cstride);
+    S.maxk = std::max(a.maxk, 1);
+    S.ustride = (int64_t)h.dim * S.maxk;
+    S.usc = S.coef + nb * S.cstride;
+    S.gst = reinterpret_cast<int32_t*>(S.usc + nb * S.ustride);
     int lpp = a.qr_lanes;
     if (lpp != 1 && lpp != 2 && lpp != 4 && lpp != 8 && lpp != 16 && lpp != 32) lpp = qr_lanes_auto(S);
     // a lane grouping whose work space does not fit is refused before any launch

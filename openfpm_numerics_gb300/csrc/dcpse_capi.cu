@@ -1069,11 +1069,12 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     a.nnz = nnz;
     a.warps = P->asm_warps;
     a.qr_lanes = P->asm_qr_lanes;
+    a.maxk = P->maxk;
     a.order = nullptr;
     if (n > 0) {
         // batches of at most kAsmScratchBytes of scratch (Gram entries and
         // coefficients of the particles in flight)
-        const int64_t per = assembly_scratch_bytes(*P->htab, flags);
+        const int64_t per = assembly_scratch_bytes(*P->htab, flags, P->maxk);
         const int64_t nb = std::min<int64_t>(n, std::max<int64_t>(4096, kAsmScratchBytes / per));
         const int64_t bytes = nb * per + 16;
         if (P->asm_scratch_bytes < bytes) {

@@ -126,13 +126,15 @@ struct AsmArgs {
     const int32_t* order; // processing order of the particles (k-binned) or nullptr
     int warps;            // warps per CTA of the Gram and weight kernels (2, 4 or 8)
     int qr_lanes;         // lanes per particle of the QR kernel (0 = automatic)
+    int maxk;             // longest neighbour row
     double* scratch;      // assembly_scratch_bytes() per particle of a batch
     int64_t scratch_particles;  // batch size the scratch holds
 };
 
 // Scratch bytes per particle of an assembly batch (Gram entries,
-// coefficients and a status word) for the plan's tables and flags.
-int64_t assembly_scratch_bytes(const AsmTables& h, int flags);
+// coefficients, the scaled offsets of its rows and a status word) for the
+// plan's tables and flags and the longest row maxk.
+int64_t assembly_scratch_bytes(const AsmTables& h, int flags, int maxk);
 
 // Particle order binned by neighbour count: bins of `width` counts
 // ascending (a counting sort on k / width); order[n], tmp sized by
