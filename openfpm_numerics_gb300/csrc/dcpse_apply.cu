@@ -46,7 +46,23 @@ __global__ void __launch_bounds__(256) apply_term_f64_kernel(int64_t n, const in
         const double fxp = sign * f[p];
         double D = 0.0;
         const int64_t e = rowptr[p + 1];
-        for (int64_t j = rowptr[p]; j < e; ++j) D = D + (f[cols[j]] + fxp) * K[j];
+        int64_t j = rowptr[p];
+        // 4 entries in flight: all loads of a batch are issued first, the
+        // sum then takes them in row order
+        for (; j + 4 <= e; j += 4) {
+            int32_t q[4];
+            double k[4], fq[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                q[u] = cols[j + u];
+                k[u] = K[j + u];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) fq[u] = f[q[u]];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) D = D + (fq[u] + fxp) * k[u];
+        }
+        for (; j < e; ++j) D = D + (f[cols[j]] + fxp) * K[j];
         D = D * eip[p];
         out[p] = accumulate ? out[p] + D : D;
     }
@@ -62,7 +78,22 @@ __global__ void __launch_bounds__(256) p2p_f64_kernel(int64_t n, const int64_t* 
         const int64_t b = rowptr[p], e = rowptr[p + 1];
         for (int c = 0; c < ncomp; ++c) {
             double D = 0.0;
-            for (int64_t j = b; j < e; ++j) D = D + f[(int64_t)cols[j] * ncomp + c] * K[j];
+            int64_t j = b;
+            // 4 entries in flight, summed in row order
+            for (; j + 4 <= e; j += 4) {
+                int32_t q[4];
+                double k[4], fq[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    q[u] = cols[j + u];
+                    k[u] = K[j + u];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) fq[u] = f[(int64_t)q[u] * ncomp + c];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) D = D + fq[u] * k[u];
+            }
+            for (; j < e; ++j) D = D + f[(int64_t)cols[j] * ncomp + c] * K[j];
             out[p * ncomp + c] = eip[p] * D;
         }
     }
