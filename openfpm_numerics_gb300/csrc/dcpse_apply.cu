@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(256) apply_f32_tma_kernel(F32Args a, TmaCfg c,
     }
 }
 
-template <int G, int NO>
+template <int G, int NO, int U>
 __global__ void __launch_bounds__(256) apply_f64_kernel(int64_t n, const int64_t* __restrict__ rowptr,
                                                         const int32_t* __restrict__ cols,
                                                         const double* __restrict__ w, int64_t nnz,
@@ -437,7 +437,28 @@ __global__ void __launch_bounds__(256) apply_f64_kernel(int64_t n, const int64_t
         if (row < n) {
             const double fp = no_self ? 0.0 : f[row * fs];
             const int64_t e = rowptr[row + 1];
-            for (int64_t j = rowptr[row] + sub; j < e; j += G) {
+            int64_t j = rowptr[row] + sub;
+            // U entries per lane in flight: columns, then the gathered field
+            // values and the weights, then the FMAs
+            for (; j + (U - 1) * G < e; j += U * G) {
+                int32_t q[U];
+                double fq[U], wv[U][NO];
+#pragma unroll
+                for (int u = 0; u < U; ++u) q[u] = cols[j + u * G];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    fq[u] = f[(int64_t)q[u] * fs];
+#pragma unroll
+                    for (int o = 0; o < NO; ++o) wv[u][o] = w[(int64_t)o * nnz + j + u * G];
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const double d = fq[u] - fp;
+#pragma unroll
+                    for (int o = 0; o < NO; ++o) acc[o] = fma(wv[u][o], d, acc[o]);
+                }
+            }
+            for (; j < e; j += G) {
                 const double d = f[(int64_t)cols[j] * fs] - fp;
 #pragma unroll
                 for (int o = 0; o < NO; ++o) acc[o] = fma(w[(int64_t)o * nnz + j], d, acc[o]);
@@ -464,12 +485,13 @@ int grid_rows(int64_t rows, int rows_per_block) {
     return (int)g;
 }
 
-// FP64 batched apply: one entry per lane per step
+// FP64 batched apply (4-deep load batches up to 4 outputs, 2-deep above):
+// 8 to 16 entries per lane, as for the FP32 apply
 int lanes_for(int64_t n, int64_t nnz) {
-    double avg = n > 0 ? (double)nnz / (double)n : 0.0;
-    if (avg <= 24.0) return 8;
-    if (avg <= 96.0) return 16;
-    return 32;
+    const double avg = n > 0 ? (double)nnz / (double)n : 0.0;
+    int g = 4;
+    while (g < 32 && avg / (2 * g) >= 8.0) g *= 2;
+    return g;
 }
 
 // FP32 batched apply (4-deep load batches): 8 to 16 entries per lane, the
@@ -557,7 +579,8 @@ cudaError_t launch_f64(int64_t n, int nout, const int64_t* rowptr, const int32_t
     const int grid = grid_rows(n, 256 / G);
 #define DCPSE_F64_CASE(NO)                                                                                     \
     case NO:                                                                                                   \
-        apply_f64_kernel<G, NO><<<grid, 256, 0, s>>>(n, rowptr, cols, w, nnz, f, out, no_self, oos, ors, fs);  \
+        apply_f64_kernel<G, NO, (NO <= 4 ? 4 : 2)>                                                             \
+            <<<grid, 256, 0, s>>>(n, rowptr, cols, w, nnz, f, out, no_self, oos, ors, fs);                     \
         break;
     switch (nout) {
         DCPSE_F64_CASE(1)
@@ -673,6 +696,7 @@ cudaError_t apply_batched_f64(int64_t n, int nout, const int64_t* rowptr, const 
     if (ors == 0) ors = 1;
     if (fs == 0) fs = 1;
     switch (lanes_for(n, nnz)) {
+        case 4: return launch_f64<4>(n, nout, rowptr, cols, w, nnz, f, out, no_self, oos, ors, fs, s);
         case 8: return launch_f64<8>(n, nout, rowptr, cols, w, nnz, f, out, no_self, oos, ors, fs, s);
         case 16: return launch_f64<16>(n, nout, rowptr, cols, w, nnz, f, out, no_self, oos, ors, fs, s);
         default: return launch_f64<32>(n, nout, rowptr, cols, w, nnz, f, out, no_self, oos, ors, fs, s);

@@ -1305,6 +1305,29 @@ int dcpse_vjp_positions(dcpse_plan_t* P, const double* d_pos, const double* d_ep
     return DCPSE_OK;
 }
 
+// RK4 stage kernels: lanes per row for 16 to 32 neighbour entries per lane in
+// 4-deep batches (96^3 periodic cloud, 84 entries per row: 4 lanes 0.79 ms
+// per step, 8 lanes 0.85 ms, 16 lanes 1.26 ms)
+static int rk_lanes(const dcpse_plan_t* P) {
+    if (P->apply_lanes) return P->apply_lanes;
+    const double avg = P->n > 0 ? (double)P->nnz / (double)P->n : 0.0;
+    int lanes = 4;
+    while (lanes < 32 && avg / (2 * lanes) >= 16.0) lanes *= 2;
+    return lanes;
+}
+
+// the gathered input of an RK4 stage or adjoint stage as (u, v) pairs: plan
+// scratch, 16 bytes per particle
+static int ensure_rk_pack(dcpse_plan_t* P) {
+    if (P->rk_pack_n < P->n) {
+        dfree(P->rk_pack);
+        P->rk_pack_n = 0;
+        DCPSE_CK(dalloc(&P->rk_pack, (size_t)std::max<int64_t>(P->n, 1) * 2));
+        P->rk_pack_n = P->n;
+    }
+    return DCPSE_OK;
+}
+
 int dcpse_rk4_gs_stage(dcpse_plan_t* P, int stage, int precision, const void* Yu, const void* Yv, const void* y0u,
                        const void* y0v, void* accu, void* accv, void* outu, void* outv, const double* params) {
     if (int rc = check_plan(P)) return rc;
@@ -1313,22 +1336,8 @@ int dcpse_rk4_gs_stage(dcpse_plan_t* P, int stage, int precision, const void* Yu
     if (stage < 0 || stage > 3 || !params) return fail(DCPSE_ERR_ARG, "stage 0..3 and params {Du,Dv,F,k,dt}");
     if (P->n > 0 && (!Yu || !Yv || !y0u || !y0v || !accu || !accv || !outu || !outv))
         return fail(DCPSE_ERR_ARG, "NULL array");
-    // lanes per row: 16 to 32 neighbour entries per lane in 4-deep batches
-    // (96^3 periodic cloud, 84 entries per row: 4 lanes 0.79 ms per step,
-    // 8 lanes 0.85 ms, 16 lanes 1.26 ms)
-    int lanes = P->apply_lanes;
-    if (!lanes) {
-        const double avg = P->n > 0 ? (double)P->nnz / (double)P->n : 0.0;
-        lanes = 4;
-        while (lanes < 32 && avg / (2 * lanes) >= 16.0) lanes *= 2;
-    }
-    // the stage input as (u, v) pairs: plan scratch, 16 bytes per particle
-    if (P->rk_pack_n < P->n) {
-        dfree(P->rk_pack);
-        P->rk_pack_n = 0;
-        DCPSE_CK(dalloc(&P->rk_pack, (size_t)std::max<int64_t>(P->n, 1) * 2));
-        P->rk_pack_n = P->n;
-    }
+    const int lanes = rk_lanes(P);
+    if (int rc = ensure_rk_pack(P)) return rc;
     if (precision == DCPSE_F32) {
         if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
         RkArgs<float> a{P->n, P->rowptr, P->cols, P->w32, (const float*)Yu, (const float*)Yv, (const float*)y0u,
@@ -1365,6 +1374,7 @@ int dcpse_rk4_gs_adjoint_prepare(dcpse_plan_t* P, int precision) {
     } else {
         return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
     }
+    if (int rc = ensure_rk_pack(P)) return rc;
     DCPSE_CK(cudaStreamSynchronize(P->stream));
     return DCPSE_OK;
 }
@@ -1376,20 +1386,22 @@ int dcpse_rk4_gs_adjoint_stage(dcpse_plan_t* P, int precision, const void* Yu, c
     if (!params) return fail(DCPSE_ERR_ARG, "params {Du,Dv,F,k,dt}");
     if (P->n > 0 && (!Yu || !Yv || !kbu || !kbv || !ybu || !ybv || !accu || !accv))
         return fail(DCPSE_ERR_ARG, "NULL array");
+    if (P->rk_pack_n < P->n) return fail(DCPSE_ERR_STATE, "call dcpse_rk4_gs_adjoint_prepare first");
+    const int lanes = rk_lanes(P);
     if (precision == DCPSE_F32) {
         if (!P->wT32) return fail(DCPSE_ERR_STATE, "call dcpse_rk4_gs_adjoint_prepare first");
         RkAdjArgs<float> a{P->n, P->t_row, P->t_src, P->wT32, P->rs32, (const float*)Yu, (const float*)Yv,
                            (const float*)kbu, (const float*)kbv, (const float*)ybu, (const float*)ybv, (float*)accu,
                            (float*)accv, (float*)next_u, (float*)next_v, cy, cY, params[0], params[1], params[2],
-                           params[3]};
-        DCPSE_CK(rk_adjoint_stage<float>(a, P->stream));
+                           params[3], P->rk_pack};
+        DCPSE_CK(rk_adjoint_stage<float>(a, lanes, P->stream));
     } else if (precision == DCPSE_F64) {
         if (!P->wT64) return fail(DCPSE_ERR_STATE, "call dcpse_rk4_gs_adjoint_prepare first");
         RkAdjArgs<double> a{P->n, P->t_row, P->t_src, P->wT64, P->rs64, (const double*)Yu, (const double*)Yv,
                             (const double*)kbu, (const double*)kbv, (const double*)ybu, (const double*)ybv,
                             (double*)accu, (double*)accv, (double*)next_u, (double*)next_v, cy, cY, params[0],
-                            params[1], params[2], params[3]};
-        DCPSE_CK(rk_adjoint_stage<double>(a, P->stream));
+                            params[1], params[2], params[3], P->rk_pack};
+        DCPSE_CK(rk_adjoint_stage<double>(a, lanes, P->stream));
     } else {
         return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
     }

@@ -287,11 +287,12 @@ struct RkAdjArgs {
     T *next_u, *next_v;             // kbar of the previous stage, or null
     double cy, cY;                  // next kbar = cy ybar + cY Ybar
     double Du, Dv, F, K;
+    void* pack;                     // scratch: n (kbar_u, kbar_v) pairs
 };
 template <typename T>
 cudaError_t rk_stage(const RkArgs<T>& a, int lanes, cudaStream_t s);
 template <typename T>
-cudaError_t rk_adjoint_stage(const RkAdjArgs<T>& a, cudaStream_t s);
+cudaError_t rk_adjoint_stage(const RkAdjArgs<T>& a, int lanes, cudaStream_t s);
 template <typename T>
 cudaError_t rk_transpose_weights(const int64_t* rowptr, const int64_t* tidx, int64_t n, int64_t nnz, const T* w,
                                  T* wT, T* rs, cudaStream_t s);

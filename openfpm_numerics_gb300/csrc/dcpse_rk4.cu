@@ -141,28 +141,64 @@ __global__ void __launch_bounds__(256) gs_stage_kernel(RkArgs<T> a) {
     }
 }
 
-// adjoint stage: thread per particle over the transposed list
-template <typename T>
+// adjoint stage: G lanes per particle over its transposed row, kbar of the
+// stage gathered as packed (u, v) pairs in 4-deep batches
+template <typename T, int G>
 __global__ void __launch_bounds__(256) gs_adjoint_kernel(RkAdjArgs<T> a) {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.n; p += (int64_t)gridDim.x * blockDim.x) {
+    typedef typename Pair<T>::type P2;
+    const P2* __restrict__ KB = static_cast<const P2*>(a.pack);
+    const int lane = threadIdx.x & 31;
+    const int sub = lane & (G - 1);
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t rows_per_pass = ((int64_t)gridDim.x * blockDim.x) / G;
+    const int64_t first = (tid - lane) / G;
+    for (int64_t base = first; base < a.n; base += rows_per_pass) {
+        const int64_t row = base + lane / G;
         T lu = 0, lv = 0;
-        for (int64_t t = a.trow[p]; t < a.trow[p + 1]; ++t) {
-            const int32_t s = a.tsrc[t];
-            const T w = a.wT[t];
-            lu = tfma<T>(w, a.kbu[s], lu);
-            lv = tfma<T>(w, a.kbv[s], lv);
+        if (row < a.n) {
+            const int64_t rb = a.trow[row];
+            const int k = (int)(a.trow[row + 1] - rb);
+            const int32_t* __restrict__ c = a.tsrc + rb;
+            const T* __restrict__ w = a.wT + rb;
+            constexpr int U = 4;
+            for (int j0 = sub; j0 < k; j0 += G * U) {
+                int32_t q[U];
+                T wq[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int j = j0 + u * G;
+                    q[u] = j < k ? c[j] : (int32_t)row;
+                    wq[u] = j < k ? w[j] : (T)0;
+                }
+                P2 y[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) y[u] = KB[q[u]];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    lu = tfma<T>(wq[u], y[u].x, lu);
+                    lv = tfma<T>(wq[u], y[u].y, lv);
+                }
+            }
         }
-        const T kbu = a.kbu[p], kbv = a.kbv[p];
-        lu = lu - a.rs[p] * kbu;
-        lv = lv - a.rs[p] * kbv;
-        const T u = a.Yu[p], v = a.Yv[p];
-        const T Ybu = (T)a.Du * lu - (v * v + (T)a.F) * kbu + v * v * kbv;
-        const T Ybv = (T)a.Dv * lv - (T)2 * u * v * kbu + ((T)2 * u * v - (T)a.F - (T)a.K) * kbv;
-        a.accu[p] += Ybu;
-        a.accv[p] += Ybv;
-        if (a.next_u) {
-            a.next_u[p] = (T)a.cy * a.ybu[p] + (T)a.cY * Ybu;
-            a.next_v[p] = (T)a.cy * a.ybv[p] + (T)a.cY * Ybv;
+#pragma unroll
+        for (int m = G / 2; m > 0; m >>= 1) {
+            lu += __shfl_xor_sync(0xffffffffu, lu, m);
+            lv += __shfl_xor_sync(0xffffffffu, lv, m);
+        }
+        if (row < a.n && sub == 0) {
+            const int64_t p = row;
+            const T kbu = a.kbu[p], kbv = a.kbv[p];
+            lu = lu - a.rs[p] * kbu;
+            lv = lv - a.rs[p] * kbv;
+            const T u = a.Yu[p], v = a.Yv[p];
+            const T Ybu = (T)a.Du * lu - (v * v + (T)a.F) * kbu + v * v * kbv;
+            const T Ybv = (T)a.Dv * lv - (T)2 * u * v * kbu + ((T)2 * u * v - (T)a.F - (T)a.K) * kbv;
+            a.accu[p] += Ybu;
+            a.accv[p] += Ybv;
+            if (a.next_u) {
+                a.next_u[p] = (T)a.cy * a.ybu[p] + (T)a.cY * Ybu;
+                a.next_v[p] = (T)a.cy * a.ybv[p] + (T)a.cY * Ybv;
+            }
         }
     }
 }
@@ -205,9 +241,15 @@ cudaError_t rk_stage(const RkArgs<T>& a, int lanes, cudaStream_t s) {
 }
 
 template <typename T>
-cudaError_t rk_adjoint_stage(const RkAdjArgs<T>& a, cudaStream_t s) {
+cudaError_t rk_adjoint_stage(const RkAdjArgs<T>& a, int lanes, cudaStream_t s) {
     if (a.n == 0) return cudaSuccess;
-    gs_adjoint_kernel<T><<<grid_n(a.n, 256), 256, 0, s>>>(a);
+    pack_kernel<T><<<grid_n(a.n, 256), 256, 0, s>>>(a.kbu, a.kbv, a.n, static_cast<typename Pair<T>::type*>(a.pack));
+    switch (lanes) {
+        case 4: gs_adjoint_kernel<T, 4><<<grid_n(a.n, 64), 256, 0, s>>>(a); break;
+        case 8: gs_adjoint_kernel<T, 8><<<grid_n(a.n, 32), 256, 0, s>>>(a); break;
+        case 16: gs_adjoint_kernel<T, 16><<<grid_n(a.n, 16), 256, 0, s>>>(a); break;
+        default: gs_adjoint_kernel<T, 32><<<grid_n(a.n, 8), 256, 0, s>>>(a); break;
+    }
     return cudaGetLastError();
 }
 
@@ -221,8 +263,8 @@ cudaError_t rk_transpose_weights(const int64_t* rowptr, const int64_t* tidx, int
 
 template cudaError_t rk_stage<float>(const RkArgs<float>&, int, cudaStream_t);
 template cudaError_t rk_stage<double>(const RkArgs<double>&, int, cudaStream_t);
-template cudaError_t rk_adjoint_stage<float>(const RkAdjArgs<float>&, cudaStream_t);
-template cudaError_t rk_adjoint_stage<double>(const RkAdjArgs<double>&, cudaStream_t);
+template cudaError_t rk_adjoint_stage<float>(const RkAdjArgs<float>&, int, cudaStream_t);
+template cudaError_t rk_adjoint_stage<double>(const RkAdjArgs<double>&, int, cudaStream_t);
 template cudaError_t rk_transpose_weights<float>(const int64_t*, const int64_t*, int64_t, int64_t, const float*,
                                                  float*, float*, cudaStream_t);
 template cudaError_t rk_transpose_weights<double>(const int64_t*, const int64_t*, int64_t, int64_t, const double*,

@@ -93,3 +93,41 @@ def test_checkpointed_adjoint(cuda, dtype, tol):
     fd = (jp - jm) / (2 * h)
     ad = float((vb.double() * delta.double()).sum())
     assert abs(fd - ad) <= tol * abs(fd), (fd, ad)
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 2e-5)])
+def test_adjoint_stage_equals_transposed_jacobian(cuda, dtype, tol):
+    """One adjoint stage against J(Y)^T kbar written with the Laplacian as a
+    sparse matrix L = W - diag(row sums of W): ubar = Du L^T kbar_u
+    - (v^2 + F) kbar_u + v^2 kbar_v, vbar = Dv L^T kbar_v - 2 u v kbar_u
+    + (2 u v - F - k) kbar_v; accumulated into acc, and the next stage's kbar
+    = cy ybar + cY Ybar."""
+    import scipy.sparse as sp
+
+    plan, u, v, dt = _setup(16, dtype)
+    gs = GrayScottRK4(plan, u, v, P["Du"], P["Dv"], P["F"], P["k"], dt)
+    gs.prepare_adjoint()
+    n = u.numel()
+    rng = np.random.default_rng(9)
+    Y = tuple(torch.tensor(rng.uniform(0.2, 1.0, n), device="cuda", dtype=dtype) for _ in range(2))
+    kb = tuple(torch.tensor(rng.standard_normal(n), device="cuda", dtype=dtype) for _ in range(2))
+    yb = tuple(torch.tensor(rng.standard_normal(n), device="cuda", dtype=dtype) for _ in range(2))
+    acc0 = tuple(torch.tensor(rng.standard_normal(n), device="cuda", dtype=dtype) for _ in range(2))
+    acc = tuple(a.clone() for a in acc0)
+    nxt = (torch.empty_like(u), torch.empty_like(u))
+    cy, cY = dt / 3.0, dt / 2.0
+    gs._adj_stage(Y, kb, yb, acc, nxt, cy, cY)
+    torch.cuda.synchronize()
+    rp, cols = (x.cpu().numpy() for x in plan.neighbors())
+    w = plan.output_weights(0)[0 if dtype == torch.float64 else 1].double().cpu().numpy()
+    W_ = sp.csr_matrix((w, cols, rp), shape=(n, n))
+    L = W_ - sp.diags(np.asarray(W_.sum(axis=1)).ravel())
+    Yu, Yv, ku, kv, bu, bv = (t.double().cpu().numpy() for t in (*Y, *kb, *yb))
+    Ybu = P["Du"] * (L.T @ ku) - (Yv ** 2 + P["F"]) * ku + Yv ** 2 * kv
+    Ybv = P["Dv"] * (L.T @ kv) - 2 * Yu * Yv * ku + (2 * Yu * Yv - P["F"] - P["k"]) * kv
+    for got, ref in ((acc[0].double().cpu().numpy() - acc0[0].double().cpu().numpy(), Ybu),
+                     (acc[1].double().cpu().numpy() - acc0[1].double().cpu().numpy(), Ybv),
+                     (nxt[0].double().cpu().numpy(), cy * bu + cY * Ybu),
+                     (nxt[1].double().cpu().numpy(), cy * bv + cY * Ybv)):
+        scale = np.abs(ref).max() + np.abs(acc0[0].double().cpu().numpy()).max()
+        assert np.abs(got - ref).max() <= tol * scale
