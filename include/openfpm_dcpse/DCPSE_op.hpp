@@ -144,16 +144,30 @@ VerletList getVerlet(particles_type& parts, double rCut, bool skip_ref = true) {
 }
 
 // --------------------------------------------------------------- operators --
+// Which reference class an operator's terms follow: Dcpse (the default), or
+// Dcpse_gpu for the *_gpu aliases (DCPSE_op.hpp:3510-3530), i.e. eps = 2 <h>
+// and a support the operator builds from rCut itself (see Dcpse_gpu).
+struct dcpse_cpu_kind {
+    static constexpr bool gpu = false;
+};
+struct dcpse_gpu_kind {
+    static constexpr bool gpu = true;
+};
+
 // outputs: list of outputs, each a list of signatures summed into it.
-template <typename VerletList_type>
+template <typename VerletList_type, typename Kind = dcpse_cpu_kind>
 class DcpseOperator {
 public:
     template <typename particles_type>
     DcpseOperator(particles_type& parts, VerletList_type& verletList, unsigned int ord,
                   typename particles_type::stype rCut, std::vector<std::vector<std::vector<unsigned>>> outputs,
                   support_options opt, double h_over_eps = 0.9)
-        : vl_(verletList), outputs_(std::move(outputs)), ord_(ord), hoe_(h_over_eps), dim_(particles_type::dims) {
-        (void)rCut;
+        : vl_(verletList),
+          outputs_(std::move(outputs)),
+          ord_(ord),
+          hoe_(Kind::gpu ? 0.5 : h_over_eps),
+          dim_(particles_type::dims),
+          rcut_((double)rCut) {
         parts.ghost_get_subset();
         build(parts, opt != support_options::LOAD);
     }
@@ -238,10 +252,14 @@ private:
     template <typename particles_type>
     void build(particles_type& parts, bool assemble) {
         plan_.reset(new detail::PlanHost(dim_, outputs_, ord_, hoe_));
-        if (surf_.on)
+        if (surf_.on) {
             plan_->set_surface_particles(parts, parts, false, surf_);
-        else
+        } else if constexpr (Kind::gpu) {
+            own_vl_ = getVerlet(parts, rcut_);
+            plan_->set_particles(parts, own_vl_);
+        } else {
             plan_->set_particles(parts, vl_);
+        }
         if (!assemble) return;
         int64_t nbad = plan_->assemble(DCPSE_STORE_TERMS_F64 | DCPSE_STORE_OUT_F32);
         detail::throw_too_few(plan_->last_fail_code(), nbad);
@@ -298,6 +316,8 @@ private:
     unsigned ord_;
     double hoe_;
     int dim_;
+    double rcut_ = 0.0;
+    VerletList own_vl_;  // the support of a Dcpse_gpu-kind operator
     detail::SurfaceCfg surf_;
     std::unique_ptr<detail::PlanHost> plan_;
 };
@@ -316,13 +336,13 @@ inline std::vector<unsigned> mixed(int dim, std::initializer_list<std::pair<int,
 }  // namespace detail
 
 #define OPENFPM_DCPSE_SINGLE_OP(NAME, SIGEXPR)                                                                  \
-    template <typename VerletList_type>                                                                        \
-    class NAME : public DcpseOperator<VerletList_type> {                                                       \
+    template <typename VerletList_type, typename Kind = dcpse_cpu_kind>                                        \
+    class NAME : public DcpseOperator<VerletList_type, Kind> {                                                 \
     public:                                                                                                    \
         template <typename particles_type>                                                                     \
         NAME(particles_type& parts, VerletList_type& verletList, unsigned int ord,                             \
              typename particles_type::stype rCut, support_options opt = support_options::RADIUS)               \
-            : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut,                                     \
+            : DcpseOperator<VerletList_type, Kind>(parts, verletList, ord, rCut,                               \
                                              {{[](int dim) { return SIGEXPR; }(particles_type::dims)}}, opt) {} \
     };
 
@@ -346,19 +366,19 @@ OPENFPM_DCPSE_SINGLE_OP(Derivative_xxyy, detail::mixed(dim, {{0, 2}, {1, 2}}))
 #undef OPENFPM_DCPSE_SINGLE_OP
 
 // Derivative_G_T (DCPSE_op.hpp:3387-3482): arbitrary signature p
-template <typename VerletList_type>
-class Derivative_G : public DcpseOperator<VerletList_type> {
+template <typename VerletList_type, typename Kind = dcpse_cpu_kind>
+class Derivative_G : public DcpseOperator<VerletList_type, Kind> {
 public:
     template <typename particles_type, typename Sig>
     Derivative_G(particles_type& parts, VerletList_type& verletList, unsigned int ord,
                  typename particles_type::stype rCut, const Sig& p, support_options opt = support_options::RADIUS)
-        : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut,
+        : DcpseOperator<VerletList_type, Kind>(parts, verletList, ord, rCut,
                                          {{detail::sig_vector(p, particles_type::dims)}}, opt) {}
 };
 
 // Laplacian_T (DCPSE_op.hpp:1350-1500): one output, sum of dim terms 2e_i
-template <typename VerletList_type>
-class Laplacian : public DcpseOperator<VerletList_type> {
+template <typename VerletList_type, typename Kind = dcpse_cpu_kind>
+class Laplacian : public DcpseOperator<VerletList_type, Kind> {
     static std::vector<std::vector<std::vector<unsigned>>> outs(int dim) {
         std::vector<std::vector<unsigned>> t;
         for (int i = 0; i < dim; ++i) t.push_back(detail::unit(dim, i, 2));
@@ -369,12 +389,12 @@ public:
     template <typename particles_type>
     Laplacian(particles_type& parts, VerletList_type& verletList, unsigned int ord, typename particles_type::stype rCut,
               support_options opt = support_options::RADIUS)
-        : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut, outs(particles_type::dims), opt) {}
+        : DcpseOperator<VerletList_type, Kind>(parts, verletList, ord, rCut, outs(particles_type::dims), opt) {}
 };
 
 // Gradient_T (DCPSE_op.hpp:1081-1224): dim outputs e_i (vector result)
-template <typename VerletList_type>
-class Gradient : public DcpseOperator<VerletList_type> {
+template <typename VerletList_type, typename Kind = dcpse_cpu_kind>
+class Gradient : public DcpseOperator<VerletList_type, Kind> {
     static std::vector<std::vector<std::vector<unsigned>>> outs(int dim) {
         std::vector<std::vector<std::vector<unsigned>>> o;
         for (int i = 0; i < dim; ++i) o.push_back({detail::unit(dim, i)});
@@ -385,14 +405,14 @@ public:
     template <typename particles_type>
     Gradient(particles_type& parts, VerletList_type& verletList, unsigned int ord, typename particles_type::stype rCut,
              support_options opt = support_options::RADIUS)
-        : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut, outs(particles_type::dims), opt) {}
+        : DcpseOperator<VerletList_type, Kind>(parts, verletList, ord, rCut, outs(particles_type::dims), opt) {}
 };
 
 // Divergence_T (DCPSE_op.hpp:1503-1630): dim terms e_i applied to the
 // components of a vector property, VECT_DCPSE_V_DIV (:446-475):
 // div = ((0 + D_0 v_0) + D_1 v_1) + ...
-template <typename VerletList_type>
-class Divergence : public DcpseOperator<VerletList_type> {
+template <typename VerletList_type, typename Kind = dcpse_cpu_kind>
+class Divergence : public DcpseOperator<VerletList_type, Kind> {
     static std::vector<std::vector<std::vector<unsigned>>> outs(int dim) {
         std::vector<std::vector<std::vector<unsigned>>> o;
         for (int i = 0; i < dim; ++i) o.push_back({detail::unit(dim, i)});
@@ -403,7 +423,7 @@ public:
     template <typename particles_type>
     Divergence(particles_type& parts, VerletList_type& verletList, unsigned int ord,
                typename particles_type::stype rCut, support_options opt = support_options::RADIUS)
-        : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut, outs(particles_type::dims), opt),
+        : DcpseOperator<VerletList_type, Kind>(parts, verletList, ord, rCut, outs(particles_type::dims), opt),
           dim_(particles_type::dims) {}
 
     template <unsigned int prp, typename vector_type>
@@ -434,10 +454,10 @@ private:
 // Advection_T (DCPSE_op.hpp:1632-1781): (v . grad) f, VECT_DCPSE_V_DOT
 // (:531-565): adv = ((0 + v_0 D_0 f) + v_1 D_1 f) + ..., component-wise for a
 // vector property f
-template <typename VerletList_type>
-class Advection : public Divergence<VerletList_type> {
+template <typename VerletList_type, typename Kind = dcpse_cpu_kind>
+class Advection : public Divergence<VerletList_type, Kind> {
 public:
-    using Divergence<VerletList_type>::Divergence;
+    using Divergence<VerletList_type, Kind>::Divergence;
 
     template <unsigned int p1, typename vt1, unsigned int p2, typename vt2>
     Expr operator()(PropRef<p1, vt1> vel, PropRef<p2, vt2> arg) {
@@ -467,8 +487,8 @@ public:
 
 // Curl2D_T (DCPSE_op.hpp:1227-1340): terms e_1 and e_0, VECT_DCPSE_V_CURL2D
 // (:206-233): (D_y f, -D_x f)
-template <typename VerletList_type>
-class Curl2D : public DcpseOperator<VerletList_type> {
+template <typename VerletList_type, typename Kind = dcpse_cpu_kind>
+class Curl2D : public DcpseOperator<VerletList_type, Kind> {
     static std::vector<std::vector<std::vector<unsigned>>> outs(int dim) {
         return {{detail::unit(dim, 1)}, {detail::unit(dim, 0)}};
     }
@@ -477,11 +497,11 @@ public:
     template <typename particles_type>
     Curl2D(particles_type& parts, VerletList_type& verletList, unsigned int ord, typename particles_type::stype rCut,
            support_options opt = support_options::RADIUS)
-        : DcpseOperator<VerletList_type>(parts, verletList, ord, rCut, outs(particles_type::dims), opt) {}
+        : DcpseOperator<VerletList_type, Kind>(parts, verletList, ord, rCut, outs(particles_type::dims), opt) {}
 
     template <unsigned int prp, typename vector_type>
     Expr operator()(PropRef<prp, vector_type> arg) {
-        Expr e = DcpseOperator<VerletList_type>::operator()(arg);
+        Expr e = DcpseOperator<VerletList_type, Kind>::operator()(arg);
         auto inner = e.nodes[0].eval;
         e.nodes[0].eval = [inner](std::vector<std::vector<double>>& out) {
             inner(out);
@@ -491,25 +511,26 @@ public:
     }
 };
 
-// GPU aliases of the reference (DCPSE_op.hpp:3510-3530) name the same classes
-template <typename VL> using Derivative_x_gpu = Derivative_x<VL>;
-template <typename VL> using Derivative_y_gpu = Derivative_y<VL>;
-template <typename VL> using Derivative_z_gpu = Derivative_z<VL>;
-template <typename VL> using Derivative_xx_gpu = Derivative_xx<VL>;
-template <typename VL> using Derivative_yy_gpu = Derivative_yy<VL>;
-template <typename VL> using Derivative_zz_gpu = Derivative_zz<VL>;
-template <typename VL> using Derivative_xy_gpu = Derivative_xy<VL>;
-template <typename VL> using Laplacian_gpu = Laplacian<VL>;
-template <typename VL> using Gradient_gpu = Gradient<VL>;
-template <typename VL> using Derivative_G_gpu = Derivative_G<VL>;
-template <typename VL> using Derivative_yz_gpu = Derivative_yz<VL>;
-template <typename VL> using Derivative_xz_gpu = Derivative_xz<VL>;
-template <typename VL> using Derivative_xxx_gpu = Derivative_xxx<VL>;
-template <typename VL> using Derivative_xxy_gpu = Derivative_xxy<VL>;
-template <typename VL> using Derivative_yyx_gpu = Derivative_yyx<VL>;
-template <typename VL> using Derivative_yyy_gpu = Derivative_yyy<VL>;
-template <typename VL> using Divergence_gpu = Divergence<VL>;
-template <typename VL> using Advection_gpu = Advection<VL>;
-template <typename VL> using Curl2D_gpu = Curl2D<VL>;
+// GPU aliases of the reference (DCPSE_op.hpp:3510-3530): the same operators
+// over Dcpse_gpu (eps = 2 <h>, support built from rCut)
+template <typename VL> using Derivative_x_gpu = Derivative_x<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_y_gpu = Derivative_y<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_z_gpu = Derivative_z<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_xx_gpu = Derivative_xx<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_yy_gpu = Derivative_yy<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_zz_gpu = Derivative_zz<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_xy_gpu = Derivative_xy<VL, dcpse_gpu_kind>;
+template <typename VL> using Laplacian_gpu = Laplacian<VL, dcpse_gpu_kind>;
+template <typename VL> using Gradient_gpu = Gradient<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_G_gpu = Derivative_G<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_yz_gpu = Derivative_yz<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_xz_gpu = Derivative_xz<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_xxx_gpu = Derivative_xxx<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_xxy_gpu = Derivative_xxy<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_yyx_gpu = Derivative_yyx<VL, dcpse_gpu_kind>;
+template <typename VL> using Derivative_yyy_gpu = Derivative_yyy<VL, dcpse_gpu_kind>;
+template <typename VL> using Divergence_gpu = Divergence<VL, dcpse_gpu_kind>;
+template <typename VL> using Advection_gpu = Advection<VL, dcpse_gpu_kind>;
+template <typename VL> using Curl2D_gpu = Curl2D<VL, dcpse_gpu_kind>;
 
 }  // namespace openfpm_dcpse

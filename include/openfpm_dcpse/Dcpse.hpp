@@ -533,6 +533,27 @@ public:
     }
 
 protected:
+    // Dcpse_gpu (below): eps = <h> / h_over_eps with the class's own factor
+    template <typename Sig>
+    Dcpse(vector_type& particles, VerletList_type& verletList, const Sig& differentialSignature,
+          unsigned int convergenceOrder, T rCut, support_options opt, double h_over_eps)
+        : HOverEpsilon((T)h_over_eps),
+          verletList_(verletList),
+          sig_(detail::sig_vector(differentialSignature, dim)),
+          convergenceOrder_(convergenceOrder),
+          rCut_(rCut),
+          opt_(opt) {
+        differentialOrder_ = 0;
+        for (unsigned s : sig_) differentialOrder_ += s;
+        support_ = &particles;
+        domain_ = same_set(particles);
+        particles.ghost_get_subset();
+        plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder, (double)HOverEpsilon));
+        plan_->set_particles(particles, verletList_);
+        if (opt == support_options::LOAD) return;
+        assemble();
+    }
+
     // surface operators (SurfaceDcpse below)
     template <typename Sig>
     Dcpse(vector_type& particlesSupport, vector_type2& particlesDomain, VerletList_type& verletList,
@@ -754,6 +775,50 @@ private:
     support_options opt_;
     detail::SurfaceCfg surface_;
     std::unique_ptr<detail::PlanHost> plan_;
+};
+
+namespace detail {
+// the support list a Dcpse_gpu builds for itself (held in a base class so it
+// exists before the Dcpse base that refers to it)
+struct OwnSupport {
+    VerletList own_support;
+    OwnSupport(int dim, const std::vector<double>& pos, double rCut)
+        : own_support(build_verlet(dim, pos, nullptr, rCut, true)) {}
+};
+}  // namespace detail
+
+// Dcpse_gpu (Dcpse.cuh:35-875), the class behind the reference's *_gpu
+// operators.  What it computes differs from Dcpse in two points, both kept:
+// eps = 2 <h> (FACTOR = 2, Dcpse.cuh:799-807; no HOverEpsilon), and the
+// support is built by the class from rCut (SupportBuilderGPU,
+// SupportBuilder.cuh:14-107: |x_p - x_q| < rCut, p excluded), the Verlet list
+// argument being unused as there.  The reference solves the moment systems
+// by an unpivoted batched LU; here they go through the same column-pivoting
+// QR as Dcpse, which gives the same kernels up to the systems' conditioning.
+template <unsigned int dim, typename VerletList_type, typename vector_type>
+class Dcpse_gpu : private detail::OwnSupport, public Dcpse<dim, VerletList, vector_type> {
+    typedef Dcpse<dim, VerletList, vector_type> base;
+
+public:
+    typedef typename vector_type::stype T;
+
+    template <typename Sig>
+    Dcpse_gpu(vector_type& particles, VerletList_type& verletList, const Sig& differentialSignature,
+              unsigned int convergenceOrder, T rCut, support_options opt = support_options::RADIUS)
+        : detail::OwnSupport(dim, detail::positions(particles, dim), (double)rCut),
+          base(particles, own_support, differentialSignature, convergenceOrder, rCut, opt, 0.5),
+          rCutGpu_((double)rCut) {
+        (void)verletList;
+    }
+
+    // the support is rebuilt from the moved particles before re-assembly
+    void initializeUpdate(vector_type& particles) {
+        own_support = detail::build_verlet(dim, detail::positions(particles, dim), nullptr, rCutGpu_, true);
+        base::initializeUpdate(particles);
+    }
+
+private:
+    double rCutGpu_;
 };
 
 // SurfaceDcpse (Dcpse.hpp:829-1085): the support of every particle is

@@ -121,11 +121,15 @@ class _DcpseOp:
     """Common machinery: one plan holding the operator's reference terms."""
 
     _kind = None  # "single" | "sum" | "vector"
+    # True for the *_gpu classes: the terms follow the reference's Dcpse_gpu
+    _gpu_semantics = False
 
     def __init__(self, parts, verletList, ord, rCut, opt=support_options.RADIUS, *, outputs, kind,
                  allow_failed_particles=False, h_over_eps=0.9):
         if opt not in (support_options.RADIUS, support_options.LOAD):
             raise NotImplementedError("support option %r" % (opt,))
+        if self._gpu_semantics:
+            h_over_eps = 0.5  # eps = 2 <h> (Dcpse.cuh:799-807); Dcpse_gpu has no HOverEpsilon
         self.dim = parts.dims
         self.ord = int(ord)
         self.rCut = float(rCut)
@@ -141,7 +145,12 @@ class _DcpseOp:
             self._assemble(parts)
 
     def _prepare(self, parts):
-        """Hand the neighbour list to the plan (before every assembly)."""
+        """Hand the neighbour list to the plan (before every assembly).  A
+        *_gpu operator builds its own support from rCut, as the reference's
+        SupportBuilderGPU does (SupportBuilder.cuh:14-107: |x_p - x_q| <
+        rCut, p excluded), and ignores the list it was given."""
+        if self._gpu_semantics:
+            self.verletList = VerletList(parts, self.rCut)
         self.plan.set_neighbors(self.verletList.rowptr, self.verletList.cols)
 
     def _assemble(self, parts):
@@ -554,11 +563,23 @@ class PPInterpolation:
         self.plan.close()
 
 
-# GPU aliases of the reference (DCPSE_op.hpp:3510-3530) name the same classes
-Derivative_x_gpu, Derivative_y_gpu, Derivative_z_gpu = Derivative_x, Derivative_y, Derivative_z
-Derivative_xx_gpu, Derivative_yy_gpu, Derivative_zz_gpu = Derivative_xx, Derivative_yy, Derivative_zz
-Derivative_xy_gpu, Derivative_yz_gpu, Derivative_xz_gpu = Derivative_xy, Derivative_yz, Derivative_xz
-Laplacian_gpu, Gradient_gpu, Derivative_G_gpu = Laplacian, Gradient, Derivative_G
-Divergence_gpu, Advection_gpu, Curl2D_gpu = Divergence, Advection, Curl2D
-Derivative_xxx_gpu, Derivative_xxy_gpu = Derivative_xxx, Derivative_xxy
-Derivative_yyx_gpu, Derivative_yyy_gpu = Derivative_yyx, Derivative_yyy
+def _gpu_class(cls):
+    """The reference's cls_gpu (DCPSE_op.hpp:3510-3530: cls_T over Dcpse_gpu).
+    Dcpse_gpu (Dcpse.cuh:563-875) differs from Dcpse in what it computes:
+    eps = 2 <h> instead of <h> / 0.9, and the support is built from rCut by
+    the class itself.  Its moment systems are solved by an unpivoted batched
+    LU; here they go through the same column-pivoting QR as every other
+    operator, which gives the same kernels up to the systems' conditioning."""
+    return type(cls.__name__ + "_gpu", (cls,), {"_gpu_semantics": True, "__doc__": _gpu_class.__doc__,
+                                                "__module__": __name__})
+
+
+Derivative_x_gpu, Derivative_y_gpu, Derivative_z_gpu = map(_gpu_class, (Derivative_x, Derivative_y, Derivative_z))
+Derivative_xx_gpu, Derivative_yy_gpu, Derivative_zz_gpu = map(_gpu_class, (Derivative_xx, Derivative_yy,
+                                                                           Derivative_zz))
+Derivative_xy_gpu, Derivative_yz_gpu, Derivative_xz_gpu = map(_gpu_class, (Derivative_xy, Derivative_yz,
+                                                                           Derivative_xz))
+Laplacian_gpu, Gradient_gpu, Derivative_G_gpu = map(_gpu_class, (Laplacian, Gradient, Derivative_G))
+Divergence_gpu, Advection_gpu, Curl2D_gpu = map(_gpu_class, (Divergence, Advection, Curl2D))
+Derivative_xxx_gpu, Derivative_xxy_gpu = map(_gpu_class, (Derivative_xxx, Derivative_xxy))
+Derivative_yyx_gpu, Derivative_yyy_gpu = map(_gpu_class, (Derivative_yyx, Derivative_yyy))

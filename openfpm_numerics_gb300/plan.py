@@ -14,9 +14,13 @@ from . import _capi as C
 
 
 class _DevView:
-    """Zero-copy view of a plan-owned device array for torch.as_tensor."""
+    """Zero-copy view of a plan-owned device array for torch.as_tensor.  The
+    tensor keeps this object, and through ``owner`` the plan, alive: a view
+    never outlives the memory it reads (until the plan is closed explicitly
+    or re-assembled)."""
 
-    def __init__(self, ptr, shape, typestr):
+    def __init__(self, ptr, shape, typestr, owner=None):
+        self.owner = owner
         self.__cuda_array_interface__ = {
             "shape": tuple(int(s) for s in shape),
             "typestr": typestr,
@@ -26,11 +30,11 @@ class _DevView:
         }
 
 
-def _view(ptr, shape, dtype):
+def _view(ptr, shape, dtype, owner=None):
     ts = {torch.float64: "<f8", torch.float32: "<f4", torch.int64: "<i8", torch.int32: "<i4"}[dtype]
     if int(np.prod(shape)) == 0 or not ptr:
         return torch.empty(shape, dtype=dtype, device="cuda")
-    return torch.as_tensor(_DevView(ptr, shape, ts), device="cuda")
+    return torch.as_tensor(_DevView(ptr, shape, ts, owner), device="cuda")
 
 
 def _ptr(t):
@@ -178,7 +182,8 @@ class DcpsePlan:
         rp, cl = ctypes.c_void_p(), ctypes.c_void_p()
         C.call("dcpse_neighbors_ptr", self._h, ctypes.byref(rp), ctypes.byref(cl))
         info = self.info()
-        return (_view(rp.value, (info["n"] + 1,), torch.int64), _view(cl.value, (info["nnz"],), torch.int32))
+        return (_view(rp.value, (info["n"] + 1,), torch.int64, self),
+                _view(cl.value, (info["nnz"],), torch.int32, self))
 
     # -- assembly -------------------------------------------------------
     def assemble(self, pos, flags=C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32, eps_fixed=None,
@@ -198,14 +203,14 @@ class DcpsePlan:
         e, s = ctypes.c_void_p(), ctypes.c_void_p()
         C.call("dcpse_eps_ptr", self._h, ctypes.byref(e), ctypes.byref(s))
         n = self.info()["n"]
-        return _view(e.value, (n,), torch.float64), _view(s.value, (n,), torch.int32)
+        return _view(e.value, (n,), torch.float64, self), _view(s.value, (n,), torch.int32, self)
 
     def term_kernels(self, term):
         k, e = ctypes.c_void_p(), ctypes.c_void_p()
         C.call("dcpse_term_kernels_ptr", self._h, int(term), ctypes.byref(k), ctypes.byref(e))
         info = self.info()
-        K = _view(k.value, (info["nnz"],), torch.float64) if k.value else None
-        return K, _view(e.value, (info["n"],), torch.float64)
+        K = _view(k.value, (info["nnz"],), torch.float64, self) if k.value else None
+        return K, _view(e.value, (info["n"],), torch.float64, self)
 
     def set_term_kernels(self, term, K, eps, eip):
         """Install kernels of one term (Dcpse::load): K [nnz], eps and
@@ -219,8 +224,8 @@ class DcpsePlan:
         w64, w32 = ctypes.c_void_p(), ctypes.c_void_p()
         C.call("dcpse_output_weights_ptr", self._h, int(output), ctypes.byref(w64), ctypes.byref(w32))
         nnz = self.info()["nnz"]
-        return (_view(w64.value, (nnz,), torch.float64) if w64.value else None,
-                _view(w32.value, (nnz,), torch.float32) if w32.value else None)
+        return (_view(w64.value, (nnz,), torch.float64, self) if w64.value else None,
+                _view(w32.value, (nnz,), torch.float32, self) if w32.value else None)
 
     # -- apply ----------------------------------------------------------
     def apply_term_f64(self, term, f, out=None):

@@ -71,6 +71,9 @@ def lib():
         L.orc_assemble.restype = ctypes.c_int64
         L.orc_assemble.argtypes = [ctypes.c_int, _D, ctypes.c_int64, _D, _I64, _I32, _D, _D, _INT, _U,
                                    ctypes.c_uint, ctypes.c_double, _D, _D, _D, _D, _I32, ctypes.c_int]
+        L.orc_assemble_gpu_ref.restype = ctypes.c_int64
+        L.orc_assemble_gpu_ref.argtypes = [ctypes.c_int, _D, ctypes.c_int64, _D, _I64, _I32, _D, _D, _INT, _U,
+                                           ctypes.c_uint, _D, _D, _D, _I32, ctypes.c_int]
         L.orc_apply.argtypes = [ctypes.c_int64, _D, _D, _I64, _I32, _D, _D, ctypes.c_uint, _D, ctypes.c_int]
         L.orc_p2p.argtypes = [ctypes.c_int64, ctypes.c_int, _D, _I64, _I32, _D, _D, _D, ctypes.c_int]
         L.orc_operator_csr.argtypes = [ctypes.c_int64, _I64, _I64, _I32, ctypes.c_int, ctypes.POINTER(_D),
@@ -183,6 +186,25 @@ def assemble(pos, rowptr, cols, sig, order, *, support=None, box=None, h_over_ep
     lib().orc_assemble(dim, _p(pos, _D), n, _p(sup, _D), _p(rowptr, _I64), _p(cols, _I32), _p(lo, _D),
                        _p(hi, _D), _p(per, _INT), _p(sig, _U), order, float(h_over_eps), _p(ef, _D),
                        _p(eps, _D), _p(eip, _D), _p(K, _D), _p(st, _I32), int(nthreads))
+    return eps, eip, K[: int(rowptr[-1])], st
+
+
+def assemble_gpu_ref(pos, rowptr, cols, sig, order, *, box=None, nthreads=1):
+    """One reference Dcpse_gpu object (Dcpse.cuh:776-875): eps = 2 <h>, LU
+    without pivoting; returns (eps, eps_inv_pow, kernels, status)."""
+    pos = _c(pos, np.float64)
+    n, dim = pos.shape
+    rowptr = _c(rowptr, np.int64)
+    cols = _c(cols, np.int32)
+    sig = _c(sig, np.uint32)
+    lo, hi, per = _box(box, dim)
+    eps = np.zeros(n)
+    eip = np.zeros(n)
+    K = np.zeros(max(int(rowptr[-1]), 1))
+    st = np.zeros(n, np.int32)
+    lib().orc_assemble_gpu_ref(dim, _p(pos, _D), n, _p(pos, _D), _p(rowptr, _I64), _p(cols, _I32), _p(lo, _D),
+                               _p(hi, _D), _p(per, _INT), _p(sig, _U), order, _p(eps, _D), _p(eip, _D), _p(K, _D),
+                               _p(st, _I32), int(nthreads))
     return eps, eip, K[: int(rowptr[-1])], st
 
 

@@ -389,6 +389,96 @@ int assemble_one(const AsmCtx& c, int64_t p, double* K, double& eps_out, double&
     return ST_OK;
 }
 
+// The reference's GPU assembly, Dcpse_gpu (src/DCPSE/Dcpse.cuh:776-842,
+// 844-875), for one domain particle p.  Same basis and rhs as the CPU Dcpse;
+// what differs:
+//  * eps = 2 * (sum over neighbours and axes of |x_pq,d|) / k, one running
+//    sum (FACTOR = 2, :799-807); epsInvPow = 1 / pow(eps, |alpha|);
+//  * V_qj = m_j(x_pq) / pow(eps, |m_j|), monomials by pow per axis
+//    (Monomial.cuh:156-163); E_qq = exp(-|x_pq|^2 / (2 eps^2));
+//  * A = B^T B by plain sums, then LU WITHOUT pivoting (cublas<t>getrfBatched
+//    with a null pivot array, Dcpse.cuh:683) and the two triangular solves
+//    (lower unit, upper non-unit, :690-691), here as Doolittle elimination in
+//    textbook order;
+//  * K_q = sum_i a_i m_i(x_pq / eps) exp(-|x_pq / eps|^2), the exponential
+//    multiplied into every term (:865-871).
+// libm exp and pow are used as they are: this form is compared with the
+// engine within a tolerance, not bit for bit.
+int assemble_one_gpu_ref(const AsmCtx& c, int64_t p, double* K, double& eps_out, double& eip_out) {
+    const int dim = c.dim;
+    const int64_t beg = c.rowptr[p];
+    const int k = (int)(c.rowptr[p + 1] - beg);
+    const int n = c.B.n;
+    std::vector<double> X((size_t)k * dim);
+    for (int q = 0; q < k; ++q) {
+        const double* xq = c.ps + (size_t)c.cols[beg + q] * dim;
+        for (int d = 0; d < dim; ++d) X[(size_t)q * dim + d] = offset1(c.g, d, c.pd[(size_t)p * dim + d], xq[d]);
+    }
+    for (int q = 0; q < k; ++q) K[q] = 0.0;
+    double s = 0.0;
+    for (int q = 0; q < k; ++q)
+        for (int d = 0; d < dim; ++d) s = s + std::fabs(X[(size_t)q * dim + d]);
+    s = s / (double)k;
+    const double eps = 2.0 * s;
+    eps_out = eps;
+    eip_out = 1.0 / std::pow(eps, (double)c.ord);
+    if (k < n) return ST_TOO_FEW;
+    if (!(eps > 0.0) || !std::isfinite(eps)) return ST_BAD_EPS;
+    auto mono_pow = [&](int j, const double* x) {
+        double r = (double)c.B.scalars[j];
+        for (int d = 0; d < dim; ++d) r = r * std::pow(x[d], (double)c.B.exps[j * dim + d]);
+        return r;
+    };
+    std::vector<double> Bm((size_t)k * n);
+    for (int q = 0; q < k; ++q) {
+        const double* x = &X[(size_t)q * dim];
+        const double e = std::exp(-norm2(dim, x) / (2.0 * eps * eps));
+        for (int j = 0; j < n; ++j) {
+            unsigned order = 0;
+            for (int d = 0; d < dim; ++d) order += c.B.exps[j * dim + d];
+            Bm[(size_t)q * n + j] = e * (mono_pow(j, x) / std::pow(eps, (double)order));
+        }
+    }
+    std::vector<double> A((size_t)n * n);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            double acc = 0.0;
+            for (int q = 0; q < k; ++q) acc = acc + Bm[(size_t)q * n + i] * Bm[(size_t)q * n + j];
+            A[(size_t)i * n + j] = acc;
+        }
+    // LU without pivoting: A = L U, L unit lower (multipliers below the diagonal)
+    for (int col = 0; col < n; ++col) {
+        const double piv = A[(size_t)col * n + col];
+        if (piv == 0.0 || !std::isfinite(piv)) return ST_SINGULAR;
+        for (int r = col + 1; r < n; ++r) {
+            const double l = A[(size_t)r * n + col] / piv;
+            A[(size_t)r * n + col] = l;
+            for (int j = col + 1; j < n; ++j) A[(size_t)r * n + j] = A[(size_t)r * n + j] - l * A[(size_t)col * n + j];
+        }
+    }
+    std::vector<double> a(c.b);
+    for (int r = 1; r < n; ++r)
+        for (int j = 0; j < r; ++j) a[r] = a[r] - A[(size_t)r * n + j] * a[j];
+    for (int r = n - 1; r >= 0; --r) {
+        for (int j = r + 1; j < n; ++j) a[r] = a[r] - A[(size_t)r * n + j] * a[j];
+        a[r] = a[r] / A[(size_t)r * n + r];
+    }
+    std::vector<double> u(dim);
+    for (int q = 0; q < k; ++q) {
+        for (int d = 0; d < dim; ++d) u[d] = X[(size_t)q * dim + d] / eps;
+        const double ef = std::exp(-norm2(dim, u.data()));
+        double res = 0.0;
+        for (int i = 0; i < n; ++i) res = res + a[i] * mono_pow(i, u.data()) * ef;
+        K[q] = res;
+    }
+    for (int q = 0; q < k; ++q)
+        if (!std::isfinite(K[q])) {
+            for (int r = 0; r < k; ++r) K[r] = 0.0;
+            return ST_NONFINITE;
+        }
+    return ST_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -606,6 +696,43 @@ int64_t orc_assemble(int dim, const double* pd, int64_t n_dom, const double* ps,
             nb += (st != 0);
         }
         // accumulate without a lock: one slot per range start
+        __atomic_fetch_add(&bad[0], nb, __ATOMIC_RELAXED);
+    });
+    return bad[0];
+}
+
+// Dcpse_gpu's assembly (Dcpse.cuh:776-875) of one reference Dcpse_gpu object
+// over the given lists; same arguments and outputs as orc_assemble, without
+// h_over_eps and eps_fixed (the GPU class has neither).
+int64_t orc_assemble_gpu_ref(int dim, const double* pd, int64_t n_dom, const double* ps, const int64_t* rowptr,
+                             const int32_t* cols, const double* box_lo, const double* box_hi, const int* periodic,
+                             const unsigned* sig, unsigned order, double* eps, double* eps_inv_pow, double* kernels,
+                             int32_t* status, int nthreads) {
+    AsmCtx c;
+    c.dim = dim;
+    c.pd = pd;
+    c.ps = ps;
+    c.rowptr = rowptr;
+    c.cols = cols;
+    c.g = make_geom(dim, box_lo, box_hi, periodic);
+    c.B = make_basis(dim, sig, order);
+    c.b.resize(c.B.n);
+    make_rhs(c.B, sig, c.b.data());
+    c.ord = 0;
+    for (int d = 0; d < dim; ++d) c.ord += sig[d];
+    c.hoe = 0.5;
+    c.eps_fixed = nullptr;
+    std::vector<int64_t> bad(1, 0);
+    parallel_for(n_dom, nthreads, [&](int64_t b, int64_t e) {
+        int64_t nb = 0;
+        for (int64_t p = b; p < e; ++p) {
+            double ep, eip;
+            int st = assemble_one_gpu_ref(c, p, kernels + rowptr[p], ep, eip);
+            eps[p] = ep;
+            eps_inv_pow[p] = eip;
+            status[p] = st;
+            nb += (st != 0);
+        }
         __atomic_fetch_add(&bad[0], nb, __ATOMIC_RELAXED);
     });
     return bad[0];

@@ -24,6 +24,10 @@ int64_t orc_assemble(int dim, const double* pd, int64_t n_dom, const double* ps,
                      const int32_t* cols, const double* box_lo, const double* box_hi, const int* periodic,
                      const unsigned* sig, unsigned order, double h_over_eps, const double* eps_fixed, double* eps,
                      double* eps_inv_pow, double* kernels, int32_t* status, int nthreads);
+int64_t orc_assemble_gpu_ref(int dim, const double* pd, int64_t n_dom, const double* ps, const int64_t* rowptr,
+                             const int32_t* cols, const double* box_lo, const double* box_hi, const int* periodic,
+                             const unsigned* sig, unsigned order, double* eps, double* eps_inv_pow, double* kernels,
+                             int32_t* status, int nthreads);
 void orc_apply(int64_t n_dom, const double* f_sup, const double* f_dom, const int64_t* rowptr, const int32_t* cols,
                const double* kernels, const double* eps_inv_pow, unsigned diff_order, double* out, int nthreads);
 void orc_p2p(int64_t n_dom, int ncomp, const double* f_sup, const int64_t* rowptr, const int32_t* cols,
@@ -388,6 +392,95 @@ static void test_surface_operators() {
     pp.deallocate();
 }
 
+// DCPSE_op_test_base_tests.cu:29-99 (dcpse_op_tests): the *_gpu operators,
+// v = 2 Dx(P) + Dy(P) on 80^2 over [0, 2 pi]^2, rCut 3.9h, worst < 0.03; and
+// :101-175 (dcpse_op_test_lap): Laplacian_gpu on 163^2, worst < 0.3.  The
+// Dcpse_gpu class equals Dcpse with HOverEpsilon = 0.5 on the list from rCut
+// bit for bit, and the oracle's restatement of the reference's own GPU
+// assembly (eps = 2 <h>, LU without pivoting) within the systems' conditioning.
+static void test_gpu_aliases() {
+    {
+        const int nside = 80;
+        const double h = 2 * M_PI / (nside - 1), rCut = 3.9 * h;
+        Parts2 domain = lattice2(nside, h);
+        for (std::size_t p = 0; p < domain.size_local(); ++p) {
+            double x = domain.getPos(p)[0], y = domain.getPos(p)[1];
+            domain.getProp<0>(p) = std::sin(x) + std::sin(y);
+            domain.getProp<2>(p) = 2 * std::cos(x) + std::cos(y);
+        }
+        VerletList vl = getVerlet(domain, rCut);
+        Derivative_x_gpu<VerletList> Dx(domain, vl, 2, rCut);
+        Derivative_y_gpu<VerletList> Dy(domain, vl, 2, rCut);
+        Gradient_gpu<VerletList> Grad(domain, vl, 2, rCut);
+        Laplacian_gpu<VerletList> Lap(domain, vl, 2, rCut);
+        getV<1>(domain) = 2 * Dx(getV<0>(domain)) + Dy(getV<0>(domain));
+        double worst = 0;
+        for (std::size_t p = 0; p < domain.size_local(); ++p)
+            worst = std::max(worst, std::fabs(domain.getProp<1>(p) - domain.getProp<2>(p)));
+        EXPECT(worst < 0.03, "_gpu operators: 2 Dx + Dy worst < 0.03");
+    }
+    {
+        const int nside = 163;
+        const double h = 2 * M_PI / (nside - 1), rCut = 3.9 * h;
+        Parts2 domain = lattice2(nside, h);
+        for (std::size_t p = 0; p < domain.size_local(); ++p) {
+            double x = domain.getPos(p)[0], y = domain.getPos(p)[1];
+            domain.getProp<0>(p) = std::sin(x) + std::sin(y);
+            domain.getProp<1>(p) = -std::sin(x) - std::sin(y);
+        }
+        VerletList vl = getVerlet(domain, rCut);
+        Laplacian_gpu<VerletList> Lap(domain, vl, 2, rCut);
+        getV<2>(domain) = Lap(getV<0>(domain));
+        double worst = 0;
+        for (std::size_t p = 0; p < domain.size_local(); ++p)
+            worst = std::max(worst, std::fabs(domain.getProp<1>(p) - domain.getProp<2>(p)));
+        EXPECT(worst < 0.3, "Laplacian_gpu worst < 0.3");
+    }
+    {
+        const int nside = 30;
+        const double h = 1.0 / (nside - 1), rCut = 3.1 * h;
+        Parts2 domain = lattice2(nside, h);
+        std::mt19937 rng(21);
+        std::uniform_real_distribution<double> jit(-0.15 * h, 0.15 * h);
+        for (std::size_t p = 0; p < domain.size_local(); ++p) {
+            domain.getPos(p)[0] += jit(rng);
+            domain.getPos(p)[1] += jit(rng);
+            domain.getProp<0>(p) = std::sin(3 * domain.getPos(p)[0]) * domain.getPos(p)[1];
+        }
+        VerletList unused;  // Dcpse_gpu builds its support from rCut
+        VerletList vl = getVerlet(domain, rCut);
+        const std::size_t n = domain.size_local();
+        for (unsigned sx = 1; sx <= 2; ++sx) {
+            Dcpse_gpu<2, VerletList, Parts2> g(domain, unused, Point<2, unsigned>({sx, 0}), 2, rCut);
+            Dcpse<2, VerletList, Parts2> c(domain, vl, Point<2, unsigned>({sx, 0}), 2, rCut);
+            c.HOverEpsilon = 0.5;
+            c.initializeUpdate(domain);
+            bool same = true;
+            for (std::size_t p = 0; p < n; p += 7) {
+                vect_dist_key_dx key(p);
+                same &= g.getNumNN(key) == c.getNumNN(key) && g.getEpsilonInvPrefactor(key) == c.getEpsilonInvPrefactor(key);
+                for (int j = 0; j < g.getNumNN(key); ++j) same &= g.getCoeffNN(key, j) == c.getCoeffNN(key, j);
+            }
+            EXPECT(same, "Dcpse_gpu equals Dcpse with HOverEpsilon 0.5 bit for bit");
+            std::vector<double> eps(n), eip(n), K(vl.cols.size());
+            std::vector<int32_t> st(n);
+            unsigned sig[2] = {sx, 0};
+            orc_assemble_gpu_ref(2, domain.posData(), (int64_t)n, domain.posData(), vl.rowptr.data(), vl.cols.data(),
+                                 nullptr, nullptr, nullptr, sig, 2, eps.data(), eip.data(), K.data(), st.data(), 1);
+            double kmax = 0, err = 0, eerr = 0;
+            for (std::size_t p = 0; p < n; ++p) {
+                vect_dist_key_dx key(p);
+                eerr = std::max(eerr, std::fabs(g.getEpsilonInvPrefactor(key) / eip[p] - 1));
+                for (int j = 0; j < g.getNumNN(key); ++j) {
+                    kmax = std::max(kmax, std::fabs(K[vl.rowptr[p] + j]));
+                    err = std::max(err, std::fabs(g.getCoeffNN(key, j) - K[vl.rowptr[p] + j]));
+                }
+            }
+            EXPECT(eerr < 1e-14 && err <= 1e-9 * kmax, "Dcpse_gpu kernels match the reference's GPU assembly");
+        }
+    }
+}
+
 int main() {
     try {
         test_dcpse_class();
@@ -398,6 +491,7 @@ int main() {
         test_interpolation_two_sets();
         test_vector_operators();
         test_surface_operators();
+        test_gpu_aliases();
     } catch (const std::exception& e) {
         std::printf("FAIL exception: %s\n", e.what());
         return 2;

@@ -383,3 +383,29 @@ def test_advection_reference_bar(orc):
         adv = adv + v[:, i] * orc.apply(P, rp, cols, ops[i][3], ops[i][2], 1, nthreads=os.cpu_count())
     exact = np.cos(x) * (np.sin(x) + np.sin(y)) + np.cos(y) * (np.cos(x) + np.cos(y))
     assert np.max(np.abs(adv - exact)) < 0.03
+
+
+@pytest.mark.parametrize("dim,nside,sigs,bar", [(2, 24, [(1, 0), (2, 0), (1, 1)], 1e-9),
+                                                (3, 10, [(1, 0, 0), (0, 2, 0)], 1e-6)])
+def test_gpu_assembly_is_the_operator_with_eps_2h(orc, dim, nside, sigs, bar):
+    """The reference's GPU assembly (Dcpse_gpu, Dcpse.cuh:776-875: eps =
+    2 <h>, V = m(x)/eps^|m|, unpivoted LU) restated in the oracle gives the
+    same operator as the CPU Dcpse with HOverEpsilon = 0.5: eps to a few ulp,
+    kernels and derivatives within the conditioning of the moment systems
+    (1e-9 normwise in 2D, 1e-6 for 3D second derivatives); the CPU default
+    (HOverEpsilon 0.9) is a different operator."""
+    pos, h = W.lattice(nside, dim, jitter=0.15, seed=5)
+    rp, cols = orc.neighbors(pos, (3.1 if dim == 2 else 2.8) * h)
+    f = np.sin(3 * pos[:, 0]) + pos[:, -1] ** 2
+    for sig in sigs:
+        e1, i1, K1, s1 = orc.assemble(pos, rp, cols, sig, 2, h_over_eps=0.5)
+        e2, i2, K2, s2 = orc.assemble_gpu_ref(pos, rp, cols, sig, 2)
+        assert (s1 == 0).all() and (s2 == 0).all()
+        assert np.abs(e1 / e2 - 1).max() < 1e-14 and np.abs(i1 / i2 - 1).max() < 1e-14
+        assert np.abs(K1 - K2).max() <= bar * np.abs(K1).max()
+        d1 = orc.apply(f, rp, cols, K1, i1, sum(sig))
+        d2 = orc.apply(f, rp, cols, K2, i2, sum(sig))
+        assert np.abs(d1 - d2).max() <= 10 * bar * np.abs(d1).max()
+        e3, _, K3, _ = orc.assemble(pos, rp, cols, sig, 2)
+        assert np.allclose(e3 * 0.9 * 2, e1, rtol=1e-14)
+        assert np.abs(K3 - K1).max() > 1e-3 * np.abs(K1).max()
