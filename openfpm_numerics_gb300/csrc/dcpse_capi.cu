@@ -897,8 +897,10 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     int32_t *cell = nullptr, *ccount = nullptr, *cidx = nullptr, *counts = nullptr, *tmp = nullptr;
     int64_t *cstart = nullptr, *fill = nullptr, *scan_tmp = nullptr;
     double* spos = nullptr;
+    float4* srel = nullptr;
     int* maxk = nullptr;
     auto cleanup = [&]() {
+        dfree(srel);
         dfree(cell);
         dfree(ccount);
         dfree(cidx);
@@ -919,9 +921,11 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     if (e == cudaSuccess) e = dalloc(&fill, ncell);
     if (e == cudaSuccess) e = dalloc(&scan_tmp, scan_tmp_elems(std::max<int64_t>(ncell, n)));
     if (e == cudaSuccess) e = dalloc(&spos, (size_t)ns * dim);
+    if (e == cudaSuccess) e = dalloc(&srel, (size_t)std::max<int64_t>(ns, 1));
     if (e == cudaSuccess) e = dalloc(&maxk, 1);
     if (e == cudaSuccess) e = cudaMemsetAsync(maxk, 0, sizeof(int), s);
-    if (e == cudaSuccess) e = build_cells(dim, ps, ns, cg, cell, ccount, cstart, fill, cidx, spos, scan_tmp, s);
+    P->tstart(DCPSE_K_NEIGHBORS);
+    if (e == cudaSuccess) e = build_cells(dim, ps, ns, cg, cell, ccount, cstart, fill, cidx, spos, srel, scan_tmp, s);
     NbrArgs a{};
     a.dim = dim;
     a.pd = d_pos;
@@ -934,6 +938,18 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     a.rcut = rcut;
     a.rcut_pp = d_rcut_pp;
     a.self_skip = P->two_set() ? 0 : P->self_skip;
+    a.srel = srel;
+    // FP32 classification margin 2^-14 S^2, S = 3 x the largest cell side;
+    // a periodic axis with fewer than three cells lists a cell under several
+    // images, which only the FP64 test tells apart
+    {
+        double S = 0.0;
+        for (int d = 0; d < dim; ++d) S = std::max(S, 3.0 * cg.cs[d]);
+        a.band = std::ldexp(S * S, -14);
+        a.fast = 1;
+        for (int d = 0; d < dim; ++d)
+            if (P->per[d] && cg.nc[d] < 3) a.fast = 0;
+    }
     if (e == cudaSuccess) e = count_neighbors(a, counts, maxk, s);
     if (e == cudaSuccess) e = exclusive_scan_i32(counts, n, P->rowptr, scan_tmp, s);
     int64_t nnz = 0;
@@ -944,6 +960,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     if (e == cudaSuccess) e = dalloc(&tmp, nnz);
     if (e == cudaSuccess) e = dalloc(&P->cols, nnz + kPad);
     if (e == cudaSuccess) e = fill_neighbors(a, P->rowptr, tmp, P->cols, s);
+    P->tstop(DCPSE_K_NEIGHBORS);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cleanup();
     if (e != cudaSuccess) return fail(DCPSE_ERR_CUDA, std::string("neighbour build: ") + cudaGetErrorString(e));

@@ -29,16 +29,19 @@ cudaError_t bounding_box(int dim, const double* a, int64_t na, const double* b, 
                          double* hi, unsigned long long* d_tmp /* 2*kMaxDim */, cudaStream_t s);
 
 // Cell list of the support set: cell_start[ncell+1], cidx[n], spos[n*dim]
-// (positions in cell order).  d_cell (n) and d_fill (ncell) are scratch.
+// (positions in cell order) and srel[n] (FP32 offsets from the cell's lower
+// corner, NaN for particles outside the grid).  d_cell (n) and d_fill
+// (ncell) are scratch.
 cudaError_t build_cells(int dim, const double* pos, int64_t n, const CellGrid& g, int32_t* d_cell,
                         int32_t* d_ccount, int64_t* d_cstart, int64_t* d_fill, int32_t* d_cidx, double* d_spos,
-                        int64_t* d_scan_tmp, cudaStream_t s);
+                        float4* d_srel, int64_t* d_scan_tmp, cudaStream_t s);
 
 struct NbrArgs {
     int dim;
     const double* pd;   // domain positions
     int64_t n_dom;
     const double* spos; // support positions, cell order
+    const float4* srel; // the same, FP32 offsets from the cell's lower corner
     const int32_t* cidx;
     const int64_t* cstart;
     CellGrid cells;
@@ -46,6 +49,8 @@ struct NbrArgs {
     double rcut;
     const double* rcut_pp;
     int self_skip;
+    double band;        // |d^2 - rc^2| below this: decided in FP64
+    int fast;           // 0: FP64 for every candidate
 };
 
 // Count pass: counts[p] = number of neighbours; also atomically maxes *d_maxk.

@@ -10,6 +10,16 @@
 // The list of particle p is every q != p with |x_p - x_q|^2 < rc_p^2 in
 // ascending q, so it does not depend on the cell size or on the order in
 // which atomics filled the cells.
+//
+// The FP64 predicate is what defines the list, but GB300's FP64 pipe (2
+// lanes per cycle per SM) makes it the bottleneck when it runs on every
+// candidate.  Candidates are therefore first classified in FP32 from
+// positions stored relative to their cell's lower corner: |d^2 - rc^2| below
+// a margin of 2^-14 S^2 (S = 3 x the largest cell side; the FP32 error of d^2
+// is below 100 u S^2 = 6e-6 S^2 for |x - corner| <= S) is decided by the
+// FP64 predicate itself, as are particles outside the grid, NaN positions
+// and periodic axes with fewer than three cells.  The lists are the same bit
+// for bit.
 #include <cstring>
 
 #include "dcpse_internal.h"
@@ -158,17 +168,29 @@ __global__ void cell_id_kernel(int dim, const double* __restrict__ pos, int64_t 
 }
 
 __global__ void cell_fill_kernel(int dim, const double* __restrict__ pos, int64_t n, const int32_t* __restrict__ cell,
-                                 int64_t* fill, int32_t* __restrict__ cidx, double* __restrict__ spos) {
+                                 CellGrid g, int64_t* fill, int32_t* __restrict__ cidx, double* __restrict__ spos,
+                                 float4* __restrict__ srel) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         unsigned long long slot = atomicAdd((unsigned long long*)&fill[cell[i]], 1ull);
         cidx[slot] = (int32_t)i;
-        for (int d = 0; d < dim; ++d) spos[slot * dim + d] = pos[i * dim + d];
+        float r[kMaxDim] = {0.f, 0.f, 0.f};
+        for (int d = 0; d < dim; ++d) {
+            const double x = pos[i * dim + d];
+            spos[slot * dim + d] = x;
+            // offset from the cell's lower corner; NaN (always the FP64
+            // test) for a particle clamped into an edge cell
+            const int c = cell_coord(x, g.lo[d], g.cs[d], g.nc[d]);
+            const double rel = x - (g.lo[d] + (double)c * g.cs[d]);
+            r[d] = (rel >= -0.5 * g.cs[d] && rel <= 1.5 * g.cs[d]) ? (float)rel : __int_as_float(0x7fc00000);
+        }
+        srel[slot] = make_float4(r[0], r[1], r[2], 0.f);
     }
 }
 
 // Stencil cells of particle p along one axis (deduplicated when a periodic
-// axis has fewer than three cells).
-__device__ __forceinline__ int axis_cells(int c, int nc, int per, int* out) {
+// axis has fewer than three cells); unw receives each cell's index before
+// the periodic wrap, whose lower corner is that of the image next to p.
+__device__ __forceinline__ int axis_cells(int c, int nc, int per, int* out, int* unw) {
     int cnt = 0;
     for (int o = -1; o <= 1; ++o) {
         int v = c + o;
@@ -179,7 +201,10 @@ __device__ __forceinline__ int axis_cells(int c, int nc, int per, int* out) {
         }
         bool dup = false;
         for (int t = 0; t < cnt; ++t) dup |= (out[t] == v);
-        if (!dup) out[cnt++] = v;
+        if (!dup) {
+            unw[cnt] = c + o;
+            out[cnt++] = v;
+        }
     }
     return cnt;
 }
@@ -197,13 +222,24 @@ __global__ void __launch_bounds__(256) nbr_kernel(NbrArgs a, int32_t* __restrict
         for (int d = 0; d < DIM; ++d) xp[d] = a.pd[p * DIM + d];
         const double rc = a.rcut_pp ? a.rcut_pp[p] : a.rcut;
         const double rc2 = rc * rc;
-        int lst[3][3];
+        // FP32 decisions: inside below thr_in, outside above thr_out
+        const float thr_in = (float)(rc2 - a.band), thr_out = (float)(rc2 + a.band);
+        int lst[3][3], unw[3][3];
+        float rpf[3][3];    // x_p - corner of each stencil cell, per axis
+        bool rpok[3][3];    // |x_p - corner| <= 3 cell sides (else FP64 only)
         int cnt[3] = {1, 1, 1};
         lst[0][0] = lst[1][0] = lst[2][0] = 0;
+        rpf[0][0] = rpf[1][0] = rpf[2][0] = 0.f;
+        rpok[0][0] = rpok[1][0] = rpok[2][0] = true;
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
             int c = cell_coord(xp[d], a.cells.lo[d], a.cells.cs[d], a.cells.nc[d]);
-            cnt[d] = axis_cells(c, a.cells.nc[d], a.geom.per[d], lst[d]);
+            cnt[d] = axis_cells(c, a.cells.nc[d], a.geom.per[d], lst[d], unw[d]);
+            for (int t = 0; t < cnt[d]; ++t) {
+                const double rp = xp[d] - (a.cells.lo[d] + (double)unw[d][t] * a.cells.cs[d]);
+                rpf[d][t] = (float)rp;
+                rpok[d][t] = a.fast && fabs(rp) <= 3.0 * a.cells.cs[d];
+            }
         }
         int64_t base = FILL ? rowptr[p] : 0;
         const int64_t cap = FILL ? rowptr[p + 1] - base : 0;  // the count pass's result
@@ -213,16 +249,33 @@ __global__ void __launch_bounds__(256) nbr_kernel(NbrArgs a, int32_t* __restrict
                 for (int a0 = 0; a0 < cnt[0]; ++a0) {
                     int cc = lst[0][a0] + a.cells.nc[0] * (lst[1][a1] + a.cells.nc[1] * lst[2][a2]);
                     int64_t cb = a.cstart[cc], ce = a.cstart[cc + 1];
+                    const bool fast = rpok[0][a0] && rpok[1][a1] && rpok[2][a2];
+                    const float r0 = rpf[0][a0], r1 = rpf[1][a1], r2 = rpf[2][a2];
                     for (int64_t t0 = cb; t0 < ce; t0 += 32) {
                         int64_t t = t0 + lane;
                         bool acc = false;
                         int32_t q = -1;
                         if (t < ce) {
                             q = a.cidx[t];
-                            double o[DIM];
+                            const float4 rq = a.srel[t];
+                            const float o0 = r0 - rq.x;
+                            float d2 = o0 * o0;
+                            if (DIM > 1) {
+                                const float o1 = r1 - rq.y;
+                                d2 = fmaf(o1, o1, d2);
+                            }
+                            if (DIM > 2) {
+                                const float o2 = r2 - rq.z;
+                                d2 = fmaf(o2, o2, d2);
+                            }
+                            if (fast && d2 < thr_in) {
+                                acc = true;
+                            } else if (!(fast && d2 > thr_out)) {  // the band, NaN, or no FP32 decision
+                                double o[DIM];
 #pragma unroll
-                            for (int d = 0; d < DIM; ++d) o[d] = offset1(a.geom, d, xp[d], a.spos[t * DIM + d]);
-                            acc = norm2<DIM>(o) < rc2;
+                                for (int d = 0; d < DIM; ++d) o[d] = offset1(a.geom, d, xp[d], a.spos[t * DIM + d]);
+                                acc = norm2<DIM>(o) < rc2;
+                            }
                             if (a.self_skip && (int64_t)q == p) acc = false;
                         }
                         unsigned bal = __ballot_sync(0xffffffffu, acc);
@@ -317,8 +370,8 @@ cudaError_t bounding_box(int dim, const double* a, int64_t na, const double* b, 
 }
 
 cudaError_t build_cells(int dim, const double* pos, int64_t n, const CellGrid& g, int32_t* d_cell, int32_t* d_ccount,
-                        int64_t* d_cstart, int64_t* d_fill, int32_t* d_cidx, double* d_spos, int64_t* d_scan_tmp,
-                        cudaStream_t s) {
+                        int64_t* d_cstart, int64_t* d_fill, int32_t* d_cidx, double* d_spos, float4* d_srel,
+                        int64_t* d_scan_tmp, cudaStream_t s) {
     int64_t ncell = (int64_t)g.nc[0] * g.nc[1] * g.nc[2];
     cudaError_t e = cudaMemsetAsync(d_ccount, 0, sizeof(int32_t) * ncell, s);
     if (e != cudaSuccess) return e;
@@ -327,7 +380,8 @@ cudaError_t build_cells(int dim, const double* pos, int64_t n, const CellGrid& g
     if (e != cudaSuccess) return e;
     e = cudaMemcpyAsync(d_fill, d_cstart, sizeof(int64_t) * ncell, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
-    if (n > 0) cell_fill_kernel<<<grid_for(n, 256), 256, 0, s>>>(dim, pos, n, d_cell, d_fill, d_cidx, d_spos);
+    if (n > 0)
+        cell_fill_kernel<<<grid_for(n, 256), 256, 0, s>>>(dim, pos, n, d_cell, g, d_fill, d_cidx, d_spos, d_srel);
     return cudaGetLastError();
 }
 

@@ -49,10 +49,24 @@ def _case(name):
     if name == "2d_sparse":
         pos, h = W.lattice(14, 2, jitter=0.2, seed=17)
         return dict(pos=pos, rcut=2.05 * h, outputs=[[(1, 0)], [(2, 0), (0, 2)]], order=2)
+    if name == "2d_lattice_tie":
+        # candidates exactly on the cutoff (distance 5h = |(5, 0)h| = |(3, 4)h|
+        # on an exact lattice): the FP32 pre-filter leaves them to the FP64
+        # predicate
+        pos, h = W.lattice(16, 2)
+        return dict(pos=pos, rcut=5.0 * h, outputs=[[(1, 0)], [(2, 0), (0, 2)]], order=2)
+    if name == "2d_periodic_2cells":
+        # two cells per periodic axis: every candidate takes the FP64 test
+        h = 1.0 / 8
+        pos, _ = W.lattice(8, 2, h=h, jitter=0.1, seed=18)
+        pos = np.mod(pos, 1.0)
+        return dict(pos=pos, rcut=2.8 * h, outputs=[[(1, 0)], [(2, 0), (0, 2)]], order=2,
+                    box=((0.0, 0.0), (1.0, 1.0), (1, 1)))
     raise KeyError(name)
 
 
-CASES = ["2d", "3d", "3d_periodic", "2d_lattice", "2d_order3", "2d_adaptive", "2d_hoe05", "2d_sparse"]
+CASES = ["2d", "3d", "3d_periodic", "2d_lattice", "2d_order3", "2d_adaptive", "2d_hoe05", "2d_sparse",
+         "2d_lattice_tie", "2d_periodic_2cells"]
 
 
 def _build(c, flags=C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32):
