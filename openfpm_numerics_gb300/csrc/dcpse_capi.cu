@@ -946,6 +946,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
         double S = 0.0;
         for (int d = 0; d < dim; ++d) S = std::max(S, 3.0 * cg.cs[d]);
         a.band = std::ldexp(S * S, -14);
+        for (int d = 0; d < 3; ++d) a.csf[d] = d < dim ? (float)cg.cs[d] : 0.f;
         a.fast = 1;
         for (int d = 0; d < dim; ++d)
             if (P->per[d] && cg.nc[d] < 3) a.fast = 0;

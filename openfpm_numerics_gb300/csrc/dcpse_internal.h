@@ -51,6 +51,7 @@ struct NbrArgs {
     int self_skip;
     double band;        // |d^2 - rc^2| below this: decided in FP64
     int fast;           // 0: FP64 for every candidate
+    float csf[3];       // cell sides in FP32
 };
 
 // Count pass: counts[p] = number of neighbours; also atomically maxes *d_maxk.

@@ -15,8 +15,9 @@
 // lanes per cycle per SM) makes it the bottleneck when it runs on every
 // candidate.  Candidates are therefore first classified in FP32 from
 // positions stored relative to their cell's lower corner: |d^2 - rc^2| below
-// a margin of 2^-14 S^2 (S = 3 x the largest cell side; the FP32 error of d^2
-// is below 100 u S^2 = 6e-6 S^2 for |x - corner| <= S) is decided by the
+// a margin of 2^-14 S^2 (S = 3 x the largest cell side; with both offsets
+// from the corner below S, the FP32 error of d^2 stays below 200 u S^2 =
+// 1.2e-5 S^2, u = 2^-24, corner offsets of the +-1 cells included) is decided by the
 // FP64 predicate itself, as are particles outside the grid, NaN positions
 // and periodic axes with fewer than three cells.  The lists are the same bit
 // for bit.
@@ -187,28 +188,69 @@ __global__ void cell_fill_kernel(int dim, const double* __restrict__ pos, int64_
     }
 }
 
-// Stencil cells of particle p along one axis (deduplicated when a periodic
-// axis has fewer than three cells); unw receives each cell's index before
-// the periodic wrap, whose lower corner is that of the image next to p.
-__device__ __forceinline__ int axis_cells(int c, int nc, int per, int* out, int* unw) {
-    int cnt = 0;
-    for (int o = -1; o <= 1; ++o) {
-        int v = c + o;
-        if (per) {
-            v = ((v % nc) + nc) % nc;
-        } else if (v < 0 || v >= nc) {
+// The stencil of one domain particle: along each axis the centre cell c and
+// three slots for the cells at offsets -1, 0, +1.  A slot is dropped outside
+// a non-periodic grid, or when a periodic axis of fewer than three cells
+// would list a cell twice.  rpc = x_p minus the lower corner of the centre
+// cell; the corner of slot t (before the periodic wrap, i.e. of the image
+// next to p) is (t - 1) cell sides further.
+struct Stencil {
+    int c[3];
+    float rpc[3];
+    unsigned valid;  // bit 3 d + t: slot t of axis d is a cell
+    unsigned fast;   // bit 3 d + t: |x_p - corner| <= 3 cell sides, FP32 classification allowed
+};
+
+template <int DIM>
+__device__ __forceinline__ void make_stencil(const NbrArgs& a, const double* xp, Stencil& S) {
+    S.valid = 0;
+    S.fast = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        S.c[d] = 0;
+        S.rpc[d] = 0.f;
+        if (d >= DIM) {
+            S.valid |= 1u << (3 * d + 1);
+            S.fast |= 1u << (3 * d + 1);
             continue;
         }
-        bool dup = false;
-        for (int t = 0; t < cnt; ++t) dup |= (out[t] == v);
-        if (!dup) {
-            unw[cnt] = c + o;
-            out[cnt++] = v;
+        const int nc = a.cells.nc[d];
+        const int c = cell_coord(xp[d], a.cells.lo[d], a.cells.cs[d], nc);
+        S.c[d] = c;
+        S.rpc[d] = (float)(xp[d] - (a.cells.lo[d] + (double)c * a.cells.cs[d]));
+        int w[3];
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            const int u = c + t - 1;
+            bool ok = true;
+            w[t] = u;
+            if (a.geom.per[d]) {
+                w[t] = ((u % nc) + nc) % nc;
+#pragma unroll
+                for (int t2 = 0; t2 < t; ++t2)
+                    if (((S.valid >> (3 * d + t2)) & 1u) && w[t2] == w[t]) ok = false;
+            } else if (u < 0 || u >= nc) {
+                ok = false;
+            }
+            const double rp = xp[d] - (a.cells.lo[d] + (double)u * a.cells.cs[d]);
+            if (ok) S.valid |= 1u << (3 * d + t);
+            if (ok && a.fast && fabs(rp) <= 3.0 * a.cells.cs[d]) S.fast |= 1u << (3 * d + t);
         }
     }
-    return cnt;
 }
 
+// cell index of slot t around centre c along an axis (wrapped when periodic)
+__device__ __forceinline__ int slot_cell(int c, int t, int nc, int per) {
+    int v = c + t - 1;
+    if (per) v = v < 0 ? v + nc : (v >= nc ? v - nc : v);
+    return v;
+}
+
+// One warp per domain particle scans the 3^d stencil cells of the support
+// cell list, 32 candidates at a time.  The per-particle set-up (cells,
+// corner offsets, thresholds: FP64 work) is done one lane per particle for
+// 32 particles at once and broadcast by shuffles, since a warp instruction
+// costs the FP64 pipe the same whether one lane or 32 are active.
 template <int DIM, bool FILL>
 __global__ void __launch_bounds__(256) nbr_kernel(NbrArgs a, int32_t* __restrict__ counts, int* maxk,
                                                   const int64_t* __restrict__ rowptr, int32_t* __restrict__ tmp) {
@@ -216,79 +258,105 @@ __global__ void __launch_bounds__(256) nbr_kernel(NbrArgs a, int32_t* __restrict
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
-    for (int64_t p = warp0; p < a.n_dom; p += nwarps) {
-        double xp[DIM];
+    const unsigned full = 0xffffffffu;
+    for (int64_t pb = warp0 * 32; pb < a.n_dom; pb += nwarps * 32) {
+        // set-up of particle pb + lane
+        float tin = 0.f, tout = 0.f;
+        Stencil S;
+        {
+            double x[3] = {0.0, 0.0, 0.0};
+            const int64_t pl = pb + lane;
+            if (pl < a.n_dom) {
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) xp[d] = a.pd[p * DIM + d];
-        const double rc = a.rcut_pp ? a.rcut_pp[p] : a.rcut;
-        const double rc2 = rc * rc;
-        // FP32 decisions: inside below thr_in, outside above thr_out
-        const float thr_in = (float)(rc2 - a.band), thr_out = (float)(rc2 + a.band);
-        int lst[3][3], unw[3][3];
-        float rpf[3][3];    // x_p - corner of each stencil cell, per axis
-        bool rpok[3][3];    // |x_p - corner| <= 3 cell sides (else FP64 only)
-        int cnt[3] = {1, 1, 1};
-        lst[0][0] = lst[1][0] = lst[2][0] = 0;
-        rpf[0][0] = rpf[1][0] = rpf[2][0] = 0.f;
-        rpok[0][0] = rpok[1][0] = rpok[2][0] = true;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            int c = cell_coord(xp[d], a.cells.lo[d], a.cells.cs[d], a.cells.nc[d]);
-            cnt[d] = axis_cells(c, a.cells.nc[d], a.geom.per[d], lst[d], unw[d]);
-            for (int t = 0; t < cnt[d]; ++t) {
-                const double rp = xp[d] - (a.cells.lo[d] + (double)unw[d][t] * a.cells.cs[d]);
-                rpf[d][t] = (float)rp;
-                rpok[d][t] = a.fast && fabs(rp) <= 3.0 * a.cells.cs[d];
+                for (int d = 0; d < DIM; ++d) x[d] = a.pd[pl * DIM + d];
+                const double rc = a.rcut_pp ? a.rcut_pp[pl] : a.rcut;
+                const double rc2 = rc * rc;
+                // FP32 decisions: inside below tin, outside above tout
+                tin = (float)(rc2 - a.band);
+                tout = (float)(rc2 + a.band);
             }
+            make_stencil<DIM>(a, x, S);
         }
-        int64_t base = FILL ? rowptr[p] : 0;
-        const int64_t cap = FILL ? rowptr[p + 1] - base : 0;  // the count pass's result
-        int k = 0;
-        for (int a2 = 0; a2 < cnt[2]; ++a2)
-            for (int a1 = 0; a1 < cnt[1]; ++a1)
-                for (int a0 = 0; a0 < cnt[0]; ++a0) {
-                    int cc = lst[0][a0] + a.cells.nc[0] * (lst[1][a1] + a.cells.nc[1] * lst[2][a2]);
-                    int64_t cb = a.cstart[cc], ce = a.cstart[cc + 1];
-                    const bool fast = rpok[0][a0] && rpok[1][a1] && rpok[2][a2];
-                    const float r0 = rpf[0][a0], r1 = rpf[1][a1], r2 = rpf[2][a2];
-                    for (int64_t t0 = cb; t0 < ce; t0 += 32) {
-                        int64_t t = t0 + lane;
-                        bool acc = false;
-                        int32_t q = -1;
-                        if (t < ce) {
-                            q = a.cidx[t];
-                            const float4 rq = a.srel[t];
-                            const float o0 = r0 - rq.x;
-                            float d2 = o0 * o0;
-                            if (DIM > 1) {
-                                const float o1 = r1 - rq.y;
-                                d2 = fmaf(o1, o1, d2);
+        const int nb = (int)min((int64_t)32, a.n_dom - pb);
+        for (int i = 0; i < nb; ++i) {
+            const int64_t p = pb + i;
+            const float ptin = __shfl_sync(full, tin, i), ptout = __shfl_sync(full, tout, i);
+            const unsigned valid = __shfl_sync(full, S.valid, i), fastm = __shfl_sync(full, S.fast, i);
+            int pc[3];
+            float prc[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                pc[d] = __shfl_sync(full, S.c[d], i);
+                prc[d] = __shfl_sync(full, S.rpc[d], i);
+            }
+            int64_t base = FILL ? rowptr[p] : 0;
+            const int64_t cap = FILL ? rowptr[p + 1] - base : 0;  // the count pass's result
+            int k = 0;
+#pragma unroll 1
+            for (int a2 = 0; a2 < 3; ++a2) {
+                if (!((valid >> (6 + a2)) & 1u)) continue;
+#pragma unroll 1
+                for (int a1 = 0; a1 < 3; ++a1) {
+                    if (!((valid >> (3 + a1)) & 1u)) continue;
+#pragma unroll 1
+                    for (int a0 = 0; a0 < 3; ++a0) {
+                        if (!((valid >> a0) & 1u)) continue;
+                        const int cc = slot_cell(pc[0], a0, a.cells.nc[0], a.geom.per[0]) +
+                                       a.cells.nc[0] * (slot_cell(pc[1], a1, a.cells.nc[1], a.geom.per[1]) +
+                                                        a.cells.nc[1] * slot_cell(pc[2], a2, a.cells.nc[2],
+                                                                                  a.geom.per[2]));
+                        const bool fast = ((fastm >> a0) & 1u) && ((fastm >> (3 + a1)) & 1u) &&
+                                          ((fastm >> (6 + a2)) & 1u);
+                        // x_p - corner of this cell, per axis
+                        const float r0 = prc[0] - (float)(a0 - 1) * a.csf[0];
+                        const float r1 = prc[1] - (float)(a1 - 1) * a.csf[1];
+                        const float r2 = prc[2] - (float)(a2 - 1) * a.csf[2];
+                        const int64_t cb = a.cstart[cc], ce = a.cstart[cc + 1];
+                        for (int64_t t0 = cb; t0 < ce; t0 += 32) {
+                            const int64_t t = t0 + lane;
+                            bool acc = false, exact = false;
+                            int32_t q = -1;
+                            if (t < ce) {
+                                q = a.cidx[t];
+                                const float4 rq = a.srel[t];
+                                const float o0 = r0 - rq.x;
+                                float d2 = o0 * o0;
+                                if (DIM > 1) {
+                                    const float o1 = r1 - rq.y;
+                                    d2 = fmaf(o1, o1, d2);
+                                }
+                                if (DIM > 2) {
+                                    const float o2 = r2 - rq.z;
+                                    d2 = fmaf(o2, o2, d2);
+                                }
+                                acc = fast && d2 < ptin;
+                                exact = !acc && !(fast && d2 > ptout);  // the band, NaN, or no FP32 decision
                             }
-                            if (DIM > 2) {
-                                const float o2 = r2 - rq.z;
-                                d2 = fmaf(o2, o2, d2);
-                            }
-                            if (fast && d2 < thr_in) {
-                                acc = true;
-                            } else if (!(fast && d2 > thr_out)) {  // the band, NaN, or no FP32 decision
+                            // a warp-uniform branch: the FP64 test issues only
+                            // when some lane needs it
+                            if (__any_sync(full, exact) && exact) {
                                 double o[DIM];
 #pragma unroll
-                                for (int d = 0; d < DIM; ++d) o[d] = offset1(a.geom, d, xp[d], a.spos[t * DIM + d]);
-                                acc = norm2<DIM>(o) < rc2;
+                                for (int d = 0; d < DIM; ++d)
+                                    o[d] = offset1(a.geom, d, a.pd[p * DIM + d], a.spos[t * DIM + d]);
+                                const double rc = a.rcut_pp ? a.rcut_pp[p] : a.rcut;
+                                acc = norm2<DIM>(o) < rc * rc;
                             }
                             if (a.self_skip && (int64_t)q == p) acc = false;
+                            const unsigned bal = __ballot_sync(full, acc);
+                            if (FILL && acc) {
+                                const int64_t slot = k + __popc(bal & lt_mask);
+                                if (slot < cap) tmp[base + slot] = q;
+                            }
+                            k += __popc(bal);
                         }
-                        unsigned bal = __ballot_sync(0xffffffffu, acc);
-                        if (FILL && acc) {
-                            int64_t slot = k + __popc(bal & lt_mask);
-                            if (slot < cap) tmp[base + slot] = q;
-                        }
-                        k += __popc(bal);
                     }
                 }
-        if (!FILL && lane == 0) {
-            counts[p] = k;
-            atomicMax(maxk, k);
+            }
+            if (!FILL && lane == 0) {
+                counts[p] = k;
+                atomicMax(maxk, k);
+            }
         }
     }
 }
