@@ -868,31 +868,40 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
         rmax = std::max(rcut > 0 ? rcut : 0.0, rhi[0]);
     }
     dfree(mm);
-    // the cell list holds the support set
-    // cells no smaller than the largest radius; total bounded by ~4 n
-    CellGrid cg{};
-    double cmin = rmax * (1.0 + 1e-9);
-    double cap = std::max(4.0 * (double)std::max(n, ns), 1024.0);
-    for (int it = 0; it < 64; ++it) {
-        double total = 1.0;
-        for (int d = 0; d < kMaxDim; ++d) {
-            if (d < dim) {
-                double L = hi[d] - lo[d];
-                double m = (L > 0.0) ? std::floor(L / cmin) : 1.0;
-                if (!(m >= 1.0)) m = 1.0;
-                cg.nc[d] = (int)std::min(m, 1.0e6);
-                cg.cs[d] = (L > 0.0) ? L / (double)cg.nc[d] : 1.0;
-                cg.lo[d] = lo[d];
-            } else {
-                cg.nc[d] = 1;
-                cg.cs[d] = 1.0;
-                cg.lo[d] = 0.0;
+    // the cell list holds the support set; total cells bounded by ~4 n
+    const double cap = std::max(4.0 * (double)std::max(n, ns), 1024.0);
+    auto make_grid = [&](double cmin) {
+        CellGrid g{};
+        for (int it = 0; it < 64; ++it) {
+            double total = 1.0;
+            for (int d = 0; d < kMaxDim; ++d) {
+                if (d < dim) {
+                    double L = hi[d] - lo[d];
+                    double m = (L > 0.0) ? std::floor(L / cmin) : 1.0;
+                    if (!(m >= 1.0)) m = 1.0;
+                    g.nc[d] = (int)std::min(m, 1.0e6);
+                    g.cs[d] = (L > 0.0) ? L / (double)g.nc[d] : 1.0;
+                    g.lo[d] = lo[d];
+                } else {
+                    g.nc[d] = 1;
+                    g.cs[d] = 1.0;
+                    g.lo[d] = 0.0;
+                }
+                total *= g.nc[d];
             }
-            total *= cg.nc[d];
+            if (total <= cap) break;
+            cmin *= 1.25;
         }
-        if (total <= cap) break;
-        cmin *= 1.25;
-    }
+        return g;
+    };
+    // cells no smaller than half the largest radius, +-2 stencil (packed
+    // rows), when every periodic axis then has at least five cells; else
+    // cells no smaller than the largest radius and a +-1 stencil
+    CellGrid cg = make_grid(0.5 * rmax * (1.0 + 1e-9));
+    int packed = 1;
+    for (int d = 0; d < dim; ++d)
+        if (P->per[d] && cg.nc[d] < 5) packed = 0;
+    if (!packed) cg = make_grid(rmax * (1.0 + 1e-9));
     const int64_t ncell = (int64_t)cg.nc[0] * cg.nc[1] * cg.nc[2];
     int32_t *cell = nullptr, *ccount = nullptr, *cidx = nullptr, *counts = nullptr, *tmp = nullptr;
     int64_t *cstart = nullptr, *fill = nullptr, *scan_tmp = nullptr;
@@ -947,6 +956,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
         for (int d = 0; d < dim; ++d) S = std::max(S, 3.0 * cg.cs[d]);
         a.band = std::ldexp(S * S, -14);
         for (int d = 0; d < 3; ++d) a.csf[d] = d < dim ? (float)cg.cs[d] : 0.f;
+        a.packed = packed;
         a.fast = 1;
         for (int d = 0; d < dim; ++d)
             if (P->per[d] && cg.nc[d] < 3) a.fast = 0;
@@ -960,7 +970,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e == cudaSuccess) e = dalloc(&tmp, nnz);
     if (e == cudaSuccess) e = dalloc(&P->cols, nnz + kPad);
-    if (e == cudaSuccess) e = fill_neighbors(a, P->rowptr, tmp, P->cols, s);
+    if (e == cudaSuccess) e = fill_neighbors(a, P->rowptr, tmp, P->cols, hk, s);
     P->tstop(DCPSE_K_NEIGHBORS);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cleanup();

@@ -52,13 +52,14 @@ struct NbrArgs {
     double band;        // |d^2 - rc^2| below this: decided in FP64
     int fast;           // 0: FP64 for every candidate
     float csf[3];       // cell sides in FP32
+    int packed;         // cells >= rc / 2, +-2 stencil, packed candidate rows
 };
 
 // Count pass: counts[p] = number of neighbours; also atomically maxes *d_maxk.
 cudaError_t count_neighbors(const NbrArgs& a, int32_t* counts, int* d_maxk, cudaStream_t s);
 // Fill pass: unsorted neighbours of p into tmp[rowptr[p] ...], then sorted
-// ascending into cols.
-cudaError_t fill_neighbors(const NbrArgs& a, const int64_t* rowptr, int32_t* tmp, int32_t* cols,
+// ascending into cols (maxk: the longest row, from the count pass).
+cudaError_t fill_neighbors(const NbrArgs& a, const int64_t* rowptr, int32_t* tmp, int32_t* cols, int maxk,
                            cudaStream_t s);
 
 // --------------------------------------------------------------- assembly --

@@ -21,6 +21,7 @@
 // FP64 predicate itself, as are particles outside the grid, NaN positions
 // and periodic axes with fewer than three cells.  The lists are the same bit
 // for bit.
+#include <cstdint>
 #include <cstring>
 
 #include "dcpse_internal.h"
@@ -175,16 +176,20 @@ __global__ void cell_fill_kernel(int dim, const double* __restrict__ pos, int64_
         unsigned long long slot = atomicAdd((unsigned long long*)&fill[cell[i]], 1ull);
         cidx[slot] = (int32_t)i;
         float r[kMaxDim] = {0.f, 0.f, 0.f};
+        int cx = 0;
         for (int d = 0; d < dim; ++d) {
             const double x = pos[i * dim + d];
             spos[slot * dim + d] = x;
             // offset from the cell's lower corner; NaN (always the FP64
             // test) for a particle clamped into an edge cell
             const int c = cell_coord(x, g.lo[d], g.cs[d], g.nc[d]);
+            if (d == 0) cx = c;
             const double rel = x - (g.lo[d] + (double)c * g.cs[d]);
             r[d] = (rel >= -0.5 * g.cs[d] && rel <= 1.5 * g.cs[d]) ? (float)rel : __int_as_float(0x7fc00000);
         }
-        srel[slot] = make_float4(r[0], r[1], r[2], 0.f);
+        // w: the cell's index along axis 0, for candidates taken from a run
+        // of cells along that axis
+        srel[slot] = make_float4(r[0], r[1], r[2], __int_as_float(cx));
     }
 }
 
@@ -361,6 +366,236 @@ __global__ void __launch_bounds__(256) nbr_kernel(NbrArgs a, int32_t* __restrict
     }
 }
 
+// ------------------------------------------------------------------------
+// Packed variant, cells of side >= rc / 2 and a stencil of +-2 cells per
+// axis (43 % fewer candidates than 3^d cells of side rc).  The cells of a
+// stencil row along axis 0 are adjacent in the cell order, so each row is
+// one contiguous range of the cell-ordered support; the warp concatenates
+// the ranges of all rows (lane r owns row r, a warp scan gives the offsets)
+// and walks the concatenation 32 candidates at a time, every lane finding
+// its row by a binary search over the row ends.  Used when every periodic
+// axis has at least five cells; a particle whose row would wrap around a
+// periodic axis 0 walks its cells one by one.
+constexpr int kPackR = 2;
+constexpr int kPackW = 2 * kPackR + 1;
+
+struct PackStencil {
+    int c[3];
+    float rpc[3];
+    unsigned valid;  // bit kPackW d + t: slot t (offset t - kPackR) of axis d is a cell
+    unsigned fast;   // bit kPackW d + t: |x_p - corner| <= 3 cell sides
+    bool xwrap;      // the row along axis 0 wraps around a periodic boundary
+};
+
+template <int DIM>
+__device__ __forceinline__ void make_pack_stencil(const NbrArgs& a, const double* xp, PackStencil& S) {
+    S.valid = 0;
+    S.fast = 0;
+    S.xwrap = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        S.c[d] = 0;
+        S.rpc[d] = 0.f;
+        if (d >= DIM) {
+            S.valid |= 1u << (kPackW * d + kPackR);
+            S.fast |= 1u << (kPackW * d + kPackR);
+            continue;
+        }
+        const int nc = a.cells.nc[d];
+        const int c = cell_coord(xp[d], a.cells.lo[d], a.cells.cs[d], nc);
+        S.c[d] = c;
+        S.rpc[d] = (float)(xp[d] - (a.cells.lo[d] + (double)c * a.cells.cs[d]));
+        if (d == 0 && a.geom.per[0] && (c - kPackR < 0 || c + kPackR >= nc)) S.xwrap = true;
+#pragma unroll
+        for (int t = 0; t < kPackW; ++t) {
+            const int u = c + t - kPackR;
+            const bool ok = a.geom.per[d] || (u >= 0 && u < nc);
+            const double rp = xp[d] - (a.cells.lo[d] + (double)u * a.cells.cs[d]);
+            if (ok) S.valid |= 1u << (kPackW * d + t);
+            if (ok && a.fast && fabs(rp) <= 3.0 * a.cells.cs[d]) S.fast |= 1u << (kPackW * d + t);
+        }
+    }
+}
+
+__device__ __forceinline__ int pack_cell(int c, int t, int nc, int per) {
+    int v = c + t - kPackR;
+    if (per) v = v < 0 ? v + nc : (v >= nc ? v - nc : v);
+    return v;
+}
+
+template <int DIM, bool FILL>
+__global__ void __launch_bounds__(256) nbr_packed_kernel(NbrArgs a, int32_t* __restrict__ counts, int* maxk,
+                                                         const int64_t* __restrict__ rowptr,
+                                                         int32_t* __restrict__ tmp) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const unsigned full = 0xffffffffu;
+    constexpr int NR = DIM == 3 ? kPackW * kPackW : (DIM == 2 ? kPackW : 1);  // stencil rows
+    for (int64_t pb = warp0 * 32; pb < a.n_dom; pb += nwarps * 32) {
+        float tin = 0.f, tout = 0.f;
+        PackStencil S;
+        {
+            double x[3] = {0.0, 0.0, 0.0};
+            const int64_t pl = pb + lane;
+            if (pl < a.n_dom) {
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) x[d] = a.pd[pl * DIM + d];
+                const double rc = a.rcut_pp ? a.rcut_pp[pl] : a.rcut;
+                const double rc2 = rc * rc;
+                tin = (float)(rc2 - a.band);
+                tout = (float)(rc2 + a.band);
+            }
+            make_pack_stencil<DIM>(a, x, S);
+        }
+        const int nb = (int)min((int64_t)32, a.n_dom - pb);
+        for (int i = 0; i < nb; ++i) {
+            const int64_t p = pb + i;
+            const float ptin = __shfl_sync(full, tin, i), ptout = __shfl_sync(full, tout, i);
+            const unsigned valid = __shfl_sync(full, S.valid, i), fastm = __shfl_sync(full, S.fast, i);
+            const bool xwrap = __shfl_sync(full, (int)S.xwrap, i) != 0;
+            int pc[3];
+            float prc[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                pc[d] = __shfl_sync(full, S.c[d], i);
+                prc[d] = __shfl_sync(full, S.rpc[d], i);
+            }
+            const int64_t base = FILL ? rowptr[p] : 0;
+            const int64_t cap = FILL ? rowptr[p + 1] - base : 0;  // the count pass's result
+            int k = 0;
+            // classifies candidate t (valid when has) of the cell-ordered
+            // support; r0..r2 = x_p - corner of its cell, fast = FP32 allowed
+            auto visit = [&](bool has, int64_t t, float r0, float r1, float r2, bool fast) {
+                bool acc = false, exact = false;
+                int32_t q = -1;
+                if (has) {
+                    q = a.cidx[t];
+                    const float4 rq = a.srel[t];
+                    const float o0 = r0 - rq.x;
+                    float d2 = o0 * o0;
+                    if (DIM > 1) {
+                        const float o1 = r1 - rq.y;
+                        d2 = fmaf(o1, o1, d2);
+                    }
+                    if (DIM > 2) {
+                        const float o2 = r2 - rq.z;
+                        d2 = fmaf(o2, o2, d2);
+                    }
+                    acc = fast && d2 < ptin;
+                    exact = !acc && !(fast && d2 > ptout);  // the band, NaN, or no FP32 decision
+                }
+                if (__any_sync(full, exact) && exact) {
+                    double o[DIM];
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) o[d] = offset1(a.geom, d, a.pd[p * DIM + d], a.spos[t * DIM + d]);
+                    const double rc = a.rcut_pp ? a.rcut_pp[p] : a.rcut;
+                    acc = norm2<DIM>(o) < rc * rc;
+                }
+                if (a.self_skip && (int64_t)q == p) acc = false;
+                const unsigned bal = __ballot_sync(full, acc);
+                if (FILL && acc) {
+                    const int64_t slot = k + __popc(bal & lt_mask);
+                    if (slot < cap) tmp[base + slot] = q;
+                }
+                k += __popc(bal);
+            };
+            if (!xwrap) {
+                // lane r < NR owns stencil row r: (a1, a2) = (r % W, r / W)
+                int rlen = 0;
+                int64_t rstart = 0;
+                float ry = 0.f, rz = 0.f;
+                int rfast = 0;
+                if (lane < NR) {
+                    const int a1 = DIM > 1 ? lane % kPackW : kPackR;
+                    const int a2 = DIM > 2 ? lane / kPackW : kPackR;
+                    if (((valid >> (kPackW + a1)) & 1u) && ((valid >> (2 * kPackW + a2)) & 1u)) {
+                        const int nc0 = a.cells.nc[0];
+                        const int x0 = a.geom.per[0] ? pc[0] - kPackR : max(pc[0] - kPackR, 0);
+                        const int x1 = a.geom.per[0] ? pc[0] + kPackR : min(pc[0] + kPackR, nc0 - 1);
+                        const int yz = DIM > 1 ? nc0 * (pack_cell(pc[1], a1, a.cells.nc[1], a.geom.per[1]) +
+                                                        a.cells.nc[1] * (DIM > 2 ? pack_cell(pc[2], a2, a.cells.nc[2],
+                                                                                             a.geom.per[2])
+                                                                                   : 0))
+                                               : 0;
+                        rstart = a.cstart[x0 + yz];
+                        rlen = (int)(a.cstart[x1 + yz + 1] - rstart);
+                        ry = prc[1] - (float)(a1 - kPackR) * a.csf[1];
+                        rz = prc[2] - (float)(a2 - kPackR) * a.csf[2];
+                        rfast = ((fastm >> (kPackW + a1)) & 1u) && ((fastm >> (2 * kPackW + a2)) & 1u);
+                    }
+                }
+                // inclusive scan of the row lengths
+                int rend = rlen;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(full, rend, o);
+                    if (lane >= o) rend += v;
+                }
+                const int total = __shfl_sync(full, rend, 31);
+                for (int g0 = 0; g0 < total; g0 += 32) {
+                    const int g = g0 + lane;
+                    // first row whose end exceeds g
+                    int lo = 0, hi = NR - 1;
+#pragma unroll
+                    for (int it = 0; it < 5; ++it) {
+                        const int mid = (lo + hi) >> 1;
+                        const int e = __shfl_sync(full, rend, mid);
+                        if (lo < hi) {
+                            if (e > g)
+                                hi = mid;
+                            else
+                                lo = mid + 1;
+                        }
+                    }
+                    const int e_r = __shfl_sync(full, rend, lo), l_r = __shfl_sync(full, rlen, lo);
+                    const int64_t s_r = __shfl_sync(full, rstart, lo);
+                    const float y_r = __shfl_sync(full, ry, lo), z_r = __shfl_sync(full, rz, lo);
+                    const int f_r = __shfl_sync(full, rfast, lo);
+                    const bool has = g < total;
+                    const int64_t t = s_r + (g - (e_r - l_r));
+                    // the candidate's cell along axis 0 is in its srel.w
+                    int dx = 0;
+                    if (has) dx = __float_as_int(a.srel[t].w) - pc[0];
+                    if (a.geom.per[0]) dx = dx < -kPackR ? dx + a.cells.nc[0] : (dx > kPackR ? dx - a.cells.nc[0] : dx);
+                    const bool fx = dx >= -kPackR && dx <= kPackR && ((fastm >> (dx + kPackR)) & 1u);
+                    visit(has, t, prc[0] - (float)dx * a.csf[0], y_r, z_r, f_r && fx);
+                }
+            } else {
+                // the row along the periodic axis 0 wraps: cell by cell
+#pragma unroll 1
+                for (int a2 = 0; a2 < kPackW; ++a2) {
+                    if (!((valid >> (2 * kPackW + a2)) & 1u)) continue;
+#pragma unroll 1
+                    for (int a1 = 0; a1 < kPackW; ++a1) {
+                        if (!((valid >> (kPackW + a1)) & 1u)) continue;
+#pragma unroll 1
+                        for (int a0 = 0; a0 < kPackW; ++a0) {
+                            if (!((valid >> a0) & 1u)) continue;
+                            const int cc = pack_cell(pc[0], a0, a.cells.nc[0], a.geom.per[0]) +
+                                           a.cells.nc[0] * (pack_cell(pc[1], a1, a.cells.nc[1], a.geom.per[1]) +
+                                                            a.cells.nc[1] * pack_cell(pc[2], a2, a.cells.nc[2],
+                                                                                      a.geom.per[2]));
+                            const bool fast = ((fastm >> a0) & 1u) && ((fastm >> (kPackW + a1)) & 1u) &&
+                                              ((fastm >> (2 * kPackW + a2)) & 1u);
+                            const float r0 = prc[0] - (float)(a0 - kPackR) * a.csf[0];
+                            const float r1 = prc[1] - (float)(a1 - kPackR) * a.csf[1];
+                            const float r2 = prc[2] - (float)(a2 - kPackR) * a.csf[2];
+                            const int64_t cb = a.cstart[cc], ce = a.cstart[cc + 1];
+                            for (int64_t t0 = cb; t0 < ce; t0 += 32) visit(t0 + lane < ce, t0 + lane, r0, r1, r2, fast);
+                        }
+                    }
+                }
+            }
+            if (!FILL && lane == 0) {
+                counts[p] = k;
+                atomicMax(maxk, k);
+            }
+        }
+    }
+}
+
 // Warp per row: rank of each entry among the row's entries -> sorted output.
 __global__ void __launch_bounds__(256) sort_rows_kernel(int64_t n, const int64_t* __restrict__ rowptr,
                                                         const int32_t* __restrict__ tmp, int32_t* __restrict__ cols) {
@@ -376,6 +611,73 @@ __global__ void __launch_bounds__(256) sort_rows_kernel(int64_t n, const int64_t
             int rank = 0;
             for (int j = 0; j < k; ++j) rank += (tmp[b + j] < v);
             if (i < k) cols[b + rank] = v;
+        }
+    }
+}
+
+// Warp per row, rows of up to 32 KPL entries: a bitonic sort in registers
+// (lane l holds entries l KPL .. l KPL + KPL - 1; partners KPL or more apart
+// are exchanged by shuffles).  Longer rows take the rank sort above.
+template <int KPL>
+__global__ void __launch_bounds__(256) sort_rows_bitonic_kernel(int64_t n, const int64_t* __restrict__ rowptr,
+                                                                const int32_t* __restrict__ tmp,
+                                                                int32_t* __restrict__ cols) {
+    constexpr int N = 32 * KPL;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t p = warp0; p < n; p += nwarps) {
+        const int64_t b = rowptr[p];
+        const int k = (int)(rowptr[p + 1] - b);
+        if (k > N) {
+            for (int i0 = 0; i0 < k; i0 += 32) {
+                const int i = i0 + lane;
+                const int32_t v = (i < k) ? tmp[b + i] : 0;
+                int rank = 0;
+                for (int j = 0; j < k; ++j) rank += (tmp[b + j] < v);
+                if (i < k) cols[b + rank] = v;
+            }
+            continue;
+        }
+        int32_t v[KPL];
+#pragma unroll
+        for (int s = 0; s < KPL; ++s) {
+            const int e = lane * KPL + s;
+            v[s] = e < k ? tmp[b + e] : INT32_MAX;
+        }
+#pragma unroll
+        for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                if (stride < KPL) {
+#pragma unroll
+                    for (int s = 0; s < KPL; ++s) {
+                        const int s2 = s ^ stride;
+                        if (s2 > s) {
+                            const bool asc = ((lane * KPL + s) & size) == 0;
+                            const int32_t x = v[s], y = v[s2];
+                            if ((x > y) == asc) {
+                                v[s] = y;
+                                v[s2] = x;
+                            }
+                        }
+                    }
+                } else {
+                    const int ls = stride / KPL;
+                    const bool lower = (lane & ls) == 0;
+#pragma unroll
+                    for (int s = 0; s < KPL; ++s) {
+                        const int32_t o = __shfl_xor_sync(0xffffffffu, v[s], ls);
+                        const bool asc = ((lane * KPL + s) & size) == 0;
+                        v[s] = (lower == asc) ? min(v[s], o) : max(v[s], o);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < KPL; ++s) {
+            const int e = lane * KPL + s;
+            if (e < k) cols[b + e] = v[s];
         }
     }
 }
@@ -456,19 +758,39 @@ cudaError_t build_cells(int dim, const double* pos, int64_t n, const CellGrid& g
 cudaError_t count_neighbors(const NbrArgs& a, int32_t* counts, int* d_maxk, cudaStream_t s) {
     if (a.n_dom == 0) return cudaSuccess;
     int grid = grid_for(a.n_dom * 32, 256);
+    if (a.packed) {
+        if (a.dim == 1) nbr_packed_kernel<1, false><<<grid, 256, 0, s>>>(a, counts, d_maxk, nullptr, nullptr);
+        else if (a.dim == 2) nbr_packed_kernel<2, false><<<grid, 256, 0, s>>>(a, counts, d_maxk, nullptr, nullptr);
+        else nbr_packed_kernel<3, false><<<grid, 256, 0, s>>>(a, counts, d_maxk, nullptr, nullptr);
+        return cudaGetLastError();
+    }
     if (a.dim == 1) nbr_kernel<1, false><<<grid, 256, 0, s>>>(a, counts, d_maxk, nullptr, nullptr);
     else if (a.dim == 2) nbr_kernel<2, false><<<grid, 256, 0, s>>>(a, counts, d_maxk, nullptr, nullptr);
     else nbr_kernel<3, false><<<grid, 256, 0, s>>>(a, counts, d_maxk, nullptr, nullptr);
     return cudaGetLastError();
 }
 
-cudaError_t fill_neighbors(const NbrArgs& a, const int64_t* rowptr, int32_t* tmp, int32_t* cols, cudaStream_t s) {
+cudaError_t fill_neighbors(const NbrArgs& a, const int64_t* rowptr, int32_t* tmp, int32_t* cols, int maxk,
+                           cudaStream_t s) {
     if (a.n_dom == 0) return cudaSuccess;
     int grid = grid_for(a.n_dom * 32, 256);
-    if (a.dim == 1) nbr_kernel<1, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
-    else if (a.dim == 2) nbr_kernel<2, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
-    else nbr_kernel<3, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
-    sort_rows_kernel<<<grid, 256, 0, s>>>(a.n_dom, rowptr, tmp, cols);
+    if (a.packed) {
+        if (a.dim == 1) nbr_packed_kernel<1, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
+        else if (a.dim == 2) nbr_packed_kernel<2, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
+        else nbr_packed_kernel<3, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
+    } else if (a.dim == 1) {
+        nbr_kernel<1, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
+    } else if (a.dim == 2) {
+        nbr_kernel<2, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
+    } else {
+        nbr_kernel<3, true><<<grid, 256, 0, s>>>(a, nullptr, nullptr, rowptr, tmp);
+    }
+    if (maxk <= 128)
+        sort_rows_bitonic_kernel<4><<<grid, 256, 0, s>>>(a.n_dom, rowptr, tmp, cols);
+    else if (maxk <= 256)
+        sort_rows_bitonic_kernel<8><<<grid, 256, 0, s>>>(a.n_dom, rowptr, tmp, cols);
+    else
+        sort_rows_kernel<<<grid, 256, 0, s>>>(a.n_dom, rowptr, tmp, cols);
     return cudaGetLastError();
 }
 
