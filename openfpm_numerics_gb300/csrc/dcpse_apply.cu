@@ -628,6 +628,11 @@ cudaError_t p2p_f64(int64_t n, const int64_t* rowptr, const int32_t* cols, const
     return cudaGetLastError();
 }
 
+int64_t f32_rows_per_wave(int64_t n, int64_t nnz, int lanes) {
+    const int G = lanes ? lanes : lanes_for_f32(n, nnz);
+    return (int64_t)num_sms() * 8 * (256 / G);
+}
+
 cudaError_t apply_batched_f32x(const ApplyF32& p, cudaStream_t s) {
     if (p.n == 0) return cudaSuccess;
     F32Args a{};

@@ -107,13 +107,40 @@ __global__ void index_check_kernel(const int64_t* idx, int64_t m, int64_t n, uns
         if (idx[i] < 0 || idx[i] >= n) atomicAdd(bad, 1ull);
 }
 
-// largest field index each row chunk reads (its neighbours and itself);
-// chunk c holds rows [n c / nch, n (c + 1) / nch)
-__global__ void chunk_reach_kernel(const int64_t* rowptr, const int32_t* cols, int64_t n, int nch,
+// Host-buffer applies move the field up and the outputs back in row chunks
+// overlapped with the apply of other chunks.  Chunk boundaries fall on whole
+// waves of the apply kernel's grid (a chunk of 1.7 waves would run its second
+// wave two thirds full), with sizes tapering at both ends, 1 1 2 4 4 4 4 4 4
+// 2 1 1 32nds of the waves: small first chunks start the apply after a short
+// upload, small last chunks leave a short copy after the last apply.
+constexpr int kHostChunks = 12;
+constexpr int64_t kHostChunkMinRows = 65536;
+struct ChunkBounds {
+    int nch;
+    int64_t b[kHostChunks + 1];  // chunk c = rows [b[c], b[c + 1])
+};
+
+ChunkBounds make_chunk_bounds(int64_t n, int64_t rows_per_wave) {
+    static const int cum[kHostChunks + 1] = {0, 1, 2, 4, 8, 12, 16, 20, 24, 28, 30, 31, 32};
+    ChunkBounds c{};
+    const int64_t waves = (n + rows_per_wave - 1) / rows_per_wave;
+    if (waves <= kHostChunks) {
+        c.nch = (int)std::max<int64_t>(waves, 1);
+        for (int i = 0; i <= c.nch; ++i) c.b[i] = std::min(n, (int64_t)i * rows_per_wave);
+        c.b[c.nch] = n;
+        return c;
+    }
+    c.nch = kHostChunks;
+    for (int i = 0; i <= kHostChunks; ++i) c.b[i] = n * cum[i] / 32;
+    return c;
+}
+
+// largest field index each row chunk reads (its neighbours and itself)
+__global__ void chunk_reach_kernel(const int64_t* rowptr, const int32_t* cols, int64_t n, ChunkBounds cb,
                                    unsigned long long* reach) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         int c = 0;
-        while (c + 1 < nch && n * (c + 1) / nch <= r) ++c;
+        while (c + 1 < cb.nch && cb.b[c + 1] <= r) ++c;
         int64_t m = r;
         for (int64_t j = rowptr[r]; j < rowptr[r + 1]; ++j) m = max(m, (int64_t)cols[j]);
         atomicMax(&reach[c], (unsigned long long)m);
@@ -162,7 +189,7 @@ struct dcpse_plan_s {
     // optional event timing per kernel id
     bool timing = false;
     KernelTimer timers[DCPSE_K_COUNT];
-    void tstart(int k) {
+    void tstart(int k, cudaStream_t on = nullptr) {
         if (!timing) return;
         KernelTimer& T = timers[k];
         if (T.used == T.ev.size()) {
@@ -171,12 +198,12 @@ struct dcpse_plan_s {
             cudaEventCreate(&b);
             T.ev.emplace_back(a, b);
         }
-        cudaEventRecord(T.ev[T.used].first, stream);
+        cudaEventRecord(T.ev[T.used].first, on ? on : stream);
     }
-    void tstop(int k) {
+    void tstop(int k, cudaStream_t on = nullptr) {
         if (!timing) return;
         KernelTimer& T = timers[k];
-        cudaEventRecord(T.ev[T.used].second, stream);
+        cudaEventRecord(T.ev[T.used].second, on ? on : stream);
         T.used++;
     }
     void free_timers() {
@@ -275,10 +302,11 @@ struct dcpse_plan_s {
     // host-buffer applies: the field arrives in pieces on h2d_stream, row
     // chunks start once the pieces they read have arrived, and their outputs
     // go back on copy_stream while later chunks run
-    cudaStream_t copy_stream = nullptr, h2d_stream = nullptr;
-    cudaEvent_t chunk_ev[8] = {};
-    cudaEvent_t piece_ev[8] = {};
-    int64_t chunk_reach[8] = {};
+    cudaStream_t copy_stream = nullptr, h2d_stream = nullptr, apply2_stream = nullptr;
+    cudaEvent_t chunk_ev[kHostChunks] = {};
+    cudaEvent_t piece_ev[kHostChunks] = {};
+    int64_t chunk_reach[kHostChunks] = {};
+    ChunkBounds chunks{};                // row chunks the reaches are for
     int64_t list_version = 0;            // bumped whenever the neighbour list changes
     int64_t reach_version = -1;          // list version the reaches were computed for
     double* hf = nullptr;    // device copy of a host field (host apply)
@@ -319,14 +347,17 @@ struct dcpse_plan_s {
             cudaStreamSynchronize(copy_stream);
             cudaStreamSynchronize(h2d_stream);
             for (auto* evs : {chunk_ev, piece_ev})
-                for (int i = 0; i < 8; ++i) {
+                for (int i = 0; i < kHostChunks; ++i) {
                     if (evs[i]) cudaEventDestroy(evs[i]);
                     evs[i] = nullptr;
                 }
+            cudaStreamSynchronize(apply2_stream);
             cudaStreamDestroy(copy_stream);
             cudaStreamDestroy(h2d_stream);
+            cudaStreamDestroy(apply2_stream);
             copy_stream = nullptr;
             h2d_stream = nullptr;
+            apply2_stream = nullptr;
         }
         reach_version = -1;
         dfree(surf_ext);
@@ -1496,7 +1527,9 @@ int dcpse_apply_output_f64(dcpse_plan_t* P, int output, const double* d_f, doubl
 namespace {
 // The FP32 batched apply of rows [r0, r1) (0, 0: all rows) from the plan's
 // split field into d_out ([n_outputs][n]).
-int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, int64_t r1) {
+int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, int64_t r1,
+                   cudaStream_t on = nullptr) {
+    cudaStream_t st = on ? on : P->stream;
     ApplyF32 ap{};
     ap.n = P->n;
     ap.nout = P->nout;
@@ -1524,9 +1557,9 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
     }
     // the residual correction only pays off with compensated sums
     if ((P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) || precision == DCPSE_F32_RESID) ap.comp = 0xffffffffu;
-    P->tstart(DCPSE_K_APPLY_BATCHED);
-    cudaError_t e = apply_batched_f32x(ap, P->stream);
-    P->tstop(DCPSE_K_APPLY_BATCHED);
+    P->tstart(DCPSE_K_APPLY_BATCHED, st);
+    cudaError_t e = apply_batched_f32x(ap, st);
+    P->tstop(DCPSE_K_APPLY_BATCHED, st);
     if (e == cudaErrorInvalidConfiguration && (P->apply_mode & 15) == 2)
         return fail(DCPSE_ERR_CAPACITY, "TMA-staged tiles of this plan do not fit in shared memory "
                                         "(fewer lanes per row or another mode)");
@@ -1541,10 +1574,6 @@ int check_f32_weights(dcpse_plan_t* P, int precision) {
     return DCPSE_OK;
 }
 
-// Host-buffer applies copy the outputs back in this many row chunks on a
-// second stream, each chunk's copy overlapping the next chunk's apply.
-constexpr int kHostChunks = 8;
-constexpr int64_t kHostChunkMinRows = 65536;
 }  // namespace
 
 int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int precision) {
@@ -1574,6 +1603,7 @@ int ensure_host_pipeline(dcpse_plan_t* P) {
     if (P->copy_stream) return DCPSE_OK;
     cudaError_t e = cudaStreamCreateWithFlags(&P->copy_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->h2d_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->apply2_stream, cudaStreamNonBlocking);
     for (int c = 0; c < kHostChunks && e == cudaSuccess; ++c) {
         e = cudaEventCreateWithFlags(&P->chunk_ev[c], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->piece_ev[c], cudaEventDisableTiming);
@@ -1586,7 +1616,8 @@ int ensure_host_pipeline(dcpse_plan_t* P) {
         }
         if (P->copy_stream) cudaStreamDestroy(P->copy_stream);
         if (P->h2d_stream) cudaStreamDestroy(P->h2d_stream);
-        P->copy_stream = P->h2d_stream = nullptr;
+        if (P->apply2_stream) cudaStreamDestroy(P->apply2_stream);
+        P->copy_stream = P->h2d_stream = P->apply2_stream = nullptr;
         return fail(DCPSE_ERR_CUDA, cudaGetErrorString(e));
     }
     return DCPSE_OK;
@@ -1594,13 +1625,16 @@ int ensure_host_pipeline(dcpse_plan_t* P) {
 
 // largest field index read by each row chunk, for the current list
 int ensure_chunk_reach(dcpse_plan_t* P) {
-    if (P->reach_version == P->list_version) return DCPSE_OK;
+    const ChunkBounds cb = make_chunk_bounds(P->n, f32_rows_per_wave(P->n, P->nnz, P->apply_lanes));
+    bool same = P->reach_version == P->list_version && cb.nch == P->chunks.nch;
+    for (int c = 0; same && c <= cb.nch; ++c) same = cb.b[c] == P->chunks.b[c];
+    if (same) return DCPSE_OK;
     unsigned long long* d = nullptr;
     DCPSE_CK(dalloc(&d, kHostChunks));
     cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * kHostChunks, P->stream);
     if (e == cudaSuccess) {
         chunk_reach_kernel<<<std::max(1, std::min(num_sms() * 8, (int)((P->n + 255) / 256))), 256, 0, P->stream>>>(
-            P->rowptr, P->cols, P->n, kHostChunks, d);
+            P->rowptr, P->cols, P->n, cb, d);
         e = cudaGetLastError();
     }
     unsigned long long h[kHostChunks] = {};
@@ -1609,6 +1643,7 @@ int ensure_chunk_reach(dcpse_plan_t* P) {
     dfree(d);
     DCPSE_CK(e);
     for (int c = 0; c < kHostChunks; ++c) P->chunk_reach[c] = (int64_t)h[c];
+    P->chunks = cb;
     P->reach_version = P->list_version;
     return DCPSE_OK;
 }
@@ -1631,7 +1666,8 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
         return dcpse_plan_check(P);
     }
     // Pipelined: the field goes up in kHostChunks pieces (copy + split on
-    // h2d_stream); row chunk c starts once the pieces up to its largest read
+    // h2d_stream, pieces and row chunks share the bounds); row chunk c
+    // starts once the pieces up to its largest read
     // index have arrived; its outputs go back on copy_stream while later
     // chunks run.
     if (int rc = check_f32_weights(P, precision)) return rc;
@@ -1644,47 +1680,123 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
         DCPSE_CK(dalloc(&P->f2, (size_t)n));
         P->f2_len = n;
     }
+    // Pinned host outputs with a device mapping (cudaHostAlloc /
+    // cudaHostRegister; over NVLink-C2C the GPU stores into them at full
+    // rate): the apply writes them directly, with no copies back and only
+    // three row chunks (for the upload of the field)
+    auto mapped = [](const void* h) -> void* {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, h) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+            return at.devicePointer;
+        cudaGetLastError();  // an unregistered pointer is not an error here
+        return nullptr;
+    };
+    double* out_mapped = static_cast<double*>(mapped(h_out));
+    const double* f_mapped = out_mapped ? static_cast<const double*>(mapped(h_f)) : nullptr;
     // earlier work of the plan's stream on these buffers comes first
     DCPSE_CK(cudaEventRecord(P->chunk_ev[0], P->stream));
     DCPSE_CK(cudaStreamWaitEvent(P->h2d_stream, P->chunk_ev[0], 0));
+    DCPSE_CK(cudaStreamWaitEvent(P->apply2_stream, P->chunk_ev[0], 0));
     // pieces are issued just ahead of the first chunk that reads them, so the
     // first chunk's launch is not queued behind the whole upload
-    int issued = -1, waited = -1;
+    const ChunkBounds& cb = P->chunks;
+    const int nch = cb.nch;
+    int issued = -1, waited[2] = {-1, -1};
     auto issue_piece = [&](int i) -> cudaError_t {
-        const int64_t i0 = n * i / kHostChunks, i1 = n * (i + 1) / kHostChunks;
+        const int64_t i0 = cb.b[i], i1 = cb.b[i + 1];
         cudaError_t e = cudaMemcpyAsync(P->hf + i0, h_f + i0, sizeof(double) * (size_t)(i1 - i0),
                                         cudaMemcpyHostToDevice, P->h2d_stream);
         if (e == cudaSuccess) e = split_f64(P->hf + i0, i1 - i0, P->f2 + i0, P->h2d_stream);
         if (e == cudaSuccess) e = cudaEventRecord(P->piece_ev[i], P->h2d_stream);
         return e;
     };
-    for (int c = 0; c < kHostChunks; ++c) {
-        const int64_t r0 = n * c / kHostChunks, r1 = n * (c + 1) / kHostChunks;
+    if (out_mapped && f_mapped) {
+        // the field is pinned too: the split kernel reads it in place, in two
+        // pieces, the first covering every index that rows [0, b[3]) read
+        int64_t reach = 0;
+        for (int c = 0; c < std::min(3, nch); ++c) reach = std::max(reach, P->chunk_reach[c]);
+        const int64_t p0 = std::min(n, reach + 1);
+        DCPSE_CK(split_f64(f_mapped, p0, P->f2, P->h2d_stream));
+        DCPSE_CK(cudaEventRecord(P->piece_ev[0], P->h2d_stream));
+        if (p0 < n) DCPSE_CK(split_f64(f_mapped + p0, n - p0, P->f2 + p0, P->h2d_stream));
+        DCPSE_CK(cudaEventRecord(P->piece_ev[1], P->h2d_stream));
+        DCPSE_CK(cudaStreamWaitEvent(P->stream, P->piece_ev[0], 0));
+        const int64_t g[4] = {0, cb.b[std::min(1, nch)], cb.b[std::min(3, nch)], n};
+        for (int gi = 0; gi < 3; ++gi) {
+            if (gi == 2) DCPSE_CK(cudaStreamWaitEvent(P->stream, P->piece_ev[1], 0));
+            if (g[gi] >= g[gi + 1]) continue;
+            if (int rc = apply_f32_rows(P, precision, out_mapped, g[gi], g[gi + 1])) {
+                cudaStreamSynchronize(P->h2d_stream);
+                return rc;
+            }
+        }
+        // the direct kernels of the row ranges report no device errors: a
+        // synchronisation of the plan's stream puts the outputs in place
+        DCPSE_CK(cudaStreamSynchronize(P->h2d_stream));
+        DCPSE_CK(cudaStreamSynchronize(P->stream));
+        return DCPSE_OK;
+    }
+    if (out_mapped) {
+        // row chunks = pieces [0, 1), [1, 3), [3, nch): the first starts after
+        // a short upload, the last is one kernel for the bulk of the rows
+        const int groups[4] = {0, std::min(1, nch), std::min(3, nch), nch};
+        for (int gi = 0; gi < 3; ++gi) {
+            const int c0 = groups[gi], c1 = groups[gi + 1];
+            if (c0 >= c1) continue;
+            int64_t reach = 0;
+            for (int c = c0; c < c1; ++c) reach = std::max(reach, P->chunk_reach[c]);
+            int need = 0;
+            while (need + 1 < nch && cb.b[need + 1] <= reach) ++need;
+            const int upto = std::min(nch - 1, std::max(need, c1));
+            while (issued < upto) DCPSE_CK(issue_piece(++issued));
+            if (need > waited[0]) {
+                DCPSE_CK(cudaStreamWaitEvent(P->stream, P->piece_ev[need], 0));
+                waited[0] = need;
+            }
+            if (int rc = apply_f32_rows(P, precision, out_mapped, cb.b[c0], cb.b[c1])) {
+                cudaStreamSynchronize(P->h2d_stream);
+                return rc;
+            }
+        }
+        while (issued < nch - 1) DCPSE_CK(issue_piece(++issued));
+        DCPSE_CK(cudaStreamSynchronize(P->h2d_stream));
+        DCPSE_CK(cudaStreamSynchronize(P->stream));
+        return DCPSE_OK;
+    }
+    for (int c = 0; c < nch; ++c) {
+        const int64_t r0 = cb.b[c], r1 = cb.b[c + 1];
         // the piece holding the largest index this chunk reads
         int need = 0;
-        while (need + 1 < kHostChunks && n * (need + 1) / kHostChunks <= P->chunk_reach[c]) ++need;
+        while (need + 1 < nch && cb.b[need + 1] <= P->chunk_reach[c]) ++need;
         // one piece of look-ahead keeps the copy engine busy
-        const int upto = std::min(kHostChunks - 1, std::max(need, c + 1));
+        const int upto = std::min(nch - 1, std::max(need, c + 1));
         while (issued < upto) DCPSE_CK(issue_piece(++issued));
-        if (need > waited) {
-            DCPSE_CK(cudaStreamWaitEvent(P->stream, P->piece_ev[need], 0));
-            waited = need;
+        // consecutive chunks alternate between two streams (they are
+        // independent), so one chunk's last blocks overlap the next one's
+        // first instead of draining the GPU at every kernel boundary
+        const int sid = c & 1;
+        cudaStream_t cs = sid ? P->apply2_stream : P->stream;
+        if (need > waited[sid]) {
+            DCPSE_CK(cudaStreamWaitEvent(cs, P->piece_ev[need], 0));
+            waited[sid] = need;
         }
-        if (int rc = apply_f32_rows(P, precision, P->hout, r0, r1)) {
+        if (int rc = apply_f32_rows(P, precision, P->hout, r0, r1, cs)) {
             cudaStreamSynchronize(P->h2d_stream);
+            cudaStreamSynchronize(P->apply2_stream);
             cudaStreamSynchronize(P->copy_stream);
             return rc;
         }
-        DCPSE_CK(cudaEventRecord(P->chunk_ev[c], P->stream));
+        DCPSE_CK(cudaEventRecord(P->chunk_ev[c], cs));
         DCPSE_CK(cudaStreamWaitEvent(P->copy_stream, P->chunk_ev[c], 0));
         // rows [r0, r1) of every output: one strided copy
         DCPSE_CK(cudaMemcpy2DAsync(h_out + r0, sizeof(double) * (size_t)n, P->hout + r0, sizeof(double) * (size_t)n,
                                    sizeof(double) * (size_t)(r1 - r0), (size_t)P->nout, cudaMemcpyDeviceToHost,
                                    P->copy_stream));
     }
-    while (issued < kHostChunks - 1) DCPSE_CK(issue_piece(++issued));
+    while (issued < nch - 1) DCPSE_CK(issue_piece(++issued));
     // rows never wait on pieces beyond their reach; the last piece must
-    // still be done before the call returns
+    // still be done before the call returns (the copy stream waited for
+    // every chunk, on both apply streams)
     DCPSE_CK(cudaStreamSynchronize(P->h2d_stream));
     DCPSE_CK(cudaStreamSynchronize(P->copy_stream));
     return dcpse_plan_check(P);

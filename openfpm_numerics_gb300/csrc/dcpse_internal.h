@@ -306,6 +306,10 @@ cudaError_t rk_transpose_weights(const int64_t* rowptr, const int64_t* tidx, int
 
 int num_sms();
 
+// Rows one full wave of the direct FP32 apply kernel covers (every block
+// slot of the GPU busy once), for the given or the automatic lane count.
+int64_t f32_rows_per_wave(int64_t n, int64_t nnz, int lanes);
+
 // Records msg as this thread's dcpse_last_error() and returns code.
 int set_error(int code, const char* msg);
 

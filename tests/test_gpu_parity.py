@@ -325,7 +325,8 @@ def test_term_basis_matches_oracle(cuda, orc):
 
 def test_host_apply_chunked_equals_device(cuda):
     """Host buffers above the chunking threshold: the outputs come back in row
-    chunks overlapped with the apply; they equal the device apply bit for bit
+    chunks overlapped with the apply (pageable outputs) or are stored by the
+    apply itself (pinned outputs); both equal the device apply bit for bit
     (also with the bf16 residual stream)."""
     pos, h = W.lattice(48, 3, jitter=0.15, seed=19)
     plan = DcpsePlan(3, GRAD_LAP_3D, order=2)
@@ -333,9 +334,19 @@ def test_host_apply_chunked_equals_device(cuda):
     plan.build_neighbors(pt, 2.8 * h)
     plan.assemble(pt, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID)
     f = np.cos(5 * pos[:, 0]) * pos[:, 2] + pos[:, 1]
+    # pinned outputs are written by the kernels directly (mapped host memory)
+    pinned = torch.empty((plan.n_outputs, pos.shape[0]), dtype=torch.float64, pin_memory=True)
+    pinned_f = torch.tensor(f).pin_memory()
     for prec in (C.F32, C.F32_RESID):
         dev = plan.apply(torch.tensor(f, device="cuda"), prec).cpu().numpy()
         for _ in range(2):
             host = plan.apply_host(f, precision=prec)
             assert np.array_equal(host, dev)
+            pinned.fill_(np.nan)
+            plan.apply_host(f, pinned.numpy(), precision=prec)
+            assert np.array_equal(pinned.numpy(), dev)
+            # pinned field as well: split in place from host memory
+            pinned.fill_(np.nan)
+            plan.apply_host(pinned_f.numpy(), pinned.numpy(), precision=prec)
+            assert np.array_equal(pinned.numpy(), dev)
     plan.close()
