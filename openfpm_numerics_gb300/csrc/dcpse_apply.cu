@@ -36,13 +36,42 @@ namespace dcpse {
 namespace {
 
 // ------------------------------------------------------------ FP64 term ---
+// The thread-per-row FP64 kernels below are bound by the FP64 pipe, where a
+// warp instruction costs the same with idle lanes: a warp whose rows differ
+// in length runs every lane to its longest row.  Each block therefore takes
+// a window of 256 consecutive rows (neighbourhoods that overlap, so gathers
+// stay in L1) and hands them to its threads longest first: the 32 rows of a
+// warp then have nearly equal lengths.  Which thread sums a row does not
+// change the row's sum.  blockDim.x must be 256.
+__device__ __forceinline__ int64_t row_by_length(int64_t base, int64_t n, const int64_t* __restrict__ rowptr,
+                                                 int* s_len, int* s_row) {
+    const int t = threadIdx.x;
+    const int64_t p0 = base + t;
+    const int len = p0 < n ? (int)(rowptr[p0 + 1] - rowptr[p0]) : -1;
+    s_len[t] = len;
+    __syncthreads();
+    int rank = 0;  // longer rows first, ties in row order
+    for (int j = 0; j < 256; ++j) {
+        const int lj = s_len[j];
+        rank += (lj > len) | ((lj == len) & (j < t));
+    }
+    s_row[rank] = t;
+    __syncthreads();
+    const int64_t p = base + s_row[t];
+    __syncthreads();  // the next window rewrites s_len and s_row
+    return p;         // >= n: no row for this thread
+}
+
 __global__ void __launch_bounds__(256) apply_term_f64_kernel(int64_t n, const int64_t* __restrict__ rowptr,
                                                              const int32_t* __restrict__ cols,
                                                              const double* __restrict__ K,
                                                              const double* __restrict__ eip, double sign,
                                                              const double* __restrict__ f, double* __restrict__ out,
                                                              int accumulate) {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    __shared__ int s_len[256], s_row[256];
+    for (int64_t base = (int64_t)blockIdx.x * 256; base < n; base += (int64_t)gridDim.x * 256) {
+        const int64_t p = row_by_length(base, n, rowptr, s_len, s_row);
+        if (p >= n) continue;
         const double fxp = sign * f[p];
         double D = 0.0;
         const int64_t e = rowptr[p + 1];
@@ -74,7 +103,10 @@ __global__ void __launch_bounds__(256) p2p_f64_kernel(int64_t n, const int64_t* 
                                                       const int32_t* __restrict__ cols, const double* __restrict__ K,
                                                       const double* __restrict__ eip, int ncomp,
                                                       const double* __restrict__ f, double* __restrict__ out) {
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    __shared__ int s_len[256], s_row[256];
+    for (int64_t base = (int64_t)blockIdx.x * 256; base < n; base += (int64_t)gridDim.x * 256) {
+        const int64_t p = row_by_length(base, n, rowptr, s_len, s_row);
+        if (p >= n) continue;
         const int64_t b = rowptr[p], e = rowptr[p + 1];
         for (int c = 0; c < ncomp; ++c) {
             double D = 0.0;
