@@ -143,6 +143,16 @@ VerletList getVerlet(particles_type& parts, double rCut, bool skip_ref = true) {
     return detail::build_verlet(dim, detail::positions(parts, dim), nullptr, rCut, skip_ref);
 }
 
+// vector_dist::getVerletAdaptRCut: every particle's cutoff is its property
+// 0; q is a neighbour of p when |x_p - x_q|^2 < rCut_p^2
+template <typename particles_type>
+VerletList getVerletAdaptRCut(particles_type& parts, bool skip_ref = true) {
+    const int dim = particles_type::dims;
+    std::vector<double> rc(parts.size_local());
+    for (std::size_t p = 0; p < parts.size_local(); ++p) rc[p] = (double)parts.template getProp<0>(p);
+    return detail::build_verlet(dim, detail::positions(parts, dim), nullptr, 0.0, skip_ref, &rc);
+}
+
 // --------------------------------------------------------------- operators --
 // Which reference class an operator's terms follow: Dcpse (the default), or
 // Dcpse_gpu for the *_gpu aliases (DCPSE_op.hpp:3510-3530), i.e. eps = 2 <h>
@@ -176,7 +186,7 @@ public:
     // operator extends the support again from the current normals
     template <typename particles_type>
     void update(particles_type& parts) {
-        if (surf_.on) surf_.normals = surf_.read_normals();
+        if (surf_.on) surf_.refresh();
         build(parts, true);
     }
 

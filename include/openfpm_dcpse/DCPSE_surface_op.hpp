@@ -21,7 +21,7 @@ public:
                     std::vector<unsigned> sig, support_options opt)
         : DcpseOperator<VerletList_type>(parts, verletList, ord, {{sig}}, opt,
                                          detail::surface_cfg<NORMAL_ID>(parts, verletList, (double)rCut,
-                                                                        (double)nSpacing, nCount)) {}
+                                                                        (double)nSpacing, nCount, opt)) {}
 };
 
 #define OPENFPM_DCPSE_SURFACE_OP(NAME, SIGEXPR)                                                                 \

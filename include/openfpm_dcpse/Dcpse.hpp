@@ -86,6 +86,19 @@ struct SurfaceCfg {
     double spacing = 0.0;
     double rcut = 0.0;
     bool skip_ref = true;
+    // support_options::ADAPTIVE: spacing along the normal per support particle
+    // (property 0 / nCount) and the adaptive list's per-particle cutoffs
+    std::vector<double> spacings;
+    std::function<std::vector<double>()> read_spacings;
+    std::vector<double> rcuts;
+    std::function<std::vector<double>()> read_rcuts;
+
+    // re-read what depends on the particles (an update after they moved)
+    void refresh() {
+        if (read_normals) normals = read_normals();
+        if (read_spacings) spacings = read_spacings();
+        if (read_rcuts) rcuts = read_rcuts();
+    }
 };
 
 template <typename VL>
@@ -104,11 +117,37 @@ bool list_skip_ref(const VL& vl) {
         return true;
 }
 
+template <typename VL>
+std::vector<double> list_rcuts(const VL& vl) {
+    if constexpr (std::is_same<VL, VerletList>::value)
+        return vl.rcuts;
+    else
+        return {};
+}
+
 template <unsigned int NORMAL_ID, typename Parts, typename VL>
-SurfaceCfg surface_cfg(Parts& sup, const VL& vl, double rCut, double nSpacing, unsigned nCount) {
+SurfaceCfg surface_cfg(Parts& sup, const VL& vl, double rCut, double nSpacing, unsigned nCount,
+                       support_options opt = support_options::RADIUS) {
     SurfaceCfg c;
     c.on = true;
     Parts* ps = &sup;
+    if (opt == support_options::ADAPTIVE) {
+        // nSpacing_p = property 0 / nCount (Dcpse.hpp:1055-1066); the support
+        // of particle p reaches the cutoff of the adaptive list
+        if (nCount == 0) throw std::invalid_argument("support_options::ADAPTIVE needs nCount > 0");
+        c.read_spacings = [ps, nCount]() {
+            std::vector<double> sp(ps->size_local());
+            for (std::size_t p = 0; p < ps->size_local(); ++p)
+                sp[p] = (double)ps->template getProp<0>(p) / (double)nCount;
+            return sp;
+        };
+        c.spacings = c.read_spacings();
+        const VL* pvl = &vl;
+        c.read_rcuts = [pvl]() { return list_rcuts(*pvl); };
+        c.rcuts = c.read_rcuts();
+        if (c.rcuts.size() != sup.size_local())
+            throw std::invalid_argument("support_options::ADAPTIVE needs an adaptive Verlet list (getVerletAdaptRCut)");
+    }
     c.read_normals = [ps]() {
         const int dim = Parts::dims;
         std::vector<double> nrm(ps->size_local() * dim);
@@ -243,8 +282,18 @@ public:
         nrm_.upload(c.normals.data(), std::max<std::size_t>(c.normals.size(), 1) * sizeof(double));
         check(dcpse_plan_set_support(plan_, two_set ? (const double*)spos_.get() : nullptr, two_set ? n_sup_ : 0,
                                      c.skip_ref ? 1 : 0));
-        check(dcpse_plan_set_surface(plan_, (const double*)nrm_.get(), c.n_count, c.spacing, nullptr));
-        check(dcpse_build_neighbors(plan_, (const double*)pos_.get(), n_, c.rcut, nullptr));
+        const double* d_spacings = nullptr;
+        if (!c.spacings.empty()) {
+            spc_.upload(c.spacings.data(), c.spacings.size() * sizeof(double));
+            d_spacings = (const double*)spc_.get();
+        }
+        check(dcpse_plan_set_surface(plan_, (const double*)nrm_.get(), c.n_count, c.spacing, d_spacings));
+        const double* d_rcuts = nullptr;
+        if (!c.rcuts.empty()) {
+            rcs_.upload(c.rcuts.data(), c.rcuts.size() * sizeof(double));
+            d_rcuts = (const double*)rcs_.get();
+        }
+        check(dcpse_build_neighbors(plan_, (const double*)pos_.get(), n_, d_rcuts ? 0.0 : c.rcut, d_rcuts));
         surface_ = true;
         cache_valid_ = false;
     }
@@ -338,7 +387,7 @@ private:
     std::vector<unsigned> term_order_;
     std::vector<int64_t> rowptr_;
     std::vector<int32_t> cols_;
-    DevBuf pos_, spos_, nrm_, fd_, od_;
+    DevBuf pos_, spos_, nrm_, spc_, rcs_, fd_, od_;
     bool surface_ = false;
     bool cache_valid_ = false;
     std::vector<std::vector<double>> K_, eip_;
@@ -428,7 +477,7 @@ OPENFPM_DCPSE_NO_CONTRACT T reference_sum(std::size_t k, FQ fq, T fxp, const dou
 // the particles at sup (or dom itself, with or without the particle in its
 // own list when sup is null).
 inline VerletList build_verlet(int dim, const std::vector<double>& dom, const std::vector<double>* sup, double rCut,
-                               bool skip_ref) {
+                               bool skip_ref, const std::vector<double>* rcut_pp = nullptr) {
     std::vector<unsigned> sig(dim, 0);
     sig[0] = 1;
     int terms = 1;
@@ -444,10 +493,14 @@ inline VerletList build_verlet(int dim, const std::vector<double>& dom, const st
     } else {
         check(dcpse_plan_set_support(plan, nullptr, 0, skip_ref ? 1 : 0));
     }
-    check(dcpse_build_neighbors(plan, (const double*)dpos.get(), n, rCut, nullptr));
+    DevBuf drc;
+    if (rcut_pp) drc.upload(rcut_pp->data(), std::max<std::size_t>(rcut_pp->size(), 1) * sizeof(double));
+    check(dcpse_build_neighbors(plan, (const double*)dpos.get(), n, rCut,
+                                rcut_pp ? (const double*)drc.get() : nullptr));
     VerletList vl;
     vl.rCut = rCut;
     vl.skip_ref = skip_ref && !sup;
+    if (rcut_pp) vl.rcuts = *rcut_pp;
     int64_t nn = 0, nnz = 0;
     check(dcpse_plan_info(plan, &nn, &nnz, nullptr, nullptr, nullptr));
     const int64_t* drp = nullptr;
@@ -645,7 +698,7 @@ public:
         domain_ = same_set(particles);
         plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder_, (double)HOverEpsilon));
         if (surface_.on) {
-            surface_.normals = surface_.read_normals();
+            surface_.refresh();
             set_sets();
         } else {
             plan_->set_particles(particles, verletList_);
@@ -656,7 +709,7 @@ public:
         support_ = &particlesSupport;
         domain_ = &particlesDomain;
         plan_.reset(new detail::PlanHost(dim, {{sig_}}, convergenceOrder_, (double)HOverEpsilon));
-        if (surface_.on) surface_.normals = surface_.read_normals();
+        if (surface_.on) surface_.refresh();
         set_sets();
         assemble();
     }
@@ -827,7 +880,9 @@ private:
 // extended support and every virtual particle's kernel is added onto its
 // surface particle.  The Verlet list handed in gives the cutoff and whether
 // a particle is its own neighbour, and receives the accumulated lists.
-// support_options::ADAPTIVE (per-particle spacings) is not provided here.
+// support_options::ADAPTIVE takes the spacing along the normal per particle
+// from property 0 / nCount and the cutoffs of an adaptive Verlet list
+// (getVerletAdaptRCut), as the reference does (Dcpse.hpp:1055-1066, 881-909).
 template <unsigned int dim, typename VerletList_type, typename vector_type, typename vector_type2 = vector_type>
 class SurfaceDcpse : public Dcpse<dim, VerletList_type, vector_type, vector_type2> {
     typedef Dcpse<dim, VerletList_type, vector_type, vector_type2> base;
@@ -839,7 +894,8 @@ public:
                  typename base::T nSpacing, unsigned int nCount, value_t<NORMAL_ID>,
                  support_options opt = support_options::RADIUS)
         : base(particlesSupport, particlesDomain, verletList, differentialSignature, convergenceOrder, rCut, opt,
-               detail::surface_cfg<NORMAL_ID>(particlesSupport, verletList, (double)rCut, (double)nSpacing, nCount)) {}
+               detail::surface_cfg<NORMAL_ID>(particlesSupport, verletList, (double)rCut, (double)nSpacing, nCount,
+                                              opt)) {}
 };
 
 }  // namespace openfpm_dcpse

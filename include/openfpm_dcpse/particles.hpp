@@ -106,6 +106,9 @@ public:
     std::vector<int32_t> cols;
     double rCut = 0.0;        // cutoff the list was built with
     bool skip_ref = true;     // VL_SKIP_REF_PART: a particle is not its own neighbour
+    std::vector<double> rcuts;  // per-particle cutoffs of an adaptive list (empty: rCut for all)
+
+    double getRCuts(std::size_t p) const { return rcuts.empty() ? rCut : rcuts[p]; }
 
     std::size_t getNNPart(std::size_t p) const { return (std::size_t)(rowptr[p + 1] - rowptr[p]); }
     std::size_t getNNPart(vect_dist_key_dx p) const { return getNNPart(p.getKey()); }

@@ -481,6 +481,59 @@ static void test_gpu_aliases() {
     }
 }
 
+// DCPSE_op_Surface_tests.cpp:756-900 (dcpse_surface_adaptive_unitSphere):
+// Laplace-Beltrami of Y_2^0 on 2000 Fibonacci points, once with a regular
+// list (rCut = 2 h, nSpacing = h, nCount = 2) and once with
+// support_options::ADAPTIVE (cutoff and 2 x spacing per particle in property
+// 0); the reference requires equal L2 and Linf errors within 0.001 %.
+typedef vector_dist<3, double, double, std::array<double, 3>, double, double, double> Parts3S;
+
+static void test_surface_adaptive() {
+    const int n = 2000;
+    const double h = std::sqrt(4 * M_PI / n);
+    Parts3S part(n);
+    const double ga = M_PI * (3.0 - std::sqrt(5.0));
+    std::vector<double> analyt(n);
+    for (int i = 0; i < n; ++i) {
+        const double y = 1.0 - 2.0 * (i / double(n - 1));
+        const double rad = std::sqrt(1.0 - y * y), th = ga * i;
+        const double x = std::cos(th) * rad, z = std::sin(th) * rad;
+        const double thetaB = std::atan2(std::sqrt(x * x + y * y), z), phi = std::atan2(y, x);
+        part.getPos(i)[0] = x;
+        part.getPos(i)[1] = y;
+        part.getPos(i)[2] = z;
+        part.getProp<1>(i) = {std::sin(thetaB) * std::cos(phi), std::sin(thetaB) * std::sin(phi), std::cos(thetaB)};
+        part.getProp<0>(i) = 2 * h;
+        part.getProp<2>(i) = 0.25 * std::sqrt(5 / M_PI) * (3 * std::cos(thetaB) * std::cos(thetaB) - 1);
+        analyt[i] = -6 * part.getProp<2>(i);
+    }
+    VerletList vreg = getVerlet(part, 2 * h);
+    VerletList vad = getVerletAdaptRCut(part);
+    EXPECT(vad.rcuts.size() == (std::size_t)n && vad.getRCuts(7) == 2 * h, "adaptive list keeps the per-particle cutoffs");
+    SurfaceDerivative_xx<1, VerletList> xr(part, vreg, 2, 0, h, 2);
+    SurfaceDerivative_yy<1, VerletList> yr(part, vreg, 2, 0, h, 2);
+    SurfaceDerivative_zz<1, VerletList> zr(part, vreg, 2, 0, h, 2);
+    getV<3>(part) = xr(getV<2>(part)) + yr(getV<2>(part)) + zr(getV<2>(part));
+    SurfaceDerivative_xx<1, VerletList> xa(part, vad, 2, 0, 0, 2, support_options::ADAPTIVE);
+    SurfaceDerivative_yy<1, VerletList> ya(part, vad, 2, 0, 0, 2, support_options::ADAPTIVE);
+    SurfaceDerivative_zz<1, VerletList> za(part, vad, 2, 0, 0, 2, support_options::ADAPTIVE);
+    getV<4>(part) = xa(getV<2>(part)) + ya(getV<2>(part)) + za(getV<2>(part));
+    double l2r = 0, l2a = 0, lir = 0, lia = 0;
+    for (int i = 0; i < n; ++i) {
+        const double er = std::fabs(part.getProp<3>(i) - analyt[i]), ea = std::fabs(part.getProp<4>(i) - analyt[i]);
+        l2r += er * er;
+        l2a += ea * ea;
+        lir = std::max(lir, er);
+        lia = std::max(lia, ea);
+    }
+    l2r = std::sqrt(l2r / n);
+    l2a = std::sqrt(l2a / n);
+    std::printf("     adaptive sphere: L2 %.6e / %.6e, Linf %.6e / %.6e\n", l2r, l2a, lir, lia);
+    EXPECT(std::fabs(l2r - l2a) <= 1e-5 * l2r && std::fabs(lir - lia) <= 1e-5 * lir,
+           "ADAPTIVE surface Laplacian equals the regular one within 0.001 %");
+    EXPECT(l2r < 0.5, "surface Laplacian of Y_2^0 on 2000 points: L2 error < 0.5");
+}
+
 int main() {
     try {
         test_dcpse_class();
@@ -492,6 +545,7 @@ int main() {
         test_vector_operators();
         test_surface_operators();
         test_gpu_aliases();
+        test_surface_adaptive();
     } catch (const std::exception& e) {
         std::printf("FAIL exception: %s\n", e.what());
         return 2;

@@ -144,3 +144,34 @@ def test_surface_interpolation_sphere(cuda, orc):
     ref = orc.p2p(Y(pf), rp2, c2, K2[0], eip)
     assert np.array_equal(dom.props[0].cpu().numpy(), ref)
     pp.deallocate()
+
+
+def test_surface_adaptive_equals_regular_sphere(cuda):
+    """DCPSE_op_Surface_tests.cpp:756-900 (dcpse_surface_adaptive_unitSphere):
+    Laplace-Beltrami of Y_2^0 on 2000 Fibonacci points with a regular list
+    (rCut = 2 h, nSpacing = h, nCount = 2) and with support_options.ADAPTIVE
+    (cutoff 2 h per particle in property 0, spacing = property 0 / nCount);
+    the reference requires equal L2 and Linf errors within 0.001 %."""
+    n = 2000
+    h = np.sqrt(4 * np.pi / n)
+    ga = np.pi * (3.0 - np.sqrt(5.0))
+    i = np.arange(n)
+    y = 1.0 - 2.0 * (i / (n - 1.0))
+    rad = np.sqrt(1.0 - y * y)
+    x, z = np.cos(ga * i) * rad, np.sin(ga * i) * rad
+    tb, ph = np.arctan2(np.sqrt(x * x + y * y), z), np.arctan2(y, x)
+    pos = np.stack([x, y, z], 1)
+    nrm = np.stack([np.sin(tb) * np.cos(ph), np.sin(tb) * np.sin(ph), np.cos(tb)], 1)
+    y20 = 0.25 * np.sqrt(5 / np.pi) * (3 * np.cos(tb) ** 2 - 1)
+    parts = O.ParticleSet(pos)
+    parts.props[0] = torch.full((n,), 2 * h, dtype=torch.float64, device="cuda")
+    parts.props[1] = torch.tensor(nrm, device="cuda")
+    f = torch.tensor(y20, device="cuda")
+    vreg = parts.getVerlet(2 * h)
+    vad = O.VerletList(parts, 0.0, rcut_pp=parts.props[0])
+    classes = (O.SurfaceDerivative_xx, O.SurfaceDerivative_yy, O.SurfaceDerivative_zz)
+    lap_r = sum(c(parts, vreg, 2, 0.0, h, 2, normal=1)(f) for c in classes).cpu().numpy()
+    lap_a = sum(c(parts, vad, 2, 0.0, 0.0, 2, O.support_options.ADAPTIVE, normal=1)(f) for c in classes).cpu().numpy()
+    er, ea = np.abs(lap_r + 6 * y20), np.abs(lap_a + 6 * y20)
+    l2r, l2a = np.sqrt((er ** 2).mean()), np.sqrt((ea ** 2).mean())
+    assert abs(l2r - l2a) <= 1e-5 * l2r and abs(er.max() - ea.max()) <= 1e-5 * er.max()
