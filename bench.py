@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--only", choices=["apply", "assemble", "gray-scott", "graded", "interp"], default=None,
                     help="small-footprint run of one kernel family (for profiler captures)")
     ap.add_argument("--lanes", type=int, default=0)
-    ap.add_argument("--mode", type=int, default=0, help="apply loading: 0 auto, 1 direct, 2 TMA-staged")
+    ap.add_argument("--mode", type=int, default=0, help="apply kernel: 0 auto, 1 CSR direct, 2 CSR TMA-staged, 3 CSR 8-deep, 4 sliced ELL")
     ap.add_argument("--qr-lanes", type=int, default=0, help="assembly QR lanes per particle (0 = automatic)")
     return ap.parse_args()
 
@@ -345,7 +345,10 @@ def run_ours(args):
     t_kernel = k_ms / 1e3 / max(k_launch, 1)
     achieved = bytes_apply / t_kernel / 1e9
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "apply_f32_grad_lap_128cube.txt")
+    kname = {"tma-staged": "apply_f32_tma_kernel", "sliced-ell": "apply_sell_kernel"}.get(tuned["mode"],
+                                                                                       "apply_f32_kernel")
+    tf = os.path.join(ROOT, "profiles", ("apply_sell_grad_lap_128cube.txt" if kname == "apply_sell_kernel"
+                                         else "apply_f32_grad_lap_128cube.txt"))
     if os.path.exists(tf):
         for ln in open(tf):
             if ln.startswith("traffic_bytes_per_launch:"):
@@ -380,7 +383,7 @@ def run_ours(args):
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "apply_f32_tma_kernel" if tuned["mode"] == "tma-staged" else "apply_f32_kernel",
+                         "kernel": kname,
                          "algorithmic_bytes_per_launch": bytes_apply, "kernel_ms": t_kernel * 1e3},
             "e2e": {"value": world * N * NOUT / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": N * 8,
                     "d2h_bytes_per_step": NOUT * N * 8, "ms_per_step": t_e2e * 1e3,

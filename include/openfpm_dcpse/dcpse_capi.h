@@ -286,12 +286,18 @@ int dcpse_plan_set_timing(dcpse_plan_t* plan, int enable);
  * (2 flops per FMA): the ceiling the FP64 assembly is reported against.
  * No counterpart in the reference. */
 int dcpse_measure_fp64_peak(void* stream, double* tflops);
-/* Apply schedule knobs (autotuning): lanes per row (0 = from the mean row
- * length, else 4/8/16/32) and loading mode (0 = automatic: direct loads,
- * which beat the staged kernel at every size measured on GB300; 1 = direct
- * loads, 2 = TMA-staged, 3 = direct loads with 8-deep batches).  OR-ing DCPSE_APPLY_COMPENSATE_ALL into the mode makes
- * every output of the FP32 apply use the compensated sum (by default only
- * outputs with a term of order >= 2 do; the others take plain fused sums). */
+/* Apply schedule knobs (autotuning): lanes per row of the CSR kernels (0 =
+ * from the mean row length, else 4/8/16/32) and the kernel (0 = automatic:
+ * the sliced ELL kernel for DCPSE_F32 applies of whole operators, the direct
+ * CSR kernel otherwise; 1 = CSR, direct loads; 2 = CSR, TMA-staged tiles;
+ * 3 = CSR, direct loads in 8-deep batches; 4 = sliced ELL: the FP32 weights
+ * in slices of 32 rows stored entry-major, rows sorted by length within
+ * windows of 256, a row per thread; it keeps a second copy of the FP32
+ * weights, built at assembly, and falls back to the CSR kernels when that
+ * copy does not fit in device memory).  OR-ing DCPSE_APPLY_COMPENSATE_ALL
+ * into the mode makes every output of the FP32 apply use the compensated sum
+ * (by default only outputs with a term of order >= 2 do; the others take
+ * plain fused sums). */
 #define DCPSE_APPLY_COMPENSATE_ALL 16
 int dcpse_plan_set_apply_config(dcpse_plan_t* plan, int lanes, int mode);
 /* Assembly schedule knobs (autotuning): particles are processed in bins of

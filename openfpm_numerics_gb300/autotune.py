@@ -1,10 +1,12 @@
 """Autotuner of the batched apply schedule.
 
 Sweeps the lanes that share a neighbour row (4/8/16/32) and the loading mode
-(direct loads vs TMA-staged tiles) for a plan and a field, times each
-candidate with CUDA events on the plan's stream, keeps the fastest and sets
-it on the plan.  All candidates compute the same result up to the order of
-the FP32 partial sums (identical bits for the same lane count).
+of the CSR kernels (direct loads, TMA-staged tiles, 8-deep batches), and the
+sliced ELL kernel (a row per thread, lanes do not apply), for a plan and a
+field; times each candidate with CUDA events on the plan's stream, keeps the
+fastest and sets it on the plan.  All candidates compute the same result up
+to the order of the FP32 partial sums (identical bits for the same CSR lane
+count).
 """
 from __future__ import annotations
 
@@ -12,36 +14,36 @@ import torch
 
 from . import _capi as C
 
-MODES = {1: "direct", 2: "tma-staged", 3: "direct-x8"}
+MODES = {1: "direct", 2: "tma-staged", 3: "direct-x8", 4: "sliced-ell"}
 
 
-def tune_apply(plan, f, precision=C.F32, lanes=(4, 8, 16), modes=(1, 2, 3), reps=10, warmup=2):
+def tune_apply(plan, f, precision=C.F32, lanes=(4, 8, 16), modes=(1, 2, 3, 4), reps=10, warmup=2):
     out = torch.empty((plan.n_outputs, f.shape[0]), dtype=torch.float64, device=f.device)
     stream = plan.stream or torch.cuda.current_stream()
     table = []
     best = None
-    for ln in lanes:
-        for md in modes:
-            plan.set_apply_config(ln, md)
-            try:
-                plan.apply(f, precision, out)
-            except C.DcpseError as e:
-                if e.code != C.ERR_CAPACITY:
-                    raise
-                table.append({"lanes": ln, "mode": MODES[md], "ms": None, "skipped": "tiles do not fit"})
-                continue
-            for _ in range(warmup):
-                plan.apply(f, precision, out)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(reps):
-                plan.apply(f, precision, out)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / reps
-            table.append({"lanes": ln, "mode": MODES[md], "ms": ms})
-            if best is None or ms < best[2]:
-                best = (ln, md, ms)
+    cands = [(ln, md) for ln in lanes for md in modes if md != 4] + ([(0, 4)] if 4 in modes else [])
+    for ln, md in cands:
+        plan.set_apply_config(ln, md)
+        try:
+            plan.apply(f, precision, out)
+        except C.DcpseError as e:
+            if e.code != C.ERR_CAPACITY:
+                raise
+            table.append({"lanes": ln, "mode": MODES[md], "ms": None, "skipped": "tiles do not fit"})
+            continue
+        for _ in range(warmup):
+            plan.apply(f, precision, out)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            plan.apply(f, precision, out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        table.append({"lanes": ln, "mode": MODES[md], "ms": ms})
+        if best is None or ms < best[2]:
+            best = (ln, md, ms)
     plan.set_apply_config(best[0], best[1])
     plan.check()
     return {"lanes": best[0], "mode": MODES[best[1]], "ms": best[2], "sweep": table}

@@ -167,6 +167,33 @@ cudaError_t p2p_f64(int64_t n, const int64_t* rowptr, const int32_t* cols, const
 cudaError_t apply_batched_f32(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const float* w,
                               int64_t nnz, const float2* f2, double* out, cudaStream_t s);
 
+// Batched FP32 apply on the sliced ELL layout (SELL-32, rows sorted by length
+// within windows of 256): windows [w0, w1) of rows, thread per row.
+struct SellArgs {
+    int64_t n;             // rows
+    int64_t nslices;
+    const int32_t* srow;   // row of (slice, lane), -1 past the last row
+    const int64_t* off;    // [nslices + 1] first entry of each slice
+    const int32_t* cols;   // [total] entry-major within a slice
+    const float* w;        // [NO][total]
+    int64_t total;
+    const float2* f2;
+    double* out;           // output o of row r at out[o * oos + r * ors]
+    int64_t oos, ors;
+    int64_t w0, w1;        // windows of 256 rows
+    uint32_t comp;
+    int no_self;
+};
+int64_t sell_slices(int64_t n);
+// srow [sell_slices(n) * 32], slen32 [sell_slices(n)], off [sell_slices(n) + 1],
+// scan_tmp [scan_tmp_elems(sell_slices(n))]
+cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t* slen32, int64_t* off,
+                       int64_t* scan_tmp, cudaStream_t s);
+cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, int64_t ws, int nout, int64_t n,
+                      const int32_t* srow, const int64_t* off, int64_t total, int32_t* scols, float* sw,
+                      cudaStream_t s);
+cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s);
+
 // Full description of a batched FP32 apply (plan-owned, padded arrays).
 struct ApplyF32 {
     int64_t n;

@@ -1,0 +1,176 @@
+// dcpse_sell.cu -- the batched FP32 apply on a sliced ELL layout (SELL-32,
+// rows sorted by length within windows of 256).
+//
+// The CSR apply gives a row to G lanes and reduces their partial sums by
+// shuffles.  Here a row belongs to one thread: rows are grouped in slices of
+// 32 (one warp) whose entries are stored entry-major, so that entry j of the
+// 32 rows of a slice is one 128-byte line per stream, and no reduction is
+// needed.  Within each window of 256 consecutive rows the rows are ordered
+// by length (longest first) before they are cut into slices, so a slice pads
+// its rows to nearly their own length; the window keeps the rows of a block
+// spatially close, so the field gathers of its warps share L1 lines.
+// Padding entries point at the row's own particle with weight 0, which adds
+// exactly nothing.  The per-entry arithmetic (exact differences, compensated
+// sums for outputs of order >= 2) is the CSR kernel's (RowAcc).
+#include "dcpse_internal.h"
+#include "dcpse_f32_row.cuh"
+
+namespace dcpse {
+namespace {
+
+constexpr int kWin = 256;            // rows per window (one block)
+constexpr int kSlice = 32;           // rows per slice (one warp)
+constexpr int kSlicesPerWin = kWin / kSlice;
+
+// window w: rank its rows by length (longest first, ties in row order),
+// record the row of every (slice, lane) and each slice's length x 32
+__global__ void __launch_bounds__(kWin) sell_order_kernel(const int64_t* __restrict__ rowptr, int64_t n,
+                                                          int64_t nwin, int32_t* __restrict__ srow,
+                                                          int32_t* __restrict__ slen32) {
+    __shared__ int s_len[kWin];
+    for (int64_t w = blockIdx.x; w < nwin; w += gridDim.x) {
+        const int t = threadIdx.x;
+        const int64_t r = w * kWin + t;
+        const int len = r < n ? (int)(rowptr[r + 1] - rowptr[r]) : -1;
+        s_len[t] = len;
+        __syncthreads();
+        int rank = 0;
+        for (int j = 0; j < kWin; ++j) {
+            const int lj = s_len[j];
+            rank += (lj > len) | ((lj == len) & (j < t));
+        }
+        srow[w * kWin + rank] = r < n ? (int32_t)r : -1;
+        // the first row of a slice is its longest
+        if ((rank & (kSlice - 1)) == 0) slen32[w * kSlicesPerWin + rank / kSlice] = (len > 0 ? len : 0) * kSlice;
+        __syncthreads();
+    }
+}
+
+// warp per slice: copy the CSR entries of its rows into the slice, entry-major
+__global__ void __launch_bounds__(256) sell_fill_kernel(const int64_t* __restrict__ rowptr,
+                                                        const int32_t* __restrict__ cols,
+                                                        const float* __restrict__ w, int64_t ws, int nout,
+                                                        int64_t nslices, const int32_t* __restrict__ srow,
+                                                        const int64_t* __restrict__ off, int64_t total,
+                                                        int32_t* __restrict__ scols, float* __restrict__ sw) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp0; s < nslices; s += nwarps) {
+        const int32_t row = srow[s * kSlice + lane];
+        const int64_t b = off[s];
+        const int64_t L = (off[s + 1] - b) / kSlice;
+        const int64_t rb = row >= 0 ? rowptr[row] : 0;
+        const int64_t k = row >= 0 ? rowptr[row + 1] - rb : 0;
+        const int32_t self = row >= 0 ? row : 0;
+        for (int64_t j = 0; j < L; ++j) {
+            const int64_t idx = b + j * kSlice + lane;
+            const bool ok = j < k;
+            scols[idx] = ok ? cols[rb + j] : self;
+            for (int o = 0; o < nout; ++o) sw[(int64_t)o * total + idx] = ok ? w[(int64_t)o * ws + rb + j] : 0.0f;
+        }
+    }
+}
+
+// thread per row; block = one window of 8 slices (five blocks per SM fit the
+// registers without spills up to four outputs)
+template <int NO, int U>
+__global__ void __launch_bounds__(256, (NO <= 4 ? 5 : 4)) apply_sell_kernel(SellArgs a) {
+    // the window's outputs, staged so that they leave in row order (rows of a
+    // slice are permuted; scattered 8-byte stores are slow, above all into
+    // host memory over NVLink-C2C)
+    __shared__ double tile[NO][kWin];
+    const int lane = threadIdx.x & 31;
+    const float r0[NO] = {};
+    for (int64_t win = a.w0 + blockIdx.x; win < a.w1; win += gridDim.x) {
+        const int64_t s = win * kSlicesPerWin + (threadIdx.x >> 5);  // < nslices: windows hold 8 slices
+        const int32_t row = a.srow[s * kSlice + lane];
+        const int64_t b = a.off[s];
+        const int L = (int)((a.off[s + 1] - b) / kSlice);
+        const int32_t self = row >= 0 ? row : 0;
+        const float2 fp = (row >= 0 && !a.no_self) ? a.f2[row] : make_float2(0.f, 0.f);
+        RowAcc<NO, false> acc;
+        acc.init();
+        const int32_t* __restrict__ c = a.cols + b + lane;
+        const float* __restrict__ w = a.w + b + lane;
+        for (int j0 = 0; j0 < L; j0 += U) {
+            int32_t q[U];
+            float wv[U][NO];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = j0 + u;
+                const bool ok = j < L;
+                q[u] = ok ? c[(int64_t)j * kSlice] : self;
+#pragma unroll
+                for (int o = 0; o < NO; ++o) wv[u][o] = ok ? w[(int64_t)o * a.total + (int64_t)j * kSlice] : 0.0f;
+            }
+            float2 fq[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) fq[u] = a.f2[q[u]];
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc.add(wv[u], r0, fq[u], fp, a.comp);
+        }
+        if (row >= 0) {
+#pragma unroll
+            for (int o = 0; o < NO; ++o) tile[o][row - win * kWin] = acc.value(o);
+        }
+        __syncthreads();
+        const int64_t r = win * kWin + threadIdx.x;
+        if (r < a.n) {
+#pragma unroll
+            for (int o = 0; o < NO; ++o) a.out[(int64_t)o * a.oos + r * a.ors] = tile[o][threadIdx.x];
+        }
+        __syncthreads();  // the next window rewrites the tile
+    }
+}
+
+}  // namespace
+
+int64_t sell_slices(int64_t n) { return ((n + kWin - 1) / kWin) * kSlicesPerWin; }
+
+cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t* slen32, int64_t* off,
+                       int64_t* scan_tmp, cudaStream_t s) {
+    const int64_t nwin = (n + kWin - 1) / kWin;
+    if (nwin == 0) return cudaSuccess;
+    const int grid = (int)std::min<int64_t>(nwin, (int64_t)num_sms() * 8);
+    sell_order_kernel<<<grid, kWin, 0, s>>>(rowptr, n, nwin, srow, slen32);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return exclusive_scan_i32(slen32, nwin * kSlicesPerWin, off, scan_tmp, s);
+}
+
+cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, int64_t ws, int nout, int64_t n,
+                      const int32_t* srow, const int64_t* off, int64_t total, int32_t* scols, float* sw,
+                      cudaStream_t s) {
+    const int64_t ns = sell_slices(n);
+    if (ns == 0) return cudaSuccess;
+    const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 8);
+    sell_fill_kernel<<<grid, 256, 0, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, scols, sw);
+    return cudaGetLastError();
+}
+
+cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s) {
+    if (a.w1 <= a.w0) return cudaSuccess;
+    // one block per window: the block scheduler balances the windows
+    const int64_t grid = a.w1 - a.w0;
+    if (grid > 0x7fffffff) return cudaErrorInvalidValue;
+    constexpr int U = 4;
+    switch (nout) {
+#define DCPSE_SELL_CASE(NO) \
+    case NO: apply_sell_kernel<NO, U><<<(unsigned)grid, 256, 0, s>>>(a); break;
+        DCPSE_SELL_CASE(1)
+        DCPSE_SELL_CASE(2)
+        DCPSE_SELL_CASE(3)
+        DCPSE_SELL_CASE(4)
+        DCPSE_SELL_CASE(5)
+        DCPSE_SELL_CASE(6)
+        DCPSE_SELL_CASE(7)
+        DCPSE_SELL_CASE(8)
+#undef DCPSE_SELL_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace dcpse

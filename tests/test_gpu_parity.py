@@ -232,6 +232,18 @@ def test_apply_schedules(cuda, orc, name):
                 err = np.abs(g[o] - refs[o]).max() / np.abs(refs[o]).max()
                 assert err <= 1e-9, (lanes, mode, o, err)
     assert staged >= 1  # the TMA-staged kernel ran for at least one lane count
+    # sliced ELL layout (thread per row): within the FP32 bar, with and
+    # without compensated sums for every output; the residual precision
+    # falls back to the CSR kernels
+    for mode in (4, 4 | 16):
+        plan.set_apply_config(0, mode)
+        got = plan.apply(f, C.F32).cpu().numpy()
+        plan.check()
+        for o in range(len(refs)):
+            assert np.abs(got[o] - refs[o]).max() <= 1e-6 * np.abs(refs[o]).max(), (mode, o)
+        g = plan.apply(f, C.F32_RESID).cpu().numpy()
+        for o in range(len(refs)):
+            assert np.abs(g[o] - refs[o]).max() <= 1e-9 * np.abs(refs[o]).max(), (mode, o)
     plan.set_apply_config(0, 0)
 
 
@@ -265,7 +277,9 @@ def test_autotune(cuda):
     f = torch.tensor(np.random.default_rng(9).standard_normal(c["pos"].shape[0]), device="cuda")
     ref = plan.apply(f, C.F32).clone()
     best = autotune.tune_apply(plan, f, reps=2, warmup=1)
-    assert len(best["sweep"]) == 9 and best["lanes"] in (4, 8, 16)
+    # 3 lane counts x 3 CSR kernels + the sliced ELL kernel (lanes do not apply: 0)
+    assert len(best["sweep"]) == 10 and best["lanes"] in (0, 4, 8, 16)
+    assert any(e["mode"] == "sliced-ell" and e["ms"] is not None for e in best["sweep"])
     got = plan.apply(f, C.F32)
     assert torch.allclose(got, ref, rtol=0, atol=1e-6 * ref.abs().max().item())
 
