@@ -1574,7 +1574,7 @@ int ensure_sell(dcpse_plan_t* P) {
     if (e == cudaSuccess) e = dalloc(&P->sell_cols, (size_t)total + kPad);
     if (e == cudaSuccess) e = dalloc(&P->sell_w, (size_t)P->nout * total + kPad);
     if (e == cudaSuccess)
-        e = sell_fill(P->rowptr, P->cols, P->w32, P->nnz, P->nout, P->n, P->sell_row, P->sell_off, total,
+        e = sell_fill(P->rowptr, P->cols, P->w32, P->nnz, P->nout, P->n, P->maxk, P->sell_row, P->sell_off, total,
                       P->sell_cols, P->sell_w, P->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
     if (e == cudaErrorMemoryAllocation) {

@@ -72,6 +72,51 @@ __global__ void __launch_bounds__(256) sell_fill_kernel(const int64_t* __restric
     }
 }
 
+// the same through shared memory, warp per slice: each stream (columns, then
+// every output's weights) is read row by row with coalesced loads into a
+// [L][33] tile and leaves entry-major with coalesced stores.  tile_l: entries
+// per tile row (>= every slice length).
+__global__ void __launch_bounds__(256) sell_fill_tiled_kernel(const int64_t* __restrict__ rowptr,
+                                                              const int32_t* __restrict__ cols,
+                                                              const float* __restrict__ w, int64_t ws, int nout,
+                                                              int64_t nslices, const int32_t* __restrict__ srow,
+                                                              const int64_t* __restrict__ off, int64_t total,
+                                                              int tile_l, int32_t* __restrict__ scols,
+                                                              float* __restrict__ sw) {
+    extern __shared__ uint32_t tiles[];
+    const int lane = threadIdx.x & 31;
+    uint32_t* tile = tiles + (size_t)(threadIdx.x >> 5) * tile_l * 33;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp0; s < nslices; s += nwarps) {
+        const int32_t myrow = srow[s * kSlice + lane];
+        const int64_t b = off[s];
+        const int L = (int)((off[s + 1] - b) / kSlice);
+        const int myk = myrow >= 0 ? (int)(rowptr[myrow + 1] - rowptr[myrow]) : 0;
+        const uint32_t myself = (uint32_t)(myrow >= 0 ? myrow : 0);
+        for (int st = -1; st < nout; ++st) {  // -1: columns, o >= 0: weights of output o
+            for (int r = 0; r < kSlice; ++r) {
+                const int32_t row = __shfl_sync(0xffffffffu, myrow, r);
+                if (row < 0) continue;
+                const int64_t rb = rowptr[row];
+                const int k = (int)(rowptr[row + 1] - rb);
+                for (int j = lane; j < k; j += 32)
+                    tile[j * 33 + r] = st < 0 ? (uint32_t)cols[rb + j] : __float_as_uint(w[(int64_t)st * ws + rb + j]);
+            }
+            __syncwarp();
+            for (int j = 0; j < L; ++j) {
+                const int64_t idx = b + (int64_t)j * kSlice + lane;
+                const bool ok = j < myk;
+                if (st < 0)
+                    scols[idx] = ok ? (int32_t)tile[j * 33 + lane] : (int32_t)myself;
+                else
+                    sw[(int64_t)st * total + idx] = ok ? __uint_as_float(tile[j * 33 + lane]) : 0.0f;
+            }
+            __syncwarp();
+        }
+    }
+}
+
 // thread per row; block = one window of 8 slices (five blocks per SM fit the
 // registers without spills up to four outputs)
 template <int NO, int U>
@@ -140,10 +185,26 @@ cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t*
 }
 
 cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, int64_t ws, int nout, int64_t n,
-                      const int32_t* srow, const int64_t* off, int64_t total, int32_t* scols, float* sw,
+                      int maxk, const int32_t* srow, const int64_t* off, int64_t total, int32_t* scols, float* sw,
                       cudaStream_t s) {
     const int64_t ns = sell_slices(n);
     if (ns == 0) return cudaSuccess;
+    // shared-memory transpose when 8 tiles of [maxk][33] words fit (two
+    // blocks per SM), else the direct copy
+    const int tile_l = std::max(maxk, 1);
+    const size_t smem = (size_t)8 * tile_l * 33 * sizeof(uint32_t);
+    int dev = 0, smax = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (smem <= (size_t)smax / 2) {
+        cudaError_t e = cudaFuncSetAttribute(sell_fill_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 2);
+        sell_fill_tiled_kernel<<<grid, 256, smem, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, tile_l, scols,
+                                                       sw);
+        return cudaGetLastError();
+    }
     const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 8);
     sell_fill_kernel<<<grid, 256, 0, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, scols, sw);
     return cudaGetLastError();
