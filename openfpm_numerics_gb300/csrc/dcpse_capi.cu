@@ -1574,8 +1574,8 @@ int ensure_sell(dcpse_plan_t* P) {
     if (e == cudaSuccess) e = dalloc(&P->sell_cols, (size_t)total + kPad);
     if (e == cudaSuccess) e = dalloc(&P->sell_w, (size_t)P->nout * total + kPad);
     if (e == cudaSuccess)
-        e = sell_fill(P->rowptr, P->cols, P->w32, P->nnz, P->nout, P->n, P->maxk, P->sell_row, P->sell_off, total,
-                      P->sell_cols, P->sell_w, P->stream);
+        e = sell_fill(P->rowptr, P->cols, P->w32, P->nnz, P->nout, P->n, P->maxk, P->two_set() ? 0 : 1, P->sell_row,
+                      P->sell_off, total, P->sell_cols, P->sell_w, P->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
     if (e == cudaErrorMemoryAllocation) {
         // a second copy of the weights does not fit: the CSR kernels serve
@@ -1945,6 +1945,33 @@ int dcpse_p2p(dcpse_plan_t* P, const double* d_f_support, int ncomp, double* d_o
             ap.lanes = P->apply_lanes;
             ap.comp = (P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) ? 0xffffffffu : 0u;
             ap.no_self = 1;
+            const int mode = P->apply_mode & 15;
+            if ((mode == 0 || mode == 4) && nf > 0) {
+                if (int rc = ensure_sell(P)) return rc;
+                if (P->sell_w) {
+                    SellArgs sa{};
+                    sa.n = P->n;
+                    sa.nslices = sell_slices(P->n);
+                    sa.srow = P->sell_row;
+                    sa.off = P->sell_off;
+                    sa.cols = P->sell_cols;
+                    sa.w = P->sell_w;
+                    sa.total = P->sell_total;
+                    sa.f2 = P->f2;
+                    sa.out = d_out + c;
+                    sa.oos = P->n * ncomp;
+                    sa.ors = ncomp;
+                    sa.w0 = 0;
+                    sa.w1 = (P->n + 255) / 256;
+                    sa.comp = ap.comp;
+                    sa.no_self = 1;
+                    P->tstart(DCPSE_K_APPLY_BATCHED);
+                    cudaError_t e = apply_sell(sa, P->nout, P->stream);
+                    P->tstop(DCPSE_K_APPLY_BATCHED);
+                    DCPSE_CK(e);
+                    continue;
+                }
+            }
             P->tstart(DCPSE_K_APPLY_BATCHED);
             cudaError_t e = apply_batched_f32x(ap, P->stream);
             P->tstop(DCPSE_K_APPLY_BATCHED);

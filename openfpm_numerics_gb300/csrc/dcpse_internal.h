@@ -189,10 +189,10 @@ int64_t sell_slices(int64_t n);
 // scan_tmp [scan_tmp_elems(sell_slices(n))]
 cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t* slen32, int64_t* off,
                        int64_t* scan_tmp, cudaStream_t s);
-// (maxk: the longest row)
+// (maxk: the longest row; one_set: columns index the rows' own set)
 cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, int64_t ws, int nout, int64_t n,
-                      int maxk, const int32_t* srow, const int64_t* off, int64_t total, int32_t* scols, float* sw,
-                      cudaStream_t s);
+                      int maxk, int one_set, const int32_t* srow, const int64_t* off, int64_t total, int32_t* scols,
+                      float* sw, cudaStream_t s);
 cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s);
 
 // Full description of a batched FP32 apply (plan-owned, padded arrays).

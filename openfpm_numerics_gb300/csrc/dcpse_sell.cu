@@ -9,9 +9,10 @@
 // by length (longest first) before they are cut into slices, so a slice pads
 // its rows to nearly their own length; the window keeps the rows of a block
 // spatially close, so the field gathers of its warps share L1 lines.
-// Padding entries point at the row's own particle with weight 0, which adds
-// exactly nothing.  The per-entry arithmetic (exact differences, compensated
-// sums for outputs of order >= 2) is the CSR kernel's (RowAcc).
+// Padding entries carry weight 0 and a column whose value the row reads
+// anyway (the row itself on one set), which adds exactly nothing.  The
+// per-entry arithmetic (exact differences, compensated sums for outputs of
+// order >= 2) is the CSR kernel's (RowAcc).
 #include "dcpse_internal.h"
 #include "dcpse_f32_row.cuh"
 
@@ -46,13 +47,25 @@ __global__ void __launch_bounds__(kWin) sell_order_kernel(const int64_t* __restr
     }
 }
 
+// Column of a padding entry: the row itself on one particle set (its
+// difference is exactly 0), the row's first neighbour on two sets (the row
+// index need not be a support index; the row reads that value anyway), 0
+// for an empty row or a lane past the last row.
+__device__ __forceinline__ int32_t pad_column(int one_set, int32_t row, int64_t k, const int32_t* __restrict__ cols,
+                                              int64_t rb) {
+    if (row < 0) return 0;
+    if (one_set) return row;
+    return k > 0 ? cols[rb] : 0;
+}
+
 // warp per slice: copy the CSR entries of its rows into the slice, entry-major
 __global__ void __launch_bounds__(256) sell_fill_kernel(const int64_t* __restrict__ rowptr,
                                                         const int32_t* __restrict__ cols,
                                                         const float* __restrict__ w, int64_t ws, int nout,
                                                         int64_t nslices, const int32_t* __restrict__ srow,
                                                         const int64_t* __restrict__ off, int64_t total,
-                                                        int32_t* __restrict__ scols, float* __restrict__ sw) {
+                                                        int one_set, int32_t* __restrict__ scols,
+                                                        float* __restrict__ sw) {
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -62,7 +75,7 @@ __global__ void __launch_bounds__(256) sell_fill_kernel(const int64_t* __restric
         const int64_t L = (off[s + 1] - b) / kSlice;
         const int64_t rb = row >= 0 ? rowptr[row] : 0;
         const int64_t k = row >= 0 ? rowptr[row + 1] - rb : 0;
-        const int32_t self = row >= 0 ? row : 0;
+        const int32_t self = pad_column(one_set, row, k, cols, rb);
         for (int64_t j = 0; j < L; ++j) {
             const int64_t idx = b + j * kSlice + lane;
             const bool ok = j < k;
@@ -81,7 +94,7 @@ __global__ void __launch_bounds__(256) sell_fill_tiled_kernel(const int64_t* __r
                                                               const float* __restrict__ w, int64_t ws, int nout,
                                                               int64_t nslices, const int32_t* __restrict__ srow,
                                                               const int64_t* __restrict__ off, int64_t total,
-                                                              int tile_l, int32_t* __restrict__ scols,
+                                                              int tile_l, int one_set, int32_t* __restrict__ scols,
                                                               float* __restrict__ sw) {
     extern __shared__ uint32_t tiles[];
     const int lane = threadIdx.x & 31;
@@ -92,8 +105,9 @@ __global__ void __launch_bounds__(256) sell_fill_tiled_kernel(const int64_t* __r
         const int32_t myrow = srow[s * kSlice + lane];
         const int64_t b = off[s];
         const int L = (int)((off[s + 1] - b) / kSlice);
-        const int myk = myrow >= 0 ? (int)(rowptr[myrow + 1] - rowptr[myrow]) : 0;
-        const uint32_t myself = (uint32_t)(myrow >= 0 ? myrow : 0);
+        const int64_t myrb = myrow >= 0 ? rowptr[myrow] : 0;
+        const int myk = myrow >= 0 ? (int)(rowptr[myrow + 1] - myrb) : 0;
+        const uint32_t myself = (uint32_t)pad_column(one_set, myrow, myk, cols, myrb);
         for (int st = -1; st < nout; ++st) {  // -1: columns, o >= 0: weights of output o
             for (int r = 0; r < kSlice; ++r) {
                 const int32_t row = __shfl_sync(0xffffffffu, myrow, r);
@@ -118,9 +132,9 @@ __global__ void __launch_bounds__(256) sell_fill_tiled_kernel(const int64_t* __r
 }
 
 // thread per row; block = one window of 8 slices (five blocks per SM fit the
-// registers without spills up to four outputs)
+// registers without spills up to four outputs, four up to six, three above)
 template <int NO, int U>
-__global__ void __launch_bounds__(256, (NO <= 4 ? 5 : 4)) apply_sell_kernel(SellArgs a) {
+__global__ void __launch_bounds__(256, (NO <= 4 ? 5 : (NO <= 6 ? 4 : 3))) apply_sell_kernel(SellArgs a) {
     // the window's outputs, staged so that they leave in row order (rows of a
     // slice are permuted; scattered 8-byte stores are slow, above all into
     // host memory over NVLink-C2C)
@@ -132,7 +146,6 @@ __global__ void __launch_bounds__(256, (NO <= 4 ? 5 : 4)) apply_sell_kernel(Sell
         const int32_t row = a.srow[s * kSlice + lane];
         const int64_t b = a.off[s];
         const int L = (int)((a.off[s + 1] - b) / kSlice);
-        const int32_t self = row >= 0 ? row : 0;
         const float2 fp = (row >= 0 && !a.no_self) ? a.f2[row] : make_float2(0.f, 0.f);
         RowAcc<NO, false> acc;
         acc.init();
@@ -145,13 +158,15 @@ __global__ void __launch_bounds__(256, (NO <= 4 ? 5 : 4)) apply_sell_kernel(Sell
             for (int u = 0; u < U; ++u) {
                 const int j = j0 + u;
                 const bool ok = j < L;
-                q[u] = ok ? c[(int64_t)j * kSlice] : self;
+                q[u] = ok ? c[(int64_t)j * kSlice] : 0;
 #pragma unroll
                 for (int o = 0; o < NO; ++o) wv[u][o] = ok ? w[(int64_t)o * a.total + (int64_t)j * kSlice] : 0.0f;
             }
+            // entries past the slice end take the row's own value (a zero
+            // difference; zero for interpolation) with weight 0: no gather
             float2 fq[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) fq[u] = a.f2[q[u]];
+            for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? a.f2[q[u]] : fp;
 #pragma unroll
             for (int u = 0; u < U; ++u) acc.add(wv[u], r0, fq[u], fp, a.comp);
         }
@@ -185,8 +200,8 @@ cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t*
 }
 
 cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, int64_t ws, int nout, int64_t n,
-                      int maxk, const int32_t* srow, const int64_t* off, int64_t total, int32_t* scols, float* sw,
-                      cudaStream_t s) {
+                      int maxk, int one_set, const int32_t* srow, const int64_t* off, int64_t total, int32_t* scols,
+                      float* sw, cudaStream_t s) {
     const int64_t ns = sell_slices(n);
     if (ns == 0) return cudaSuccess;
     // shared-memory transpose when 8 tiles of [maxk][33] words fit (two
@@ -201,12 +216,12 @@ cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w
                                              (int)smem);
         if (e != cudaSuccess) return e;
         const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 2);
-        sell_fill_tiled_kernel<<<grid, 256, smem, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, tile_l, scols,
-                                                       sw);
+        sell_fill_tiled_kernel<<<grid, 256, smem, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, tile_l,
+                                                       one_set, scols, sw);
         return cudaGetLastError();
     }
     const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 8);
-    sell_fill_kernel<<<grid, 256, 0, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, scols, sw);
+    sell_fill_kernel<<<grid, 256, 0, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, one_set, scols, sw);
     return cudaGetLastError();
 }
 
@@ -215,10 +230,11 @@ cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s) {
     // one block per window: the block scheduler balances the windows
     const int64_t grid = a.w1 - a.w0;
     if (grid > 0x7fffffff) return cudaErrorInvalidValue;
-    constexpr int U = 4;
+    // entries in flight per thread: 8 for one output (a row per thread walks
+    // its whole row; one weight stream leaves the registers), 4 above
     switch (nout) {
 #define DCPSE_SELL_CASE(NO) \
-    case NO: apply_sell_kernel<NO, U><<<(unsigned)grid, 256, 0, s>>>(a); break;
+    case NO: apply_sell_kernel<NO, (NO == 1 ? 8 : 4)><<<(unsigned)grid, 256, 0, s>>>(a); break;
         DCPSE_SELL_CASE(1)
         DCPSE_SELL_CASE(2)
         DCPSE_SELL_CASE(3)
