@@ -545,10 +545,9 @@ def run_interp(args):
     res["p2p_f64_batched_ms"] = timed(lambda: plan.p2p(f, C.F64, outb))
     b64 = outb[0].clone()
     sweep = []
-    for lanes in (4, 8, 16):
-        for mode in (1, 3):
-            plan.set_apply_config(lanes, mode)
-            sweep.append({"lanes": lanes, "mode": mode, "ms": timed(lambda: plan.p2p(f, C.F32, outb))})
+    for lanes, mode in [(ln, md) for ln in (4, 8, 16) for md in (1, 3)] + [(0, 4)]:
+        plan.set_apply_config(lanes, mode)
+        sweep.append({"lanes": lanes, "mode": mode, "ms": timed(lambda: plan.p2p(f, C.F32, outb))})
     best = min(sweep, key=lambda r: r["ms"])
     res["p2p_f32_sweep"] = sweep
     plan.set_apply_config(0, 0)
