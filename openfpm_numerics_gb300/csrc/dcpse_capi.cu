@@ -1430,13 +1430,27 @@ int dcpse_rk4_gs_stage(dcpse_plan_t* P, int stage, int precision, const void* Yu
         if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
         RkArgs<float> a{P->n, P->rowptr, P->cols, P->w32, (const float*)Yu, (const float*)Yv, (const float*)y0u,
                         (const float*)y0v, (float*)accu, (float*)accv, (float*)outu, (float*)outv,
-                        params[0], params[1], params[2], params[3], params[4], stage, P->rk_pack};
+                        params[0], params[1], params[2], params[3], params[4], stage, P->rk_pack,
+                        nullptr, nullptr, nullptr, nullptr};
+        // the sliced ELL layout of the Laplacian's weights (output 0), unless
+        // a CSR schedule was asked for
+        const int mode = P->apply_mode & 15;
+        if (mode == 0 || mode == 4) {
+            if (int rc = ensure_sell(P)) return rc;
+            if (P->sell_w) {
+                a.srow = P->sell_row;
+                a.soff = P->sell_off;
+                a.scols = P->sell_cols;
+                a.sw = P->sell_w;
+            }
+        }
         DCPSE_CK(rk_stage<float>(a, lanes, P->stream));
     } else if (precision == DCPSE_F64) {
         if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
         RkArgs<double> a{P->n, P->rowptr, P->cols, P->w64, (const double*)Yu, (const double*)Yv, (const double*)y0u,
                          (const double*)y0v, (double*)accu, (double*)accv, (double*)outu, (double*)outv,
-                         params[0], params[1], params[2], params[3], params[4], stage, P->rk_pack};
+                         params[0], params[1], params[2], params[3], params[4], stage, P->rk_pack,
+                         nullptr, nullptr, nullptr, nullptr};
         DCPSE_CK(rk_stage<double>(a, lanes, P->stream));
     } else {
         return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");

@@ -307,6 +307,11 @@ struct RkArgs {
     double Du, Dv, F, K, dt;
     int stage;                      // 0..3
     void* pack;                     // scratch [n] of (u, v) pairs (float2 / double2) for the gathers
+    // the weights on the sliced ELL layout (FP32 state; null: CSR kernel)
+    const int32_t* srow;
+    const int64_t* soff;
+    const int32_t* scols;
+    const float* sw;
 };
 template <typename T>
 struct RkAdjArgs {

@@ -19,6 +19,8 @@
 //   Ybar3 = J3^T kbar3; kbar2 = dt/3 ybar + dt/2 Ybar3; Ybar2 = J2^T kbar2;
 //   kbar1 = dt/6 ybar + dt/2 Ybar2; Ybar1 = J1^T kbar1;
 //   ybar_n = ybar + Ybar1 + Ybar2 + Ybar3 + Ybar4.
+#include <type_traits>
+
 #include "dcpse_internal.h"
 
 namespace dcpse {
@@ -56,6 +58,41 @@ __global__ void pack_kernel(const T* __restrict__ u, const T* __restrict__ v, in
         p.x = u[i];
         p.y = v[i];
         out[i] = p;
+    }
+}
+
+// reaction terms and the RK4 stage combination of one row, given its
+// Laplacian sums lu, lv and its stage input (up, vp)
+template <typename T>
+__device__ __forceinline__ void stage_update(const RkArgs<T>& a, int64_t row, T up, T vp, T lu, T lv) {
+    const T uvv = up * vp * vp;
+    const T ku = (T)a.Du * lu - uvv + (T)a.F * ((T)1 - up);
+    const T kv = (T)a.Dv * lv + uvv - ((T)a.F + (T)a.K) * vp;
+    const T dt = (T)a.dt;
+    const T y0u = a.y0u[row], y0v = a.y0v[row];
+    switch (a.stage) {
+        case 0:
+            a.accu[row] = ku;
+            a.accv[row] = kv;
+            a.outu[row] = y0u + (dt / (T)2) * ku;
+            a.outv[row] = y0v + (dt / (T)2) * kv;
+            break;
+        case 1:
+            a.accu[row] += (T)2 * ku;
+            a.accv[row] += (T)2 * kv;
+            a.outu[row] = y0u + (dt / (T)2) * ku;
+            a.outv[row] = y0v + (dt / (T)2) * kv;
+            break;
+        case 2:
+            a.accu[row] += (T)2 * ku;
+            a.accv[row] += (T)2 * kv;
+            a.outu[row] = y0u + dt * ku;
+            a.outv[row] = y0v + dt * kv;
+            break;
+        default:
+            a.outu[row] = y0u + (dt / (T)6) * (a.accu[row] + ku);
+            a.outv[row] = y0v + (dt / (T)6) * (a.accv[row] + kv);
+            break;
     }
 }
 
@@ -107,37 +144,47 @@ __global__ void __launch_bounds__(256) gs_stage_kernel(RkArgs<T> a) {
             lu += __shfl_xor_sync(0xffffffffu, lu, m);
             lv += __shfl_xor_sync(0xffffffffu, lv, m);
         }
-        if (row < a.n && sub == 0) {
-            const T uvv = up * vp * vp;
-            const T ku = (T)a.Du * lu - uvv + (T)a.F * ((T)1 - up);
-            const T kv = (T)a.Dv * lv + uvv - ((T)a.F + (T)a.K) * vp;
-            const T dt = (T)a.dt;
-            const T y0u = a.y0u[row], y0v = a.y0v[row];
-            switch (a.stage) {
-                case 0:
-                    a.accu[row] = ku;
-                    a.accv[row] = kv;
-                    a.outu[row] = y0u + (dt / (T)2) * ku;
-                    a.outv[row] = y0v + (dt / (T)2) * kv;
-                    break;
-                case 1:
-                    a.accu[row] += (T)2 * ku;
-                    a.accv[row] += (T)2 * kv;
-                    a.outu[row] = y0u + (dt / (T)2) * ku;
-                    a.outv[row] = y0v + (dt / (T)2) * kv;
-                    break;
-                case 2:
-                    a.accu[row] += (T)2 * ku;
-                    a.accv[row] += (T)2 * kv;
-                    a.outu[row] = y0u + dt * ku;
-                    a.outv[row] = y0v + dt * kv;
-                    break;
-                default:
-                    a.outu[row] = y0u + (dt / (T)6) * (a.accu[row] + ku);
-                    a.outv[row] = y0v + (dt / (T)6) * (a.accv[row] + kv);
-                    break;
+        if (row < a.n && sub == 0) stage_update(a, row, up, vp, lu, lv);
+    }
+}
+
+// FP32 stage on the sliced ELL layout of the weights (slices of 32 rows
+// stored entry-major, rows sorted by length within windows of 256): a row per
+// thread, 8 gathers of (u, v) pairs in flight; entries past the slice end
+// take the row's own pair with weight 0 (an exact zero)
+__global__ void __launch_bounds__(256) gs_stage_sell_kernel(RkArgs<float> a, int64_t nwin) {
+    const float2* __restrict__ Y2 = static_cast<const float2*>(a.pack);
+    const int lane = threadIdx.x & 31;
+    constexpr int U = 8;
+    for (int64_t win = blockIdx.x; win < nwin; win += gridDim.x) {
+        const int64_t s = win * 8 + (threadIdx.x >> 5);
+        const int32_t row = a.srow[s * 32 + lane];
+        if (row < 0) continue;
+        const int64_t b = a.soff[s];
+        const int L = (int)((a.soff[s + 1] - b) / 32);
+        const float2 yp = Y2[row];
+        const int32_t* __restrict__ c = a.scols + b + lane;
+        const float* __restrict__ w = a.sw + b + lane;
+        float lu = 0.f, lv = 0.f;
+        for (int j0 = 0; j0 < L; j0 += U) {
+            int32_t q[U];
+            float wq[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = j0 + u;
+                q[u] = j < L ? c[(int64_t)j * 32] : 0;
+                wq[u] = j < L ? w[(int64_t)j * 32] : 0.f;
+            }
+            float2 y[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) y[u] = j0 + u < L ? Y2[q[u]] : yp;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                lu = fmaf(wq[u], y[u].x - yp.x, lu);
+                lv = fmaf(wq[u], y[u].y - yp.y, lv);
             }
         }
+        stage_update(a, row, yp.x, yp.y, lu, lv);
     }
 }
 
@@ -231,6 +278,13 @@ template <typename T>
 cudaError_t rk_stage(const RkArgs<T>& a, int lanes, cudaStream_t s) {
     if (a.n == 0) return cudaSuccess;
     pack_kernel<T><<<grid_n(a.n, 256), 256, 0, s>>>(a.Yu, a.Yv, a.n, static_cast<typename Pair<T>::type*>(a.pack));
+    if constexpr (std::is_same<T, float>::value) {
+        if (a.srow) {
+            const int64_t nwin = (a.n + 255) / 256;
+            gs_stage_sell_kernel<<<(unsigned)nwin, 256, 0, s>>>(a, nwin);
+            return cudaGetLastError();
+        }
+    }
     switch (lanes) {
         case 4: gs_stage_kernel<T, 4><<<grid_n(a.n, 64), 256, 0, s>>>(a); break;
         case 8: gs_stage_kernel<T, 8><<<grid_n(a.n, 32), 256, 0, s>>>(a); break;
