@@ -319,6 +319,7 @@ struct dcpse_plan_s {
     int64_t* sell_off = nullptr;
     int32_t* sell_cols = nullptr;
     float* sell_w = nullptr;
+    void* sell_r = nullptr;  // bf16 residuals on the same layout (with r16)
     int64_t sell_total = 0;
     bool sell_no_room = false;  // the copy did not fit in device memory: CSR kernels only
     void free_sell() {
@@ -326,6 +327,8 @@ struct dcpse_plan_s {
         dfree(sell_off);
         dfree(sell_cols);
         dfree(sell_w);
+        if (sell_r) cudaFree(sell_r);
+        sell_r = nullptr;
         sell_total = 0;
         sell_no_room = false;
     }
@@ -1588,8 +1591,8 @@ int ensure_sell(dcpse_plan_t* P) {
     if (e == cudaSuccess) e = dalloc(&P->sell_cols, (size_t)total + kPad);
     if (e == cudaSuccess) e = dalloc(&P->sell_w, (size_t)P->nout * total + kPad);
     if (e == cudaSuccess)
-        e = sell_fill(P->rowptr, P->cols, P->w32, P->nnz, P->nout, P->n, P->maxk, P->two_set() ? 0 : 1, P->sell_row,
-                      P->sell_off, total, P->sell_cols, P->sell_w, P->stream);
+        e = sell_fill(P->rowptr, P->cols, P->w32, nullptr, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
+                      P->sell_row, P->sell_off, total, P->sell_cols, P->sell_w, nullptr, P->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
     if (e == cudaErrorMemoryAllocation) {
         // a second copy of the weights does not fit: the CSR kernels serve
@@ -1603,6 +1606,27 @@ int ensure_sell(dcpse_plan_t* P) {
         return fail(DCPSE_ERR_CUDA, std::string("sliced ELL weights: ") + cudaGetErrorString(e));
     }
     P->sell_total = total;
+    return DCPSE_OK;
+}
+
+// The bf16 residual streams on the sliced layout, built on the first apply
+// that asks for them (the weights' layout must exist).
+int ensure_sell_resid(dcpse_plan_t* P) {
+    if (P->sell_r || !P->sell_w || !P->r16) return DCPSE_OK;
+    cudaError_t e = cudaMalloc(&P->sell_r, ((size_t)P->nout * P->sell_total + kPad) * 2);
+    if (e == cudaSuccess)
+        e = sell_fill(P->rowptr, P->cols, nullptr, P->r16, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
+                      P->sell_row, P->sell_off, P->sell_total, P->sell_cols, nullptr, P->sell_r, P->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+    if (e != cudaSuccess) {
+        if (P->sell_r) cudaFree(P->sell_r);
+        P->sell_r = nullptr;
+        if (e == cudaErrorMemoryAllocation || e == cudaErrorInvalidValue) {
+            cudaGetLastError();
+            return DCPSE_OK;  // the CSR kernels serve this precision
+        }
+        return fail(DCPSE_ERR_CUDA, std::string("sliced ELL residuals: ") + cudaGetErrorString(e));
+    }
     return DCPSE_OK;
 }
 
@@ -1642,10 +1666,13 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
     // (the automatic schedule: 15 % faster than the CSR kernels at 128^3)
     const int64_t rr0 = r0, rr1 = r1 ? r1 : P->n;
     const int mode = P->apply_mode & 15;
-    if ((mode == 0 || mode == 4) && precision == DCPSE_F32 && rr0 % 256 == 0 && (rr1 % 256 == 0 || rr1 == P->n)) {
+    const bool resid = precision == DCPSE_F32_RESID;
+    if ((mode == 0 || mode == 4) && rr0 % 256 == 0 && (rr1 % 256 == 0 || rr1 == P->n)) {
         if (int rc = ensure_sell(P)) return rc;
+        if (resid)
+            if (int rc = ensure_sell_resid(P)) return rc;
     }
-    if ((mode == 0 || mode == 4) && precision == DCPSE_F32 && P->sell_w && rr0 % 256 == 0 &&
+    if ((mode == 0 || mode == 4) && P->sell_w && (!resid || P->sell_r) && rr0 % 256 == 0 &&
         (rr1 % 256 == 0 || rr1 == P->n)) {
         SellArgs sa{};
         sa.n = P->n;
@@ -1654,6 +1681,7 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
         sa.off = P->sell_off;
         sa.cols = P->sell_cols;
         sa.w = P->sell_w;
+        sa.r = resid ? static_cast<const __nv_bfloat16*>(P->sell_r) : nullptr;
         sa.total = P->sell_total;
         sa.f2 = P->f2;
         sa.out = d_out;

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "dcpse_common.cuh"
@@ -176,6 +177,7 @@ struct SellArgs {
     const int64_t* off;    // [nslices + 1] first entry of each slice
     const int32_t* cols;   // [total] entry-major within a slice
     const float* w;        // [NO][total]
+    const __nv_bfloat16* r; // [NO][total] bf16 residuals of the weights, or null
     int64_t total;
     const float2* f2;
     double* out;           // output o of row r at out[o * oos + r * ors]
@@ -189,10 +191,12 @@ int64_t sell_slices(int64_t n);
 // scan_tmp [scan_tmp_elems(sell_slices(n))]
 cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t* slen32, int64_t* off,
                        int64_t* scan_tmp, cudaStream_t s);
-// (maxk: the longest row; one_set: columns index the rows' own set)
-cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, int64_t ws, int nout, int64_t n,
-                      int maxk, int one_set, const int32_t* srow, const int64_t* off, int64_t total, int32_t* scols,
-                      float* sw, cudaStream_t s);
+// Copies the CSR columns and weights (w / sw given) and the bf16 residual
+// streams (r16 / sr16 given) into the sliced layout; one_set: the columns
+// index the rows' own set.
+cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, const void* r16, int64_t ws,
+                      int nout, int64_t n, int one_set, const int32_t* srow, const int64_t* off, int64_t total,
+                      int32_t* scols, float* sw, void* sr16, cudaStream_t s);
 cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s);
 
 // Full description of a batched FP32 apply (plan-owned, padded arrays).

@@ -13,6 +13,8 @@
 // anyway (the row itself on one set), which adds exactly nothing.  The
 // per-entry arithmetic (exact differences, compensated sums for outputs of
 // order >= 2) is the CSR kernel's (RowAcc).
+#include <cuda_bf16.h>
+
 #include "dcpse_internal.h"
 #include "dcpse_f32_row.cuh"
 
@@ -58,47 +60,22 @@ __device__ __forceinline__ int32_t pad_column(int one_set, int32_t row, int64_t 
     return k > 0 ? cols[rb] : 0;
 }
 
-// warp per slice: copy the CSR entries of its rows into the slice, entry-major
+// warp per slice: copy the CSR entries of its 32 rows into the slice,
+// entry-major, 32 entries at a time through a [32][33] shared-memory block
+// per warp: each row's 32 entries are read with one coalesced load, each
+// entry of the 32 rows is written with one coalesced store.  Streams: -1 the
+// columns, [0, nout) the weights, [nout, 2 nout) the bf16 residuals.
 __global__ void __launch_bounds__(256) sell_fill_kernel(const int64_t* __restrict__ rowptr,
                                                         const int32_t* __restrict__ cols,
                                                         const float* __restrict__ w, int64_t ws, int nout,
                                                         int64_t nslices, const int32_t* __restrict__ srow,
-                                                        const int64_t* __restrict__ off, int64_t total,
-                                                        int one_set, int32_t* __restrict__ scols,
-                                                        float* __restrict__ sw) {
+                                                        const int64_t* __restrict__ off, int64_t total, int one_set,
+                                                        int32_t* __restrict__ scols, float* __restrict__ sw,
+                                                        const uint16_t* __restrict__ r16, uint16_t* __restrict__ sr16,
+                                                        int st_begin, int st_end) {
+    __shared__ uint32_t tiles[8][32 * 33];
     const int lane = threadIdx.x & 31;
-    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t s = warp0; s < nslices; s += nwarps) {
-        const int32_t row = srow[s * kSlice + lane];
-        const int64_t b = off[s];
-        const int64_t L = (off[s + 1] - b) / kSlice;
-        const int64_t rb = row >= 0 ? rowptr[row] : 0;
-        const int64_t k = row >= 0 ? rowptr[row + 1] - rb : 0;
-        const int32_t self = pad_column(one_set, row, k, cols, rb);
-        for (int64_t j = 0; j < L; ++j) {
-            const int64_t idx = b + j * kSlice + lane;
-            const bool ok = j < k;
-            scols[idx] = ok ? cols[rb + j] : self;
-            for (int o = 0; o < nout; ++o) sw[(int64_t)o * total + idx] = ok ? w[(int64_t)o * ws + rb + j] : 0.0f;
-        }
-    }
-}
-
-// the same through shared memory, warp per slice: each stream (columns, then
-// every output's weights) is read row by row with coalesced loads into a
-// [L][33] tile and leaves entry-major with coalesced stores.  tile_l: entries
-// per tile row (>= every slice length).
-__global__ void __launch_bounds__(256) sell_fill_tiled_kernel(const int64_t* __restrict__ rowptr,
-                                                              const int32_t* __restrict__ cols,
-                                                              const float* __restrict__ w, int64_t ws, int nout,
-                                                              int64_t nslices, const int32_t* __restrict__ srow,
-                                                              const int64_t* __restrict__ off, int64_t total,
-                                                              int tile_l, int one_set, int32_t* __restrict__ scols,
-                                                              float* __restrict__ sw) {
-    extern __shared__ uint32_t tiles[];
-    const int lane = threadIdx.x & 31;
-    uint32_t* tile = tiles + (size_t)(threadIdx.x >> 5) * tile_l * 33;
+    uint32_t* tile = tiles[threadIdx.x >> 5];
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t s = warp0; s < nslices; s += nwarps) {
@@ -107,60 +84,71 @@ __global__ void __launch_bounds__(256) sell_fill_tiled_kernel(const int64_t* __r
         const int L = (int)((off[s + 1] - b) / kSlice);
         const int64_t myrb = myrow >= 0 ? rowptr[myrow] : 0;
         const int myk = myrow >= 0 ? (int)(rowptr[myrow + 1] - myrb) : 0;
-        const uint32_t myself = (uint32_t)pad_column(one_set, myrow, myk, cols, myrb);
-        for (int st = -1; st < nout; ++st) {  // -1: columns, o >= 0: weights of output o
-            for (int r = 0; r < kSlice; ++r) {
-                const int32_t row = __shfl_sync(0xffffffffu, myrow, r);
-                if (row < 0) continue;
-                const int64_t rb = rowptr[row];
-                const int k = (int)(rowptr[row + 1] - rb);
-                for (int j = lane; j < k; j += 32)
-                    tile[j * 33 + r] = st < 0 ? (uint32_t)cols[rb + j] : __float_as_uint(w[(int64_t)st * ws + rb + j]);
+        const uint32_t mypad = (uint32_t)pad_column(one_set, myrow, myk, cols, myrb);
+        for (int st = st_begin; st < st_end; ++st) {
+            for (int j0 = 0; j0 < L; j0 += 32) {
+                for (int r = 0; r < kSlice; ++r) {
+                    const int64_t rb = __shfl_sync(0xffffffffu, myrb, r);
+                    const int k = __shfl_sync(0xffffffffu, myk, r);
+                    const int j = j0 + lane;
+                    if (j < k)
+                        tile[lane * 33 + r] = st < 0      ? (uint32_t)cols[rb + j]
+                                              : st < nout ? __float_as_uint(w[(int64_t)st * ws + rb + j])
+                                                          : (uint32_t)r16[(int64_t)(st - nout) * ws + rb + j];
+                }
+                __syncwarp();
+                const int jn = min(32, L - j0);
+                for (int jj = 0; jj < jn; ++jj) {
+                    const int j = j0 + jj;
+                    const int64_t idx = b + (int64_t)j * kSlice + lane;
+                    const bool ok = j < myk;
+                    const uint32_t v = tile[jj * 33 + lane];
+                    if (st < 0)
+                        scols[idx] = ok ? (int32_t)v : (int32_t)mypad;
+                    else if (st < nout)
+                        sw[(int64_t)st * total + idx] = ok ? __uint_as_float(v) : 0.0f;
+                    else
+                        sr16[(int64_t)(st - nout) * total + idx] = ok ? (uint16_t)v : (uint16_t)0;
+                }
+                __syncwarp();
             }
-            __syncwarp();
-            for (int j = 0; j < L; ++j) {
-                const int64_t idx = b + (int64_t)j * kSlice + lane;
-                const bool ok = j < myk;
-                if (st < 0)
-                    scols[idx] = ok ? (int32_t)tile[j * 33 + lane] : (int32_t)myself;
-                else
-                    sw[(int64_t)st * total + idx] = ok ? __uint_as_float(tile[j * 33 + lane]) : 0.0f;
-            }
-            __syncwarp();
         }
     }
 }
 
 // thread per row; block = one window of 8 slices (five blocks per SM fit the
 // registers without spills up to four outputs, four up to six, three above)
-template <int NO, int U>
-__global__ void __launch_bounds__(256, (NO <= 4 ? 5 : (NO <= 6 ? 4 : 3))) apply_sell_kernel(SellArgs a) {
+template <int NO, int U, bool RESID>
+__global__ void __launch_bounds__(256, (NO <= 4 && !RESID ? 5 : (NO <= 6 ? 4 : 3))) apply_sell_kernel(SellArgs a) {
     // the window's outputs, staged so that they leave in row order (rows of a
     // slice are permuted; scattered 8-byte stores are slow, above all into
     // host memory over NVLink-C2C)
     __shared__ double tile[NO][kWin];
     const int lane = threadIdx.x & 31;
-    const float r0[NO] = {};
     for (int64_t win = a.w0 + blockIdx.x; win < a.w1; win += gridDim.x) {
         const int64_t s = win * kSlicesPerWin + (threadIdx.x >> 5);  // < nslices: windows hold 8 slices
         const int32_t row = a.srow[s * kSlice + lane];
         const int64_t b = a.off[s];
         const int L = (int)((a.off[s + 1] - b) / kSlice);
         const float2 fp = (row >= 0 && !a.no_self) ? a.f2[row] : make_float2(0.f, 0.f);
-        RowAcc<NO, false> acc;
+        RowAcc<NO, RESID> acc;
         acc.init();
         const int32_t* __restrict__ c = a.cols + b + lane;
         const float* __restrict__ w = a.w + b + lane;
+        const __nv_bfloat16* __restrict__ rr = RESID ? a.r + b + lane : nullptr;
         for (int j0 = 0; j0 < L; j0 += U) {
             int32_t q[U];
-            float wv[U][NO];
+            float wv[U][NO], rv[U][NO];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int j = j0 + u;
                 const bool ok = j < L;
                 q[u] = ok ? c[(int64_t)j * kSlice] : 0;
 #pragma unroll
-                for (int o = 0; o < NO; ++o) wv[u][o] = ok ? w[(int64_t)o * a.total + (int64_t)j * kSlice] : 0.0f;
+                for (int o = 0; o < NO; ++o) {
+                    wv[u][o] = ok ? w[(int64_t)o * a.total + (int64_t)j * kSlice] : 0.0f;
+                    rv[u][o] = (RESID && ok) ? __bfloat162float(rr[(int64_t)o * a.total + (int64_t)j * kSlice]) : 0.0f;
+                }
             }
             // entries past the slice end take the row's own value (a zero
             // difference; zero for interpolation) with weight 0: no gather
@@ -168,7 +156,7 @@ __global__ void __launch_bounds__(256, (NO <= 4 ? 5 : (NO <= 6 ? 4 : 3))) apply_
 #pragma unroll
             for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? a.f2[q[u]] : fp;
 #pragma unroll
-            for (int u = 0; u < U; ++u) acc.add(wv[u], r0, fq[u], fp, a.comp);
+            for (int u = 0; u < U; ++u) acc.add(wv[u], rv[u], fq[u], fp, a.comp);
         }
         if (row >= 0) {
 #pragma unroll
@@ -199,29 +187,17 @@ cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t*
     return exclusive_scan_i32(slen32, nwin * kSlicesPerWin, off, scan_tmp, s);
 }
 
-cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, int64_t ws, int nout, int64_t n,
-                      int maxk, int one_set, const int32_t* srow, const int64_t* off, int64_t total, int32_t* scols,
-                      float* sw, cudaStream_t s) {
+cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, const void* r16, int64_t ws,
+                      int nout, int64_t n, int one_set, const int32_t* srow, const int64_t* off, int64_t total,
+                      int32_t* scols, float* sw, void* sr16, cudaStream_t s) {
     const int64_t ns = sell_slices(n);
     if (ns == 0) return cudaSuccess;
-    // shared-memory transpose when 8 tiles of [maxk][33] words fit (two
-    // blocks per SM), else the direct copy
-    const int tile_l = std::max(maxk, 1);
-    const size_t smem = (size_t)8 * tile_l * 33 * sizeof(uint32_t);
-    int dev = 0, smax = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (smem <= (size_t)smax / 2) {
-        cudaError_t e = cudaFuncSetAttribute(sell_fill_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 2);
-        sell_fill_tiled_kernel<<<grid, 256, smem, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, tile_l,
-                                                       one_set, scols, sw);
-        return cudaGetLastError();
-    }
-    const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 8);
-    sell_fill_kernel<<<grid, 256, 0, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, one_set, scols, sw);
+    // columns and weights when sw is given, the residual streams when sr16 is
+    const int st_begin = sw ? -1 : nout, st_end = sr16 ? 2 * nout : nout;
+    const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 6);
+    sell_fill_kernel<<<grid, 256, 0, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, one_set, scols, sw,
+                                          static_cast<const uint16_t*>(r16), static_cast<uint16_t*>(sr16), st_begin,
+                                          st_end);
     return cudaGetLastError();
 }
 
@@ -231,10 +207,17 @@ cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s) {
     const int64_t grid = a.w1 - a.w0;
     if (grid > 0x7fffffff) return cudaErrorInvalidValue;
     // entries in flight per thread: 8 for one output (a row per thread walks
-    // its whole row; one weight stream leaves the registers), 4 above
+    // its whole row; one weight stream leaves the registers), 4 above, 2 with
+    // the residual streams beyond two outputs (no register spills)
     switch (nout) {
-#define DCPSE_SELL_CASE(NO) \
-    case NO: apply_sell_kernel<NO, (NO == 1 ? 8 : 4)><<<(unsigned)grid, 256, 0, s>>>(a); break;
+#define DCPSE_SELL_CASE(NO)                                                                      \
+    case NO:                                                                                     \
+        if (a.r)                                                                                 \
+            apply_sell_kernel<NO, (NO == 1 ? 8 : (NO <= 2 ? 4 : 2)), true>                      \
+                <<<(unsigned)grid, 256, 0, s>>>(a);                                              \
+        else                                                                                     \
+            apply_sell_kernel<NO, (NO == 1 ? 8 : 4), false><<<(unsigned)grid, 256, 0, s>>>(a);   \
+        break;
         DCPSE_SELL_CASE(1)
         DCPSE_SELL_CASE(2)
         DCPSE_SELL_CASE(3)
