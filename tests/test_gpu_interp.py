@@ -136,3 +136,32 @@ def test_ppinterpolation_reference_scenarios(cuda, orc):
     f32 = Fx2(sup.props[0], precision="f32")
     assert (f32 - dom.props[1]).abs().max().item() <= 1e-6 * 2
     Fx2.deallocate()
+
+
+def test_p2p_support_smaller_than_domain(cuda, orc):
+    """Interpolation from a coarse support set onto a finer domain set (more
+    rows than support particles): the FP32 p2p on the sliced layout pads rows
+    with support indices (never a row index), equals the reference-order p2p
+    within 1e-6 and reproduces linear fields."""
+    dom, h = W.lattice(40, 2)
+    sup, hs = W.lattice(18, 2, jitter=0.1, seed=77)
+    rcut = 3.1 * hs
+    plan = DcpsePlan(2, [[(0, 0)]], order=2)
+    plan.set_support(torch.tensor(sup, device="cuda"))
+    dt = torch.tensor(dom, device="cuda")
+    plan.build_neighbors(dt, rcut)
+    plan.assemble(dt, C.STORE_TERMS_F64 | C.STORE_OUT_F32)
+    assert dom.shape[0] > sup.shape[0]
+    f = np.sin(2 * sup[:, 0]) + sup[:, 1] ** 2
+    ft = torch.tensor(f, device="cuda")
+    ref = plan.p2p_f64(0, ft).cpu().numpy()
+    got = plan.p2p(ft, C.F32)[0].cpu().numpy()
+    st = plan.eps()[1].cpu().numpy()
+    ok = st == 0
+    assert ok.sum() > 0.9 * dom.shape[0]
+    assert np.abs(got - ref)[ok].max() <= 1e-6 * np.abs(f).max()
+    lin = 0.5 + sup[:, 0] - 2 * sup[:, 1]
+    gl = plan.p2p(torch.tensor(lin, device="cuda"), C.F32)[0].cpu().numpy()
+    assert np.abs(gl - (0.5 + dom[:, 0] - 2 * dom[:, 1]))[ok].max() < 1e-5
+    plan.check()
+    plan.close()
