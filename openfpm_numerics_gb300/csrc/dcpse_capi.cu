@@ -320,6 +320,7 @@ struct dcpse_plan_s {
     int32_t* sell_cols = nullptr;
     float* sell_w = nullptr;
     void* sell_r = nullptr;  // bf16 residuals on the same layout (with r16)
+    double* sell_w64 = nullptr;  // FP64 summed weights on the same layout (with w64)
     int64_t sell_total = 0;
     bool sell_no_room = false;  // the copy did not fit in device memory: CSR kernels only
     void free_sell() {
@@ -327,6 +328,7 @@ struct dcpse_plan_s {
         dfree(sell_off);
         dfree(sell_cols);
         dfree(sell_w);
+        dfree(sell_w64);
         if (sell_r) cudaFree(sell_r);
         sell_r = nullptr;
         sell_total = 0;
@@ -1093,6 +1095,7 @@ int dcpse_neighbors_ptr(dcpse_plan_t* P, const int64_t** d_rowptr, const int32_t
 
 namespace {
 int ensure_sell(dcpse_plan_t* P);
+int ensure_sell64(dcpse_plan_t* P);
 }  // namespace
 
 int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fixed, int flags) {
@@ -1573,8 +1576,10 @@ int dcpse_apply_output_f64(dcpse_plan_t* P, int output, const double* d_f, doubl
 namespace {
 // The FP32 output weights on the sliced ELL layout, built from the CSR
 // weights on first use after each assembly.
-int ensure_sell(dcpse_plan_t* P) {
-    if (P->sell_w || P->n == 0 || P->sell_no_room) return DCPSE_OK;
+// The sliced layout of the current list (row order, slice offsets, columns),
+// built on first use after each assembly.
+int ensure_sell_layout(dcpse_plan_t* P) {
+    if (P->sell_cols || P->n == 0 || P->sell_no_room) return DCPSE_OK;
     const int64_t ns = sell_slices(P->n);
     int32_t* slen = nullptr;
     int64_t* tmp = nullptr;
@@ -1589,13 +1594,12 @@ int ensure_sell(dcpse_plan_t* P) {
     dfree(slen);
     dfree(tmp);
     if (e == cudaSuccess) e = dalloc(&P->sell_cols, (size_t)total + kPad);
-    if (e == cudaSuccess) e = dalloc(&P->sell_w, (size_t)P->nout * total + kPad);
     if (e == cudaSuccess)
-        e = sell_fill(P->rowptr, P->cols, P->w32, nullptr, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
-                      P->sell_row, P->sell_off, total, P->sell_cols, P->sell_w, nullptr, P->stream);
+        e = sell_fill(P->rowptr, P->cols, nullptr, nullptr, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
+                      P->sell_row, P->sell_off, total, P->sell_cols, nullptr, nullptr, P->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
     if (e == cudaErrorMemoryAllocation) {
-        // a second copy of the weights does not fit: the CSR kernels serve
+        // the layout does not fit: the CSR kernels serve
         P->free_sell();
         cudaGetLastError();
         P->sell_no_room = true;
@@ -1603,31 +1607,73 @@ int ensure_sell(dcpse_plan_t* P) {
     }
     if (e != cudaSuccess) {
         P->free_sell();
-        return fail(DCPSE_ERR_CUDA, std::string("sliced ELL weights: ") + cudaGetErrorString(e));
+        return fail(DCPSE_ERR_CUDA, std::string("sliced ELL layout: ") + cudaGetErrorString(e));
     }
     P->sell_total = total;
     return DCPSE_OK;
 }
 
+// One set of weights on the sliced layout: a failed allocation leaves it
+// absent (the CSR kernels serve), other errors fail.
+extern "C++" template <typename Alloc, typename Fill, typename Release>
+int sell_stream(dcpse_plan_t* P, const char* what, Alloc alloc, Fill fill, Release release) {
+    cudaError_t e = alloc();
+    if (e == cudaSuccess) e = fill();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+    if (e == cudaSuccess) return DCPSE_OK;
+    release();
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return DCPSE_OK;
+    }
+    return fail(DCPSE_ERR_CUDA, std::string(what) + cudaGetErrorString(e));
+}
+
+// The FP32 output weights on the sliced layout, built at assembly.
+int ensure_sell(dcpse_plan_t* P) {
+    if (P->sell_w || !P->w32) return DCPSE_OK;
+    if (int rc = ensure_sell_layout(P)) return rc;
+    if (!P->sell_cols) return DCPSE_OK;
+    return sell_stream(
+        P, "sliced ELL weights: ", [&] { return dalloc(&P->sell_w, (size_t)P->nout * P->sell_total + kPad); },
+        [&] {
+            return sell_fill(P->rowptr, P->cols, P->w32, nullptr, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
+                             P->sell_row, P->sell_off, P->sell_total, nullptr, P->sell_w, nullptr, P->stream);
+        },
+        [&] { dfree(P->sell_w); });
+}
+
+// The FP64 summed weights on the sliced layout, built on the first batched
+// FP64 apply.
+int ensure_sell64(dcpse_plan_t* P) {
+    if (P->sell_w64 || !P->w64) return DCPSE_OK;
+    if (int rc = ensure_sell_layout(P)) return rc;
+    if (!P->sell_cols) return DCPSE_OK;
+    return sell_stream(
+        P, "sliced ELL FP64 weights: ",
+        [&] { return dalloc(&P->sell_w64, (size_t)P->nout * P->sell_total + kPad); },
+        [&] {
+            return sell_fill64(P->rowptr, P->w64, P->nnz, P->nout, P->n, P->sell_row, P->sell_off, P->sell_total,
+                               P->sell_w64, P->stream);
+        },
+        [&] { dfree(P->sell_w64); });
+}
+
 // The bf16 residual streams on the sliced layout, built on the first apply
-// that asks for them (the weights' layout must exist).
+// that asks for them (the FP32 weights' layout must exist).
 int ensure_sell_resid(dcpse_plan_t* P) {
     if (P->sell_r || !P->sell_w || !P->r16) return DCPSE_OK;
-    cudaError_t e = cudaMalloc(&P->sell_r, ((size_t)P->nout * P->sell_total + kPad) * 2);
-    if (e == cudaSuccess)
-        e = sell_fill(P->rowptr, P->cols, nullptr, P->r16, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
-                      P->sell_row, P->sell_off, P->sell_total, P->sell_cols, nullptr, P->sell_r, P->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
-    if (e != cudaSuccess) {
-        if (P->sell_r) cudaFree(P->sell_r);
-        P->sell_r = nullptr;
-        if (e == cudaErrorMemoryAllocation || e == cudaErrorInvalidValue) {
-            cudaGetLastError();
-            return DCPSE_OK;  // the CSR kernels serve this precision
-        }
-        return fail(DCPSE_ERR_CUDA, std::string("sliced ELL residuals: ") + cudaGetErrorString(e));
-    }
-    return DCPSE_OK;
+    return sell_stream(
+        P, "sliced ELL residuals: ",
+        [&] { return cudaMalloc(&P->sell_r, ((size_t)P->nout * P->sell_total + kPad) * 2); },
+        [&] {
+            return sell_fill(P->rowptr, P->cols, nullptr, P->r16, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
+                             P->sell_row, P->sell_off, P->sell_total, nullptr, nullptr, P->sell_r, P->stream);
+        },
+        [&] {
+            if (P->sell_r) cudaFree(P->sell_r);
+            P->sell_r = nullptr;
+        });
 }
 
 // The FP32 batched apply of rows [r0, r1) (0, 0: all rows) from the plan's
@@ -1689,7 +1735,10 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
         sa.ors = 1;
         sa.w0 = rr0 / 256;
         sa.w1 = (rr1 + 255) / 256;
-        sa.comp = ap.comp;
+        // a row's entries are summed by one thread: the compensated sum for
+        // every output keeps first-order outputs at the CSR kernel's accuracy
+        // (128^3 gradient: 5e-7 plain, ~1e-7 compensated; 1.5 % slower)
+        sa.comp = 0xffffffffu;
         sa.no_self = 0;
         P->tstart(DCPSE_K_APPLY_BATCHED, st);
         cudaError_t e = apply_sell(sa, P->nout, st);
@@ -1727,6 +1776,30 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
         return apply_f32_rows(P, precision, d_out, 0, 0);
     } else if (precision == DCPSE_F64) {
         if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
+        const int mode = P->apply_mode & 15;
+        if (mode == 0 || mode == 4) {
+            if (int rc = ensure_sell64(P)) return rc;
+            if (P->sell_w64) {
+                Sell64Args sa{};
+                sa.n = P->n;
+                sa.nwin = (P->n + 255) / 256;
+                sa.srow = P->sell_row;
+                sa.off = P->sell_off;
+                sa.cols = P->sell_cols;
+                sa.w = P->sell_w64;
+                sa.total = P->sell_total;
+                sa.f = d_f;
+                sa.fs = 1;
+                sa.out = d_out;
+                sa.oos = P->n;
+                sa.ors = 1;
+                P->tstart(DCPSE_K_APPLY_BATCHED);
+                cudaError_t e = apply_sell64(sa, P->nout, P->stream);
+                P->tstop(DCPSE_K_APPLY_BATCHED);
+                DCPSE_CK(e);
+                return DCPSE_OK;
+            }
+        }
         P->tstart(DCPSE_K_APPLY_BATCHED);
         cudaError_t e = apply_batched_f64(P->n, P->nout, P->rowptr, P->cols, P->w64, P->nnz, d_f, d_out, P->stream);
         P->tstop(DCPSE_K_APPLY_BATCHED);
@@ -2005,7 +2078,7 @@ int dcpse_p2p(dcpse_plan_t* P, const double* d_f_support, int ncomp, double* d_o
                     sa.ors = ncomp;
                     sa.w0 = 0;
                     sa.w1 = (P->n + 255) / 256;
-                    sa.comp = ap.comp;
+                    sa.comp = 0xffffffffu;  // one thread sums the whole row
                     sa.no_self = 1;
                     P->tstart(DCPSE_K_APPLY_BATCHED);
                     cudaError_t e = apply_sell(sa, P->nout, P->stream);
@@ -2022,6 +2095,31 @@ int dcpse_p2p(dcpse_plan_t* P, const double* d_f_support, int ncomp, double* d_o
             DCPSE_CK(e);
         } else if (precision == DCPSE_F64) {
             if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
+            const int mode = P->apply_mode & 15;
+            if ((mode == 0 || mode == 4) && nf > 0) {
+                if (int rc = ensure_sell64(P)) return rc;
+                if (P->sell_w64) {
+                    Sell64Args sa{};
+                    sa.n = P->n;
+                    sa.nwin = (P->n + 255) / 256;
+                    sa.srow = P->sell_row;
+                    sa.off = P->sell_off;
+                    sa.cols = P->sell_cols;
+                    sa.w = P->sell_w64;
+                    sa.total = P->sell_total;
+                    sa.f = d_f_support + c;
+                    sa.fs = ncomp;
+                    sa.out = d_out + c;
+                    sa.oos = P->n * ncomp;
+                    sa.ors = ncomp;
+                    sa.no_self = 1;
+                    P->tstart(DCPSE_K_APPLY_BATCHED);
+                    cudaError_t e = apply_sell64(sa, P->nout, P->stream);
+                    P->tstop(DCPSE_K_APPLY_BATCHED);
+                    DCPSE_CK(e);
+                    continue;
+                }
+            }
             P->tstart(DCPSE_K_APPLY_BATCHED);
             cudaError_t e = apply_batched_f64(P->n, P->nout, P->rowptr, P->cols, P->w64, P->nnz,
                                               nf > 0 ? d_f_support + c : nullptr, d_out + c, P->stream, 1,

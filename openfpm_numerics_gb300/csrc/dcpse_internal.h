@@ -191,13 +191,31 @@ int64_t sell_slices(int64_t n);
 // scan_tmp [scan_tmp_elems(sell_slices(n))]
 cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t* slen32, int64_t* off,
                        int64_t* scan_tmp, cudaStream_t s);
-// Copies the CSR columns and weights (w / sw given) and the bf16 residual
-// streams (r16 / sr16 given) into the sliced layout; one_set: the columns
+// Copies into the sliced layout the columns (scols given), the FP32 weights
+// (w / sw given) and the bf16 residual streams (r16 / sr16 given); the
+// streams asked for must be consecutive in that order.  one_set: the columns
 // index the rows' own set.
 cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, const void* r16, int64_t ws,
                       int nout, int64_t n, int one_set, const int32_t* srow, const int64_t* off, int64_t total,
                       int32_t* scols, float* sw, void* sr16, cudaStream_t s);
 cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s);
+// FP64 summed weights on the same slices ([nout][total]) and their apply
+cudaError_t sell_fill64(const int64_t* rowptr, const double* w, int64_t ws, int nout, int64_t n,
+                        const int32_t* srow, const int64_t* off, int64_t total, double* sw, cudaStream_t s);
+struct Sell64Args {
+    int64_t n, nwin;
+    const int32_t* srow;
+    const int64_t* off;
+    const int32_t* cols;
+    const double* w;        // [NO][total]
+    int64_t total;
+    const double* f;        // field, element i at f[i * fs]
+    int64_t fs;
+    double* out;            // output o of row r at out[o * oos + r * ors]
+    int64_t oos, ors;
+    int no_self;
+};
+cudaError_t apply_sell64(const Sell64Args& a, int nout, cudaStream_t s);
 
 // Full description of a batched FP32 apply (plan-owned, padded arrays).
 struct ApplyF32 {

@@ -116,6 +116,99 @@ __global__ void __launch_bounds__(256) sell_fill_kernel(const int64_t* __restric
     }
 }
 
+// FP64 weights on the same slices: warp per slice, 16 entries at a time
+// through a [16][33] block of doubles per warp (coalesced reads and writes)
+__global__ void __launch_bounds__(256) sell_fill64_kernel(const int64_t* __restrict__ rowptr,
+                                                          const double* __restrict__ w, int64_t ws, int nout,
+                                                          int64_t nslices, const int32_t* __restrict__ srow,
+                                                          const int64_t* __restrict__ off, int64_t total,
+                                                          double* __restrict__ sw) {
+    __shared__ double tiles[8][16 * 33];
+    const int lane = threadIdx.x & 31;
+    double* tile = tiles[threadIdx.x >> 5];
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp0; s < nslices; s += nwarps) {
+        const int32_t myrow = srow[s * kSlice + lane];
+        const int64_t b = off[s];
+        const int L = (int)((off[s + 1] - b) / kSlice);
+        const int64_t myrb = myrow >= 0 ? rowptr[myrow] : 0;
+        const int myk = myrow >= 0 ? (int)(rowptr[myrow + 1] - myrb) : 0;
+        for (int o = 0; o < nout; ++o) {
+            for (int j0 = 0; j0 < L; j0 += 16) {
+                // lanes 0-15 read entries of row r, lanes 16-31 of row r + 1
+                for (int r = 0; r < kSlice; r += 2) {
+                    const int rr = r + (lane >> 4);
+                    const int64_t rb = __shfl_sync(0xffffffffu, myrb, rr);
+                    const int k = __shfl_sync(0xffffffffu, myk, rr);
+                    const int j = j0 + (lane & 15);
+                    if (j < k) tile[(lane & 15) * 33 + rr] = w[(int64_t)o * ws + rb + j];
+                }
+                __syncwarp();
+                const int jn = min(16, L - j0);
+                for (int jj = 0; jj < jn; ++jj) {
+                    const int j = j0 + jj;
+                    sw[(int64_t)o * total + b + (int64_t)j * kSlice + lane] = j < myk ? tile[jj * 33 + lane] : 0.0;
+                }
+                __syncwarp();
+            }
+        }
+    }
+}
+
+// FP64 batched apply on the slices: a row per thread, summed weights, the
+// difference form acc_o += w_o (f_q - f_p) with fused multiply-adds (the
+// CSR FP64 kernel's arithmetic without its cross-lane reduction)
+template <int NO>
+__global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
+    __shared__ double tile[NO][kWin];
+    const int lane = threadIdx.x & 31;
+    constexpr int U = 2;  // 38 registers at four outputs: six CTAs per SM
+    for (int64_t win = blockIdx.x; win < a.nwin; win += gridDim.x) {
+        const int64_t s = win * kSlicesPerWin + (threadIdx.x >> 5);
+        const int32_t row = a.srow[s * kSlice + lane];
+        const int64_t b = a.off[s];
+        const int L = (int)((a.off[s + 1] - b) / kSlice);
+        const double fp = (row >= 0 && !a.no_self) ? a.f[(int64_t)row * a.fs] : 0.0;
+        double acc[NO];
+#pragma unroll
+        for (int o = 0; o < NO; ++o) acc[o] = 0.0;
+        const int32_t* __restrict__ c = a.cols + b + lane;
+        const double* __restrict__ w = a.w + b + lane;
+        for (int j0 = 0; j0 < L; j0 += U) {
+            int32_t q[U];
+            double wv[U][NO], fq[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = j0 + u;
+                const bool ok = j < L;
+                q[u] = ok ? c[(int64_t)j * kSlice] : 0;
+#pragma unroll
+                for (int o = 0; o < NO; ++o) wv[u][o] = ok ? w[(int64_t)o * a.total + (int64_t)j * kSlice] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? a.f[(int64_t)q[u] * a.fs] : fp;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const double d = fq[u] - fp;
+#pragma unroll
+                for (int o = 0; o < NO; ++o) acc[o] = fma(wv[u][o], d, acc[o]);
+            }
+        }
+        if (row >= 0) {
+#pragma unroll
+            for (int o = 0; o < NO; ++o) tile[o][row - win * kWin] = acc[o];
+        }
+        __syncthreads();
+        const int64_t r = win * kWin + threadIdx.x;
+        if (r < a.n) {
+#pragma unroll
+            for (int o = 0; o < NO; ++o) a.out[(int64_t)o * a.oos + r * a.ors] = tile[o][threadIdx.x];
+        }
+        __syncthreads();
+    }
+}
+
 // thread per row; block = one window of 8 slices (five blocks per SM fit the
 // registers without spills up to four outputs, four up to six, three above)
 template <int NO, int U, bool RESID>
@@ -192,12 +285,45 @@ cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w
                       int32_t* scols, float* sw, void* sr16, cudaStream_t s) {
     const int64_t ns = sell_slices(n);
     if (ns == 0) return cudaSuccess;
-    // columns and weights when sw is given, the residual streams when sr16 is
-    const int st_begin = sw ? -1 : nout, st_end = sr16 ? 2 * nout : nout;
+    // the columns when scols is given, the weights when sw is, the residual
+    // streams when sr16 is (consecutive stream ranges)
+    const int st_begin = scols ? -1 : (sw ? 0 : nout);
+    const int st_end = sr16 ? 2 * nout : (sw ? nout : 0);
+    if (st_end <= st_begin) return cudaSuccess;
     const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 6);
     sell_fill_kernel<<<grid, 256, 0, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, one_set, scols, sw,
                                           static_cast<const uint16_t*>(r16), static_cast<uint16_t*>(sr16), st_begin,
                                           st_end);
+    return cudaGetLastError();
+}
+
+cudaError_t sell_fill64(const int64_t* rowptr, const double* w, int64_t ws, int nout, int64_t n,
+                        const int32_t* srow, const int64_t* off, int64_t total, double* sw, cudaStream_t s) {
+    const int64_t ns = sell_slices(n);
+    if (ns == 0) return cudaSuccess;
+    const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 6);
+    sell_fill64_kernel<<<grid, 256, 0, s>>>(rowptr, w, ws, nout, ns, srow, off, total, sw);
+    return cudaGetLastError();
+}
+
+cudaError_t apply_sell64(const Sell64Args& a, int nout, cudaStream_t s) {
+    if (a.nwin == 0) return cudaSuccess;
+    if (a.nwin > 0x7fffffff) return cudaErrorInvalidValue;
+    switch (nout) {
+#define DCPSE_SELL64_CASE(NO) \
+    case NO: apply_sell64_kernel<NO><<<(unsigned)a.nwin, 256, 0, s>>>(a); break;
+        DCPSE_SELL64_CASE(1)
+        DCPSE_SELL64_CASE(2)
+        DCPSE_SELL64_CASE(3)
+        DCPSE_SELL64_CASE(4)
+        DCPSE_SELL64_CASE(5)
+        DCPSE_SELL64_CASE(6)
+        DCPSE_SELL64_CASE(7)
+        DCPSE_SELL64_CASE(8)
+#undef DCPSE_SELL64_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

@@ -199,7 +199,7 @@ def test_apply_schedules(cuda, orc, name):
     """Direct and TMA-staged loading give identical bits; every lane count
     and the bf16-residual correction stay within their bars."""
     c = _case(name)
-    plan, pos, _ = _build(c, C.STORE_TERMS_F64 | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID)
+    plan, pos, _ = _build(c, C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID)
     f = torch.tensor(np.random.default_rng(8).standard_normal(c["pos"].shape[0]), device="cuda")
     refs = torch.stack([plan.apply_output_f64(o, f) for o in range(len(c["outputs"]))]).cpu().numpy()
     staged = 0
@@ -244,6 +244,13 @@ def test_apply_schedules(cuda, orc, name):
         g = plan.apply(f, C.F32_RESID).cpu().numpy()
         for o in range(len(refs)):
             assert np.abs(g[o] - refs[o]).max() <= 1e-9 * np.abs(refs[o]).max(), (mode, o)
+    # batched FP64: CSR kernel (mode 1) and sliced layout (modes 0 and 4)
+    if plan.output_weights(0)[0] is not None:
+        for mode in (1, 4, 0):
+            plan.set_apply_config(0, mode)
+            g = plan.apply(f, C.F64).cpu().numpy()
+            for o in range(len(refs)):
+                assert np.abs(g[o] - refs[o]).max() <= 1e-12 * np.abs(refs[o]).max(), (mode, o)
     plan.set_apply_config(0, 0)
 
 
