@@ -114,6 +114,24 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def max_over_ranks(times, dist=None, device="cpu"):
+    """Per-rank times -> their maxima over all ranks (the slowest rank sets
+    the job's time); unchanged in a single process."""
+    if dist is None:
+        return [float(t) for t in times]
+    import torch
+
+    t = torch.tensor([float(x) for x in times], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def job_value(world, n, nout, t):
+    """Whole-job throughput in Gparticle-ops/s: every rank applies nout
+    outputs to its own n particles in time t (replicas, weak scaling)."""
+    return world * n * nout / t / 1e9
+
+
 def rel_err(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
@@ -306,10 +324,7 @@ def run_ours(args):
     s_ms, s_launch = plan.timing(C.K_SPLIT)
     clk = clocks.stop()
     plan.check()
-    if dist:
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    (t_step,) = max_over_ranks([t_step], dist, dev)
     res32 = out.cpu().numpy()
 
     # end to end through the host-buffer entry point (pinned host memory)
@@ -320,6 +335,8 @@ def run_ours(args):
     for _ in range(3):
         plan.apply_host(hf_np, hout_np, C.F32)
     n_e2e = max(3, min(args.steps, 200))
+    if dist:
+        dist.barrier()
     torch.cuda.synchronize()
     ev0.record(stream)
     for _ in range(n_e2e):
@@ -327,6 +344,7 @@ def run_ours(args):
     ev1.record(stream)
     torch.cuda.synchronize()
     t_e2e = ev0.elapsed_time(ev1) / 1e3 / n_e2e
+    (t_e2e,) = max_over_ranks([t_e2e], dist, dev)
     assert np.array_equal(hout_np, res32)
 
     # accuracy
@@ -362,7 +380,7 @@ def run_ours(args):
     _pk = _ct.c_double()
     C.call("dcpse_measure_fp64_peak", _ct.c_void_p(stream.cuda_stream), _ct.byref(_pk))
     fp64_peak = _pk.value
-    value = world * N * NOUT / t_step / 1e9
+    value = job_value(world, N, NOUT, t_step)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -387,7 +405,7 @@ def run_ours(args):
                          "traffic": traffic, "peak_source": peak_kind,
                          "kernel": kname,
                          "algorithmic_bytes_per_launch": bytes_apply, "kernel_ms": t_kernel * 1e3},
-            "e2e": {"value": world * N * NOUT / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": N * 8,
+            "e2e": {"value": job_value(world, N, NOUT, t_e2e), "unit": UNIT, "h2d_bytes_per_step": N * 8,
                     "d2h_bytes_per_step": NOUT * N * 8, "ms_per_step": t_e2e * 1e3,
                     "api": "dcpse_apply_batched_host"},
             "gpu_launches": int(k_launch + s_launch),
