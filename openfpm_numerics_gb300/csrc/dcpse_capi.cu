@@ -311,8 +311,9 @@ struct dcpse_plan_s {
     ChunkBounds chunks{};                // row chunks the reaches are for
     int64_t list_version = 0;            // bumped whenever the neighbour list changes
     int64_t reach_version = -1;          // list version the reaches were computed for
-    double* hf = nullptr;    // device copy of a host field (host apply)
-    double* hout = nullptr;  // device output for host apply
+    double* hf = nullptr;    // device copy of a host field (host apply), hf_len values
+    double* hout = nullptr;  // device outputs for host apply, nout * hf_len values
+    int64_t hf_len = 0;      // particles hf and hout were sized for (the list may change n)
 
     // the FP32 output weights on the sliced ELL layout (built on first use)
     int32_t* sell_row = nullptr;
@@ -360,6 +361,7 @@ struct dcpse_plan_s {
         dfree(f2);
         dfree(hf);
         dfree(hout);
+        hf_len = 0;
         dfree(summary);
         dfree(d_err);
         dfree(asm_scratch);
@@ -1867,8 +1869,16 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
     if (int rc = check_single_set(P)) return rc;
     if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
     if (P->n > 0 && (!h_f || !h_out)) return fail(DCPSE_ERR_ARG, "NULL field");
-    if (!P->hf) DCPSE_CK(dalloc(&P->hf, P->n));
-    if (!P->hout) DCPSE_CK(dalloc(&P->hout, (size_t)P->nout * P->n));
+    // staging for pageable buffers, sized for the current particle count
+    // (a new neighbour list may have more particles than the last call saw)
+    if (P->hf_len < P->n || !P->hf) {
+        dfree(P->hf);
+        dfree(P->hout);
+        P->hf_len = 0;
+        DCPSE_CK(dalloc(&P->hf, P->n));
+        DCPSE_CK(dalloc(&P->hout, (size_t)P->nout * P->n));
+        P->hf_len = P->n;
+    }
     const bool f32 = precision == DCPSE_F32 || precision == DCPSE_F32_RESID;
     if (!f32 || (P->apply_mode & 15) == 2 || P->n < kHostChunkMinRows) {
         DCPSE_CK(cudaMemcpyAsync(P->hf, h_f, sizeof(double) * P->n, cudaMemcpyHostToDevice, P->stream));

@@ -371,3 +371,20 @@ def test_host_apply_chunked_equals_device(cuda):
             plan.apply_host(pinned_f.numpy(), pinned.numpy(), precision=prec)
             assert np.array_equal(pinned.numpy(), dev)
     plan.close()
+
+
+def test_host_apply_after_particle_count_grows(cuda):
+    """A new neighbour list with more particles than the last host-buffer
+    call saw: the device staging of pageable buffers is re-sized (copy
+    pipeline and the single-copy FP64 path)."""
+    plan = DcpsePlan(3, GRAD_LAP_3D, order=2)
+    for nside in (44, 52):
+        pos, h = W.lattice(nside, 3, jitter=0.15, seed=nside)
+        pt = torch.tensor(pos, device="cuda")
+        plan.build_neighbors(pt, 2.8 * h)
+        plan.assemble(pt, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F64)
+        f = np.sin(3 * pos[:, 0]) + pos[:, 1] * pos[:, 2]
+        for prec in (C.F32, C.F64):
+            dev = plan.apply(torch.tensor(f, device="cuda"), prec).cpu().numpy()
+            assert np.array_equal(plan.apply_host(f, precision=prec), dev)
+    plan.close()
