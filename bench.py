@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--nside", type=int, default=128)
     ap.add_argument("--cpu-sample", type=int, default=32768, help="particles in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["apply", "assemble", "gray-scott", "graded", "interp"], default=None,
+    ap.add_argument("--only", choices=["apply", "apply64", "assemble", "gray-scott", "graded", "interp"], default=None,
                     help="small-footprint run of one kernel family (for profiler captures)")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--mode", type=int, default=0, help="apply kernel: 0 auto, 1 CSR direct, 2 CSR TMA-staged, 3 CSR 8-deep, 4 sliced ELL")
@@ -661,8 +661,9 @@ def run_graded(args):
 
 def run_only(args):
     """One kernel family on the benchmark geometry, nothing else resident:
-    --only apply keeps just the FP32 weights (fast assembly), --only assemble
-    runs the reference-order and fast assemblies."""
+    --only apply keeps just the FP32 weights (fast assembly), --only apply64
+    just the FP64 summed weights (batched FP64 apply), --only assemble runs
+    the reference-order and fast assemblies."""
     import torch
 
     from openfpm_numerics_gb300 import _capi as C
@@ -703,6 +704,21 @@ def run_only(args):
         ms, k = plan.timing(C.K_APPLY_BATCHED)
         res["apply_ms"] = ms / max(k, 1)
         res["achieved_gbs"] = W.apply_bytes(N, nnz, NOUT, 4) / (ms / max(k, 1) / 1e3) / 1e9
+    elif args.only == "apply64":
+        plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F64)
+        out = torch.empty((NOUT, N), dtype=torch.float64, device="cuda")
+        for _ in range(args.warmup):
+            plan.apply(f, C.F64, out)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.apply(f, C.F64, out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / max(args.steps, 1)
+        res["apply64_ms"] = t
+        res["apply64_gbs"] = W.apply_bytes(N, nnz, NOUT, 8) / (t / 1e3) / 1e9
     else:
         plan.set_assembly_config(0, 4, args.qr_lanes)
         for _ in range(max(1, args.steps)):
