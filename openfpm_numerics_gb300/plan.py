@@ -189,8 +189,10 @@ class DcpsePlan:
     def assemble(self, pos, flags=C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32, eps_fixed=None,
                  allow_failed_particles=True):
         pos = self._check_pos(pos)
+        self._check_rows(pos.shape[0], self.n, "positions")
         if eps_fixed is not None:
             eps_fixed = eps_fixed.contiguous().to(torch.float64)
+            self._check_rows(eps_fixed.numel(), self.n, "eps_fixed")
         allow = (C.ERR_PARTICLES,) if allow_failed_particles else ()
         return C.call("dcpse_assemble", self._h, _ptr(pos), _ptr(eps_fixed), int(flags), allow=allow)
 
@@ -230,13 +232,13 @@ class DcpsePlan:
     # -- apply ----------------------------------------------------------
     def apply_term_f64(self, term, f, out=None):
         f = self._check_field(f)
-        out = torch.empty_like(f) if out is None else out
+        out = torch.empty_like(f) if out is None else self._check_out(out, f.shape)
         C.call("dcpse_apply_term_f64", self._h, int(term), _ptr(f), _ptr(out))
         return out
 
     def apply_output_f64(self, output, f, out=None):
         f = self._check_field(f)
-        out = torch.empty_like(f) if out is None else out
+        out = torch.empty_like(f) if out is None else self._check_out(out, f.shape)
         C.call("dcpse_apply_output_f64", self._h, int(output), _ptr(f), _ptr(out))
         return out
 
@@ -245,23 +247,33 @@ class DcpsePlan:
         f = self._check_field(f)
         if out is None:
             out = torch.empty((self.n_outputs, f.shape[0]), dtype=torch.float64, device=f.device)
+        else:
+            self._check_out(out, (self.n_outputs, f.shape[0]))
         C.call("dcpse_apply_batched", self._h, _ptr(f), _ptr(out), int(precision))
         return out
 
     def apply_host(self, f_host, out_host=None, precision=C.F32):
         """Host numpy arrays in and out (the copies are part of the call)."""
         f_host = np.ascontiguousarray(f_host, dtype=np.float64)
+        if f_host.ndim != 1:
+            raise ValueError("fields are float64 [n] arrays")
+        self._check_rows(f_host.shape[0], self.n, "field")
         if out_host is None:
             out_host = np.empty((self.n_outputs, f_host.shape[0]), dtype=np.float64)
+        elif (out_host.dtype != np.float64 or out_host.shape != (self.n_outputs, f_host.shape[0])
+              or not out_host.flags.c_contiguous or not out_host.flags.writeable):
+            raise ValueError("out_host must be a writeable C-contiguous float64 array of shape %s"
+                             % ((self.n_outputs, f_host.shape[0]),))
         C.call("dcpse_apply_batched_host", self._h, f_host.ctypes.data_as(ctypes.c_void_p),
                out_host.ctypes.data_as(ctypes.c_void_p), int(precision))
         return out_host
 
     # -- particle to particle interpolation -----------------------------
-    @staticmethod
-    def _check_support_field(f):
+    def _check_support_field(self, f):
         if f.dtype != torch.float64 or f.dim() not in (1, 2):
             raise ValueError("support fields are float64 [n_support] or [n_support, ncomp] CUDA tensors")
+        sup = getattr(self, "_support", None)
+        self._check_rows(f.shape[0], sup.shape[0] if sup is not None else self.n, "support field")
         return f.contiguous()
 
     def p2p_f64(self, term, f, out=None):
@@ -271,7 +283,7 @@ class DcpsePlan:
         ncomp = 1 if f.dim() == 1 else f.shape[1]
         n = self.info()["n"]
         shape = (n,) if f.dim() == 1 else (n, ncomp)
-        out = torch.empty(shape, dtype=torch.float64, device=f.device) if out is None else out
+        out = torch.empty(shape, dtype=torch.float64, device=f.device) if out is None else self._check_out(out, shape)
         C.call("dcpse_p2p_f64", self._h, int(term), _ptr(f), int(ncomp), _ptr(out))
         return out
 
@@ -282,7 +294,7 @@ class DcpsePlan:
         ncomp = 1 if f.dim() == 1 else f.shape[1]
         n = self.info()["n"]
         shape = (self.n_outputs, n) if f.dim() == 1 else (self.n_outputs, n, ncomp)
-        out = torch.empty(shape, dtype=torch.float64, device=f.device) if out is None else out
+        out = torch.empty(shape, dtype=torch.float64, device=f.device) if out is None else self._check_out(out, shape)
         C.call("dcpse_p2p", self._h, _ptr(f), int(ncomp), _ptr(out), int(precision))
         return out
 
@@ -312,7 +324,9 @@ class DcpsePlan:
         g = g.contiguous().to(torch.float64)
         if g.dim() == 1:
             g = g.unsqueeze(0)
-        out = torch.empty(g.shape[1], dtype=torch.float64, device=g.device) if out is None else out
+        self._check_cotangent(g)
+        out = torch.empty(g.shape[1], dtype=torch.float64, device=g.device) if out is None else \
+            self._check_out(out, (g.shape[1],))
         C.call("dcpse_vjp_field", self._h, _ptr(g), _ptr(out), int(precision))
         return out
 
@@ -320,12 +334,15 @@ class DcpsePlan:
         """d/dpos of sum_o,p g[o,p] (L_o f)_p with the neighbour list fixed
         -> [n, dim] (FP64; pos must be the assembled positions)."""
         pos = self._check_pos(pos)
+        self._check_rows(pos.shape[0], self.n, "positions")
         f = self._check_field(f)
         g = g.contiguous().to(torch.float64)
         if g.dim() == 1:
             g = g.unsqueeze(0)
+        self._check_cotangent(g)
         if eps_fixed is not None:
             eps_fixed = eps_fixed.contiguous().to(torch.float64)
+            self._check_rows(eps_fixed.numel(), self.n, "eps_fixed")
         grad = torch.empty_like(pos)
         C.call("dcpse_vjp_positions", self._h, _ptr(pos), _ptr(eps_fixed), _ptr(f), _ptr(g), _ptr(grad))
         return grad
@@ -368,4 +385,25 @@ class DcpsePlan:
     def _check_field(self, f):
         if f.dtype != torch.float64 or f.dim() != 1:
             raise ValueError("fields are float64 [n] CUDA tensors")
+        self._check_rows(f.shape[0], self.n, "field")
         return f.contiguous()
+
+    # The C-ABI takes bare pointers sized by the plan's particle count, so
+    # lengths are checked here: a short array would be read or written out of
+    # bounds on the device.  (No list yet: the library reports the state.)
+    @staticmethod
+    def _check_rows(rows, n, what):
+        if n is not None and n >= 0 and rows != n:
+            raise ValueError("%s has %d rows, the plan's particle set has %d" % (what, rows, n))
+
+    def _check_cotangent(self, g):
+        if g.dim() != 2 or g.shape[0] != self.n_outputs:
+            raise ValueError("cotangents are [n_outputs, n] = [%d, n] tensors" % self.n_outputs)
+        self._check_rows(g.shape[1], self.n, "cotangent")
+
+    @staticmethod
+    def _check_out(out, shape):
+        if out.dtype != torch.float64 or tuple(out.shape) != tuple(shape):
+            raise ValueError("out must be a float64 tensor of shape %s, not %s %s"
+                             % (tuple(shape), out.dtype, tuple(out.shape)))
+        return out

@@ -388,3 +388,26 @@ def test_host_apply_after_particle_count_grows(cuda):
             dev = plan.apply(torch.tensor(f, device="cuda"), prec).cpu().numpy()
             assert np.array_equal(plan.apply_host(f, precision=prec), dev)
     plan.close()
+
+
+def test_lengths_checked_before_the_device(cuda):
+    """Arrays whose length does not match the plan's particle set are refused
+    on the host (the C-ABI takes bare pointers sized by the plan)."""
+    pos, h = W.lattice(12, 2, jitter=0.1, seed=20)
+    plan = DcpsePlan(2, [[(1, 0)], [(2, 0), (0, 2)]], order=2)
+    pt = torch.tensor(pos, device="cuda")
+    plan.build_neighbors(pt, 3.1 * h)
+    plan.assemble(pt)
+    n = pos.shape[0]
+    short = torch.zeros(n - 1, dtype=torch.float64, device="cuda")
+    good = torch.zeros(n, dtype=torch.float64, device="cuda")
+    for call in (lambda: plan.apply(short), lambda: plan.apply_term_f64(0, short),
+                 lambda: plan.apply_output_f64(0, short), lambda: plan.apply_host(np.zeros(n + 1)),
+                 lambda: plan.assemble(pt[:-1]), lambda: plan.vjp_field(torch.zeros((2, n - 1), device="cuda")),
+                 lambda: plan.apply(good, C.F32, torch.empty((2, n - 1), dtype=torch.float64, device="cuda")),
+                 lambda: plan.apply_host(np.zeros(n), np.empty((2, n), dtype=np.float32))):
+        with pytest.raises(ValueError):
+            call()
+    # the plan is untouched
+    assert plan.apply(good).shape == (2, n)
+    plan.close()
