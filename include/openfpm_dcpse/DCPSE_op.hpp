@@ -20,6 +20,7 @@
 #include <array>
 #include <functional>
 #include <memory>
+#include <stdexcept>
 #include <string>
 #include <tuple>
 #include <type_traits>
@@ -80,6 +81,15 @@ struct prop_ncomp<V, std::enable_if_t<(std::tuple_size<V>::value > 0)>>
     : std::integral_constant<int, (int)std::tuple_size<V>::value> {};
 template <typename T, std::size_t N>
 struct prop_ncomp<T[N], void> : std::integral_constant<int, (int)N> {};
+
+// the C-ABI reads and writes n values per field: a property of another
+// particle count (particles added or removed without update()) is refused
+inline void check_rows(std::size_t rows, int64_t n) {
+    if (n >= 0 && (int64_t)rows != n)
+        throw std::invalid_argument("DC-PSE operator: the property has " + std::to_string(rows) +
+                                    " values, the operator was built for " + std::to_string(n) +
+                                    " particles (call update() after changing the particle set)");
+}
 }  // namespace detail
 
 // getV<prp>(parts): a property of a particle set, usable as an operand and
@@ -204,6 +214,7 @@ public:
         const std::size_t outs = outputs_.size();
         nd.eval = [P, arg, outs](std::vector<std::vector<double>>& out) {
             std::vector<double> f = arg.values();
+            detail::check_rows(f.size(), P->n());
             out.assign(outs, std::vector<double>(f.size()));
             for (std::size_t o = 0; o < outs; ++o) P->apply_output((int)o, f.data(), out[o].data());
         };
@@ -216,6 +227,7 @@ public:
     template <unsigned int prp, typename vector_type>
     std::vector<std::vector<double>> apply_f32(PropRef<prp, vector_type> arg) {
         std::vector<double> f = arg.values();
+        detail::check_rows(f.size(), plan_->n());
         std::vector<double> flat(outputs_.size() * f.size());
         detail::check(dcpse_apply_batched_host(plan_->plan(), f.data(), flat.data(), DCPSE_F32));
         std::vector<std::vector<double>> out(outputs_.size());

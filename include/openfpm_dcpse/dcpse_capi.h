@@ -10,6 +10,12 @@
  * Threading: a plan is not thread-safe; every call is enqueued on the plan's
  * stream (default: the legacy default stream) and calls that return data to
  * the host synchronise that stream.
+ *
+ * Array sizes: fields, outputs and positions are bare pointers whose lengths
+ * follow from the plan (n domain particles from the neighbour list, n_support
+ * for support-set fields, n_outputs), as the reference's own property
+ * vectors do; a shorter array is read or written out of bounds.  The C++ and
+ * Python mirrors check the lengths before calling.
  */
 #ifndef OPENFPM_DCPSE_CAPI_H
 #define OPENFPM_DCPSE_CAPI_H
