@@ -123,6 +123,31 @@ def test_moment_identity(orc):
             assert np.allclose(mom, b, atol=1e-9)
 
 
+def test_quadratic_reproduction_3d(orc):
+    """Order 2: the moment conditions cover every monomial of degree 1 ..
+    |alpha| + 1, so a quadratic field's first and second derivatives come out
+    exact up to rounding, on boundary particles too (the property the
+    full-size GPU checks rest on)."""
+    h = 1.0 / 127
+    pos, _ = W.lattice(12, 3, h=h, jitter=0.15, seed=2)
+    rp, cols = orc.neighbors(pos, 2.8 * h)
+    x, y, z = pos.T
+    f = 1 + 3 * x - 2 * y + 0.5 * z + 7 * x * x - 5 * y * z + 11 * z * z + 4 * x * y
+    grads = {(1, 0, 0): 3 + 14 * x + 4 * y, (0, 1, 0): -2 - 5 * z + 4 * x, (0, 0, 1): 0.5 - 5 * y + 22 * z}
+    for sig, exact in grads.items():
+        eps, eip, K, st = orc.assemble(pos, rp, cols, sig, 2)
+        assert np.all(st == 0)
+        got = orc.apply(f, rp, cols, K, eip, 1)
+        assert np.abs(got - exact).max() < 1e-10 * np.abs(exact).max()
+    Ks, E = [], []
+    for sig in [(2, 0, 0), (0, 2, 0), (0, 0, 2)]:
+        eps, eip, K, st = orc.assemble(pos, rp, cols, sig, 2)
+        Ks.append(K)
+        E.append(eip)
+    lap = orc.apply_sum(f, rp, cols, Ks, E, [2, 2, 2])
+    assert np.abs(lap - 36.0).max() < 1e-7 * 36.0
+
+
 def _grid(nside, dim, h, jitter_sigma=None, seed=None):
     ax = np.arange(nside) * h
     g = np.meshgrid(*([ax] * dim), indexing="ij")
