@@ -81,15 +81,6 @@ struct prop_ncomp<V, std::enable_if_t<(std::tuple_size<V>::value > 0)>>
     : std::integral_constant<int, (int)std::tuple_size<V>::value> {};
 template <typename T, std::size_t N>
 struct prop_ncomp<T[N], void> : std::integral_constant<int, (int)N> {};
-
-// the C-ABI reads and writes n values per field: a property of another
-// particle count (particles added or removed without update()) is refused
-inline void check_rows(std::size_t rows, int64_t n) {
-    if (n >= 0 && (int64_t)rows != n)
-        throw std::invalid_argument("DC-PSE operator: the property has " + std::to_string(rows) +
-                                    " values, the operator was built for " + std::to_string(n) +
-                                    " particles (call update() after changing the particle set)");
-}
 }  // namespace detail
 
 // getV<prp>(parts): a property of a particle set, usable as an operand and
@@ -456,6 +447,7 @@ public:
         const int dim = dim_;
         nd.eval = [P, arg, dim](std::vector<std::vector<double>>& out) {
             const std::size_t n = arg.v.size_local();
+            detail::check_rows(n, P->n());
             out.assign(1, std::vector<double>(n, 0.0));
             std::vector<double> d(n);
             for (int i = 0; i < dim; ++i) {
@@ -489,6 +481,8 @@ public:
         const int dim = vt1::dims;
         nd.eval = [P, vel, arg, dim](std::vector<std::vector<double>>& out) {
             const std::size_t n = arg.v.size_local();
+            detail::check_rows(n, P->n());
+            detail::check_rows(vel.v.size_local(), P->n());
             const int nc = PropRef<p2, vt2>::ncomp;
             out.assign(nc, std::vector<double>(n, 0.0));
             std::vector<double> d(n);

@@ -45,6 +45,16 @@ inline void check(int rc, bool allow_particles = false) {
     throw std::runtime_error(std::string("DC-PSE: ") + dcpse_last_error());
 }
 
+// the C-ABI reads and writes as many values per field as the plan has
+// particles: a property of another particle count (particles added or
+// removed without update()) is refused
+inline void check_rows(std::size_t rows, int64_t n) {
+    if (n >= 0 && (int64_t)rows != n)
+        throw std::invalid_argument("DC-PSE operator: the property has " + std::to_string(rows) +
+                                    " values, the operator was built for " + std::to_string(n) +
+                                    " particles (call update() after changing the particle set)");
+}
+
 // Device buffer owned by host code.
 class DevBuf {
 public:
@@ -635,6 +645,8 @@ public:
     template <unsigned int prp1, unsigned int prp2>
     void p2p() {
         const int64_t ns = plan_->n_support(), n = plan_->n();
+        detail::check_rows(support_->size_local(), ns);
+        detail::check_rows(domain_->size_local(), n);
         std::vector<double> f((std::size_t)ns), out((std::size_t)n);
         for (int64_t q = 0; q < ns; ++q) f[(std::size_t)q] = (double)support_->template getProp<prp1>(q);
         plan_->p2p(0, f.data(), 1, out.data());
@@ -646,6 +658,8 @@ public:
     template <unsigned int prp1, unsigned int prp2, std::size_t N1>
     void p2p() {
         const int64_t ns = plan_->n_support(), n = plan_->n();
+        detail::check_rows(support_->size_local(), ns);
+        detail::check_rows(domain_->size_local(), n);
         std::vector<double> f((std::size_t)ns * N1), out((std::size_t)n * N1);
         for (int64_t q = 0; q < ns; ++q)
             for (std::size_t c = 0; c < N1; ++c)
