@@ -28,3 +28,23 @@ def test_host_only_calls():
     assert rc == C.OK
     rc = lib.dcpse_apply_batched(None, None, None, 0)
     assert rc == C.ERR_ARG
+
+
+def test_python_length_checks():
+    """The Python plan checks array lengths and output shapes before any
+    bare-pointer C-ABI call (host logic only)."""
+    import pytest
+    import torch
+
+    from openfpm_numerics_gb300.plan import DcpsePlan
+
+    DcpsePlan._check_rows(5, 5, "field")
+    DcpsePlan._check_rows(7, None, "field")  # no list yet: the library reports the state
+    DcpsePlan._check_rows(7, -1, "field")
+    with pytest.raises(ValueError):
+        DcpsePlan._check_rows(4, 5, "field")
+    out = torch.empty((2, 5), dtype=torch.float64)
+    assert DcpsePlan._check_out(out, (2, 5)) is out
+    for bad in (torch.empty((2, 4), dtype=torch.float64), torch.empty((2, 5), dtype=torch.float32)):
+        with pytest.raises(ValueError):
+            DcpsePlan._check_out(bad, (2, 5))
