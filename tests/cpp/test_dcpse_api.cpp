@@ -195,6 +195,18 @@ static void test_laplacian() {
     bool eq = true;
     for (std::size_t p = 0; p < domain.size_local(); ++p) eq &= domain.getProp<2>(p) == domain.getProp<3>(p);
     EXPECT(eq, "update() equals re-construction");
+
+    // the batched FP32 apply (host buffers, one pass over the summed FP32
+    // weights) against the FP64 reference-order output: FP32 weight rounding
+    // (6e-8) times sums whose terms are ~20x the Laplacian here
+    std::vector<std::vector<double>> f32 = Lap.apply_f32(getV<0>(domain));
+    double num = 0, den = 0;
+    for (std::size_t p = 0; p < domain.size_local(); ++p) {
+        num = std::max(num, std::fabs(f32[0][p] - domain.getProp<2>(p)));
+        den = std::max(den, std::fabs(domain.getProp<2>(p)));
+    }
+    EXPECT(f32.size() == 1 && f32[0].size() == domain.size_local() && num <= 1e-4 * den,
+           "FP32 batched apply within 1e-4 of the FP64 output");
 }
 
 // too few neighbours raise std::length_error (Vandermonde.hpp:109-112)
