@@ -55,11 +55,14 @@ extern "C" {
                                    per output and basis) instead of per-term sums */
 #define DCPSE_ASSEMBLE_ASYNC 16 /* do not synchronise; query dcpse_particle_status */
 #define DCPSE_STORE_OUT_F32_RESID 32 /* also bf16 residuals w64 - w32 of the FP32 weights */
+#define DCPSE_STORE_OUT_F32_CORR 64  /* also FP32 residuals w64 - w32 (for DCPSE_F32_BUDGET) */
 
 /* precision of dcpse_apply_batched */
 #define DCPSE_F64 0
 #define DCPSE_F32 1       /* FP32 weights, exact differences, compensated sums */
 #define DCPSE_F32_RESID 2 /* FP32 weights + bf16 residual correction (near-FP64 accuracy) */
+#define DCPSE_F32_BUDGET 3 /* FP32 weights, then an FP64 residual correction of exactly the
+                              rows whose FP32 error bound exceeds the plan's error budget */
 
 typedef struct dcpse_plan_s dcpse_plan_t;
 
@@ -192,6 +195,47 @@ int dcpse_apply_batched(dcpse_plan_t* plan, const double* d_f, double* d_out, in
  * the call (the reference's bulk apply reads and writes host particles). */
 int dcpse_apply_batched_host(dcpse_plan_t* plan, const double* h_f, double* h_out, int precision);
 
+/* Error budget of DCPSE_F32_BUDGET applies (default 1e-6): every output o
+ * of the call satisfies
+ *     max_p |out_o,p - out64_o,p| <= budget * max_p |out64_o,p|
+ * against the FP64 summed weights out64 (DCPSE_F64).  The FP32 kernel bounds
+ * each row's weight-rounding error, 2^-24 sum_q |w32_o,pq| |f_q - f_p|, and
+ * a second pass adds sum_q (w64 - w32)_o,pq (f_q - f_p) in FP64 to exactly
+ * the rows whose bound exceeds budget/2 of the call's largest |output|.
+ * Needs DCPSE_STORE_OUT_F32_CORR at assembly.  With the bf16 residual
+ * streams also stored (DCPSE_STORE_OUT_F32_RESID) the first pass adds them
+ * and its bound shrinks to 2^-32 sum_q ..., so far fewer rows need the
+ * second pass.  Floor: a corrected row is exact to about 2^-48 sum_q
+ * |w| |f_q - f_p|, the order of the FP64 apply's own rounding, so budgets
+ * below that relative to max|out| (e.g. outputs that vanish identically)
+ * cannot be resolved.  The reference stores its
+ * weights in FP64 only (Dcpse.hpp:59-63, applied at Dcpse.hpp:467-499); this
+ * is how the FP32 weights keep to its results.  budget in (0, 1). */
+int dcpse_plan_set_error_budget(dcpse_plan_t* plan, double budget);
+/* (row, output) pairs the DCPSE_F32_BUDGET applies corrected since the last
+ * reset (synchronises the plan's stream; reset != 0 zeroes the count). */
+int dcpse_plan_budget_stats(dcpse_plan_t* plan, int64_t* pairs_corrected, int reset);
+
+/* Particle numbering of the batched applies' sliced layout.  The apply
+ * gathers f_q for every neighbour q; in the caller's numbering those reads
+ * are local only if the caller's particles are stored in spatial order.  A
+ * neighbour list built by dcpse_build_neighbors (one particle set) carries
+ * the particles' cell order, and the layout built at assembly renumbers rows
+ * and columns by it when the caller's numbering scatters the reads at least
+ * twice as far (mean |q - p| over the entries against the cell order's),
+ * policy 0 (default); policy 1 always renumbers, -1 never.  Results are the
+ * same bit for bit either way (each row keeps its entries' order); outputs
+ * stay in the caller's numbering.  The reference's GPU support builder walks
+ * particles cell by cell for the same reason (SupportBuilder.cuh:14-61).
+ * Applies on row ranges, RK4 stages and p2p keep the caller's numbering
+ * (CSR kernels) on a renumbered layout.  Changing the policy rebuilds the
+ * layout. */
+int dcpse_plan_set_reorder(dcpse_plan_t* plan, int policy);
+/* Whether the current layout is renumbered, and the mean |q - p| of the
+ * list's entries in the caller's numbering and in the cell order (0 when no
+ * cell order is known: caller-built lists, two sets, surface operators). */
+int dcpse_plan_reorder_info(dcpse_plan_t* plan, int* renumbered, double* mean_dist_list, double* mean_dist_cells);
+
 /* ---- particle to particle interpolation --------------------------------
  * Replaces Dcpse::p2p<prp1,prp2>() and p2p<prp1,prp2,N1>() (Dcpse.hpp:198-
  * 297) behind PPInterpolation::p2p (DcpseInterpolation.hpp:133-160): for every
@@ -257,21 +301,30 @@ int dcpse_rk4_gs_adjoint_stage(dcpse_plan_t* plan, int precision, const void* Yu
 /* ---- batched FP32 apply that allocates nothing --------------------------
  * No counterpart in the reference.  For callers that must not allocate
  * device memory: code running inside an allocator or memory-pool callback,
- * in a host function enqueued on a stream, in a latency-critical loop that
- * cannot wait on the driver's allocator, or next to a framework that owns all
- * device memory.  The caller passes everything as device pointers (the CSR
- * list, the FP32 weights of n_outputs outputs laid out [o * w_stride + j],
- * the FP64 field and the [n_outputs * n] output); the only scratch, the
- * (hi, lo) split of the field, is a fixed device array inside the library.
+ * in a latency-critical loop that cannot wait on the driver's allocator, or
+ * next to a framework that owns all device memory.  (A host function
+ * enqueued with cudaLaunchHostFunc may make no CUDA call, this one included:
+ * call it from ordinary host code with the stream instead.)  The caller
+ * passes everything as device pointers (the CSR list, the FP32 weights of
+ * n_outputs outputs laid out [o * w_stride + j], the FP64 field and the
+ * [n_outputs * n] output); the only scratch, the (hi, lo) split of the
+ * field, is a fixed device array inside the library.
  * Limits: n <= DCPSE_NOALLOC_MAX_PARTICLES (larger n is rejected with
- * DCPSE_ERR_CAPACITY); that array (16 MiB) is held on every GPU that loads
- * the library until the process exits.  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress), so make that first
- * call before any stream capture.  All calls share the array: calls that
- * overlap on the GPU (e.g. on two streams) race and must be serialised by
- * the caller.  Every output takes the compensated FP32 sum, so results equal
- * dcpse_apply_batched(..., DCPSE_F32) of a plan configured with
- * DCPSE_APPLY_COMPENSATE_ALL and direct loading (mode 1) at the same lanes. */
+ * DCPSE_ERR_CAPACITY).  w_stride must be at least rowptr[n] (with one output
+ * it may be 0); a smaller stride makes the weight streams overlap.
+ * Set-up: the array (16 MiB) belongs to the library's device code, which the
+ * CUDA runtime loads onto a GPU lazily, on the first call there; that call
+ * also looks up the array's device address (cudaGetSymbolAddress).  So make
+ * one call with n = 0 per device at start-up, before any callback or stream
+ * capture: it does exactly that set-up and nothing else.  The array is then
+ * held until the process exits; the cached address is stale after
+ * cudaDeviceReset, so do not use this entry point after a reset.
+ * All calls share the array: calls that overlap on the GPU (e.g. on two
+ * streams) race and must be serialised by the caller.  Every output takes
+ * the compensated FP32 sum; with w_stride equal to the list's entry count
+ * the results equal dcpse_apply_batched(..., DCPSE_F32) of a plan
+ * configured with DCPSE_APPLY_COMPENSATE_ALL and direct loading (mode 1)
+ * bit for bit (the lanes per row follow from w_stride / n). */
 #define DCPSE_NOALLOC_MAX_PARTICLES 2097152
 int dcpse_apply_batched_f32_noalloc(int64_t n, int n_outputs, const int64_t* d_rowptr, const int32_t* d_cols,
                                     const float* d_w, int64_t w_stride, const double* d_f, double* d_out,
@@ -286,7 +339,8 @@ int dcpse_apply_batched_f32_noalloc(int64_t n, int n_outputs, const int64_t* d_r
 #define DCPSE_K_ASSEMBLE 2
 #define DCPSE_K_APPLY_TERM 3
 #define DCPSE_K_NEIGHBORS 4
-#define DCPSE_K_COUNT 5
+#define DCPSE_K_CORRECT 5 /* the FP64 correction pass of DCPSE_F32_BUDGET */
+#define DCPSE_K_COUNT 6
 int dcpse_plan_set_timing(dcpse_plan_t* plan, int enable);
 /* Measured FP64 fused multiply-add throughput of the current GPU in TFLOP/s
  * (2 flops per FMA): the ceiling the FP64 assembly is reported against.

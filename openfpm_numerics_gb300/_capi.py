@@ -47,6 +47,10 @@ SIGNATURES = {
     "dcpse_apply_output_f64": (_I, [_P, _I, _P, _P]),
     "dcpse_apply_batched": (_I, [_P, _P, _P, _I]),
     "dcpse_apply_batched_host": (_I, [_P, _P, _P, _I]),
+    "dcpse_plan_set_error_budget": (_I, [_P, _D]),
+    "dcpse_plan_budget_stats": (_I, [_P, _PI64, _I]),
+    "dcpse_plan_set_reorder": (_I, [_P, _I]),
+    "dcpse_plan_reorder_info": (_I, [_P, _PI, _c.POINTER(_D), _c.POINTER(_D)]),
     "dcpse_apply_batched_f32_noalloc": (_I, [_I64, _I, _P, _P, _P, _I64, _P, _P, _P]),
     "dcpse_p2p_f64": (_I, [_P, _I, _P, _I, _P]),
     "dcpse_p2p": (_I, [_P, _P, _I, _P, _I]),
@@ -69,7 +73,7 @@ SIGNATURES = {
     "dcpse_plan_reset_timing": (_I, [_P]),
 }
 
-K_APPLY_BATCHED, K_SPLIT, K_ASSEMBLE, K_APPLY_TERM, K_NEIGHBORS = range(5)
+K_APPLY_BATCHED, K_SPLIT, K_ASSEMBLE, K_APPLY_TERM, K_NEIGHBORS, K_CORRECT = range(6)
 
 OK = 0
 ERR_ARG = 1
@@ -86,10 +90,12 @@ STORE_OUT_F32 = 4
 ASSEMBLE_FAST = 8
 ASSEMBLE_ASYNC = 16
 STORE_OUT_F32_RESID = 32
+STORE_OUT_F32_CORR = 64
 
 F64 = 0
 F32 = 1
 F32_RESID = 2
+F32_BUDGET = 3
 
 PART_OK, PART_TOO_FEW, PART_BAD_EPS, PART_SINGULAR, PART_NONFINITE = range(5)
 

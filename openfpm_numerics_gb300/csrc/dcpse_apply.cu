@@ -601,6 +601,27 @@ cudaError_t p2p_f64(int64_t n, const int64_t* rowptr, const int32_t* cols, const
     return cudaGetLastError();
 }
 
+// Loads the split kernel and every direct FP32 kernel apply_batched_f32 may
+// launch (4-deep batches, no residuals, 4..32 lanes, 1..8 outputs) onto the
+// current device.  Under lazy module loading a kernel's code is placed on
+// the GPU at its first launch; cudaFuncGetAttributes does that up front.
+cudaError_t preload_apply_f32_direct() {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, split_kernel);
+#define DCPSE_PRELOAD_NO(GG, NO) \
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, apply_f32_kernel<GG, NO, false, 4>);
+#define DCPSE_PRELOAD_G(GG)                                                                     \
+    DCPSE_PRELOAD_NO(GG, 1) DCPSE_PRELOAD_NO(GG, 2) DCPSE_PRELOAD_NO(GG, 3) DCPSE_PRELOAD_NO(GG, 4) \
+    DCPSE_PRELOAD_NO(GG, 5) DCPSE_PRELOAD_NO(GG, 6) DCPSE_PRELOAD_NO(GG, 7) DCPSE_PRELOAD_NO(GG, 8)
+    DCPSE_PRELOAD_G(4)
+    DCPSE_PRELOAD_G(8)
+    DCPSE_PRELOAD_G(16)
+    DCPSE_PRELOAD_G(32)
+#undef DCPSE_PRELOAD_G
+#undef DCPSE_PRELOAD_NO
+    return e;
+}
+
 int64_t f32_rows_per_wave(int64_t n, int64_t nnz, int lanes) {
     const int G = lanes ? lanes : lanes_for_f32(n, nnz);
     return (int64_t)num_sms() * 8 * (256 / G);

@@ -456,6 +456,7 @@ __global__ void __launch_bounds__(256) weights_kernel(AsmArgs a, Split S, int64_
                 if (a.r16)
                     reinterpret_cast<__nv_bfloat16*>(a.r16)[(int64_t)t * a.nnz + beg + q] =
                         __float2bfloat16_rn((float)(w - (double)w32));
+                if (a.r32) a.r32[(int64_t)t * a.nnz + beg + q] = (float)(w - (double)w32);
             }
         }
         nonfinite = __any_sync(0xffffffffu, nonfinite);
@@ -470,6 +471,7 @@ __global__ void __launch_bounds__(256) weights_kernel(AsmArgs a, Split S, int64_
                     if (a.w32) a.w32[(int64_t)t * a.nnz + beg + q] = 0.0f;
                     if (a.r16)
                         reinterpret_cast<__nv_bfloat16*>(a.r16)[(int64_t)t * a.nnz + beg + q] = __float2bfloat16_rn(0.0f);
+                    if (a.r32) a.r32[(int64_t)t * a.nnz + beg + q] = 0.0f;
                 }
             }
         }

@@ -263,6 +263,16 @@ struct dcpse_plan_s {
     double* w64 = nullptr;
     float* w32 = nullptr;
     void* r16 = nullptr;  // bf16 residuals of w32
+    float* r32 = nullptr;  // FP32 residuals w64 - w32 (budget-driven correction)
+    // budget-driven FP32 apply: relative error budget per output, the FP32
+    // kernel's bounds [nout][n], the call's largest |output| per output and
+    // the (row, output) pairs corrected since the last reset
+    double budget = 1e-6;
+    float* bnd = nullptr;
+    uint2* blist = nullptr;  // rows to correct (scratch)
+    int64_t bnd_len = 0;
+    unsigned* maxabs = nullptr;  // [kMaxOutputs] largest |output|, then the list length
+    unsigned long long* budget_count = nullptr;
     unsigned long long* summary = nullptr;  // [count, first]
     int* d_err = nullptr;                   // set by kernels whose bounded wait ran out
     int apply_lanes = 0, apply_mode = 0;
@@ -315,7 +325,18 @@ struct dcpse_plan_s {
     double* hout = nullptr;  // device outputs for host apply, nout * hf_len values
     int64_t hf_len = 0;      // particles hf and hout were sized for (the list may change n)
 
-    // the FP32 output weights on the sliced ELL layout (built on first use)
+    // cell order of the particles from the neighbour build (one set only):
+    // cell_order[k] = the particle in position k
+    int32_t* cell_order = nullptr;
+    int reorder = 0;  // -1: keep the list's numbering, 0: automatic, 1: cell order
+    // the FP32 output weights on the sliced ELL layout (built on first use);
+    // with sell_perm the layout is in cell order (sell_perm = cell_order,
+    // sell_inv its inverse)
+    const int32_t* sell_perm = nullptr;
+    int32_t* sell_inv = nullptr;
+    double* fperm = nullptr;  // the FP64 field at positions (FP64 applies on a renumbered layout)
+    int64_t fperm_len = 0;
+    unsigned long long loc_sum[2] = {0, 0};  // locality of the list / cell numbering (sum |q - p|)
     int32_t* sell_row = nullptr;
     int64_t* sell_off = nullptr;
     int32_t* sell_cols = nullptr;
@@ -325,6 +346,10 @@ struct dcpse_plan_s {
     int64_t sell_total = 0;
     bool sell_no_room = false;  // the copy did not fit in device memory: CSR kernels only
     void free_sell() {
+        sell_perm = nullptr;
+        dfree(sell_inv);
+        dfree(fperm);
+        fperm_len = 0;
         dfree(sell_row);
         dfree(sell_off);
         dfree(sell_cols);
@@ -345,6 +370,10 @@ struct dcpse_plan_s {
         dfree(w32);
         if (r16) cudaFree(r16);
         r16 = nullptr;
+        dfree(r32);
+        dfree(bnd);
+        dfree(blist);
+        bnd_len = 0;
         dfree(rowsum);
         rowsum_prec = -1;
         dfree(wT32);
@@ -358,12 +387,15 @@ struct dcpse_plan_s {
         free_transpose();
         dfree(rowptr);
         dfree(cols);
+        dfree(cell_order);
         dfree(f2);
         dfree(hf);
         dfree(hout);
         hf_len = 0;
         dfree(summary);
         dfree(d_err);
+        dfree(maxabs);
+        dfree(budget_count);
         dfree(asm_scratch);
         asm_scratch_bytes = 0;
         dfree(rk_pack);
@@ -577,8 +609,9 @@ int check_single_set(dcpse_plan_t* P) {
     return DCPSE_OK;
 }
 
-// FP32 split of n field values (stride apart) into the plan's scratch
-int split_into_plan(dcpse_plan_t* P, const double* d_f, int64_t n, int64_t stride) {
+// FP32 split of n field values (stride apart) into the plan's scratch; with
+// inv (stride 1) value i goes to position inv[i] (a renumbered layout)
+int split_into_plan(dcpse_plan_t* P, const double* d_f, int64_t n, int64_t stride, const int32_t* inv = nullptr) {
     if (P->f2_len < n) {
         dfree(P->f2);
         P->f2_len = 0;
@@ -586,7 +619,7 @@ int split_into_plan(dcpse_plan_t* P, const double* d_f, int64_t n, int64_t strid
         P->f2_len = n;
     }
     P->tstart(DCPSE_K_SPLIT);
-    cudaError_t e = split_f64(d_f, n, P->f2, P->stream, stride);
+    cudaError_t e = inv ? split_f64_perm(d_f, n, inv, P->f2, P->stream) : split_f64(d_f, n, P->f2, P->stream, stride);
     P->tstop(DCPSE_K_SPLIT);
     DCPSE_CK(e);
     return DCPSE_OK;
@@ -653,6 +686,7 @@ int surface_finish(dcpse_plan_s* P, int flags) {
     // the plan now holds the accumulated operator over the base particles
     P->free_transpose();
     P->free_sell();
+    dfree(P->cell_order);
     dfree(P->rowptr);
     P->list_version++;
     dfree(P->cols);
@@ -661,6 +695,7 @@ int surface_finish(dcpse_plan_s* P, int flags) {
     dfree(P->w32);
     if (P->r16) cudaFree(P->r16);
     P->r16 = nullptr;
+    dfree(P->r32);
     P->rowptr = rp2;
     P->cols = cols2;
     P->k_term = k2;
@@ -688,7 +723,8 @@ int surface_finish(dcpse_plan_s* P, int flags) {
             DCPSE_CK(cudaMalloc(&P->r16, ((size_t)P->nout * nnz2 + kPad) * 2));
             DCPSE_CK(cudaMemsetAsync(P->r16, 0, ((size_t)P->nout * nnz2 + kPad) * 2, s));
         }
-        DCPSE_CK(narrow_weights(P->w64, (int64_t)P->nout * nnz2, P->w32, P->r16, s));
+        if (flags & DCPSE_STORE_OUT_F32_CORR) DCPSE_CK(dalloc(&P->r32, (size_t)P->nout * nnz2 + kPad));
+        DCPSE_CK(narrow_weights(P->w64, (int64_t)P->nout * nnz2, P->w32, P->r16, s, P->r32));
         if (!(flags & DCPSE_STORE_OUT_F64)) dfree(P->w64);
     }
     return DCPSE_OK;
@@ -858,6 +894,7 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     P->free_assembly();
     P->free_transpose();
     dfree(P->rowptr);
+    dfree(P->cell_order);
     P->list_version++;
     dfree(P->cols);
     P->n = n;
@@ -1030,6 +1067,12 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     if (e == cudaSuccess) e = fill_neighbors(a, P->rowptr, tmp, P->cols, hk, s);
     P->tstop(DCPSE_K_NEIGHBORS);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && !other_support) {
+        // the cell order of the particles (one set): the apply's sliced
+        // layout may renumber rows and columns by it
+        P->cell_order = cidx;
+        cidx = nullptr;
+    }
     cleanup();
     if (e != cudaSuccess) return fail(DCPSE_ERR_CUDA, std::string("neighbour build: ") + cudaGetErrorString(e));
     P->nnz = nnz;
@@ -1046,6 +1089,7 @@ int dcpse_set_neighbors(dcpse_plan_t* P, int64_t n, int64_t nnz, const int64_t* 
     P->free_assembly();
     P->free_transpose();
     dfree(P->rowptr);
+    dfree(P->cell_order);
     P->list_version++;
     dfree(P->cols);
     P->n = n;
@@ -1108,7 +1152,7 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
         return fail(DCPSE_ERR_ARG, "nothing to store");
     if ((flags & DCPSE_ASSEMBLE_FAST) && (flags & DCPSE_STORE_TERMS_F64))
         return fail(DCPSE_ERR_ARG, "per-term kernels need the reference (non-fast) assembly");
-    if ((flags & DCPSE_STORE_OUT_F32_RESID) && !(flags & DCPSE_STORE_OUT_F32))
+    if ((flags & (DCPSE_STORE_OUT_F32_RESID | DCPSE_STORE_OUT_F32_CORR)) && !(flags & DCPSE_STORE_OUT_F32))
         return fail(DCPSE_ERR_ARG, "residuals need DCPSE_STORE_OUT_F32");
     if (P->surface() && !P->surf_pending)
         return fail(DCPSE_ERR_STATE, "surface operators assemble once per neighbour build (build it again)");
@@ -1116,7 +1160,7 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     const int user_flags = flags;
     if (P->surface()) {
         if (flags & DCPSE_STORE_OUT_F32) flags |= DCPSE_STORE_OUT_F64;
-        flags &= ~(DCPSE_STORE_OUT_F32 | DCPSE_STORE_OUT_F32_RESID);
+        flags &= ~(DCPSE_STORE_OUT_F32 | DCPSE_STORE_OUT_F32_RESID | DCPSE_STORE_OUT_F32_CORR);
     }
     cudaStream_t s = P->stream;
     const int64_t n = P->n, nnz = P->nnz;
@@ -1138,6 +1182,8 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
         cudaFree(P->r16);
         P->r16 = nullptr;
     }
+    if ((flags & DCPSE_STORE_OUT_F32_CORR) && !P->r32) DCPSE_CK(dalloc(&P->r32, (size_t)P->nout * nnz + kPad));
+    if (!(flags & DCPSE_STORE_OUT_F32_CORR)) dfree(P->r32);
     AsmArgs a{};
     a.tab = P->dtab;
     a.dim = P->dim;
@@ -1157,6 +1203,7 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     a.w64 = P->w64;
     a.w32 = P->w32;
     a.r16 = P->r16;
+    a.r32 = P->r32;
     a.nnz = nnz;
     a.warps = P->asm_warps;
     a.qr_lanes = P->asm_qr_lanes;
@@ -1445,7 +1492,7 @@ int dcpse_rk4_gs_stage(dcpse_plan_t* P, int stage, int precision, const void* Yu
         const int mode = P->apply_mode & 15;
         if (mode == 0 || mode == 4) {
             if (int rc = ensure_sell(P)) return rc;
-            if (P->sell_w) {
+            if (P->sell_w && !P->sell_perm) {  // the stage kernels read fields in list order
                 a.srow = P->sell_row;
                 a.soff = P->sell_off;
                 a.scols = P->sell_cols;
@@ -1585,11 +1632,33 @@ int ensure_sell_layout(dcpse_plan_t* P) {
     const int64_t ns = sell_slices(P->n);
     int32_t* slen = nullptr;
     int64_t* tmp = nullptr;
-    cudaError_t e = dalloc(&P->sell_row, (size_t)ns * 32);
+    cudaError_t e = cudaSuccess;
+    // Renumbering: with the particles' cell order (one set, from the
+    // neighbour build) the layout takes it when the list's own numbering
+    // scatters the field reads at least twice as far (sum over the entries
+    // of |q - p| against |inv[q] - inv[p]|), or when asked to
+    P->sell_perm = nullptr;
+    P->loc_sum[0] = P->loc_sum[1] = 0;
+    if (P->cell_order && !P->two_set() && !P->surface() && P->reorder >= 0) {
+        unsigned long long* sums = nullptr;
+        e = dalloc(&P->sell_inv, (size_t)P->n);
+        if (e == cudaSuccess) e = invert_perm(P->cell_order, P->n, P->sell_inv, P->stream);
+        if (e == cudaSuccess) e = dalloc(&sums, 2);
+        if (e == cudaSuccess) e = sell_locality(P->rowptr, P->cols, P->n, P->sell_inv, sums, P->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(P->loc_sum, sums, sizeof P->loc_sum, cudaMemcpyDeviceToHost, P->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+        dfree(sums);
+        if (e == cudaSuccess && (P->reorder > 0 || 2 * P->loc_sum[1] < P->loc_sum[0]))
+            P->sell_perm = P->cell_order;
+        else
+            dfree(P->sell_inv);
+    }
+    if (e == cudaSuccess) e = dalloc(&P->sell_row, (size_t)ns * 32);
     if (e == cudaSuccess) e = dalloc(&P->sell_off, (size_t)ns + 1);
     if (e == cudaSuccess) e = dalloc(&slen, (size_t)ns);
     if (e == cudaSuccess) e = dalloc(&tmp, (size_t)scan_tmp_elems(ns));
-    if (e == cudaSuccess) e = sell_order(P->rowptr, P->n, P->sell_row, slen, P->sell_off, tmp, P->stream);
+    if (e == cudaSuccess) e = sell_order(P->rowptr, P->n, P->sell_row, slen, P->sell_off, tmp, P->stream, P->sell_perm);
     int64_t total = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&total, P->sell_off + ns, sizeof total, cudaMemcpyDeviceToHost, P->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
@@ -1598,7 +1667,8 @@ int ensure_sell_layout(dcpse_plan_t* P) {
     if (e == cudaSuccess) e = dalloc(&P->sell_cols, (size_t)total + kPad);
     if (e == cudaSuccess)
         e = sell_fill(P->rowptr, P->cols, nullptr, nullptr, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
-                      P->sell_row, P->sell_off, total, P->sell_cols, nullptr, nullptr, P->stream);
+                      P->sell_row, P->sell_off, total, P->sell_cols, nullptr, nullptr, P->stream, P->sell_perm,
+                      P->sell_perm ? P->sell_inv : nullptr);
     if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
     if (e == cudaErrorMemoryAllocation) {
         // the layout does not fit: the CSR kernels serve
@@ -1640,7 +1710,8 @@ int ensure_sell(dcpse_plan_t* P) {
         P, "sliced ELL weights: ", [&] { return dalloc(&P->sell_w, (size_t)P->nout * P->sell_total + kPad); },
         [&] {
             return sell_fill(P->rowptr, P->cols, P->w32, nullptr, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
-                             P->sell_row, P->sell_off, P->sell_total, nullptr, P->sell_w, nullptr, P->stream);
+                             P->sell_row, P->sell_off, P->sell_total, nullptr, P->sell_w, nullptr, P->stream,
+                             P->sell_perm);
         },
         [&] { dfree(P->sell_w); });
 }
@@ -1656,7 +1727,7 @@ int ensure_sell64(dcpse_plan_t* P) {
         [&] { return dalloc(&P->sell_w64, (size_t)P->nout * P->sell_total + kPad); },
         [&] {
             return sell_fill64(P->rowptr, P->w64, P->nnz, P->nout, P->n, P->sell_row, P->sell_off, P->sell_total,
-                               P->sell_w64, P->stream);
+                               P->sell_w64, P->stream, P->sell_perm);
         },
         [&] { dfree(P->sell_w64); });
 }
@@ -1670,7 +1741,8 @@ int ensure_sell_resid(dcpse_plan_t* P) {
         [&] { return cudaMalloc(&P->sell_r, ((size_t)P->nout * P->sell_total + kPad) * 2); },
         [&] {
             return sell_fill(P->rowptr, P->cols, nullptr, P->r16, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
-                             P->sell_row, P->sell_off, P->sell_total, nullptr, nullptr, P->sell_r, P->stream);
+                             P->sell_row, P->sell_off, P->sell_total, nullptr, nullptr, P->sell_r, P->stream,
+                             P->sell_perm);
         },
         [&] {
             if (P->sell_r) cudaFree(P->sell_r);
@@ -1681,7 +1753,7 @@ int ensure_sell_resid(dcpse_plan_t* P) {
 // The FP32 batched apply of rows [r0, r1) (0, 0: all rows) from the plan's
 // split field into d_out ([n_outputs][n]).
 int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, int64_t r1,
-                   cudaStream_t on = nullptr) {
+                   cudaStream_t on = nullptr, bool comp_all = false, bool csr_only = false) {
     cudaStream_t st = on ? on : P->stream;
     ApplyF32 ap{};
     ap.n = P->n;
@@ -1709,20 +1781,24 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
         if (ord >= 2) ap.comp |= 1u << P->term_output[t];
     }
     // the residual correction only pays off with compensated sums
-    if ((P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) || precision == DCPSE_F32_RESID) ap.comp = 0xffffffffu;
+    if ((P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) || precision == DCPSE_F32_RESID || comp_all)
+        ap.comp = 0xffffffffu;
     // sliced ELL layout: rows in whole windows of 256
     // (the automatic schedule: 15 % faster than the CSR kernels at 128^3)
     const int64_t rr0 = r0, rr1 = r1 ? r1 : P->n;
     const int mode = P->apply_mode & 15;
     const bool resid = precision == DCPSE_F32_RESID;
-    if ((mode == 0 || mode == 4) && rr0 % 256 == 0 && (rr1 % 256 == 0 || rr1 == P->n)) {
+    if (!csr_only && (mode == 0 || mode == 4) && rr0 % 256 == 0 && (rr1 % 256 == 0 || rr1 == P->n)) {
         if (int rc = ensure_sell(P)) return rc;
         if (resid)
             if (int rc = ensure_sell_resid(P)) return rc;
     }
-    if ((mode == 0 || mode == 4) && P->sell_w && (!resid || P->sell_r) && rr0 % 256 == 0 &&
-        (rr1 % 256 == 0 || rr1 == P->n)) {
+    // (a renumbered layout serves whole-list applies only: the split field
+    // is then at positions)
+    if (!csr_only && (mode == 0 || mode == 4) && P->sell_w && (!resid || P->sell_r) && rr0 % 256 == 0 &&
+        (rr1 % 256 == 0 || rr1 == P->n) && (!P->sell_perm || (rr0 == 0 && rr1 == P->n))) {
         SellArgs sa{};
+        sa.perm = P->sell_perm;
         sa.n = P->n;
         sa.nslices = sell_slices(P->n);
         sa.srow = P->sell_row;
@@ -1762,6 +1838,118 @@ int check_f32_weights(dcpse_plan_t* P, int precision) {
     if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
     if (precision == DCPSE_F32_RESID && !P->r16)
         return fail(DCPSE_ERR_STATE, "FP32 residuals not stored (DCPSE_STORE_OUT_F32_RESID)");
+    if (precision == DCPSE_F32_BUDGET && !P->r32)
+        return fail(DCPSE_ERR_STATE, "FP32 residuals for the correction not stored (DCPSE_STORE_OUT_F32_CORR)");
+    return DCPSE_OK;
+}
+
+// Whether a whole-list FP32 apply of this precision runs the sliced kernel
+// (its layout and streams are built on first use).
+int sell_ready(dcpse_plan_t* P, int precision, bool* ready) {
+    *ready = false;
+    const int mode = P->apply_mode & 15;
+    if (mode != 0 && mode != 4) return DCPSE_OK;
+    if (int rc = ensure_sell(P)) return rc;
+    const bool resid = precision == DCPSE_F32_RESID || (precision == DCPSE_F32_BUDGET && P->r16);
+    if (resid)
+        if (int rc = ensure_sell_resid(P)) return rc;
+    *ready = P->sell_w && (!resid || P->sell_r);
+    return DCPSE_OK;
+}
+
+// The split of a whole-list FP32 apply's field, at positions when the sliced
+// kernel will run on a renumbered layout.
+int split_for_apply(dcpse_plan_t* P, const double* d_f, int precision) {
+    bool ready = false;
+    if (int rc = sell_ready(P, precision, &ready)) return rc;
+    return split_into_plan(P, d_f, P->n, 1, (ready && P->sell_perm) ? P->sell_inv : nullptr);
+}
+
+// The budget-driven FP32 apply of every row from the plan's split field into
+// d_out ([n_outputs][n]): the sliced FP32 kernel with its weight-rounding
+// bounds, then the FP64 residual correction of the rows whose bound exceeds
+// the budget (every row when the sliced layout is not available).  When the
+// plan also holds the bf16 residual streams (DCPSE_STORE_OUT_F32_RESID) the
+// first pass adds them: its bound is 2^8 times smaller, so far fewer rows
+// need the second pass (worth it where many rows would, e.g. second
+// derivatives on strongly graded clouds).
+int apply_budget(dcpse_plan_t* P, double* d_out) {
+    cudaStream_t st = P->stream;
+    const int64_t n = P->n;
+    if (n == 0) return DCPSE_OK;
+    if (!P->maxabs) DCPSE_CK(dalloc(&P->maxabs, kMaxOutputs + 1));
+    if (P->bnd_len < (int64_t)P->nout * n) {
+        dfree(P->bnd);
+        dfree(P->blist);
+        P->bnd_len = 0;
+        DCPSE_CK(dalloc(&P->bnd, (size_t)P->nout * n));
+        DCPSE_CK(dalloc(&P->blist, (size_t)n));
+        P->bnd_len = (int64_t)P->nout * n;
+    }
+    // the largest |output| per output and the list length start at zero
+    DCPSE_CK(cudaMemsetAsync(P->maxabs, 0, sizeof(unsigned) * (kMaxOutputs + 1), st));
+    if (!P->budget_count) {
+        DCPSE_CK(dalloc(&P->budget_count, 1));
+        DCPSE_CK(cudaMemsetAsync(P->budget_count, 0, sizeof(unsigned long long), st));
+    }
+    bool bounded = false, with_r16 = false, ready = false;
+    if (int rc = sell_ready(P, DCPSE_F32_BUDGET, &ready)) return rc;
+    {
+        if (ready) {
+            with_r16 = P->r16 != nullptr;
+            SellArgs sa{};
+            sa.perm = P->sell_perm;
+            sa.n = n;
+            sa.nslices = sell_slices(n);
+            sa.srow = P->sell_row;
+            sa.off = P->sell_off;
+            sa.cols = P->sell_cols;
+            sa.w = P->sell_w;
+            sa.r = with_r16 ? static_cast<const __nv_bfloat16*>(P->sell_r) : nullptr;
+            sa.total = P->sell_total;
+            sa.f2 = P->f2;
+            sa.out = d_out;
+            sa.oos = n;
+            sa.ors = 1;
+            sa.w0 = 0;
+            sa.w1 = (n + 255) / 256;
+            sa.comp = 0xffffffffu;
+            sa.no_self = 0;
+            sa.bnd = P->bnd;
+            sa.maxabs = P->maxabs;
+            P->tstart(DCPSE_K_APPLY_BATCHED, st);
+            cudaError_t e = apply_sell(sa, P->nout, st);
+            P->tstop(DCPSE_K_APPLY_BATCHED, st);
+            DCPSE_CK(e);
+            bounded = true;
+        }
+    }
+    if (!bounded)
+        if (int rc = apply_f32_rows(P, DCPSE_F32, d_out, 0, 0, nullptr, true, true)) return rc;
+    BudgetArgs b{};
+    b.n = n;
+    b.rowptr = P->rowptr;
+    b.cols = P->cols;
+    b.r32 = P->r32;
+    b.r16 = with_r16 ? P->r16 : nullptr;
+    b.ws = P->nnz;
+    b.f2 = P->f2;
+    b.out = d_out;
+    b.oos = n;
+    b.ors = 1;
+    b.bnd = P->bnd;
+    b.maxabs = P->maxabs;
+    b.budget = P->budget;
+    b.bound_scale = with_r16 ? 0x1p-32 : 0x1p-24;
+    b.flag_all = bounded ? 0 : 1;
+    b.count = P->budget_count;
+    b.list = P->blist;
+    b.list_len = P->maxabs + kMaxOutputs;
+    b.inv = bounded ? (P->sell_perm ? P->sell_inv : nullptr) : nullptr;
+    P->tstart(DCPSE_K_CORRECT, st);
+    cudaError_t e = budget_correct(b, P->nout, st);
+    P->tstop(DCPSE_K_CORRECT, st);
+    DCPSE_CK(e);
     return DCPSE_OK;
 }
 
@@ -1774,15 +1962,30 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
     if (P->n > 0 && (!d_f || !d_out)) return fail(DCPSE_ERR_ARG, "NULL field");
     if (precision == DCPSE_F32 || precision == DCPSE_F32_RESID) {
         if (int rc = check_f32_weights(P, precision)) return rc;
-        if (int rc = split_into_plan(P, d_f, P->n, 1)) return rc;
+        if (int rc = split_for_apply(P, d_f, precision)) return rc;
         return apply_f32_rows(P, precision, d_out, 0, 0);
+    } else if (precision == DCPSE_F32_BUDGET) {
+        if (int rc = check_f32_weights(P, precision)) return rc;
+        if (int rc = split_for_apply(P, d_f, precision)) return rc;
+        return apply_budget(P, d_out);
     } else if (precision == DCPSE_F64) {
         if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
         const int mode = P->apply_mode & 15;
         if (mode == 0 || mode == 4) {
             if (int rc = ensure_sell64(P)) return rc;
+            if (P->sell_w64 && P->sell_perm && P->n > 0) {
+                // a renumbered layout reads the field at positions
+                if (P->fperm_len < P->n) {
+                    dfree(P->fperm);
+                    P->fperm_len = 0;
+                    DCPSE_CK(dalloc(&P->fperm, (size_t)P->n));
+                    P->fperm_len = P->n;
+                }
+                DCPSE_CK(permute_f64(d_f, P->n, P->sell_inv, P->fperm, P->stream));
+            }
             if (P->sell_w64) {
                 Sell64Args sa{};
+                sa.perm = P->sell_perm;
                 sa.n = P->n;
                 sa.nwin = (P->n + 255) / 256;
                 sa.srow = P->sell_row;
@@ -1790,7 +1993,7 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
                 sa.cols = P->sell_cols;
                 sa.w = P->sell_w64;
                 sa.total = P->sell_total;
-                sa.f = d_f;
+                sa.f = P->sell_perm ? P->fperm : d_f;
                 sa.fs = 1;
                 sa.out = d_out;
                 sa.oos = P->n;
@@ -1807,12 +2010,65 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
         P->tstop(DCPSE_K_APPLY_BATCHED);
         DCPSE_CK(e);
     } else {
-        return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
+        return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32, DCPSE_F32_RESID, DCPSE_F32_BUDGET or DCPSE_F64");
     }
     return DCPSE_OK;
 }
 
+int dcpse_plan_set_error_budget(dcpse_plan_t* P, double rel) {
+    if (int rc = check_plan(P)) return rc;
+    if (!(rel > 0.0) || !(rel < 1.0)) return fail(DCPSE_ERR_ARG, "the error budget must lie in (0, 1)");
+    P->budget = rel;
+    return DCPSE_OK;
+}
+
+int dcpse_plan_set_reorder(dcpse_plan_t* P, int policy) {
+    if (int rc = check_plan(P)) return rc;
+    if (policy < -1 || policy > 1) return fail(DCPSE_ERR_ARG, "policy must be -1, 0 or 1");
+    if (policy != P->reorder) {
+        P->reorder = policy;
+        // the sliced layouts are rebuilt on next use
+        const bool had = P->sell_w != nullptr;
+        P->free_sell();
+        if (had && P->assembled)
+            if (int rc = ensure_sell(P)) return rc;
+    }
+    return DCPSE_OK;
+}
+
+int dcpse_plan_reorder_info(dcpse_plan_t* P, int* renumbered, double* mean_dist_list, double* mean_dist_cells) {
+    if (int rc = check_plan(P)) return rc;
+    if (renumbered) *renumbered = P->sell_perm ? 1 : 0;
+    const double m = P->nnz > 0 ? (double)P->nnz : 1.0;
+    if (mean_dist_list) *mean_dist_list = (double)P->loc_sum[0] / m;
+    if (mean_dist_cells) *mean_dist_cells = (double)P->loc_sum[1] / m;
+    return DCPSE_OK;
+}
+
+int dcpse_plan_budget_stats(dcpse_plan_t* P, int64_t* pairs_corrected, int reset) {
+    if (int rc = check_plan(P)) return rc;
+    if (!pairs_corrected) return fail(DCPSE_ERR_ARG, "NULL output");
+    unsigned long long h = 0;
+    if (P->budget_count) {
+        DCPSE_CK(cudaMemcpyAsync(&h, P->budget_count, sizeof h, cudaMemcpyDeviceToHost, P->stream));
+        DCPSE_CK(cudaStreamSynchronize(P->stream));
+        if (reset) DCPSE_CK(cudaMemsetAsync(P->budget_count, 0, sizeof h, P->stream));
+    }
+    *pairs_corrected = (int64_t)h;
+    return DCPSE_OK;
+}
+
 namespace {
+// Device address of a pinned host buffer with a device mapping (cudaHostAlloc
+// / cudaHostRegister), or null for pageable memory.
+double* mapped_host(const void* h) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, h) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+        return static_cast<double*>(at.devicePointer);
+    cudaGetLastError();  // an unregistered pointer is not an error here
+    return nullptr;
+}
+
 // streams and events of the pipelined host-buffer apply (created once)
 int ensure_host_pipeline(dcpse_plan_t* P) {
     if (P->copy_stream) return DCPSE_OK;
@@ -1880,6 +2136,19 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
         P->hf_len = P->n;
     }
     const bool f32 = precision == DCPSE_F32 || precision == DCPSE_F32_RESID;
+    if (precision == DCPSE_F32_BUDGET && P->n > 0) {
+        // pinned field and outputs: the split reads the field in place, the
+        // FP32 kernel and the correction write the outputs in place
+        double* om = mapped_host(h_out);
+        const double* fm = om ? mapped_host(h_f) : nullptr;
+        if (om && fm) {
+            if (int rc = check_f32_weights(P, precision)) return rc;
+            if (int rc = split_for_apply(P, fm, precision)) return rc;
+            if (int rc = apply_budget(P, om)) return rc;
+            DCPSE_CK(cudaStreamSynchronize(P->stream));
+            return DCPSE_OK;
+        }
+    }
     if (!f32 || (P->apply_mode & 15) == 2 || P->n < kHostChunkMinRows) {
         DCPSE_CK(cudaMemcpyAsync(P->hf, h_f, sizeof(double) * P->n, cudaMemcpyHostToDevice, P->stream));
         int rc = dcpse_apply_batched(P, P->hf, P->hout, precision);
@@ -1921,7 +2190,7 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
         // one apply of all rows stores the outputs (128^3: 0.68 ms; splitting
         // the field in two pieces, the second beside the apply of the first
         // rows, took 0.71-0.74 ms for any first-row share from 1/32 to 1/4)
-        DCPSE_CK(split_f64(f_mapped, n, P->f2, P->stream));
+        if (int rc = split_for_apply(P, f_mapped, precision)) return rc;
         if (int rc = apply_f32_rows(P, precision, out_mapped, 0, 0)) return rc;
         // the direct kernels report no device errors: a synchronisation of
         // the plan's stream puts the outputs in place
@@ -2059,7 +2328,7 @@ int dcpse_p2p(dcpse_plan_t* P, const double* d_f_support, int ncomp, double* d_o
             const int mode = P->apply_mode & 15;
             if ((mode == 0 || mode == 4) && nf > 0) {
                 if (int rc = ensure_sell(P)) return rc;
-                if (P->sell_w) {
+                if (P->sell_w && !P->sell_perm) {  // fields in list order
                     SellArgs sa{};
                     sa.n = P->n;
                     sa.nslices = sell_slices(P->n);
@@ -2094,7 +2363,7 @@ int dcpse_p2p(dcpse_plan_t* P, const double* d_f_support, int ncomp, double* d_o
             const int mode = P->apply_mode & 15;
             if ((mode == 0 || mode == 4) && nf > 0) {
                 if (int rc = ensure_sell64(P)) return rc;
-                if (P->sell_w64) {
+                if (P->sell_w64 && !P->sell_perm) {  // fields in list order
                     Sell64Args sa{};
                     sa.n = P->n;
                     sa.nwin = (P->n + 255) / 256;

@@ -130,6 +130,7 @@ struct AsmArgs {
     double* w64;         // [noutputs][nnz] (summed, eps folded) or nullptr
     float* w32;          // [noutputs][nnz] or nullptr
     void* r16;           // bf16 [noutputs][nnz]: w64 - w32, or nullptr
+    float* r32;          // FP32 [noutputs][nnz]: w64 - w32, or nullptr
     int64_t nnz;
     const int32_t* order; // processing order of the particles (k-binned) or nullptr
     int warps;            // warps per CTA of the Gram and weight kernels (2, 4 or 8)
@@ -168,9 +169,18 @@ cudaError_t p2p_f64(int64_t n, const int64_t* rowptr, const int32_t* cols, const
 cudaError_t apply_batched_f32(int64_t n, int nout, const int64_t* rowptr, const int32_t* cols, const float* w,
                               int64_t nnz, const float2* f2, double* out, cudaStream_t s);
 
+// Loads the kernels apply_batched_f32 and split_f64 launch onto the current
+// device (cudaFuncGetAttributes), so that a later call loads no code.
+cudaError_t preload_apply_f32_direct();
+
 // Batched FP32 apply on the sliced ELL layout (SELL-32, rows sorted by length
-// within windows of 256): windows [w0, w1) of rows, thread per row.
+// within windows of 256): windows [w0, w1) of rows, thread per row.  The
+// layout may renumber the rows and columns (perm[position] = list row,
+// inv[list row] = position, e.g. a cell order of the particles): its columns
+// are then positions, the field pair is read at positions, and outputs go to
+// list rows.
 struct SellArgs {
+    const int32_t* perm;   // position -> list row, or null (identity)
     int64_t n;             // rows
     int64_t nslices;
     const int32_t* srow;   // row of (slice, lane), -1 past the last row
@@ -185,24 +195,40 @@ struct SellArgs {
     int64_t w0, w1;        // windows of 256 rows
     uint32_t comp;
     int no_self;
+    // optional: weight-rounding bound of every output of every row,
+    // bnd[o * n + r] = sum_q |w_o,pq| |f_q - f_p|, and the call's largest
+    // |output| per output as float bits (atomic max; zero it before the call)
+    float* bnd;
+    unsigned* maxabs;
 };
 int64_t sell_slices(int64_t n);
 // srow [sell_slices(n) * 32], slen32 [sell_slices(n)], off [sell_slices(n) + 1],
-// scan_tmp [scan_tmp_elems(sell_slices(n))]
+// scan_tmp [scan_tmp_elems(sell_slices(n))]; rows are positions (list row
+// perm[position], or the position itself without perm)
 cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t* slen32, int64_t* off,
-                       int64_t* scan_tmp, cudaStream_t s);
+                       int64_t* scan_tmp, cudaStream_t s, const int32_t* perm = nullptr);
+// d_sums[0] = sum over entries |q - p|, d_sums[1] = sum |inv[q] - inv[p]|
+cudaError_t sell_locality(const int64_t* rowptr, const int32_t* cols, int64_t n, const int32_t* inv,
+                          unsigned long long* d_sums, cudaStream_t s);
+cudaError_t invert_perm(const int32_t* perm, int64_t n, int32_t* inv, cudaStream_t s);
+// f2[inv[i]] = (hi, lo) of f[i];  g[inv[i]] = f[i]
+cudaError_t split_f64_perm(const double* f, int64_t n, const int32_t* inv, float2* f2, cudaStream_t s);
+cudaError_t permute_f64(const double* f, int64_t n, const int32_t* inv, double* g, cudaStream_t s);
 // Copies into the sliced layout the columns (scols given), the FP32 weights
 // (w / sw given) and the bf16 residual streams (r16 / sr16 given); the
 // streams asked for must be consecutive in that order.  one_set: the columns
 // index the rows' own set.
 cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, const void* r16, int64_t ws,
                       int nout, int64_t n, int one_set, const int32_t* srow, const int64_t* off, int64_t total,
-                      int32_t* scols, float* sw, void* sr16, cudaStream_t s);
+                      int32_t* scols, float* sw, void* sr16, cudaStream_t s, const int32_t* perm = nullptr,
+                      const int32_t* inv = nullptr);
 cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s);
 // FP64 summed weights on the same slices ([nout][total]) and their apply
 cudaError_t sell_fill64(const int64_t* rowptr, const double* w, int64_t ws, int nout, int64_t n,
-                        const int32_t* srow, const int64_t* off, int64_t total, double* sw, cudaStream_t s);
+                        const int32_t* srow, const int64_t* off, int64_t total, double* sw, cudaStream_t s,
+                        const int32_t* perm = nullptr);
 struct Sell64Args {
+    const int32_t* perm;    // position -> list row, or null (the field f is then at positions)
     int64_t n, nwin;
     const int32_t* srow;
     const int64_t* off;
@@ -216,6 +242,30 @@ struct Sell64Args {
     int no_self;
 };
 cudaError_t apply_sell64(const Sell64Args& a, int nout, cudaStream_t s);
+
+// FP64 residual correction of a batched FP32 apply where its weight-rounding
+// bound exceeds the error budget (see dcpse_budget.cu).
+struct BudgetArgs {
+    int64_t n;
+    const int64_t* rowptr;
+    const int32_t* cols;
+    const float* r32;          // [nout][ws] FP32 residuals w64 - w32
+    const void* r16;           // [nout][ws] bf16 residuals the FP32 apply already added, or null
+    int64_t ws;
+    const float2* f2;          // the field's float pair (what the FP32 apply read)
+    double* out;               // output o of row r at out[o * oos + r * ors]
+    int64_t oos, ors;
+    const float* bnd;          // [nout][n] bounds of the FP32 apply (unused with flag_all)
+    const unsigned* maxabs;    // [nout] largest |output| (float bits)
+    double budget;             // relative error budget per output
+    double bound_scale;        // error of the FP32 apply <= bound_scale * bnd (2^-24, 2^-32 with r16)
+    int flag_all;              // correct every row
+    unsigned long long* count; // (row, output) pairs corrected, accumulated, or null
+    uint2* list;               // [n] scratch: flagged rows (row, output mask)
+    unsigned* list_len;        // its length (zero it before the call)
+    const int32_t* inv;        // field pair of list row i at f2[inv[i]], or null (at i)
+};
+cudaError_t budget_correct(const BudgetArgs& a, int nout, cudaStream_t s);
 
 // Full description of a batched FP32 apply (plan-owned, padded arrays).
 struct ApplyF32 {
@@ -285,8 +335,10 @@ struct SurfAcc {
     double* out[kMaxStreams];
 };
 cudaError_t surface_fill(const SurfAcc& a, cudaStream_t s);
-// w32 = (float)w64 and the bf16 residual w64 - w32 (r16 may be null)
-cudaError_t narrow_weights(const double* w64, int64_t m, float* w32, void* r16, cudaStream_t s);
+// w32 = (float)w64 and the bf16 and FP32 residuals w64 - w32 (r16 and r32
+// may be null)
+cudaError_t narrow_weights(const double* w64, int64_t m, float* w32, void* r16, cudaStream_t s,
+                           float* r32 = nullptr);
 
 // --------------------------------------------------------------- adjoint --
 // transposed list: trow[n+1], per entry the source row tsrc and entry index tidx

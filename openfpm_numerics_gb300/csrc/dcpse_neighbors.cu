@@ -21,6 +21,7 @@
 // FP64 predicate itself, as are particles outside the grid, NaN positions
 // and periodic axes with fewer than three cells.  The lists are the same bit
 // for bit.
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 
@@ -692,13 +693,21 @@ int grid_for(int64_t items, int per_block) {
 
 }  // namespace
 
+// SM count of the current device, cached per device (a process may drive
+// GPUs with different SM counts).
 int num_sms() {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
+    constexpr int kDevs = 64;
+    static std::atomic<int> cache[kDevs];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+    std::atomic<int>* slot = dev < kDevs ? &cache[dev] : nullptr;
+    int sms = slot ? slot->load(std::memory_order_relaxed) : 0;
+    if (sms > 0) return sms;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        sms = 1;
+    } else if (slot) {
+        slot->store(sms, std::memory_order_relaxed);
     }
     return sms;
 }

@@ -26,15 +26,17 @@ constexpr int kSlice = 32;           // rows per slice (one warp)
 constexpr int kSlicesPerWin = kWin / kSlice;
 
 // window w: rank its rows by length (longest first, ties in row order),
-// record the row of every (slice, lane) and each slice's length x 32
+// record the row of every (slice, lane) and each slice's length x 32.  Rows
+// are positions: position r holds list row perm[r] (r without perm).
 __global__ void __launch_bounds__(kWin) sell_order_kernel(const int64_t* __restrict__ rowptr, int64_t n,
-                                                          int64_t nwin, int32_t* __restrict__ srow,
-                                                          int32_t* __restrict__ slen32) {
+                                                          int64_t nwin, const int32_t* __restrict__ perm,
+                                                          int32_t* __restrict__ srow, int32_t* __restrict__ slen32) {
     __shared__ int s_len[kWin];
     for (int64_t w = blockIdx.x; w < nwin; w += gridDim.x) {
         const int t = threadIdx.x;
         const int64_t r = w * kWin + t;
-        const int len = r < n ? (int)(rowptr[r + 1] - rowptr[r]) : -1;
+        const int64_t lr = (r < n && perm) ? (int64_t)perm[r] : r;
+        const int len = r < n ? (int)(rowptr[lr + 1] - rowptr[lr]) : -1;
         s_len[t] = len;
         __syncthreads();
         int rank = 0;
@@ -72,18 +74,21 @@ __global__ void __launch_bounds__(256) sell_fill_kernel(const int64_t* __restric
                                                         const int64_t* __restrict__ off, int64_t total, int one_set,
                                                         int32_t* __restrict__ scols, float* __restrict__ sw,
                                                         const uint16_t* __restrict__ r16, uint16_t* __restrict__ sr16,
-                                                        int st_begin, int st_end) {
+                                                        int st_begin, int st_end, const int32_t* __restrict__ perm,
+                                                        const int32_t* __restrict__ inv) {
     __shared__ uint32_t tiles[8][32 * 33];
     const int lane = threadIdx.x & 31;
     uint32_t* tile = tiles[threadIdx.x >> 5];
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t s = warp0; s < nslices; s += nwarps) {
-        const int32_t myrow = srow[s * kSlice + lane];
+        const int32_t myrow = srow[s * kSlice + lane];  // position
+        const int32_t lrow = (myrow >= 0 && perm) ? perm[myrow] : myrow;
         const int64_t b = off[s];
         const int L = (int)((off[s + 1] - b) / kSlice);
-        const int64_t myrb = myrow >= 0 ? rowptr[myrow] : 0;
-        const int myk = myrow >= 0 ? (int)(rowptr[myrow + 1] - myrb) : 0;
+        const int64_t myrb = lrow >= 0 ? rowptr[lrow] : 0;
+        const int myk = lrow >= 0 ? (int)(rowptr[lrow + 1] - myrb) : 0;
+        // one set: the position itself; two sets are never permuted
         const uint32_t mypad = (uint32_t)pad_column(one_set, myrow, myk, cols, myrb);
         for (int st = st_begin; st < st_end; ++st) {
             for (int j0 = 0; j0 < L; j0 += 32) {
@@ -92,7 +97,7 @@ __global__ void __launch_bounds__(256) sell_fill_kernel(const int64_t* __restric
                     const int k = __shfl_sync(0xffffffffu, myk, r);
                     const int j = j0 + lane;
                     if (j < k)
-                        tile[lane * 33 + r] = st < 0      ? (uint32_t)cols[rb + j]
+                        tile[lane * 33 + r] = st < 0      ? (uint32_t)(inv ? inv[cols[rb + j]] : cols[rb + j])
                                               : st < nout ? __float_as_uint(w[(int64_t)st * ws + rb + j])
                                                           : (uint32_t)r16[(int64_t)(st - nout) * ws + rb + j];
                 }
@@ -122,7 +127,7 @@ __global__ void __launch_bounds__(256) sell_fill64_kernel(const int64_t* __restr
                                                           const double* __restrict__ w, int64_t ws, int nout,
                                                           int64_t nslices, const int32_t* __restrict__ srow,
                                                           const int64_t* __restrict__ off, int64_t total,
-                                                          double* __restrict__ sw) {
+                                                          double* __restrict__ sw, const int32_t* __restrict__ perm) {
     __shared__ double tiles[8][16 * 33];
     const int lane = threadIdx.x & 31;
     double* tile = tiles[threadIdx.x >> 5];
@@ -130,10 +135,11 @@ __global__ void __launch_bounds__(256) sell_fill64_kernel(const int64_t* __restr
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t s = warp0; s < nslices; s += nwarps) {
         const int32_t myrow = srow[s * kSlice + lane];
+        const int32_t lrow = (myrow >= 0 && perm) ? perm[myrow] : myrow;
         const int64_t b = off[s];
         const int L = (int)((off[s + 1] - b) / kSlice);
-        const int64_t myrb = myrow >= 0 ? rowptr[myrow] : 0;
-        const int myk = myrow >= 0 ? (int)(rowptr[myrow + 1] - myrb) : 0;
+        const int64_t myrb = lrow >= 0 ? rowptr[lrow] : 0;
+        const int myk = lrow >= 0 ? (int)(rowptr[lrow + 1] - myrb) : 0;
         for (int o = 0; o < nout; ++o) {
             for (int j0 = 0; j0 < L; j0 += 16) {
                 // lanes 0-15 read entries of row r, lanes 16-31 of row r + 1
@@ -202,21 +208,29 @@ __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
         __syncthreads();
         const int64_t r = win * kWin + threadIdx.x;
         if (r < a.n) {
+            const int64_t lr = a.perm ? (int64_t)a.perm[r] : r;
 #pragma unroll
-            for (int o = 0; o < NO; ++o) a.out[(int64_t)o * a.oos + r * a.ors] = tile[o][threadIdx.x];
+            for (int o = 0; o < NO; ++o) a.out[(int64_t)o * a.oos + lr * a.ors] = tile[o][threadIdx.x];
         }
         __syncthreads();
     }
 }
 
 // thread per row; block = one window of 8 slices (five blocks per SM fit the
-// registers without spills up to four outputs, four up to six, three above)
-template <int NO, int U, bool RESID>
-__global__ void __launch_bounds__(256, (NO <= 4 && !RESID ? 5 : (NO <= 6 ? 4 : 3))) apply_sell_kernel(SellArgs a) {
+// registers without spills up to four outputs, four up to six, three above).
+// BOUND: also the weight-rounding bound of every output of every row,
+// B_o = sum_q |w_o,pq| |f_q - f_p| (FP32), stored to bnd[o * n + r], and the
+// largest |output| of the call per output, atomically maxed into maxabs[o]
+// (float bits; the values are >= 0, so unsigned order is float order).
+template <int NO, int U, bool RESID, bool BOUND = false>
+__global__ void __launch_bounds__(256, (NO <= 4 && !RESID && !BOUND ? 5 : (NO <= 6 ? 4 : 3)))
+    apply_sell_kernel(SellArgs a) {
     // the window's outputs, staged so that they leave in row order (rows of a
     // slice are permuted; scattered 8-byte stores are slow, above all into
     // host memory over NVLink-C2C)
     __shared__ double tile[NO][kWin];
+    __shared__ float btile[BOUND ? NO : 1][BOUND ? kWin : 1];
+    __shared__ unsigned wmax[BOUND ? NO : 1][BOUND ? kSlicesPerWin : 1];
     const int lane = threadIdx.x & 31;
     for (int64_t win = a.w0 + blockIdx.x; win < a.w1; win += gridDim.x) {
         const int64_t s = win * kSlicesPerWin + (threadIdx.x >> 5);  // < nslices: windows hold 8 slices
@@ -226,6 +240,9 @@ __global__ void __launch_bounds__(256, (NO <= 4 && !RESID ? 5 : (NO <= 6 ? 4 : 3
         const float2 fp = (row >= 0 && !a.no_self) ? a.f2[row] : make_float2(0.f, 0.f);
         RowAcc<NO, RESID> acc;
         acc.init();
+        float bs[NO];
+#pragma unroll
+        for (int o = 0; o < NO; ++o) bs[o] = 0.0f;
         const int32_t* __restrict__ c = a.cols + b + lane;
         const float* __restrict__ w = a.w + b + lane;
         const __nv_bfloat16* __restrict__ rr = RESID ? a.r + b + lane : nullptr;
@@ -250,31 +267,149 @@ __global__ void __launch_bounds__(256, (NO <= 4 && !RESID ? 5 : (NO <= 6 ? 4 : 3
             for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? a.f2[q[u]] : fp;
 #pragma unroll
             for (int u = 0; u < U; ++u) acc.add(wv[u], rv[u], fq[u], fp, a.comp);
+            if (BOUND) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const float df = fabsf(fq[u].x - fp.x);
+#pragma unroll
+                    for (int o = 0; o < NO; ++o) bs[o] = fmaf(fabsf(wv[u][o]), df, bs[o]);
+                }
+            }
         }
         if (row >= 0) {
 #pragma unroll
-            for (int o = 0; o < NO; ++o) tile[o][row - win * kWin] = acc.value(o);
+            for (int o = 0; o < NO; ++o) {
+                tile[o][row - win * kWin] = acc.value(o);
+                if (BOUND) btile[o][row - win * kWin] = bs[o];
+            }
+        }
+        if (BOUND) {
+            // largest |output| of the window: warp maxima, then one thread
+            // per output updates the call's maximum (skipped when the stored
+            // maximum is already larger)
+#pragma unroll
+            for (int o = 0; o < NO; ++o) {
+                const unsigned v = row >= 0 ? __float_as_uint(fabsf((float)acc.value(o))) : 0u;
+                const unsigned m = __reduce_max_sync(0xffffffffu, v);
+                if (lane == 0) wmax[o][threadIdx.x >> 5] = m;
+            }
         }
         __syncthreads();
         const int64_t r = win * kWin + threadIdx.x;
         if (r < a.n) {
+            // position r holds list row perm[r]: outputs and bounds go to it
+            const int64_t lr = a.perm ? (int64_t)a.perm[r] : r;
 #pragma unroll
-            for (int o = 0; o < NO; ++o) a.out[(int64_t)o * a.oos + r * a.ors] = tile[o][threadIdx.x];
+            for (int o = 0; o < NO; ++o) {
+                a.out[(int64_t)o * a.oos + lr * a.ors] = tile[o][threadIdx.x];
+                if (BOUND) a.bnd[(int64_t)o * a.n + lr] = btile[o][threadIdx.x];
+            }
+        }
+        if (BOUND && threadIdx.x < NO) {
+            const int o = threadIdx.x;
+            unsigned m = wmax[o][0];
+#pragma unroll
+            for (int i = 1; i < kSlicesPerWin; ++i) m = max(m, wmax[o][i]);
+            if (m > __ldcg(&a.maxabs[o])) atomicMax(&a.maxabs[o], m);
         }
         __syncthreads();  // the next window rewrites the tile
     }
 }
 
+// Sums over all entries (p, q) of |q - p| (the list's own numbering) and of
+// |inv[q] - inv[p]| (the cell order's): one warp per row, one atomic pair
+// per warp.
+__global__ void __launch_bounds__(256) locality_kernel(const int64_t* __restrict__ rowptr,
+                                                       const int32_t* __restrict__ cols, int64_t n,
+                                                       const int32_t* __restrict__ inv,
+                                                       unsigned long long* __restrict__ sums) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long a0 = 0, a1 = 0;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < n; p += nw) {
+        const int64_t ip = inv[p];
+        for (int64_t j = rowptr[p] + lane; j < rowptr[p + 1]; j += 32) {
+            const int64_t q = cols[j];
+            a0 += (unsigned long long)(q > p ? q - p : p - q);
+            const int64_t iq = inv[q];
+            a1 += (unsigned long long)(iq > ip ? iq - ip : ip - iq);
+        }
+    }
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, m);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, m);
+    }
+    if (lane == 0) {
+        atomicAdd(&sums[0], a0);
+        atomicAdd(&sums[1], a1);
+    }
+}
+
+// (hi, lo) float pair of f[i] stored at position inv[i]
+__global__ void split_perm_kernel(const double* __restrict__ f, int64_t n, const int32_t* __restrict__ inv,
+                                  float2* __restrict__ f2) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = f[i];
+        const float hi = (float)v;
+        f2[inv[i]] = make_float2(hi, (float)(v - (double)hi));
+    }
+}
+
+// f[i] stored at position inv[i] (FP64)
+__global__ void permute_f64_kernel(const double* __restrict__ f, int64_t n, const int32_t* __restrict__ inv,
+                                   double* __restrict__ g) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        g[inv[i]] = f[i];
+}
+
+__global__ void invert_kernel(const int32_t* __restrict__ perm, int64_t n, int32_t* __restrict__ inv) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        inv[perm[i]] = (int32_t)i;
+}
+
+int grid_for(int64_t n) {
+    const int64_t g = (n + 255) / 256;
+    const int64_t cap = (int64_t)num_sms() * 8;
+    return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+
 }  // namespace
+
+cudaError_t sell_locality(const int64_t* rowptr, const int32_t* cols, int64_t n, const int32_t* inv,
+                          unsigned long long* d_sums, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(d_sums, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess || n == 0) return e;
+    locality_kernel<<<grid_for(n * 32), 256, 0, s>>>(rowptr, cols, n, inv, d_sums);
+    return cudaGetLastError();
+}
+
+cudaError_t invert_perm(const int32_t* perm, int64_t n, int32_t* inv, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    invert_kernel<<<grid_for(n), 256, 0, s>>>(perm, n, inv);
+    return cudaGetLastError();
+}
+
+cudaError_t split_f64_perm(const double* f, int64_t n, const int32_t* inv, float2* f2, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    split_perm_kernel<<<grid_for(n), 256, 0, s>>>(f, n, inv, f2);
+    return cudaGetLastError();
+}
+
+cudaError_t permute_f64(const double* f, int64_t n, const int32_t* inv, double* g, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    permute_f64_kernel<<<grid_for(n), 256, 0, s>>>(f, n, inv, g);
+    return cudaGetLastError();
+}
 
 int64_t sell_slices(int64_t n) { return ((n + kWin - 1) / kWin) * kSlicesPerWin; }
 
 cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t* slen32, int64_t* off,
-                       int64_t* scan_tmp, cudaStream_t s) {
+                       int64_t* scan_tmp, cudaStream_t s, const int32_t* perm) {
     const int64_t nwin = (n + kWin - 1) / kWin;
     if (nwin == 0) return cudaSuccess;
     const int grid = (int)std::min<int64_t>(nwin, (int64_t)num_sms() * 8);
-    sell_order_kernel<<<grid, kWin, 0, s>>>(rowptr, n, nwin, srow, slen32);
+    sell_order_kernel<<<grid, kWin, 0, s>>>(rowptr, n, nwin, perm, srow, slen32);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return exclusive_scan_i32(slen32, nwin * kSlicesPerWin, off, scan_tmp, s);
@@ -282,7 +417,8 @@ cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t*
 
 cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w, const void* r16, int64_t ws,
                       int nout, int64_t n, int one_set, const int32_t* srow, const int64_t* off, int64_t total,
-                      int32_t* scols, float* sw, void* sr16, cudaStream_t s) {
+                      int32_t* scols, float* sw, void* sr16, cudaStream_t s, const int32_t* perm,
+                      const int32_t* inv) {
     const int64_t ns = sell_slices(n);
     if (ns == 0) return cudaSuccess;
     // the columns when scols is given, the weights when sw is, the residual
@@ -293,16 +429,17 @@ cudaError_t sell_fill(const int64_t* rowptr, const int32_t* cols, const float* w
     const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 6);
     sell_fill_kernel<<<grid, 256, 0, s>>>(rowptr, cols, w, ws, nout, ns, srow, off, total, one_set, scols, sw,
                                           static_cast<const uint16_t*>(r16), static_cast<uint16_t*>(sr16), st_begin,
-                                          st_end);
+                                          st_end, perm, inv);
     return cudaGetLastError();
 }
 
 cudaError_t sell_fill64(const int64_t* rowptr, const double* w, int64_t ws, int nout, int64_t n,
-                        const int32_t* srow, const int64_t* off, int64_t total, double* sw, cudaStream_t s) {
+                        const int32_t* srow, const int64_t* off, int64_t total, double* sw, cudaStream_t s,
+                        const int32_t* perm) {
     const int64_t ns = sell_slices(n);
     if (ns == 0) return cudaSuccess;
     const int grid = (int)std::min<int64_t>((ns + 7) / 8, (int64_t)num_sms() * 6);
-    sell_fill64_kernel<<<grid, 256, 0, s>>>(rowptr, w, ws, nout, ns, srow, off, total, sw);
+    sell_fill64_kernel<<<grid, 256, 0, s>>>(rowptr, w, ws, nout, ns, srow, off, total, sw, perm);
     return cudaGetLastError();
 }
 
@@ -338,8 +475,14 @@ cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s) {
     switch (nout) {
 #define DCPSE_SELL_CASE(NO)                                                                      \
     case NO:                                                                                     \
-        if (a.r)                                                                                 \
+        if (a.r && a.bnd)                                                                        \
+            apply_sell_kernel<NO, (NO == 1 ? 8 : (NO <= 2 ? 4 : 2)), true, true>                \
+                <<<(unsigned)grid, 256, 0, s>>>(a);                                              \
+        else if (a.r)                                                                            \
             apply_sell_kernel<NO, (NO == 1 ? 8 : (NO <= 2 ? 4 : 2)), true>                      \
+                <<<(unsigned)grid, 256, 0, s>>>(a);                                              \
+        else if (a.bnd)                                                                          \
+            apply_sell_kernel<NO, (NO == 1 ? 8 : 4), false, true>                               \
                 <<<(unsigned)grid, 256, 0, s>>>(a);                                              \
         else                                                                                     \
             apply_sell_kernel<NO, (NO == 1 ? 8 : 4), false><<<(unsigned)grid, 256, 0, s>>>(a);   \

@@ -82,12 +82,14 @@ __global__ void acc_fill_kernel(SurfAcc a) {
     }
 }
 
-__global__ void narrow_kernel(const double* __restrict__ w64, int64_t m, float* __restrict__ w32, void* r16) {
+__global__ void narrow_kernel(const double* __restrict__ w64, int64_t m, float* __restrict__ w32, void* r16,
+                              float* __restrict__ r32) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         const double w = w64[i];
         const float f = (float)w;
         w32[i] = f;
         if (r16) reinterpret_cast<__nv_bfloat16*>(r16)[i] = __float2bfloat16_rn((float)(w - (double)f));
+        if (r32) r32[i] = (float)(w - (double)f);
     }
 }
 
@@ -121,9 +123,9 @@ cudaError_t surface_fill(const SurfAcc& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t narrow_weights(const double* w64, int64_t m, float* w32, void* r16, cudaStream_t s) {
+cudaError_t narrow_weights(const double* w64, int64_t m, float* w32, void* r16, cudaStream_t s, float* r32) {
     if (m == 0) return cudaSuccess;
-    narrow_kernel<<<grid_of(m), 256, 0, s>>>(w64, m, w32, r16);
+    narrow_kernel<<<grid_of(m), 256, 0, s>>>(w64, m, w32, r16, r32);
     return cudaGetLastError();
 }
 

@@ -268,6 +268,31 @@ class DcpsePlan:
                out_host.ctypes.data_as(ctypes.c_void_p), int(precision))
         return out_host
 
+    def set_error_budget(self, budget=1e-6):
+        """Relative error budget per output of the F32_BUDGET applies (the
+        FP32 result against the FP64 summed weights, normwise)."""
+        C.call("dcpse_plan_set_error_budget", self._h, float(budget))
+
+    def budget_stats(self, reset=False):
+        """(row, output) pairs the F32_BUDGET applies corrected in FP64 since
+        the last reset."""
+        n = ctypes.c_int64()
+        C.call("dcpse_plan_budget_stats", self._h, ctypes.byref(n), int(bool(reset)))
+        return n.value
+
+    def set_reorder(self, policy=0):
+        """Numbering of the apply's sliced layout: 0 automatic (cell order
+        when the caller's numbering scatters the field reads), 1 always the
+        cell order, -1 never."""
+        C.call("dcpse_plan_set_reorder", self._h, int(policy))
+
+    def reorder_info(self):
+        """(renumbered, mean |q - p| in the caller's numbering, the same in
+        the cell order)."""
+        r, a, b = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        C.call("dcpse_plan_reorder_info", self._h, ctypes.byref(r), ctypes.byref(a), ctypes.byref(b))
+        return bool(r.value), a.value, b.value
+
     # -- particle to particle interpolation -----------------------------
     def _check_support_field(self, f):
         if f.dtype != torch.float64 or f.dim() not in (1, 2):
