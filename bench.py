@@ -34,6 +34,12 @@ sys.path.insert(0, ROOT)
 METRIC = "DC-PSE apply Gparticle-ops/s & assembly Mparticles/s: FP32-batched vs FP64 @≤1e-6"
 UNIT = "Gparticle-ops/s"
 NOUT = 4
+# one protocol for every CPU timing (the cpu_baseline leg and the reference
+# arm): the first CPU_SAMPLE particles' rows with their full neighbourhoods,
+# CPU_WARM untimed and CPU_STEPS timed applies on all host cores
+CPU_SAMPLE = 32768
+CPU_STEPS = 20
+CPU_WARM = 3
 
 
 def parse():
@@ -43,8 +49,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--nside", type=int, default=128)
-    ap.add_argument("--cpu-sample", type=int, default=32768, help="particles in the CPU sample")
+    ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE, help="particles in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the graded-cloud, adjoint, Gray-Scott and shuffled-order sections")
     ap.add_argument("--only", choices=["apply", "apply64", "assemble", "gray-scott", "graded", "interp"], default=None,
                     help="small-footprint run of one kernel family (for profiler captures)")
     ap.add_argument("--lanes", type=int, default=0)
@@ -137,20 +145,24 @@ def rel_err(a, b):
 
 
 # ----------------------------------------------------------------- CPU leg --
+SIGS6 = [(1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (0, 2, 0), (0, 0, 2)]
+
+
 def cpu_oracle_run(pos, rcut, f, sample, steps, warmup, nthreads):
     """The reference algorithm restated on the CPU (oracle/): the S first
     particles' rows (full neighbourhoods), 6 reference Dcpse objects
     (Dx, Dy, Dz, Dxx, Dyy, Dzz), each assembled with the dense E of the
-    reference; a step applies the 4 outputs (Laplacian = sum of 3)."""
+    reference; a step applies the 4 outputs (Laplacian = sum of 3).  Also
+    returns the lists, kernels and outputs, against which the GPU's rows are
+    checked."""
     import oracle
 
     S = min(sample, pos.shape[0])
     rp, cols = oracle.neighbors(pos[:S], rcut, support=pos)
-    sigs = [(1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (0, 2, 0), (0, 0, 2)]
     t0 = time.perf_counter()
-    terms = [oracle.assemble(pos[:S], rp, cols, s, 2, support=pos, nthreads=nthreads) for s in sigs]
+    terms = [oracle.assemble(pos[:S], rp, cols, s, 2, support=pos, nthreads=nthreads) for s in SIGS6]
     t_asm = time.perf_counter() - t0
-    multi = oracle.MultiApply(rp, cols, [(t[2], t[1], sum(s)) for t, s in zip(terms, sigs)],
+    multi = oracle.MultiApply(rp, cols, [(t[2], t[1], sum(s)) for t, s in zip(terms, SIGS6)],
                               [0, 1, 2, 3, 3, 3], NOUT, f, f_dom=f[:S])
 
     def step():
@@ -163,7 +175,13 @@ def cpu_oracle_run(pos, rcut, f, sample, steps, warmup, nthreads):
         step()
     t_apply = (time.perf_counter() - t0) / max(steps, 1)
     return dict(S=S, nnz=int(rp[-1]), t_asm=t_asm, t_apply=t_apply,
-                apply_value=S * NOUT / t_apply / 1e9, asm_value=S / t_asm / 1e6)
+                apply_value=S * NOUT / t_apply / 1e9, asm_value=S / t_asm / 1e6,
+                rp=rp, cols=cols, kernels=[t[2] for t in terms], out=multi.out.copy())
+
+
+def cpu_sample_text(r, n, steps):
+    return ("first %d of %d particles (full neighbourhoods, %d entries), 6 reference Dcpse objects, "
+            "%d timed applies after %d untimed" % (r["S"], n, r["nnz"], steps, CPU_WARM))
 
 
 def host_cores():
@@ -180,11 +198,9 @@ def run_reference(args):
     pos = cfg["pos"]
     f, _, _ = W.field2(pos)
     cores = host_cores()
-    steps = max(1, min(args.steps, 20))
-    warm = max(1, min(args.warmup, 3))
+    steps, warm = CPU_STEPS, CPU_WARM
     r = cpu_oracle_run(pos, cfg["rcut"], f, args.cpu_sample, steps, warm, cores)
-    sample = ("first %d of %d particles (full neighbourhoods, %d entries); %d timed steps"
-              % (r["S"], pos.shape[0], r["nnz"], steps))
+    sample = cpu_sample_text(r, pos.shape[0], steps)
     line = {
         "impl": "reference", "metric": METRIC, "value": r["apply_value"], "unit": UNIT, "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": r["t_apply"] * 1e3, "higher_is_better": True,
@@ -246,6 +262,12 @@ def run_ours(args):
     plan.assemble(pos, C.STORE_TERMS_F64 | C.STORE_OUT_F64)
     t_asm_ref = plan.timing(C.K_ASSEMBLE)[0] / 1e3
     nbad, first_bad, code = plan.particle_status()
+    # the rows the CPU oracle recomputes: their lists and per-term kernels
+    S = min(args.cpu_sample, N)
+    g_rp, g_cols = plan.neighbors()
+    g_rp = g_rp[: S + 1].cpu().numpy()
+    g_cols = g_cols[: int(g_rp[-1])].cpu().numpy()
+    g_kernels = [plan.term_kernels(t)[0][: int(g_rp[-1])].cpu().numpy() for t in range(6)]
 
     # plain FP64 GPU path: the reference's apply, one pass per Dcpse object
     out64 = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
@@ -281,8 +303,10 @@ def run_ours(args):
 
     # fast assembly (summed right-hand sides) -> FP32 weights for the headline
     plan.reset_timing()
-    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID)
+    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
     t_asm_fast = plan.timing(C.K_ASSEMBLE)[0] / 1e3
+    # the same with the residual streams of the corrected FP32 applies
+    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID | C.STORE_OUT_F32_CORR)
 
     # schedule autotuning (untimed): lanes per row x direct / TMA-staged loads
     from openfpm_numerics_gb300 import autotune
@@ -304,6 +328,26 @@ def run_ours(args):
     torch.cuda.synchronize()
     t_resid = ev0.elapsed_time(ev1) / 1e3 / nplain
     resr = outr.cpu().numpy()
+
+    # budget-driven FP32 (rows whose FP32 error bound exceeds 1e-6 corrected
+    # toward the FP64 weights; the bf16 residual streams are stored, so the
+    # first pass adds them); kernel times from the plan's timers
+    outg = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
+    plan.set_error_budget(1e-6)
+    for _ in range(3):
+        plan.apply(f, C.F32_BUDGET, outg)
+    plan.budget_stats(reset=True)
+    plan.reset_timing()
+    ev0.record(stream)
+    for _ in range(nplain):
+        plan.apply(f, C.F32_BUDGET, outg)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_budget = ev0.elapsed_time(ev1) / 1e3 / nplain
+    budget_pairs = plan.budget_stats() / nplain
+    budget_k = plan.timing(C.K_APPLY_BATCHED)[0] / nplain
+    budget_c = plan.timing(C.K_CORRECT)[0] / nplain
+    resg = outg.cpu().numpy()
 
     out = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
     clocks = Clocks(local)
@@ -356,6 +400,7 @@ def run_ours(args):
                                                     np.sqrt(np.mean(ref_out[o] ** 2))) for o in range(NOUT)),
         "fp32_per_output_normwise": [rel_err(res32[o], ref_out[o]) for o in range(NOUT)],
         "fp32_resid_vs_fp64_reference_order_normwise": max(rel_err(resr[o], ref_out[o]) for o in range(NOUT)),
+        "fp32_budget_vs_fp64_reference_order_normwise": max(rel_err(resg[o], ref_out[o]) for o in range(NOUT)),
         "fp64_batched_vs_reference_order_normwise": max(rel_err(b64[o], ref_out[o]) for o in range(NOUT)),
         "fp64_analytic_interior_normwise": [rel_err(ref_out[o][inner], analytic[o][inner]) for o in range(NOUT)],
         "fp32_analytic_interior_normwise": [rel_err(res32[o][inner], analytic[o][inner]) for o in range(NOUT)],
@@ -383,12 +428,26 @@ def run_ours(args):
     value = job_value(world, N, NOUT, t_step)
 
     cpu = None
+    oracle_rows = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        r = cpu_oracle_run(pos_np, cfg["rcut"], f_np, args.cpu_sample, 3, 1, host_cores())
+        r = cpu_oracle_run(pos_np, cfg["rcut"], f_np, args.cpu_sample, CPU_STEPS, CPU_WARM, host_cores())
         cpu = {"value": r["apply_value"], "unit": UNIT, "cores": host_cores(), "kind": "port",
-               "sample": "first %d of %d particles (full neighbourhoods), 6 reference Dcpse objects, "
-                         "3 timed applies" % (r["S"], N),
-               "assembly_mparticles_s": r["asm_value"]}
+               "sample": cpu_sample_text(r, N, CPU_STEPS), "assembly_mparticles_s": r["asm_value"]}
+        # the GPU's rows against the oracle's on the same sample
+        S = r["S"]
+        o_out = r["out"]
+
+        def vs_orc(a):
+            return max(rel_err(a[o][:S], o_out[o]) for o in range(NOUT))
+
+        oracle_rows = {
+            "rows": S, "entries": r["nnz"],
+            "neighbor_lists_equal": bool(np.array_equal(r["rp"], g_rp) and np.array_equal(r["cols"], g_cols)),
+            "term_kernels_bit_exact": bool(all(np.array_equal(a, b) for a, b in zip(r["kernels"], g_kernels))),
+            "fp64_reference_order_bit_exact": bool(np.array_equal(ref_out[:, :S], o_out)),
+            "fp64_batched_normwise": vs_orc(b64), "fp32_normwise": vs_orc(res32),
+            "fp32_resid_normwise": vs_orc(resr), "fp32_budget_normwise": vs_orc(resg),
+            "definition": "max|gpu-oracle| / max|oracle| over the sample rows, max over the 4 outputs"}
 
     if rank == 0:
         line = {
@@ -424,19 +483,269 @@ def run_ours(args):
             "fp64_batched": {"value": N * NOUT / t_b64 / 1e9, "ms_per_step": t_b64 * 1e3},
             "fp32_resid": {"value": N * NOUT / t_resid / 1e9, "ms_per_step": t_resid * 1e3,
                            "note": "FP32 weights + bf16 residual stream (2 B/entry/output)"},
+            "fp32_budget": {"value": N * NOUT / t_budget / 1e9, "ms_per_step": t_budget * 1e3,
+                            "first_pass_kernel_ms": budget_k, "correction_ms": budget_c,
+                            "pairs_corrected_per_call": budget_pairs,
+                            "fraction_corrected": budget_pairs / (N * NOUT), "budget": 1e-6,
+                            "error_vs_fp64_reference_order": errors["fp32_budget_vs_fp64_reference_order_normwise"],
+                            "note": "FP32 + bf16 residual first pass with per-row error bounds, FP64-weight "
+                                    "residual correction of the rows over the budget"},
             "autotune": tuned,
             "speedup_fp32_batched_vs_fp64_plain": t_plain / t_step,
             "errors": errors,
+            "oracle_rows": oracle_rows,
             "cpu_baseline": cpu,
         }
-        print(json.dumps(line), flush=True)
     plan.close()
+    del plan
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and not args.no_extras:
+        line["graded"] = extra_graded(args)
+        line["adjoint"] = extra_adjoint(args, pos_np, cfg["rcut"])
+        line["gray_scott"] = extra_gray_scott(args)
+        line["shuffled"] = extra_shuffled(args, pos_np, cfg["rcut"], f_np, res32)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------- extra workloads --
+def _events_ms(stream, fn, reps, warm=3):
+    """Mean CUDA-event time of fn on stream in ms (warm-up calls first)."""
+    import torch
+
+    for _ in range(warm):
+        fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _pct(a, b, mask=None):
+    """|a - b| / max|b| over the rows in mask: p50, p99, max."""
+    if mask is not None:
+        a, b = a[mask], b[mask]
+    e = np.abs(a - b) / max(float(np.abs(b).max()), 1e-300)
+    return {"p50": float(np.percentile(e, 50)), "p99": float(np.percentile(e, 99)), "max": float(e.max())}
+
+
+def extra_graded(args):
+    """Graded 2D cloud (1,000,000 particles, density growing 4x along x by
+    inverse-CDF sampling, seed 3, per-particle cutoff 3.1 h_p): Dx, Dy, Dxx,
+    Dyy, Dxy assembled in one FP64 pass (bins and CTA sizes autotuned),
+    applied in FP32, budget-driven FP32 and FP64; errors against the FP64
+    apply, the analytic derivatives and the oracle on 2000 sampled rows."""
+    import torch
+
+    import oracle
+    from openfpm_numerics_gb300 import _capi as C
+    from openfpm_numerics_gb300 import autotune
+    from openfpm_numerics_gb300 import workloads as W
+    from openfpm_numerics_gb300.plan import DcpsePlan
+
+    cfg = W.config3()
+    pos_np, rpp_np = cfg["pos"], cfg["rcut_pp"]
+    N = pos_np.shape[0]
+    stream = torch.cuda.current_stream()
+    pos = torch.tensor(pos_np, device="cuda")
+    rpp = torch.tensor(rpp_np, device="cuda")
+    plan = DcpsePlan(2, W.five_ops_2d(), order=2, stream=stream)
+    plan.set_timing(True)
+    plan.build_neighbors(pos, 0.0, rpp)
+    plan.reset_timing()
+    plan.build_neighbors(pos, 0.0, rpp)
+    t_nbr = plan.timing(C.K_NEIGHBORS)[0]
+    rp_t, cols_t = plan.neighbors()
+    k = (rp_t[1:] - rp_t[:-1]).cpu().numpy()
+    nnz = plan.info()["nnz"]
+    flags = C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F64 | C.STORE_OUT_F32_RESID | C.STORE_OUT_F32_CORR
+    tuned = autotune.tune_assembly(plan, pos, flags)
+    plan.assemble(pos, flags)
+    nbad = plan.particle_status()[0]
+    ok = plan.eps()[1].cpu().numpy() == 0
+    x, y = pos_np[:, 0], pos_np[:, 1]
+    f_np = np.sin(2 * np.pi * x) * np.cos(2 * np.pi * y)
+    f = torch.tensor(f_np, device="cuda")
+    out = torch.empty((5, N), dtype=torch.float64, device="cuda")
+    res = {"particles": N, "nnz": nnz, "k_min": int(k.min()), "k_mean": float(k.mean()), "k_max": int(k.max()),
+           "failed_particles": nbad, "neighbors_ms": t_nbr, "assembly_ms": tuned["ms"],
+           "assembly_mparticles_s": N / tuned["ms"] / 1e3,
+           "assembly_schedule": {kk: tuned[kk] for kk in ("bin_width", "warps", "qr_lanes")},
+           "reorder": plan.reorder_info()}
+    t64 = _events_ms(stream, lambda: plan.apply(f, C.F64, out), 20)
+    o64 = out.cpu().numpy()
+    t32 = _events_ms(stream, lambda: plan.apply(f, C.F32, out), 20)
+    o32 = out.cpu().numpy()
+    plan.apply(f, C.F32_BUDGET, out)
+    plan.budget_stats(reset=True)
+    plan.reset_timing()
+    tb = _events_ms(stream, lambda: plan.apply(f, C.F32_BUDGET, out), 20, warm=0)
+    pairs = plan.budget_stats() / 20
+    tbk = plan.timing(C.K_APPLY_BATCHED)[0] / 20
+    tbc = plan.timing(C.K_CORRECT)[0] / 20
+    ob = out.cpu().numpy()
+    tp = 2 * np.pi
+    sx, cx, sy, cy = np.sin(tp * x), np.cos(tp * x), np.sin(tp * y), np.cos(tp * y)
+    exact = [tp * cx * cy, -tp * sx * sy, -tp * tp * sx * cy, -tp * tp * sx * cy, -tp * tp * cx * sy]
+    margin = float(rpp_np.max())
+    inner = (x > margin) & (x < 1 - margin) & (y > margin) & (y < 1 - margin) & ok
+    res["apply_ms"] = {"fp64": t64, "fp32": t32, "fp32_budget": tb, "budget_first_pass_kernel": tbk,
+                       "budget_correction": tbc}
+    res["gparticle_ops_s"] = {"fp64": N * 5 / t64 / 1e6, "fp32": N * 5 / t32 / 1e6, "fp32_budget": N * 5 / tb / 1e6}
+    res["budget"] = {"budget": 1e-6, "pairs_corrected_per_call": pairs, "fraction_corrected": pairs / (N * 5)}
+    res["fp32_vs_fp64"] = [_pct(o32[o], o64[o], ok) for o in range(5)]
+    res["fp32_budget_vs_fp64"] = [_pct(ob[o], o64[o], ok) for o in range(5)]
+    res["fp32_budget_max_normwise"] = max(_pct(ob[o], o64[o], ok)["max"] for o in range(5))
+    res["fp64_vs_analytic_interior"] = [_pct(o64[o], exact[o], inner) for o in range(5)]
+    # the oracle on 2000 sampled rows (lists, per-term reference assembly,
+    # reference-order apply)
+    rows = np.sort(np.random.default_rng(8).choice(N, 2000, replace=False))
+    o_rp, o_cols = oracle.neighbors(pos_np[rows], 0.0, support=pos_np, rcut_pp=rpp_np[rows])
+    g_rp = rp_t.cpu().numpy()
+    g_cols = cols_t.cpu().numpy()
+    same = all(np.array_equal(o_cols[o_rp[i]:o_rp[i + 1]], g_cols[g_rp[r]:g_rp[r + 1]]) for i, r in enumerate(rows))
+    sigs = [s_[0] for s_ in W.five_ops_2d()]
+    terms = [oracle.assemble(pos_np[rows], o_rp, o_cols, sg, 2, support=pos_np, nthreads=host_cores())
+             for sg in sigs]
+    multi = oracle.MultiApply(o_rp, o_cols, [(t[2], t[1], sum(sg)) for t, sg in zip(terms, sigs)],
+                              [0, 1, 2, 3, 4], 5, f_np, f_dom=f_np[rows])
+    o_ref = multi(host_cores())
+    okr = ok[rows] & np.all([t[3] == 0 for t in terms], axis=0)
+    res["oracle_rows"] = {"rows": int(rows.size), "neighbor_lists_equal": bool(same),
+                          "fp64_normwise": max(_pct(o64[o][rows], o_ref[o], okr)["max"] for o in range(5)),
+                          "fp32_normwise": max(_pct(o32[o][rows], o_ref[o], okr)["max"] for o in range(5)),
+                          "fp32_budget_normwise": max(_pct(ob[o][rows], o_ref[o], okr)["max"] for o in range(5)),
+                          "definition": "max|gpu-oracle| / max|oracle| over assembled sample rows, max over "
+                                        "the 5 operators"}
+    hbm, _ = peaks()
+    b32 = W.apply_bytes(N, nnz, 5, 4)
+    res["roofline_fp32"] = {"algorithmic_bytes": b32, "achieved_gbs": b32 / t32 / 1e6, "frac": b32 / t32 / 1e6 / hbm}
+    plan.check()
+    plan.close()
+    return res
+
+
+def extra_adjoint(args, pos2, rcut2):
+    """Adjoint timings: the field VJP (transposed apply) and the position VJP
+    (through every moment-matrix solve) of the Laplacian at 256^2 (jitter
+    0.1h, seed 4, f and g N(0,1)) and of Gradient + Laplacian at 128^3,
+    against the oracle's reference adjoint on all host cores (all rows at
+    256^2, the first 16384 rows at 128^3); FD and oracle parity are
+    tests/test_gpu_adjoint.py's."""
+    import torch
+
+    import oracle
+    from openfpm_numerics_gb300 import _capi as C
+    from openfpm_numerics_gb300 import workloads as W
+    from openfpm_numerics_gb300.plan import DcpsePlan
+
+    stream = torch.cuda.current_stream()
+    res = {"host_cores": host_cores()}
+    cases = [("lap_256sq", W.config4(), [[(2, 0), (0, 2)]], None),
+             ("grad_lap_128cube", {"pos": pos2, "rcut": rcut2}, W.grad_lap_outputs(3), 16384)]
+    for name, cfg, outputs, host_rows in cases:
+        pos_np = cfg["pos"]
+        n, dim = pos_np.shape
+        rng = np.random.default_rng(4)
+        if "f" in cfg:
+            f_np, g_np = cfg["f"], cfg["g"][None, :]
+        else:
+            f_np = rng.standard_normal(n)
+            g_np = rng.standard_normal((len(outputs), n))
+        pos = torch.tensor(pos_np, device="cuda")
+        plan = DcpsePlan(dim, outputs, order=2, stream=stream)
+        plan.build_neighbors(pos, cfg["rcut"])
+        plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+        f = torch.tensor(f_np, device="cuda")
+        g = torch.tensor(g_np, device="cuda")
+        gout = torch.empty(n, dtype=torch.float64, device="cuda")
+        r = {"particles": n, "nnz": plan.info()["nnz"]}
+        r["vjp_field_fp64_ms"] = _events_ms(stream, lambda: plan.vjp_field(g, C.F64, gout), 10)
+        r["vjp_field_fp32_ms"] = _events_ms(stream, lambda: plan.vjp_field(g, C.F32, gout), 10)
+        r["vjp_positions_ms"] = _events_ms(stream, lambda: plan.vjp_positions(pos, f, g), 3, warm=1)
+        grad = plan.vjp_positions(pos, f, g).cpu().numpy()
+        rp, cols = (x.cpu().numpy() for x in plan.neighbors())
+        rows = (0, n if host_rows is None else min(host_rows, n))
+        t0 = time.perf_counter()
+        ref = oracle.vjp_positions(pos_np, rp, cols, outputs, f_np, g_np, rows=rows, nthreads=host_cores())
+        t_host = (time.perf_counter() - t0) * 1e3
+        r["host_rows"] = rows[1] - rows[0]
+        r["host_vjp_positions_ms"] = t_host
+        r["vjp_positions_vs_host"] = (t_host / r["host_rows"]) / (r["vjp_positions_ms"] / n)
+        if host_rows is None:
+            r["vjp_positions_vs_oracle_normwise"] = float(np.abs(grad - ref).max() / np.abs(ref).max())
+        plan.check()
+        plan.close()
+        del plan
+        torch.cuda.empty_cache()
+        res[name] = r
+    res["definition"] = ("vjp_positions_vs_host: host ms per row / GPU ms per row (host: the oracle's reference "
+                         "adjoint, same lists, all host cores)")
+    return res
+
+
+def extra_shuffled(args, pos_np, rcut, f_np, res32):
+    """The benchmark set in a seeded random particle order (seed 11): the
+    apply's sliced layout is renumbered by the particles' cell order, so the
+    field gathers stay local whatever the caller's order; outputs come back
+    in the caller's order."""
+    import torch
+
+    from openfpm_numerics_gb300 import _capi as C
+    from openfpm_numerics_gb300 import workloads as W
+    from openfpm_numerics_gb300.plan import DcpsePlan
+
+    N = pos_np.shape[0]
+    perm = np.random.default_rng(11).permutation(N)
+    sp = np.ascontiguousarray(pos_np[perm])
+    stream = torch.cuda.current_stream()
+    pos = torch.tensor(sp, device="cuda")
+    f = torch.tensor(np.ascontiguousarray(f_np[perm]), device="cuda")
+    plan = DcpsePlan(3, W.grad_lap_outputs(3), order=2, stream=stream)
+    plan.set_timing(True)
+    plan.build_neighbors(pos, rcut)
+    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
+    out = torch.empty((NOUT, N), dtype=torch.float64, device="cuda")
+    nnz = plan.info()["nnz"]
+    hbm, _ = peaks()
+    res = {"reorder": plan.reorder_info()}
+    for label, pol in (("cell_order", 0), ("caller_order", -1)):
+        plan.set_reorder(pol)
+        for _ in range(5):
+            plan.apply(f, C.F32, out)
+        plan.reset_timing()
+        for _ in range(50):
+            plan.apply(f, C.F32, out)
+        ms, kn = plan.timing(C.K_APPLY_BATCHED)
+        sm, sn = plan.timing(C.K_SPLIT)
+        t = ms / kn / 1e3
+        b = W.apply_bytes(N, nnz, NOUT, 4)
+        res[label] = {"kernel_ms": t * 1e3, "split_ms": sm / max(sn, 1), "achieved_gbs": b / t / 1e9,
+                      "frac": b / t / 1e9 / hbm, "renumbered": plan.reorder_info()[0]}
+        if pol == 0:
+            o = out.cpu().numpy()
+            res["fp32_vs_ordered_fp32_normwise"] = max(rel_err(o[k], res32[k][perm]) for k in range(NOUT))
+    plan.check()
+    plan.close()
+    return res
+
+
 def run_gray_scott(args):
+    print(json.dumps(gray_scott_run(args)), flush=True)
+
+
+def extra_gray_scott(args):
+    return gray_scott_run(args)
+
+
+def gray_scott_run(args):
     """3D Gray-Scott on 96^3 = 884,736 jittered particles in a periodic unit
     cube (jitter +-0.1h, seed 6), DC-PSE Laplacian order 2, rCut = 2.8h, two
     FP32 species, Du=2e-5, Dv=1e-5, F=0.04, k=0.06, dt = 0.2 h^2/Du,
@@ -498,7 +807,8 @@ def run_gray_scott(args):
     # (read and written), the stage output
     step_bytes = 4 * (8 * (n + 1) + 8 * nnz + 8 * n + 8 * n + 16 * n + 8 * n)
     hbm, peak_kind = peaks()
-    res = {"only": "gray-scott", "particles": n, "nnz": nnz, "steps": total,
+    res = {"workload": "96^3 periodic Gray-Scott, 1000 RK4 steps from 10-step CUDA graphs",
+           "particles": n, "nnz": nnz, "steps": total,
            "ms_per_step_graph": t_fwd,
            "roofline": {"bound": "hbm", "algorithmic_bytes_per_step": step_bytes,
                         "achieved_gbs": step_bytes / t_fwd / 1e6, "peak_gbs": hbm,
@@ -506,8 +816,10 @@ def run_gray_scott(args):
            "backward_ms": t_bwd, "backward_ms_per_step": t_bwd / window,
            "v_final_mean": float(gs.v.mean()), "grad_v_norm": float(vb.norm()),
            "finite": bool(torch.isfinite(gs.v).all() and torch.isfinite(vb).all())}
+    res["backward_over_forward"] = res["backward_ms_per_step"] / t_fwd
     plan.check()
-    print(json.dumps(res), flush=True)
+    plan.close()
+    return res
 
 
 def run_interp(args):

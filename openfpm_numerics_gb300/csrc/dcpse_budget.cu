@@ -17,13 +17,14 @@
 // A row is corrected when its bound exceeds half the budget against the
 // call's own largest |output| M_o (the FP32 outputs: M_o overestimates the
 // FP64 maximum by at most the largest FP32 error, which the factor 1/2 and
-// the corrected rows themselves cover).  The correction adds, in FP64,
+// the corrected rows themselves cover).  The correction adds
 //     sum_q (r_o,pq - r16_o,pq) (f_q - f_p),   r = RN32(w64 - w32)
 // (r16 = 0 without the bf16 streams; r - r16 is exact in FP32 since r16 is
 // within a factor 2 of r; |w64 - w32 - r| <= 2^-24 |w64 - w32|, so the
-// corrected row is exact up to 2^-48 B_o,p).  The differences are formed
-// from the field's float pair in FP64 (hi and lo differences are exact in
-// double), the field the FP32 kernel read.
+// corrected row is exact up to 2^-48 B_o,p).  The correction is summed with
+// the FP32 apply's own arithmetic (the field's float pair, exact
+// differences, compensated sums): it needs only FP32 relative accuracy,
+// being 2^-24 of the output's terms.
 //
 // Two kernels.  The first tests every row against the thresholds (one lane
 // per row, reading the bounds coalesced) and appends the flagged rows, with
@@ -37,6 +38,7 @@
 #include <cuda_bf16.h>
 
 #include "dcpse_internal.h"
+#include "dcpse_f32_row.cuh"
 
 namespace dcpse {
 namespace {
@@ -90,31 +92,37 @@ __global__ void __launch_bounds__(256) budget_apply_kernel(BudgetArgs a) {
         const unsigned pm = item.y;
         const int64_t beg = a.rowptr[row], end = a.rowptr[row + 1];
         const float2 fp = a.f2[a.inv ? (int64_t)a.inv[row] : row];
-        double acc[NO];
+        // the FP32 apply's exact differences and compensated sums: the
+        // residuals are 2^-24 of the weights, so the correction needs only
+        // FP32 relative accuracy (GB300's FP64 pipe is narrow)
+        RowAcc<NO, false> acc;
+        acc.init();
+        float rz[NO];
 #pragma unroll
-        for (int o = 0; o < NO; ++o) acc[o] = 0.0;
+        for (int o = 0; o < NO; ++o) rz[o] = 0.0f;
         for (int64_t j = beg + lane; j < end; j += 32) {
             const int32_t q = a.cols[j];
             const float2 fq = a.f2[a.inv ? a.inv[q] : q];
-            const double d = ((double)fq.x - (double)fp.x) + ((double)fq.y - (double)fp.y);
+            float r[NO];
+#pragma unroll
+            for (int o = 0; o < NO; ++o) {
+                r[o] = 0.0f;
+                if (pm & (1u << o)) {
+                    r[o] = a.r32[(int64_t)o * a.ws + j];
+                    if (R16)
+                        r[o] -= __bfloat162float(static_cast<const __nv_bfloat16*>(a.r16)[(int64_t)o * a.ws + j]);
+                }
+            }
+            acc.add(r, rz, fq, fp, 0xffffffffu);
+        }
+        acc.template reduce<32>();
+        if (lane < NO && (pm & (1u << lane))) {
 #pragma unroll
             for (int o = 0; o < NO; ++o)
-                if (pm & (1u << o)) {
-                    float r = a.r32[(int64_t)o * a.ws + j];
-                    if (R16) r -= __bfloat162float(static_cast<const __nv_bfloat16*>(a.r16)[(int64_t)o * a.ws + j]);
-                    acc[o] = fma((double)r, d, acc[o]);
+                if (o == lane) {
+                    double* dst = a.out + (int64_t)o * a.oos + row * a.ors;
+                    *dst = *dst + acc.value(o);
                 }
-        }
-#pragma unroll
-        for (int o = 0; o < NO; ++o) {
-            if (!(pm & (1u << o))) continue;  // uniform over the warp
-            double v = acc[o];
-#pragma unroll
-            for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
-            if (lane == o) {
-                double* dst = a.out + (int64_t)o * a.oos + row * a.ors;
-                *dst = *dst + v;
-            }
         }
     }
 }

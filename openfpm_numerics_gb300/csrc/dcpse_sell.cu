@@ -12,7 +12,10 @@
 // Padding entries carry weight 0 and a column whose value the row reads
 // anyway (the row itself on one set), which adds exactly nothing.  The
 // per-entry arithmetic (exact differences, compensated sums for outputs of
-// order >= 2) is the CSR kernel's (RowAcc).
+// order >= 2) is the CSR kernel's (RowAcc).  The column, weight and residual
+// streams are read once per apply, with the streaming (evict-first) cache
+// hint, so that L2 keeps the field that every row gathers from and the
+// outputs that a renumbered layout writes out of order.
 #include <cuda_bf16.h>
 
 #include "dcpse_internal.h"
@@ -188,9 +191,9 @@ __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
             for (int u = 0; u < U; ++u) {
                 const int j = j0 + u;
                 const bool ok = j < L;
-                q[u] = ok ? c[(int64_t)j * kSlice] : 0;
+                q[u] = ok ? __ldcs(c + (int64_t)j * kSlice) : 0;
 #pragma unroll
-                for (int o = 0; o < NO; ++o) wv[u][o] = ok ? w[(int64_t)o * a.total + (int64_t)j * kSlice] : 0.0;
+                for (int o = 0; o < NO; ++o) wv[u][o] = ok ? __ldcs(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0;
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? a.f[(int64_t)q[u] * a.fs] : fp;
@@ -253,11 +256,12 @@ __global__ void __launch_bounds__(256, (NO <= 4 && !RESID && !BOUND ? 5 : (NO <=
             for (int u = 0; u < U; ++u) {
                 const int j = j0 + u;
                 const bool ok = j < L;
-                q[u] = ok ? c[(int64_t)j * kSlice] : 0;
+                q[u] = ok ? __ldcs(c + (int64_t)j * kSlice) : 0;
 #pragma unroll
                 for (int o = 0; o < NO; ++o) {
-                    wv[u][o] = ok ? w[(int64_t)o * a.total + (int64_t)j * kSlice] : 0.0f;
-                    rv[u][o] = (RESID && ok) ? __bfloat162float(rr[(int64_t)o * a.total + (int64_t)j * kSlice]) : 0.0f;
+                    wv[u][o] = ok ? __ldcs(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
+                    rv[u][o] = (RESID && ok) ? __bfloat162float(__ldcs(rr + (int64_t)o * a.total + (int64_t)j * kSlice))
+                                             : 0.0f;
                 }
             }
             // entries past the slice end take the row's own value (a zero

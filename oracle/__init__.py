@@ -90,6 +90,10 @@ def lib():
         L.orc_vjp_positions.restype = ctypes.c_int64
         L.orc_vjp_positions.argtypes = [ctypes.c_int, _D, ctypes.c_int64, _I64, _I32, ctypes.c_int, _U, _INT,
                                         ctypes.c_uint, ctypes.c_double, _D, _D, _D]
+        L.orc_vjp_positions_rows.restype = ctypes.c_int64
+        L.orc_vjp_positions_rows.argtypes = [ctypes.c_int, _D, ctypes.c_int64, _I64, _I32, ctypes.c_int, _U, _INT,
+                                             ctypes.c_uint, ctypes.c_double, _D, _D, ctypes.c_int64, ctypes.c_int64,
+                                             ctypes.c_int, _D]
         _lib = L
     return _lib
 
@@ -308,9 +312,10 @@ def apply_sum(f, rowptr, cols, Ks, eips, diff_orders, *, nthreads=1):
     return out
 
 
-def vjp_positions(pos, rowptr, cols, outputs, f, g, order=2, h_over_eps=0.9):
+def vjp_positions(pos, rowptr, cols, outputs, f, g, order=2, h_over_eps=0.9, rows=None, nthreads=1):
     """Reference adjoint: d/dx of sum_o,p g[o,p] (L_o f)_p, lists fixed.
-    outputs: list of outputs, each a list of term signatures."""
+    outputs: list of outputs, each a list of term signatures.  rows=(r0, r1)
+    restricts the sum to rows [r0, r1), computed on nthreads threads."""
     pos = _c(pos, np.float64)
     n, dim = pos.shape
     sigs = _c([x for o in outputs for s in o for x in s], np.uint32)
@@ -320,8 +325,14 @@ def vjp_positions(pos, rowptr, cols, outputs, f, g, order=2, h_over_eps=0.9):
     grad = np.zeros((n, dim))
     rowptr = _c(rowptr, np.int64)
     cols = _c(cols, np.int32)
-    lib().orc_vjp_positions(dim, _p(pos, _D), n, _p(rowptr, _I64), _p(cols, _I32), len(tout), _p(sigs, _U),
-                            _p(tout, _INT), order, float(h_over_eps), _p(f, _D), _p(g, _D), _p(grad, _D))
+    if rows is None and nthreads <= 1:
+        lib().orc_vjp_positions(dim, _p(pos, _D), n, _p(rowptr, _I64), _p(cols, _I32), len(tout), _p(sigs, _U),
+                                _p(tout, _INT), order, float(h_over_eps), _p(f, _D), _p(g, _D), _p(grad, _D))
+        return grad
+    r0, r1 = (0, n) if rows is None else rows
+    lib().orc_vjp_positions_rows(dim, _p(pos, _D), n, _p(rowptr, _I64), _p(cols, _I32), len(tout), _p(sigs, _U),
+                                 _p(tout, _INT), order, float(h_over_eps), _p(f, _D), _p(g, _D), int(r0), int(r1),
+                                 int(nthreads), _p(grad, _D))
     return grad
 
 

@@ -786,9 +786,14 @@ void orc_apply_sum(int64_t n_dom, int ncomp, const double* f_sup, const double* 
 // then the chain rule through u_q, eps and e_t = eps^-|alpha_t|.
 // grad is [n][dim] and accumulated (zero it first).  Positions, f, g: domain
 // arrays; sigs: nterms x dim; term_output: output of each term; g: [nout][n].
-int64_t orc_vjp_positions(int dim, const double* pos, int64_t n, const int64_t* rowptr, const int32_t* cols,
-                          int nterms, const unsigned* sigs, const int* term_output, unsigned order, double h_over_eps,
-                          const double* f, const double* g, double* grad) {
+}  // extern "C"
+
+namespace {
+// The adjoint of rows [row0, row1): emit(i, d, v) adds v to d/dx_i,d.
+template <typename Emit>
+int64_t vjp_rows(int dim, const double* pos, int64_t n, const int64_t* rowptr, const int32_t* cols, int nterms,
+                 const unsigned* sigs, const int* term_output, unsigned order, double h_over_eps, const double* f,
+                 const double* g, int64_t row0, int64_t row1, Emit emit) {
     Geom geo = make_geom(dim, nullptr, nullptr, nullptr);
     std::vector<Basis> bases;
     std::vector<std::vector<double>> rhs;
@@ -799,7 +804,7 @@ int64_t orc_vjp_positions(int dim, const double* pos, int64_t n, const int64_t* 
         rhs.push_back(b);
     }
     int64_t skipped = 0;
-    for (int64_t p = 0; p < n; ++p) {
+    for (int64_t p = row0; p < row1; ++p) {
         const int64_t beg = rowptr[p];
         const int k = (int)(rowptr[p + 1] - beg);
         std::vector<double> X((size_t)k * dim);
@@ -902,10 +907,58 @@ int64_t orc_vjp_positions(int dim, const double* pos, int64_t n, const int64_t* 
                 const double x = X[(size_t)q * dim + d];
                 const double sg = x > 0 ? 1.0 : (x < 0 ? -1.0 : 0.0);
                 const double G = Gq[(size_t)q * dim + d] / eps + Dtot * sg / (k * h_over_eps);
-                grad[p * dim + d] += G;
-                grad[qq * dim + d] -= G;
+                emit(p, d, G);
+                emit(qq, d, -G);
             }
         }
+    }
+    return skipped;
+}
+}  // namespace
+
+extern "C" {
+
+int64_t orc_vjp_positions(int dim, const double* pos, int64_t n, const int64_t* rowptr, const int32_t* cols,
+                          int nterms, const unsigned* sigs, const int* term_output, unsigned order, double h_over_eps,
+                          const double* f, const double* g, double* grad) {
+    return vjp_rows(dim, pos, n, rowptr, cols, nterms, sigs, term_output, order, h_over_eps, f, g, 0, n,
+                    [&](int64_t i, int d, double v) { grad[i * dim + d] += v; });
+}
+
+// The same for rows [row0, row1) on nthreads threads: each thread records
+// its contributions, which are then added in thread order (grad is not
+// zeroed first).
+int64_t orc_vjp_positions_rows(int dim, const double* pos, int64_t n, const int64_t* rowptr, const int32_t* cols,
+                               int nterms, const unsigned* sigs, const int* term_output, unsigned order,
+                               double h_over_eps, const double* f, const double* g, int64_t row0, int64_t row1,
+                               int nthreads, double* grad) {
+    const int nt = std::max(1, nthreads);
+    struct Part {
+        std::vector<int64_t> idx;
+        std::vector<double> val;
+        int64_t skipped = 0;
+    };
+    std::vector<Part> parts((size_t)nt);
+    const int64_t rows = row1 - row0;
+    const int64_t chunk = (rows + nt - 1) / nt;
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t) {
+        const int64_t b = row0 + t * chunk, e = std::min(row1, b + chunk);
+        if (b >= e) continue;
+        th.emplace_back([&, t, b, e] {
+            Part& P = parts[(size_t)t];
+            P.skipped = vjp_rows(dim, pos, n, rowptr, cols, nterms, sigs, term_output, order, h_over_eps, f, g, b, e,
+                                 [&](int64_t i, int d, double v) {
+                                     P.idx.push_back(i * dim + d);
+                                     P.val.push_back(v);
+                                 });
+        });
+    }
+    for (auto& x : th) x.join();
+    int64_t skipped = 0;
+    for (auto& P : parts) {
+        for (size_t j = 0; j < P.idx.size(); ++j) grad[P.idx[j]] += P.val[j];
+        skipped += P.skipped;
     }
     return skipped;
 }
