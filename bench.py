@@ -330,10 +330,10 @@ def run_ours(args):
     resr = outr.cpu().numpy()
 
     # budget-driven FP32 (rows whose FP32 error bound exceeds 1e-6 corrected
-    # toward the FP64 weights; the bf16 residual streams are stored, so the
-    # first pass adds them); kernel times from the plan's timers
+    # toward the FP64 weights; FP32 first pass); kernel times from the plan's
+    # timers
     outg = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
-    plan.set_error_budget(1e-6)
+    plan.set_error_budget(1e-6, C.F32)
     for _ in range(3):
         plan.apply(f, C.F32_BUDGET, outg)
     plan.budget_stats(reset=True)
@@ -438,7 +438,10 @@ def run_ours(args):
         o_out = r["out"]
 
         def vs_orc(a):
-            return max(rel_err(a[o][:S], o_out[o]) for o in range(NOUT))
+            # normalised by the largest output over all rows, as the metric's
+            # normwise error (the GPU's reference-order output, bit-exact with
+            # the oracle on these rows)
+            return max(float(np.abs(a[o][:S] - o_out[o]).max() / np.abs(ref_out[o]).max()) for o in range(NOUT))
 
         oracle_rows = {
             "rows": S, "entries": r["nnz"],
@@ -447,7 +450,8 @@ def run_ours(args):
             "fp64_reference_order_bit_exact": bool(np.array_equal(ref_out[:, :S], o_out)),
             "fp64_batched_normwise": vs_orc(b64), "fp32_normwise": vs_orc(res32),
             "fp32_resid_normwise": vs_orc(resr), "fp32_budget_normwise": vs_orc(resg),
-            "definition": "max|gpu-oracle| / max|oracle| over the sample rows, max over the 4 outputs"}
+            "definition": "max over the sample rows |gpu - oracle| / max over all rows |FP64 reference-order "
+                          "output|, max over the 4 outputs"}
 
     if rank == 0:
         line = {
@@ -488,8 +492,8 @@ def run_ours(args):
                             "pairs_corrected_per_call": budget_pairs,
                             "fraction_corrected": budget_pairs / (N * NOUT), "budget": 1e-6,
                             "error_vs_fp64_reference_order": errors["fp32_budget_vs_fp64_reference_order_normwise"],
-                            "note": "FP32 + bf16 residual first pass with per-row error bounds, FP64-weight "
-                                    "residual correction of the rows over the budget"},
+                            "note": "FP32 first pass with per-row error bounds, FP64-weight residual "
+                                    "correction of the rows over the budget"},
             "autotune": tuned,
             "speedup_fp32_batched_vs_fp64_plain": t_plain / t_step,
             "errors": errors,
@@ -568,6 +572,9 @@ def extra_graded(args):
     flags = C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F64 | C.STORE_OUT_F32_RESID | C.STORE_OUT_F32_CORR
     tuned = autotune.tune_assembly(plan, pos, flags)
     plan.assemble(pos, flags)
+    # most second-derivative rows of this cloud exceed the budget in FP32
+    # alone: the first pass also streams the bf16 residuals
+    plan.set_error_budget(1e-6, C.F32_RESID)
     nbad = plan.particle_status()[0]
     ok = plan.eps()[1].cpu().numpy() == 0
     x, y = pos_np[:, 0], pos_np[:, 1]
@@ -607,7 +614,15 @@ def extra_graded(args):
     # the oracle on 2000 sampled rows (lists, per-term reference assembly,
     # reference-order apply)
     rows = np.sort(np.random.default_rng(8).choice(N, 2000, replace=False))
-    o_rp, o_cols = oracle.neighbors(pos_np[rows], 0.0, support=pos_np, rcut_pp=rpp_np[rows])
+    # lists of the sampled rows against the whole set: the oracle's self test
+    # compares indices, so the sample keeps its particle and drops it here
+    a_rp, a_cols = oracle.neighbors(pos_np[rows], 0.0, support=pos_np, rcut_pp=rpp_np[rows], self_skip=False)
+    keep = np.ones(a_cols.size, bool)
+    for i, r in enumerate(rows):
+        seg = slice(a_rp[i], a_rp[i + 1])
+        keep[seg] = a_cols[seg] != r
+    o_cols = a_cols[keep]
+    o_rp = np.concatenate([[0], np.cumsum([keep[a_rp[i]:a_rp[i + 1]].sum() for i in range(rows.size)])])
     g_rp = rp_t.cpu().numpy()
     g_cols = cols_t.cpu().numpy()
     same = all(np.array_equal(o_cols[o_rp[i]:o_rp[i + 1]], g_cols[g_rp[r]:g_rp[r + 1]]) for i, r in enumerate(rows))
@@ -618,12 +633,15 @@ def extra_graded(args):
                               [0, 1, 2, 3, 4], 5, f_np, f_dom=f_np[rows])
     o_ref = multi(host_cores())
     okr = ok[rows] & np.all([t[3] == 0 for t in terms], axis=0)
+
+    def vs_orc(a):
+        return max(float(np.abs(a[o][rows][okr] - o_ref[o][okr]).max() / np.abs(o64[o][ok]).max())
+                   for o in range(5))
+
     res["oracle_rows"] = {"rows": int(rows.size), "neighbor_lists_equal": bool(same),
-                          "fp64_normwise": max(_pct(o64[o][rows], o_ref[o], okr)["max"] for o in range(5)),
-                          "fp32_normwise": max(_pct(o32[o][rows], o_ref[o], okr)["max"] for o in range(5)),
-                          "fp32_budget_normwise": max(_pct(ob[o][rows], o_ref[o], okr)["max"] for o in range(5)),
-                          "definition": "max|gpu-oracle| / max|oracle| over assembled sample rows, max over "
-                                        "the 5 operators"}
+                          "fp64_normwise": vs_orc(o64), "fp32_normwise": vs_orc(o32), "fp32_budget_normwise": vs_orc(ob),
+                          "definition": "max over assembled sample rows |gpu - oracle| / max over all rows |FP64 "
+                                        "output|, max over the 5 operators"}
     hbm, _ = peaks()
     b32 = W.apply_bytes(N, nnz, 5, 4)
     res["roofline_fp32"] = {"algorithmic_bytes": b32, "achieved_gbs": b32 / t32 / 1e6, "frac": b32 / t32 / 1e6 / hbm}

@@ -202,16 +202,18 @@ int dcpse_apply_batched_host(dcpse_plan_t* plan, const double* h_f, double* h_ou
  * each row's weight-rounding error, 2^-24 sum_q |w32_o,pq| |f_q - f_p|, and
  * a second pass adds sum_q (w64 - w32)_o,pq (f_q - f_p) in FP64 to exactly
  * the rows whose bound exceeds budget/2 of the call's largest |output|.
- * Needs DCPSE_STORE_OUT_F32_CORR at assembly.  With the bf16 residual
- * streams also stored (DCPSE_STORE_OUT_F32_RESID) the first pass adds them
- * and its bound shrinks to 2^-32 sum_q ..., so far fewer rows need the
- * second pass.  Floor: a corrected row is exact to about 2^-48 sum_q
+ * Needs DCPSE_STORE_OUT_F32_CORR at assembly.  first_pass DCPSE_F32 (the
+ * default) streams the FP32 weights alone: the cheapest when few rows need
+ * the second pass (smooth fields on near-uniform sets).  DCPSE_F32_RESID
+ * also streams the bf16 residuals (DCPSE_STORE_OUT_F32_RESID at assembly):
+ * its bound shrinks to 2^-32 sum_q ..., so far fewer rows need the second
+ * pass (second derivatives on strongly graded clouds).  Floor: a corrected row is exact to about 2^-48 sum_q
  * |w| |f_q - f_p|, the order of the FP64 apply's own rounding, so budgets
  * below that relative to max|out| (e.g. outputs that vanish identically)
  * cannot be resolved.  The reference stores its
  * weights in FP64 only (Dcpse.hpp:59-63, applied at Dcpse.hpp:467-499); this
  * is how the FP32 weights keep to its results.  budget in (0, 1). */
-int dcpse_plan_set_error_budget(dcpse_plan_t* plan, double budget);
+int dcpse_plan_set_error_budget(dcpse_plan_t* plan, double budget, int first_pass);
 /* (row, output) pairs the DCPSE_F32_BUDGET applies corrected since the last
  * reset (synchronises the plan's stream; reset != 0 zeroes the count). */
 int dcpse_plan_budget_stats(dcpse_plan_t* plan, int64_t* pairs_corrected, int reset);
@@ -359,6 +361,11 @@ int dcpse_measure_fp64_peak(void* stream, double* tflops);
  * (by default only outputs with a term of order >= 2 do; the others take
  * plain fused sums). */
 #define DCPSE_APPLY_COMPENSATE_ALL 16
+/* The sliced kernels read their column and weight streams with the
+ * streaming (evict-first) cache hint on a renumbered layout only (see
+ * dcpse_plan_set_reorder); these bits force the hint on or off. */
+#define DCPSE_APPLY_STREAM_HINT_ON 32
+#define DCPSE_APPLY_STREAM_HINT_OFF 64
 int dcpse_plan_set_apply_config(dcpse_plan_t* plan, int lanes, int mode);
 /* Assembly schedule knobs (autotuning): particles are processed in bins of
  * neighbour count of width bin_width (0 = index order; uneven clouds keep

@@ -47,7 +47,7 @@ SIGNATURES = {
     "dcpse_apply_output_f64": (_I, [_P, _I, _P, _P]),
     "dcpse_apply_batched": (_I, [_P, _P, _P, _I]),
     "dcpse_apply_batched_host": (_I, [_P, _P, _P, _I]),
-    "dcpse_plan_set_error_budget": (_I, [_P, _D]),
+    "dcpse_plan_set_error_budget": (_I, [_P, _D, _I]),
     "dcpse_plan_budget_stats": (_I, [_P, _PI64, _I]),
     "dcpse_plan_set_reorder": (_I, [_P, _I]),
     "dcpse_plan_reorder_info": (_I, [_P, _PI, _c.POINTER(_D), _c.POINTER(_D)]),

@@ -268,6 +268,7 @@ struct dcpse_plan_s {
     // kernel's bounds [nout][n], the call's largest |output| per output and
     // the (row, output) pairs corrected since the last reset
     double budget = 1e-6;
+    int budget_pass = DCPSE_F32;  // first pass: DCPSE_F32 or DCPSE_F32_RESID (adds the bf16 streams)
     float* bnd = nullptr;
     uint2* blist = nullptr;  // rows to correct (scratch)
     int64_t bnd_len = 0;
@@ -1750,6 +1751,14 @@ int ensure_sell_resid(dcpse_plan_t* P) {
         });
 }
 
+// The evict-first hint of the sliced kernels' streams: on a renumbered layout
+// unless the apply configuration says otherwise.
+int stream_hint(const dcpse_plan_t* P) {
+    if (P->apply_mode & DCPSE_APPLY_STREAM_HINT_ON) return 1;
+    if (P->apply_mode & DCPSE_APPLY_STREAM_HINT_OFF) return 0;
+    return P->sell_perm ? 1 : 0;
+}
+
 // The FP32 batched apply of rows [r0, r1) (0, 0: all rows) from the plan's
 // split field into d_out ([n_outputs][n]).
 int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, int64_t r1,
@@ -1799,6 +1808,7 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
         (rr1 % 256 == 0 || rr1 == P->n) && (!P->sell_perm || (rr0 == 0 && rr1 == P->n))) {
         SellArgs sa{};
         sa.perm = P->sell_perm;
+        sa.stream = stream_hint(P);
         sa.n = P->n;
         sa.nslices = sell_slices(P->n);
         sa.srow = P->sell_row;
@@ -1840,6 +1850,8 @@ int check_f32_weights(dcpse_plan_t* P, int precision) {
         return fail(DCPSE_ERR_STATE, "FP32 residuals not stored (DCPSE_STORE_OUT_F32_RESID)");
     if (precision == DCPSE_F32_BUDGET && !P->r32)
         return fail(DCPSE_ERR_STATE, "FP32 residuals for the correction not stored (DCPSE_STORE_OUT_F32_CORR)");
+    if (precision == DCPSE_F32_BUDGET && P->budget_pass == DCPSE_F32_RESID && !P->r16)
+        return fail(DCPSE_ERR_STATE, "the bf16 first pass needs DCPSE_STORE_OUT_F32_RESID");
     return DCPSE_OK;
 }
 
@@ -1850,7 +1862,7 @@ int sell_ready(dcpse_plan_t* P, int precision, bool* ready) {
     const int mode = P->apply_mode & 15;
     if (mode != 0 && mode != 4) return DCPSE_OK;
     if (int rc = ensure_sell(P)) return rc;
-    const bool resid = precision == DCPSE_F32_RESID || (precision == DCPSE_F32_BUDGET && P->r16);
+    const bool resid = precision == DCPSE_F32_RESID || (precision == DCPSE_F32_BUDGET && P->budget_pass == DCPSE_F32_RESID);
     if (resid)
         if (int rc = ensure_sell_resid(P)) return rc;
     *ready = P->sell_w && (!resid || P->sell_r);
@@ -1868,11 +1880,11 @@ int split_for_apply(dcpse_plan_t* P, const double* d_f, int precision) {
 // The budget-driven FP32 apply of every row from the plan's split field into
 // d_out ([n_outputs][n]): the sliced FP32 kernel with its weight-rounding
 // bounds, then the FP64 residual correction of the rows whose bound exceeds
-// the budget (every row when the sliced layout is not available).  When the
-// plan also holds the bf16 residual streams (DCPSE_STORE_OUT_F32_RESID) the
-// first pass adds them: its bound is 2^8 times smaller, so far fewer rows
-// need the second pass (worth it where many rows would, e.g. second
-// derivatives on strongly graded clouds).
+// the budget (every row when the sliced layout is not available).  With the
+// DCPSE_F32_RESID first pass (dcpse_plan_set_error_budget) it adds the bf16
+// residual streams: its bound is 2^8 times smaller, so far fewer rows need
+// the second pass (worth it where many rows would, e.g. second derivatives
+// on strongly graded clouds).
 int apply_budget(dcpse_plan_t* P, double* d_out) {
     cudaStream_t st = P->stream;
     const int64_t n = P->n;
@@ -1896,9 +1908,10 @@ int apply_budget(dcpse_plan_t* P, double* d_out) {
     if (int rc = sell_ready(P, DCPSE_F32_BUDGET, &ready)) return rc;
     {
         if (ready) {
-            with_r16 = P->r16 != nullptr;
+            with_r16 = P->budget_pass == DCPSE_F32_RESID;
             SellArgs sa{};
             sa.perm = P->sell_perm;
+            sa.stream = stream_hint(P);
             sa.n = n;
             sa.nslices = sell_slices(n);
             sa.srow = P->sell_row;
@@ -1986,6 +1999,7 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
             if (P->sell_w64) {
                 Sell64Args sa{};
                 sa.perm = P->sell_perm;
+                sa.stream = stream_hint(P);
                 sa.n = P->n;
                 sa.nwin = (P->n + 255) / 256;
                 sa.srow = P->sell_row;
@@ -2015,10 +2029,13 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
     return DCPSE_OK;
 }
 
-int dcpse_plan_set_error_budget(dcpse_plan_t* P, double rel) {
+int dcpse_plan_set_error_budget(dcpse_plan_t* P, double rel, int first_pass) {
     if (int rc = check_plan(P)) return rc;
     if (!(rel > 0.0) || !(rel < 1.0)) return fail(DCPSE_ERR_ARG, "the error budget must lie in (0, 1)");
+    if (first_pass != DCPSE_F32 && first_pass != DCPSE_F32_RESID)
+        return fail(DCPSE_ERR_ARG, "the first pass must be DCPSE_F32 or DCPSE_F32_RESID");
     P->budget = rel;
+    P->budget_pass = first_pass;
     return DCPSE_OK;
 }
 
@@ -2477,8 +2494,10 @@ int dcpse_plan_set_apply_config(dcpse_plan_t* P, int lanes, int mode) {
     if (int rc = check_plan(P)) return rc;
     if (lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
         return fail(DCPSE_ERR_ARG, "lanes must be 0, 4, 8, 16 or 32");
-    if ((mode & ~(15 | DCPSE_APPLY_COMPENSATE_ALL)) != 0 || (mode & 15) > 4)
-        return fail(DCPSE_ERR_ARG, "mode must be 0..4, optionally | DCPSE_APPLY_COMPENSATE_ALL");
+    if ((mode & ~(15 | DCPSE_APPLY_COMPENSATE_ALL | DCPSE_APPLY_STREAM_HINT_ON | DCPSE_APPLY_STREAM_HINT_OFF)) != 0 ||
+        (mode & 15) > 4 || ((mode & DCPSE_APPLY_STREAM_HINT_ON) && (mode & DCPSE_APPLY_STREAM_HINT_OFF)))
+        return fail(DCPSE_ERR_ARG, "mode must be 0..4, optionally | DCPSE_APPLY_COMPENSATE_ALL and one "
+                                   "DCPSE_APPLY_STREAM_HINT_* bit");
     P->apply_lanes = lanes;
     P->apply_mode = mode;
     return DCPSE_OK;

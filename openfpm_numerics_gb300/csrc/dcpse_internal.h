@@ -200,6 +200,7 @@ struct SellArgs {
     // |output| per output as float bits (atomic max; zero it before the call)
     float* bnd;
     unsigned* maxabs;
+    int stream;            // evict-first hint on the column, weight and residual streams
 };
 int64_t sell_slices(int64_t n);
 // srow [sell_slices(n) * 32], slen32 [sell_slices(n)], off [sell_slices(n) + 1],
@@ -240,6 +241,7 @@ struct Sell64Args {
     double* out;            // output o of row r at out[o * oos + r * ors]
     int64_t oos, ors;
     int no_self;
+    int stream;             // evict-first hint on the column and weight streams
 };
 cudaError_t apply_sell64(const Sell64Args& a, int nout, cudaStream_t s);
 

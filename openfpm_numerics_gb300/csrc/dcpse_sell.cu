@@ -12,10 +12,10 @@
 // Padding entries carry weight 0 and a column whose value the row reads
 // anyway (the row itself on one set), which adds exactly nothing.  The
 // per-entry arithmetic (exact differences, compensated sums for outputs of
-// order >= 2) is the CSR kernel's (RowAcc).  The column, weight and residual
-// streams are read once per apply, with the streaming (evict-first) cache
-// hint, so that L2 keeps the field that every row gathers from and the
-// outputs that a renumbered layout writes out of order.
+// order >= 2) is the CSR kernel's (RowAcc).  On a renumbered layout the
+// column, weight and residual streams (read once per apply) take the
+// streaming (evict-first) cache hint, so that L2 keeps the outputs, which
+// leave in the caller's order, until their sectors are complete.
 #include <cuda_bf16.h>
 
 #include "dcpse_internal.h"
@@ -23,6 +23,15 @@
 
 namespace dcpse {
 namespace {
+
+// a load of a once-read stream, with the evict-first hint when S
+template <bool S, typename T>
+__device__ __forceinline__ T ld_stream(const T* p) {
+    if constexpr (S)
+        return __ldcs(p);
+    else
+        return *p;
+}
 
 constexpr int kWin = 256;            // rows per window (one block)
 constexpr int kSlice = 32;           // rows per slice (one warp)
@@ -168,7 +177,7 @@ __global__ void __launch_bounds__(256) sell_fill64_kernel(const int64_t* __restr
 // FP64 batched apply on the slices: a row per thread, summed weights, the
 // difference form acc_o += w_o (f_q - f_p) with fused multiply-adds (the
 // CSR FP64 kernel's arithmetic without its cross-lane reduction)
-template <int NO>
+template <int NO, bool STREAM>
 __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
     __shared__ double tile[NO][kWin];
     const int lane = threadIdx.x & 31;
@@ -191,9 +200,10 @@ __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
             for (int u = 0; u < U; ++u) {
                 const int j = j0 + u;
                 const bool ok = j < L;
-                q[u] = ok ? __ldcs(c + (int64_t)j * kSlice) : 0;
+                q[u] = ok ? ld_stream<STREAM>(c + (int64_t)j * kSlice) : 0;
 #pragma unroll
-                for (int o = 0; o < NO; ++o) wv[u][o] = ok ? __ldcs(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0;
+                for (int o = 0; o < NO; ++o)
+                    wv[u][o] = ok ? ld_stream<STREAM>(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0;
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? a.f[(int64_t)q[u] * a.fs] : fp;
@@ -225,7 +235,7 @@ __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
 // B_o = sum_q |w_o,pq| |f_q - f_p| (FP32), stored to bnd[o * n + r], and the
 // largest |output| of the call per output, atomically maxed into maxabs[o]
 // (float bits; the values are >= 0, so unsigned order is float order).
-template <int NO, int U, bool RESID, bool BOUND = false>
+template <int NO, int U, bool RESID, bool BOUND, bool STREAM>
 __global__ void __launch_bounds__(256, (NO <= 4 && !RESID && !BOUND ? 5 : (NO <= 6 ? 4 : 3)))
     apply_sell_kernel(SellArgs a) {
     // the window's outputs, staged so that they leave in row order (rows of a
@@ -256,12 +266,13 @@ __global__ void __launch_bounds__(256, (NO <= 4 && !RESID && !BOUND ? 5 : (NO <=
             for (int u = 0; u < U; ++u) {
                 const int j = j0 + u;
                 const bool ok = j < L;
-                q[u] = ok ? __ldcs(c + (int64_t)j * kSlice) : 0;
+                q[u] = ok ? ld_stream<STREAM>(c + (int64_t)j * kSlice) : 0;
 #pragma unroll
                 for (int o = 0; o < NO; ++o) {
-                    wv[u][o] = ok ? __ldcs(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
-                    rv[u][o] = (RESID && ok) ? __bfloat162float(__ldcs(rr + (int64_t)o * a.total + (int64_t)j * kSlice))
-                                             : 0.0f;
+                    wv[u][o] = ok ? ld_stream<STREAM>(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
+                    rv[u][o] = (RESID && ok)
+                                   ? __bfloat162float(ld_stream<STREAM>(rr + (int64_t)o * a.total + (int64_t)j * kSlice))
+                                   : 0.0f;
                 }
             }
             // entries past the slice end take the row's own value (a zero
@@ -451,8 +462,13 @@ cudaError_t apply_sell64(const Sell64Args& a, int nout, cudaStream_t s) {
     if (a.nwin == 0) return cudaSuccess;
     if (a.nwin > 0x7fffffff) return cudaErrorInvalidValue;
     switch (nout) {
-#define DCPSE_SELL64_CASE(NO) \
-    case NO: apply_sell64_kernel<NO><<<(unsigned)a.nwin, 256, 0, s>>>(a); break;
+#define DCPSE_SELL64_CASE(NO)                                                     \
+    case NO:                                                                      \
+        if (a.stream)                                                             \
+            apply_sell64_kernel<NO, true><<<(unsigned)a.nwin, 256, 0, s>>>(a);    \
+        else                                                                      \
+            apply_sell64_kernel<NO, false><<<(unsigned)a.nwin, 256, 0, s>>>(a);   \
+        break;
         DCPSE_SELL64_CASE(1)
         DCPSE_SELL64_CASE(2)
         DCPSE_SELL64_CASE(3)
@@ -468,6 +484,22 @@ cudaError_t apply_sell64(const Sell64Args& a, int nout, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+namespace {
+template <int NO, bool ST>
+void launch_sell(const SellArgs& a, unsigned grid, cudaStream_t s) {
+    constexpr int UR = NO == 1 ? 8 : (NO <= 2 ? 4 : 2);  // with the residual streams
+    constexpr int U = NO == 1 ? 8 : 4;
+    if (a.r && a.bnd)
+        apply_sell_kernel<NO, UR, true, true, ST><<<grid, 256, 0, s>>>(a);
+    else if (a.r)
+        apply_sell_kernel<NO, UR, true, false, ST><<<grid, 256, 0, s>>>(a);
+    else if (a.bnd)
+        apply_sell_kernel<NO, U, false, true, ST><<<grid, 256, 0, s>>>(a);
+    else
+        apply_sell_kernel<NO, U, false, false, ST><<<grid, 256, 0, s>>>(a);
+}
+}  // namespace
+
 cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s) {
     if (a.w1 <= a.w0) return cudaSuccess;
     // one block per window: the block scheduler balances the windows
@@ -479,17 +511,10 @@ cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s) {
     switch (nout) {
 #define DCPSE_SELL_CASE(NO)                                                                      \
     case NO:                                                                                     \
-        if (a.r && a.bnd)                                                                        \
-            apply_sell_kernel<NO, (NO == 1 ? 8 : (NO <= 2 ? 4 : 2)), true, true>                \
-                <<<(unsigned)grid, 256, 0, s>>>(a);                                              \
-        else if (a.r)                                                                            \
-            apply_sell_kernel<NO, (NO == 1 ? 8 : (NO <= 2 ? 4 : 2)), true>                      \
-                <<<(unsigned)grid, 256, 0, s>>>(a);                                              \
-        else if (a.bnd)                                                                          \
-            apply_sell_kernel<NO, (NO == 1 ? 8 : 4), false, true>                               \
-                <<<(unsigned)grid, 256, 0, s>>>(a);                                              \
+        if (a.stream)                                                                            \
+            launch_sell<NO, true>(a, (unsigned)grid, s);                                         \
         else                                                                                     \
-            apply_sell_kernel<NO, (NO == 1 ? 8 : 4), false><<<(unsigned)grid, 256, 0, s>>>(a);   \
+            launch_sell<NO, false>(a, (unsigned)grid, s);                                        \
         break;
         DCPSE_SELL_CASE(1)
         DCPSE_SELL_CASE(2)

@@ -268,10 +268,12 @@ class DcpsePlan:
                out_host.ctypes.data_as(ctypes.c_void_p), int(precision))
         return out_host
 
-    def set_error_budget(self, budget=1e-6):
+    def set_error_budget(self, budget=1e-6, first_pass=C.F32):
         """Relative error budget per output of the F32_BUDGET applies (the
-        FP32 result against the FP64 summed weights, normwise)."""
-        C.call("dcpse_plan_set_error_budget", self._h, float(budget))
+        FP32 result against the FP64 summed weights, normwise) and their
+        first pass: C.F32 (FP32 weights alone) or C.F32_RESID (also the bf16
+        residual streams, for sets where many rows would need correcting)."""
+        C.call("dcpse_plan_set_error_budget", self._h, float(budget), int(first_pass))
 
     def budget_stats(self, reset=False):
         """(row, output) pairs the F32_BUDGET applies corrected in FP64 since

@@ -102,6 +102,7 @@ def test_budget_on_bf16_residual_first_pass(cuda):
     f = torch.tensor(_fields(pos)["sin_cos"], device="cuda")
     ref = plain.apply(f, C.F64).cpu().numpy()
     counts = []
+    resid.set_error_budget(1e-6, C.F32_RESID)
     for plan in (plain, resid):
         plan.budget_stats(reset=True)
         out = plan.apply(f, C.F32_BUDGET).cpu().numpy()
@@ -159,4 +160,13 @@ def test_budget_needs_the_residuals(cuda):
     assert e.value.code == C.ERR_STATE
     with pytest.raises(C.DcpseError):
         plan.set_error_budget(0.0)
+    plan.set_error_budget(1e-6, C.F32_RESID)  # the bf16 first pass needs its streams
+    plan2 = DcpsePlan(2, [[(2, 0), (0, 2)]], order=2)
+    plan2.build_neighbors(pt, 3.1 * h)
+    plan2.assemble(pt, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F32_CORR)
+    plan2.set_error_budget(1e-6, C.F32_RESID)
+    with pytest.raises(C.DcpseError) as e:
+        plan2.apply(torch.zeros(pos.shape[0], dtype=torch.float64, device="cuda"), C.F32_BUDGET)
+    assert e.value.code == C.ERR_STATE
+    plan2.close()
     plan.close()

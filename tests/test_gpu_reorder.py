@@ -50,6 +50,9 @@ def test_shuffled_set_is_renumbered_and_bit_identical(shuffled):
         a = auto.apply(f, prec).clone()
         b = keep.apply(f, prec).clone()
         assert torch.equal(a, b), prec
+    for plan in (auto, keep):
+        plan.set_error_budget(1e-7, C.F32_RESID)
+    assert torch.equal(auto.apply(f, C.F32_BUDGET), keep.apply(f, C.F32_BUDGET))
     auto.close()
     keep.close()
 
