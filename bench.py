@@ -508,6 +508,7 @@ def run_ours(args):
         line["adjoint"] = extra_adjoint(args, pos_np, cfg["rcut"])
         line["gray_scott"] = extra_gray_scott(args)
         line["shuffled"] = extra_shuffled(args, pos_np, cfg["rcut"], f_np, res32)
+        line["cpp_dropin"] = extra_cpp_dropin(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -752,6 +753,36 @@ def extra_shuffled(args, pos_np, rcut, f_np, res32):
             res["fp32_vs_ordered_fp32_normwise"] = max(rel_err(o[k], res32[k][perm]) for k in range(NOUT))
     plan.check()
     plan.close()
+    return res
+
+
+def extra_cpp_dropin(args):
+    """The C++ drop-in end to end (tests/cpp/bench_dcpse_api.cpp): the
+    reference's user code getV<1>(parts) = Lap(getV<0>(parts)) and the
+    Gradient on 128^3 host-resident particles, FP64 expression path and the
+    opt-in batched FP32 paths; built here with the host compiler against the
+    library."""
+    import subprocess
+    import tempfile
+
+    from openfpm_numerics_gb300 import build as b
+
+    lib = b.build()
+    with tempfile.TemporaryDirectory() as tmp:
+        exe = os.path.join(tmp, "bench_dcpse_api")
+        cmd = ["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"),
+               os.path.join(ROOT, "tests", "cpp", "bench_dcpse_api.cpp"), "-L" + os.path.dirname(lib),
+               "-ldcpse_gb300", "-Wl,-rpath," + os.path.dirname(lib), "-o", exe]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            return {"error": "compile failed: " + r.stderr[-500:]}
+        r = subprocess.run([exe, str(args.nside)], capture_output=True, text=True, timeout=900)
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+        if r.returncode != 0 or not lines:
+            return {"error": "run failed (rc %d): %s" % (r.returncode, r.stderr[-500:])}
+        res = json.loads(lines[-1])
+    res["workload"] = ("128^3 jittered particles (std::mt19937_64 seed 2, +-0.15h), rCut 2.8h, order 2; "
+                       "timings include the host property gather and scatter of each assignment")
     return res
 
 

@@ -109,7 +109,17 @@ struct PropRef {
     PropRef& operator=(const Expr& e) {
         const std::size_t n = v.size_local();
         int ncomp = e.nodes.empty() ? 1 : e.nodes[0].ncomp;
-        std::vector<std::vector<double>> acc(ncomp, std::vector<double>(n, 0.0)), tmp;
+        typedef typename std::remove_reference<decltype(v.template getProp<prp>(0))>::type PT;
+        std::vector<std::vector<double>> tmp;
+        if (e.nodes.size() == 1 && e.nodes[0].coef == 1.0) {
+            // one operator: its result goes straight into the property
+            e.nodes[0].eval(tmp);
+            for (std::size_t p = 0; p < n; ++p)
+                for (int c = 0; c < ncomp; ++c)
+                    detail::prop_component(v.template getProp<prp>(p), c, detail::is_indexable<PT>{}) = tmp[c][p];
+            return *this;
+        }
+        std::vector<std::vector<double>> acc(ncomp, std::vector<double>(n, 0.0));
         bool first = true;
         for (const auto& node : e.nodes) {
             if (node.ncomp != ncomp) throw std::invalid_argument("mixing scalar and vector operator results");
@@ -119,7 +129,6 @@ struct PropRef {
                     acc[c][p] = (first && node.coef == 1.0) ? tmp[c][p] : acc[c][p] + node.coef * tmp[c][p];
             first = false;
         }
-        typedef typename std::remove_reference<decltype(v.template getProp<prp>(0))>::type PT;
         for (std::size_t p = 0; p < n; ++p)
             for (int c = 0; c < ncomp; ++c) {
                 auto& slot = detail::prop_component(v.template getProp<prp>(p), c, detail::is_indexable<PT>{});
@@ -196,16 +205,25 @@ public:
         plan_.reset();
     }
 
-    // operand: getV<i>(parts)
+    // operand: getV<i>(parts).  By default every output is the reference's
+    // own sum of its Dcpse terms in FP64, in the reference's order (one pass
+    // per term).  After set_apply_precision(DCPSE_F32 / DCPSE_F32_RESID /
+    // DCPSE_F32_BUDGET) all outputs come from one batched pass over the
+    // summed weights (see dcpse_capi.h), through pinned staging buffers.
     template <unsigned int prp, typename vector_type>
     Expr operator()(PropRef<prp, vector_type> arg) {
         Node nd;
         nd.ncomp = (int)outputs_.size();
         detail::PlanHost* P = plan_.get();
         const std::size_t outs = outputs_.size();
-        nd.eval = [P, arg, outs](std::vector<std::vector<double>>& out) {
+        const int prec = precision_;
+        nd.eval = [P, arg, outs, prec](std::vector<std::vector<double>>& out) {
             std::vector<double> f = arg.values();
             detail::check_rows(f.size(), P->n());
+            if (prec != DCPSE_F64) {
+                P->apply_batched(prec, f.data(), out);
+                return;
+            }
             out.assign(outs, std::vector<double>(f.size()));
             for (std::size_t o = 0; o < outs; ++o) P->apply_output((int)o, f.data(), out[o].data());
         };
@@ -213,6 +231,27 @@ public:
         e.nodes.push_back(nd);
         return e;
     }
+
+    // Precision of the expression applies (no counterpart in the reference,
+    // whose operators apply in FP64 only): DCPSE_F64 (default), DCPSE_F32,
+    // DCPSE_F32_RESID or DCPSE_F32_BUDGET (with the plan's error budget,
+    // 1e-6 unless set_error_budget says otherwise).  Re-assembles when the
+    // weights it needs are not stored yet.
+    void set_apply_precision(int precision) {
+        int flags = DCPSE_STORE_TERMS_F64 | DCPSE_STORE_OUT_F32;
+        if (precision == DCPSE_F32_RESID) flags |= DCPSE_STORE_OUT_F32_RESID;
+        if (precision == DCPSE_F32_BUDGET) flags |= DCPSE_STORE_OUT_F32_CORR;
+        if (precision != DCPSE_F64 && precision != DCPSE_F32 && precision != DCPSE_F32_RESID &&
+            precision != DCPSE_F32_BUDGET)
+            throw std::invalid_argument("DC-PSE operator: unknown precision");
+        if ((flags | asm_flags_) != asm_flags_) {
+            asm_flags_ |= flags;
+            int64_t nbad = plan_->assemble(asm_flags_);
+            detail::throw_too_few(plan_->last_fail_code(), nbad);
+        }
+        precision_ = precision;
+    }
+    void set_error_budget(double budget) { detail::check(dcpse_plan_set_error_budget(plan_->plan(), budget, DCPSE_F32)); }
 
     // FP32 batched apply of every output of this operator (one pass)
     template <unsigned int prp, typename vector_type>
@@ -274,7 +313,7 @@ private:
             plan_->set_particles(parts, vl_);
         }
         if (!assemble) return;
-        int64_t nbad = plan_->assemble(DCPSE_STORE_TERMS_F64 | DCPSE_STORE_OUT_F32);
+        int64_t nbad = plan_->assemble(asm_flags_);
         detail::throw_too_few(plan_->last_fail_code(), nbad);
         // a surface operator hands the accumulated lists back (Dcpse.hpp:1001-1005)
         if constexpr (std::is_same<VerletList_type, VerletList>::value)
@@ -330,6 +369,8 @@ private:
     double hoe_;
     int dim_;
     double rcut_ = 0.0;
+    int precision_ = DCPSE_F64;
+    int asm_flags_ = DCPSE_STORE_TERMS_F64 | DCPSE_STORE_OUT_F32;
     VerletList own_vl_;  // the support of a Dcpse_gpu-kind operator
     detail::SurfaceCfg surf_;
     std::unique_ptr<detail::PlanHost> plan_;

@@ -85,6 +85,32 @@ private:
     std::size_t bytes_ = 0;
 };
 
+// Page-locked (pinned) host buffer owned by host code: the batched applies
+// read their field from it and write their outputs into it in place.
+class PinBuf {
+public:
+    PinBuf() = default;
+    PinBuf(const PinBuf&) = delete;
+    PinBuf& operator=(const PinBuf&) = delete;
+    ~PinBuf() { release(); }
+    double* get() const { return static_cast<double*>(p_); }
+    void ensure(std::size_t count) {
+        if (count <= count_) return;
+        release();
+        check(dcpse_host_alloc(&p_, count * sizeof(double)));
+        count_ = count;
+    }
+    void release() {
+        if (p_) dcpse_host_free(p_);
+        p_ = nullptr;
+        count_ = 0;
+    }
+
+private:
+    void* p_ = nullptr;
+    std::size_t count_ = 0;
+};
+
 // Surface operator set-up (SurfaceDcpse, Dcpse.hpp:829-1085): unit normals
 // of the support particles, nCount virtual particles per side at spacing
 // nSpacing, and the cutoff / self option of the Verlet list handed in.
@@ -266,6 +292,20 @@ public:
     }
     int last_fail_code() const { return last_fail_code_; }
 
+    // every output of the field f in one batched pass (precision DCPSE_F32,
+    // DCPSE_F32_RESID or DCPSE_F32_BUDGET): f and the outputs go through
+    // pinned staging buffers, which the kernels read and write in place;
+    // out[o] gets output o
+    void apply_batched(int precision, const double* f, std::vector<std::vector<double>>& out) {
+        const std::size_t n = (std::size_t)std::max<int64_t>(n_, 0);
+        pin_f_.ensure(std::max<std::size_t>(n, 1));
+        pin_o_.ensure(std::max<std::size_t>(n * nout_, 1));
+        std::copy(f, f + n, pin_f_.get());
+        check(dcpse_apply_batched_host(plan_, pin_f_.get(), pin_o_.get(), precision));
+        out.resize(nout_);
+        for (int o = 0; o < nout_; ++o) out[o].assign(pin_o_.get() + o * n, pin_o_.get() + (o + 1) * n);
+    }
+
     // FP64 output o of the field f (host arrays of n values)
     void apply_output(int o, const double* f, double* out) {
         fd_.upload(f, (std::size_t)n_ * sizeof(double));
@@ -398,6 +438,7 @@ private:
     std::vector<int64_t> rowptr_;
     std::vector<int32_t> cols_;
     DevBuf pos_, spos_, nrm_, spc_, rcs_, fd_, od_;
+    PinBuf pin_f_, pin_o_;
     bool surface_ = false;
     bool cache_valid_ = false;
     std::vector<std::vector<double>> K_, eip_;

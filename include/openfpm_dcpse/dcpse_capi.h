@@ -172,6 +172,10 @@ int dcpse_set_term_kernels(dcpse_plan_t* plan, int term, const double* d_kernels
  * of openfpm_devices' CudaMemory (hostToDevice / deviceToHost). */
 int dcpse_device_alloc(void** ptr, uint64_t bytes);
 int dcpse_device_free(void* ptr);
+/* Page-locked host memory mapped into the device address space: host
+ * buffers that dcpse_apply_batched_host reads and writes in place. */
+int dcpse_host_alloc(void** ptr, uint64_t bytes);
+int dcpse_host_free(void* ptr);
 /* synchronous copy between any host / device pointers */
 int dcpse_copy(void* dst, const void* src, uint64_t bytes);
 

@@ -63,6 +63,8 @@ SIGNATURES = {
     "dcpse_rk4_gs_adjoint_stage": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _D, _c.POINTER(_D)]),
     "dcpse_device_alloc": (_I, [_PP, _c.c_uint64]),
     "dcpse_device_free": (_I, [_P]),
+    "dcpse_host_alloc": (_I, [_PP, _c.c_uint64]),
+    "dcpse_host_free": (_I, [_P]),
     "dcpse_copy": (_I, [_P, _P, _c.c_uint64]),
     "dcpse_plan_set_timing": (_I, [_P, _I]),
     "dcpse_plan_set_apply_config": (_I, [_P, _I, _I]),

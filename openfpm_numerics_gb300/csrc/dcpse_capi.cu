@@ -289,9 +289,19 @@ struct dcpse_plan_s {
     double* rowsum = nullptr;
     int rowsum_prec = -1;
     double* gentry = nullptr;
-    // transposed Laplacian weights of output 0 for the RK4 adjoint
+    // transposed Laplacian weights of output 0 for the RK4 adjoint, and the
+    // FP32 ones on a sliced ELL layout of the transposed list
     float *wT32 = nullptr, *rs32 = nullptr;
     double *wT64 = nullptr, *rs64 = nullptr;
+    int32_t *tsell_row = nullptr, *tsell_cols = nullptr;
+    int64_t* tsell_off = nullptr;
+    float* tsell_w = nullptr;
+    void free_tsell() {
+        dfree(tsell_row);
+        dfree(tsell_cols);
+        dfree(tsell_off);
+        dfree(tsell_w);
+    }
     void free_transpose() {
         dfree(korder);
         korder_width = 0;
@@ -304,6 +314,7 @@ struct dcpse_plan_s {
         dfree(rs32);
         dfree(wT64);
         dfree(rs64);
+        free_tsell();
         rowsum_prec = -1;
     }
     // RK4 stage scratch: (u, v) pairs, as doubles
@@ -381,6 +392,7 @@ struct dcpse_plan_s {
         dfree(rs32);
         dfree(wT64);
         dfree(rs64);
+        free_tsell();
         assembled = false;
     }
     void free_all() {
@@ -1524,6 +1536,36 @@ int dcpse_rk4_gs_adjoint_prepare(dcpse_plan_t* P, int precision) {
         if (!P->wT32) DCPSE_CK(dalloc(&P->wT32, P->nnz));
         if (!P->rs32) DCPSE_CK(dalloc(&P->rs32, P->n));
         DCPSE_CK(rk_transpose_weights<float>(P->rowptr, P->t_idx, P->n, P->nnz, P->w32, P->wT32, P->rs32, P->stream));
+        // the transposed list and weights on a sliced ELL layout (the forward
+        // stage's layout, for the adjoint stage): kept only if it fits
+        P->free_tsell();
+        if (P->n > 0) {
+            const int64_t ns = sell_slices(P->n);
+            int32_t* slen = nullptr;
+            int64_t* tmp = nullptr;
+            int64_t total = 0;
+            cudaError_t e = dalloc(&P->tsell_row, (size_t)ns * 32);
+            if (e == cudaSuccess) e = dalloc(&P->tsell_off, (size_t)ns + 1);
+            if (e == cudaSuccess) e = dalloc(&slen, (size_t)ns);
+            if (e == cudaSuccess) e = dalloc(&tmp, (size_t)scan_tmp_elems(ns));
+            if (e == cudaSuccess) e = sell_order(P->t_row, P->n, P->tsell_row, slen, P->tsell_off, tmp, P->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(&total, P->tsell_off + ns, sizeof total, cudaMemcpyDeviceToHost, P->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+            dfree(slen);
+            dfree(tmp);
+            if (e == cudaSuccess) e = dalloc(&P->tsell_cols, (size_t)total + kPad);
+            if (e == cudaSuccess) e = dalloc(&P->tsell_w, (size_t)total + kPad);
+            if (e == cudaSuccess)
+                e = sell_fill(P->t_row, P->t_src, P->wT32, nullptr, P->nnz, 1, P->n, 1, P->tsell_row, P->tsell_off,
+                              total, P->tsell_cols, P->tsell_w, nullptr, P->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+            if (e != cudaSuccess) {
+                P->free_tsell();
+                if (e != cudaErrorMemoryAllocation) return fail(DCPSE_ERR_CUDA, cudaGetErrorString(e));
+                cudaGetLastError();  // no room: the CSR adjoint kernel serves
+            }
+        }
     } else if (precision == DCPSE_F64) {
         if (!P->w64) return fail(DCPSE_ERR_STATE, "FP64 output weights not stored");
         if (!P->wT64) DCPSE_CK(dalloc(&P->wT64, P->nnz));
@@ -1551,14 +1593,16 @@ int dcpse_rk4_gs_adjoint_stage(dcpse_plan_t* P, int precision, const void* Yu, c
         RkAdjArgs<float> a{P->n, P->t_row, P->t_src, P->wT32, P->rs32, (const float*)Yu, (const float*)Yv,
                            (const float*)kbu, (const float*)kbv, (const float*)ybu, (const float*)ybv, (float*)accu,
                            (float*)accv, (float*)next_u, (float*)next_v, cy, cY, params[0], params[1], params[2],
-                           params[3], P->rk_pack};
+                           params[3], P->rk_pack, P->tsell_row, P->tsell_off, P->tsell_cols, P->tsell_w};
+        const int mode = P->apply_mode & 15;
+        if (!(mode == 0 || mode == 4) || !P->tsell_w) a.srow = nullptr;  // a CSR schedule was asked for
         DCPSE_CK(rk_adjoint_stage<float>(a, lanes, P->stream));
     } else if (precision == DCPSE_F64) {
         if (!P->wT64) return fail(DCPSE_ERR_STATE, "call dcpse_rk4_gs_adjoint_prepare first");
         RkAdjArgs<double> a{P->n, P->t_row, P->t_src, P->wT64, P->rs64, (const double*)Yu, (const double*)Yv,
                             (const double*)kbu, (const double*)kbv, (const double*)ybu, (const double*)ybv,
                             (double*)accu, (double*)accv, (double*)next_u, (double*)next_v, cy, cY, params[0],
-                            params[1], params[2], params[3], P->rk_pack};
+                            params[1], params[2], params[3], P->rk_pack, nullptr, nullptr, nullptr, nullptr};
         DCPSE_CK(rk_adjoint_stage<double>(a, lanes, P->stream));
     } else {
         return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
@@ -1575,6 +1619,18 @@ int dcpse_device_alloc(void** ptr, uint64_t bytes) {
 
 int dcpse_device_free(void* ptr) {
     if (ptr) DCPSE_CK(cudaFree(ptr));
+    return DCPSE_OK;
+}
+
+int dcpse_host_alloc(void** ptr, uint64_t bytes) {
+    if (!ptr) return fail(DCPSE_ERR_ARG, "NULL pointer");
+    *ptr = nullptr;
+    DCPSE_CK(cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocMapped | cudaHostAllocPortable));
+    return DCPSE_OK;
+}
+
+int dcpse_host_free(void* ptr) {
+    if (ptr) DCPSE_CK(cudaFreeHost(ptr));
     return DCPSE_OK;
 }
 

@@ -404,6 +404,11 @@ struct RkAdjArgs {
     double cy, cY;                  // next kbar = cy ybar + cY Ybar
     double Du, Dv, F, K;
     void* pack;                     // scratch: n (kbar_u, kbar_v) pairs
+    // the transposed weights on the sliced ELL layout (FP32; null: CSR kernel)
+    const int32_t* srow;
+    const int64_t* soff;
+    const int32_t* scols;
+    const float* sw;
 };
 template <typename T>
 cudaError_t rk_stage(const RkArgs<T>& a, int lanes, cudaStream_t s);

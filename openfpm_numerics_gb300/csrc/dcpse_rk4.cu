@@ -250,6 +250,55 @@ __global__ void __launch_bounds__(256) gs_adjoint_kernel(RkAdjArgs<T> a) {
     }
 }
 
+// FP32 adjoint stage on the sliced ELL layout of the transposed weights: a
+// row per thread, 8 gathers of (kbar_u, kbar_v) pairs in flight; entries past
+// the slice end add the row's own pair with weight 0 (an exact zero)
+__global__ void __launch_bounds__(256) gs_adjoint_sell_kernel(RkAdjArgs<float> a, int64_t nwin) {
+    const float2* __restrict__ KB = static_cast<const float2*>(a.pack);
+    const int lane = threadIdx.x & 31;
+    constexpr int U = 8;
+    for (int64_t win = blockIdx.x; win < nwin; win += gridDim.x) {
+        const int64_t s = win * 8 + (threadIdx.x >> 5);
+        const int32_t p = a.srow[s * 32 + lane];
+        if (p < 0) continue;
+        const int64_t b = a.soff[s];
+        const int L = (int)((a.soff[s + 1] - b) / 32);
+        const int32_t* __restrict__ c = a.scols + b + lane;
+        const float* __restrict__ w = a.sw + b + lane;
+        float lu = 0.f, lv = 0.f;
+        for (int j0 = 0; j0 < L; j0 += U) {
+            int32_t q[U];
+            float wq[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = j0 + u;
+                q[u] = j < L ? c[(int64_t)j * 32] : p;
+                wq[u] = j < L ? w[(int64_t)j * 32] : 0.f;
+            }
+            float2 y[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) y[u] = KB[q[u]];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                lu = fmaf(wq[u], y[u].x, lu);
+                lv = fmaf(wq[u], y[u].y, lv);
+            }
+        }
+        const float kbu = a.kbu[p], kbv = a.kbv[p];
+        lu = lu - a.rs[p] * kbu;
+        lv = lv - a.rs[p] * kbv;
+        const float u = a.Yu[p], v = a.Yv[p];
+        const float Ybu = (float)a.Du * lu - (v * v + (float)a.F) * kbu + v * v * kbv;
+        const float Ybv = (float)a.Dv * lv - 2.f * u * v * kbu + (2.f * u * v - (float)a.F - (float)a.K) * kbv;
+        a.accu[p] += Ybu;
+        a.accv[p] += Ybv;
+        if (a.next_u) {
+            a.next_u[p] = (float)a.cy * a.ybu[p] + (float)a.cY * Ybu;
+            a.next_v[p] = (float)a.cy * a.ybv[p] + (float)a.cY * Ybv;
+        }
+    }
+}
+
 template <typename T>
 __global__ void gather_kernel(const int64_t* __restrict__ tidx, int64_t nnz, const T* __restrict__ w,
                               T* __restrict__ wT) {
@@ -298,6 +347,13 @@ template <typename T>
 cudaError_t rk_adjoint_stage(const RkAdjArgs<T>& a, int lanes, cudaStream_t s) {
     if (a.n == 0) return cudaSuccess;
     pack_kernel<T><<<grid_n(a.n, 256), 256, 0, s>>>(a.kbu, a.kbv, a.n, static_cast<typename Pair<T>::type*>(a.pack));
+    if constexpr (std::is_same<T, float>::value) {
+        if (a.srow) {
+            const int64_t nwin = (a.n + 255) / 256;
+            gs_adjoint_sell_kernel<<<(unsigned)nwin, 256, 0, s>>>(a, nwin);
+            return cudaGetLastError();
+        }
+    }
     switch (lanes) {
         case 4: gs_adjoint_kernel<T, 4><<<grid_n(a.n, 64), 256, 0, s>>>(a); break;
         case 8: gs_adjoint_kernel<T, 8><<<grid_n(a.n, 32), 256, 0, s>>>(a); break;

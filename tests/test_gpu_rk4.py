@@ -131,3 +131,33 @@ def test_adjoint_stage_equals_transposed_jacobian(cuda, dtype, tol):
                      (nxt[1].double().cpu().numpy(), cy * bv + cY * Ybv)):
         scale = np.abs(ref).max() + np.abs(acc0[0].double().cpu().numpy()).max()
         assert np.abs(got - ref).max() <= tol * scale
+
+
+@pytest.mark.parametrize("dtype,bar", [(torch.float64, 1e-10), (torch.float32, 2e-5)])
+def test_rk4_matches_oracle_rk4(cuda, orc, dtype, bar):
+    """Five fused RK4 steps against a classic RK4 whose Laplacian is the
+    oracle's (the reference's three Dcpse terms 2e_i, assembled and applied
+    in the reference's order on the periodic set); src/OdeIntegrators/tests/
+    OdeIntegratores_base_tests.cpp:33-72 defines the stepping."""
+    cfg = W.config5(12)
+    plan, u, v, dt = _setup(12, dtype)
+    pos = cfg["pos"]
+    rp, cols = orc.neighbors(pos, cfg["rcut"], box=cfg["box"])
+    terms = [orc.assemble(pos, rp, cols, s, 2, box=cfg["box"]) for s in [(2, 0, 0), (0, 2, 0), (0, 0, 2)]]
+
+    def L(fld):
+        return orc.apply_sum(fld, rp, cols, [t[2] for t in terms], [t[1] for t in terms], [2, 2, 2])
+
+    def rhs(y, t):
+        uu, vv = y
+        uvv = uu * vv * vv
+        return (P["Du"] * L(uu) - uvv + P["F"] * (1 - uu), P["Dv"] * L(vv) + uvv - (P["F"] + P["k"]) * vv)
+
+    gs = GrayScottRK4(plan, u, v, P["Du"], P["Dv"], P["F"], P["k"], dt)
+    y = (u.double().cpu().numpy(), v.double().cpu().numpy())
+    for _ in range(5):
+        gs.step()
+        y = runge_kutta4(rhs, y, 0.0, dt)
+    for a, b in ((gs.u, y[0]), (gs.v, y[1])):
+        a = a.double().cpu().numpy()
+        assert np.abs(a - b).max() <= bar * np.abs(b).max()
