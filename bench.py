@@ -845,7 +845,7 @@ def gray_scott_run(args):
         s.synchronize()
         ybar = (torch.zeros_like(gs.u), torch.ones_like(gs.v))
         ev0.record(s)
-        ub, vb = gs.backward(ckpts, every, ybar)
+        ub, vb = gs.backward(ckpts, every, ybar, stream=s)
         ev1.record(s)
     s.synchronize()
     t_bwd = ev0.elapsed_time(ev1)

@@ -118,22 +118,63 @@ class GrayScottRK4:
         self._adj_stage(stages[0], k_b, ybar, acc, None, 0.0, 0.0)           # Ybar1
         return acc
 
-    def backward(self, checkpoints, every, ybar):
+    def _reverse_step_into(self, stages, yb, acc, k_a, k_b):
+        """reverse_step with preallocated buffers: yb (ybar of y_{n+1}) is
+        replaced by ybar of y_n."""
+        dt = self.dt
+        acc[0].copy_(yb[0])
+        acc[1].copy_(yb[1])
+        torch.mul(yb[0], dt / 6.0, out=k_a[0])
+        torch.mul(yb[1], dt / 6.0, out=k_a[1])
+        self._adj_stage(stages[3], k_a, yb, acc, k_b, dt / 3.0, dt)
+        self._adj_stage(stages[2], k_b, yb, acc, k_a, dt / 3.0, dt / 2.0)
+        self._adj_stage(stages[1], k_a, yb, acc, k_b, dt / 6.0, dt / 2.0)
+        self._adj_stage(stages[0], k_b, yb, acc, None, 0.0, 0.0)
+        yb[0].copy_(acc[0])
+        yb[1].copy_(acc[1])
+
+    def backward(self, checkpoints, every, ybar, stream=None):
         """Reverse over len(checkpoints) * every steps: checkpoints[i] is the
         (u, v) state at the start of segment i (segments of `every` steps,
         the last ending at the current state); returns ybar at checkpoints[0].
         Each segment is recomputed forward from its checkpoint with the stage
-        states recorded, then reversed step by step."""
+        states recorded, then reversed step by step.  With a stream, which
+        must be the plan's stream, one segment's recompute and reversal are
+        captured in a CUDA graph and replayed for the other segments."""
         self.prepare_adjoint()
         u_save, v_save = self.u.clone(), self.v.clone()
         hist = [[(torch.empty_like(self.u), torch.empty_like(self.v)) for _ in range(4)] for _ in range(every)]
-        for seg in reversed(range(len(checkpoints))):
-            self.u.copy_(checkpoints[seg][0])
-            self.v.copy_(checkpoints[seg][1])
+        yb = (ybar[0].clone(), ybar[1].clone())
+        acc, k_a, k_b = [(torch.empty_like(self.u), torch.empty_like(self.v)) for _ in range(3)]
+
+        def segment():
             for s in range(every):
                 self.step(record=hist[s])
             for s in reversed(range(every)):
-                ybar = self.reverse_step(hist[s], ybar)
+                self._reverse_step_into(hist[s], yb, acc, k_a, k_b)
+
+        segs = list(reversed(range(len(checkpoints))))
+        if stream is None or not segs:
+            for seg in segs:
+                self.u.copy_(checkpoints[seg][0])
+                self.v.copy_(checkpoints[seg][1])
+                segment()
+        else:
+            with torch.cuda.stream(stream):
+                # the last segment runs eagerly (warming up every call), the
+                # others replay its graph
+                self.u.copy_(checkpoints[segs[0]][0])
+                self.v.copy_(checkpoints[segs[0]][1])
+                segment()
+                if len(segs) > 1:
+                    stream.synchronize()
+                    g = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g, stream=stream):  # records, runs nothing
+                        segment()
+                    for seg in segs[1:]:
+                        self.u.copy_(checkpoints[seg][0])
+                        self.v.copy_(checkpoints[seg][1])
+                        g.replay()
         self.u.copy_(u_save)
         self.v.copy_(v_save)
-        return ybar
+        return yb
