@@ -56,6 +56,12 @@ extern "C" {
 #define DCPSE_ASSEMBLE_ASYNC 16 /* do not synchronise; query dcpse_particle_status */
 #define DCPSE_STORE_OUT_F32_RESID 32 /* also bf16 residuals w64 - w32 of the FP32 weights */
 #define DCPSE_STORE_OUT_F32_CORR 64  /* also FP32 residuals w64 - w32 (for DCPSE_F32_BUDGET) */
+#define DCPSE_ASSEMBLE_TC 128   /* with DCPSE_ASSEMBLE_FAST: the Gram products B^T B on the tensor
+                                   cores (tcgen05), from a 56-bit fixed-point B: not bit-identical
+                                   to the sequential FP64 sums, within their order sensitivity;
+                                   taken when the union basis has <= 32 functions and no row has
+                                   more than 112 neighbours, else the FP64 kernel serves
+                                   (dcpse_plan_assembly_info tells which) */
 
 /* precision of dcpse_apply_batched */
 #define DCPSE_F64 0
@@ -151,6 +157,9 @@ int dcpse_neighbors_ptr(dcpse_plan_t* plan, const int64_t** d_rowptr, const int3
  * Replaces: Dcpse::initializeStaticSize (src/DCPSE/Dcpse.hpp:690-796),
  * Dcpse_gpu::assembleLocalMatrices (src/DCPSE/Dcpse.cuh:620-717). */
 int dcpse_assemble(dcpse_plan_t* plan, const double* d_pos, const double* d_eps_fixed, int flags);
+/* Whether the last assembly took its Gram products on the tensor cores
+ * (DCPSE_ASSEMBLE_TC). */
+int dcpse_plan_assembly_info(dcpse_plan_t* plan, int* gram_on_tensor_cores);
 int dcpse_particle_status(dcpse_plan_t* plan, int64_t* n_bad, int64_t* first_bad, int* first_code);
 /* Device arrays owned by the plan (valid until the next assemble/destroy). */
 int dcpse_eps_ptr(dcpse_plan_t* plan, const double** d_eps, const int32_t** d_status);

@@ -40,6 +40,7 @@ SIGNATURES = {
     "dcpse_neighbors_ptr": (_I, [_P, _PP, _PP]),
     "dcpse_assemble": (_I, [_P, _P, _P, _I]),
     "dcpse_particle_status": (_I, [_P, _PI64, _PI64, _PI]),
+    "dcpse_plan_assembly_info": (_I, [_P, _PI]),
     "dcpse_eps_ptr": (_I, [_P, _PP, _PP]),
     "dcpse_term_kernels_ptr": (_I, [_P, _I, _PP, _PP]),
     "dcpse_output_weights_ptr": (_I, [_P, _I, _PP, _PP]),
@@ -93,6 +94,7 @@ ASSEMBLE_FAST = 8
 ASSEMBLE_ASYNC = 16
 STORE_OUT_F32_RESID = 32
 STORE_OUT_F32_CORR = 64
+ASSEMBLE_TC = 128
 
 F64 = 0
 F32 = 1

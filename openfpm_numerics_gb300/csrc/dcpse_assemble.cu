@@ -60,12 +60,14 @@ struct Split {
     int ldb;                 // row stride of the B chunk of the Gram kernel
     int nslots;              // monomial program slots per lane
     int nout;                // outputs of the plan
+    int npairs;              // Gram entries per particle
     double* gram;            // [nb][gstride]
     double* coef;            // [nb][cstride]
     double* usc;             // [nb][dim][maxk] scaled offsets u = x_pq / eps of every row
     int64_t ustride;         // dim * maxk
     int maxk;
     int32_t* gst;            // [nb] group status words
+    bool tc;                 // Gram products on the tensor cores (DCPSE_ASSEMBLE_TC)
 };
 
 template <int DIM>
@@ -222,6 +224,8 @@ __global__ void __launch_bounds__(256) gram_kernel(AsmArgs a, Split S, int64_t b
             if (t * 32 + lane < npairs) G[t * 32 + lane] = acc[t];
     }
 }
+
+#include "dcpse_gram_tc.cuh"
 
 // ------------------------------------------------------------------ 2. QR --
 // All lanes of a warp run the same loop trip counts (the basis sizes are the
@@ -593,12 +597,25 @@ cudaError_t launch_qr_any(const AsmArgs& a, const Split& S, int lpp, int64_t nb,
     }
 }
 
+template <int DIM>
+cudaError_t launch_gram_tc(const AsmArgs& a, const Split& S, int64_t b0, int64_t b1, cudaStream_t s) {
+    const TcLayout L = tc_layout(S.maxk, S.nslots, S.npairs);
+    auto kern = gram_tc_kernel<DIM>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes);
+    if (e != cudaSuccess) return e;
+    // one CTA per SM holds all its tensor memory, two particles per CTA at a time
+    const int64_t grid = std::min<int64_t>((b1 - b0 + 1) / 2, (int64_t)num_sms());
+    kern<<<(unsigned)grid, kTcThreads, L.bytes, s>>>(a, S, b0, b1, L);
+    return cudaGetLastError();
+}
+
 template <int DIM, int NPP>
-cudaError_t run(const AsmArgs& a, const Split& S, int lpp, cudaStream_t s) {
+cudaError_t run(const AsmArgs& a, const AsmTables& h, const Split& S, int lpp, cudaStream_t s) {
     for (int64_t b0 = 0; b0 < a.n; b0 += a.scratch_particles) {
         const int64_t b1 = std::min(a.n, b0 + a.scratch_particles);
         cudaError_t e = launch_eps<DIM>(a, S, b0, b1, s);
-        if (e == cudaSuccess) e = launch_gram<DIM, NPP>(a, S, b0, b1, s);
+        if (e == cudaSuccess)
+            e = S.tc ? launch_gram_tc<DIM>(a, S, b0, b1, s) : launch_gram<DIM, NPP>(a, S, b0, b1, s);
         if (e == cudaSuccess) e = launch_qr_any(a, S, lpp, b1 - b0, s);
         if (e == cudaSuccess) e = launch_weights<DIM>(a, S, b0, b1, s);
         if (e != cudaSuccess) return e;
@@ -611,12 +628,12 @@ cudaError_t dispatch(const AsmArgs& a, const AsmTables& h, const Split& S, int l
     // Gram entries per lane: the smallest instantiated count that holds them
     // all (a slot no lane uses would still occupy the FP64 pipe every row)
     const int npp = (h.npairs + 31) / 32;
-    if (npp <= 2) return run<DIM, 2>(a, S, lpp, s);
-    if (npp <= 4) return run<DIM, 4>(a, S, lpp, s);
-    if (npp <= 7) return run<DIM, 7>(a, S, lpp, s);
-    if (npp <= 8) return run<DIM, 8>(a, S, lpp, s);
-    if (npp <= 16) return run<DIM, 16>(a, S, lpp, s);
-    return run<DIM, 40>(a, S, lpp, s);
+    if (npp <= 2) return run<DIM, 2>(a, h, S, lpp, s);
+    if (npp <= 4) return run<DIM, 4>(a, h, S, lpp, s);
+    if (npp <= 7) return run<DIM, 7>(a, h, S, lpp, s);
+    if (npp <= 8) return run<DIM, 8>(a, h, S, lpp, s);
+    if (npp <= 16) return run<DIM, 16>(a, h, S, lpp, s);
+    return run<DIM, 40>(a, h, S, lpp, s);
 }
 
 Split make_split(const AsmTables& h, int flags) {
@@ -638,15 +655,25 @@ Split make_split(const AsmTables& h, int flags) {
     S.ldb = h.nu | 1;
     S.nslots = h.nslots;
     S.nout = h.noutputs;
+    S.npairs = h.npairs;
     return S;
 }
 
 }  // namespace
 
+bool assembly_uses_tc(const AsmTables& h, int flags, int maxk) {
+    if (!(flags & DCPSE_ASSEMBLE_TC) || !(flags & DCPSE_ASSEMBLE_FAST_FLAG) || h.nu > kTcMaxNu || maxk > kTcMaxK)
+        return false;
+    // the planes, the monomial scratch and the pair sums fit in one CTA
+    const TcLayout L = tc_layout(maxk, h.nslots, h.npairs);
+    return L.bytes + 4096 <= (size_t)smem_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, 227 * 1024);
+}
+
 int64_t assembly_scratch_bytes(const AsmTables& h, int flags, int maxk) {
     const Split S = make_split(h, flags);
-    return (int64_t)(S.gstride + S.cstride + (int64_t)h.dim * std::max(maxk, 1)) * (int64_t)sizeof(double) +
-           (int64_t)sizeof(int32_t);
+    int64_t b = (int64_t)(S.gstride + S.cstride + (int64_t)h.dim * std::max(maxk, 1)) * (int64_t)sizeof(double) +
+                (int64_t)sizeof(int32_t);
+    return b;
 }
 
 int64_t binning_tmp_elems(int64_t n, int maxk, int width) {
@@ -696,6 +723,7 @@ cudaError_t assemble(const AsmArgs& a, const AsmTables& h, cudaStream_t s) {
     S.maxk = std::max(a.maxk, 1);
     S.ustride = (int64_t)h.dim * S.maxk;
     S.usc = S.coef + nb * S.cstride;
+    S.tc = assembly_uses_tc(h, a.flags, a.maxk);
     S.gst = reinterpret_cast<int32_t*>(S.usc + nb * S.ustride);
     int lpp = a.qr_lanes;
     if (lpp != 1 && lpp != 2 && lpp != 4 && lpp != 8 && lpp != 16 && lpp != 32) lpp = qr_lanes_auto(S);

@@ -277,6 +277,7 @@ struct dcpse_plan_s {
     unsigned long long* summary = nullptr;  // [count, first]
     int* d_err = nullptr;                   // set by kernels whose bounded wait ran out
     int apply_lanes = 0, apply_mode = 0;
+    bool asm_tc = false;  // the last assembly's Gram products ran on the tensor cores
     int asm_bin_width = 0, asm_warps = 4, asm_qr_lanes = 0;
     double* asm_scratch = nullptr;  // assembly batch scratch
     int64_t asm_scratch_bytes = 0;
@@ -1221,6 +1222,7 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     a.warps = P->asm_warps;
     a.qr_lanes = P->asm_qr_lanes;
     a.maxk = P->maxk;
+    a.err = P->d_err;
     a.order = nullptr;
     if (n > 0) {
         // batches of at most kAsmScratchBytes of scratch (Gram entries and
@@ -1254,6 +1256,7 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
         }
         a.order = P->korder;
     }
+    P->asm_tc = assembly_uses_tc(*P->htab, flags, P->maxk);
     P->tstart(DCPSE_K_ASSEMBLE);
     cudaError_t e = assemble(a, *P->htab, s);
     if (e == cudaErrorInvalidConfiguration)
@@ -2092,6 +2095,13 @@ int dcpse_plan_set_error_budget(dcpse_plan_t* P, double rel, int first_pass) {
         return fail(DCPSE_ERR_ARG, "the first pass must be DCPSE_F32 or DCPSE_F32_RESID");
     P->budget = rel;
     P->budget_pass = first_pass;
+    return DCPSE_OK;
+}
+
+int dcpse_plan_assembly_info(dcpse_plan_t* P, int* gram_on_tensor_cores) {
+    if (int rc = check_plan(P)) return rc;
+    if (!gram_on_tensor_cores) return fail(DCPSE_ERR_ARG, "NULL output");
+    *gram_on_tensor_cores = P->asm_tc ? 1 : 0;
     return DCPSE_OK;
 }
 

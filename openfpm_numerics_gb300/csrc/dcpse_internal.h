@@ -138,6 +138,7 @@ struct AsmArgs {
     int maxk;             // longest neighbour row
     double* scratch;      // assembly_scratch_bytes() per particle of a batch
     int64_t scratch_particles;  // batch size the scratch holds
+    int* err;             // device error word (bounded waits of the tensor-core Gram)
 };
 
 // Scratch bytes per particle of an assembly batch (Gram entries,
@@ -154,6 +155,11 @@ cudaError_t bin_by_count(const int64_t* rowptr, int64_t n, int maxk, int width, 
 
 // h: host copy of *a.tab (launch configuration is derived from it)
 cudaError_t assemble(const AsmArgs& a, const AsmTables& h, cudaStream_t s);
+// whether an assembly with these tables, flags and longest row takes its
+// Gram products on the tensor cores (DCPSE_ASSEMBLE_TC with the fast
+// assembly, at most 32 union monomials and 128 neighbours)
+bool assembly_uses_tc(const AsmTables& h, int flags, int maxk);
+
 
 // ----------------------------------------------------------------- apply --
 cudaError_t apply_term_f64(int64_t n, const int64_t* rowptr, const int32_t* cols, const double* K,

@@ -196,6 +196,12 @@ class DcpsePlan:
         allow = (C.ERR_PARTICLES,) if allow_failed_particles else ()
         return C.call("dcpse_assemble", self._h, _ptr(pos), _ptr(eps_fixed), int(flags), allow=allow)
 
+    def gram_on_tensor_cores(self):
+        """Whether the last assembly took its Gram products on the tensor cores."""
+        v = ctypes.c_int()
+        C.call("dcpse_plan_assembly_info", self._h, ctypes.byref(v))
+        return bool(v.value)
+
     def particle_status(self):
         nb, fb, fc = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
         C.call("dcpse_particle_status", self._h, ctypes.byref(nb), ctypes.byref(fb), ctypes.byref(fc))

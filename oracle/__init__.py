@@ -71,6 +71,10 @@ def lib():
         L.orc_assemble.restype = ctypes.c_int64
         L.orc_assemble.argtypes = [ctypes.c_int, _D, ctypes.c_int64, _D, _I64, _I32, _D, _D, _INT, _U,
                                    ctypes.c_uint, ctypes.c_double, _D, _D, _D, _D, _I32, ctypes.c_int]
+        L.orc_assemble_mode.restype = ctypes.c_int64
+        L.orc_assemble_mode.argtypes = [ctypes.c_int, _D, ctypes.c_int64, _D, _I64, _I32, _D, _D, _INT, _U,
+                                        ctypes.c_uint, ctypes.c_double, _D, _D, _D, _D, _I32, ctypes.c_int,
+                                        ctypes.c_int]
         L.orc_assemble_gpu_ref.restype = ctypes.c_int64
         L.orc_assemble_gpu_ref.argtypes = [ctypes.c_int, _D, ctypes.c_int64, _D, _I64, _I32, _D, _D, _INT, _U,
                                            ctypes.c_uint, _D, _D, _D, _I32, ctypes.c_int]
@@ -173,8 +177,12 @@ def neighbors(pos, rcut, *, support=None, self_skip=True, rcut_pp=None, box=None
 
 
 def assemble(pos, rowptr, cols, sig, order, *, support=None, box=None, h_over_eps=0.9, eps_fixed=None,
-             nthreads=1):
-    """One reference Dcpse object: returns (eps, eps_inv_pow, kernels, status)."""
+             nthreads=1, exact_gram=False):
+    """One reference Dcpse object: returns (eps, eps_inv_pow, kernels, status).
+
+    exact_gram=True sums the Gram matrix B^T B in double-double and rounds it
+    once (instead of the reference's sequential FP64 sum): a yardstick for
+    how far the kernels move when only the Gram's rounding changes."""
     pos = _c(pos, np.float64)
     n, dim = pos.shape
     sup = pos if support is None else _c(support, np.float64)
@@ -187,9 +195,9 @@ def assemble(pos, rowptr, cols, sig, order, *, support=None, box=None, h_over_ep
     eip = np.zeros(n)
     K = np.zeros(max(int(rowptr[-1]), 1))
     st = np.zeros(n, np.int32)
-    lib().orc_assemble(dim, _p(pos, _D), n, _p(sup, _D), _p(rowptr, _I64), _p(cols, _I32), _p(lo, _D),
-                       _p(hi, _D), _p(per, _INT), _p(sig, _U), order, float(h_over_eps), _p(ef, _D),
-                       _p(eps, _D), _p(eip, _D), _p(K, _D), _p(st, _I32), int(nthreads))
+    lib().orc_assemble_mode(dim, _p(pos, _D), n, _p(sup, _D), _p(rowptr, _I64), _p(cols, _I32), _p(lo, _D),
+                            _p(hi, _D), _p(per, _INT), _p(sig, _U), order, float(h_over_eps), _p(ef, _D),
+                            _p(eps, _D), _p(eip, _D), _p(K, _D), _p(st, _I32), int(nthreads), int(bool(exact_gram)))
     return eps, eip, K[: int(rowptr[-1])], st
 
 

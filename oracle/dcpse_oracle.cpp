@@ -311,6 +311,7 @@ struct AsmCtx {
     unsigned ord;
     double hoe;
     const double* eps_fixed;  // optional per-particle eps override (extension)
+    bool exact_gram = false;  // A = B^T B summed in double-double, rounded once (test aid)
 };
 
 // Dcpse.hpp:716-785 for one domain particle p.
@@ -363,7 +364,24 @@ int assemble_one(const AsmCtx& c, int64_t p, double* K, double& eps_out, double&
     for (int i = 0; i < n; ++i)
         for (int j = 0; j < n; ++j) {
             double acc = 0.0;
-            for (int q = 0; q < k; ++q) acc = std::fma(Bm[(size_t)q * n + i], Bm[(size_t)q * n + j], acc);
+            if (!c.exact_gram) {
+                for (int q = 0; q < k; ++q) acc = std::fma(Bm[(size_t)q * n + i], Bm[(size_t)q * n + j], acc);
+            } else {
+                // the same sum with error-free products (fma) and additions
+                // (Knuth's two-sum) carried in a second double: the
+                // correctly rounded Gram entry but for rare ties, against
+                // which rounding orders of the Gram can be judged
+                double lo = 0.0;
+                for (int q = 0; q < k; ++q) {
+                    const double x = Bm[(size_t)q * n + i], y = Bm[(size_t)q * n + j];
+                    const double pr = x * y, pe = std::fma(x, y, -pr);
+                    const double sm = acc + pr, bb = sm - acc;
+                    const double se = (acc - (sm - bb)) + (pr - bb);
+                    acc = sm;
+                    lo = lo + (se + pe);
+                }
+                acc = acc + lo;
+            }
             A[(size_t)i * n + j] = acc;
         }
     // a = A^-1 b (Dcpse.hpp:760-766)
@@ -666,11 +684,13 @@ int64_t orc_neighbors_brute(int dim, const double* pd, int64_t n_dom, const doub
 // neighbour order) for every domain particle.  status[p] != 0 marks a particle
 // whose system could not be built (kernels set to zero).  Returns the number
 // of such particles.
-int64_t orc_assemble(int dim, const double* pd, int64_t n_dom, const double* ps, const int64_t* rowptr,
-                     const int32_t* cols, const double* box_lo, const double* box_hi, const int* periodic,
-                     const unsigned* sig, unsigned order, double h_over_eps, const double* eps_fixed,
-                     double* eps, double* eps_inv_pow, double* kernels, int32_t* status, int nthreads) {
+int64_t orc_assemble_mode(int dim, const double* pd, int64_t n_dom, const double* ps, const int64_t* rowptr,
+                          const int32_t* cols, const double* box_lo, const double* box_hi, const int* periodic,
+                          const unsigned* sig, unsigned order, double h_over_eps, const double* eps_fixed,
+                          double* eps, double* eps_inv_pow, double* kernels, int32_t* status, int nthreads,
+                          int exact_gram) {
     AsmCtx c;
+    c.exact_gram = exact_gram != 0;
     c.dim = dim;
     c.pd = pd;
     c.ps = ps;
@@ -699,6 +719,14 @@ int64_t orc_assemble(int dim, const double* pd, int64_t n_dom, const double* ps,
         __atomic_fetch_add(&bad[0], nb, __ATOMIC_RELAXED);
     });
     return bad[0];
+}
+
+int64_t orc_assemble(int dim, const double* pd, int64_t n_dom, const double* ps, const int64_t* rowptr,
+                     const int32_t* cols, const double* box_lo, const double* box_hi, const int* periodic,
+                     const unsigned* sig, unsigned order, double h_over_eps, const double* eps_fixed,
+                     double* eps, double* eps_inv_pow, double* kernels, int32_t* status, int nthreads) {
+    return orc_assemble_mode(dim, pd, n_dom, ps, rowptr, cols, box_lo, box_hi, periodic, sig, order, h_over_eps,
+                             eps_fixed, eps, eps_inv_pow, kernels, status, nthreads, 0);
 }
 
 // Dcpse_gpu's assembly (Dcpse.cuh:776-875) of one reference Dcpse_gpu object
