@@ -67,7 +67,12 @@ struct Split {
     int64_t ustride;         // dim * maxk
     int maxk;
     int32_t* gst;            // [nb] group status words
-    bool tc;                 // Gram products on the tensor cores (DCPSE_ASSEMBLE_TC)
+    // tensor-core Gram (DCPSE_ASSEMBLE_TC): B of every particle of the batch
+    // and the exponents of its columns' largest entries
+    bool tc;
+    int kpad;                // row stride of bmat (maxk rounded up to 16)
+    double* bmat;            // [nb][nu][kpad]
+    int32_t* bexp;           // [nb][32]
 };
 
 template <int DIM>
@@ -226,6 +231,76 @@ __global__ void __launch_bounds__(256) gram_kernel(AsmArgs a, Split S, int64_t b
 }
 
 #include "dcpse_gram_tc.cuh"
+
+// B for the tensor-core products: the SIMT Gram kernel's rows of B (u, E,
+// the monomial program, in the same operations), stored to bmat[slot][j][q]
+// in FP64, and for every column the exponent E_j with |B_qj| < 2^E_j (from
+// the largest exponent field of the column), to bexp[slot][j].  One warp per
+// particle, many per SM: the FP64 work of this part needs the latency hiding.
+template <int DIM>
+__global__ void __launch_bounds__(256) gram_b_kernel(AsmArgs a, Split S, int64_t b0, int64_t b1) {
+    extern __shared__ double smem[];
+    __shared__ ProgShared P;
+    const AsmTables& T = *a.tab;
+    stage_program(T, P);
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    double* V = smem + (size_t)wib * (S.nslots * 32);
+    const int nu = T.nu;
+    const int ngroups = T.ngroups;
+    const int nprog = T.nprog;
+    const int wpc = blockDim.x >> 5;
+    const int64_t nw = (int64_t)gridDim.x * wpc;
+    for (int64_t it = b0 + (int64_t)blockIdx.x * wpc + wib; it < b1; it += nw) {
+        const int64_t slot = it - b0;
+        const int32_t word = S.gst[slot];
+        bool any_ok = false;
+        for (int g = 0; g < ngroups; ++g) any_ok |= group_status(word, g) == ST_OK;
+        if (!any_ok) continue;  // warp-uniform
+        const int64_t p = a.order ? (int64_t)a.order[it] : it;
+        const int64_t beg = a.rowptr[p];
+        const int k = (int)(a.rowptr[p + 1] - beg);
+        const double eps = a.eps[p];
+        double xp[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xp[d] = a.pos[p * DIM + d];
+        double* Bm = S.bmat + slot * (int64_t)nu * S.kpad;
+        unsigned emax[kTcMaxNu];
+#pragma unroll
+        for (int j = 0; j < kTcMaxNu; ++j) emax[j] = 0;
+        for (int c0 = 0; c0 < k; c0 += kCh) {
+            const int q = c0 + lane;
+            if (q < k) {
+                double o[DIM], u[DIM];
+                load_offset<DIM>(a, xp, a.cols[beg + q], o);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) u[d] = o[d] / eps;
+                double* Ur = S.usc + slot * S.ustride;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) Ur[d * S.maxk + q] = u[d];
+                const double E = cw_exp(-norm2<DIM>(o) / (2.0 * eps * eps));
+                monomials<DIM>(u, V, P, nprog, lane);
+#pragma unroll
+                for (int j = 0; j < kTcMaxNu; ++j)
+                    if (j < nu) {
+                        const double b = E * V[P.uslot[j] * 32 + lane];
+                        Bm[(int64_t)j * S.kpad + q] = b;
+                        emax[j] = max(emax[j], ((unsigned)__double2hiint(b) >> 20) & 0x7ffu);
+                    }
+            }
+            __syncwarp();
+        }
+        // |x| < 2^(e - 1022) for a normal x with exponent field e
+        int mine = 0;
+#pragma unroll
+        for (int j = 0; j < kTcMaxNu; ++j) {
+            const unsigned m = __reduce_max_sync(0xffffffffu, emax[j]);
+            if (lane == j) mine = max((int)m, 1) - 1022;
+        }
+        S.bexp[slot * 32 + lane] = mine;
+    }
+}
+
 
 // ------------------------------------------------------------------ 2. QR --
 // All lanes of a warp run the same loop trip counts (the basis sizes are the
@@ -599,8 +674,19 @@ cudaError_t launch_qr_any(const AsmArgs& a, const Split& S, int lpp, int64_t nb,
 
 template <int DIM>
 cudaError_t launch_gram_tc(const AsmArgs& a, const Split& S, int64_t b0, int64_t b1, cudaStream_t s) {
-    const TcLayout L = tc_layout(S.maxk, S.nslots, S.npairs);
-    auto kern = gram_tc_kernel<DIM>;
+    {
+        const int warps = warps_of(a);
+        const size_t bytes = (size_t)(S.nslots * 32) * sizeof(double) * warps;
+        auto kb = gram_b_kernel<DIM>;
+        int grid = 0;
+        cudaError_t e = persistent(kb, warps * 32, bytes, warps, b1 - b0, grid);
+        if (e != cudaSuccess) return e;
+        kb<<<grid, warps * 32, bytes, s>>>(a, S, b0, b1);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    const TcLayout L = tc_layout(S.maxk, S.npairs);
+    auto kern = gram_tc_kernel;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes);
     if (e != cudaSuccess) return e;
     // one CTA per SM holds all its tensor memory, two particles per CTA at a time
@@ -659,13 +745,15 @@ Split make_split(const AsmTables& h, int flags) {
     return S;
 }
 
+int tc_kpad(int maxk) { return ((std::max(maxk, 1) + 15) / 16) * 16; }
+
 }  // namespace
 
 bool assembly_uses_tc(const AsmTables& h, int flags, int maxk) {
     if (!(flags & DCPSE_ASSEMBLE_TC) || !(flags & DCPSE_ASSEMBLE_FAST_FLAG) || h.nu > kTcMaxNu || maxk > kTcMaxK)
         return false;
     // the planes, the monomial scratch and the pair sums fit in one CTA
-    const TcLayout L = tc_layout(maxk, h.nslots, h.npairs);
+    const TcLayout L = tc_layout(maxk, h.npairs);
     return L.bytes + 4096 <= (size_t)smem_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, 227 * 1024);
 }
 
@@ -673,6 +761,8 @@ int64_t assembly_scratch_bytes(const AsmTables& h, int flags, int maxk) {
     const Split S = make_split(h, flags);
     int64_t b = (int64_t)(S.gstride + S.cstride + (int64_t)h.dim * std::max(maxk, 1)) * (int64_t)sizeof(double) +
                 (int64_t)sizeof(int32_t);
+    if (assembly_uses_tc(h, flags, maxk))
+        b += (int64_t)h.nu * tc_kpad(maxk) * (int64_t)sizeof(double) + 32 * (int64_t)sizeof(int32_t);
     return b;
 }
 
@@ -724,7 +814,14 @@ cudaError_t assemble(const AsmArgs& a, const AsmTables& h, cudaStream_t s) {
     S.ustride = (int64_t)h.dim * S.maxk;
     S.usc = S.coef + nb * S.cstride;
     S.tc = assembly_uses_tc(h, a.flags, a.maxk);
-    S.gst = reinterpret_cast<int32_t*>(S.usc + nb * S.ustride);
+    if (S.tc) {
+        S.kpad = tc_kpad(a.maxk);
+        S.bmat = S.usc + nb * S.ustride;
+        S.bexp = reinterpret_cast<int32_t*>(S.bmat + nb * (int64_t)h.nu * S.kpad);
+        S.gst = S.bexp + nb * 32;
+    } else {
+        S.gst = reinterpret_cast<int32_t*>(S.usc + nb * S.ustride);
+    }
     int lpp = a.qr_lanes;
     if (lpp != 1 && lpp != 2 && lpp != 4 && lpp != 8 && lpp != 16 && lpp != 32) lpp = qr_lanes_auto(S);
     // a lane grouping whose work space does not fit is refused before any launch
