@@ -301,10 +301,26 @@ def run_ours(args):
     t_b64 = ev0.elapsed_time(ev1) / 1e3 / nplain
     b64 = outb.cpu().numpy()
 
+    # fast assembly with the Gram products on the tensor cores (warm-up call
+    # first: it sizes the scratch for B), and its FP32 outputs against those
+    # of the FP64-Gram assembly below
+    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.ASSEMBLE_TC)
+    plan.reset_timing()
+    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.ASSEMBLE_TC)
+    t_asm_tc = plan.timing(C.K_ASSEMBLE)[0] / 1e3
+    tc_used = plan.gram_on_tensor_cores()
+    out_tc = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
+    plan.apply(f, C.F32, out_tc)
+
     # fast assembly (summed right-hand sides) -> FP32 weights for the headline
     plan.reset_timing()
     plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
     t_asm_fast = plan.timing(C.K_ASSEMBLE)[0] / 1e3
+    out_fast = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
+    plan.apply(f, C.F32, out_fast)
+    tc_vs_fp64_gram = float(max(((out_tc[o] - out_fast[o]).abs().max() / out_fast[o].abs().max()).item()
+                                for o in range(NOUT)))
+    del out_tc, out_fast
     # the same with the residual streams of the corrected FP32 applies
     plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID | C.STORE_OUT_F32_CORR)
 
@@ -481,6 +497,11 @@ def run_ours(args):
                                        "bases (n=10, R=3) and (n=19, R=1)",
                          "reference_order": {"value": N / t_asm_ref / 1e6, "ms": t_asm_ref * 1e3,
                                              "fp64_tflops": flops_ref / t_asm_ref / 1e12},
+                         "tensor_core_gram": {"value": N / t_asm_tc / 1e6, "ms": t_asm_tc * 1e3,
+                                              "tensor_cores_used": bool(tc_used),
+                                              "fp32_outputs_vs_fp64_gram_normwise": tc_vs_fp64_gram,
+                                              "note": "DCPSE_ASSEMBLE_TC: Gram from 8-bit digit planes of a "
+                                                      "62-bit fixed-point B on tcgen05, FP32 accumulators"},
                          "failed_particles": nbad, "neighbors_ms": t_nbr * 1e3},
             "fp64_plain": {"value": N * NOUT / t_plain / 1e9, "ms_per_step": t_plain * 1e3,
                            "note": "one pass per reference Dcpse object (6), reference order"},
