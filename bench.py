@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the graded-cloud, adjoint, Gray-Scott and shuffled-order sections")
-    ap.add_argument("--only", choices=["apply", "apply64", "assemble", "gray-scott", "graded", "interp"], default=None,
+    ap.add_argument("--only", choices=["apply", "apply64", "assemble", "assemble-tc", "gray-scott", "graded", "interp"],
+                    default=None,
                     help="small-footprint run of one kernel family (for profiler captures)")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--mode", type=int, default=0, help="apply kernel: 0 auto, 1 CSR direct, 2 CSR TMA-staged, 3 CSR 8-deep, 4 sliced ELL")
@@ -1045,7 +1046,8 @@ def run_only(args):
     """One kernel family on the benchmark geometry, nothing else resident:
     --only apply keeps just the FP32 weights (fast assembly), --only apply64
     just the FP64 summed weights (batched FP64 apply), --only assemble runs
-    the reference-order and fast assemblies."""
+    the reference-order and fast assemblies, --only assemble-tc the fast
+    assembly with the FP64 Gram and with the tensor-core Gram."""
     import torch
 
     from openfpm_numerics_gb300 import _capi as C
@@ -1101,6 +1103,16 @@ def run_only(args):
         t = e0.elapsed_time(e1) / max(args.steps, 1)
         res["apply64_ms"] = t
         res["apply64_gbs"] = W.apply_bytes(N, nnz, NOUT, 8) / (t / 1e3) / 1e9
+    elif args.only == "assemble-tc":
+        plan.set_assembly_config(0, 4, args.qr_lanes)
+        ts = {"fp64_gram_ms": [], "tc_gram_ms": []}
+        for _ in range(max(1, args.steps)):
+            for key, extra in (("fp64_gram_ms", 0), ("tc_gram_ms", C.ASSEMBLE_TC)):
+                plan.reset_timing()
+                plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | extra)
+                ts[key].append(plan.timing(C.K_ASSEMBLE)[0])
+        res.update(ts)
+        res["tensor_cores_used"] = plan.gram_on_tensor_cores()
     else:
         plan.set_assembly_config(0, 4, args.qr_lanes)
         for _ in range(max(1, args.steps)):
