@@ -366,8 +366,8 @@ __global__ void __launch_bounds__(kWarps * 32) vjp_pos_kernel(VjpArgs a, VjpLayo
                     const double* lm = at + L.nmax;
                     const double ee = 1.0 / ipow(eps, (unsigned)T.gord[g]);
                     double va = 0.0, vl = 0.0;
-                    double vi[kMaxBasis];
-                    double dvi[kMaxBasis][DIM];
+                    double vi[kMaxBasisSmall];
+                    double dvi[kMaxBasisSmall][DIM];
                     for (int i = 0; i < n; ++i) {
                         mono_and_grad<DIM>(u, T.uexp[T.gidx[g][i]], vi[i], dvi[i]);
                         va += vi[i] * at[i];

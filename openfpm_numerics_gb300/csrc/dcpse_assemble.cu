@@ -69,6 +69,8 @@ struct Split {
     int32_t* gst;            // [nb] group status words
     // tensor-core Gram (DCPSE_ASSEMBLE_TC): B of every particle of the batch
     // and the exponents of its columns' largest entries
+    double* qws;             // global QR work space (one slot per lane group) or nullptr
+    int* qperm;              // its column permutations
     bool tc;
     int kpad;                // row stride of bmat (maxk rounded up to 16)
     double* bmat;            // [nb][nu][kpad]
@@ -232,6 +234,68 @@ __global__ void __launch_bounds__(256) gram_kernel(AsmArgs a, Split S, int64_t b
 
 #include "dcpse_gram_tc.cuh"
 
+// Gram kernel for bases whose entries do not fit in the lanes' registers
+// (more than 40 x 32 pairs, e.g. 7260 for the 120-function basis of
+// |alpha| = 6 in 3D): the same rows of B, and every entry's sum continued
+// from the batch scratch chunk after chunk, in the same sequential order, so
+// the entries equal the register version's (and the reference's) bit for bit.
+template <int DIM>
+__global__ void __launch_bounds__(256) gram_wide_kernel(AsmArgs a, Split S, int64_t b0, int64_t b1) {
+    extern __shared__ double smem[];
+    __shared__ ProgShared P;
+    const AsmTables& T = *a.tab;
+    stage_program(T, P);
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    double* Bs = smem + (size_t)wib * (kCh * S.ldb + S.nslots * 32);
+    double* V = Bs + kCh * S.ldb;
+    const int nu = T.nu;
+    const int npairs = T.npairs;
+    const int ngroups = T.ngroups;
+    const int nprog = T.nprog;
+    const int wpc = blockDim.x >> 5;
+    const int64_t nw = (int64_t)gridDim.x * wpc;
+    for (int64_t it = b0 + (int64_t)blockIdx.x * wpc + wib; it < b1; it += nw) {
+        const int64_t slot = it - b0;
+        const int64_t p = a.order ? (int64_t)a.order[it] : it;
+        const int64_t beg = a.rowptr[p];
+        const int k = (int)(a.rowptr[p + 1] - beg);
+        const int32_t word = S.gst[slot];
+        bool any_ok = false;
+        for (int g = 0; g < ngroups; ++g) any_ok |= group_status(word, g) == ST_OK;
+        if (!any_ok) continue;  // warp-uniform
+        const double eps = a.eps[p];
+        double xp[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xp[d] = a.pos[p * DIM + d];
+        double* G = S.gram + slot * S.gstride;
+        for (int c0 = 0; c0 < k; c0 += kCh) {
+            const int q = c0 + lane;
+            const int cnt = min(kCh, k - c0);
+            if (q < k) {
+                double o[DIM], u[DIM];
+                load_offset<DIM>(a, xp, a.cols[beg + q], o);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) u[d] = o[d] / eps;
+                double* Ur = S.usc + slot * S.ustride;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) Ur[d * S.maxk + q] = u[d];
+                const double E = cw_exp(-norm2<DIM>(o) / (2.0 * eps * eps));
+                monomials<DIM>(u, V, P, nprog, lane);
+                for (int j = 0; j < nu; ++j) Bs[lane * S.ldb + j] = E * V[P.uslot[j] * 32 + lane];
+            }
+            __syncwarp();
+            for (int e = lane; e < npairs; e += 32) {
+                const int pi = T.pi[e], pj = T.pj[e];
+                double acc = c0 == 0 ? 0.0 : G[e];
+                for (int r = 0; r < cnt; ++r) acc = fma(Bs[r * S.ldb + pi], Bs[r * S.ldb + pj], acc);
+                G[e] = acc;
+            }
+            __syncwarp();
+        }
+    }
+}
+
 // B for the tensor-core products: the SIMT Gram kernel's rows of B (u, E,
 // the monomial program, in the same operations), stored to bmat[slot][j][q]
 // in FP64, and for every column the exponent E_j with |B_qj| < 2^E_j (from
@@ -320,8 +384,12 @@ __global__ void __launch_bounds__(kQrWarps * 32) qr_kernel(AsmArgs a, Split S, i
     const int wib = threadIdx.x >> 5;
     const int wpc = blockDim.x >> 5;
     const int pidx = wib * PPW + sub;  // particle slot of this lane group in the CTA
-    double* R = smem + (size_t)pidx * S.pstride;
-    int* perm = reinterpret_cast<int*>(smem + (size_t)wpc * PPW * S.pstride) + pidx * S.nmax;
+    // work space: shared memory, or a global slot per lane group when the
+    // basis is too large for it (S.qws)
+    const int64_t gslot = ((int64_t)blockIdx.x * wpc + wib) * PPW + sub;
+    double* R = S.qws ? S.qws + gslot * S.pstride : smem + (size_t)pidx * S.pstride;
+    int* perm = S.qws ? S.qperm + gslot * S.nmax
+                      : reinterpret_cast<int*>(smem + (size_t)wpc * PPW * S.pstride) + pidx * S.nmax;
     const int ngroups = T.ngroups;
 
     for (int64_t w0 = ((int64_t)blockIdx.x * wpc + wib) * PPW; w0 < nb; w0 += (int64_t)gridDim.x * wpc * PPW) {
@@ -568,6 +636,12 @@ __global__ void __launch_bounds__(256) weights_kernel(AsmArgs a, Split S, int64_
 // ---------------------------------------------------------------- launches --
 int warps_of(const AsmArgs& a) { return (a.warps == 2 || a.warps == 8) ? a.warps : kWarps; }
 
+int smem_attr(cudaDeviceAttr attr, int fallback) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, attr, dev) != cudaSuccess) return fallback;
+    return v;
+}
+
 template <typename K>
 cudaError_t persistent(K kern, int threads, size_t bytes, int64_t work_per_cta, int64_t units, int& grid_out) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -596,9 +670,22 @@ cudaError_t launch_eps(const AsmArgs& a, const Split& S, int64_t b0, int64_t b1,
 
 template <int DIM, int NPP>
 cudaError_t launch_gram(const AsmArgs& a, const Split& S, int64_t b0, int64_t b1, cudaStream_t s) {
-    const int warps = warps_of(a);
-    const size_t bytes = (size_t)(kCh * S.ldb + S.nslots * 32) * sizeof(double) * warps;
-    auto kern = gram_kernel<DIM, NPP>;
+    int warps = warps_of(a);
+    const size_t per_warp = (size_t)(kCh * S.ldb + S.nslots * 32) * sizeof(double);
+    if constexpr (NPP == 0) {
+        // large bases: as many warps as their B chunks leave room for
+        const int fit = smem_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, 227 * 1024) / (int)per_warp;
+        warps = std::max(1, std::min(warps, fit));
+        const size_t bytes = per_warp * warps;
+        auto kern = gram_wide_kernel<DIM>;
+        int grid = 0;
+        cudaError_t e = persistent(kern, warps * 32, bytes, warps, b1 - b0, grid);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, warps * 32, bytes, s>>>(a, S, b0, b1);
+        return cudaGetLastError();
+    }
+    const size_t bytes = per_warp * warps;
+    auto kern = gram_kernel<DIM, NPP == 0 ? 1 : NPP>;
     int grid = 0;
     cudaError_t e = persistent(kern, warps * 32, bytes, warps, b1 - b0, grid);
     if (e != cudaSuccess) return e;
@@ -615,10 +702,19 @@ size_t qr_bytes(const Split& S, int lpp) {
     return (size_t)kQrWarps * (32 / lpp) * (qr_pstride(S, lpp) * sizeof(double) + S.nmax * sizeof(int));
 }
 
+// CTAs per SM of the QR with its work space in global memory (one warp and
+// one particle each)
+constexpr int kQrGlobalPerSm = 4;
+
 template <int LPP>
 cudaError_t launch_qr(const AsmArgs& a, Split S, int64_t nb, cudaStream_t s) {
     constexpr int PPW = 32 / LPP;
     S.pstride = qr_pstride(S, LPP);
+    if (S.qws) {
+        const int64_t grid = std::min<int64_t>((int64_t)num_sms() * kQrGlobalPerSm, nb);
+        qr_kernel<LPP><<<(unsigned)std::max<int64_t>(grid, 1), 32, 0, s>>>(a, S, nb);
+        return cudaGetLastError();
+    }
     const size_t bytes = qr_bytes(S, LPP);
     auto kern = qr_kernel<LPP>;
     int grid = 0;
@@ -630,20 +726,17 @@ cudaError_t launch_qr(const AsmArgs& a, Split S, int64_t nb, cudaStream_t s) {
 
 template <int DIM>
 cudaError_t launch_weights(const AsmArgs& a, const Split& S, int64_t b0, int64_t b1, cudaStream_t s) {
-    const int warps = warps_of(a);
-    const size_t bytes = (size_t)(S.cstride + (S.nslots + S.nout) * 32) * sizeof(double) * warps;
+    int warps = warps_of(a);
+    const size_t per_warp = (size_t)(S.cstride + (S.nslots + S.nout) * 32) * sizeof(double);
+    // large bases: as many warps as their coefficients and monomials leave room for
+    warps = std::max(1, std::min(warps, smem_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, 227 * 1024) / (int)per_warp));
+    const size_t bytes = per_warp * warps;
     auto kern = weights_kernel<DIM>;
     int grid = 0;
     cudaError_t e = persistent(kern, warps * 32, bytes, warps, b1 - b0, grid);
     if (e != cudaSuccess) return e;
     kern<<<grid, warps * 32, bytes, s>>>(a, S, b0, b1);
     return cudaGetLastError();
-}
-
-int smem_attr(cudaDeviceAttr attr, int fallback) {
-    int dev = 0, v = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, attr, dev) != cudaSuccess) return fallback;
-    return v;
 }
 
 // lanes per particle of the QR: the fewest that still leave >= 6 warps per SM
@@ -719,7 +812,8 @@ cudaError_t dispatch(const AsmArgs& a, const AsmTables& h, const Split& S, int l
     if (npp <= 7) return run<DIM, 7>(a, h, S, lpp, s);
     if (npp <= 8) return run<DIM, 8>(a, h, S, lpp, s);
     if (npp <= 16) return run<DIM, 16>(a, h, S, lpp, s);
-    return run<DIM, 40>(a, h, S, lpp, s);
+    if (npp <= 40) return run<DIM, 40>(a, h, S, lpp, s);
+    return run<DIM, 0>(a, h, S, lpp, s);  // the wide Gram kernel
 }
 
 Split make_split(const AsmTables& h, int flags) {
@@ -764,6 +858,13 @@ int64_t assembly_scratch_bytes(const AsmTables& h, int flags, int maxk) {
     if (assembly_uses_tc(h, flags, maxk))
         b += (int64_t)h.nu * tc_kpad(maxk) * (int64_t)sizeof(double) + 32 * (int64_t)sizeof(int32_t);
     return b;
+}
+
+int64_t assembly_qr_ws_bytes(const AsmTables& h, int flags) {
+    Split S = make_split(h, flags);
+    if (qr_bytes(S, 32) <= (size_t)smem_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, 227 * 1024)) return 0;
+    const int64_t slots = (int64_t)num_sms() * kQrGlobalPerSm;
+    return slots * ((int64_t)qr_pstride(S, 32) * (int64_t)sizeof(double) + (int64_t)S.nmax * (int64_t)sizeof(int));
 }
 
 int64_t binning_tmp_elems(int64_t n, int maxk, int width) {
@@ -824,9 +925,15 @@ cudaError_t assemble(const AsmArgs& a, const AsmTables& h, cudaStream_t s) {
     }
     int lpp = a.qr_lanes;
     if (lpp != 1 && lpp != 2 && lpp != 4 && lpp != 8 && lpp != 16 && lpp != 32) lpp = qr_lanes_auto(S);
-    // a lane grouping whose work space does not fit is refused before any launch
-    if (qr_bytes(S, lpp) > (size_t)smem_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, 227 * 1024))
+    if (a.qws) {
+        // large bases: one warp per particle, the work space in global memory
+        lpp = 32;
+        S.qws = a.qws;
+        S.qperm = reinterpret_cast<int*>(a.qws + (int64_t)num_sms() * kQrGlobalPerSm * qr_pstride(S, 32));
+    } else if (qr_bytes(S, lpp) > (size_t)smem_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, 227 * 1024)) {
+        // a lane grouping whose work space does not fit is refused before any launch
         return cudaErrorInvalidConfiguration;
+    }
     if (h.dim == 3) return dispatch<3>(a, h, S, lpp, s);
     if (h.dim == 2) return dispatch<2>(a, h, S, lpp, s);
     return dispatch<1>(a, h, S, lpp, s);

@@ -281,6 +281,8 @@ struct dcpse_plan_s {
     int asm_bin_width = 0, asm_warps = 4, asm_qr_lanes = 0;
     double* asm_scratch = nullptr;  // assembly batch scratch
     int64_t asm_scratch_bytes = 0;
+    double* qr_ws = nullptr;        // global QR work space of bases too large for shared memory
+    int64_t qr_ws_bytes = 0;
     int32_t* korder = nullptr;  // k-binned particle order of the current list
     int korder_width = 0;
     // transposed list and weight row sums (adjoint), built on demand
@@ -412,6 +414,8 @@ struct dcpse_plan_s {
         dfree(budget_count);
         dfree(asm_scratch);
         asm_scratch_bytes = 0;
+        dfree(qr_ws);
+        qr_ws_bytes = 0;
         dfree(rk_pack);
         rk_pack_n = 0;
         if (copy_stream) {
@@ -1237,6 +1241,14 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
             P->asm_scratch_bytes = bytes;
         }
         a.scratch = P->asm_scratch;
+        const int64_t qb = assembly_qr_ws_bytes(*P->htab, flags);
+        if (qb > 0 && P->qr_ws_bytes < qb) {
+            dfree(P->qr_ws);
+            P->qr_ws_bytes = 0;
+            DCPSE_CK(dalloc(&P->qr_ws, (size_t)(qb + 7) / 8));
+            P->qr_ws_bytes = qb;
+        }
+        a.qws = qb > 0 ? P->qr_ws : nullptr;
         a.scratch_particles = nb;
     }
     if (P->asm_bin_width > 0 && n > 0) {
@@ -1446,6 +1458,9 @@ int dcpse_vjp_positions(dcpse_plan_t* P, const double* d_pos, const double* d_ep
     if (int rc = check_single_set(P)) return rc;
     if (P->n < 0) return fail(DCPSE_ERR_STATE, "no neighbour list");
     if (P->n > 0 && (!d_pos || !d_f || !d_g || !d_grad)) return fail(DCPSE_ERR_ARG, "NULL array");
+    for (int g = 0; g < P->htab->ngroups; ++g)
+        if (P->htab->gn[g] > kMaxBasisSmall)
+            return fail(DCPSE_ERR_CAPACITY, "position VJP: bases of at most 35 functions");
     if (int rc = ensure_transpose(P)) return rc;
     if (!P->gentry) DCPSE_CK(dalloc(&P->gentry, (size_t)P->nnz * P->dim));
     VjpArgs a{};

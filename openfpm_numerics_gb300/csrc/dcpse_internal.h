@@ -65,15 +65,16 @@ cudaError_t fill_neighbors(const NbrArgs& a, const int64_t* rowptr, int32_t* tmp
 
 // --------------------------------------------------------------- assembly --
 // Tables describing the bases of a plan, resident on the device.
-constexpr int kMaxUnion = 64;    // distinct monomials over all bases
+constexpr int kMaxUnion = 128;   // distinct monomials over all bases
 constexpr int kMaxGroups = 4;    // distinct |alpha| among the terms
-constexpr int kMaxBasis = 35;    // basis size per group (3D order 4 = 34)
+constexpr int kMaxBasis = 120;   // basis size per group (3D |alpha| = 6, order 2: Laplace_Beltrami)
+constexpr int kMaxBasisSmall = 35;  // kernels with per-thread basis arrays (3D order 4 = 34)
 constexpr int kMaxTerms = 16;    // reference Dcpse objects per plan
 constexpr int kMaxOutputs = 8;
 constexpr int kMaxRhs = 8;       // right-hand sides per group
-constexpr int kMaxPairs = 1280;  // Gram entries (i <= j) needed by some group
+constexpr int kMaxPairs = 8256;  // Gram entries (i <= j) needed by some group (128 x 129 / 2)
 constexpr int kMaxExp = 8;       // highest exponent + 1
-constexpr int kMaxSlots = 192;   // monomial program: inputs, constant and products
+constexpr int kMaxSlots = 255;   // monomial program: inputs, constant and products (byte indices)
 
 struct AsmTables {
     int dim;
@@ -139,12 +140,16 @@ struct AsmArgs {
     double* scratch;      // assembly_scratch_bytes() per particle of a batch
     int64_t scratch_particles;  // batch size the scratch holds
     int* err;             // device error word (bounded waits of the tensor-core Gram)
+    double* qws;          // global QR work space for bases too large for shared memory, or nullptr
 };
 
 // Scratch bytes per particle of an assembly batch (Gram entries,
 // coefficients, the scaled offsets of its rows and a status word) for the
 // plan's tables and flags and the longest row maxk.
 int64_t assembly_scratch_bytes(const AsmTables& h, int flags, int maxk);
+// bytes of the global QR work space an assembly with these tables and flags
+// needs (0 when the QR's work space fits in shared memory)
+int64_t assembly_qr_ws_bytes(const AsmTables& h, int flags);
 
 // Particle order binned by neighbour count: bins of `width` counts
 // ascending (a counting sort on k / width); order[n], tmp sized by
