@@ -866,6 +866,10 @@ def gray_scott_run(args):
             gs.run(every)
         s.synchronize()
         ybar = (torch.zeros_like(gs.u), torch.ones_like(gs.v))
+        # warm-up call: the adjoint set-up, the kernels' first loads and the
+        # graph capture happen once; the timed call repeats the same window
+        gs.backward(ckpts, every, ybar, stream=s)
+        s.synchronize()
         ev0.record(s)
         ub, vb = gs.backward(ckpts, every, ybar, stream=s)
         ev1.record(s)

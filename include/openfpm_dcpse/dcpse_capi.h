@@ -312,6 +312,14 @@ int dcpse_rk4_gs_adjoint_prepare(dcpse_plan_t* plan, int precision);
 int dcpse_rk4_gs_adjoint_stage(dcpse_plan_t* plan, int precision, const void* Yu, const void* Yv, const void* kbu,
                                const void* kbv, const void* ybu, const void* ybv, void* accu, void* accv, void* next_u,
                                void* next_v, double cy, double cY, const double* params);
+/* One whole reverse RK4 step: ybar (ybu, ybv) of y_(n+1) is replaced by ybar
+ * of y_n, from the step's stage states stages = {Y1u, Y1v, Y2u, Y2v, Y3u,
+ * Y3v, Y4u, Y4v}; acc (accu, accv) is work space.  The same arithmetic as
+ * the four adjoint stages with their kbar scalings and copies, bit for bit,
+ * in five kernels (kbar kept as pairs, the accumulator started and handed
+ * back by the first and last stage).  No synchronisation or allocation. */
+int dcpse_rk4_gs_reverse_step(dcpse_plan_t* plan, int precision, const void* const* stages, void* ybu, void* ybv,
+                              void* accu, void* accv, const double* params);
 
 /* ---- batched FP32 apply that allocates nothing --------------------------
  * No counterpart in the reference.  For callers that must not allocate

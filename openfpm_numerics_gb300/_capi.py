@@ -62,6 +62,7 @@ SIGNATURES = {
     "dcpse_rk4_gs_stage": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _c.POINTER(_D)]),
     "dcpse_rk4_gs_adjoint_prepare": (_I, [_P, _I]),
     "dcpse_rk4_gs_adjoint_stage": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _D, _c.POINTER(_D)]),
+    "dcpse_rk4_gs_reverse_step": (_I, [_P, _I, _c.POINTER(_P), _P, _P, _P, _P, _c.POINTER(_D)]),
     "dcpse_device_alloc": (_I, [_PP, _c.c_uint64]),
     "dcpse_device_free": (_I, [_P]),
     "dcpse_host_alloc": (_I, [_PP, _c.c_uint64]),

@@ -1496,7 +1496,8 @@ static int ensure_rk_pack(dcpse_plan_t* P) {
     if (P->rk_pack_n < P->n) {
         dfree(P->rk_pack);
         P->rk_pack_n = 0;
-        DCPSE_CK(dalloc(&P->rk_pack, (size_t)std::max<int64_t>(P->n, 1) * 2));
+        // two areas of n pairs: stage input, and the fused reverse step's second kbar
+        DCPSE_CK(dalloc(&P->rk_pack, (size_t)std::max<int64_t>(P->n, 1) * 4));
         P->rk_pack_n = P->n;
     }
     return DCPSE_OK;
@@ -1626,6 +1627,70 @@ int dcpse_rk4_gs_adjoint_stage(dcpse_plan_t* P, int precision, const void* Yu, c
         return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
     }
     return DCPSE_OK;
+}
+
+int dcpse_rk4_gs_reverse_step(dcpse_plan_t* P, int precision, const void* const* stages, void* ybu, void* ybv,
+                              void* accu, void* accv, const double* params) {
+    if (int rc = check_plan(P)) return rc;
+    if (!params || !stages) return fail(DCPSE_ERR_ARG, "stages {Y1u,Y1v,...,Y4u,Y4v} and params {Du,Dv,F,k,dt}");
+    if (P->n > 0 && (!ybu || !ybv || !accu || !accv)) return fail(DCPSE_ERR_ARG, "NULL array");
+    for (int i = 0; i < 8 && P->n > 0; ++i)
+        if (!stages[i]) return fail(DCPSE_ERR_ARG, "NULL stage state");
+    if (P->rk_pack_n < P->n) return fail(DCPSE_ERR_STATE, "call dcpse_rk4_gs_adjoint_prepare first");
+    const int lanes = rk_lanes(P);
+    const double dt = params[4];
+    // kbar of stages 4..1 alternate between the two pair areas; the
+    // coefficients of the next kbar (RK4's weights 1/6, 1/3, 1/3, 1/6 and
+    // stage offsets 1, 1/2, 1/2)
+    const double cy[4] = {0.0, dt / 6.0, dt / 3.0, dt / 3.0}, cY[4] = {0.0, dt / 2.0, dt / 2.0, dt};
+    auto run = [&](auto tag) -> int {
+        typedef decltype(tag) T;
+        typedef typename std::conditional<std::is_same<T, float>::value, float, double>::type R;
+        const bool f32 = std::is_same<R, float>::value;
+        const R* wT = f32 ? (const R*)(const void*)P->wT32 : (const R*)(const void*)P->wT64;
+        const R* rs = f32 ? (const R*)(const void*)P->rs32 : (const R*)(const void*)P->rs64;
+        if (!wT || !rs) return fail(DCPSE_ERR_STATE, "call dcpse_rk4_gs_adjoint_prepare first");
+        void* area[2] = {P->rk_pack, P->rk_pack + 2 * P->rk_pack_n};
+        DCPSE_CK(rk_pack_scaled<R>((const R*)ybu, (const R*)ybv, P->n, dt / 6.0, area[0], P->stream));
+        for (int st = 3, cur = 0; st >= 0; --st, cur ^= 1) {
+            RkAdjArgs<R> a{};
+            a.n = P->n;
+            a.trow = P->t_row;
+            a.tsrc = P->t_src;
+            a.wT = wT;
+            a.rs = rs;
+            a.Yu = (const R*)stages[2 * st];
+            a.Yv = (const R*)stages[2 * st + 1];
+            a.ybu = (const R*)ybu;
+            a.ybv = (const R*)ybv;
+            a.accu = (R*)accu;
+            a.accv = (R*)accv;
+            a.cy = cy[st];
+            a.cY = cY[st];
+            a.Du = params[0];
+            a.Dv = params[1];
+            a.F = params[2];
+            a.K = params[3];
+            a.pack = area[cur];
+            a.kb_packed = true;
+            a.pack_out = st > 0 ? area[cur ^ 1] : nullptr;
+            a.acc_mode = st == 3 ? 1 : (st == 0 ? 2 : 0);
+            a.yb_out_u = (R*)ybu;
+            a.yb_out_v = (R*)ybv;
+            const int mode = P->apply_mode & 15;
+            if (f32 && (mode == 0 || mode == 4) && P->tsell_w) {
+                a.srow = P->tsell_row;
+                a.soff = P->tsell_off;
+                a.scols = P->tsell_cols;
+                a.sw = P->tsell_w;
+            }
+            DCPSE_CK(rk_adjoint_stage<R>(a, lanes, P->stream));
+        }
+        return DCPSE_OK;
+    };
+    if (precision == DCPSE_F32) return run(float{});
+    if (precision == DCPSE_F64) return run(double{});
+    return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32 or DCPSE_F64");
 }
 
 int dcpse_device_alloc(void** ptr, uint64_t bytes) {

@@ -420,11 +420,22 @@ struct RkAdjArgs {
     const int64_t* soff;
     const int32_t* scols;
     const float* sw;
+    // fused reverse step: the row's own kbar read from the pairs (kbu, kbv
+    // unused), the next kbar written as pairs to pack_out (next_u, next_v
+    // unused), and acc_mode 1: acc = ybar + Ybar, 2: ybar = acc + Ybar (in
+    // place; acc not written), 0: acc += Ybar
+    bool kb_packed;
+    void* pack_out;
+    int acc_mode;
+    T *yb_out_u, *yb_out_v;
 };
 template <typename T>
 cudaError_t rk_stage(const RkArgs<T>& a, int lanes, cudaStream_t s);
 template <typename T>
 cudaError_t rk_adjoint_stage(const RkAdjArgs<T>& a, int lanes, cudaStream_t s);
+// pairs (scale ybar_u, scale ybar_v) into pack: the kbar of a step's last stage
+template <typename T>
+cudaError_t rk_pack_scaled(const T* ybu, const T* ybv, int64_t n, double scale, void* pack, cudaStream_t s);
 template <typename T>
 cudaError_t rk_transpose_weights(const int64_t* rowptr, const int64_t* tidx, int64_t n, int64_t nnz, const T* w,
                                  T* wT, T* rs, cudaStream_t s);

@@ -188,6 +188,46 @@ __global__ void __launch_bounds__(256) gs_stage_sell_kernel(RkArgs<float> a, int
     }
 }
 
+// the end of an adjoint stage for row p, from the gathered lu = (W^T kbar_u)_p
+// and lv: Ybar of the stage, the accumulator, and the next stage's kbar
+template <typename T>
+__device__ __forceinline__ void adj_finish(const RkAdjArgs<T>& a, int64_t p, T lu, T lv) {
+    typedef typename Pair<T>::type P2;
+    T kbu, kbv;
+    if (a.kb_packed) {
+        const P2 kb = static_cast<const P2*>(a.pack)[p];
+        kbu = kb.x;
+        kbv = kb.y;
+    } else {
+        kbu = a.kbu[p];
+        kbv = a.kbv[p];
+    }
+    lu = lu - a.rs[p] * kbu;
+    lv = lv - a.rs[p] * kbv;
+    const T u = a.Yu[p], v = a.Yv[p];
+    const T Ybu = (T)a.Du * lu - (v * v + (T)a.F) * kbu + v * v * kbv;
+    const T Ybv = (T)a.Dv * lv - (T)2 * u * v * kbu + ((T)2 * u * v - (T)a.F - (T)a.K) * kbv;
+    if (a.acc_mode == 2) {
+        a.yb_out_u[p] = a.accu[p] + Ybu;
+        a.yb_out_v[p] = a.accv[p] + Ybv;
+    } else if (a.acc_mode == 1) {
+        a.accu[p] = a.ybu[p] + Ybu;
+        a.accv[p] = a.ybv[p] + Ybv;
+    } else {
+        a.accu[p] += Ybu;
+        a.accv[p] += Ybv;
+    }
+    if (a.pack_out) {
+        P2 nx;
+        nx.x = (T)a.cy * a.ybu[p] + (T)a.cY * Ybu;
+        nx.y = (T)a.cy * a.ybv[p] + (T)a.cY * Ybv;
+        static_cast<P2*>(a.pack_out)[p] = nx;
+    } else if (a.next_u) {
+        a.next_u[p] = (T)a.cy * a.ybu[p] + (T)a.cY * Ybu;
+        a.next_v[p] = (T)a.cy * a.ybv[p] + (T)a.cY * Ybv;
+    }
+}
+
 // adjoint stage: G lanes per particle over its transposed row, kbar of the
 // stage gathered as packed (u, v) pairs in 4-deep batches
 template <typename T, int G>
@@ -232,21 +272,7 @@ __global__ void __launch_bounds__(256) gs_adjoint_kernel(RkAdjArgs<T> a) {
             lu += __shfl_xor_sync(0xffffffffu, lu, m);
             lv += __shfl_xor_sync(0xffffffffu, lv, m);
         }
-        if (row < a.n && sub == 0) {
-            const int64_t p = row;
-            const T kbu = a.kbu[p], kbv = a.kbv[p];
-            lu = lu - a.rs[p] * kbu;
-            lv = lv - a.rs[p] * kbv;
-            const T u = a.Yu[p], v = a.Yv[p];
-            const T Ybu = (T)a.Du * lu - (v * v + (T)a.F) * kbu + v * v * kbv;
-            const T Ybv = (T)a.Dv * lv - (T)2 * u * v * kbu + ((T)2 * u * v - (T)a.F - (T)a.K) * kbv;
-            a.accu[p] += Ybu;
-            a.accv[p] += Ybv;
-            if (a.next_u) {
-                a.next_u[p] = (T)a.cy * a.ybu[p] + (T)a.cY * Ybu;
-                a.next_v[p] = (T)a.cy * a.ybv[p] + (T)a.cY * Ybv;
-            }
-        }
+        if (row < a.n && sub == 0) adj_finish<T>(a, row, lu, lv);
     }
 }
 
@@ -284,18 +310,7 @@ __global__ void __launch_bounds__(256) gs_adjoint_sell_kernel(RkAdjArgs<float> a
                 lv = fmaf(wq[u], y[u].y, lv);
             }
         }
-        const float kbu = a.kbu[p], kbv = a.kbv[p];
-        lu = lu - a.rs[p] * kbu;
-        lv = lv - a.rs[p] * kbv;
-        const float u = a.Yu[p], v = a.Yv[p];
-        const float Ybu = (float)a.Du * lu - (v * v + (float)a.F) * kbu + v * v * kbv;
-        const float Ybv = (float)a.Dv * lv - 2.f * u * v * kbu + (2.f * u * v - (float)a.F - (float)a.K) * kbv;
-        a.accu[p] += Ybu;
-        a.accv[p] += Ybv;
-        if (a.next_u) {
-            a.next_u[p] = (float)a.cy * a.ybu[p] + (float)a.cY * Ybu;
-            a.next_v[p] = (float)a.cy * a.ybv[p] + (float)a.cY * Ybv;
-        }
+        adj_finish<float>(a, p, lu, lv);
     }
 }
 
@@ -344,9 +359,30 @@ cudaError_t rk_stage(const RkArgs<T>& a, int lanes, cudaStream_t s) {
 }
 
 template <typename T>
+__global__ void pack_scaled_kernel(const T* __restrict__ u, const T* __restrict__ v, int64_t n, T scale,
+                                   typename Pair<T>::type* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        typename Pair<T>::type p;
+        p.x = u[i] * scale;
+        p.y = v[i] * scale;
+        out[i] = p;
+    }
+}
+
+template <typename T>
+cudaError_t rk_pack_scaled(const T* ybu, const T* ybv, int64_t n, double scale, void* pack, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    pack_scaled_kernel<T><<<grid_n(n, 256), 256, 0, s>>>(ybu, ybv, n, (T)scale,
+                                                          static_cast<typename Pair<T>::type*>(pack));
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t rk_adjoint_stage(const RkAdjArgs<T>& a, int lanes, cudaStream_t s) {
     if (a.n == 0) return cudaSuccess;
-    pack_kernel<T><<<grid_n(a.n, 256), 256, 0, s>>>(a.kbu, a.kbv, a.n, static_cast<typename Pair<T>::type*>(a.pack));
+    // the stage's kbar as pairs (already so in a fused reverse step)
+    if (!a.kb_packed)
+        pack_kernel<T><<<grid_n(a.n, 256), 256, 0, s>>>(a.kbu, a.kbv, a.n, static_cast<typename Pair<T>::type*>(a.pack));
     if constexpr (std::is_same<T, float>::value) {
         if (a.srow) {
             const int64_t nwin = (a.n + 255) / 256;
@@ -375,6 +411,8 @@ template cudaError_t rk_stage<float>(const RkArgs<float>&, int, cudaStream_t);
 template cudaError_t rk_stage<double>(const RkArgs<double>&, int, cudaStream_t);
 template cudaError_t rk_adjoint_stage<float>(const RkAdjArgs<float>&, int, cudaStream_t);
 template cudaError_t rk_adjoint_stage<double>(const RkAdjArgs<double>&, int, cudaStream_t);
+template cudaError_t rk_pack_scaled<float>(const float*, const float*, int64_t, double, void*, cudaStream_t);
+template cudaError_t rk_pack_scaled<double>(const double*, const double*, int64_t, double, void*, cudaStream_t);
 template cudaError_t rk_transpose_weights<float>(const int64_t*, const int64_t*, int64_t, int64_t, const float*,
                                                  float*, float*, cudaStream_t);
 template cudaError_t rk_transpose_weights<double>(const int64_t*, const int64_t*, int64_t, int64_t, const double*,

@@ -118,9 +118,17 @@ class GrayScottRK4:
         self._adj_stage(stages[0], k_b, ybar, acc, None, 0.0, 0.0)           # Ybar1
         return acc
 
-    def _reverse_step_into(self, stages, yb, acc, k_a, k_b):
+    def _reverse_step_into(self, stages, yb, acc, k_a=None, k_b=None):
         """reverse_step with preallocated buffers: yb (ybar of y_{n+1}) is
-        replaced by ybar of y_n."""
+        replaced by ybar of y_n (one fused call: the four adjoint stages with
+        their kbar scalings and copies; k_a and k_b are not needed)."""
+        ptrs = (ctypes.c_void_p * 8)(*[_vp(stages[st][sp]) for st in range(4) for sp in range(2)])
+        C.call("dcpse_rk4_gs_reverse_step", self.plan._h, self.prec, ptrs, _vp(yb[0]), _vp(yb[1]), _vp(acc[0]),
+               _vp(acc[1]), self.params)
+
+    def _reverse_step_stages(self, stages, yb, acc, k_a, k_b):
+        """The same reverse step as four separate adjoint stages (reference
+        for the fused call)."""
         dt = self.dt
         acc[0].copy_(yb[0])
         acc[1].copy_(yb[1])

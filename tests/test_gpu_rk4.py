@@ -181,3 +181,25 @@ def test_graph_backward_equals_eager(cuda):
         graph = gs.backward(ckpts, 4, ybar, stream=s)
     s.synchronize()
     assert torch.equal(eager[0], graph[0]) and torch.equal(eager[1], graph[1])
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_fused_reverse_step_equals_stages(cuda, dtype):
+    """dcpse_rk4_gs_reverse_step (the four adjoint stages in five kernels,
+    kbar kept as pairs) gives the separate stages' ybar bit for bit."""
+    plan, u, v, dt = _setup(16, dtype)
+    gs = GrayScottRK4(plan, u, v, P["Du"], P["Dv"], P["F"], P["k"], dt)
+    gs.run(3)
+    gs.prepare_adjoint()
+    hist = [(torch.empty_like(gs.u), torch.empty_like(gs.v)) for _ in range(4)]
+    gs.step(record=hist)
+    g = torch.Generator(device="cuda").manual_seed(7)
+    yb0 = (torch.rand(gs.u.shape, generator=g, device="cuda", dtype=dtype),
+           torch.rand(gs.v.shape, generator=g, device="cuda", dtype=dtype))
+    bufs = [(torch.empty_like(gs.u), torch.empty_like(gs.v)) for _ in range(3)]
+    ref = (yb0[0].clone(), yb0[1].clone())
+    gs._reverse_step_stages(hist, ref, *bufs)
+    got = (yb0[0].clone(), yb0[1].clone())
+    gs._reverse_step_into(hist, got, bufs[0])
+    torch.cuda.synchronize()
+    assert torch.equal(got[0], ref[0]) and torch.equal(got[1], ref[1])
