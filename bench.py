@@ -734,9 +734,9 @@ def extra_adjoint(args, pos2, rcut2):
 
 def extra_shuffled(args, pos_np, rcut, f_np, res32):
     """The benchmark set in a seeded random particle order (seed 11): the
-    apply's sliced layout is renumbered by the particles' cell order, so the
-    field gathers stay local whatever the caller's order; outputs come back
-    in the caller's order."""
+    apply's sliced layout is renumbered (row-major order at the mean spacing,
+    and the Z-order of the list's cells), so the field gathers stay local
+    whatever the caller's order; outputs come back in the caller's order."""
     import torch
 
     from openfpm_numerics_gb300 import _capi as C
@@ -749,15 +749,20 @@ def extra_shuffled(args, pos_np, rcut, f_np, res32):
     stream = torch.cuda.current_stream()
     pos = torch.tensor(sp, device="cuda")
     f = torch.tensor(np.ascontiguousarray(f_np[perm]), device="cuda")
-    plan = DcpsePlan(3, W.grad_lap_outputs(3), order=2, stream=stream)
-    plan.set_timing(True)
-    plan.build_neighbors(pos, rcut)
-    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
     out = torch.empty((NOUT, N), dtype=torch.float64, device="cuda")
-    nnz = plan.info()["nnz"]
     hbm, _ = peaks()
-    res = {"reorder": plan.reorder_info()}
-    for label, pol in (("cell_order", 0), ("caller_order", -1)):
+    res = {}
+    for label, order, pol in (("row_major_order", 1, 0), ("cell_order", 0, 0), ("caller_order", 0, -1)):
+        if label != "caller_order":
+            if label != "row_major_order":
+                plan.close()
+            plan = DcpsePlan(3, W.grad_lap_outputs(3), order=2, stream=stream)
+            plan.set_timing(True)
+            plan.set_reorder_order(order)
+            plan.build_neighbors(pos, rcut)
+            plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32)
+            nnz = plan.info()["nnz"]
+            res["reorder_" + label] = plan.reorder_info()
         plan.set_reorder(pol)
         for _ in range(5):
             plan.apply(f, C.F32, out)
@@ -770,7 +775,7 @@ def extra_shuffled(args, pos_np, rcut, f_np, res32):
         b = W.apply_bytes(N, nnz, NOUT, 4)
         res[label] = {"kernel_ms": t * 1e3, "split_ms": sm / max(sn, 1), "achieved_gbs": b / t / 1e9,
                       "frac": b / t / 1e9 / hbm, "renumbered": plan.reorder_info()[0]}
-        if pol == 0:
+        if label == "cell_order":
             o = out.cpu().numpy()
             res["fp32_vs_ordered_fp32_normwise"] = max(rel_err(o[k], res32[k][perm]) for k in range(NOUT))
     plan.check()

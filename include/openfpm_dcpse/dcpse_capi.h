@@ -246,6 +246,10 @@ int dcpse_plan_budget_stats(dcpse_plan_t* plan, int64_t* pairs_corrected, int re
  * (CSR kernels) on a renumbered layout.  Changing the policy rebuilds the
  * layout. */
 int dcpse_plan_set_reorder(dcpse_plan_t* plan, int policy);
+/* The renumbering order the next dcpse_build_neighbors computes: 0 (default)
+ * the Z-order of the list's cells, 1 row-major order of a grid at the
+ * particles' mean spacing.  No counterpart in the reference. */
+int dcpse_plan_set_reorder_order(dcpse_plan_t* plan, int order);
 /* Whether the current layout is renumbered, and the mean |q - p| of the
  * list's entries in the caller's numbering and in the cell order (0 when no
  * cell order is known: caller-built lists, two sets, surface operators). */

@@ -51,6 +51,7 @@ SIGNATURES = {
     "dcpse_plan_set_error_budget": (_I, [_P, _D, _I]),
     "dcpse_plan_budget_stats": (_I, [_P, _PI64, _I]),
     "dcpse_plan_set_reorder": (_I, [_P, _I]),
+    "dcpse_plan_set_reorder_order": (_I, [_P, _I]),
     "dcpse_plan_reorder_info": (_I, [_P, _PI, _c.POINTER(_D), _c.POINTER(_D)]),
     "dcpse_apply_batched_f32_noalloc": (_I, [_I64, _I, _P, _P, _P, _I64, _P, _P, _P]),
     "dcpse_p2p_f64": (_I, [_P, _I, _P, _I, _P]),

@@ -340,10 +340,11 @@ struct dcpse_plan_s {
     double* hout = nullptr;  // device outputs for host apply, nout * hf_len values
     int64_t hf_len = 0;      // particles hf and hout were sized for (the list may change n)
 
-    // cell order of the particles from the neighbour build (one set only):
-    // cell_order[k] = the particle in position k
+    // Z-order of the particles' cells from the neighbour build (one set
+    // only): cell_order[k] = the particle in position k
     int32_t* cell_order = nullptr;
     int reorder = 0;  // -1: keep the list's numbering, 0: automatic, 1: cell order
+    int reorder_order = 0;  // the renumbering order built with the list (0 Z-order of cells, 1 row-major)
     // the FP32 output weights on the sliced ELL layout (built on first use);
     // with sell_perm the layout is in cell order (sell_perm = cell_order,
     // sell_inv its inverse)
@@ -1086,10 +1087,26 @@ int dcpse_build_neighbors(dcpse_plan_t* P, const double* d_pos, int64_t n, doubl
     P->tstop(DCPSE_K_NEIGHBORS);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e == cudaSuccess && !other_support) {
-        // the cell order of the particles (one set): the apply's sliced
-        // layout may renumber rows and columns by it
-        P->cell_order = cidx;
-        cidx = nullptr;
+        // the particles' renumbering order (one set; P->reorder_order): the
+        // apply's sliced layout may renumber rows and columns by it (the
+        // cells' own order, if the order's work space cannot be had)
+        int32_t *key = nullptr, *zord = nullptr;
+        int64_t* ztmp = nullptr;
+        cudaError_t ez = dalloc(&key, (size_t)std::max<int64_t>(ns, 1));
+        if (ez == cudaSuccess) ez = dalloc(&zord, (size_t)std::max<int64_t>(ns, 1));
+        if (ez == cudaSuccess) ez = dalloc(&ztmp, (size_t)order_tmp_elems(dim, ns, cg, P->reorder_order));
+        if (ez == cudaSuccess) ez = particle_order(dim, ps, ns, cg, P->reorder_order, key, ztmp, zord, s);
+        if (ez == cudaSuccess) ez = cudaStreamSynchronize(s);
+        dfree(key);
+        dfree(ztmp);
+        if (ez == cudaSuccess) {
+            P->cell_order = zord;
+        } else {
+            dfree(zord);
+            cudaGetLastError();
+            P->cell_order = cidx;
+            cidx = nullptr;
+        }
     }
     cleanup();
     if (e != cudaSuccess) return fail(DCPSE_ERR_CUDA, std::string("neighbour build: ") + cudaGetErrorString(e));
@@ -2196,6 +2213,13 @@ int dcpse_plan_set_reorder(dcpse_plan_t* P, int policy) {
         if (had && P->assembled)
             if (int rc = ensure_sell(P)) return rc;
     }
+    return DCPSE_OK;
+}
+
+int dcpse_plan_set_reorder_order(dcpse_plan_t* P, int order) {
+    if (int rc = check_plan(P)) return rc;
+    if (order < 0 || order > 1) return fail(DCPSE_ERR_ARG, "order must be 0 (Z-order of cells) or 1 (row-major)");
+    P->reorder_order = order;  // used by the next neighbour build
     return DCPSE_OK;
 }
 

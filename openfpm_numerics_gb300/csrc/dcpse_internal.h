@@ -33,6 +33,16 @@ cudaError_t bounding_box(int dim, const double* a, int64_t na, const double* b, 
 // (positions in cell order) and srel[n] (FP32 offsets from the cell's lower
 // corner, NaN for particles outside the grid).  d_cell (n) and d_fill
 // (ncell) are scratch.
+// Particles in a renumbering order for the apply's layout: mode 0, the
+// Z-order (Morton order) of their cells (cell coordinates coarsened so that
+// a key has at most kOrderKeyBits bits), whose windows of consecutive rows
+// cover compact blocks of cells; mode 1, row-major order of a grid at the
+// particles' mean spacing (close to a jittered lattice's own order).
+// tmp: order_tmp_elems() int64; key: n int32.
+constexpr int kOrderKeyBits = 23;
+int64_t order_tmp_elems(int dim, int64_t n, const CellGrid& g, int mode);
+cudaError_t particle_order(int dim, const double* pos, int64_t n, const CellGrid& g, int mode, int32_t* key,
+                           int64_t* tmp, int32_t* order, cudaStream_t s);
 cudaError_t build_cells(int dim, const double* pos, int64_t n, const CellGrid& g, int32_t* d_cell,
                         int32_t* d_ccount, int64_t* d_cstart, int64_t* d_fill, int32_t* d_cidx, double* d_spos,
                         float4* d_srel, int64_t* d_scan_tmp, cudaStream_t s);

@@ -764,6 +764,104 @@ cudaError_t build_cells(int dim, const double* pos, int64_t n, const CellGrid& g
     return cudaGetLastError();
 }
 
+// Renumbering keys.  Z-order (Morton) of a particle's cell: the bits of the
+// cell coordinates, shifted right by `shift`, interleaved (axis 0 lowest).
+// Row-major: the index of its cell in a grid whose side is the particles'
+// mean spacing, axis 0 fastest (on a jittered lattice close to the lattice's
+// own order, whose consecutive rows share their neighbour offsets).
+struct OrderGrid {
+    int mode;                 // 0 Z-order of the list's cells, 1 row-major at the mean spacing
+    int bits, shift;          // Z-order
+    double lo[kMaxDim], cs[kMaxDim];
+    int nc[kMaxDim];          // row-major grid
+};
+
+__device__ __forceinline__ int32_t order_key(const double* x, int dim, const CellGrid& g, const OrderGrid& o) {
+    int32_t k = 0;
+    if (o.mode == 0) {
+        int c[kMaxDim] = {0, 0, 0};
+        for (int d = 0; d < dim; ++d) c[d] = cell_coord(x[d], g.lo[d], g.cs[d], g.nc[d]);
+        for (int b = 0; b < o.bits; ++b)
+            for (int d = 0; d < dim; ++d) k |= ((c[d] >> (o.shift + b)) & 1) << (b * dim + d);
+    } else {
+        for (int d = dim - 1; d >= 0; --d) k = k * o.nc[d] + cell_coord(x[d], o.lo[d], o.cs[d], o.nc[d]);
+    }
+    return k;
+}
+
+__global__ void order_key_kernel(int dim, const double* __restrict__ pos, int64_t n, CellGrid g, OrderGrid o,
+                                 int32_t* __restrict__ key, int32_t* __restrict__ hist) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double x[kMaxDim] = {0.0, 0.0, 0.0};
+        for (int d = 0; d < dim; ++d) x[d] = pos[i * dim + d];
+        const int32_t k = order_key(x, dim, g, o);
+        key[i] = k;
+        atomicAdd(&hist[k], 1);
+    }
+}
+
+__global__ void order_scatter_kernel(const int32_t* __restrict__ key, int64_t n, int64_t* fill,
+                                     int32_t* __restrict__ order) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        order[atomicAdd((unsigned long long*)&fill[key[i]], 1ull)] = (int32_t)i;
+}
+
+// the key grid of a renumbering order, and its number of keys
+OrderGrid order_grid(int dim, int64_t n, const CellGrid& g, int mode, int64_t* nkeys) {
+    OrderGrid o{};
+    o.mode = mode;
+    if (mode == 0) {
+        int bits = 0;
+        for (int d = 0; d < dim; ++d)
+            while ((1 << bits) < g.nc[d]) ++bits;
+        const int cap = kOrderKeyBits / std::max(dim, 1);
+        o.shift = bits > cap ? bits - cap : 0;
+        o.bits = std::min(bits, cap);
+        *nkeys = (int64_t)1 << (dim * o.bits);
+        return o;
+    }
+    double vol = 1.0;
+    for (int d = 0; d < dim; ++d) vol *= g.nc[d] * g.cs[d];
+    double side = std::pow(vol / (double)std::max<int64_t>(n, 1), 1.0 / dim);
+    for (;;) {
+        int64_t total = 1;
+        for (int d = 0; d < dim; ++d) {
+            o.lo[d] = g.lo[d];
+            o.nc[d] = std::max(1, (int)std::ceil(g.nc[d] * g.cs[d] / side));
+            o.cs[d] = g.nc[d] * g.cs[d] / o.nc[d];
+            total *= o.nc[d];
+        }
+        if (total <= ((int64_t)1 << kOrderKeyBits)) {
+            *nkeys = total;
+            return o;
+        }
+        side *= 1.25;
+    }
+}
+
+int64_t order_tmp_elems(int dim, int64_t n, const CellGrid& g, int mode) {
+    int64_t nkeys = 0;
+    order_grid(dim, n, g, mode, &nkeys);
+    return 3 * nkeys + scan_tmp_elems(nkeys) + 1;
+}
+
+cudaError_t particle_order(int dim, const double* pos, int64_t n, const CellGrid& g, int mode, int32_t* key,
+                           int64_t* tmp, int32_t* order, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    int64_t nkeys = 0;
+    const OrderGrid o = order_grid(dim, n, g, mode, &nkeys);
+    int32_t* hist = reinterpret_cast<int32_t*>(tmp);  // nkeys int32 in the first nkeys int64
+    int64_t* starts = tmp + nkeys;                     // nkeys + 1
+    int64_t* scan_tmp = starts + nkeys + 1;
+    cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(int32_t) * nkeys, s);
+    if (e != cudaSuccess) return e;
+    order_key_kernel<<<grid_for(n, 256), 256, 0, s>>>(dim, pos, n, g, o, key, hist);
+    e = exclusive_scan_i32(hist, nkeys, starts, scan_tmp, s);
+    if (e != cudaSuccess) return e;
+    order_scatter_kernel<<<grid_for(n, 256), 256, 0, s>>>(key, n, starts, order);
+    return cudaGetLastError();
+}
+
 cudaError_t count_neighbors(const NbrArgs& a, int32_t* counts, int* d_maxk, cudaStream_t s) {
     if (a.n_dom == 0) return cudaSuccess;
     int grid = grid_for(a.n_dom * 32, 256);

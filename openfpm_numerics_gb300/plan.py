@@ -294,6 +294,12 @@ class DcpsePlan:
         cell order, -1 never."""
         C.call("dcpse_plan_set_reorder", self._h, int(policy))
 
+    def set_reorder_order(self, order=0):
+        """The renumbering order the next build_neighbors computes: 0 the
+        Z-order of the list's cells, 1 row-major order of a grid at the
+        particles' mean spacing."""
+        C.call("dcpse_plan_set_reorder_order", self._h, int(order))
+
     def reorder_info(self):
         """(renumbered, mean |q - p| in the caller's numbering, the same in
         the cell order)."""

@@ -22,9 +22,10 @@ pytestmark = pytest.mark.gpu
 FLAGS = (C.ASSEMBLE_FAST | C.STORE_OUT_F64 | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID | C.STORE_OUT_F32_CORR)
 
 
-def _plan(pos, h, policy):
+def _plan(pos, h, policy, order=0):
     plan = DcpsePlan(3, W.grad_lap_outputs(3), order=2)
     plan.set_reorder(policy)
+    plan.set_reorder_order(order)
     pt = torch.tensor(pos, device="cuda")
     plan.build_neighbors(pt, 2.8 * h)
     plan.assemble(pt, FLAGS)
@@ -55,6 +56,20 @@ def test_shuffled_set_is_renumbered_and_bit_identical(shuffled):
     assert torch.equal(auto.apply(f, C.F32_BUDGET), keep.apply(f, C.F32_BUDGET))
     auto.close()
     keep.close()
+
+
+def test_renumbering_orders_agree(shuffled):
+    """The row-major renumbering (a grid at the mean spacing) gives the Z-order
+    renumbering's outputs bit for bit: each row keeps its list order."""
+    pos, h, _ = shuffled
+    z = _plan(pos, h, 1, 0)
+    r = _plan(pos, h, 1, 1)
+    assert z.reorder_info()[0] and r.reorder_info()[0]
+    f = torch.tensor(W.field2(pos)[0], device="cuda")
+    for prec in (C.F32, C.F32_RESID, C.F64):
+        assert torch.equal(z.apply(f, prec).clone(), r.apply(f, prec).clone()), prec
+    z.close()
+    r.close()
 
 
 def test_shuffled_matches_ordered_set(shuffled):
