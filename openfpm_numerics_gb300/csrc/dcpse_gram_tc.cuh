@@ -369,11 +369,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             // for nu <= 24)
             const uint32_t acc = tmem + (uint32_t)g * kTcAccCols + lanes;
 #pragma unroll 1
+            // the quarter's batches of both row blocks alternate between its two warps
+            int batch = 0;
             for (int half = 0; half < 2; ++half) {
                 if (half && !n2) break;
                 const int i = i1 + 16 * half, j0 = 4 * ew + 16 * half;
                 const uint32_t c0 = half ? n1 : 0u;
-                for (int jb = j0 + 4 * part; jb < nu; jb += 8) {  // warp-uniform: from the quarter's smallest i
+                for (int jb = j0; jb < nu; jb += 4) {  // warp-uniform: from the quarter's smallest i
+                    if ((batch++ & 1) != part) continue;
                     uint32_t r[32];
                     tc_ld32(acc + c0 + (uint32_t)(8 * (jb - 16 * half)), r);
 #pragma unroll
