@@ -322,8 +322,10 @@ def run_ours(args):
     tc_vs_fp64_gram = float(max(((out_tc[o] - out_fast[o]).abs().max() / out_fast[o].abs().max()).item()
                                 for o in range(NOUT)))
     del out_tc, out_fast
-    # the same with the residual streams of the corrected FP32 applies
-    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID | C.STORE_OUT_F32_CORR)
+    # the same with the residual streams of the corrected FP32 applies (and
+    # the FP64 weights, the yardstick of the weight pairs' apply)
+    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F32_RESID | C.STORE_OUT_F32_CORR |
+                  C.STORE_OUT_F64)
 
     # schedule autotuning (untimed): lanes per row x direct / TMA-staged loads
     from openfpm_numerics_gb300 import autotune
@@ -345,6 +347,26 @@ def run_ours(args):
     torch.cuda.synchronize()
     t_resid = ev0.elapsed_time(ev1) / 1e3 / nplain
     resr = outr.cpu().numpy()
+
+    # FP32 weight pairs with the fixed-point field (FP64-class results off the
+    # FP64 pipe), against the batched FP64 apply of the same weights
+    outp = torch.empty((NOUT, N), dtype=torch.float64, device=dev)
+    for _ in range(3):
+        plan.apply(f, C.F32_PAIR, outp)
+    plan.reset_timing()
+    ev0.record(stream)
+    for _ in range(nplain):
+        plan.apply(f, C.F32_PAIR, outp)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_pair = ev0.elapsed_time(ev1) / 1e3 / nplain
+    pair_k = plan.timing(C.K_APPLY_BATCHED)
+    resp = outp.cpu().numpy()
+    plan.apply(f, C.F64, outp)
+    b64_fast = outp.cpu().numpy()
+    pair_vs_b64 = max(rel_err(resp[o], b64_fast[o]) for o in range(NOUT))
+    b64_fast_vs_ref = max(rel_err(b64_fast[o], ref_out[o]) for o in range(NOUT))
+    del outp, b64_fast
 
     # budget-driven FP32 (rows whose FP32 error bound exceeds 1e-6 corrected
     # toward the FP64 weights; FP32 first pass); kernel times from the plan's
@@ -419,6 +441,8 @@ def run_ours(args):
         "fp32_resid_vs_fp64_reference_order_normwise": max(rel_err(resr[o], ref_out[o]) for o in range(NOUT)),
         "fp32_budget_vs_fp64_reference_order_normwise": max(rel_err(resg[o], ref_out[o]) for o in range(NOUT)),
         "fp64_batched_vs_reference_order_normwise": max(rel_err(b64[o], ref_out[o]) for o in range(NOUT)),
+        "fp32_pair_vs_fp64_reference_order_normwise": max(rel_err(resp[o], ref_out[o]) for o in range(NOUT)),
+        "fp32_pair_vs_fp64_batched_same_weights_normwise": pair_vs_b64,
         "fp64_analytic_interior_normwise": [rel_err(ref_out[o][inner], analytic[o][inner]) for o in range(NOUT)],
         "fp32_analytic_interior_normwise": [rel_err(res32[o][inner], analytic[o][inner]) for o in range(NOUT)],
         "definition": "max|a-b| / max|b| per output, max over the 4 outputs",
@@ -507,6 +531,15 @@ def run_ours(args):
             "fp64_plain": {"value": N * NOUT / t_plain / 1e9, "ms_per_step": t_plain * 1e3,
                            "note": "one pass per reference Dcpse object (6), reference order"},
             "fp64_batched": {"value": N * NOUT / t_b64 / 1e9, "ms_per_step": t_b64 * 1e3},
+            "fp32_pair": {"value": N * NOUT / t_pair / 1e9, "ms_per_step": t_pair * 1e3,
+                          "kernel_ms": pair_k[0] / max(pair_k[1], 1),
+                          "hbm_frac": W.apply_bytes(N, nnz, NOUT, 8, fbytes=8, obytes=8) /
+                                      (pair_k[0] / 1e3 / max(pair_k[1], 1)) / 1e9 / hbm,
+                          "error_vs_fp64_batched_same_weights": pair_vs_b64,
+                          "error_vs_fp64_reference_order": errors["fp32_pair_vs_fp64_reference_order_normwise"],
+                          "fp64_batched_same_weights_vs_reference_order": b64_fast_vs_ref,
+                          "note": "DCPSE_F32_PAIR: FP32 weight pairs (8 B/entry/output), field in 62-bit "
+                                  "fixed point, compensated FP32 sums"},
             "fp32_resid": {"value": N * NOUT / t_resid / 1e9, "ms_per_step": t_resid * 1e3,
                            "note": "FP32 weights + bf16 residual stream (2 B/entry/output)"},
             "fp32_budget": {"value": N * NOUT / t_budget / 1e9, "ms_per_step": t_budget * 1e3,

@@ -208,7 +208,7 @@ public:
     // operand: getV<i>(parts).  By default every output is the reference's
     // own sum of its Dcpse terms in FP64, in the reference's order (one pass
     // per term).  After set_apply_precision(DCPSE_F32 / DCPSE_F32_RESID /
-    // DCPSE_F32_BUDGET) all outputs come from one batched pass over the
+    // DCPSE_F32_BUDGET / DCPSE_F32_PAIR) all outputs come from one batched pass over the
     // summed weights (see dcpse_capi.h), through pinned staging buffers.
     template <unsigned int prp, typename vector_type>
     Expr operator()(PropRef<prp, vector_type> arg) {
@@ -240,9 +240,9 @@ public:
     void set_apply_precision(int precision) {
         int flags = DCPSE_STORE_TERMS_F64 | DCPSE_STORE_OUT_F32;
         if (precision == DCPSE_F32_RESID) flags |= DCPSE_STORE_OUT_F32_RESID;
-        if (precision == DCPSE_F32_BUDGET) flags |= DCPSE_STORE_OUT_F32_CORR;
+        if (precision == DCPSE_F32_BUDGET || precision == DCPSE_F32_PAIR) flags |= DCPSE_STORE_OUT_F32_CORR;
         if (precision != DCPSE_F64 && precision != DCPSE_F32 && precision != DCPSE_F32_RESID &&
-            precision != DCPSE_F32_BUDGET)
+            precision != DCPSE_F32_BUDGET && precision != DCPSE_F32_PAIR)
             throw std::invalid_argument("DC-PSE operator: unknown precision");
         if ((flags | asm_flags_) != asm_flags_) {
             asm_flags_ |= flags;

@@ -57,11 +57,11 @@ extern "C" {
 #define DCPSE_STORE_OUT_F32_RESID 32 /* also bf16 residuals w64 - w32 of the FP32 weights */
 #define DCPSE_STORE_OUT_F32_CORR 64  /* also FP32 residuals w64 - w32 (for DCPSE_F32_BUDGET) */
 #define DCPSE_ASSEMBLE_TC 128   /* with DCPSE_ASSEMBLE_FAST: the Gram products B^T B on the tensor
-                                   cores (tcgen05), from a 56-bit fixed-point B: not bit-identical
-                                   to the sequential FP64 sums, within their order sensitivity;
-                                   taken when the union basis has <= 32 functions and no row has
-                                   more than 112 neighbours, else the FP64 kernel serves
-                                   (dcpse_plan_assembly_info tells which) */
+                                   cores (tcgen05), from a 62-bit fixed-point B: not bit-identical
+                                   to the sequential FP64 sums, closer to the correctly rounded
+                                   Gram than they are; taken when the union basis has <= 24
+                                   functions and no row has more than 128 neighbours, else the
+                                   FP64 kernel serves (dcpse_plan_assembly_info tells which) */
 
 /* precision of dcpse_apply_batched */
 #define DCPSE_F64 0
@@ -69,6 +69,13 @@ extern "C" {
 #define DCPSE_F32_RESID 2 /* FP32 weights + bf16 residual correction (near-FP64 accuracy) */
 #define DCPSE_F32_BUDGET 3 /* FP32 weights, then an FP64 residual correction of exactly the
                               rows whose FP32 error bound exceeds the plan's error budget */
+#define DCPSE_F32_PAIR 4   /* weights as FP32 pairs w32 + (w64 - w32) (48 bits), the field in 62-bit
+                              fixed point (one power-of-two scale from the call's largest |f|: exact
+                              differences f_q - f_p), compensated FP32 sums: FP64-class results
+                              (<= 1e-12 normwise) at the FP64 weights' bytes, off the FP64 pipe.
+                              A NaN or an infinity in the field makes every output NaN.  Needs
+                              DCPSE_STORE_OUT_F32 | DCPSE_STORE_OUT_F32_CORR; without the sliced
+                              layout the batched FP64 apply serves.  Batched applies only. */
 
 typedef struct dcpse_plan_s dcpse_plan_t;
 

@@ -102,6 +102,7 @@ F64 = 0
 F32 = 1
 F32_RESID = 2
 F32_BUDGET = 3
+F32_PAIR = 4
 
 PART_OK, PART_TOO_FEW, PART_BAD_EPS, PART_SINGULAR, PART_NONFINITE = range(5)
 

@@ -326,6 +326,7 @@ struct dcpse_plan_s {
     // apply scratch
     float2* f2 = nullptr;
     int64_t f2_len = 0;
+    long long* fx_meta = nullptr;  // [2] of the fixed-point field (the weight pairs' apply)
     // host-buffer applies: the field arrives in pieces on h2d_stream, row
     // chunks start once the pieces they read have arrived, and their outputs
     // go back on copy_stream while later chunks run
@@ -358,6 +359,7 @@ struct dcpse_plan_s {
     int32_t* sell_cols = nullptr;
     float* sell_w = nullptr;
     void* sell_r = nullptr;  // bf16 residuals on the same layout (with r16)
+    float* sell_r32 = nullptr;  // FP32 residuals on the same layout (with r32: the weight pairs)
     double* sell_w64 = nullptr;  // FP64 summed weights on the same layout (with w64)
     int64_t sell_total = 0;
     bool sell_no_room = false;  // the copy did not fit in device memory: CSR kernels only
@@ -373,6 +375,7 @@ struct dcpse_plan_s {
         dfree(sell_w64);
         if (sell_r) cudaFree(sell_r);
         sell_r = nullptr;
+        dfree(sell_r32);
         sell_total = 0;
         sell_no_room = false;
     }
@@ -406,6 +409,7 @@ struct dcpse_plan_s {
         dfree(cols);
         dfree(cell_order);
         dfree(f2);
+        dfree(fx_meta);
         dfree(hf);
         dfree(hout);
         hf_len = 0;
@@ -639,6 +643,24 @@ int split_into_plan(dcpse_plan_t* P, const double* d_f, int64_t n, int64_t strid
     }
     P->tstart(DCPSE_K_SPLIT);
     cudaError_t e = inv ? split_f64_perm(d_f, n, inv, P->f2, P->stream) : split_f64(d_f, n, P->f2, P->stream, stride);
+    P->tstop(DCPSE_K_SPLIT);
+    DCPSE_CK(e);
+    return DCPSE_OK;
+}
+
+// The field in fixed point into the plan's scratch (the float-pair buffer,
+// 8 bytes per value either way), at positions when inv is given.
+int fixed_into_plan(dcpse_plan_t* P, const double* d_f, const int32_t* inv) {
+    static_assert(sizeof(float2) == sizeof(long long), "the fixed-point field shares the pair buffer");
+    if (P->f2_len < P->n) {
+        dfree(P->f2);
+        P->f2_len = 0;
+        DCPSE_CK(dalloc(&P->f2, (size_t)P->n));
+        P->f2_len = P->n;
+    }
+    if (!P->fx_meta) DCPSE_CK(dalloc(&P->fx_meta, 2));
+    P->tstart(DCPSE_K_SPLIT);
+    cudaError_t e = fixed_field(d_f, P->n, inv, reinterpret_cast<long long*>(P->f2), P->fx_meta, P->stream);
     P->tstop(DCPSE_K_SPLIT);
     DCPSE_CK(e);
     return DCPSE_OK;
@@ -1907,6 +1929,22 @@ int ensure_sell_resid(dcpse_plan_t* P) {
         });
 }
 
+// The FP32 residual streams on the sliced layout (the second float of each
+// weight pair), built on the first apply that asks for them.
+int ensure_sell_pair(dcpse_plan_t* P) {
+    if (P->sell_r32 || !P->sell_w || !P->r32) return DCPSE_OK;
+    return sell_stream(
+        P, "sliced ELL weight pairs: ",
+        [&] { return dalloc(&P->sell_r32, (size_t)P->nout * P->sell_total + kPad); },
+        [&] {
+            // the residuals take the weight streams' path of the fill
+            return sell_fill(P->rowptr, P->cols, P->r32, nullptr, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
+                             P->sell_row, P->sell_off, P->sell_total, nullptr, P->sell_r32, nullptr, P->stream,
+                             P->sell_perm);
+        },
+        [&] { dfree(P->sell_r32); });
+}
+
 // The evict-first hint of the sliced kernels' streams: on a renumbered layout
 // unless the apply configuration says otherwise.
 int stream_hint(const dcpse_plan_t* P) {
@@ -1946,21 +1984,26 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
         if (ord >= 2) ap.comp |= 1u << P->term_output[t];
     }
     // the residual correction only pays off with compensated sums
-    if ((P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) || precision == DCPSE_F32_RESID || comp_all)
+    if ((P->apply_mode & DCPSE_APPLY_COMPENSATE_ALL) || precision == DCPSE_F32_RESID ||
+        precision == DCPSE_F32_PAIR || comp_all)
         ap.comp = 0xffffffffu;
     // sliced ELL layout: rows in whole windows of 256
     // (the automatic schedule: 15 % faster than the CSR kernels at 128^3)
     const int64_t rr0 = r0, rr1 = r1 ? r1 : P->n;
     const int mode = P->apply_mode & 15;
     const bool resid = precision == DCPSE_F32_RESID;
+    const bool pair = precision == DCPSE_F32_PAIR;
     if (!csr_only && (mode == 0 || mode == 4) && rr0 % 256 == 0 && (rr1 % 256 == 0 || rr1 == P->n)) {
         if (int rc = ensure_sell(P)) return rc;
         if (resid)
             if (int rc = ensure_sell_resid(P)) return rc;
+        if (pair)
+            if (int rc = ensure_sell_pair(P)) return rc;
     }
     // (a renumbered layout serves whole-list applies only: the split field
     // is then at positions)
-    if (!csr_only && (mode == 0 || mode == 4) && P->sell_w && (!resid || P->sell_r) && rr0 % 256 == 0 &&
+    if (!csr_only && (mode == 0 || mode == 4) && P->sell_w && (!resid || P->sell_r) && (!pair || P->sell_r32) &&
+        rr0 % 256 == 0 &&
         (rr1 % 256 == 0 || rr1 == P->n) && (!P->sell_perm || (rr0 == 0 && rr1 == P->n))) {
         SellArgs sa{};
         sa.perm = P->sell_perm;
@@ -1972,8 +2015,11 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
         sa.cols = P->sell_cols;
         sa.w = P->sell_w;
         sa.r = resid ? static_cast<const __nv_bfloat16*>(P->sell_r) : nullptr;
+        sa.r32 = pair ? P->sell_r32 : nullptr;
         sa.total = P->sell_total;
         sa.f2 = P->f2;
+        sa.fx = pair ? reinterpret_cast<const long long*>(P->f2) : nullptr;
+        sa.fx_meta = pair ? P->fx_meta : nullptr;
         sa.out = d_out;
         sa.oos = P->n;
         sa.ors = 1;
@@ -1990,6 +2036,8 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
         DCPSE_CK(e);
         return DCPSE_OK;
     }
+    // the weight pairs run on the sliced layout only (their field is in fixed point)
+    if (pair) return fail(DCPSE_ERR_STATE, "DCPSE_F32_PAIR needs the sliced layout");
     P->tstart(DCPSE_K_APPLY_BATCHED, st);
     cudaError_t e = apply_batched_f32x(ap, st);
     P->tstop(DCPSE_K_APPLY_BATCHED, st);
@@ -2004,8 +2052,8 @@ int check_f32_weights(dcpse_plan_t* P, int precision) {
     if (!P->w32) return fail(DCPSE_ERR_STATE, "FP32 weights not stored");
     if (precision == DCPSE_F32_RESID && !P->r16)
         return fail(DCPSE_ERR_STATE, "FP32 residuals not stored (DCPSE_STORE_OUT_F32_RESID)");
-    if (precision == DCPSE_F32_BUDGET && !P->r32)
-        return fail(DCPSE_ERR_STATE, "FP32 residuals for the correction not stored (DCPSE_STORE_OUT_F32_CORR)");
+    if ((precision == DCPSE_F32_BUDGET || precision == DCPSE_F32_PAIR) && !P->r32)
+        return fail(DCPSE_ERR_STATE, "FP32 residuals not stored (DCPSE_STORE_OUT_F32_CORR)");
     if (precision == DCPSE_F32_BUDGET && P->budget_pass == DCPSE_F32_RESID && !P->r16)
         return fail(DCPSE_ERR_STATE, "the bf16 first pass needs DCPSE_STORE_OUT_F32_RESID");
     return DCPSE_OK;
@@ -2019,9 +2067,12 @@ int sell_ready(dcpse_plan_t* P, int precision, bool* ready) {
     if (mode != 0 && mode != 4) return DCPSE_OK;
     if (int rc = ensure_sell(P)) return rc;
     const bool resid = precision == DCPSE_F32_RESID || (precision == DCPSE_F32_BUDGET && P->budget_pass == DCPSE_F32_RESID);
+    const bool pair = precision == DCPSE_F32_PAIR;
     if (resid)
         if (int rc = ensure_sell_resid(P)) return rc;
-    *ready = P->sell_w && (!resid || P->sell_r);
+    if (pair)
+        if (int rc = ensure_sell_pair(P)) return rc;
+    *ready = P->sell_w && (!resid || P->sell_r) && (!pair || P->sell_r32);
     return DCPSE_OK;
 }
 
@@ -2129,6 +2180,18 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
     if (int rc = check_single_set(P)) return rc;
     if (!P->assembled) return fail(DCPSE_ERR_STATE, "not assembled");
     if (P->n > 0 && (!d_f || !d_out)) return fail(DCPSE_ERR_ARG, "NULL field");
+    if (precision == DCPSE_F32_PAIR) {
+        // FP64-class weights as float pairs on the sliced layout; without it
+        // (no room, or a CSR schedule) the batched FP64 apply serves
+        if (int rc = check_f32_weights(P, precision)) return rc;
+        bool ready = false;
+        if (int rc = sell_ready(P, precision, &ready)) return rc;
+        if (ready) {
+            if (int rc = fixed_into_plan(P, d_f, P->sell_perm ? P->sell_inv : nullptr)) return rc;
+            return apply_f32_rows(P, precision, d_out, 0, 0);
+        }
+        precision = DCPSE_F64;
+    }
     if (precision == DCPSE_F32 || precision == DCPSE_F32_RESID) {
         if (int rc = check_f32_weights(P, precision)) return rc;
         if (int rc = split_for_apply(P, d_f, precision)) return rc;
@@ -2180,7 +2243,8 @@ int dcpse_apply_batched(dcpse_plan_t* P, const double* d_f, double* d_out, int p
         P->tstop(DCPSE_K_APPLY_BATCHED);
         DCPSE_CK(e);
     } else {
-        return fail(DCPSE_ERR_ARG, "precision must be DCPSE_F32, DCPSE_F32_RESID, DCPSE_F32_BUDGET or DCPSE_F64");
+        return fail(DCPSE_ERR_ARG,
+                    "precision must be DCPSE_F32, DCPSE_F32_RESID, DCPSE_F32_BUDGET, DCPSE_F32_PAIR or DCPSE_F64");
     }
     return DCPSE_OK;
 }

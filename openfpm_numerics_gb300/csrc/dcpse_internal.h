@@ -209,8 +209,14 @@ struct SellArgs {
     const int32_t* cols;   // [total] entry-major within a slice
     const float* w;        // [NO][total]
     const __nv_bfloat16* r; // [NO][total] bf16 residuals of the weights, or null
+    const float* r32;      // [NO][total] FP32 residuals w64 - w32 (weight pairs), or null
     int64_t total;
     const float2* f2;
+    // the field in fixed point (with r32): fx[i] = f_i 2^shift rounded to an
+    // integer, shift = fx_meta[1] (kFixedNonFinite: the field holds a NaN or
+    // an infinity, and every output is NaN)
+    const long long* fx;
+    const long long* fx_meta;
     double* out;           // output o of row r at out[o * oos + r * ors]
     int64_t oos, ors;
     int64_t w0, w1;        // windows of 256 rows
@@ -233,6 +239,14 @@ cudaError_t sell_order(const int64_t* rowptr, int64_t n, int32_t* srow, int32_t*
 cudaError_t sell_locality(const int64_t* rowptr, const int32_t* cols, int64_t n, const int32_t* inv,
                           unsigned long long* d_sums, cudaStream_t s);
 cudaError_t invert_perm(const int32_t* perm, int64_t n, int32_t* inv, cudaStream_t s);
+// The field in fixed point for the weight pairs' apply: meta[0] = the bits of
+// max |f|, meta[1] = shift = 62 - e with max |f| < 2^e (|fx| < 2^62, so that
+// differences stay below 2^63), fx[inv[i]] (fx[i] without inv) = f[i] 2^shift
+// rounded to the nearest integer; a NaN or an infinity sets shift to
+// kFixedNonFinite.
+constexpr long long kFixedNonFinite = -(1ll << 40);
+cudaError_t fixed_field(const double* f, int64_t n, const int32_t* inv, long long* fx, long long* meta,
+                        cudaStream_t s);
 // f2[inv[i]] = (hi, lo) of f[i];  g[inv[i]] = f[i]
 cudaError_t split_f64_perm(const double* f, int64_t n, const int32_t* inv, float2* f2, cudaStream_t s);
 cudaError_t permute_f64(const double* f, int64_t n, const int32_t* inv, double* g, cudaStream_t s);

@@ -18,6 +18,8 @@
 // leave in the caller's order, until their sectors are complete.
 #include <cuda_bf16.h>
 
+#include <type_traits>
+
 #include "dcpse_internal.h"
 #include "dcpse_f32_row.cuh"
 
@@ -235,8 +237,8 @@ __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
 // B_o = sum_q |w_o,pq| |f_q - f_p| (FP32), stored to bnd[o * n + r], and the
 // largest |output| of the call per output, atomically maxed into maxabs[o]
 // (float bits; the values are >= 0, so unsigned order is float order).
-template <int NO, int U, bool RESID, bool BOUND, bool STREAM>
-__global__ void __launch_bounds__(256, (NO <= 4 && !RESID && !BOUND ? 5 : (NO <= 6 ? 4 : 3)))
+template <int NO, int U, int RK, bool BOUND, bool STREAM>
+__global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 && !BOUND ? 5 : (NO <= 6 ? 4 : 3)))
     apply_sell_kernel(SellArgs a) {
     // the window's outputs, staged so that they leave in row order (rows of a
     // slice are permuted; scattered 8-byte stores are slow, above all into
@@ -250,15 +252,20 @@ __global__ void __launch_bounds__(256, (NO <= 4 && !RESID && !BOUND ? 5 : (NO <=
         const int32_t row = a.srow[s * kSlice + lane];
         const int64_t b = a.off[s];
         const int L = (int)((a.off[s + 1] - b) / kSlice);
-        const float2 fp = (row >= 0 && !a.no_self) ? a.f2[row] : make_float2(0.f, 0.f);
-        RowAcc<NO, RESID> acc;
+        // the field: float pairs, or (weight pairs) fixed point
+        using FT = typename std::conditional<RK == 2, long long, float2>::type;
+        const FT* __restrict__ fld = RK == 2 ? reinterpret_cast<const FT*>(a.fx) : reinterpret_cast<const FT*>(a.f2);
+        const FT fp = (row >= 0 && !a.no_self) ? fld[row] : FT{};
+        RowAcc<NO, (RK != 0)> acc;
         acc.init();
         float bs[NO];
 #pragma unroll
         for (int o = 0; o < NO; ++o) bs[o] = 0.0f;
         const int32_t* __restrict__ c = a.cols + b + lane;
         const float* __restrict__ w = a.w + b + lane;
-        const __nv_bfloat16* __restrict__ rr = RESID ? a.r + b + lane : nullptr;
+        // residual streams: bf16 (RK 1) or FP32 (RK 2, the weight pairs)
+        const __nv_bfloat16* __restrict__ rr = RK == 1 ? a.r + b + lane : nullptr;
+        const float* __restrict__ rf = RK == 2 ? a.r32 + b + lane : nullptr;
         for (int j0 = 0; j0 < L; j0 += U) {
             int32_t q[U];
             float wv[U][NO], rv[U][NO];
@@ -270,19 +277,23 @@ __global__ void __launch_bounds__(256, (NO <= 4 && !RESID && !BOUND ? 5 : (NO <=
 #pragma unroll
                 for (int o = 0; o < NO; ++o) {
                     wv[u][o] = ok ? ld_stream<STREAM>(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
-                    rv[u][o] = (RESID && ok)
-                                   ? __bfloat162float(ld_stream<STREAM>(rr + (int64_t)o * a.total + (int64_t)j * kSlice))
-                                   : 0.0f;
+                    if (RK == 1)
+                        rv[u][o] = ok ? __bfloat162float(ld_stream<STREAM>(rr + (int64_t)o * a.total + (int64_t)j * kSlice))
+                                      : 0.0f;
+                    else if (RK == 2)
+                        rv[u][o] = ok ? ld_stream<STREAM>(rf + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
+                    else
+                        rv[u][o] = 0.0f;
                 }
             }
             // entries past the slice end take the row's own value (a zero
             // difference; zero for interpolation) with weight 0: no gather
-            float2 fq[U];
+            FT fq[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? a.f2[q[u]] : fp;
+            for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? fld[q[u]] : fp;
 #pragma unroll
             for (int u = 0; u < U; ++u) acc.add(wv[u], rv[u], fq[u], fp, a.comp);
-            if (BOUND) {
+            if constexpr (BOUND) {
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const float df = fabsf(fq[u].x - fp.x);
@@ -292,9 +303,14 @@ __global__ void __launch_bounds__(256, (NO <= 4 && !RESID && !BOUND ? 5 : (NO <=
             }
         }
         if (row >= 0) {
+            // fixed point: the sums are in units of 2^(64 - shift)
+            const long long shift = RK == 2 ? a.fx_meta[1] : 0;
 #pragma unroll
             for (int o = 0; o < NO; ++o) {
-                tile[o][row - win * kWin] = acc.value(o);
+                double v = acc.value(o);
+                if (RK == 2)
+                    v = shift == kFixedNonFinite ? __longlong_as_double(0x7ff8000000000000ll) : ldexp(v, (int)(64 - shift));
+                tile[o][row - win * kWin] = v;
                 if (BOUND) btile[o][row - win * kWin] = bs[o];
             }
         }
@@ -371,6 +387,42 @@ __global__ void split_perm_kernel(const double* __restrict__ f, int64_t n, const
     }
 }
 
+// max |f| as the bits of a non-negative double (their unsigned order is the
+// values' order; a NaN or an infinity compares above every finite value)
+__global__ void __launch_bounds__(256) fixed_max_kernel(const double* __restrict__ f, int64_t n,
+                                                        unsigned long long* __restrict__ mx) {
+    unsigned long long m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, (unsigned long long)__double_as_longlong(f[i]) & 0x7fffffffffffffffull);
+#pragma unroll
+    for (int k = 16; k > 0; k >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, k));
+    __shared__ unsigned long long wm[8];
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) m = max(m, wm[k]);
+        if (m) atomicMax(mx, m);
+    }
+}
+
+// fx[inv[i]] = f[i] 2^shift rounded to the nearest integer, shift = 62 - e
+// with max |f| < 2^e (frexp), so |fx| < 2^62: every |f| >= 2^-9 max |f| is
+// held exactly (its ulp is at least the quantum), smaller ones to 2^-62 max |f|
+__global__ void __launch_bounds__(256) fixed_quant_kernel(const double* __restrict__ f, int64_t n,
+                                                          const int32_t* __restrict__ inv,
+                                                          long long* __restrict__ fx, long long* meta) {
+    const unsigned long long mb = (unsigned long long)meta[0];
+    const bool finite = mb < 0x7ff0000000000000ull;
+    int e = 0;
+    if (finite) frexp(__longlong_as_double((long long)mb), &e);
+    const int shift = 62 - e;
+    if (blockIdx.x == 0 && threadIdx.x == 0) meta[1] = finite ? shift : kFixedNonFinite;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const long long v = finite ? __double2ll_rn(ldexp(f[i], shift)) : 0;
+        fx[inv ? (int64_t)inv[i] : i] = v;
+    }
+}
+
 // f[i] stored at position inv[i] (FP64)
 __global__ void permute_f64_kernel(const double* __restrict__ f, int64_t n, const int32_t* __restrict__ inv,
                                    double* __restrict__ g) {
@@ -408,6 +460,17 @@ cudaError_t invert_perm(const int32_t* perm, int64_t n, int32_t* inv, cudaStream
 cudaError_t split_f64_perm(const double* f, int64_t n, const int32_t* inv, float2* f2, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     split_perm_kernel<<<grid_for(n), 256, 0, s>>>(f, n, inv, f2);
+    return cudaGetLastError();
+}
+
+cudaError_t fixed_field(const double* f, int64_t n, const int32_t* inv, long long* fx, long long* meta,
+                        cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(meta, 0, 2 * sizeof(long long), s);
+    if (e != cudaSuccess || n == 0) return e;
+    const int grid = grid_for(n);
+    fixed_max_kernel<<<grid, 256, 0, s>>>(f, n, reinterpret_cast<unsigned long long*>(meta));
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    fixed_quant_kernel<<<grid, 256, 0, s>>>(f, n, inv, fx, meta);
     return cudaGetLastError();
 }
 
@@ -489,14 +552,16 @@ template <int NO, bool ST>
 void launch_sell(const SellArgs& a, unsigned grid, cudaStream_t s) {
     constexpr int UR = NO == 1 ? 8 : (NO <= 2 ? 4 : 2);  // with the residual streams
     constexpr int U = NO == 1 ? 8 : 4;
-    if (a.r && a.bnd)
-        apply_sell_kernel<NO, UR, true, true, ST><<<grid, 256, 0, s>>>(a);
+    if (a.r32)
+        apply_sell_kernel<NO, UR, 2, false, ST><<<grid, 256, 0, s>>>(a);
+    else if (a.r && a.bnd)
+        apply_sell_kernel<NO, UR, 1, true, ST><<<grid, 256, 0, s>>>(a);
     else if (a.r)
-        apply_sell_kernel<NO, UR, true, false, ST><<<grid, 256, 0, s>>>(a);
+        apply_sell_kernel<NO, UR, 1, false, ST><<<grid, 256, 0, s>>>(a);
     else if (a.bnd)
-        apply_sell_kernel<NO, U, false, true, ST><<<grid, 256, 0, s>>>(a);
+        apply_sell_kernel<NO, U, 0, true, ST><<<grid, 256, 0, s>>>(a);
     else
-        apply_sell_kernel<NO, U, false, false, ST><<<grid, 256, 0, s>>>(a);
+        apply_sell_kernel<NO, U, 0, false, ST><<<grid, 256, 0, s>>>(a);
 }
 }  // namespace
 

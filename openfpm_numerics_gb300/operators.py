@@ -12,7 +12,8 @@ Derivative_G_T; CPU aliases at :3485-3508, GPU aliases at :3510-3530):
 
 Calling an operator applies it in FP64 in the reference's operation order
 (bit-exact with the CPU oracle).  ``op(f, precision="f32")`` uses the batched
-FP32-weight path instead.  Errors follow the reference: too few neighbours
+FP32-weight path instead, ``"f32-pair"`` the FP32 weight pairs (FP64-class
+results off the FP64 pipe) and ``"f64-batched"`` the batched FP64 apply.  Errors follow the reference: too few neighbours
 raise ``ValueError`` (std::length_error in Vandermonde.hpp:109-112) unless the
 operator was built with ``allow_failed_particles=True``.
 """
@@ -26,6 +27,13 @@ import torch
 
 from . import _capi as C
 from .plan import DcpsePlan
+
+# what the operators store at assembly: the reference's per-term kernels, the
+# summed FP64 and FP32 weights and the FP32 residuals of the weight pairs
+_OP_FLAGS = C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32 | C.STORE_OUT_F32_CORR
+# the batched applies by name
+_BATCHED = {"f32": C.F32, "f32-pair": C.F32_PAIR, "f64-batched": C.F64}
+_PREC_MSG = "precision must be 'f64', 'f64-batched', 'f32' or 'f32-pair'"
 
 dcpse_oversampling_factor = 1.9  # DCPSE_op.hpp:20
 rcut_verlet = 3.1                # DCPSE_op.hpp:21
@@ -154,8 +162,7 @@ class _DcpseOp:
         self.plan.set_neighbors(self.verletList.rowptr, self.verletList.cols)
 
     def _assemble(self, parts):
-        rc = self.plan.assemble(parts.getPosTensor(),
-                                C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+        rc = self.plan.assemble(parts.getPosTensor(), _OP_FLAGS)
         if rc == C.ERR_PARTICLES and not self._allow:
             nb, first, code = self.plan.particle_status()
             if code == C.PART_TOO_FEW:
@@ -216,11 +223,11 @@ class _DcpseOp:
         if precision == "f64":
             res = [self.plan.apply_output_f64(o, f) for o in range(len(self._outputs))]
             out = torch.stack(res) if len(res) > 1 else res[0]
-        elif precision in ("f32", "f64-batched"):
-            out = self.plan.apply(f, C.F32 if precision == "f32" else C.F64)
+        elif precision in _BATCHED:
+            out = self.plan.apply(f, _BATCHED[precision])
             out = out if len(self._outputs) > 1 else out[0]
         else:
-            raise ValueError("precision must be 'f64', 'f64-batched' or 'f32'")
+            raise ValueError(_PREC_MSG)
         return out
 
     # accessors of the reference (Dcpse.hpp:507-550), for the first term
@@ -327,9 +334,9 @@ class Divergence(_DcpseOp):
     def _component(self, i, f, precision):
         if precision == "f64":
             return self.plan.apply_output_f64(i, f)
-        if precision in ("f32", "f64-batched"):
-            return self.plan.apply(f, C.F32 if precision == "f32" else C.F64)[i]
-        raise ValueError("precision must be 'f64', 'f64-batched' or 'f32'")
+        if precision in _BATCHED:
+            return self.plan.apply(f, _BATCHED[precision])[i]
+        raise ValueError(_PREC_MSG)
 
 
 class Advection(Divergence):
@@ -525,8 +532,7 @@ class PPInterpolation:
             self.plan.build_neighbors(self.particlesDomain.getPosTensor(), self.verletList.rCut)
         else:
             self.plan.set_neighbors(self.verletList.rowptr, self.verletList.cols)
-        rc = self.plan.assemble(self.particlesDomain.getPosTensor(),
-                                C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+        rc = self.plan.assemble(self.particlesDomain.getPosTensor(), _OP_FLAGS)
         if rc == C.ERR_PARTICLES and not self._allow:
             nb, first, code = self.plan.particle_status()
             if code == C.PART_TOO_FEW:

@@ -70,10 +70,10 @@ int main(int argc, char** argv) {
         l64[p] = parts.getProp<1>(p);
         g64[p] = parts.getProp<2>(p);
     }
-    double res[2][3];
-    double err[2][2];
-    const int precs[2] = {DCPSE_F32, DCPSE_F32_BUDGET};
-    for (int m = 0; m < 2; ++m) {
+    double res[3][3];
+    double err[3][2];
+    const int precs[3] = {DCPSE_F32, DCPSE_F32_BUDGET, DCPSE_F32_PAIR};
+    for (int m = 0; m < 3; ++m) {
         t0 = now_s();
         Lap.set_apply_precision(precs[m]);
         Grad.set_apply_precision(precs[m]);
@@ -95,13 +95,14 @@ int main(int argc, char** argv) {
     const double nd = (double)n;
     std::printf("{\"particles\": %zu, \"verlet_ms\": %.3f, \"operators_ms\": %.3f, "
                 "\"fp64_reference_order\": {\"laplacian_ms\": %.3f, \"gradient_ms\": %.3f, "
-                "\"gparticle_ops_s\": %.5f}, "
-                "\"fp32_batched\": {\"laplacian_ms\": %.3f, \"gradient_ms\": %.3f, \"gparticle_ops_s\": %.5f, "
-                "\"set_up_ms\": %.3f, \"laplacian_vs_fp64\": %.3e, \"gradient_vs_fp64\": %.3e}, "
-                "\"fp32_budget\": {\"laplacian_ms\": %.3f, \"gradient_ms\": %.3f, \"gparticle_ops_s\": %.5f, "
-                "\"set_up_ms\": %.3f, \"laplacian_vs_fp64\": %.3e, \"gradient_vs_fp64\": %.3e}}\n",
-                n, t_verlet, t_ops, lap64, grad64, 4 * nd / ((lap64 + grad64) * 1e6), res[0][0], res[0][1],
-                4 * nd / ((res[0][0] + res[0][1]) * 1e6), res[0][2], err[0][0], err[0][1], res[1][0], res[1][1],
-                4 * nd / ((res[1][0] + res[1][1]) * 1e6), res[1][2], err[1][0], err[1][1]);
+                "\"gparticle_ops_s\": %.5f}",
+                n, t_verlet, t_ops, lap64, grad64, 4 * nd / ((lap64 + grad64) * 1e6));
+    const char* names[3] = {"fp32_batched", "fp32_budget", "fp32_pair"};
+    for (int m = 0; m < 3; ++m)
+        std::printf(", \"%s\": {\"laplacian_ms\": %.3f, \"gradient_ms\": %.3f, \"gparticle_ops_s\": %.5f, "
+                    "\"set_up_ms\": %.3f, \"laplacian_vs_fp64\": %.3e, \"gradient_vs_fp64\": %.3e}",
+                    names[m], res[m][0], res[m][1], 4 * nd / ((res[m][0] + res[m][1]) * 1e6), res[m][2], err[m][0],
+                    err[m][1]);
+    std::printf("}\n");
     return 0;
 }

@@ -47,7 +47,7 @@ def test_shuffled_set_is_renumbered_and_bit_identical(shuffled):
     assert renum and d_cells * 2 < d_list, (d_list, d_cells)
     assert not keep.reorder_info()[0]
     f = torch.tensor(W.field2(pos)[0], device="cuda")
-    for prec in (C.F32, C.F32_RESID, C.F32_BUDGET, C.F64):
+    for prec in (C.F32, C.F32_RESID, C.F32_BUDGET, C.F32_PAIR, C.F64):
         a = auto.apply(f, prec).clone()
         b = keep.apply(f, prec).clone()
         assert torch.equal(a, b), prec

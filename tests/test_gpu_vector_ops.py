@@ -35,6 +35,9 @@ def test_divergence(cuda, orc):
     assert np.array_equal(div, ref)
     d32 = Div(vt, precision="f32").cpu().numpy()
     assert np.abs(d32 - ref).max() <= 1e-6 * np.abs(ref).max() * 4
+    # the FP32 weight pairs: the FP64 bar
+    dp = Div(vt, precision="f32-pair").cpu().numpy()
+    assert np.abs(dp - ref).max() <= 1e-12 * np.abs(ref).max()
     Div.deallocate()
 
 
