@@ -398,6 +398,18 @@ int dcpse_measure_fp64_peak(void* stream, double* tflops);
  * dcpse_plan_set_reorder); these bits force the hint on or off. */
 #define DCPSE_APPLY_STREAM_HINT_ON 32
 #define DCPSE_APPLY_STREAM_HINT_OFF 64
+/* Scheduling of the sliced kernels.  Warp-scheduled: each warp takes the
+ * next slice from a counter and stores its rows' outputs directly, so no
+ * warp waits for the longest slice of its window.  Window-scheduled: a block
+ * takes one window of 8 slices and its outputs leave in row order after the
+ * window's barrier (always so for host-memory outputs, row chunks on their
+ * own streams and the error-budget pass).  By default device-memory applies
+ * with residual streams (DCPSE_F32_RESID, DCPSE_F32_PAIR) are warp-scheduled,
+ * and plain FP32 applies are when the window barrier would idle 15 % or more
+ * of the warp time (slices of unequal length: graded clouds).  These bits
+ * force one schedule. */
+#define DCPSE_APPLY_SLICE_WINDOWS 128
+#define DCPSE_APPLY_SLICE_WARPS 256
 int dcpse_plan_set_apply_config(dcpse_plan_t* plan, int lanes, int mode);
 /* Assembly schedule knobs (autotuning): particles are processed in bins of
  * neighbour count of width bin_width (0 = index order; uneven clouds keep

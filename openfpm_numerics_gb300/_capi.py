@@ -104,6 +104,13 @@ F32_RESID = 2
 F32_BUDGET = 3
 F32_PAIR = 4
 
+# apply schedule bits (dcpse_plan_set_apply_config mode)
+APPLY_COMPENSATE_ALL = 16
+APPLY_STREAM_HINT_ON = 32
+APPLY_STREAM_HINT_OFF = 64
+APPLY_SLICE_WINDOWS = 128
+APPLY_SLICE_WARPS = 256
+
 PART_OK, PART_TOO_FEW, PART_BAD_EPS, PART_SINGULAR, PART_NONFINITE = range(5)
 
 

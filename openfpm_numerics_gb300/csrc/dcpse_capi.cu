@@ -274,6 +274,8 @@ struct dcpse_plan_s {
     int64_t bnd_len = 0;
     unsigned* maxabs = nullptr;  // [kMaxOutputs] largest |output|, then the list length
     unsigned long long* budget_count = nullptr;
+    unsigned* slice_counter = nullptr;  // the warp-scheduled sliced kernels' slice counter
+    double sell_idle = 0.0;  // share of warp time the window barrier would idle on the sliced layout
     unsigned long long* summary = nullptr;  // [count, first]
     int* d_err = nullptr;                   // set by kernels whose bounded wait ran out
     int apply_lanes = 0, apply_mode = 0;
@@ -417,6 +419,7 @@ struct dcpse_plan_s {
         dfree(d_err);
         dfree(maxabs);
         dfree(budget_count);
+        dfree(slice_counter);
         dfree(asm_scratch);
         asm_scratch_bytes = 0;
         dfree(qr_ws);
@@ -1839,10 +1842,27 @@ int ensure_sell_layout(dcpse_plan_t* P) {
     if (e == cudaSuccess) e = dalloc(&tmp, (size_t)scan_tmp_elems(ns));
     if (e == cudaSuccess) e = sell_order(P->rowptr, P->n, P->sell_row, slen, P->sell_off, tmp, P->stream, P->sell_perm);
     int64_t total = 0;
+    std::vector<int32_t> hlen((size_t)ns);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&total, P->sell_off + ns, sizeof total, cudaMemcpyDeviceToHost, P->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hlen.data(), slen, sizeof(int32_t) * ns, cudaMemcpyDeviceToHost, P->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
     dfree(slen);
     dfree(tmp);
+    if (e == cudaSuccess) {
+        // the share of warp time a window's barrier would idle: per window
+        // 8 x its longest slice against the sum of its slices
+        int64_t busy = 0, held = 0;
+        for (int64_t w = 0; w < ns / 8; ++w) {
+            int32_t mx = 0;
+            for (int k = 0; k < 8; ++k) {
+                busy += hlen[(size_t)(w * 8 + k)];
+                mx = std::max(mx, hlen[(size_t)(w * 8 + k)]);
+            }
+            held += 8 * (int64_t)mx;
+        }
+        P->sell_idle = busy > 0 ? (double)(held - busy) / (double)busy : 0.0;
+    }
     if (e == cudaSuccess) e = dalloc(&P->sell_cols, (size_t)total + kPad);
     if (e == cudaSuccess)
         e = sell_fill(P->rowptr, P->cols, nullptr, nullptr, P->nnz, P->nout, P->n, P->two_set() ? 0 : 1,
@@ -1953,10 +1973,26 @@ int stream_hint(const dcpse_plan_t* P) {
     return P->sell_perm ? 1 : 0;
 }
 
+// The slice counter of the warp-scheduled sliced kernels, or null for the
+// window-per-block kernel: outputs in host memory (their scattered stores
+// are slow over NVLink-C2C), DCPSE_APPLY_SLICE_WINDOWS, or plain FP32
+// weights on a layout whose windows hold slices of nearly equal length
+// (128^3 lattice: 6 % idle at the barrier, 0.591 ms with windows against
+// 0.614 ms; graded 2D cloud: 37 %, 0.178 ms against 0.150 ms; with residual
+// streams the warp schedule is faster on both).
+constexpr double kSliceIdleWarps = 0.15;
+unsigned* slice_counter(dcpse_plan_t* P, bool host_out, bool plain = false) {
+    if (host_out || (P->apply_mode & DCPSE_APPLY_SLICE_WINDOWS)) return nullptr;
+    if (plain && P->sell_idle < kSliceIdleWarps && !(P->apply_mode & DCPSE_APPLY_SLICE_WARPS)) return nullptr;
+    if (!P->slice_counter && dalloc(&P->slice_counter, 1) != cudaSuccess) return nullptr;
+    return P->slice_counter;
+}
+
 // The FP32 batched apply of rows [r0, r1) (0, 0: all rows) from the plan's
-// split field into d_out ([n_outputs][n]).
+// split field into d_out ([n_outputs][n]; in host memory with host_out).
 int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, int64_t r1,
-                   cudaStream_t on = nullptr, bool comp_all = false, bool csr_only = false) {
+                   cudaStream_t on = nullptr, bool comp_all = false, bool csr_only = false,
+                   bool host_out = false) {
     cudaStream_t st = on ? on : P->stream;
     ApplyF32 ap{};
     ap.n = P->n;
@@ -2030,6 +2066,9 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
         // (128^3 gradient: 5e-7 plain, ~1e-7 compensated; 1.5 % slower)
         sa.comp = 0xffffffffu;
         sa.no_self = 0;
+        // (row chunks on their own streams run concurrently: one counter
+        // per plan serves calls on the plan's stream only)
+        sa.counter = on ? nullptr : slice_counter(P, host_out, !resid && !pair);
         P->tstart(DCPSE_K_APPLY_BATCHED, st);
         cudaError_t e = apply_sell(sa, P->nout, st);
         P->tstop(DCPSE_K_APPLY_BATCHED, st);
@@ -2442,7 +2481,7 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
         // the field in two pieces, the second beside the apply of the first
         // rows, took 0.71-0.74 ms for any first-row share from 1/32 to 1/4)
         if (int rc = split_for_apply(P, f_mapped, precision)) return rc;
-        if (int rc = apply_f32_rows(P, precision, out_mapped, 0, 0)) return rc;
+        if (int rc = apply_f32_rows(P, precision, out_mapped, 0, 0, nullptr, false, false, true)) return rc;
         // the direct kernels report no device errors: a synchronisation of
         // the plan's stream puts the outputs in place
         DCPSE_CK(cudaStreamSynchronize(P->stream));
@@ -2482,7 +2521,7 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
                 DCPSE_CK(cudaStreamWaitEvent(P->stream, P->piece_ev[need], 0));
                 waited[0] = need;
             }
-            if (int rc = apply_f32_rows(P, precision, out_mapped, cb.b[c0], cb.b[c1])) {
+            if (int rc = apply_f32_rows(P, precision, out_mapped, cb.b[c0], cb.b[c1], nullptr, false, false, true)) {
                 cudaStreamSynchronize(P->h2d_stream);
                 return rc;
             }
@@ -2596,6 +2635,7 @@ int dcpse_p2p(dcpse_plan_t* P, const double* d_f_support, int ncomp, double* d_o
                     sa.w1 = (P->n + 255) / 256;
                     sa.comp = 0xffffffffu;  // one thread sums the whole row
                     sa.no_self = 1;
+                    sa.counter = slice_counter(P, false, true);
                     P->tstart(DCPSE_K_APPLY_BATCHED);
                     cudaError_t e = apply_sell(sa, P->nout, P->stream);
                     P->tstop(DCPSE_K_APPLY_BATCHED);
@@ -2728,10 +2768,12 @@ int dcpse_plan_set_apply_config(dcpse_plan_t* P, int lanes, int mode) {
     if (int rc = check_plan(P)) return rc;
     if (lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
         return fail(DCPSE_ERR_ARG, "lanes must be 0, 4, 8, 16 or 32");
-    if ((mode & ~(15 | DCPSE_APPLY_COMPENSATE_ALL | DCPSE_APPLY_STREAM_HINT_ON | DCPSE_APPLY_STREAM_HINT_OFF)) != 0 ||
-        (mode & 15) > 4 || ((mode & DCPSE_APPLY_STREAM_HINT_ON) && (mode & DCPSE_APPLY_STREAM_HINT_OFF)))
-        return fail(DCPSE_ERR_ARG, "mode must be 0..4, optionally | DCPSE_APPLY_COMPENSATE_ALL and one "
-                                   "DCPSE_APPLY_STREAM_HINT_* bit");
+    if ((mode & ~(15 | DCPSE_APPLY_COMPENSATE_ALL | DCPSE_APPLY_STREAM_HINT_ON | DCPSE_APPLY_STREAM_HINT_OFF |
+                  DCPSE_APPLY_SLICE_WINDOWS | DCPSE_APPLY_SLICE_WARPS)) != 0 ||
+        (mode & 15) > 4 || ((mode & DCPSE_APPLY_STREAM_HINT_ON) && (mode & DCPSE_APPLY_STREAM_HINT_OFF)) ||
+        ((mode & DCPSE_APPLY_SLICE_WINDOWS) && (mode & DCPSE_APPLY_SLICE_WARPS)))
+        return fail(DCPSE_ERR_ARG, "mode must be 0..4, optionally | DCPSE_APPLY_COMPENSATE_ALL, one "
+                                   "DCPSE_APPLY_STREAM_HINT_* bit and one DCPSE_APPLY_SLICE_* bit");
     P->apply_lanes = lanes;
     P->apply_mode = mode;
     return DCPSE_OK;

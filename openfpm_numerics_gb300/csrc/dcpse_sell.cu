@@ -231,6 +231,74 @@ __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
     }
 }
 
+// One slice: lane `lane` sums row `row` (a position, -1 past the last row)
+// over the slice's entries into acc (and, with BOUND, its weight-rounding
+// bound into bs).
+template <int NO, int U, int RK, bool BOUND, bool STREAM>
+__device__ __forceinline__ void sell_slice(const SellArgs& a, int64_t s, int lane, int32_t row,
+                                           RowAcc<NO, (RK != 0)>& acc, float (&bs)[NO]) {
+    const int64_t b = a.off[s];
+    const int L = (int)((a.off[s + 1] - b) / kSlice);
+    // the field: float pairs, or (weight pairs) fixed point
+    using FT = typename std::conditional<RK == 2, long long, float2>::type;
+    const FT* __restrict__ fld = RK == 2 ? reinterpret_cast<const FT*>(a.fx) : reinterpret_cast<const FT*>(a.f2);
+    const FT fp = (row >= 0 && !a.no_self) ? fld[row] : FT{};
+    acc.init();
+#pragma unroll
+    for (int o = 0; o < NO; ++o) bs[o] = 0.0f;
+    const int32_t* __restrict__ c = a.cols + b + lane;
+    const float* __restrict__ w = a.w + b + lane;
+    // residual streams: bf16 (RK 1) or FP32 (RK 2, the weight pairs)
+    const __nv_bfloat16* __restrict__ rr = RK == 1 ? a.r + b + lane : nullptr;
+    const float* __restrict__ rf = RK == 2 ? a.r32 + b + lane : nullptr;
+    for (int j0 = 0; j0 < L; j0 += U) {
+        int32_t q[U];
+        float wv[U][NO], rv[U][NO];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = j0 + u;
+            const bool ok = j < L;
+            q[u] = ok ? ld_stream<STREAM>(c + (int64_t)j * kSlice) : 0;
+#pragma unroll
+            for (int o = 0; o < NO; ++o) {
+                wv[u][o] = ok ? ld_stream<STREAM>(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
+                if (RK == 1)
+                    rv[u][o] = ok ? __bfloat162float(ld_stream<STREAM>(rr + (int64_t)o * a.total + (int64_t)j * kSlice))
+                                  : 0.0f;
+                else if (RK == 2)
+                    rv[u][o] = ok ? ld_stream<STREAM>(rf + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
+                else
+                    rv[u][o] = 0.0f;
+            }
+        }
+        // entries past the slice end take the row's own value (a zero
+        // difference; zero for interpolation) with weight 0: no gather
+        FT fq[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? fld[q[u]] : fp;
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc.add(wv[u], rv[u], fq[u], fp, a.comp);
+        if constexpr (BOUND) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const float df = fabsf(fq[u].x - fp.x);
+#pragma unroll
+                for (int o = 0; o < NO; ++o) bs[o] = fmaf(fabsf(wv[u][o]), df, bs[o]);
+            }
+        }
+    }
+}
+
+// output o of a summed row (fixed point: the sums are in units of
+// 2^(64 - shift))
+template <int NO, int RK>
+__device__ __forceinline__ double sell_value(const RowAcc<NO, (RK != 0)>& acc, int o, long long shift) {
+    const double v = acc.value(o);
+    if constexpr (RK == 2)
+        return shift == kFixedNonFinite ? __longlong_as_double(0x7ff8000000000000ll) : ldexp(v, (int)(64 - shift));
+    return v;
+}
+
 // thread per row; block = one window of 8 slices (five blocks per SM fit the
 // registers without spills up to four outputs, four up to six, three above).
 // BOUND: also the weight-rounding bound of every output of every row,
@@ -247,70 +315,17 @@ __global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 && !BOUND ? 5 : (NO <
     __shared__ float btile[BOUND ? NO : 1][BOUND ? kWin : 1];
     __shared__ unsigned wmax[BOUND ? NO : 1][BOUND ? kSlicesPerWin : 1];
     const int lane = threadIdx.x & 31;
+    const long long shift = RK == 2 ? a.fx_meta[1] : 0;
     for (int64_t win = a.w0 + blockIdx.x; win < a.w1; win += gridDim.x) {
         const int64_t s = win * kSlicesPerWin + (threadIdx.x >> 5);  // < nslices: windows hold 8 slices
         const int32_t row = a.srow[s * kSlice + lane];
-        const int64_t b = a.off[s];
-        const int L = (int)((a.off[s + 1] - b) / kSlice);
-        // the field: float pairs, or (weight pairs) fixed point
-        using FT = typename std::conditional<RK == 2, long long, float2>::type;
-        const FT* __restrict__ fld = RK == 2 ? reinterpret_cast<const FT*>(a.fx) : reinterpret_cast<const FT*>(a.f2);
-        const FT fp = (row >= 0 && !a.no_self) ? fld[row] : FT{};
         RowAcc<NO, (RK != 0)> acc;
-        acc.init();
         float bs[NO];
-#pragma unroll
-        for (int o = 0; o < NO; ++o) bs[o] = 0.0f;
-        const int32_t* __restrict__ c = a.cols + b + lane;
-        const float* __restrict__ w = a.w + b + lane;
-        // residual streams: bf16 (RK 1) or FP32 (RK 2, the weight pairs)
-        const __nv_bfloat16* __restrict__ rr = RK == 1 ? a.r + b + lane : nullptr;
-        const float* __restrict__ rf = RK == 2 ? a.r32 + b + lane : nullptr;
-        for (int j0 = 0; j0 < L; j0 += U) {
-            int32_t q[U];
-            float wv[U][NO], rv[U][NO];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int j = j0 + u;
-                const bool ok = j < L;
-                q[u] = ok ? ld_stream<STREAM>(c + (int64_t)j * kSlice) : 0;
-#pragma unroll
-                for (int o = 0; o < NO; ++o) {
-                    wv[u][o] = ok ? ld_stream<STREAM>(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
-                    if (RK == 1)
-                        rv[u][o] = ok ? __bfloat162float(ld_stream<STREAM>(rr + (int64_t)o * a.total + (int64_t)j * kSlice))
-                                      : 0.0f;
-                    else if (RK == 2)
-                        rv[u][o] = ok ? ld_stream<STREAM>(rf + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
-                    else
-                        rv[u][o] = 0.0f;
-                }
-            }
-            // entries past the slice end take the row's own value (a zero
-            // difference; zero for interpolation) with weight 0: no gather
-            FT fq[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? fld[q[u]] : fp;
-#pragma unroll
-            for (int u = 0; u < U; ++u) acc.add(wv[u], rv[u], fq[u], fp, a.comp);
-            if constexpr (BOUND) {
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const float df = fabsf(fq[u].x - fp.x);
-#pragma unroll
-                    for (int o = 0; o < NO; ++o) bs[o] = fmaf(fabsf(wv[u][o]), df, bs[o]);
-                }
-            }
-        }
+        sell_slice<NO, U, RK, BOUND, STREAM>(a, s, lane, row, acc, bs);
         if (row >= 0) {
-            // fixed point: the sums are in units of 2^(64 - shift)
-            const long long shift = RK == 2 ? a.fx_meta[1] : 0;
 #pragma unroll
             for (int o = 0; o < NO; ++o) {
-                double v = acc.value(o);
-                if (RK == 2)
-                    v = shift == kFixedNonFinite ? __longlong_as_double(0x7ff8000000000000ll) : ldexp(v, (int)(64 - shift));
-                tile[o][row - win * kWin] = v;
+                tile[o][row - win * kWin] = sell_value<NO, RK>(acc, o, shift);
                 if (BOUND) btile[o][row - win * kWin] = bs[o];
             }
         }
@@ -344,6 +359,37 @@ __global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 && !BOUND ? 5 : (NO <
             if (m > __ldcg(&a.maxabs[o])) atomicMax(&a.maxabs[o], m);
         }
         __syncthreads();  // the next window rewrites the tile
+    }
+}
+
+// The same sums with warps scheduled one slice at a time: each warp takes the
+// next slice of [w0 * 8, w1 * 8) from a counter (zeroed before the launch;
+// the next index is fetched while the current slice is summed) and stores its
+// rows' outputs directly.  Slices of a window differ in length (rows sorted
+// by length within it), so the tile kernel's warps wait at the window's
+// barrier for its longest slice; here no warp waits for another.  The
+// stores scatter within the window's 256 rows: device-memory outputs only
+// (L2 completes their sectors).
+template <int NO, int U, int RK, bool STREAM>
+__global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 ? 5 : (NO <= 6 ? 4 : 3)))
+    apply_sell_dyn_kernel(SellArgs a) {
+    const int lane = threadIdx.x & 31;
+    const long long shift = RK == 2 ? a.fx_meta[1] : 0;
+    const int64_t s0 = a.w0 * kSlicesPerWin, s1 = a.w1 * kSlicesPerWin;
+    unsigned next = lane == 0 ? atomicAdd(a.counter, 1u) : 0u;
+    int64_t s = s0 + __shfl_sync(0xffffffffu, next, 0);
+    while (s < s1) {
+        next = lane == 0 ? atomicAdd(a.counter, 1u) : 0u;
+        const int32_t row = a.srow[s * kSlice + lane];
+        RowAcc<NO, (RK != 0)> acc;
+        float bs[NO];
+        sell_slice<NO, U, RK, false, STREAM>(a, s, lane, row, acc, bs);
+        if (row >= 0) {
+            const int64_t lr = a.perm ? (int64_t)a.perm[row] : row;
+#pragma unroll
+            for (int o = 0; o < NO; ++o) a.out[(int64_t)o * a.oos + lr * a.ors] = sell_value<NO, RK>(acc, o, shift);
+        }
+        s = s0 + __shfl_sync(0xffffffffu, next, 0);
     }
 }
 
@@ -548,10 +594,34 @@ cudaError_t apply_sell64(const Sell64Args& a, int nout, cudaStream_t s) {
 }
 
 namespace {
+// blocks of the warp-scheduled kernel: as many as fit on the GPU at once,
+// fewer when the range has fewer slices than their warps
+template <auto K>
+unsigned dyn_grid(int64_t slices) {
+    // blocks per SM: a property of the kernel on this architecture
+    static const int per_sm = [] {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, K, 256, 0) != cudaSuccess || b < 1) b = 1;
+        return b;
+    }();
+    const int64_t full = (int64_t)per_sm * num_sms();
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(full, (slices + 7) / 8));
+}
+
 template <int NO, bool ST>
 void launch_sell(const SellArgs& a, unsigned grid, cudaStream_t s) {
     constexpr int UR = NO == 1 ? 8 : (NO <= 2 ? 4 : 2);  // with the residual streams
     constexpr int U = NO == 1 ? 8 : 4;
+    if (a.counter && !a.bnd) {
+        const int64_t slices = (a.w1 - a.w0) * kSlicesPerWin;
+        if (a.r32)
+            apply_sell_dyn_kernel<NO, UR, 2, ST><<<dyn_grid<apply_sell_dyn_kernel<NO, UR, 2, ST>>(slices), 256, 0, s>>>(a);
+        else if (a.r)
+            apply_sell_dyn_kernel<NO, UR, 1, ST><<<dyn_grid<apply_sell_dyn_kernel<NO, UR, 1, ST>>(slices), 256, 0, s>>>(a);
+        else
+            apply_sell_dyn_kernel<NO, U, 0, ST><<<dyn_grid<apply_sell_dyn_kernel<NO, U, 0, ST>>(slices), 256, 0, s>>>(a);
+        return;
+    }
     if (a.r32)
         apply_sell_kernel<NO, UR, 2, false, ST><<<grid, 256, 0, s>>>(a);
     else if (a.r && a.bnd)
@@ -567,6 +637,10 @@ void launch_sell(const SellArgs& a, unsigned grid, cudaStream_t s) {
 
 cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s) {
     if (a.w1 <= a.w0) return cudaSuccess;
+    if (a.counter && !a.bnd) {
+        cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) return e;
+    }
     // one block per window: the block scheduler balances the windows
     const int64_t grid = a.w1 - a.w0;
     if (grid > 0x7fffffff) return cudaErrorInvalidValue;
