@@ -404,10 +404,9 @@ int dcpse_measure_fp64_peak(void* stream, double* tflops);
  * takes one window of 8 slices and its outputs leave in row order after the
  * window's barrier (always so for host-memory outputs, row chunks on their
  * own streams and the error-budget pass).  By default device-memory applies
- * with residual streams (DCPSE_F32_RESID, DCPSE_F32_PAIR) are warp-scheduled,
- * and plain FP32 applies are when the window barrier would idle 15 % or more
- * of the warp time (slices of unequal length: graded clouds).  These bits
- * force one schedule. */
+ * are warp-scheduled when the window barrier would idle 15 % or more of the
+ * warp time (slices of unequal length: graded clouds), measured when the
+ * layout is built.  These bits force one schedule. */
 #define DCPSE_APPLY_SLICE_WINDOWS 128
 #define DCPSE_APPLY_SLICE_WARPS 256
 int dcpse_plan_set_apply_config(dcpse_plan_t* plan, int lanes, int mode);

@@ -1975,15 +1975,15 @@ int stream_hint(const dcpse_plan_t* P) {
 
 // The slice counter of the warp-scheduled sliced kernels, or null for the
 // window-per-block kernel: outputs in host memory (their scattered stores
-// are slow over NVLink-C2C), DCPSE_APPLY_SLICE_WINDOWS, or plain FP32
-// weights on a layout whose windows hold slices of nearly equal length
-// (128^3 lattice: 6 % idle at the barrier, 0.591 ms with windows against
-// 0.614 ms; graded 2D cloud: 37 %, 0.178 ms against 0.150 ms; with residual
-// streams the warp schedule is faster on both).
+// are slow over NVLink-C2C), DCPSE_APPLY_SLICE_WINDOWS, or a layout whose
+// windows hold slices of nearly equal length.  Measured (kernel ms, windows
+// against warps): 128^3 lattice, 6 % idle at the barrier: FP32 0.591 /
+// 0.614, bf16 residual streams 0.880 / 0.958, weight pairs 1.035 / 1.10;
+// graded 2D cloud, 37 % idle: 0.161 / 0.146, 0.232 / 0.213, 0.261 / 0.260.
 constexpr double kSliceIdleWarps = 0.15;
-unsigned* slice_counter(dcpse_plan_t* P, bool host_out, bool plain = false) {
+unsigned* slice_counter(dcpse_plan_t* P, bool host_out) {
     if (host_out || (P->apply_mode & DCPSE_APPLY_SLICE_WINDOWS)) return nullptr;
-    if (plain && P->sell_idle < kSliceIdleWarps && !(P->apply_mode & DCPSE_APPLY_SLICE_WARPS)) return nullptr;
+    if (P->sell_idle < kSliceIdleWarps && !(P->apply_mode & DCPSE_APPLY_SLICE_WARPS)) return nullptr;
     if (!P->slice_counter && dalloc(&P->slice_counter, 1) != cudaSuccess) return nullptr;
     return P->slice_counter;
 }
@@ -2068,7 +2068,7 @@ int apply_f32_rows(dcpse_plan_t* P, int precision, double* d_out, int64_t r0, in
         sa.no_self = 0;
         // (row chunks on their own streams run concurrently: one counter
         // per plan serves calls on the plan's stream only)
-        sa.counter = on ? nullptr : slice_counter(P, host_out, !resid && !pair);
+        sa.counter = on ? nullptr : slice_counter(P, host_out);
         P->tstart(DCPSE_K_APPLY_BATCHED, st);
         cudaError_t e = apply_sell(sa, P->nout, st);
         P->tstop(DCPSE_K_APPLY_BATCHED, st);
@@ -2635,7 +2635,7 @@ int dcpse_p2p(dcpse_plan_t* P, const double* d_f_support, int ncomp, double* d_o
                     sa.w1 = (P->n + 255) / 256;
                     sa.comp = 0xffffffffu;  // one thread sums the whole row
                     sa.no_self = 1;
-                    sa.counter = slice_counter(P, false, true);
+                    sa.counter = slice_counter(P, false);
                     P->tstart(DCPSE_K_APPLY_BATCHED);
                     cudaError_t e = apply_sell(sa, P->nout, P->stream);
                     P->tstop(DCPSE_K_APPLY_BATCHED);

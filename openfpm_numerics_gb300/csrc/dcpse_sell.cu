@@ -231,6 +231,15 @@ __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
     }
 }
 
+// Whether a slice loads its column stream one chunk ahead (U more registers
+// a thread): everywhere but one output, the plain FP32 instances with 4 or 6
+// outputs and the bound pass, which would spill under their launch bounds.
+// Measured at 128^3 (window schedule): bf16 residual streams 1.090 -> 0.880
+// ms, weight pairs 1.168 -> 1.035 ms; graded 2D cloud, FP32: 0.150 -> 0.146
+// ms (warp schedule).
+template <int NO, int RK, bool BOUND>
+constexpr bool kPipeColumns = NO != 1 && !BOUND && (RK != 0 || (NO != 4 && NO != 6));
+
 // One slice: lane `lane` sums row `row` (a position, -1 past the last row)
 // over the slice's entries into acc (and, with BOUND, its weight-rounding
 // bound into bs).
@@ -251,31 +260,58 @@ __device__ __forceinline__ void sell_slice(const SellArgs& a, int64_t s, int lan
     // residual streams: bf16 (RK 1) or FP32 (RK 2, the weight pairs)
     const __nv_bfloat16* __restrict__ rr = RK == 1 ? a.r + b + lane : nullptr;
     const float* __restrict__ rf = RK == 2 ? a.r32 + b + lane : nullptr;
+    // with kPipeColumns the column stream runs one chunk ahead: a chunk's
+    // field gathers are issued beside its weight loads, not after a round
+    // trip for its columns
+    constexpr bool PIPE = kPipeColumns<NO, RK, BOUND>;
+    int32_t qn[PIPE ? U : 1];
+    if constexpr (PIPE) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) qn[u] = u < L ? ld_stream<STREAM>(c + (int64_t)u * kSlice) : 0;
+    }
     for (int j0 = 0; j0 < L; j0 += U) {
         int32_t q[U];
         float wv[U][NO], rv[U][NO];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int j = j0 + u;
-            const bool ok = j < L;
-            q[u] = ok ? ld_stream<STREAM>(c + (int64_t)j * kSlice) : 0;
-#pragma unroll
-            for (int o = 0; o < NO; ++o) {
-                wv[u][o] = ok ? ld_stream<STREAM>(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
-                if (RK == 1)
-                    rv[u][o] = ok ? __bfloat162float(ld_stream<STREAM>(rr + (int64_t)o * a.total + (int64_t)j * kSlice))
-                                  : 0.0f;
-                else if (RK == 2)
-                    rv[u][o] = ok ? ld_stream<STREAM>(rf + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
-                else
-                    rv[u][o] = 0.0f;
-            }
-        }
         // entries past the slice end take the row's own value (a zero
         // difference; zero for interpolation) with weight 0: no gather
         FT fq[U];
+        // the chunk's weight (and residual) streams
+        auto load_weights = [&] {
 #pragma unroll
-        for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? fld[q[u]] : fp;
+            for (int u = 0; u < U; ++u) {
+                const int j = j0 + u;
+                const bool ok = j < L;
+                if constexpr (!PIPE) q[u] = ok ? ld_stream<STREAM>(c + (int64_t)j * kSlice) : 0;
+#pragma unroll
+                for (int o = 0; o < NO; ++o) {
+                    wv[u][o] = ok ? ld_stream<STREAM>(w + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
+                    if (RK == 1)
+                        rv[u][o] = ok ? __bfloat162float(
+                                            ld_stream<STREAM>(rr + (int64_t)o * a.total + (int64_t)j * kSlice))
+                                      : 0.0f;
+                    else if (RK == 2)
+                        rv[u][o] = ok ? ld_stream<STREAM>(rf + (int64_t)o * a.total + (int64_t)j * kSlice) : 0.0f;
+                    else
+                        rv[u][o] = 0.0f;
+                }
+            }
+        };
+        if constexpr (PIPE) {
+            // gathers of this chunk, columns of the next, then the weights
+#pragma unroll
+            for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? fld[qn[u]] : fp;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = j0 + U + u;
+                qn[u] = j < L ? ld_stream<STREAM>(c + (int64_t)j * kSlice) : 0;
+            }
+            load_weights();
+        } else {
+            // columns and weights, then the gathers
+            load_weights();
+#pragma unroll
+            for (int u = 0; u < U; ++u) fq[u] = j0 + u < L ? fld[q[u]] : fp;
+        }
 #pragma unroll
         for (int u = 0; u < U; ++u) acc.add(wv[u], rv[u], fq[u], fp, a.comp);
         if constexpr (BOUND) {
