@@ -2131,7 +2131,7 @@ int split_for_apply(dcpse_plan_t* P, const double* d_f, int precision) {
 // residual streams: its bound is 2^8 times smaller, so far fewer rows need
 // the second pass (worth it where many rows would, e.g. second derivatives
 // on strongly graded clouds).
-int apply_budget(dcpse_plan_t* P, double* d_out) {
+int apply_budget(dcpse_plan_t* P, double* d_out, bool host_out = false) {
     cudaStream_t st = P->stream;
     const int64_t n = P->n;
     if (n == 0) return DCPSE_OK;
@@ -2176,6 +2176,7 @@ int apply_budget(dcpse_plan_t* P, double* d_out) {
             sa.no_self = 0;
             sa.bnd = P->bnd;
             sa.maxabs = P->maxabs;
+            sa.counter = slice_counter(P, host_out);
             P->tstart(DCPSE_K_APPLY_BATCHED, st);
             cudaError_t e = apply_sell(sa, P->nout, st);
             P->tstop(DCPSE_K_APPLY_BATCHED, st);
@@ -2434,7 +2435,7 @@ int dcpse_apply_batched_host(dcpse_plan_t* P, const double* h_f, double* h_out, 
         if (om && fm) {
             if (int rc = check_f32_weights(P, precision)) return rc;
             if (int rc = split_for_apply(P, fm, precision)) return rc;
-            if (int rc = apply_budget(P, om)) return rc;
+            if (int rc = apply_budget(P, om, true)) return rc;
             DCPSE_CK(cudaStreamSynchronize(P->stream));
             return DCPSE_OK;
         }

@@ -228,8 +228,8 @@ struct SellArgs {
     float* bnd;
     unsigned* maxabs;
     int stream;            // evict-first hint on the column, weight and residual streams
-    // non-null (device outputs, no bounds): warps take slices one at a time
-    // from this counter (zeroed by apply_sell) and store their rows directly
+    // non-null (device outputs): warps take slices one at a time from this
+    // counter (zeroed by apply_sell) and store their rows directly
     unsigned* counter;
 };
 int64_t sell_slices(int64_t n);

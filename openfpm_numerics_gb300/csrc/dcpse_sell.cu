@@ -232,13 +232,15 @@ __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
 }
 
 // Whether a slice loads its column stream one chunk ahead (U more registers
-// a thread): everywhere but one output, the plain FP32 instances with 4 or 6
-// outputs and the bound pass, which would spill under their launch bounds.
-// Measured at 128^3 (window schedule): bf16 residual streams 1.090 -> 0.880
-// ms, weight pairs 1.168 -> 1.035 ms; graded 2D cloud, FP32: 0.150 -> 0.146
-// ms (warp schedule).
+// a thread): wherever ptxas reports no spills under the kernels' launch
+// bounds, i.e. not for one output, not for plain FP32 with 4 or 6 outputs,
+// and in the bound pass only with bf16 residual streams (but 6 outputs) or
+// plain FP32 with 2-4 or 7 outputs.  Measured at 128^3 (window schedule):
+// bf16 residual streams 1.090 -> 0.880 ms, weight pairs 1.168 -> 1.035 ms;
+// graded 2D cloud, FP32: 0.150 -> 0.146 ms (warp schedule).
 template <int NO, int RK, bool BOUND>
-constexpr bool kPipeColumns = NO != 1 && !BOUND && (RK != 0 || (NO != 4 && NO != 6));
+constexpr bool kPipeColumns =
+    NO != 1 && (BOUND ? (RK == 1 ? NO != 6 : (NO <= 4 || NO == 7)) : (RK != 0 || (NO != 4 && NO != 6)));
 
 // One slice: lane `lane` sums row `row` (a position, -1 past the last row)
 // over the slice's entries into acc (and, with BOUND, its weight-rounding
@@ -405,9 +407,13 @@ __global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 && !BOUND ? 5 : (NO <
 // by length within it), so the tile kernel's warps wait at the window's
 // barrier for its longest slice; here no warp waits for another.  The
 // stores scatter within the window's 256 rows: device-memory outputs only
-// (L2 completes their sectors).
-template <int NO, int U, int RK, bool STREAM>
-__global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 ? 5 : (NO <= 6 ? 4 : 3)))
+// (L2 completes their sectors).  BOUND: the bounds are stored per row and
+// each warp maxes |output| into maxabs (one atomic per output and slice,
+// skipped when the stored maximum is already larger).
+// (launch bounds as the tile kernel's, but three blocks per SM for the bound
+// pass of six outputs, which spills at four)
+template <int NO, int U, int RK, bool BOUND, bool STREAM>
+__global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 && !BOUND ? 5 : (NO < 6 || (NO == 6 && !BOUND) ? 4 : 3)))
     apply_sell_dyn_kernel(SellArgs a) {
     const int lane = threadIdx.x & 31;
     const long long shift = RK == 2 ? a.fx_meta[1] : 0;
@@ -419,11 +425,22 @@ __global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 ? 5 : (NO <= 6 ? 4 : 
         const int32_t row = a.srow[s * kSlice + lane];
         RowAcc<NO, (RK != 0)> acc;
         float bs[NO];
-        sell_slice<NO, U, RK, false, STREAM>(a, s, lane, row, acc, bs);
+        sell_slice<NO, U, RK, BOUND, STREAM>(a, s, lane, row, acc, bs);
         if (row >= 0) {
             const int64_t lr = a.perm ? (int64_t)a.perm[row] : row;
 #pragma unroll
-            for (int o = 0; o < NO; ++o) a.out[(int64_t)o * a.oos + lr * a.ors] = sell_value<NO, RK>(acc, o, shift);
+            for (int o = 0; o < NO; ++o) {
+                a.out[(int64_t)o * a.oos + lr * a.ors] = sell_value<NO, RK>(acc, o, shift);
+                if (BOUND) a.bnd[(int64_t)o * a.n + lr] = bs[o];
+            }
+        }
+        if constexpr (BOUND) {
+#pragma unroll
+            for (int o = 0; o < NO; ++o) {
+                const unsigned v = row >= 0 ? __float_as_uint(fabsf((float)acc.value(o))) : 0u;
+                const unsigned m = __reduce_max_sync(0xffffffffu, v);
+                if (lane == 0 && m > __ldcg(&a.maxabs[o])) atomicMax(&a.maxabs[o], m);
+            }
         }
         s = s0 + __shfl_sync(0xffffffffu, next, 0);
     }
@@ -648,14 +665,21 @@ template <int NO, bool ST>
 void launch_sell(const SellArgs& a, unsigned grid, cudaStream_t s) {
     constexpr int UR = NO == 1 ? 8 : (NO <= 2 ? 4 : 2);  // with the residual streams
     constexpr int U = NO == 1 ? 8 : 4;
-    if (a.counter && !a.bnd) {
+    if (a.counter) {
         const int64_t slices = (a.w1 - a.w0) * kSlicesPerWin;
+#define DCPSE_DYN(UU, RK, B) \
+    apply_sell_dyn_kernel<NO, UU, RK, B, ST><<<dyn_grid<apply_sell_dyn_kernel<NO, UU, RK, B, ST>>(slices), 256, 0, s>>>(a)
         if (a.r32)
-            apply_sell_dyn_kernel<NO, UR, 2, ST><<<dyn_grid<apply_sell_dyn_kernel<NO, UR, 2, ST>>(slices), 256, 0, s>>>(a);
+            DCPSE_DYN(UR, 2, false);
+        else if (a.r && a.bnd)
+            DCPSE_DYN(UR, 1, true);
         else if (a.r)
-            apply_sell_dyn_kernel<NO, UR, 1, ST><<<dyn_grid<apply_sell_dyn_kernel<NO, UR, 1, ST>>(slices), 256, 0, s>>>(a);
+            DCPSE_DYN(UR, 1, false);
+        else if (a.bnd)
+            DCPSE_DYN(U, 0, true);
         else
-            apply_sell_dyn_kernel<NO, U, 0, ST><<<dyn_grid<apply_sell_dyn_kernel<NO, U, 0, ST>>(slices), 256, 0, s>>>(a);
+            DCPSE_DYN(U, 0, false);
+#undef DCPSE_DYN
         return;
     }
     if (a.r32)
@@ -673,7 +697,7 @@ void launch_sell(const SellArgs& a, unsigned grid, cudaStream_t s) {
 
 cudaError_t apply_sell(const SellArgs& a, int nout, cudaStream_t s) {
     if (a.w1 <= a.w0) return cudaSuccess;
-    if (a.counter && !a.bnd) {
+    if (a.counter) {
         cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
         if (e != cudaSuccess) return e;
     }

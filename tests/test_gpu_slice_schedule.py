@@ -72,3 +72,28 @@ def test_lattice_and_p2p_schedules_agree(cuda):
     b = ip.p2p(fs, C.F32).clone()
     assert torch.equal(a, b)
     ip.close()
+
+
+@pytest.mark.parametrize("first", [C.F32, C.F32_RESID])
+def test_budget_pass_schedules_agree(cuda, first):
+    """The error-budget apply's bound pass under both schedules: the same
+    outputs, bounds and maxima, so the same rows corrected."""
+    cfg = W.config3(60_000, seed=15)
+    pos = torch.tensor(cfg["pos"], device="cuda")
+    plan = DcpsePlan(2, W.five_ops_2d(), order=2)
+    plan.build_neighbors(pos, 0.0, torch.tensor(cfg["rcut_pp"], device="cuda"))
+    plan.assemble(pos, FLAGS)
+    plan.set_error_budget(1e-7, first)
+    x, y = cfg["pos"][:, 0], cfg["pos"][:, 1]
+    f = torch.tensor(np.sin(2 * np.pi * x) * np.cos(2 * np.pi * y), device="cuda")
+    res = []
+    for mode in (C.APPLY_SLICE_WARPS, C.APPLY_SLICE_WINDOWS):
+        plan.set_apply_config(0, mode)
+        plan.budget_stats(reset=True)
+        out = plan.apply(f, C.F32_BUDGET).clone()
+        res.append((out, plan.budget_stats()))
+    assert torch.equal(res[0][0], res[1][0])
+    assert res[0][1] == res[1][1]
+    if first == C.F32:
+        assert res[0][1] > 0  # FP32 bounds exceed the budget on some rows of this cloud
+    plan.close()
