@@ -166,18 +166,21 @@ __global__ void __launch_bounds__(256) gs_stage_sell_kernel(RkArgs<float> a, int
         const int32_t* __restrict__ c = a.scols + b + lane;
         const float* __restrict__ w = a.sw + b + lane;
         float lu = 0.f, lv = 0.f;
+        // the column stream runs one chunk ahead of the gathers
+        int32_t qn[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) qn[u] = u < L ? c[(int64_t)u * 32] : 0;
         for (int j0 = 0; j0 < L; j0 += U) {
-            int32_t q[U];
+            float2 y[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) y[u] = j0 + u < L ? Y2[qn[u]] : yp;
             float wq[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int j = j0 + u;
-                q[u] = j < L ? c[(int64_t)j * 32] : 0;
+                qn[u] = j + U < L ? c[(int64_t)(j + U) * 32] : 0;
                 wq[u] = j < L ? w[(int64_t)j * 32] : 0.f;
             }
-            float2 y[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) y[u] = j0 + u < L ? Y2[q[u]] : yp;
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 lu = fmaf(wq[u], y[u].x - yp.x, lu);
@@ -292,18 +295,21 @@ __global__ void __launch_bounds__(256) gs_adjoint_sell_kernel(RkAdjArgs<float> a
         const int32_t* __restrict__ c = a.scols + b + lane;
         const float* __restrict__ w = a.sw + b + lane;
         float lu = 0.f, lv = 0.f;
+        // the column stream runs one chunk ahead of the gathers
+        int32_t qn[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) qn[u] = u < L ? c[(int64_t)u * 32] : p;
         for (int j0 = 0; j0 < L; j0 += U) {
-            int32_t q[U];
+            float2 y[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) y[u] = KB[qn[u]];
             float wq[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int j = j0 + u;
-                q[u] = j < L ? c[(int64_t)j * 32] : p;
+                qn[u] = j + U < L ? c[(int64_t)(j + U) * 32] : p;
                 wq[u] = j < L ? w[(int64_t)j * 32] : 0.f;
             }
-            float2 y[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) y[u] = KB[q[u]];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 lu = fmaf(wq[u], y[u].x, lu);
