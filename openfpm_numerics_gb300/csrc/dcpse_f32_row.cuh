@@ -41,12 +41,21 @@ __device__ __forceinline__ void fixed_pair(long long d, float& dh, float& dl) {
     dl = t - (dh - s);
 }
 
-template <int NO, bool RESID>
+// LOW2: the low sum c is itself compensated (TwoSum, its errors collected in
+// cc), for the weight pairs, whose results are held to the FP64 apply's
+// accuracy: with plain FP32 low sums, rows whose terms cancel ~1e3-fold lost
+// ~1e-12 normwise there
+template <int NO, bool RESID, bool LOW2 = false>
 struct RowAcc {
     float s[NO], c[NO];
+    float cc[LOW2 ? NO : 1];
     __device__ __forceinline__ void init() {
 #pragma unroll
         for (int o = 0; o < NO; ++o) s[o] = c[o] = 0.0f;
+        if constexpr (LOW2) {
+#pragma unroll
+            for (int o = 0; o < NO; ++o) cc[o] = 0.0f;
+        }
     }
     // one neighbour: weights w[o] (and residuals r[o]), field pair fq, fp.
     // Outputs whose bit is set in comp take the compensated sum (derivatives
@@ -79,7 +88,14 @@ struct RowAcc {
                 float t = fmaf(w[o], dh, -p) + e;
                 t = fmaf(w[o], dl, t);
                 if (RESID) t = fmaf(r[o], dh, t);
-                c[o] = c[o] + t;
+                if constexpr (LOW2) {
+                    float nc, e2;
+                    two_sum(c[o], t, nc, e2);
+                    c[o] = nc;
+                    cc[o] = cc[o] + e2;
+                } else {
+                    c[o] = c[o] + t;
+                }
             } else {
                 s[o] = fmaf(w[o], dh, s[o]);
                 float t = fmaf(w[o], dl, c[o]);
@@ -103,7 +119,10 @@ struct RowAcc {
             }
         }
     }
-    __device__ __forceinline__ double value(int o) const { return (double)s[o] + (double)c[o]; }
+    __device__ __forceinline__ double value(int o) const {
+        if constexpr (LOW2) return (double)s[o] + ((double)c[o] + (double)cc[o]);
+        return (double)s[o] + (double)c[o];
+    }
 };
 
 }  // namespace dcpse

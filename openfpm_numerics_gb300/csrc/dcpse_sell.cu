@@ -233,21 +233,21 @@ __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
 
 // Whether a slice loads its column stream one chunk ahead (U more registers
 // a thread): wherever ptxas reports no spills under the kernels' launch
-// bounds, i.e. not for one output, not for plain FP32 with 4 or 6 outputs,
-// and in the bound pass only with bf16 residual streams (but 6 outputs) or
-// plain FP32 with 2-4 or 7 outputs.  Measured at 128^3 (window schedule):
+// bounds, i.e. not for one output, not for 6 outputs of plain FP32 or weight
+// pairs, not for 4 outputs of plain FP32, and in the bound pass only with
+// bf16 residual streams (but 6 outputs) or plain FP32 with 2-4 or 7 outputs.  Measured at 128^3 (window schedule):
 // bf16 residual streams 1.090 -> 0.880 ms, weight pairs 1.168 -> 1.035 ms;
 // graded 2D cloud, FP32: 0.150 -> 0.146 ms (warp schedule).
 template <int NO, int RK, bool BOUND>
 constexpr bool kPipeColumns =
-    NO != 1 && (BOUND ? (RK == 1 ? NO != 6 : (NO <= 4 || NO == 7)) : (RK != 0 || (NO != 4 && NO != 6)));
+    NO != 1 && (BOUND ? (RK == 1 ? NO != 6 : (NO <= 4 || NO == 7)) : (RK == 1 || (NO != 6 && (RK == 2 || NO != 4))));
 
 // One slice: lane `lane` sums row `row` (a position, -1 past the last row)
 // over the slice's entries into acc (and, with BOUND, its weight-rounding
 // bound into bs).
 template <int NO, int U, int RK, bool BOUND, bool STREAM>
 __device__ __forceinline__ void sell_slice(const SellArgs& a, int64_t s, int lane, int32_t row,
-                                           RowAcc<NO, (RK != 0)>& acc, float (&bs)[NO]) {
+                                           RowAcc<NO, (RK != 0), (RK == 2)>& acc, float (&bs)[NO]) {
     const int64_t b = a.off[s];
     const int L = (int)((a.off[s + 1] - b) / kSlice);
     // the field: float pairs, or (weight pairs) fixed point
@@ -330,7 +330,7 @@ __device__ __forceinline__ void sell_slice(const SellArgs& a, int64_t s, int lan
 // output o of a summed row (fixed point: the sums are in units of
 // 2^(64 - shift))
 template <int NO, int RK>
-__device__ __forceinline__ double sell_value(const RowAcc<NO, (RK != 0)>& acc, int o, long long shift) {
+__device__ __forceinline__ double sell_value(const RowAcc<NO, (RK != 0), (RK == 2)>& acc, int o, long long shift) {
     const double v = acc.value(o);
     if constexpr (RK == 2)
         return shift == kFixedNonFinite ? __longlong_as_double(0x7ff8000000000000ll) : ldexp(v, (int)(64 - shift));
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 && !BOUND ? 5 : (NO <
     for (int64_t win = a.w0 + blockIdx.x; win < a.w1; win += gridDim.x) {
         const int64_t s = win * kSlicesPerWin + (threadIdx.x >> 5);  // < nslices: windows hold 8 slices
         const int32_t row = a.srow[s * kSlice + lane];
-        RowAcc<NO, (RK != 0)> acc;
+        RowAcc<NO, (RK != 0), (RK == 2)> acc;
         float bs[NO];
         sell_slice<NO, U, RK, BOUND, STREAM>(a, s, lane, row, acc, bs);
         if (row >= 0) {
@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 && !BOUND ? 5 : (NO <
     while (s < s1) {
         next = lane == 0 ? atomicAdd(a.counter, 1u) : 0u;
         const int32_t row = a.srow[s * kSlice + lane];
-        RowAcc<NO, (RK != 0)> acc;
+        RowAcc<NO, (RK != 0), (RK == 2)> acc;
         float bs[NO];
         sell_slice<NO, U, RK, BOUND, STREAM>(a, s, lane, row, acc, bs);
         if (row >= 0) {
@@ -651,7 +651,8 @@ namespace {
 // fewer when the range has fewer slices than their warps
 template <auto K>
 unsigned dyn_grid(int64_t slices) {
-    // blocks per SM: a property of the kernel on this architecture
+    // blocks per SM: a property of the kernel and the architecture (the SM
+    // count is looked up per device); a wrong value would only size the grid
     static const int per_sm = [] {
         int b = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, K, 256, 0) != cudaSuccess || b < 1) b = 1;
