@@ -111,19 +111,30 @@ struct VjpLayout {
     int off_b, off_g, off_r, off_z, off_ab, off_perm, words;
 };
 
+// powers u_d^t, t = 0..8, of one entry (computed once, then shared by all
+// its monomials: the same products each monomial used to form itself)
 template <int DIM>
-__device__ __forceinline__ void mono_and_grad(const double* u, const unsigned char* e, double& m, double* dm) {
-    // m = prod_d u_d^e_d;  dm_d = e_d u_d^(e_d - 1) prod_{d' != d} u_d'^e_d'
-    double pw[DIM][9];
+__device__ __forceinline__ void powers(const double* u, double (&pw)[DIM][9]) {
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         pw[d][0] = 1.0;
 #pragma unroll
         for (int t = 1; t < 9; ++t) pw[d][t] = pw[d][t - 1] * u[d];
     }
-    m = 1.0;
+}
+
+// m = prod_d u_d^e_d
+template <int DIM>
+__device__ __forceinline__ double mono(const double (&pw)[DIM][9], const unsigned char* e) {
+    double m = 1.0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) m *= pw[d][e[d]];
+    return m;
+}
+
+// dm_d = e_d u_d^(e_d - 1) prod_{d' != d} u_d'^e_d'
+template <int DIM>
+__device__ __forceinline__ void mono_grad(const double (&pw)[DIM][9], const unsigned char* e, double* dm) {
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         if (e[d] == 0) {
@@ -213,11 +224,9 @@ __global__ void __launch_bounds__(kWarps * 32) vjp_pos_kernel(VjpArgs a, VjpLayo
                     u[d] = o[d] / eps;
                 }
                 const double E = exp(-0.5 * norm2<DIM>(u));  // E^2 = omega
-                for (int j = 0; j < nu; ++j) {
-                    double m, dm[DIM];
-                    mono_and_grad<DIM>(u, T.uexp[j], m, dm);
-                    Bs[lane * L.ldb + j] = E * m;
-                }
+                double pw[DIM][9];
+                powers<DIM>(u, pw);
+                for (int j = 0; j < nu; ++j) Bs[lane * L.ldb + j] = E * mono<DIM>(pw, T.uexp[j]);
                 Bs[lane * L.ldb + nu] = E * (a.f[qq] - fp);
             }
             __syncwarp();
@@ -339,62 +348,64 @@ __global__ void __launch_bounds__(kWarps * 32) vjp_pos_kernel(VjpArgs a, VjpLayo
                 for (int d = 0; d < DIM; ++d) a.gentry[(beg + q) * DIM + d] = 0.0;
             continue;
         }
-        // per-entry chain rule; the eps term needs sum_q gu_q.u_q first
+        // per-entry chain rule: the first pass stores gu / eps and sums
+        // gu_q.u_q, which the eps term needs; the second adds that term
         double gsum = 0.0;
-        for (int pass = 0; pass < 2; ++pass) {
-            double Dtot = 0.0;
-            if (pass == 1) {
-                for (int o = 16; o > 0; o >>= 1) gsum += __shfl_xor_sync(0xffffffffu, gsum, o);
-                Dtot = Dsc - gsum / eps;
+        for (int c0 = 0; c0 < k; c0 += kCh) {
+            const int q = c0 + lane;
+            if (q >= k) break;
+            const int64_t qq = a.cols[beg + q];
+            double u[DIM], gu[DIM];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                u[d] = offset1(a.geom, d, xp[d], a.pos[qq * DIM + d]) / eps;
+                gu[d] = 0.0;
             }
-            for (int c0 = 0; c0 < k; c0 += kCh) {
-                const int q = c0 + lane;
-                if (q >= k) break;
-                const int64_t qq = a.cols[beg + q];
-                double o[DIM], u[DIM], gu[DIM];
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) {
-                    o[d] = offset1(a.geom, d, xp[d], a.pos[qq * DIM + d]);
-                    u[d] = o[d] / eps;
-                    gu[d] = 0.0;
+            const double om = exp(-norm2<DIM>(u));
+            const double cq = a.f[qq] - fp;
+            double pw[DIM][9];
+            powers<DIM>(u, pw);
+            for (int g = 0; g < ngroups; ++g) {
+                const int n = T.gn[g];
+                const double* at = AB + g * 2 * L.nmax;
+                const double* lm = at + L.nmax;
+                const double ee = 1.0 / ipow(eps, (unsigned)T.gord[g]);
+                double va = 0.0, vl = 0.0;
+                for (int i = 0; i < n; ++i) {
+                    const double vi = mono<DIM>(pw, T.uexp[T.gidx[g][i]]);
+                    va += vi * at[i];
+                    vl += vi * lm[i];
                 }
-                const double om = exp(-norm2<DIM>(u));
-                const double cq = a.f[qq] - fp;
-                for (int g = 0; g < ngroups; ++g) {
-                    const int n = T.gn[g];
-                    const double* at = AB + g * 2 * L.nmax;
-                    const double* lm = at + L.nmax;
-                    const double ee = 1.0 / ipow(eps, (unsigned)T.gord[g]);
-                    double va = 0.0, vl = 0.0;
-                    double vi[kMaxBasisSmall];
-                    double dvi[kMaxBasisSmall][DIM];
-                    for (int i = 0; i < n; ++i) {
-                        mono_and_grad<DIM>(u, T.uexp[T.gidx[g][i]], vi[i], dvi[i]);
-                        va += vi[i] * at[i];
-                        vl += vi[i] * lm[i];
-                    }
-                    const double alpha_q = ee * va * (cq - vl);
+                const double alpha_q = ee * va * (cq - vl);
 #pragma unroll
-                    for (int d = 0; d < DIM; ++d) gu[d] += alpha_q * (-2.0 * om * u[d]);
-                    for (int i = 0; i < n; ++i) {
-                        const double beta_i = ee * om * ((cq - vl) * at[i] - va * lm[i]);
+                for (int d = 0; d < DIM; ++d) gu[d] += alpha_q * (-2.0 * om * u[d]);
+                for (int i = 0; i < n; ++i) {
+                    double dvi[DIM];
+                    mono_grad<DIM>(pw, T.uexp[T.gidx[g][i]], dvi);
+                    const double beta_i = ee * om * ((cq - vl) * at[i] - va * lm[i]);
 #pragma unroll
-                        for (int d = 0; d < DIM; ++d) gu[d] += beta_i * dvi[i][d];
-                    }
+                    for (int d = 0; d < DIM; ++d) gu[d] += beta_i * dvi[d];
                 }
-                if (pass == 0) {
-                    double t = 0.0;
+            }
+            double t = 0.0;
 #pragma unroll
-                    for (int d = 0; d < DIM; ++d) t += gu[d] * u[d];
-                    gsum += t;
-                } else {
-                    const double dd = fixed ? 0.0 : Dtot / ((double)k * a.h_over_eps);
+            for (int d = 0; d < DIM; ++d) {
+                t += gu[d] * u[d];
+                a.gentry[(beg + q) * DIM + d] = gu[d] / eps;
+            }
+            gsum += t;
+        }
+        for (int o = 16; o > 0; o >>= 1) gsum += __shfl_xor_sync(0xffffffffu, gsum, o);
+        // (with a fixed eps the term is zero; adding it keeps the sign of
+        // zero entries as the fused expression gu / eps + dd sg gave it)
+        const double dd = fixed ? 0.0 : (Dsc - gsum / eps) / ((double)k * a.h_over_eps);
+        for (int q = lane; q < k; q += 32) {
+            const int64_t qq = a.cols[beg + q];
 #pragma unroll
-                    for (int d = 0; d < DIM; ++d) {
-                        const double sg = (o[d] > 0.0) ? 1.0 : ((o[d] < 0.0) ? -1.0 : 0.0);
-                        a.gentry[(beg + q) * DIM + d] = gu[d] / eps + dd * sg;
-                    }
-                }
+            for (int d = 0; d < DIM; ++d) {
+                const double o = offset1(a.geom, d, xp[d], a.pos[qq * DIM + d]);
+                const double sg = (o > 0.0) ? 1.0 : ((o < 0.0) ? -1.0 : 0.0);
+                a.gentry[(beg + q) * DIM + d] = a.gentry[(beg + q) * DIM + d] + dd * sg;
             }
         }
     }
