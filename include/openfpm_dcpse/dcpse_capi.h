@@ -402,8 +402,8 @@ int dcpse_measure_fp64_peak(void* stream, double* tflops);
  * next slice from a counter and stores its rows' outputs directly, so no
  * warp waits for the longest slice of its window.  Window-scheduled: a block
  * takes one window of 8 slices and its outputs leave in row order after the
- * window's barrier (always so for host-memory outputs, row chunks on their
- * own streams and the error-budget pass).  By default device-memory applies
+ * window's barrier (always so for host-memory outputs and row chunks on
+ * their own streams).  By default device-memory applies
  * are warp-scheduled when the window barrier would idle 15 % or more of the
  * warp time (slices of unequal length: graded clouds), measured when the
  * layout is built.  These bits force one schedule. */
