@@ -48,3 +48,16 @@ def test_python_length_checks():
     for bad in (torch.empty((2, 4), dtype=torch.float64), torch.empty((2, 5), dtype=torch.float32)):
         with pytest.raises(ValueError):
             DcpsePlan._check_out(bad, (2, 5))
+
+
+def test_python_constants_match_the_header():
+    """Every DCPSE_* constant the Python binding mirrors has the header's
+    value (store flags, precisions, apply schedule bits, status codes)."""
+    import re
+
+    text = open(C.HEADER).read()
+    defines = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define DCPSE_([A-Z0-9_]+)\s+(\d+)\b", text)}
+    for name in ("F32_PAIR", "APPLY_SLICE_WINDOWS", "APPLY_SLICE_WARPS", "STORE_OUT_F32_CORR", "ASSEMBLE_TC"):
+        assert name in defines and hasattr(C, name), name
+    mismatched = {n: (v, getattr(C, n)) for n, v in defines.items() if hasattr(C, n) and getattr(C, n) != v}
+    assert not mismatched, mismatched
