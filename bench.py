@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the graded-cloud, adjoint, Gray-Scott and shuffled-order sections")
-    ap.add_argument("--only", choices=["apply", "apply64", "assemble", "assemble-tc", "gray-scott", "graded", "interp"],
+    ap.add_argument("--only", choices=["apply", "apply-pair", "apply64", "assemble", "assemble-tc", "gray-scott", "graded",
+                                       "interp"],
                     default=None,
                     help="small-footprint run of one kernel family (for profiler captures)")
     ap.add_argument("--lanes", type=int, default=0)
@@ -1151,6 +1152,19 @@ def run_only(args):
         ms, k = plan.timing(C.K_APPLY_BATCHED)
         res["apply_ms"] = ms / max(k, 1)
         res["achieved_gbs"] = W.apply_bytes(N, nnz, NOUT, 4) / (ms / max(k, 1) / 1e3) / 1e9
+    elif args.only == "apply-pair":
+        # the FP32 weight pairs (DCPSE_F32_PAIR): 8 bytes per entry and output
+        plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F32 | C.STORE_OUT_F32_CORR)
+        plan.set_apply_config(args.lanes, args.mode)
+        out = torch.empty((NOUT, N), dtype=torch.float64, device="cuda")
+        for _ in range(args.warmup):
+            plan.apply(f, C.F32_PAIR, out)
+        plan.reset_timing()
+        for _ in range(args.steps):
+            plan.apply(f, C.F32_PAIR, out)
+        ms, k = plan.timing(C.K_APPLY_BATCHED)
+        res["apply_pair_ms"] = ms / max(k, 1)
+        res["achieved_gbs"] = W.apply_bytes(N, nnz, NOUT, 8) / (ms / max(k, 1) / 1e3) / 1e9
     elif args.only == "apply64":
         plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F64)
         out = torch.empty((NOUT, N), dtype=torch.float64, device="cuda")
