@@ -100,6 +100,68 @@ __global__ void vjp_field_kernel(const int64_t* __restrict__ trow, const int32_t
     }
 }
 
+// (L^T g)_q on the sliced ELL layout of the transposed list (slices of 32
+// rows stored entry-major, rows sorted by length within windows of 256; the
+// weights of every output gathered into it): a row per thread, coalesced
+// column and weight streams, the cotangents gathered per output.  Each row
+// sums its entries in the CSR kernel's order (by source particle, outputs
+// innermost) and subtracts the row-sum terms last, so the results are the
+// CSR kernel's bit for bit; padding entries have weight 0 on the row itself.
+// FP32 weights come widened to double at the layout's build (exact, as the
+// CSR kernel's per-use conversion is, which runs at the FP64 rate here).
+template <int NO>
+__global__ void __launch_bounds__(256) vjp_field_sell_kernel(VjpSellArgs a) {
+    const double* __restrict__ wt = a.w;
+    const int lane = threadIdx.x & 31;
+    constexpr int U = NO <= 2 ? 4 : 2;  // entries in flight per thread
+    for (int64_t win = blockIdx.x; win < a.nwin; win += gridDim.x) {
+        const int64_t s = win * 8 + (threadIdx.x >> 5);
+        const int32_t row = a.srow[s * 32 + lane];
+        if (row < 0) continue;
+        const int64_t b = a.off[s];
+        const int L = (int)((a.off[s + 1] - b) / 32);
+        const int32_t* __restrict__ c = a.cols + b + lane;
+        const double* __restrict__ w = wt + b + lane;
+        double acc = 0.0;
+        for (int j0 = 0; j0 < L; j0 += U) {
+            int32_t q[U];
+            double wv[U][NO], gv[U][NO];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = j0 + u;
+                q[u] = j < L ? c[(int64_t)j * 32] : row;
+#pragma unroll
+                for (int o = 0; o < NO; ++o) wv[u][o] = j < L ? w[(int64_t)o * a.total + (int64_t)j * 32] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int o = 0; o < NO; ++o) gv[u][o] = a.g[(int64_t)o * a.n + q[u]];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (j0 + u < L) {
+#pragma unroll
+                    for (int o = 0; o < NO; ++o) acc = fma(wv[u][o], gv[u][o], acc);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 0; o < NO; ++o) acc = fma(-a.g[(int64_t)o * a.n + row], a.rs[(int64_t)o * a.n + row], acc);
+        a.out[row] = acc;
+    }
+}
+
+// transposed weights of every output, as doubles: wt[o * nnz + t] =
+// w[o * ws + tidx[t]] (FP32 weights widened, exactly)
+template <typename T>
+__global__ void transpose_outputs_kernel(const int64_t* __restrict__ tidx, int64_t nnz, int nout,
+                                         const T* __restrict__ w, int64_t ws, double* __restrict__ wt) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nnz; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = tidx[t];
+        for (int o = 0; o < nout; ++o) wt[(int64_t)o * nnz + t] = (double)w[(int64_t)o * ws + j];
+    }
+}
+
 // ------------------------------------------------------------ position VJP --
 constexpr int kWarps = 4;
 constexpr int kCh = 32;
@@ -476,6 +538,40 @@ cudaError_t vjp_field(const int64_t* trow, const int32_t* tsrc, const int64_t* t
                       cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     vjp_field_kernel<<<grid_for(n), 256, 0, s>>>(trow, tsrc, tidx, n, nout, w64, w32, ws, rs, g, out);
+    return cudaGetLastError();
+}
+
+cudaError_t vjp_field_sell(const VjpSellArgs& a, int nout, cudaStream_t s) {
+    if (a.nwin == 0) return cudaSuccess;
+    if (a.nwin > 0x7fffffff) return cudaErrorInvalidValue;
+    const unsigned grid = (unsigned)a.nwin;
+    switch (nout) {
+#define DCPSE_VJPS_CASE(NO)                                       \
+    case NO:                                                      \
+        vjp_field_sell_kernel<NO><<<grid, 256, 0, s>>>(a);        \
+        break;
+        DCPSE_VJPS_CASE(1)
+        DCPSE_VJPS_CASE(2)
+        DCPSE_VJPS_CASE(3)
+        DCPSE_VJPS_CASE(4)
+        DCPSE_VJPS_CASE(5)
+        DCPSE_VJPS_CASE(6)
+        DCPSE_VJPS_CASE(7)
+        DCPSE_VJPS_CASE(8)
+#undef DCPSE_VJPS_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t transpose_outputs(const int64_t* tidx, int64_t nnz, int nout, const double* w64, const float* w32,
+                              int64_t ws, double* wt, cudaStream_t s) {
+    if (nnz == 0) return cudaSuccess;
+    if (w64)
+        transpose_outputs_kernel<double><<<grid_for(nnz), 256, 0, s>>>(tidx, nnz, nout, w64, ws, wt);
+    else
+        transpose_outputs_kernel<float><<<grid_for(nnz), 256, 0, s>>>(tidx, nnz, nout, w32, ws, wt);
     return cudaGetLastError();
 }
 

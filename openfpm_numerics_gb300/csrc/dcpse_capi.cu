@@ -307,7 +307,28 @@ struct dcpse_plan_s {
         dfree(tsell_off);
         dfree(tsell_w);
     }
+    // the transposed list on a sliced ELL layout with the weights of every
+    // output gathered into it (the field VJP), per precision
+    int32_t *vsell_row = nullptr, *vsell_cols = nullptr;
+    int64_t* vsell_off = nullptr;
+    int64_t vsell_total = 0;
+    bool vsell_no_room = false;
+    double* vsell_w64 = nullptr;
+    double* vsell_w32 = nullptr;  // the FP32 weights, widened
+    void free_vsell_weights() {
+        dfree(vsell_w64);
+        dfree(vsell_w32);
+    }
+    void free_vsell() {
+        dfree(vsell_row);
+        dfree(vsell_cols);
+        dfree(vsell_off);
+        vsell_total = 0;
+        vsell_no_room = false;
+        free_vsell_weights();
+    }
     void free_transpose() {
+        free_vsell();
         dfree(korder);
         korder_width = 0;
         dfree(t_row);
@@ -397,6 +418,7 @@ struct dcpse_plan_s {
         bnd_len = 0;
         dfree(rowsum);
         rowsum_prec = -1;
+        free_vsell_weights();
         dfree(wT32);
         dfree(rs32);
         dfree(wT64);
@@ -1234,6 +1256,10 @@ int dcpse_assemble(dcpse_plan_t* P, const double* d_pos, const double* d_eps_fix
     if ((flags & DCPSE_STORE_OUT_F64) && !P->w64) DCPSE_CK(dalloc(&P->w64, (size_t)P->nout * nnz));
     if (!(flags & DCPSE_STORE_OUT_F64)) dfree(P->w64);
     P->free_sell();  // the FP32 weights are rewritten
+    // so are the field VJP's row sums and transposed weights
+    dfree(P->rowsum);
+    P->rowsum_prec = -1;
+    P->free_vsell_weights();
     if ((flags & DCPSE_STORE_OUT_F32) && !P->w32) DCPSE_CK(dalloc(&P->w32, (size_t)P->nout * nnz + kPad));
     if (!(flags & DCPSE_STORE_OUT_F32)) dfree(P->w32);
     if ((flags & DCPSE_STORE_OUT_F32_RESID) && !P->r16)
@@ -1421,6 +1447,7 @@ int dcpse_set_term_kernels(dcpse_plan_t* P, int term, const double* d_kernels, c
     P->flags &= ~(DCPSE_STORE_OUT_F64 | DCPSE_STORE_OUT_F32 | DCPSE_STORE_OUT_F32_RESID);
     dfree(P->rowsum);
     P->rowsum_prec = -1;
+    P->free_vsell_weights();
     cudaStream_t s = P->stream;
     if (nnz > 0)
         DCPSE_CK(cudaMemcpyAsync(P->k_term + (size_t)term * nnz, d_kernels, sizeof(double) * nnz,
@@ -1467,6 +1494,70 @@ int ensure_transpose(dcpse_plan_t* P) {
 }
 }  // namespace
 
+namespace {
+// The field VJP's sliced layout of the transposed list and, for precision,
+// the transposed weights of every output on it; without room the CSR
+// kernel serves (*ready false).
+int ensure_vjp_sell(dcpse_plan_t* P, int precision, bool* ready) {
+    *ready = false;
+    if (P->n == 0 || P->vsell_no_room) return DCPSE_OK;
+    cudaStream_t st = P->stream;
+    cudaError_t e = cudaSuccess;
+    if (!P->vsell_row) {
+        const int64_t ns = sell_slices(P->n);
+        int32_t* slen = nullptr;
+        int64_t* tmp = nullptr;
+        int64_t total = 0;
+        e = dalloc(&P->vsell_row, (size_t)ns * 32);
+        if (e == cudaSuccess) e = dalloc(&P->vsell_off, (size_t)ns + 1);
+        if (e == cudaSuccess) e = dalloc(&slen, (size_t)ns);
+        if (e == cudaSuccess) e = dalloc(&tmp, (size_t)scan_tmp_elems(ns));
+        if (e == cudaSuccess) e = sell_order(P->t_row, P->n, P->vsell_row, slen, P->vsell_off, tmp, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&total, P->vsell_off + ns, sizeof total, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        dfree(slen);
+        dfree(tmp);
+        if (e == cudaSuccess) e = dalloc(&P->vsell_cols, (size_t)total + kPad);
+        // the columns: the source particles, padding on the row itself
+        if (e == cudaSuccess)
+            e = sell_fill(P->t_row, P->t_src, nullptr, nullptr, P->nnz, P->nout, P->n, 1, P->vsell_row, P->vsell_off,
+                          total, P->vsell_cols, nullptr, nullptr, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) P->vsell_total = total;
+    }
+    const bool f64 = precision == DCPSE_F64;
+    double*& lw = f64 ? P->vsell_w64 : P->vsell_w32;
+    if (e == cudaSuccess && !lw) {
+        // transposed weights of every output (CSR order, as doubles: FP32
+        // weights widened once here instead of at every use), then on the
+        // layout
+        double* wt = nullptr;
+        e = dalloc(&wt, (size_t)P->nout * P->nnz + kPad);
+        if (e == cudaSuccess)
+            e = transpose_outputs(P->t_idx, P->nnz, P->nout, f64 ? P->w64 : nullptr, f64 ? nullptr : P->w32, P->nnz,
+                                  wt, st);
+        if (e == cudaSuccess) e = dalloc(&lw, (size_t)P->nout * P->vsell_total + kPad);
+        if (e == cudaSuccess)
+            e = sell_fill64(P->t_row, wt, P->nnz, P->nout, P->n, P->vsell_row, P->vsell_off, P->vsell_total, lw, st,
+                            nullptr);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        dfree(wt);
+    }
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        P->free_vsell();
+        P->vsell_no_room = true;
+        return DCPSE_OK;
+    }
+    if (e != cudaSuccess) {
+        P->free_vsell();
+        return fail(DCPSE_ERR_CUDA, std::string("field VJP layout: ") + cudaGetErrorString(e));
+    }
+    *ready = true;
+    return DCPSE_OK;
+}
+}  // namespace
+
 int dcpse_vjp_field(dcpse_plan_t* P, const double* d_g, double* d_out, int precision) {
     if (int rc = check_plan(P)) return rc;
     if (int rc = check_single_set(P)) return rc;
@@ -1488,6 +1579,27 @@ int dcpse_vjp_field(dcpse_plan_t* P, const double* d_g, double* d_out, int preci
         if (!P->rowsum) DCPSE_CK(dalloc(&P->rowsum, (size_t)P->nout * P->n));
         DCPSE_CK(row_sums(P->rowptr, P->n, P->nout, w64, w32, P->nnz, P->rowsum, P->stream));
         P->rowsum_prec = precision;
+    }
+    // the sliced kernel unless a CSR schedule was asked for
+    const int mode = P->apply_mode & 15;
+    if (mode == 0 || mode == 4) {
+        bool ready = false;
+        if (int rc = ensure_vjp_sell(P, precision, &ready)) return rc;
+        if (ready) {
+            VjpSellArgs a{};
+            a.n = P->n;
+            a.nwin = (P->n + 255) / 256;
+            a.srow = P->vsell_row;
+            a.off = P->vsell_off;
+            a.cols = P->vsell_cols;
+            a.w = w64 ? P->vsell_w64 : P->vsell_w32;
+            a.total = P->vsell_total;
+            a.rs = P->rowsum;
+            a.g = d_g;
+            a.out = d_out;
+            DCPSE_CK(vjp_field_sell(a, P->nout, P->stream));
+            return DCPSE_OK;
+        }
     }
     DCPSE_CK(vjp_field(P->t_row, P->t_src, P->t_idx, P->n, P->nout, w64, w32, P->nnz, P->rowsum, d_g, d_out,
                        P->stream));

@@ -390,6 +390,24 @@ cudaError_t row_sums(const int64_t* rowptr, int64_t n, int nout, const double* w
 cudaError_t vjp_field(const int64_t* trow, const int32_t* tsrc, const int64_t* tidx, int64_t n, int nout,
                       const double* w64, const float* w32, int64_t ws, const double* rs, const double* g, double* out,
                       cudaStream_t s);
+// The field VJP on the sliced ELL layout of the transposed list (w: the
+// transposed weights of every output on that layout as doubles, FP32 weights
+// widened; output o at w + o * total)
+struct VjpSellArgs {
+    int64_t n, nwin;
+    const int32_t* srow;
+    const int64_t* off;
+    const int32_t* cols;
+    const double* w;
+    int64_t total;
+    const double* rs;   // [nout][n] row sums of the weights
+    const double* g;    // [nout][n] cotangents
+    double* out;        // [n]
+};
+cudaError_t vjp_field_sell(const VjpSellArgs& a, int nout, cudaStream_t s);
+// wt[o * nnz + t] = w[o * ws + tidx[t]] (w64, else w32 widened)
+cudaError_t transpose_outputs(const int64_t* tidx, int64_t nnz, int nout, const double* w64, const float* w32,
+                              int64_t ws, double* wt, cudaStream_t s);
 
 struct VjpArgs {
     const AsmTables* tab;

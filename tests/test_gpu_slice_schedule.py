@@ -97,3 +97,46 @@ def test_budget_pass_schedules_agree(cuda, first):
     if first == C.F32:
         assert res[0][1] > 0  # FP32 bounds exceed the budget on some rows of this cloud
     plan.close()
+
+
+@pytest.mark.parametrize("prec", [C.F64, C.F32])
+@pytest.mark.parametrize("cloud", ["lattice", "graded"])
+def test_field_vjp_sliced_equals_csr(cuda, prec, cloud):
+    """The field VJP on the sliced layout of the transposed list sums each
+    row in the CSR kernel's order: bit-identical results, on a lattice and on
+    a graded cloud, with FP64 and FP32 weights; a new assembly replaces the
+    layout's weights."""
+    if cloud == "lattice":
+        pos_np, h = W.lattice(24, 3, jitter=0.15, seed=16)
+        outputs, dim = W.grad_lap_outputs(3), 3
+        build = lambda plan, pos: plan.build_neighbors(pos, 2.8 * h)
+    else:
+        cfg = W.config3(40_000, seed=17)
+        pos_np, outputs, dim = cfg["pos"], W.five_ops_2d(), 2
+        rpp = torch.tensor(cfg["rcut_pp"], device="cuda")
+        build = lambda plan, pos: plan.build_neighbors(pos, 0.0, rpp)
+    pos = torch.tensor(pos_np, device="cuda")
+    plan = DcpsePlan(dim, outputs, order=2)
+    build(plan, pos)
+    plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+    g = torch.tensor(np.random.default_rng(18).standard_normal((len(outputs), pos_np.shape[0])), device="cuda")
+    plan.set_apply_config(0, 0)
+    a = plan.vjp_field(g, prec).clone()
+    plan.set_apply_config(0, 1)  # CSR schedule: the thread-per-row CSR kernel
+    b = plan.vjp_field(g, prec).clone()
+    assert torch.equal(a, b)
+    # the weights change with a new assembly: the layout follows
+    plan.assemble(pos, C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+    plan.set_apply_config(0, 0)
+    a2 = plan.vjp_field(g, prec).clone()
+    plan.set_apply_config(0, 1)
+    assert torch.equal(a2, plan.vjp_field(g, prec))
+    if prec == C.F64:  # (the two assemblies' FP32 weights can round alike)
+        assert not torch.equal(a2, a)
+    # and equal a fresh plan's (row sums and transposed weights are rebuilt)
+    fresh = DcpsePlan(dim, outputs, order=2)
+    build(fresh, pos)
+    fresh.assemble(pos, C.STORE_TERMS_F64 | C.STORE_OUT_F64 | C.STORE_OUT_F32)
+    assert torch.equal(a2, fresh.vjp_field(g, prec))
+    fresh.close()
+    plan.close()
