@@ -1993,6 +1993,13 @@ int ensure_sell_layout(dcpse_plan_t* P) {
         return fail(DCPSE_ERR_CUDA, std::string("sliced ELL layout: ") + cudaGetErrorString(e));
     }
     P->sell_total = total;
+    // the warp-scheduled kernels' slice counter, allocated here rather than
+    // at the first apply (which may run inside a stream capture); without it
+    // the window kernel serves
+    if (!P->slice_counter && dalloc(&P->slice_counter, 1) != cudaSuccess) {
+        cudaGetLastError();
+        P->slice_counter = nullptr;
+    }
     return DCPSE_OK;
 }
 
@@ -2096,8 +2103,7 @@ constexpr double kSliceIdleWarps = 0.15;
 unsigned* slice_counter(dcpse_plan_t* P, bool host_out) {
     if (host_out || (P->apply_mode & DCPSE_APPLY_SLICE_WINDOWS)) return nullptr;
     if (P->sell_idle < kSliceIdleWarps && !(P->apply_mode & DCPSE_APPLY_SLICE_WARPS)) return nullptr;
-    if (!P->slice_counter && dalloc(&P->slice_counter, 1) != cudaSuccess) return nullptr;
-    return P->slice_counter;
+    return P->slice_counter;  // (allocated with the layout)
 }
 
 // The FP32 batched apply of rows [r0, r1) (0, 0: all rows) from the plan's
