@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the graded-cloud, adjoint, Gray-Scott and shuffled-order sections")
     ap.add_argument("--only", choices=["apply", "apply-pair", "apply64", "assemble", "assemble-tc", "gray-scott", "graded",
-                                       "interp"],
+                                       "interp", "vjp"],
                     default=None,
                     help="small-footprint run of one kernel family (for profiler captures)")
     ap.add_argument("--lanes", type=int, default=0)
@@ -1165,6 +1165,21 @@ def run_only(args):
         ms, k = plan.timing(C.K_APPLY_BATCHED)
         res["apply_pair_ms"] = ms / max(k, 1)
         res["achieved_gbs"] = W.apply_bytes(N, nnz, NOUT, 8) / (ms / max(k, 1) / 1e3) / 1e9
+    elif args.only == "vjp":
+        # the position VJP (FP64, through eps, the moment systems and the
+        # kernels) with N(0, 1) cotangents
+        plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F64)
+        g = torch.tensor(np.random.default_rng(4).standard_normal((NOUT, N)), device="cuda")
+        for _ in range(args.warmup):
+            plan.vjp_positions(pos, f, g)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.vjp_positions(pos, f, g)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res["vjp_positions_ms"] = e0.elapsed_time(e1) / max(args.steps, 1)
     elif args.only == "apply64":
         plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F64)
         out = torch.empty((NOUT, N), dtype=torch.float64, device="cuda")

@@ -194,6 +194,11 @@ __device__ __forceinline__ double mono(const double (&pw)[DIM][9], const unsigne
     return m;
 }
 
+// small integers as doubles (an int -> double conversion runs on the FP64
+// pipe; the exponent is the same for all lanes, so the constant cache
+// broadcasts it)
+__constant__ double kSmallInt[9] = {0.0, 1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0, 8.0};
+
 // dm_d = e_d u_d^(e_d - 1) prod_{d' != d} u_d'^e_d'
 template <int DIM>
 __device__ __forceinline__ void mono_grad(const double (&pw)[DIM][9], const unsigned char* e, double* dm) {
@@ -203,7 +208,7 @@ __device__ __forceinline__ void mono_grad(const double (&pw)[DIM][9], const unsi
             dm[d] = 0.0;
             continue;
         }
-        double r = (double)e[d] * pw[d][e[d] - 1];
+        double r = kSmallInt[e[d]] * pw[d][e[d] - 1];
 #pragma unroll
         for (int d2 = 0; d2 < DIM; ++d2)
             if (d2 != d) r *= pw[d2][e[d2]];
@@ -270,6 +275,10 @@ __global__ void __launch_bounds__(kWarps * 32) vjp_pos_kernel(VjpArgs a, VjpLayo
                 for (int d = 0; d < DIM; ++d) a.gentry[(beg + q) * DIM + d] = 0.0;
             continue;
         }
+        // one reciprocal of eps per particle (u = x_pq / eps as a product:
+        // within an ulp of the assembly's quotient, well inside this
+        // adjoint's tolerance)
+        const double ieps = 1.0 / eps;
         // Gram + s
         double acc[NPP];
 #pragma unroll
@@ -283,7 +292,7 @@ __global__ void __launch_bounds__(kWarps * 32) vjp_pos_kernel(VjpArgs a, VjpLayo
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) {
                     o[d] = offset1(a.geom, d, xp[d], a.pos[qq * DIM + d]);
-                    u[d] = o[d] / eps;
+                    u[d] = o[d] * ieps;
                 }
                 const double E = exp(-0.5 * norm2<DIM>(u));  // E^2 = omega
                 double pw[DIM][9];
@@ -412,6 +421,9 @@ __global__ void __launch_bounds__(kWarps * 32) vjp_pos_kernel(VjpArgs a, VjpLayo
         }
         // per-entry chain rule: the first pass stores gu / eps and sums
         // gu_q.u_q, which the eps term needs; the second adds that term
+        double eeg[kMaxGroups];
+#pragma unroll
+        for (int g = 0; g < kMaxGroups; ++g) eeg[g] = g < ngroups ? 1.0 / ipow(eps, (unsigned)T.gord[g]) : 0.0;
         double gsum = 0.0;
         for (int c0 = 0; c0 < k; c0 += kCh) {
             const int q = c0 + lane;
@@ -420,7 +432,7 @@ __global__ void __launch_bounds__(kWarps * 32) vjp_pos_kernel(VjpArgs a, VjpLayo
             double u[DIM], gu[DIM];
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
-                u[d] = offset1(a.geom, d, xp[d], a.pos[qq * DIM + d]) / eps;
+                u[d] = offset1(a.geom, d, xp[d], a.pos[qq * DIM + d]) * ieps;
                 gu[d] = 0.0;
             }
             const double om = exp(-norm2<DIM>(u));
@@ -431,29 +443,35 @@ __global__ void __launch_bounds__(kWarps * 32) vjp_pos_kernel(VjpArgs a, VjpLayo
                 const int n = T.gn[g];
                 const double* at = AB + g * 2 * L.nmax;
                 const double* lm = at + L.nmax;
-                const double ee = 1.0 / ipow(eps, (unsigned)T.gord[g]);
+                double ee = eeg[0];
+#pragma unroll
+                for (int t = 1; t < kMaxGroups; ++t)
+                    if (t == g) ee = eeg[t];
                 double va = 0.0, vl = 0.0;
                 for (int i = 0; i < n; ++i) {
                     const double vi = mono<DIM>(pw, T.uexp[T.gidx[g][i]]);
-                    va += vi * at[i];
-                    vl += vi * lm[i];
+                    va = fma(vi, at[i], va);
+                    vl = fma(vi, lm[i], vl);
                 }
-                const double alpha_q = ee * va * (cq - vl);
+                const double r = cq - vl;
+                const double alpha_q = ee * va * r;
+                const double ga = alpha_q * (-2.0 * om);
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) gu[d] += alpha_q * (-2.0 * om * u[d]);
+                for (int d = 0; d < DIM; ++d) gu[d] = fma(ga, u[d], gu[d]);
+                const double eo = ee * om;
                 for (int i = 0; i < n; ++i) {
                     double dvi[DIM];
                     mono_grad<DIM>(pw, T.uexp[T.gidx[g][i]], dvi);
-                    const double beta_i = ee * om * ((cq - vl) * at[i] - va * lm[i]);
+                    const double beta_i = eo * fma(r, at[i], -va * lm[i]);
 #pragma unroll
-                    for (int d = 0; d < DIM; ++d) gu[d] += beta_i * dvi[d];
+                    for (int d = 0; d < DIM; ++d) gu[d] = fma(beta_i, dvi[d], gu[d]);
                 }
             }
             double t = 0.0;
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
-                t += gu[d] * u[d];
-                a.gentry[(beg + q) * DIM + d] = gu[d] / eps;
+                t = fma(gu[d], u[d], t);
+                a.gentry[(beg + q) * DIM + d] = gu[d] * ieps;
             }
             gsum += t;
         }
