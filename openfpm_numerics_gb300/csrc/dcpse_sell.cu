@@ -234,13 +234,15 @@ __global__ void __launch_bounds__(256) apply_sell64_kernel(Sell64Args a) {
 // Whether a slice loads its column stream one chunk ahead (U more registers
 // a thread): wherever ptxas reports no spills under the kernels' launch
 // bounds, i.e. not for one output, not for 6 outputs of plain FP32 or weight
-// pairs, not for 4 outputs of plain FP32, and in the bound pass only with
-// bf16 residual streams (but 6 outputs) or plain FP32 with 2-4 or 7 outputs.  Measured at 128^3 (window schedule):
+// pairs, and in the bound pass only with bf16 residual streams (but 6
+// outputs) or plain FP32 with 2-4 or 7 outputs.  Plain FP32 with 4 outputs
+// takes it at four blocks per SM (56 registers; 128^3 lattice 0.591 -> 0.577
+// ms against five blocks without it).  Measured at 128^3 (window schedule):
 // bf16 residual streams 1.090 -> 0.880 ms, weight pairs 1.168 -> 1.035 ms;
 // graded 2D cloud, FP32: 0.150 -> 0.146 ms (warp schedule).
 template <int NO, int RK, bool BOUND>
 constexpr bool kPipeColumns =
-    NO != 1 && (BOUND ? (RK == 1 ? NO != 6 : (NO <= 4 || NO == 7)) : (RK == 1 || (NO != 6 && (RK == 2 || NO != 4))));
+    NO != 1 && (BOUND ? (RK == 1 ? NO != 6 : (NO <= 4 || NO == 7)) : (RK == 1 || (NO != 6)));
 
 // One slice: lane `lane` sums row `row` (a position, -1 past the last row)
 // over the slice's entries into acc (and, with BOUND, its weight-rounding
@@ -338,13 +340,13 @@ __device__ __forceinline__ double sell_value(const RowAcc<NO, (RK != 0), (RK == 
 }
 
 // thread per row; block = one window of 8 slices (five blocks per SM fit the
-// registers without spills up to four outputs, four up to six, three above).
+// registers without spills up to three outputs, four up to six, three above).
 // BOUND: also the weight-rounding bound of every output of every row,
 // B_o = sum_q |w_o,pq| |f_q - f_p| (FP32), stored to bnd[o * n + r], and the
 // largest |output| of the call per output, atomically maxed into maxabs[o]
 // (float bits; the values are >= 0, so unsigned order is float order).
 template <int NO, int U, int RK, bool BOUND, bool STREAM>
-__global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 && !BOUND ? 5 : (NO <= 6 ? 4 : 3)))
+__global__ void __launch_bounds__(256, (NO <= 3 && RK == 0 && !BOUND ? 5 : (NO <= 6 ? 4 : 3)))
     apply_sell_kernel(SellArgs a) {
     // the window's outputs, staged so that they leave in row order (rows of a
     // slice are permuted; scattered 8-byte stores are slow, above all into
@@ -413,7 +415,7 @@ __global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 && !BOUND ? 5 : (NO <
 // (launch bounds as the tile kernel's, but three blocks per SM for the bound
 // pass of six outputs, which spills at four)
 template <int NO, int U, int RK, bool BOUND, bool STREAM>
-__global__ void __launch_bounds__(256, (NO <= 4 && RK == 0 && !BOUND ? 5 : (NO < 6 || (NO == 6 && !BOUND) ? 4 : 3)))
+__global__ void __launch_bounds__(256, (NO <= 3 && RK == 0 && !BOUND ? 5 : (NO < 6 || (NO == 6 && !BOUND) ? 4 : 3)))
     apply_sell_dyn_kernel(SellArgs a) {
     const int lane = threadIdx.x & 31;
     const long long shift = RK == 2 ? a.fx_meta[1] : 0;
