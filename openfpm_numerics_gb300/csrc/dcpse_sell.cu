@@ -16,6 +16,14 @@
 // column, weight and residual streams (read once per apply) take the
 // streaming (evict-first) cache hint, so that L2 keeps the outputs, which
 // leave in the caller's order, until their sectors are complete.
+//
+// Two schedules sum the same rows in the same order: one window of 8 slices
+// per block (outputs staged and stored in row order after the window's
+// barrier) or warps taking slices one at a time from a counter (for layouts
+// whose slices differ in length, where that barrier would idle the warps).
+// Residual streams: bf16 (RK 1, the weights' FP32 rounding to 2^-32), or FP32
+// (RK 2, the weight pairs, with the field in 62-bit fixed point and a
+// compensated low sum: FP64-class results).
 #include <cuda_bf16.h>
 
 #include <type_traits>
