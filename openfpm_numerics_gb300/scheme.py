@@ -106,45 +106,66 @@ class DCPSE_scheme:
         return x
 
 
-def bicgstab(A, b, x0=None, tol=1e-10, maxiter=20000):
+def bicgstab(A, b, x0=None, tol=1e-10, maxiter=20000, check_every=16):
     """Jacobi-preconditioned BiCGSTAB (van der Vorst 1992) on the device.
-    Returns (x, iterations, relative residual)."""
+    Returns (x, iterations, relative residual).
+
+    The scalars stay on the device: the host reads the residual and a
+    breakdown flag once every `check_every` iterations (one synchronisation
+    instead of six per iteration), so up to check_every - 1 iterations run
+    past convergence, each only reducing the residual further.  A breakdown
+    (rho = 0 or omega = 0) freezes the iterate, and the next check stops."""
     d = _diagonal(A)
     dinv = torch.where(d != 0, 1.0 / d, torch.ones_like(d))
     x = torch.zeros_like(b) if x0 is None else x0.clone()
     r = b - A @ x
-    bn = torch.linalg.vector_norm(b).item() or 1.0
+    bn = torch.linalg.vector_norm(b)
+    bn = torch.where(bn > 0, bn, torch.ones_like(bn))
+    res = float((torch.linalg.vector_norm(r) / bn).item())
+    if not (res > tol) or maxiter <= 0:
+        return x, 0, res
     rhat = r.clone()
-    rho = alpha = omega = 1.0
+    zero = torch.zeros((), dtype=b.dtype, device=b.device)
+    rho = alpha = omega = torch.ones((), dtype=b.dtype, device=b.device)
     v = torch.zeros_like(b)
     p = torch.zeros_like(b)
-    res = torch.linalg.vector_norm(r).item() / bn
+    live = torch.ones((), dtype=torch.bool, device=b.device)  # no breakdown yet
+
+    def safe_div(num, den):
+        ok = den != 0
+        return torch.where(ok, num / torch.where(ok, den, torch.ones_like(den)), zero), ok
+
     it = 0
-    while res > tol and it < maxiter:
-        it += 1
-        rho_new = torch.dot(rhat, r).item()
-        if rho_new == 0.0:
-            break
-        beta = (rho_new / rho) * (alpha / omega) if it > 1 else 0.0
-        p = r + beta * (p - omega * v) if it > 1 else r.clone()
-        ph = dinv * p
-        v = A @ ph
-        alpha = rho_new / torch.dot(rhat, v).item()
-        s = r - alpha * v
-        if torch.linalg.vector_norm(s).item() / bn <= tol:
-            x = x + alpha * ph
-            r = s
-            res = torch.linalg.vector_norm(r).item() / bn
-            break
-        sh = dinv * s
-        t = A @ sh
-        tt = torch.dot(t, t).item()
-        omega = torch.dot(t, s).item() / tt if tt != 0 else 0.0
-        x = x + alpha * ph + omega * sh
-        r = s - omega * t
-        rho = rho_new
-        res = torch.linalg.vector_norm(r).item() / bn
-        if omega == 0.0:
+    while it < maxiter:
+        for _ in range(min(check_every, maxiter - it)):
+            it += 1
+            rho_new = torch.dot(rhat, r)
+            live = live & (rho_new != 0)
+            if it == 1:
+                p = r.clone()
+            else:
+                q1, _ = safe_div(rho_new, rho)
+                q2, _ = safe_div(alpha, omega)
+                p = r + (q1 * q2) * (p - omega * v)
+            ph = dinv * p
+            v = A @ ph
+            alpha_n, ok_a = safe_div(rho_new, torch.dot(rhat, v))
+            live = live & ok_a
+            a_ = torch.where(live, alpha_n, zero)
+            s = r - a_ * v
+            sh = dinv * s
+            t = A @ sh
+            omega_n, _ = safe_div(torch.dot(t, s), torch.dot(t, t))
+            o_ = torch.where(live, omega_n, zero)
+            x = x + a_ * ph + o_ * sh
+            r = s - o_ * t
+            live = live & (omega_n != 0)
+            rho = torch.where(live, rho_new, rho)
+            alpha = torch.where(live, alpha_n, alpha)
+            omega = torch.where(live, omega_n, omega)
+        state = torch.stack([torch.linalg.vector_norm(r) / bn, live.to(b.dtype)]).cpu()
+        res = float(state[0])
+        if not (res > tol) or state[1] == 0:
             break
     return x, it, res
 
