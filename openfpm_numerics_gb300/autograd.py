@@ -21,6 +21,7 @@ class DcpseApply(torch.autograd.Function):
         y = plan.apply(f.detach(), C.F64)
         ctx.plan = plan
         ctx.eps_fixed = eps_fixed
+        ctx.generation = plan.generation
         ctx.save_for_backward(f.detach(), pos.detach())
         return y
 
@@ -29,8 +30,11 @@ class DcpseApply(torch.autograd.Function):
         f, pos = ctx.saved_tensors
         plan = ctx.plan
         gy = gy.contiguous().to(torch.float64)
-        # the plan may have been re-assembled elsewhere since forward
-        plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F64, eps_fixed=ctx.eps_fixed)
+        # re-assemble only if the plan changed since forward (another
+        # assembly, a new list) or eps was given (a tensor autograd does not
+        # guard against in-place changes); pos itself is a saved tensor
+        if plan.generation != ctx.generation or ctx.eps_fixed is not None:
+            plan.assemble(pos, C.ASSEMBLE_FAST | C.STORE_OUT_F64, eps_fixed=ctx.eps_fixed)
         gf = plan.vjp_field(gy, C.F64) if ctx.needs_input_grad[0] else None
         gp = plan.vjp_positions(pos, f, gy, eps_fixed=ctx.eps_fixed) if ctx.needs_input_grad[1] else None
         return gf, gp, None, None

@@ -81,9 +81,20 @@ class DcpsePlan:
         self.stream = stream
         C.call("dcpse_plan_set_stream", self._h, _stream_ptr(stream))
         self.box = None
+        # bumped by every call that changes the list or the weights (see
+        # generation): lets a caller tell whether the plan still holds what
+        # it assembled
+        self._gen = 0
         if box is not None:
             self.set_box(*box)
         self.n = None
+
+    @property
+    def generation(self):
+        """A counter bumped by every call that changes the neighbour list or
+        the weights (set_box, set_support, set_surface, build_neighbors,
+        set_neighbors, assemble, set_term_kernels)."""
+        return self._gen
 
     # -- lifetime -------------------------------------------------------
     def close(self):
@@ -108,6 +119,7 @@ class DcpsePlan:
         hi = (ctypes.c_double * self.dim)(*[float(x) for x in hi])
         per = (ctypes.c_int * self.dim)(*([int(bool(p)) for p in periodic] if periodic is not None else
                                           [0] * self.dim))
+        self._gen += 1
         C.call("dcpse_plan_set_box", self._h, lo, hi, per)
         self.box = (tuple(lo), tuple(hi), tuple(per))
 
@@ -141,8 +153,10 @@ class DcpsePlan:
         tensor; the neighbour list must be built again."""
         if pos_support is not None:
             pos_support = self._check_pos(pos_support)
+            self._gen += 1
             C.call("dcpse_plan_set_support", self._h, _ptr(pos_support), pos_support.shape[0], int(bool(self_skip)))
         else:
+            self._gen += 1
             C.call("dcpse_plan_set_support", self._h, None, 0, int(bool(self_skip)))
         self._support = pos_support
         self.n = None
@@ -156,9 +170,11 @@ class DcpsePlan:
             normals = normals.to(device="cuda", dtype=torch.float64).contiguous()
             if n_spacings is not None:
                 n_spacings = n_spacings.to(device="cuda", dtype=torch.float64).contiguous()
+            self._gen += 1
             C.call("dcpse_plan_set_surface", self._h, _ptr(normals), int(n_count), float(n_spacing),
                    _ptr(n_spacings))
         else:
+            self._gen += 1
             C.call("dcpse_plan_set_surface", self._h, None, 0, 0.0, None)
         self._surface = (normals, n_spacings)
         self.n = None
@@ -167,6 +183,7 @@ class DcpsePlan:
         pos = self._check_pos(pos)
         if rcut_pp is not None:
             rcut_pp = rcut_pp.contiguous().to(torch.float64)
+        self._gen += 1
         C.call("dcpse_build_neighbors", self._h, _ptr(pos), pos.shape[0], float(rcut), _ptr(rcut_pp))
         self.n = pos.shape[0]
 
@@ -174,6 +191,7 @@ class DcpsePlan:
         rowptr = rowptr.contiguous().to(device="cuda", dtype=torch.int64)
         cols = cols.contiguous().to(device="cuda", dtype=torch.int32)
         n = rowptr.numel() - 1
+        self._gen += 1
         C.call("dcpse_set_neighbors", self._h, n, cols.numel(), _ptr(rowptr), _ptr(cols))
         self.n = n
 
@@ -194,6 +212,7 @@ class DcpsePlan:
             eps_fixed = eps_fixed.contiguous().to(torch.float64)
             self._check_rows(eps_fixed.numel(), self.n, "eps_fixed")
         allow = (C.ERR_PARTICLES,) if allow_failed_particles else ()
+        self._gen += 1
         return C.call("dcpse_assemble", self._h, _ptr(pos), _ptr(eps_fixed), int(flags), allow=allow)
 
     def gram_on_tensor_cores(self):
@@ -226,6 +245,7 @@ class DcpsePlan:
         def dev(x):
             return torch.as_tensor(x, dtype=torch.float64).to("cuda").contiguous()
         K, eps, eip = dev(K), dev(eps), dev(eip)
+        self._gen += 1
         C.call("dcpse_set_term_kernels", self._h, int(term), _ptr(K), _ptr(eps), _ptr(eip))
 
     def output_weights(self, output):

@@ -129,3 +129,34 @@ def test_config4_adjoint_fd(cuda, orc):
     cot = (2 * (y0 - g)).cpu().numpy()[None, :]
     ref = orc.vjp_positions(pos_np, rp.cpu().numpy(), cols.cpu().numpy(), outputs, f_np, cot)
     assert np.abs(gp - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+def test_backward_reassembles_only_when_the_plan_changed(cuda):
+    """The backward skips the re-assembly when the plan still holds the
+    forward's weights (same generation), and re-assembles when another
+    assembly ran in between: the gradients are the same either way."""
+    pos_np, h = W.lattice(40, 2, jitter=0.1, seed=21)
+    plan = DcpsePlan(2, [[(2, 0), (0, 2)]])
+    pos0 = torch.tensor(pos_np, device="cuda")
+    plan.build_neighbors(pos0, 3.1 * h)
+    g = torch.tensor(np.random.default_rng(22).standard_normal(pos_np.shape[0]), device="cuda")
+    f0 = torch.tensor(np.sin(3 * pos_np[:, 0]) * pos_np[:, 1], device="cuda")
+
+    def grads(between=None):
+        f = f0.clone().requires_grad_(True)
+        pos = pos0.clone().requires_grad_(True)
+        y = dcpse_apply(f, pos, plan)[0]
+        gen = plan.generation
+        if between is not None:
+            between()
+        ((y - g) ** 2).sum().backward()
+        return f.grad.clone(), pos.grad.clone(), plan.generation - gen
+
+    gf, gp, bumps = grads()
+    assert bumps == 0  # no re-assembly in backward
+    # an assembly at other positions between forward and backward
+    moved = pos0 + 0.05 * h
+    gf2, gp2, bumps2 = grads(lambda: plan.assemble(moved, C.ASSEMBLE_FAST | C.STORE_OUT_F64))
+    assert bumps2 == 2  # the intervening assembly and the backward's own
+    assert torch.equal(gf, gf2) and torch.equal(gp, gp2)
+    plan.close()
